@@ -1,0 +1,168 @@
+/*
+ * ot2d.h -- C ABI of the GB300-native OVERTURNS-2D hot path
+ * (library libturns2d_gb300.so, sm_103a).
+ *
+ * Two layers:
+ *
+ * 1. Drop-in routines (ot2d_rhsup, ot2d_visrhs, ot2d_ilu2d, ...).  Each one
+ *    replaces one Fortran subroutine of the reference and takes the same
+ *    arguments in the same order: every argument by reference, arrays in the
+ *    reference's column-major layout (q(jd,kd,nq) for one time instance of
+ *    q(jd,kd,nspec,nq) -- see OT2D_QSTRIDE below).  The module-level inputs
+ *    the reference reads from `params_global` are set once per mesh with
+ *    ot2d_set_params().  Pointers may be host memory (copied in and out
+ *    around the call), host memory registered with ot2d_register() (its
+ *    device mirror is used; no copy), or device memory (used in place).
+ *    Every routine returns an int status (0 = OK); ot2d_last_error() repeats
+ *    the last non-zero status of the calling thread.
+ *
+ * 2. A batched solver (ot2d_solver_*): many meshes of uneven size resident
+ *    in HBM, one launch per kernel family per iteration over all of them,
+ *    FP64 plain or FP32-mixed arithmetic, per-instance convergence.
+ *
+ * Nothing here allocates memory the caller must free, except the solver
+ * handle (ot2d_solver_destroy).
+ */
+#ifndef OT2D_H
+#define OT2D_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "ot2d_params.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define OT2D_OK            0
+#define OT2D_ERR_ARG       1   /* bad argument / unsupported switch combination      */
+#define OT2D_ERR_NORM      2   /* L2 norm > 1000: the reference's `stop 'norm'`      */
+#define OT2D_ERR_MONITOR   3   /* negative a^2 or NaN: the reference's mstop         */
+#define OT2D_ERR_CUDA      4   /* a CUDA call failed                                 */
+#define OT2D_ERR_NOPARAMS  5   /* no ot2d_set_params() before a drop-in routine      */
+#define OT2D_ERR_NOMEM     6   /* device allocation failed                           */
+#define OT2D_ERR_TIMEOUT   7   /* a bounded device wait gave up                      */
+
+/* precision modes of the solver and of the drop-in routines */
+#define OT2D_FP64          0   /* plain FP64, operation order of the reference       */
+#define OT2D_FP32_MIXED    1   /* FP32 residual/Jacobian/sweeps, FP64 state update   */
+
+/* ---------------------------------------------------------------------- */
+/* set-up (host)                                                           */
+/* ---------------------------------------------------------------------- */
+
+/* read_inputs derived constants + set_pointers_globals
+ * (src/setup.f:876-1268, src/setup.f:55-108, src/init.f:59-66). */
+int ot2d_params_from_inputs(const ot2d_inputs* in, ot2d_params* out);
+/* single C-mesh &bcinp table: wall(5), wake(51), far field(47) x3. */
+int ot2d_cmesh_bc_table(ot2d_inputs* in, int32_t jtail);
+/* seeded algebraic NACA 4-digit C-mesh standing in for fort.1
+ * (read by grid, src/io.f:343-380). */
+int ot2d_mesh_naca4_cmesh(int32_t jmax, int32_t kmax, int32_t n_wake, double m, double p, double t,
+                          double ds_wall, double r_far, double* xv, double* yv);
+
+/* ---------------------------------------------------------------------- */
+/* drop-in layer (one call = one reference subroutine)                     */
+/* ---------------------------------------------------------------------- */
+
+/* module params_global for the calling thread's current mesh
+ * (replaces set_pointers_globals + the namelist state, src/setup.f:55-108). */
+int ot2d_set_params(const ot2d_params* p);
+/* precision of the drop-in routines (default OT2D_FP64). */
+int ot2d_set_precision(int32_t mode);
+/* last non-zero status returned on this thread. */
+int ot2d_last_error(void);
+/* device residency: keep `bytes` at host pointer `h` mirrored on the GPU.
+ * Drop-in calls that receive `h` use the mirror without copying; call
+ * ot2d_sync_to_host / ot2d_sync_to_device around host-side reads/writes. */
+int ot2d_register(void* h, size_t bytes);
+int ot2d_unregister(void* h);
+int ot2d_sync_to_host(void* h);
+int ot2d_sync_to_device(void* h);
+
+/* src/eulerrhs.f:2-3 */
+int ot2d_rhsup(double* q, double* s, double* xx, double* xy, double* yx, double* yy, double* x, double* y,
+               double* xv, double* yv, double* xold, double* yold, double* xole, double* yole, int32_t* iblank,
+               double* ugv, double* vgv, int32_t* jd, int32_t* kd, int32_t* nei, int32_t* im, double* bt);
+/* src/visrhs.f:2-3 */
+int ot2d_visrhs(double* turmu, double* q, double* s, double* xx, double* xy, double* yx, double* yy, double* ug,
+                double* vg, double* tscale, int32_t* iblank, int32_t* jd, int32_t* kd);
+/* src/bc.f:2 */
+int ot2d_bc(double* q, double* x, double* y, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+            int32_t* im, int32_t* jd, int32_t* kd, double* bt);
+/* src/bc.f:88 */
+int ot2d_rbc(double* q, double* s, double* x, double* y, double* xx, double* xy, double* yx, double* yy, double* ug,
+             double* vg, int32_t* im, int32_t* jd, int32_t* kd, double* bt);
+/* src/time.f:2 (one time instance per call when nspec = 1) */
+int ot2d_time_step(double* q, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+                   double* tscale, double* bt, int32_t* iblank, int32_t* jd, int32_t* kd);
+/* src/lhs.f:470-471 */
+int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+               double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu,
+               double* tscale);
+/* src/samodel2d.f:2-3 */
+int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
+                double* xy, double* yx, double* yy, double* ug, double* vg, int32_t* jd, int32_t* kd,
+                double* tscale, int32_t* iblank, int32_t* im, int32_t* nsp);
+/* src/sources.f:2 (q, s: full (jd,kd,nspec,nv) arrays) */
+int ot2d_timespectralrhs(double* q, double* s, double* Ds, int32_t* jd, int32_t* kd, int32_t* nsp);
+/* src/step.f:2-7 (full arrays over nspec; norms of the last call via
+ * ot2d_last_norms) */
+int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, double* x, double* y, double* xv,
+              double* yv, int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+              double* ugv, double* vgv, double* xold, double* yold, double* xole, double* yole, double* turmu,
+              double* tscale, double* bt, double* Ds, int32_t* im, int32_t* jd, int32_t* kd);
+/* rsum, resrho, resmax per time instance of the last ot2d_step (step.f:58-93) */
+int ot2d_last_norms(double* out, int32_t n);
+/* src/step.f:332 */
+int ot2d_monitor(int32_t* mstop, double* q, int32_t* jd, int32_t* kd);
+/* src/forces.f:130-131; the four outputs are the raw integrals */
+int ot2d_force2d(int32_t* jd, int32_t* kd, double* x, double* y, double* xv, double* yv, double* q, double* xx,
+                 double* xy, double* yx, double* yy, double* cfx, double* cfy, double* cm0, double* cpower,
+                 int32_t* nsp);
+/* src/setup.f:111 and src/setup.f:440 (q: one instance, only q(:,:,nq) is written) */
+int ot2d_find_cellcenter(double* x, double* y, double* xv, double* yv, int32_t* jd, int32_t* kd, int32_t* im);
+int ot2d_metfv(double* q, double* x, double* y, double* xv, double* yv, double* xx, double* xy, double* yx,
+               double* yy, int32_t* jd, int32_t* kd, int32_t* im);
+
+/* ---------------------------------------------------------------------- */
+/* batched solver (host runtime over device-resident meshes)               */
+/* ---------------------------------------------------------------------- */
+
+typedef struct ot2d_solver ot2d_solver;
+
+/* per-instance result record */
+typedef struct ot2d_result {
+  int32_t id, status, iterations, converged;
+  double rsum_first, rsum_last;    /* L2 norm (step.f:86-93) at it 1 and last  */
+  double cl, cd, cm, cpower;       /* compute_forces, FP64 (forces.f:2-127)     */
+  double t_admit, t_done;          /* seconds since solver creation             */
+} ot2d_result;
+
+ot2d_solver* ot2d_solver_create(int32_t device, int32_t precision);
+void ot2d_solver_destroy(ot2d_solver* s);
+/* Admit one solve: params + vertex grid of time instance 1 (jmax*kmax).
+ * Returns the instance id (>= 0) or -status.  `orders` = target L2 drop in
+ * decades; max_iters caps the iterations. */
+int ot2d_solver_add(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv, double orders,
+                    int32_t max_iters);
+/* Run `iters` iterations over every live instance (one launch per kernel
+ * family per iteration).  Instances that converge, fail or reach their cap
+ * are retired and their slot freed.  Returns OT2D_OK or a CUDA status. */
+int ot2d_solver_iterate(ot2d_solver* s, int32_t iters);
+/* number of live (not yet retired) instances */
+int ot2d_solver_live(const ot2d_solver* s);
+/* copy the result of instance `id` (valid once retired, or a live snapshot) */
+int ot2d_solver_result(ot2d_solver* s, int32_t id, ot2d_result* out);
+/* download q (jd,kd,nspec,nq) of a live or retired-but-kept instance */
+int ot2d_solver_get_q(ot2d_solver* s, int32_t id, double* q_out);
+/* total device bytes held by the live instances */
+size_t ot2d_solver_device_bytes(const ot2d_solver* s);
+/* device bytes one instance with these params would take */
+size_t ot2d_instance_bytes(const ot2d_params* p, int32_t precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OT2D_H */

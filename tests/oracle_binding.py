@@ -1,0 +1,91 @@
+"""ctypes binding of the CPU FP64 oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: the oracle is the checker, never the thing
+measured or shipped.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline legs load it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from turns2d_urans_git_gb300.abi import Params, Inputs
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_SO = os.path.join(ORACLE_DIR, "liboracle.so")
+
+_lib = None
+
+_P = C.POINTER(Params)
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        L = C.CDLL(ORACLE_SO)
+        L.oro_read_inputs.argtypes = [C.POINTER(Inputs), _P]
+        L.oro_find_cellcenter.argtypes = [_P, _dp, _dp, _dp, _dp]
+        L.oro_metfv.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oro_metfv.restype = C.c_int
+        L.oro_qzero.argtypes = [_P, _dp]
+        L.oro_qdivj.argtypes = [_P, _dp]
+        L.oro_computeTScoefs.argtypes = [C.c_int, _dp]
+        L.oro_find_coord_TS_orig.argtypes = [_P, _dp, _dp, _dp, _dp, C.c_double]
+        L.oro_find_timemetrics_TS_orig.argtypes = [_P, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp]
+        L.oro_bc.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oro_rbc.argtypes = [_P, _dp, _dp]
+        L.oro_rhsup.argtypes = [_P, _dp, _dp, _dp, _dp, _ip, _dp, _dp]
+        L.oro_visrhs.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oro_time_step.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
+        L.oro_ilu2d.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oro_vmu_sa.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
+        L.oro_vmu_sa.restype = C.c_double
+        L.oro_monitor.argtypes = [_P, _dp]
+        L.oro_monitor.restype = C.c_int
+        L.oro_force2d.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oro_step.argtypes = [_P] + [_dp] * 5 + [_ip] + [_dp] * 12 + [_dp, _ip]
+        L.oro_step.restype = C.c_int
+        L.oro_solve.argtypes = [_P, _dp, _dp, C.c_int, C.c_double, _dp, _dp, _dp]
+        L.oro_solve.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    """ctypes pointer to a numpy array's data (must be contiguous)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"] or a.flags["F_CONTIGUOUS"]
+    if a.dtype == np.float64:
+        return a.ctypes.data_as(_dp)
+    if a.dtype == np.int32:
+        return a.ctypes.data_as(_ip)
+    raise TypeError(a.dtype)
+
+
+def read_inputs(inp):
+    p = Params()
+    lib().oro_read_inputs(C.byref(inp), C.byref(p))
+    return p
+
+
+def solve(p, xv, yv, nsteps, orders=0.0):
+    """Run the oracle driver; returns (iterations, hist[it, nsp], forces[nsp,5], q)."""
+    nsp = p.nspec
+    hist = np.zeros((nsteps, nsp))
+    forces = np.zeros((nsp, 5))
+    q = np.zeros(p.jd * p.kd * nsp * p.nq)
+    n = lib().oro_solve(C.byref(p), ptr(np.ascontiguousarray(xv, dtype=np.float64)),
+                        ptr(np.ascontiguousarray(yv, dtype=np.float64)), nsteps, orders,
+                        ptr(hist), ptr(forces), ptr(q))
+    return n, hist[:abs(n)], forces, q
