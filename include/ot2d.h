@@ -140,8 +140,17 @@ typedef struct ot2d_result {
   double t_admit, t_done;          /* seconds since solver creation             */
 } ot2d_result;
 
+/* solver options (ot2d_solver_set_option) */
+#define OT2D_OPT_CHECK_EVERY 1  /* iterations between host status reads (default 25) */
+#define OT2D_OPT_KEEP_Q      2  /* 1: keep q of retired instances for ot2d_solver_get_q */
+
 ot2d_solver* ot2d_solver_create(int32_t device, int32_t precision);
 void ot2d_solver_destroy(ot2d_solver* s);
+int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value);
+/* read the device status table now and retire finished instances */
+int ot2d_solver_sync(ot2d_solver* s);
+/* the CUDA stream (cudaStream_t) the solver launches on */
+void* ot2d_solver_stream(ot2d_solver* s);
 /* Admit one solve: params + vertex grid of time instance 1 (jmax*kmax).
  * Returns the instance id (>= 0) or -status.  `orders` = target L2 drop in
  * decades; max_iters caps the iterations. */

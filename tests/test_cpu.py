@@ -1,0 +1,155 @@
+"""CPU tests: the oracle's own invariants, the golden fixtures, the host-side
+set-up of the native library, and the C-ABI export list.  No GPU needed."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests import oracle_binding as ob
+from tests.helpers import Case, relerr
+from turns2d_urans_git_gb300 import api
+from turns2d_urans_git_gb300.abi import Params, default_inputs
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_abi_exports_every_declared_symbol():
+    """libturns2d_gb300.so loads without a GPU and exports every function
+    include/*.h declares."""
+    L = api.lib()
+    names = set()
+    for h in ("ot2d.h",):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(ot2d_[a-z0-9_]+)\s*\(", src))
+    assert len(names) > 20
+    missing = [n for n in sorted(names) if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_struct_sizes_match_c():
+    # two int blocks + double block + bc tables, as laid out in ot2d_params.h
+    assert C.sizeof(Params) == 40 * 4 + 34 * 8 + 8 + 6 * 25 * 4
+
+
+def test_params_match_oracle_read_inputs():
+    """ot2d_params_from_inputs (product) == the oracle's read_inputs."""
+    for kw in (dict(invisc=1, fsmach=0.8, alfa=1.25, dt=10.0, iconstant_cfl=1),
+               dict(invisc=0, lamin=0, iturb=1, fsmach=0.15, alfa=10.0, rey=6e6, vnuinf=3.0),
+               dict(invisc=0, lamin=0, iturb=1, timespectral=1, nspec=5, rf=0.1, angmax=5.0, fsmach=0.3)):
+        inp = default_inputs(jmax=129, kmax=33, **kw)
+        api.lib().ot2d_cmesh_bc_table(C.byref(inp), 17)
+        a = api.params_from_inputs(inp)
+        b = ob.read_inputs(inp)
+        assert bytes(a) == bytes(b), kw
+
+
+def test_ds_operator_antisymmetric_and_annihilates_constants():
+    for n in (3, 5, 7):
+        Ds = np.zeros(n * n)
+        ob.lib().oro_computeTScoefs(n, ob.ptr(Ds))
+        D = Ds.reshape(n, n).T  # Ds(i,j) column-major
+        assert np.allclose(D, -D.T, atol=1e-14)
+        assert np.allclose(D.sum(axis=1), 0.0, atol=1e-13)
+        # spectral derivative of sin(t) sampled at t_j = 2 pi j / n is cos(t)
+        t = 2 * np.pi * np.arange(n) / n
+        assert np.allclose(D @ np.sin(t), np.cos(t), atol=1e-12)
+
+
+def test_mesh_valid_for_all_batch_shapes():
+    rng = np.random.default_rng(3)
+    for (jmax, kmax) in ((129, 33), (257, 65), (385, 97)):
+        for _ in range(5):
+            m, p, t = rng.uniform(0, 0.06), rng.uniform(0.2, 0.6), rng.uniform(0.08, 0.18)
+            xv, yv = api.naca4_cmesh(jmax, kmax, (jmax - 1) // 8, m, p, t, 1e-6, 20.0)
+            X, Y = xv.T, yv.T
+            a3 = 0.5 * ((X[1:, 1:] - X[:-1, :-1]) * (Y[:-1, 1:] - Y[1:, :-1])
+                        - (X[:-1, 1:] - X[1:, :-1]) * (Y[1:, 1:] - Y[:-1, :-1]))
+            assert (a3 > 0).all()
+
+
+def test_host_geometry_matches_oracle_bitwise():
+    """ot2d_metfv / ot2d_find_cellcenter (host set-up) equal the oracle's
+    metfv / find_cellcenter bit for bit."""
+    from turns2d_urans_git_gb300 import routines as rt
+    c = Case(jmax=65, kmax=25, perturb=0)
+    rt.set_params(c.p)
+    x, y = np.zeros(c.n2), np.zeros(c.n2)
+    rt.find_cellcenter(x, y, c.xv, c.yv, c.jd, c.kd)
+    assert np.array_equal(x, c.x) and np.array_equal(y, c.y)
+    q = np.zeros_like(c.q)
+    xx, xy, yx, yy = (np.zeros(c.n2) for _ in range(4))
+    rt.metfv(q, x, y, c.xv, c.yv, xx, xy, yx, yy, c.jd, c.kd)
+    nq = c.p.nq
+    assert np.array_equal(q.reshape(nq, -1)[nq - 1], c.q.reshape(nq, -1)[nq - 1])
+    for a, b in ((xx, c.xx), (xy, c.xy), (yx, c.yx), (yy, c.yy)):
+        assert np.array_equal(a, b)
+
+
+def _freestream_residual(viscous, ilim):
+    c = Case(jmax=65, kmax=25, viscous=viscous, ilim=ilim, perturb=0, istep0=0)
+    L, p = ob.lib(), C.byref(c.p)
+    L.oro_bc(p, ob.ptr(c.q), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug), ob.ptr(c.vg),
+             ob.ptr(c.bt))
+    s = np.zeros(c.n2 * c.p.nv)
+    L.oro_rhsup(p, ob.ptr(c.q), ob.ptr(s), ob.ptr(c.xv), ob.ptr(c.yv), ob.ptr(c.iblank), ob.ptr(c.ugv), ob.ptr(c.vgv))
+    J = c.q.reshape(c.p.nq, -1)[c.p.nq - 1]
+    # residual per unit area against the flux scale rho*a ~ 1
+    return np.max(np.abs(s.reshape(c.p.nv, -1)[:4] * J[None, :]))
+
+
+@pytest.mark.parametrize("ilim", [0, 1, 4])
+def test_oracle_preserves_freestream(ilim):
+    """A uniform freestream on a closed finite-volume mesh has zero inviscid
+    residual (the wall ramp is off at istep0 = 0)."""
+    assert _freestream_residual(False, ilim) < 1e-9
+
+
+@pytest.mark.parametrize("ilim", [1, 4])
+def test_oracle_residual_mirror_symmetry(ilim):
+    """On the mirror-symmetric NACA 0012 grid at alpha = 0, a mirror-symmetric
+    state has a residual that is mirror-symmetric in mass, x-momentum and
+    energy and antisymmetric in y-momentum (cells j and jd-j+1)."""
+    c = Case(jmax=65, kmax=25, ilim=ilim, alfa=0.0, perturb=0.02, seed=5)
+    p, jd, kd = c.p, c.jd, c.kd
+    q = c.q.reshape(p.nq, kd, jd)
+    h = jd // 2
+    q[:, :, jd - h:] = q[:, :, :h][:, :, ::-1]
+    q[2, :, jd - h:] *= -1.0
+    if jd % 2:
+        q[2, :, h] = 0.0
+    s = np.zeros(c.n2 * p.nv)
+    L = ob.lib()
+    L.oro_rhsup(C.byref(p), ob.ptr(c.q), ob.ptr(s), ob.ptr(c.xv), ob.ptr(c.yv), ob.ptr(c.iblank), ob.ptr(c.ugv),
+                ob.ptr(c.vgv))
+    # The reference's weno reconstructs ql(is+2) with the sonic-A slope but
+    # qr(ie-2) with WENO5 (eulerrhs.f:1146-1174), so its line ends are not
+    # mirror images; compare away from the two outflow ends there.
+    e = 4 if ilim == 4 else 1
+    S = s.reshape(p.nv, kd, jd)[:, 1:-1, e:jd - e]
+    scale = np.abs(S).max()
+    for n, sgn in ((0, 1), (1, 1), (2, -1), (3, 1)):
+        assert np.abs(S[n] - sgn * S[n][:, ::-1]).max() < 1e-11 * scale, n
+
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def _golden(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+@pytest.mark.parametrize("name", ["c1_small", "c2_small"])
+def test_oracle_against_golden_history(name):
+    """The oracle reproduces its committed residual history and forces."""
+    from tests.golden.make_golden import CASES, case
+    g = _golden(name)
+    kind, kw, _ = CASES[name]
+    _, prm, xv, yv = case(kind, kw)
+    n, hist, forces, q = ob.solve(prm, xv.ravel(), yv.ravel(), int(g["nsteps"]))
+    assert n == int(g["nsteps"])
+    assert relerr(hist[:, 0], g["hist"]) < 1e-12
+    assert relerr(forces[0][:4], g["forces"]) < 1e-12
+    assert relerr(q, g["q"]) < 1e-12

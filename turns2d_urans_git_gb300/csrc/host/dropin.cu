@@ -1,0 +1,606 @@
+// dropin.cu -- the Fortran-shaped drop-in routines (ot2d_rhsup, ...).
+// Each call runs the same kernels as the batched solver on a batch of one
+// slice built from the caller's arrays.  Argument pointers are resolved as
+//   device / managed memory      -> used in place;
+//   host memory in the registry  -> its device mirror (ot2d_register);
+//   other host memory            -> copied to a staging buffer and back.
+// The module state of the reference (params_global) is the calling thread's
+// ot2d_set_params() value.  FP64 only: the drop-in path is the parity path.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "geom.h"
+#include "runtime.h"
+
+namespace ot2d {
+namespace {
+
+struct Reg { size_t bytes; void* dev; };
+std::mutex g_reg_mu;
+std::map<uintptr_t, Reg> g_reg;
+
+struct Staged { void* host; void* dev; size_t bytes; bool out; };
+
+struct Ctx {
+  ot2d_params P{};
+  bool has = false;
+  int err = 0;
+  cudaStream_t st = nullptr;
+  ot2d_params* dP = nullptr;
+  double* dwork = nullptr; size_t wcap = 0;      // scratch arrays of one slice (or nspec slices)
+  double* dred = nullptr; int32_t* dist = nullptr;
+  DevBatch<double> batch;
+  std::vector<Staged> staged;
+  std::vector<void*> pool;                         // staging buffers of this call
+  std::vector<double> norms;
+  ~Ctx() {}
+};
+thread_local Ctx g_ctx;
+
+int fail(int e) { if (e) g_ctx.err = e; return e; }
+
+int ensure_stream() {
+  if (!g_ctx.st) {
+    if (cudaStreamCreateWithFlags(&g_ctx.st, cudaStreamNonBlocking) != cudaSuccess) return OT2D_ERR_CUDA;
+    if (cudaMalloc(&g_ctx.dP, sizeof(ot2d_params)) != cudaSuccess) return OT2D_ERR_NOMEM;
+    if (cudaMalloc(&g_ctx.dred, sizeof(double) * RED_N * 64) != cudaSuccess) return OT2D_ERR_NOMEM;
+    if (cudaMalloc(&g_ctx.dist, sizeof(int32_t) * IST_N * 64) != cudaSuccess) return OT2D_ERR_NOMEM;
+  }
+  return OT2D_OK;
+}
+
+// Resolve one argument.  `in`: the routine reads it; `out`: it writes it.
+void* resolve(void* p, size_t bytes, bool in, bool out, int& err) {
+  if (!p || err) return p;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) == cudaSuccess &&
+      (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged))
+    return p;
+  cudaGetLastError();
+  {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    auto it = g_reg.upper_bound((uintptr_t)p);
+    if (it != g_reg.begin()) {
+      --it;
+      uintptr_t base = it->first;
+      if ((uintptr_t)p + bytes <= base + it->second.bytes) return (char*)it->second.dev + ((uintptr_t)p - base);
+    }
+  }
+  void* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) { err = OT2D_ERR_NOMEM; return nullptr; }
+  g_ctx.pool.push_back(d);
+  if (in) {
+    if (cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  } else if (cudaMemsetAsync(d, 0, bytes, g_ctx.st) != cudaSuccess) {
+    err = OT2D_ERR_CUDA;
+  }
+  if (out) g_ctx.staged.push_back({p, d, bytes, true});
+  return d;
+}
+
+// Copy outputs back, free the staging buffers, report errors.
+int finish(int err) {
+  if (!err) {
+    for (auto& s : g_ctx.staged)
+      if (cudaMemcpyAsync(s.host, s.dev, s.bytes, cudaMemcpyDeviceToHost, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  }
+  if (cudaStreamSynchronize(g_ctx.st) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
+  for (void* d : g_ctx.pool) cudaFree(d);
+  g_ctx.pool.clear();
+  g_ctx.staged.clear();
+  return fail(err);
+}
+
+// Host copy of an argument that may be device memory (geometry set-up).
+std::vector<double> host_copy(const double* p, size_t n) {
+  std::vector<double> v(n);
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) == cudaSuccess && (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged))
+    cudaMemcpy(v.data(), p, n * sizeof(double), cudaMemcpyDeviceToHost);
+  else {
+    cudaGetLastError();
+    std::memcpy(v.data(), p, n * sizeof(double));
+  }
+  return v;
+}
+void host_store(double* p, const double* v, size_t n) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) == cudaSuccess && (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged))
+    cudaMemcpy(p, v, n * sizeof(double), cudaMemcpyHostToDevice);
+  else {
+    cudaGetLastError();
+    std::memcpy(p, v, n * sizeof(double));
+  }
+}
+
+// Scratch arrays for nslice slices; upload params.
+int prepare(int nslice, int& err) {
+  if ((err = ensure_stream())) return err;
+  if (!g_ctx.has) return err = OT2D_ERR_NOPARAMS;
+  const size_t n2 = (size_t)g_ctx.P.jd * g_ctx.P.kd, ws = (n2 + 63) / 64 * 64;
+  const size_t need = ws * 20 * nslice + 8 * ws;
+  if (need > g_ctx.wcap) {
+    if (g_ctx.dwork) cudaFree(g_ctx.dwork);
+    if (cudaMalloc(&g_ctx.dwork, need * sizeof(double)) != cudaSuccess) { g_ctx.dwork = nullptr; g_ctx.wcap = 0; return err = OT2D_ERR_NOMEM; }
+    g_ctx.wcap = need;
+  }
+  if (cudaMemcpyAsync(g_ctx.dP, &g_ctx.P, sizeof(ot2d_params), cudaMemcpyHostToDevice, g_ctx.st) != cudaSuccess)
+    return err = OT2D_ERR_CUDA;
+  return err;
+}
+
+// A slice over caller arrays (one time instance, variable stride qs).
+Slice<double> base_slice(int nsp, int nspec, int64_t qs) {
+  Slice<double> S{};
+  const ot2d_params& p = g_ctx.P;
+  S.P = g_ctx.dP;
+  S.jd = p.jd; S.kd = p.kd; S.nsp = nsp; S.nspec = nspec; S.qs = qs;
+  const size_t n2 = (size_t)p.jd * p.kd, ws = (n2 + 63) / 64 * 64;
+  S.w = g_ctx.dwork + (size_t)(nsp - 1) * ws * 20;
+  S.wstride = (int64_t)ws;
+  S.red = g_ctx.dred + (size_t)RED_N * (nsp - 1);
+  S.ist = nullptr;
+  return S;
+}
+
+int run_batch(const std::vector<Slice<double>>& sl, int& err) {
+  if (err) return err;
+  if ((err = g_ctx.batch.build(sl, g_ctx.st))) return err;
+  return err;
+}
+
+bool dims_ok(const int32_t* jd, const int32_t* kd) {
+  return jd && kd && *jd == g_ctx.P.jd && *kd == g_ctx.P.kd;
+}
+
+// face normals (and time-spectral face speeds) from the vertex grid
+int faces_upload(double* dst4, double* dst2, const double* xv, const double* yv, const double* ugv, const double* vgv,
+                 size_t ws, int& err) {
+  const ot2d_params& p = g_ctx.P;
+  const size_t nv = (size_t)p.jmax * p.kmax, n2 = (size_t)p.jd * p.kd;
+  std::vector<double> hx = host_copy(xv, nv), hy = host_copy(yv, nv), hu, hvv;
+  std::vector<double> f(4 * n2), t(2 * n2, 0.0);
+  const bool ts = p.timespectral && ugv && vgv;
+  if (ts) { hu = host_copy(ugv, nv); hvv = host_copy(vgv, nv); }
+  face_normals(p, hx.data(), hy.data(), ts ? hu.data() : nullptr, ts ? hvv.data() : nullptr, f.data(), f.data() + n2,
+               f.data() + 2 * n2, f.data() + 3 * n2, ts ? t.data() : nullptr, ts ? t.data() + n2 : nullptr);
+  for (int a = 0; a < 4; ++a)
+    if (cudaMemcpyAsync(dst4 + a * ws, f.data() + a * n2, n2 * 8, cudaMemcpyHostToDevice, g_ctx.st) != cudaSuccess)
+      err = OT2D_ERR_CUDA;
+  if (ts && dst2)
+    for (int a = 0; a < 2; ++a)
+      if (cudaMemcpyAsync(dst2 + a * ws, t.data() + a * n2, n2 * 8, cudaMemcpyHostToDevice, g_ctx.st) != cudaSuccess)
+        err = OT2D_ERR_CUDA;
+  cudaStreamSynchronize(g_ctx.st);  // host vectors go out of scope
+  return err;
+}
+
+}  // namespace
+}  // namespace ot2d
+
+using namespace ot2d;
+
+extern "C" {
+
+int ot2d_set_params(const ot2d_params* p) {
+  if (!p) return fail(OT2D_ERR_ARG);
+  if (p->nhalo != 1 || p->jd != p->jmax + 1 || p->kd != p->kmax + 1) return fail(OT2D_ERR_ARG);
+  g_ctx.P = *p;
+  g_ctx.has = true;
+  return OT2D_OK;
+}
+
+int ot2d_set_precision(int32_t mode) { return mode == OT2D_FP64 ? OT2D_OK : fail(OT2D_ERR_ARG); }
+
+int ot2d_last_error(void) { return g_ctx.err; }
+
+int ot2d_register(void* h, size_t bytes) {
+  if (!h || !bytes) return fail(OT2D_ERR_ARG);
+  void* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return fail(OT2D_ERR_NOMEM);
+  if (cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice) != cudaSuccess) { cudaFree(d); return fail(OT2D_ERR_CUDA); }
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_reg.find((uintptr_t)h);
+  if (it != g_reg.end()) { cudaFree(it->second.dev); g_reg.erase(it); }
+  g_reg[(uintptr_t)h] = Reg{bytes, d};
+  return OT2D_OK;
+}
+
+int ot2d_unregister(void* h) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_reg.find((uintptr_t)h);
+  if (it == g_reg.end()) return fail(OT2D_ERR_ARG);
+  cudaFree(it->second.dev);
+  g_reg.erase(it);
+  return OT2D_OK;
+}
+
+int ot2d_sync_to_host(void* h) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_reg.find((uintptr_t)h);
+  if (it == g_reg.end()) return fail(OT2D_ERR_ARG);
+  if (g_ctx.st) cudaStreamSynchronize(g_ctx.st);
+  return cudaMemcpy(h, it->second.dev, it->second.bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? OT2D_OK : fail(OT2D_ERR_CUDA);
+}
+
+int ot2d_sync_to_device(void* h) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_reg.find((uintptr_t)h);
+  if (it == g_reg.end()) return fail(OT2D_ERR_ARG);
+  return cudaMemcpy(it->second.dev, h, it->second.bytes, cudaMemcpyHostToDevice) == cudaSuccess ? OT2D_OK : fail(OT2D_ERR_CUDA);
+}
+
+int ot2d_rhsup(double* q, double* s, double* xx, double* xy, double* yx, double* yy, double* x, double* y,
+               double* xv, double* yv, double* xold, double* yold, double* xole, double* yole, int32_t* iblank,
+               double* ugv, double* vgv, int32_t* jd, int32_t* kd, int32_t* nei, int32_t* im, double* bt) {
+  (void)xx; (void)xy; (void)yx; (void)yy; (void)x; (void)y; (void)xold; (void)yold; (void)xole; (void)yole; (void)im; (void)bt;
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !nei || *nei != 1 || p.iunst != 0 || !q || !s || !xv || !yv || !iblank) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  const size_t ws = (size_t)S.wstride;
+  double* faces = g_ctx.dwork + ws * 20;           // 4 face-normal arrays
+  double* tjs = faces + 4 * ws;                     // 2 face-speed arrays
+  faces_upload(faces, tjs, xv, yv, ugv, vgv, ws, err);
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, false, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
+  S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
+  S.fxa = faces; S.fya = faces + ws; S.gxa = faces + 2 * ws; S.gya = faces + 3 * ws;
+  if (p.timespectral && ugv && vgv) { S.ftj = tjs; S.gtj = tjs + ws; }
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_faces<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 1, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && launch_assemble<double>(g_ctx.batch.d_sl, g_ctx.batch.b, AS_ACC | AS_INV, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_visrhs(double* turmu, double* q, double* s, double* xx, double* xy, double* yx, double* yy, double* ug,
+                double* vg, double* tscale, int32_t* iblank, int32_t* jd, int32_t* kd) {
+  (void)ug; (void)vg; (void)tscale;
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !q || !s || !turmu || !xx || !xy || !yx || !yy || !iblank) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, false, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
+  S.turmu = (double*)resolve(turmu, n2 * 8, true, false, err);
+  S.xx = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && p.invisc == 0) {
+    if (launch_faces<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, 1, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+    if (!err && launch_assemble<double>(g_ctx.batch.d_sl, g_ctx.batch.b, AS_ACC | AS_VISC, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  }
+  return finish(err);
+}
+
+int ot2d_bc(double* q, double* x, double* y, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+            int32_t* im, int32_t* jd, int32_t* kd, double* bt) {
+  (void)x; (void)y; (void)im; (void)bt;
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !q || !xx || !xy || !yx || !yy) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
+  S.xx64 = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy64 = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx64 = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy64 = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug64 = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg64 = (double*)resolve(vg, n2 * 8, true, false, err);
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_bc<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_rbc(double* q, double* s, double* x, double* y, double* xx, double* xy, double* yx, double* yy, double* ug,
+             double* vg, int32_t* im, int32_t* jd, int32_t* kd, double* bt) {
+  (void)x; (void)y; (void)xx; (void)xy; (void)yx; (void)yy; (void)ug; (void)vg; (void)im; (void)bt;
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !q || !s) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, false, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_rbc<double>(g_ctx.batch.d_sl, g_ctx.batch.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_time_step(double* q, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+                   double* tscale, double* bt, int32_t* iblank, int32_t* jd, int32_t* kd) {
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !q || !xx || !xy || !yx || !yy || !tscale || !bt || !iblank) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, false, err);
+  S.xx = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg = (double*)resolve(vg, n2 * 8, true, false, err);
+  S.tscale = (double*)resolve(tscale, n2 * 8, false, true, err);
+  S.bt = (double*)resolve(bt, n2 * 8, false, true, err);
+  S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_time_step<double>(g_ctx.batch.d_sl, g_ctx.batch.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+               double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu,
+               double* tscale) {
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !js || !je || !ks || !ke || *js != p.jbeg || *je != p.jend || *ks != p.kbeg || *ke != p.kend)
+    return fail(OT2D_ERR_ARG);
+  if (!q || !s || !xx || !xy || !yx || !yy || !turmu || !tscale || p.iunst == 2) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
+  S.xx = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg = (double*)resolve(vg, n2 * 8, true, false, err);
+  S.turmu = (double*)resolve(turmu, n2 * 8, true, false, err);
+  S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_lusgs<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
+                double* xy, double* yx, double* yy, double* ug, double* vg, int32_t* jd, int32_t* kd,
+                double* tscale, int32_t* iblank, int32_t* im, int32_t* nsp) {
+  (void)im; (void)nsp;
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || p.iturb != 1 || p.lamin || !q || !s || !turmu || !x || !y || !xv || !yv || !tscale || !iblank)
+    return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, nv = (size_t)p.jmax * p.kmax;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  const size_t ws = (size_t)S.wstride;
+  double* dsn = g_ctx.dwork + ws * 20;
+  {
+    std::vector<double> hx = host_copy(x, n2), hy = host_copy(y, n2), hxv = host_copy(xv, nv), hyv = host_copy(yv, nv);
+    std::vector<double> sn(n2);
+    wall_distance(p, hx.data(), hy.data(), hxv.data(), hyv.data(), sn.data());
+    if (cudaMemcpy(dsn, sn.data(), n2 * 8, cudaMemcpyHostToDevice) != cudaSuccess) err = OT2D_ERR_CUDA;
+  }
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, false, err);
+  S.turmu = (double*)resolve(turmu, n2 * 8, true, true, err);
+  S.xx = S.xx64 = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = S.xy64 = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = S.yx64 = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = S.yy64 = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug = S.ug64 = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg = S.vg64 = (double*)resolve(vg, n2 * 8, true, false, err);
+  S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
+  S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
+  S.sn = dsn;
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_sa<double>(g_ctx.batch.d_sl, g_ctx.batch.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_timespectralrhs(double* q, double* s, double* Ds, int32_t* jd, int32_t* kd, int32_t* nsp) {
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !nsp || *nsp < 1 || *nsp > p.nspec || !q || !s || !Ds) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, ns = (size_t)p.nspec;
+  Slice<double> S = base_slice(1, p.nspec, (int64_t)(n2 * ns));
+  S.nsp = *nsp;
+  double* dq = (double*)resolve(q, n2 * ns * p.nq * 8, true, false, err);
+  double* ds = (double*)resolve(s, n2 * ns * p.nv * 8, true, true, err);
+  S.Ds = (double*)resolve(Ds, ns * ns * 8, true, false, err);
+  if (!err) { S.q = S.q64 = dq + (size_t)(*nsp - 1) * n2; S.s = ds + (size_t)(*nsp - 1) * n2; }
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && p.timespectral &&
+      launch_assemble<double>(g_ctx.batch.d_sl, g_ctx.batch.b, AS_ACC | AS_TS, g_ctx.st) != cudaSuccess)
+    err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, double* x, double* y, double* xv,
+              double* yv, int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+              double* ugv, double* vgv, double* xold, double* yold, double* xole, double* yole, double* turmu,
+              double* tscale, double* bt, double* Ds, int32_t* im, int32_t* jd, int32_t* kd) {
+  (void)qtn; (void)qtnm1; (void)qnewt; (void)xold; (void)yold; (void)xole; (void)yole; (void)im; (void)bt;
+  const int nspec = g_ctx.has ? g_ctx.P.nspec : 1;
+  int err = 0;
+  if (prepare(nspec, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || p.ilhs != 1 || p.itnmax > 1 || (!p.lamin && p.iturb != 1)) return fail(OT2D_ERR_ARG);
+  if (!q || !s || !x || !y || !xv || !yv || !iblank || !xx || !xy || !yx || !yy || !turmu || !tscale) return fail(OT2D_ERR_ARG);
+  if (p.timespectral && (!ugv || !vgv || !ug || !vg || !Ds)) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, ns = (size_t)nspec, nv = (size_t)p.jmax * p.kmax, qs = n2 * ns;
+  double* dq = (double*)resolve(q, qs * p.nq * 8, true, true, err);
+  double* ds = (double*)resolve(s, qs * p.nv * 8, false, true, err);
+  int32_t* dib = (int32_t*)resolve(iblank, qs * 4, true, false, err);
+  double* dxx = (double*)resolve(xx, qs * 8, true, false, err);
+  double* dxy = (double*)resolve(xy, qs * 8, true, false, err);
+  double* dyx = (double*)resolve(yx, qs * 8, true, false, err);
+  double* dyy = (double*)resolve(yy, qs * 8, true, false, err);
+  double* dug = p.timespectral ? (double*)resolve(ug, qs * 8, true, false, err) : nullptr;
+  double* dvg = p.timespectral ? (double*)resolve(vg, qs * 8, true, false, err) : nullptr;
+  double* dturmu = (double*)resolve(turmu, qs * 8, true, true, err);
+  double* dts = (double*)resolve(tscale, qs * 8, true, false, err);
+  double* dDs = p.timespectral ? (double*)resolve(Ds, ns * ns * 8, true, false, err) : nullptr;
+  // per-instance face normals and wall distance from the host grid
+  const size_t ws = (n2 + 63) / 64 * 64;
+  double* extra = nullptr;
+  if (!err && cudaMalloc(&extra, sizeof(double) * ws * 7 * ns) != cudaSuccess) err = OT2D_ERR_NOMEM;
+  if (extra) g_ctx.pool.push_back(extra);
+  std::vector<Slice<double>> sl;
+  std::vector<double> hx = host_copy(x, qs), hy = host_copy(y, qs), hxv = host_copy(xv, nv * ns), hyv = host_copy(yv, nv * ns);
+  for (int nsp = 1; nsp <= nspec && !err; ++nsp) {
+    double* e = extra + (size_t)(nsp - 1) * ws * 7;
+    faces_upload(e, e + 4 * ws, xv + (nsp - 1) * nv, yv + (nsp - 1) * nv, ugv ? ugv + (nsp - 1) * nv : nullptr,
+                 vgv ? vgv + (nsp - 1) * nv : nullptr, ws, err);
+    std::vector<double> sn(n2);
+    wall_distance(p, hx.data() + (nsp - 1) * n2, hy.data() + (nsp - 1) * n2, hxv.data() + (nsp - 1) * nv,
+                  hyv.data() + (nsp - 1) * nv, sn.data());
+    if (cudaMemcpy(e + 6 * ws, sn.data(), n2 * 8, cudaMemcpyHostToDevice) != cudaSuccess) err = OT2D_ERR_CUDA;
+    Slice<double> S = base_slice(nsp, nspec, (int64_t)qs);
+    const size_t o = (size_t)(nsp - 1) * n2;
+    S.q = S.q64 = dq + o; S.s = ds + o; S.iblank = dib + o;
+    S.xx = S.xx64 = dxx + o; S.xy = S.xy64 = dxy + o; S.yx = S.yx64 = dyx + o; S.yy = S.yy64 = dyy + o;
+    S.ug = S.ug64 = dug ? dug + o : nullptr; S.vg = S.vg64 = dvg ? dvg + o : nullptr;
+    S.turmu = dturmu + o; S.tscale = dts + o;
+    S.bt = nullptr;  // bt is 1 on the non-preconditioned path
+    S.fxa = e; S.fya = e + ws; S.gxa = e + 2 * ws; S.gya = e + 3 * ws;
+    S.ftj = p.timespectral ? e + 4 * ws : nullptr; S.gtj = p.timespectral ? e + 5 * ws : nullptr;
+    S.sn = e + 6 * ws;
+    S.Ds = dDs;
+    sl.push_back(S);
+  }
+  run_batch(sl, err);
+  const auto& B = g_ctx.batch;
+  const int visc = p.invisc ? 0 : 1, turb = (!p.lamin && p.iturb == 1) ? 1 : 0;
+  if (!err && launch_bc<double>(B.d_sl, B.b, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && launch_residual<double>(B.d_sl, B.b, visc, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && launch_rbc<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && launch_lusgs<double>(B.d_sl, B.b, 1, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && turb && launch_sa<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && launch_update<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err) {
+    std::vector<double> red((size_t)RED_N * nspec);
+    cudaMemcpyAsync(red.data(), g_ctx.dred, red.size() * 8, cudaMemcpyDeviceToHost, g_ctx.st);
+    cudaStreamSynchronize(g_ctx.st);
+    g_ctx.norms.assign(3 * nspec, 0.0);
+    for (int i = 0; i < nspec; ++i)
+      for (int c = 0; c < 3; ++c) g_ctx.norms[3 * i + c] = red[(size_t)RED_N * i + c];
+    for (int i = 0; i < nspec; ++i) if (!(g_ctx.norms[3 * i] <= 1000.0)) err = OT2D_ERR_NORM;
+  }
+  int e2 = finish(err == OT2D_ERR_NORM ? 0 : err);
+  return e2 ? e2 : fail(err);
+}
+
+int ot2d_last_norms(double* out, int32_t n) {
+  if (!out || n < 0) return fail(OT2D_ERR_ARG);
+  for (int i = 0; i < n && i < (int)g_ctx.norms.size(); ++i) out[i] = g_ctx.norms[i];
+  return OT2D_OK;
+}
+
+int ot2d_monitor(int32_t* mstop, double* q, int32_t* jd, int32_t* kd) {
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!mstop || !dims_ok(jd, kd) || !q) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, ns = (size_t)p.nspec;
+  double* dq = (double*)resolve(q, n2 * ns * p.nq * 8, true, false, err);
+  std::vector<Slice<double>> sl;
+  for (int nsp = 1; nsp <= p.nspec && !err; ++nsp) {
+    Slice<double> S = base_slice(1, 1, (int64_t)(n2 * ns));
+    S.q = S.q64 = dq + (size_t)(nsp - 1) * n2;
+    S.ist = g_ctx.dist;
+    sl.push_back(S);
+  }
+  if (!err) cudaMemsetAsync(g_ctx.dist, 0, sizeof(int32_t) * IST_N, g_ctx.st);
+  run_batch(sl, err);
+  if (!err && launch_monitor<double>(g_ctx.batch.d_sl, g_ctx.batch.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  int32_t ist[IST_N] = {0, 0, 0, 0};
+  if (!err) cudaMemcpyAsync(ist, g_ctx.dist, sizeof(ist), cudaMemcpyDeviceToHost, g_ctx.st);
+  err = finish(err);
+  *mstop = (ist[2] & 2) ? 1 : 0;
+  return err;
+}
+
+int ot2d_force2d(int32_t* jd, int32_t* kd, double* x, double* y, double* xv, double* yv, double* q, double* xx,
+                 double* xy, double* yx, double* yy, double* cfx, double* cfy, double* cm0, double* cpower,
+                 int32_t* nsp) {
+  (void)x; (void)y; (void)nsp;
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !q || !xv || !yv || !xx || !xy || !yx || !yy || !cfx || !cfy || !cm0 || !cpower)
+    return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, nv = (size_t)p.jmax * p.kmax;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, false, err);
+  S.xx64 = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy64 = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx64 = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy64 = (double*)resolve(yy, n2 * 8, true, false, err);
+  double* dxv = (double*)resolve(xv, nv * 8, true, false, err);
+  double* dyv = (double*)resolve(yv, nv * 8, true, false, err);
+  const double** ptrs = nullptr;
+  double* out = nullptr;
+  if (!err && cudaMalloc(&ptrs, 2 * sizeof(double*)) != cudaSuccess) err = OT2D_ERR_NOMEM;
+  if (ptrs) g_ctx.pool.push_back((void*)ptrs);
+  if (!err && cudaMalloc(&out, 4 * sizeof(double)) != cudaSuccess) err = OT2D_ERR_NOMEM;
+  if (out) g_ctx.pool.push_back(out);
+  const double* hp[2] = {dxv, dyv};
+  if (!err) cudaMemcpyAsync(ptrs, hp, sizeof(hp), cudaMemcpyHostToDevice, g_ctx.st);
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_forces<double>(g_ctx.batch.d_sl, g_ctx.batch.b, ptrs, ptrs + 1, out, g_ctx.st) != cudaSuccess)
+    err = OT2D_ERR_CUDA;
+  double h[4] = {0, 0, 0, 0};
+  if (!err) cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, g_ctx.st);
+  err = finish(err);
+  *cfx = h[0]; *cfy = h[1]; *cm0 = h[2]; *cpower = h[3];
+  return err;
+}
+
+int ot2d_find_cellcenter(double* x, double* y, double* xv, double* yv, int32_t* jd, int32_t* kd, int32_t* im) {
+  (void)im;
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !x || !y || !xv || !yv) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, nv = (size_t)p.jmax * p.kmax;
+  std::vector<double> hxv = host_copy(xv, nv), hyv = host_copy(yv, nv), hx(n2), hy(n2);
+  cell_centres(p, hxv.data(), hyv.data(), hx.data(), hy.data());
+  host_store(x, hx.data(), n2);
+  host_store(y, hy.data(), n2);
+  return OT2D_OK;
+}
+
+int ot2d_metfv(double* q, double* x, double* y, double* xv, double* yv, double* xx, double* xy, double* yx,
+               double* yy, int32_t* jd, int32_t* kd, int32_t* im) {
+  (void)x; (void)y; (void)im;
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !q || !xv || !yv || !xx || !xy || !yx || !yy) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, nv = (size_t)p.jmax * p.kmax;
+  std::vector<double> hxv = host_copy(xv, nv), hyv = host_copy(yv, nv);
+  std::vector<double> J(n2), a(n2), b(n2), c(n2), d(n2);
+  int nneg = metrics(p, hxv.data(), hyv.data(), J.data(), a.data(), b.data(), c.data(), d.data());
+  host_store(q + (size_t)(p.nq - 1) * n2, J.data(), n2);
+  host_store(xx, a.data(), n2); host_store(xy, b.data(), n2);
+  host_store(yx, c.data(), n2); host_store(yy, d.data(), n2);
+  return nneg ? fail(OT2D_ERR_ARG) : OT2D_OK;
+}
+
+}  // extern "C"

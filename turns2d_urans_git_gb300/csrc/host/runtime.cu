@@ -1,0 +1,309 @@
+// runtime.cu -- device residency of one solve and batch construction.
+// Layout in HBM keeps the reference's column-major arrays
+// (q(jd,kd,nspec,nq), s(jd,kd,nspec,nv), metrics (jd,kd,nspec)) so that a
+// solve's arrays can be exchanged with Fortran callers unchanged.
+#include "runtime.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "geom.h"
+
+namespace ot2d {
+
+const char* cuda_err_name(cudaError_t e) { return cudaGetErrorName(e); }
+
+namespace {
+constexpr size_t ALIGN = 256;
+inline size_t al(size_t b) { return (b + ALIGN - 1) / ALIGN * ALIGN; }
+constexpr int NSCRATCH = 20;  // scratch arrays per slice (residual phase is the largest user)
+
+struct Layout {
+  size_t total = 0;
+  size_t take(size_t bytes) { size_t o = total; total += al(bytes); return o; }
+};
+
+// Plan (and optionally carve) the allocation of one solve.
+template <class F>
+size_t plan(const ot2d_params& p, int precision, F&& assign) {
+  const size_t nspec = (size_t)p.nspec, n2 = (size_t)p.jd * p.kd, nvert = (size_t)p.jmax * p.kmax;
+  const size_t ws = (n2 + 63) / 64 * 64;
+  const bool mixed = precision == OT2D_FP32_MIXED;
+  const size_t rb = mixed ? sizeof(float) : sizeof(double);
+  const bool ts = p.timespectral != 0;
+  Layout L;
+  assign("P", L.take(sizeof(ot2d_params)));
+  assign("q64", L.take(sizeof(double) * n2 * nspec * p.nq));
+  assign("xx64", L.take(sizeof(double) * n2 * nspec));
+  assign("xy64", L.take(sizeof(double) * n2 * nspec));
+  assign("yx64", L.take(sizeof(double) * n2 * nspec));
+  assign("yy64", L.take(sizeof(double) * n2 * nspec));
+  if (ts) {
+    assign("ug64", L.take(sizeof(double) * n2 * nspec));
+    assign("vg64", L.take(sizeof(double) * n2 * nspec));
+    assign("Ds", L.take(sizeof(double) * nspec * nspec));
+  }
+  assign("xv", L.take(sizeof(double) * nvert * nspec));
+  assign("yv", L.take(sizeof(double) * nvert * nspec));
+  assign("iblank", L.take(sizeof(int32_t) * n2 * nspec));
+  if (mixed) {
+    assign("q", L.take(rb * n2 * nspec * p.nq));
+    assign("xx", L.take(rb * n2 * nspec));
+    assign("xy", L.take(rb * n2 * nspec));
+    assign("yx", L.take(rb * n2 * nspec));
+    assign("yy", L.take(rb * n2 * nspec));
+    if (ts) { assign("ug", L.take(rb * n2 * nspec)); assign("vg", L.take(rb * n2 * nspec)); }
+  }
+  assign("s", L.take(rb * n2 * nspec * p.nv));
+  assign("fxa", L.take(rb * n2 * nspec));
+  assign("fya", L.take(rb * n2 * nspec));
+  assign("gxa", L.take(rb * n2 * nspec));
+  assign("gya", L.take(rb * n2 * nspec));
+  if (ts) { assign("ftj", L.take(rb * n2 * nspec)); assign("gtj", L.take(rb * n2 * nspec)); }
+  assign("tscale", L.take(rb * n2 * nspec));
+  assign("bt", L.take(rb * n2 * nspec));
+  assign("turmu", L.take(rb * n2 * nspec));
+  assign("sn", L.take(rb * n2 * nspec));
+  assign("w", L.take(rb * ws * NSCRATCH * nspec));
+  return L.total;
+}
+
+template <class T>
+cudaError_t upload_as(void* dst, const double* src, size_t n, cudaStream_t st, std::vector<T>& tmp) {
+  if (std::is_same<T, double>::value) return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, st);
+  tmp.resize(n);
+  for (size_t i = 0; i < n; ++i) tmp[i] = (T)src[i];
+  return cudaMemcpyAsync(dst, tmp.data(), n * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+}  // namespace
+
+size_t solve_bytes(const ot2d_params& p, int precision) {
+  return plan(p, precision, [](const char*, size_t) {});
+}
+
+void solve_destroy(DevSolve& d) {
+  if (d.mem) cudaFree(d.mem);
+  d = DevSolve{};
+}
+
+int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double* xv1, const double* yv1,
+                 cudaStream_t st) {
+  if (!xv1 || !yv1 || p.nspec < 1 || p.nhalo != 1 || p.jd != p.jmax + 1 || p.kd != p.kmax + 1) return OT2D_ERR_ARG;
+  if (precision != OT2D_FP64 && precision != OT2D_FP32_MIXED) return OT2D_ERR_ARG;
+  if (p.ilhs != 1) return OT2D_ERR_ARG;            // ADI operator: not in this build
+  if (!p.lamin && p.iturb != 1) return OT2D_ERR_ARG;  // SA only
+  d = DevSolve{};
+  d.P = p; d.precision = precision; d.nspec = p.nspec;
+  d.n2 = (size_t)p.jd * p.kd; d.nvert = (size_t)p.jmax * p.kmax; d.wstride = (d.n2 + 63) / 64 * 64;
+  std::vector<std::pair<const char*, size_t>> offs;
+  d.bytes = plan(p, precision, [&](const char* n, size_t o) { offs.emplace_back(n, o); });
+  if (cudaMalloc(&d.mem, d.bytes) != cudaSuccess) { d.mem = nullptr; return OT2D_ERR_NOMEM; }
+  char* base = (char*)d.mem;
+  for (auto& o : offs) {
+    void* ptr = base + o.second;
+    std::string n = o.first;
+    if (n == "P") d.dP = (ot2d_params*)ptr;
+    else if (n == "q64") d.q64 = (double*)ptr;
+    else if (n == "xx64") d.xx64 = (double*)ptr;
+    else if (n == "xy64") d.xy64 = (double*)ptr;
+    else if (n == "yx64") d.yx64 = (double*)ptr;
+    else if (n == "yy64") d.yy64 = (double*)ptr;
+    else if (n == "ug64") d.ug64 = (double*)ptr;
+    else if (n == "vg64") d.vg64 = (double*)ptr;
+    else if (n == "Ds") d.Ds = (double*)ptr;
+    else if (n == "xv") d.xv = (double*)ptr;
+    else if (n == "yv") d.yv = (double*)ptr;
+    else if (n == "iblank") d.iblank = (int32_t*)ptr;
+    else if (n == "q") d.q = ptr;
+    else if (n == "xx") d.xx = ptr;
+    else if (n == "xy") d.xy = ptr;
+    else if (n == "yx") d.yx = ptr;
+    else if (n == "yy") d.yy = ptr;
+    else if (n == "ug") d.ug = ptr;
+    else if (n == "vg") d.vg = ptr;
+    else if (n == "s") d.s = ptr;
+    else if (n == "fxa") d.fxa = ptr;
+    else if (n == "fya") d.fya = ptr;
+    else if (n == "gxa") d.gxa = ptr;
+    else if (n == "gya") d.gya = ptr;
+    else if (n == "ftj") d.ftj = ptr;
+    else if (n == "gtj") d.gtj = ptr;
+    else if (n == "tscale") d.tscale = ptr;
+    else if (n == "bt") d.bt = ptr;
+    else if (n == "turmu") d.turmu = ptr;
+    else if (n == "sn") d.sn = ptr;
+    else if (n == "w") d.w = ptr;
+  }
+  const bool mixed = precision == OT2D_FP32_MIXED;
+  if (!mixed) { d.q = d.q64; d.xx = d.xx64; d.xy = d.xy64; d.yx = d.yx64; d.yy = d.yy64; d.ug = d.ug64; d.vg = d.vg64; }
+  // ---- host geometry, per time instance
+  const size_t n2 = d.n2, nv = d.nvert, ns = (size_t)p.nspec;
+  const size_t qs = n2 * ns;
+  std::vector<double> q(qs * p.nq, 0.0), xx(qs), xy(qs), yx(qs), yy(qs), ug(qs, 0.0), vg(qs, 0.0);
+  std::vector<double> xv(nv * ns), yv(nv * ns), ugv(nv * ns, 0.0), vgv(nv * ns, 0.0);
+  std::vector<double> x(n2), y(n2), sn(qs), fxa(qs), fya(qs), gxa(qs), gya(qs), ftj(qs, 0.0), gtj(qs, 0.0);
+  std::vector<double> Ds(ns * ns, 0.0);
+  const double pi = 4.0 * std::atan(1.0);
+  if (p.timespectral) ts_operator(p.nspec, Ds.data());
+  for (int nsp = 1; nsp <= p.nspec; ++nsp) {
+    double* xvn = xv.data() + (nsp - 1) * nv;
+    double* yvn = yv.data() + (nsp - 1) * nv;
+    double tspec = 0.0;
+    if (p.rf != 0) tspec = 2 * pi * (nsp - 1) / p.nspec / std::fabs(p.rf);
+    if (nsp == 1) { std::memcpy(xvn, xv1, nv * sizeof(double)); std::memcpy(yvn, yv1, nv * sizeof(double)); }
+    else ts_pitch_grid(p, xv1, yv1, tspec, xvn, yvn);
+    const size_t o = (nsp - 1) * n2;
+    cell_centres(p, xvn, yvn, x.data(), y.data());
+    double* J = q.data() + (p.nq - 1) * qs + o;
+    if (metrics(p, xvn, yvn, J, xx.data() + o, xy.data() + o, yx.data() + o, yy.data() + o) != 0) {
+      solve_destroy(d);
+      return OT2D_ERR_ARG;
+    }
+    if (p.timespectral)
+      ts_grid_speed(p, x.data(), y.data(), xvn, yvn, tspec, ug.data() + o, vg.data() + o, ugv.data() + (nsp - 1) * nv,
+                    vgv.data() + (nsp - 1) * nv);
+    freestream(p, q.data() + o, qs);
+    wall_distance(p, x.data(), y.data(), xvn, yvn, sn.data() + o);
+    face_normals(p, xvn, yvn, ugv.data() + (nsp - 1) * nv, vgv.data() + (nsp - 1) * nv, fxa.data() + o, fya.data() + o,
+                 gxa.data() + o, gya.data() + o, p.timespectral ? ftj.data() + o : nullptr,
+                 p.timespectral ? gtj.data() + o : nullptr);
+  }
+  bool bad = false;
+  auto chk = [&](cudaError_t e) { if (e != cudaSuccess) bad = true; };
+  chk(cudaMemcpyAsync(d.dP, &p, sizeof(p), cudaMemcpyHostToDevice, st));
+  chk(cudaMemcpyAsync(d.q64, q.data(), q.size() * 8, cudaMemcpyHostToDevice, st));
+  chk(cudaMemcpyAsync(d.xx64, xx.data(), qs * 8, cudaMemcpyHostToDevice, st));
+  chk(cudaMemcpyAsync(d.xy64, xy.data(), qs * 8, cudaMemcpyHostToDevice, st));
+  chk(cudaMemcpyAsync(d.yx64, yx.data(), qs * 8, cudaMemcpyHostToDevice, st));
+  chk(cudaMemcpyAsync(d.yy64, yy.data(), qs * 8, cudaMemcpyHostToDevice, st));
+  if (p.timespectral) {
+    chk(cudaMemcpyAsync(d.ug64, ug.data(), qs * 8, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(d.vg64, vg.data(), qs * 8, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(d.Ds, Ds.data(), ns * ns * 8, cudaMemcpyHostToDevice, st));
+  }
+  chk(cudaMemcpyAsync(d.xv, xv.data(), xv.size() * 8, cudaMemcpyHostToDevice, st));
+  chk(cudaMemcpyAsync(d.yv, yv.data(), yv.size() * 8, cudaMemcpyHostToDevice, st));
+  std::vector<int32_t> ib(qs, 1);
+  chk(cudaMemcpyAsync(d.iblank, ib.data(), qs * 4, cudaMemcpyHostToDevice, st));
+  if (mixed) {
+    std::vector<float> t1, t2, t3, t4, t5, t6, t7, t8, t9, t10, t11, t12, t13, t14, t15;
+    chk(upload_as<float>(d.q, q.data(), q.size(), st, t1));
+    chk(upload_as<float>(d.xx, xx.data(), qs, st, t2));
+    chk(upload_as<float>(d.xy, xy.data(), qs, st, t3));
+    chk(upload_as<float>(d.yx, yx.data(), qs, st, t4));
+    chk(upload_as<float>(d.yy, yy.data(), qs, st, t5));
+    if (p.timespectral) { chk(upload_as<float>(d.ug, ug.data(), qs, st, t6)); chk(upload_as<float>(d.vg, vg.data(), qs, st, t7)); }
+    chk(upload_as<float>(d.fxa, fxa.data(), qs, st, t8));
+    chk(upload_as<float>(d.fya, fya.data(), qs, st, t9));
+    chk(upload_as<float>(d.gxa, gxa.data(), qs, st, t10));
+    chk(upload_as<float>(d.gya, gya.data(), qs, st, t11));
+    if (p.timespectral) { chk(upload_as<float>(d.ftj, ftj.data(), qs, st, t12)); chk(upload_as<float>(d.gtj, gtj.data(), qs, st, t13)); }
+    chk(upload_as<float>(d.sn, sn.data(), qs, st, t14));
+    chk(cudaMemsetAsync(d.turmu, 0, qs * sizeof(float), st));
+    chk(cudaStreamSynchronize(st));
+  } else {
+    chk(cudaMemcpyAsync(d.fxa, fxa.data(), qs * 8, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(d.fya, fya.data(), qs * 8, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(d.gxa, gxa.data(), qs * 8, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(d.gya, gya.data(), qs * 8, cudaMemcpyHostToDevice, st));
+    if (p.timespectral) {
+      chk(cudaMemcpyAsync(d.ftj, ftj.data(), qs * 8, cudaMemcpyHostToDevice, st));
+      chk(cudaMemcpyAsync(d.gtj, gtj.data(), qs * 8, cudaMemcpyHostToDevice, st));
+    }
+    chk(cudaMemcpyAsync(d.sn, sn.data(), qs * 8, cudaMemcpyHostToDevice, st));
+    chk(cudaMemsetAsync(d.turmu, 0, qs * sizeof(double), st));
+    chk(cudaStreamSynchronize(st));
+  }
+  if (bad) { solve_destroy(d); return OT2D_ERR_CUDA; }
+  return OT2D_OK;
+}
+
+template <class R>
+Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
+  Slice<R> S{};
+  const ot2d_params& p = d.P;
+  const size_t o = (size_t)(nsp - 1) * d.n2;
+  auto R_ = [&](void* a) -> R* { return a ? (R*)a + o : nullptr; };
+  auto D_ = [&](double* a) -> double* { return a ? a + o : nullptr; };
+  S.P = d.dP;
+  S.jd = p.jd; S.kd = p.kd; S.nsp = nsp; S.nspec = p.nspec;
+  S.qs = (int64_t)d.n2 * p.nspec;
+  S.q = R_(d.q); S.q64 = D_(d.q64); S.s = R_(d.s);
+  S.xx = R_(d.xx); S.xy = R_(d.xy); S.yx = R_(d.yx); S.yy = R_(d.yy);
+  S.fxa = R_(d.fxa); S.fya = R_(d.fya); S.gxa = R_(d.gxa); S.gya = R_(d.gya);
+  S.ftj = p.timespectral ? R_(d.ftj) : nullptr; S.gtj = p.timespectral ? R_(d.gtj) : nullptr;
+  S.ug = p.timespectral ? R_(d.ug) : nullptr; S.vg = p.timespectral ? R_(d.vg) : nullptr;
+  S.tscale = R_(d.tscale); S.bt = R_(d.bt); S.turmu = R_(d.turmu);
+  S.iblank = d.iblank + o;
+  S.sn = R_(d.sn);
+  S.w = (R*)d.w + (size_t)(nsp - 1) * d.wstride * NSCRATCH;
+  S.wstride = (int64_t)d.wstride;
+  S.red = red; S.ist = ist;
+  S.Ds = p.timespectral ? d.Ds : nullptr;
+  S.xx64 = D_(d.xx64); S.xy64 = D_(d.xy64); S.yx64 = D_(d.yx64); S.yy64 = D_(d.yy64);
+  S.ug64 = p.timespectral ? D_(d.ug64) : nullptr; S.vg64 = p.timespectral ? D_(d.vg64) : nullptr;
+  return S;
+}
+template Slice<double> make_slice<double>(const DevSolve&, int, double*, int32_t*);
+template Slice<float> make_slice<float>(const DevSolve&, int, double*, int32_t*);
+
+template <class R>
+int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
+  const int n = (int)sl.size();
+  std::vector<int32_t> idx(3 * (n + 1));
+  std::vector<ot2d_params> hp;  // not needed: params live on the device
+  int cells = 0, jl = 0, kl = 0, maxw = 1, maxwall = 1;
+  // host copies of the dims come from the slices themselves (jd, kd); the
+  // interior extents follow from nhalo = 1
+  for (int i = 0; i < n; ++i) {
+    idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl;
+    const int jd = sl[i].jd, kd = sl[i].kd;
+    cells += (jd * kd + CELL_BS - 1) / CELL_BS;
+    jl += kd - 2;   // k-lines solved along j
+    kl += jd - 2;   // j-lines solved along k
+    maxw = std::max(maxw, (kd - 2 + 31) / 32);
+    maxwall = std::max(maxwall, jd);
+  }
+  idx[n] = cells; idx[2 * (n + 1) - 1] = jl; idx[3 * (n + 1) - 1] = kl;
+  if ((size_t)n > cap_sl) {
+    if (d_sl) cudaFree(d_sl);
+    if (d_idx) cudaFree(d_idx);
+    cap_sl = std::max((size_t)n, (size_t)2 * cap_sl);
+    if (cudaMalloc(&d_sl, cap_sl * sizeof(Slice<R>)) != cudaSuccess) return OT2D_ERR_NOMEM;
+    if (cudaMalloc(&d_idx, 3 * (cap_sl + 1) * sizeof(int32_t)) != cudaSuccess) return OT2D_ERR_NOMEM;
+  }
+  if ((size_t)cells > cap_part) {
+    if (d_part) cudaFree(d_part);
+    cap_part = std::max((size_t)cells, (size_t)2 * cap_part);
+    if (cudaMalloc(&d_part, cap_part * sizeof(NormPart)) != cudaSuccess) return OT2D_ERR_NOMEM;
+  }
+  if (cudaMemcpyAsync(d_sl, sl.data(), n * sizeof(Slice<R>), cudaMemcpyHostToDevice, st) != cudaSuccess) return OT2D_ERR_CUDA;
+  if (cudaMemcpyAsync(d_idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return OT2D_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return OT2D_ERR_CUDA;
+  b.nslice = n;
+  b.cell_blocks = cells;
+  b.max_lu_warps = maxw;
+  b.max_wall = maxwall;
+  b.jlines = jl; b.klines = kl;
+  b.d_first = d_idx; b.d_jfirst = d_idx + (n + 1); b.d_kfirst = d_idx + 2 * (n + 1);
+  b.d_part = d_part;
+  return OT2D_OK;
+}
+
+template <class R>
+void DevBatch<R>::release() {
+  if (d_sl) cudaFree(d_sl);
+  if (d_idx) cudaFree(d_idx);
+  if (d_part) cudaFree(d_part);
+  d_sl = nullptr; d_idx = nullptr; d_part = nullptr; cap_sl = cap_part = 0;
+}
+
+template struct DevBatch<double>;
+template struct DevBatch<float>;
+
+}  // namespace ot2d

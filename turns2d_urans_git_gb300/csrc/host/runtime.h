@@ -1,0 +1,68 @@
+// runtime.h -- device residency of solves and batch construction shared by
+// the batched solver (solver.cu) and the drop-in layer (dropin.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+#include "ot2d.h"
+#include "../kernels/dev_common.cuh"
+#include "../kernels/k_misc.cuh"
+#include "../kernels/launch.h"
+
+namespace ot2d {
+
+// reduction / status record of one slice (red: 8 doubles, ist: 4 ints)
+//  red: rsum, resrho, resmax, resmax key, rsum at it 1, rsum now, peak rsum, 10^-orders
+//  ist: istep0, istep, status bits (1 norm, 2 monitor), iteration of convergence
+constexpr int RED_N = 8, IST_N = 4;
+
+// All device arrays of one solve (every time instance), carved from one
+// allocation.  FP64 arrays always exist; the compute-type arrays alias the
+// FP64 ones on the plain path.
+struct DevSolve {
+  ot2d_params P{};
+  int precision = OT2D_FP64;
+  int nspec = 1;
+  size_t n2 = 0, nvert = 0, wstride = 0;
+  void* mem = nullptr;
+  size_t bytes = 0;
+  ot2d_params* dP = nullptr;
+  double *q64 = nullptr, *xx64 = nullptr, *xy64 = nullptr, *yx64 = nullptr, *yy64 = nullptr;
+  double *ug64 = nullptr, *vg64 = nullptr, *xv = nullptr, *yv = nullptr, *Ds = nullptr;
+  int32_t* iblank = nullptr;
+  // compute type (double* or float*)
+  void *q = nullptr, *s = nullptr, *xx = nullptr, *xy = nullptr, *yx = nullptr, *yy = nullptr;
+  void *fxa = nullptr, *fya = nullptr, *gxa = nullptr, *gya = nullptr, *ftj = nullptr, *gtj = nullptr;
+  void *ug = nullptr, *vg = nullptr, *tscale = nullptr, *bt = nullptr, *turmu = nullptr, *sn = nullptr, *w = nullptr;
+};
+
+// bytes one solve needs on the device
+size_t solve_bytes(const ot2d_params& p, int precision);
+// allocate + fill the geometry and the freestream state of a solve from the
+// vertex grid of time instance 1 (xv1, yv1: jmax*kmax).  Returns OT2D_OK,
+// OT2D_ERR_ARG (bad grid / params) or OT2D_ERR_NOMEM / OT2D_ERR_CUDA.
+int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double* xv1, const double* yv1,
+                 cudaStream_t st);
+void solve_destroy(DevSolve& d);
+
+// Slice view of time instance nsp (1-based) of a solve; red/ist point into
+// the caller's status table.
+template <class R>
+Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist);
+
+// Device-side batch: slice array + prefix tables, rebuilt when membership
+// changes.
+template <class R>
+struct DevBatch {
+  Batch b;
+  Slice<R>* d_sl = nullptr;
+  int32_t* d_idx = nullptr;   // first / jfirst / kfirst, 3*(n+1)
+  NormPart* d_part = nullptr;
+  size_t cap_sl = 0, cap_part = 0;
+  int build(const std::vector<Slice<R>>& sl, cudaStream_t st);  // returns OT2D status
+  void release();
+};
+
+const char* cuda_err_name(cudaError_t e);
+
+}  // namespace ot2d

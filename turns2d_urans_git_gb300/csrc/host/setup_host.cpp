@@ -247,5 +247,16 @@ extern "C" int ot2d_mesh_naca4_cmesh(int32_t jmax, int32_t kmax, int32_t n_wake,
     int jj = jmax - 1 - j;
     xv[jj] = xv[j]; yv[jj] = yv[j];
   }
+  /* a symmetric section gets an exactly mirror-symmetric grid */
+  if (m <= 0.0 || p <= 0.0) {
+    const int mid = (jmax - 1) / 2;
+    for (int k = 0; k < kmax; ++k) {
+      for (int j = 0; j < mid; ++j) {
+        size_t o = (size_t)k * jmax + j, om = (size_t)k * jmax + (jmax - 1 - j);
+        xv[om] = xv[o]; yv[om] = -yv[o];
+      }
+      yv[(size_t)k * jmax + mid] = 0.0;
+    }
+  }
   return OT2D_OK;
 }

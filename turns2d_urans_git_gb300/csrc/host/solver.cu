@@ -1,0 +1,363 @@
+// solver.cu -- batched, continuously-admitting solver over device-resident
+// meshes (the ot2d_solver_* ABI).  The iteration is the reference's
+// Turns_overset.f:360-505 loop (time_step, step, monitor) applied to every
+// live request at once: one launch per kernel family per iteration, captured
+// in a CUDA graph that is rebuilt only when the set of live requests changes.
+// Convergence, blow-up and monitor flags are raised on the device; the host
+// reads the small status table every `check_every` iterations and retires
+// finished requests (forces in FP64, slot and memory freed).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "runtime.h"
+
+namespace ot2d {
+namespace {
+
+struct Rec {
+  DevSolve d;
+  int id = -1;
+  std::vector<int> slots;
+  double orders = 10.0;
+  int max_iters = 0;
+  bool live = false;
+  ot2d_result res{};
+  std::vector<double> qkeep;
+};
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+}  // namespace ot2d
+
+using namespace ot2d;
+
+struct ot2d_solver {
+  int device = 0, precision = OT2D_FP64;
+  cudaStream_t st = nullptr;
+  int cap = 0;
+  double* d_red = nullptr; int32_t* d_ist = nullptr;
+  double* h_red = nullptr; int32_t* h_ist = nullptr;
+  std::vector<int> free_slots;
+  std::map<int, Rec> recs;
+  std::vector<int> live;
+  DevBatch<double> b64;
+  DevBatch<float> b32;
+  bool dirty = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int next_id = 0;
+  double t0 = 0;
+  int check_every = 25;
+  int keep_q = 0;
+  int since_check = 0;
+  bool any_viscous = false, any_turb = false;
+  double* d_forces = nullptr; size_t forces_cap = 0;
+  DevBatch<double> f64;
+  DevBatch<float> f32;
+  const double** d_xy = nullptr; size_t xy_cap = 0;
+  int last_err = 0;
+};
+
+namespace {
+
+int grow_slots(ot2d_solver* s, int need) {
+  if ((int)s->free_slots.size() >= need) return OT2D_OK;
+  int ncap = std::max(2 * s->cap, s->cap + need + 64);
+  double* nr = nullptr; int32_t* ni = nullptr; double* hr = nullptr; int32_t* hi = nullptr;
+  if (cudaMalloc(&nr, sizeof(double) * RED_N * ncap) != cudaSuccess) return OT2D_ERR_NOMEM;
+  if (cudaMalloc(&ni, sizeof(int32_t) * IST_N * ncap) != cudaSuccess) { cudaFree(nr); return OT2D_ERR_NOMEM; }
+  cudaMallocHost(&hr, sizeof(double) * RED_N * ncap);
+  cudaMallocHost(&hi, sizeof(int32_t) * IST_N * ncap);
+  cudaMemsetAsync(nr, 0, sizeof(double) * RED_N * ncap, s->st);
+  cudaMemsetAsync(ni, 0, sizeof(int32_t) * IST_N * ncap, s->st);
+  if (s->cap) {
+    cudaMemcpyAsync(nr, s->d_red, sizeof(double) * RED_N * s->cap, cudaMemcpyDeviceToDevice, s->st);
+    cudaMemcpyAsync(ni, s->d_ist, sizeof(int32_t) * IST_N * s->cap, cudaMemcpyDeviceToDevice, s->st);
+  }
+  cudaStreamSynchronize(s->st);
+  if (s->d_red) cudaFree(s->d_red);
+  if (s->d_ist) cudaFree(s->d_ist);
+  if (s->h_red) cudaFreeHost(s->h_red);
+  if (s->h_ist) cudaFreeHost(s->h_ist);
+  s->d_red = nr; s->d_ist = ni; s->h_red = hr; s->h_ist = hi;
+  for (int i = ncap - 1; i >= s->cap; --i) s->free_slots.push_back(i);
+  s->cap = ncap;
+  s->dirty = true;  // slot pointers moved
+  return OT2D_OK;
+}
+
+template <class R>
+void slices_of(ot2d_solver* s, const Rec& r, std::vector<Slice<R>>& out) {
+  for (int nsp = 1; nsp <= r.d.nspec; ++nsp) {
+    int sl = r.slots[nsp - 1];
+    out.push_back(make_slice<R>(r.d, nsp, s->d_red + (size_t)RED_N * sl, s->d_ist + (size_t)IST_N * sl));
+  }
+}
+
+void drop_graph(ot2d_solver* s) {
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->gexec = nullptr; s->graph = nullptr;
+}
+
+template <class R>
+int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
+  drop_graph(s);
+  std::vector<Slice<R>> sl;
+  s->any_viscous = false; s->any_turb = false;
+  for (int id : s->live) {
+    const Rec& r = s->recs[id];
+    slices_of<R>(s, r, sl);
+    if (!r.d.P.invisc) s->any_viscous = true;
+    if (!r.d.P.lamin && r.d.P.iturb == 1) s->any_turb = true;
+  }
+  s->dirty = false;
+  if (sl.empty()) return OT2D_OK;
+  int e = B.build(sl, s->st);
+  if (e) return e;
+  // The kernels branch on each slice's own params, so inviscid, laminar and
+  // SA requests can share one batch.
+  if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
+  cudaError_t le = launch_iteration<R>(B.d_sl, B.b, s->any_viscous ? 1 : 0, s->any_turb ? 1 : 0, s->st);
+  cudaError_t ce = cudaStreamEndCapture(s->st, &s->graph);
+  if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
+  if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
+  return OT2D_OK;
+}
+
+int rebuild(ot2d_solver* s) {
+  return s->precision == OT2D_FP64 ? rebuild_t<double>(s, s->b64) : rebuild_t<float>(s, s->b32);
+}
+
+template <class R>
+int forces_t(ot2d_solver* s, const std::vector<int>& ids, DevBatch<R>& tmp) {
+  std::vector<Slice<R>> sl;
+  std::vector<const double*> xy;
+  for (int id : ids) {
+    const Rec& r = s->recs[id];
+    slices_of<R>(s, r, sl);
+  }
+  for (int id : ids) {
+    const Rec& r = s->recs[id];
+    for (int nsp = 0; nsp < r.d.nspec; ++nsp) xy.push_back(r.d.xv + (size_t)nsp * r.d.nvert);
+  }
+  for (int id : ids) {
+    const Rec& r = s->recs[id];
+    for (int nsp = 0; nsp < r.d.nspec; ++nsp) xy.push_back(r.d.yv + (size_t)nsp * r.d.nvert);
+  }
+  const size_t n = sl.size();
+  if (n == 0) return OT2D_OK;
+  int e = tmp.build(sl, s->st);
+  if (e) return e;
+  if (s->forces_cap < n) {
+    if (s->d_forces) cudaFree(s->d_forces);
+    if (s->d_xy) cudaFree(s->d_xy);
+    s->forces_cap = 2 * n;
+    cudaMalloc(&s->d_forces, sizeof(double) * 4 * s->forces_cap);
+    cudaMalloc(&s->d_xy, sizeof(double*) * 2 * s->forces_cap);
+  }
+  cudaMemcpyAsync(s->d_xy, xy.data(), sizeof(double*) * 2 * n, cudaMemcpyHostToDevice, s->st);
+  if (launch_forces<R>(tmp.d_sl, tmp.b, s->d_xy, s->d_xy + n, s->d_forces, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+  std::vector<double> f(4 * n);
+  cudaMemcpyAsync(f.data(), s->d_forces, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, s->st);
+  if (cudaStreamSynchronize(s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+  size_t i = 0;
+  const double pi = 4.0 * std::atan(1.0);
+  for (int id : ids) {
+    Rec& r = s->recs[id];
+    const ot2d_params& p = r.d.P;
+    const double ca = std::cos(pi * p.alfa / 180.0), sa = std::sin(pi * p.alfa / 180.0);
+    double cl = 0, cd = 0, cm = 0, cp = 0;
+    for (int nsp = 0; nsp < r.d.nspec; ++nsp, ++i) {
+      double cfx = f[4 * i], cfy = f[4 * i + 1], cm0 = f[4 * i + 2];
+      cl = cl + (-cfx * sa + cfy * ca);
+      cd = cd + (cfx * ca + cfy * sa);
+      cm = cm + (cm0 - 0.00 * cfx + 0.25 * cfy);
+      cp = cp + f[4 * i + 3];
+    }
+    r.res.cl = cl; r.res.cd = cd; r.res.cm = cm; r.res.cpower = cp;
+  }
+  return OT2D_OK;
+}
+
+int check(ot2d_solver* s) {
+  s->since_check = 0;
+  if (s->live.empty()) return OT2D_OK;
+  cudaMemcpyAsync(s->h_red, s->d_red, sizeof(double) * RED_N * s->cap, cudaMemcpyDeviceToHost, s->st);
+  cudaMemcpyAsync(s->h_ist, s->d_ist, sizeof(int32_t) * IST_N * s->cap, cudaMemcpyDeviceToHost, s->st);
+  if (cudaStreamSynchronize(s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+  std::vector<int> done;
+  for (int id : s->live) {
+    Rec& r = s->recs[id];
+    int status = 0, conv_it = 0, its = 0; bool conv = true;
+    for (int sl : r.slots) {
+      const int32_t* ist = s->h_ist + (size_t)IST_N * sl;
+      if (ist[2] & 1) status = OT2D_ERR_NORM;
+      else if ((ist[2] & 2) && !status) status = OT2D_ERR_MONITOR;
+      if (ist[3] == 0) conv = false;
+      conv_it = std::max(conv_it, (int)ist[3]);
+      its = ist[1];
+    }
+    const double* red = s->h_red + (size_t)RED_N * r.slots[0];
+    r.res.rsum_first = red[4];
+    r.res.rsum_last = red[5];
+    r.res.iterations = conv ? conv_it : its;
+    r.res.status = status;
+    r.res.converged = (conv && !status) ? 1 : 0;
+    if (status || conv || its >= r.max_iters) done.push_back(id);
+  }
+  if (done.empty()) return OT2D_OK;
+  int e = (s->precision == OT2D_FP64) ? forces_t<double>(s, done, s->f64) : forces_t<float>(s, done, s->f32);
+  const double t = now_s() - s->t0;
+  for (int id : done) {
+    Rec& r = s->recs[id];
+    r.res.t_done = t;
+    if (s->keep_q) {
+      r.qkeep.resize((size_t)r.d.n2 * r.d.nspec * r.d.P.nq);
+      cudaMemcpy(r.qkeep.data(), r.d.q64, r.qkeep.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    for (int sl : r.slots) s->free_slots.push_back(sl);
+    r.slots.clear();
+    solve_destroy(r.d);
+    r.live = false;
+  }
+  std::vector<int> nl;
+  for (int id : s->live) if (s->recs[id].live) nl.push_back(id);
+  s->live.swap(nl);
+  s->dirty = true;
+  return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+ot2d_solver* ot2d_solver_create(int32_t device, int32_t precision) {
+  if (precision != OT2D_FP64 && precision != OT2D_FP32_MIXED) return nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+  ot2d_solver* s = new ot2d_solver();
+  s->device = device; s->precision = precision;
+  if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) { delete s; return nullptr; }
+  s->t0 = now_s();
+  return s;
+}
+
+void ot2d_solver_destroy(ot2d_solver* s) {
+  if (!s) return;
+  cudaStreamSynchronize(s->st);
+  drop_graph(s);
+  for (auto& kv : s->recs) solve_destroy(kv.second.d);
+  s->b64.release(); s->b32.release(); s->f64.release(); s->f32.release();
+  if (s->d_red) cudaFree(s->d_red);
+  if (s->d_ist) cudaFree(s->d_ist);
+  if (s->h_red) cudaFreeHost(s->h_red);
+  if (s->h_ist) cudaFreeHost(s->h_ist);
+  if (s->d_forces) cudaFree(s->d_forces);
+  if (s->d_xy) cudaFree(s->d_xy);
+  cudaStreamDestroy(s->st);
+  delete s;
+}
+
+int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value) {
+  if (!s) return OT2D_ERR_ARG;
+  if (key == OT2D_OPT_CHECK_EVERY && value >= 1) { s->check_every = value; return OT2D_OK; }
+  if (key == OT2D_OPT_KEEP_Q) { s->keep_q = value ? 1 : 0; return OT2D_OK; }
+  return OT2D_ERR_ARG;
+}
+
+int ot2d_solver_add(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv, double orders,
+                    int32_t max_iters) {
+  if (!s || !p || !xv || !yv || max_iters < 1) return -OT2D_ERR_ARG;
+  cudaSetDevice(s->device);
+  if (grow_slots(s, p->nspec) != OT2D_OK) return -OT2D_ERR_NOMEM;
+  Rec r;
+  int e = solve_create(r.d, *p, s->precision, xv, yv, s->st);
+  if (e) return -e;
+  r.id = s->next_id++;
+  r.orders = orders; r.max_iters = max_iters; r.live = true;
+  r.res.id = r.id;
+  r.res.t_admit = now_s() - s->t0;
+  std::vector<double> red(RED_N, 0.0);
+  std::vector<int32_t> ist(IST_N, 0);
+  red[7] = orders > 0 ? std::pow(10.0, -orders) : -1.0;
+  ist[0] = p->istep0; ist[1] = 0;
+  for (int nsp = 0; nsp < p->nspec; ++nsp) {
+    int sl = s->free_slots.back(); s->free_slots.pop_back();
+    r.slots.push_back(sl);
+    cudaMemcpyAsync(s->d_red + (size_t)RED_N * sl, red.data(), sizeof(double) * RED_N, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->d_ist + (size_t)IST_N * sl, ist.data(), sizeof(int32_t) * IST_N, cudaMemcpyHostToDevice, s->st);
+  }
+  cudaStreamSynchronize(s->st);
+  const int id = r.id;
+  s->recs[id] = std::move(r);
+  s->live.push_back(id);
+  s->dirty = true;
+  return id;
+}
+
+int ot2d_solver_iterate(ot2d_solver* s, int32_t iters) {
+  if (!s || iters < 0) return OT2D_ERR_ARG;
+  cudaSetDevice(s->device);
+  int done = 0;
+  while (done < iters) {
+    if (s->dirty) { int e = rebuild(s); if (e) return e; }
+    if (s->live.empty()) break;
+    int chunk = std::min(s->check_every - s->since_check, iters - done);
+    for (int i = 0; i < chunk; ++i)
+      if (cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+    s->since_check += chunk;
+    done += chunk;
+    if (s->since_check >= s->check_every) { int e = check(s); if (e) return e; }
+  }
+  return OT2D_OK;
+}
+
+int ot2d_solver_sync(ot2d_solver* s) {
+  if (!s) return OT2D_ERR_ARG;
+  return check(s);
+}
+
+int ot2d_solver_live(const ot2d_solver* s) { return s ? (int)s->live.size() : 0; }
+
+int ot2d_solver_result(ot2d_solver* s, int32_t id, ot2d_result* out) {
+  if (!s || !out) return OT2D_ERR_ARG;
+  auto it = s->recs.find(id);
+  if (it == s->recs.end()) return OT2D_ERR_ARG;
+  *out = it->second.res;
+  return OT2D_OK;
+}
+
+int ot2d_solver_get_q(ot2d_solver* s, int32_t id, double* q_out) {
+  if (!s || !q_out) return OT2D_ERR_ARG;
+  auto it = s->recs.find(id);
+  if (it == s->recs.end()) return OT2D_ERR_ARG;
+  Rec& r = it->second;
+  if (r.live) {
+    size_t n = r.d.n2 * r.d.nspec * r.d.P.nq;
+    if (cudaMemcpyAsync(q_out, r.d.q64, n * sizeof(double), cudaMemcpyDeviceToHost, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+    return cudaStreamSynchronize(s->st) == cudaSuccess ? OT2D_OK : OT2D_ERR_CUDA;
+  }
+  if (r.qkeep.empty()) return OT2D_ERR_ARG;
+  std::memcpy(q_out, r.qkeep.data(), r.qkeep.size() * sizeof(double));
+  return OT2D_OK;
+}
+
+size_t ot2d_solver_device_bytes(const ot2d_solver* s) {
+  if (!s) return 0;
+  size_t b = 0;
+  for (auto& kv : s->recs) if (kv.second.live) b += kv.second.d.bytes;
+  return b;
+}
+
+size_t ot2d_instance_bytes(const ot2d_params* p, int32_t precision) { return p ? solve_bytes(*p, precision) : 0; }
+
+void* ot2d_solver_stream(ot2d_solver* s) { return s ? (void*)s->st : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,82 @@
+// dev_common.cuh -- shared device-side definitions for the sm_103a kernels.
+//
+// Layout in HBM is the reference's: column-major q(jd,kd,nspec,nq) with j
+// fastest, 1-based Fortran indices in all index arithmetic below
+// (src/modules.f, src/step.f:17-30).  One "slice" is one time instance of one
+// solve; a launch covers a ragged batch of slices of different sizes.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "ot2d_params.h"
+
+namespace ot2d {
+
+// Device view of one time instance of one solve.  R is the arithmetic type
+// of the residual / Jacobian / sweeps (double for the plain path, float for
+// the mixed path); the conservative state is always kept in FP64 (q64).
+template <class R>
+struct Slice {
+  const ot2d_params* P;  // device copy of the instance's params_global
+  int32_t jd, kd, nsp, nspec;
+  int64_t qs;            // distance between variables of q and s (jd*kd*nspec)
+  R* q;                  // compute copy of q (== q64 for R = double)
+  double* q64;           // FP64 master state
+  R* s;                  // residual / correction (nv variables)
+  const R *xx, *xy, *yx, *yy;        // J-scaled cell metrics (setup.f:523-531)
+  const R *fxa, *fya, *gxa, *gya;    // face normals from the vertex grid (eulerrhs.f:109-115, :218-222)
+  const R *ftj, *gtj;                // face grid speeds (time-spectral), null if steady
+  const R *ug, *vg;                  // cell grid velocities, null if steady
+  R *tscale, *bt, *turmu;
+  const int32_t* iblank;
+  const R* sn;                       // SA wall distance (static geometry)
+  R* w;                              // scratch of this slice (phase dependent)
+  int64_t wstride;                   // distance between scratch arrays (>= jd*kd)
+  double* red;                       // per-slice reduction output
+  int32_t* ist;                      // per-slice counters: istep0, istep, status bits
+  const double* Ds;                  // time-spectral operator Ds(nspec,nspec)
+  // FP64 geometry kept for FP64-only work (forces, BC metrics in mixed mode)
+  const double *xx64, *xy64, *yx64, *yy64, *ug64, *vg64;
+};
+
+// Fortran SIGN(a,b): |a| with the IEEE sign of b (gfortran semantics).
+template <class R> __device__ __forceinline__ R fsign(R a, R b) { return copysign(fabs(a), b); }
+// MAX / MIN as the oracle evaluates them (first argument on ties).
+template <class R> __device__ __forceinline__ R fmax2(R a, R b) { return (b > a) ? b : a; }
+template <class R> __device__ __forceinline__ R fmin2(R a, R b) { return (b < a) ? b : a; }
+template <class R> __device__ __forceinline__ R sq(R x) { return x * x; }
+template <class R> __device__ __forceinline__ R cube(R x) { return (x * x) * x; }
+template <class R> __device__ __forceinline__ R pow6(R x) { R t = (x * x) * x; return t * t; }
+__device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
+
+// 1-based (j,k) -> linear offset inside one slice
+__device__ __forceinline__ int64_t at(int jd, int j, int k) { return (int64_t)(k - 1) * jd + (j - 1); }
+
+// Batched launch: slices are mapped onto a 1-D grid through a prefix table
+// (first block of each slice).  Returns the slice index of this block.
+__device__ __forceinline__ int find_slice(const int32_t* __restrict__ first, int nslice, int b) {
+  int lo = 0, hi = nslice - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(first + mid) <= b) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// bc.f:20-33: convert one &bcinp entry to halo-cell indices
+__device__ __forceinline__ void bc_range(const ot2d_params& p, int ib, int& js, int& je, int& ks, int& ke) {
+  js = p.jbcs[ib]; je = p.jbce[ib]; ks = p.kbcs[ib]; ke = p.kbce[ib];
+  if (js < 0) js = p.jmax + js + 1;
+  if (ks < 0) ks = p.kmax + ks + 1;
+  if (je < 0) je = p.jmax + je + 1;
+  if (ke < 0) ke = p.kmax + ke + 1;
+  if (js > 1) js = js + p.nhalo;
+  if (ks > 1) ks = ks + p.nhalo;
+  if (je < p.jmax) je = je + p.nhalo - 1;
+  if (ke < p.kmax) ke = ke + p.nhalo - 1;
+  if (je == p.jmax) je = p.jd;
+  if (ke == p.kmax) ke = p.kd;
+}
+
+__device__ __forceinline__ int isign1(int idir) { return idir >= 0 ? 1 : -1; }
+
+}  // namespace ot2d

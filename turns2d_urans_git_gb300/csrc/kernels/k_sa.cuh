@@ -1,0 +1,270 @@
+// k_sa.cuh -- Spalart-Allmaras solve vmu_sa (src/samodel2d.f:2-1385,
+// constants src/sadata.h:2-4).  The reference scatters Jacobian-band
+// contributions from each cell into its neighbours; here every interior cell
+// gathers its own band entries from the neighbours' values, adding them in
+// the reference's order, so each band entry carries the same bits.
+#pragma once
+#include "dev_common.cuh"
+
+namespace ot2d {
+
+// sadata.h:2-4 (decimal literals are doubles under -r8)
+struct SAc {
+  static constexpr double cb1 = 0.1355, sigma = 0.6666667, cb2 = 0.622, akt = 0.41, cw1 = 3.2390678;
+  static constexpr double cw2 = 0.3, cw3 = 2., cv1 = 7.1, ct3 = 1.2, ct4 = 0.5;
+};
+
+// scratch arrays of one slice (stride S.wstride)
+enum SAw { W_VMUL = 0, W_U, W_V, W_SJ, W_AJ, W_CJ, W_AK, W_CK, W_BJ, W_NSA };
+
+// lamvis (samodel2d.f:200-240) and the u,v of samodel2d.f:74-76, all cells
+template <class R>
+__device__ __forceinline__ void sa_prep_cell(const Slice<R>& S, const ot2d_params& p, int j, int k) {
+  const int64_t o = at(S.jd, j, k), qs = S.qs, ws = S.wstride;
+  const R c2b = (R)(198.6 / p.tinf), c2bp = c2b + (R)1.;
+  R q1 = S.q[o], q2 = S.q[qs + o], q3 = S.q[2 * qs + o], q4 = S.q[3 * qs + o];
+  R ra = (R)1. / q1;
+  R uvel = q2 * ra, vvel = q3 * ra;
+  R ei = q4 * ra - (R)0.5 * (sq(uvel) + sq(vvel));
+  R tt = (R)p.ggm1 * ei;
+  S.w[W_VMUL * ws + o] = c2bp * tt * sqrt(tt) / (c2b + tt);
+  S.w[W_U * ws + o] = q2 / q1;
+  S.w[W_V * ws + o] = q3 / q1;
+}
+
+template <class R>
+struct SAnb {  // convec upwind split at one cell (samodel2d.f:477-484)
+  R up, um, vp, vm;
+};
+template <class R>
+__device__ __forceinline__ SAnb<R> sa_split(const Slice<R>& S, int j, int k) {
+  const int64_t o = at(S.jd, j, k), ws = S.wstride;
+  R u = S.w[W_U * ws + o], v = S.w[W_V * ws + o];
+  R ugc = S.ug ? S.ug[o] : (R)0, vgc = S.vg ? S.vg[o] : (R)0;
+  R uu = S.xx[o] * (u - ugc) + S.xy[o] * (v - vgc);
+  R vv = S.yx[o] * (u - ugc) + S.yy[o] * (v - vgc);
+  SAnb<R> r;
+  r.up = (R)0.5 * (uu + fabs(uu)); r.um = (R)0.5 * (uu - fabs(uu));
+  r.vp = (R)0.5 * (vv + fabs(vv)); r.vm = (R)0.5 * (vv - fabs(vv));
+  return r;
+}
+
+// RHS and bands of one interior cell: rhslhs (samodel2d.f:402-450) with
+// convec (:453-542), diffus (:545-688), source (:691-824), then the time
+// scaling of vmu_sa (:96-134).  Writes sjmat, aj, cj, ak, ck, bjmat.
+template <class R>
+__device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int k, bool bodyflag) {
+  const int jd = S.jd; const int64_t qs = S.qs, ws = S.wstride;
+  const int n5 = p.nmv + 1, nq = p.nq;
+  const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
+  auto Q = [&](int jj, int kk, int n) { return S.q[(int64_t)(n - 1) * qs + at(jd, jj, kk)]; };
+  auto W = [&](int a, int jj, int kk) { return S.w[a * ws + at(jd, jj, kk)]; };
+  auto Mx = [&](const R* a, int jj, int kk) { return a[at(jd, jj, kk)]; };
+  const int64_t o = at(jd, j, k);
+  const R rey = (R)p.rey;
+  // ---- convec
+  SAnb<R> c0 = sa_split(S, j, k), cjm = sa_split(S, j - 1, k), cjp = sa_split(S, j + 1, k);
+  SAnb<R> ckm = sa_split(S, j, k - 1), ckp = sa_split(S, j, k + 1);
+  R q5 = Q(j, k, n5);
+  R sj = S.s[(int64_t)(n5 - 1) * qs + o];
+  sj = sj - c0.up * (q5 - Q(j - 1, k, n5)) - c0.um * (Q(j + 1, k, n5) - q5);
+  sj = sj - c0.vp * (q5 - Q(j, k - 1, n5)) - c0.vm * (Q(j, k + 1, n5) - q5);
+  R aj = (R)0., cj = (R)0., ak = (R)0., ck = (R)0.;
+  if (j >= js + 1) aj = aj - ((c0.up > (R)1.0e-12) ? (R)1.0 : (R)0.0) * (cjm.up + cjm.um);
+  if (j <= je - 1) cj = cj + ((c0.um < (R)-1.0e-12) ? (R)1.0 : (R)0.0) * (cjp.up + cjp.um);
+  R bj = (R)0. + c0.up - c0.um;
+  if (k >= ks + 1) ak = ak - ((c0.vp > (R)1.0e-12) ? (R)1.0 : (R)0.0) * (ckm.vp + ckm.vm);
+  if (k <= ke - 1) ck = ck + ((c0.vm < (R)-1.0e-12) ? (R)1.0 : (R)0.0) * (ckp.vp + ckp.vm);
+  R bk = (R)0. + c0.vp - c0.vm;
+  // ---- diffus
+  const R chpc = (R)((1. + SAc::cb2) / SAc::sigma) / rey;
+  const R c2c = (R)(SAc::cb2 / SAc::sigma) / rey;
+  auto nul = [&](int jj, int kk) { return W(W_VMUL, jj, kk) / Q(jj, kk, 1) / Q(jj, kk, nq); };
+  {
+    // half points j-1/2 (index j-1) and j+1/2 (index j)
+    R dmxh_m = (R)0.5 * (Mx(S.xx, j - 1, k) + Mx(S.xx, j, k)), dmyh_m = (R)0.5 * (Mx(S.xy, j - 1, k) + Mx(S.xy, j, k));
+    R dmxh_p = (R)0.5 * (Mx(S.xx, j, k) + Mx(S.xx, j + 1, k)), dmyh_p = (R)0.5 * (Mx(S.xy, j, k) + Mx(S.xy, j + 1, k));
+    R n0 = nul(j, k), nm = nul(j - 1, k), np = nul(j + 1, k);
+    R chp_m = chpc * ((R)0.5 * (nm + n0) + (R)0.5 * (Q(j - 1, k, n5) + q5));
+    R chp_p = chpc * ((R)0.5 * (n0 + np) + (R)0.5 * (q5 + Q(j + 1, k, n5)));
+    R dn_m = q5 - Q(j - 1, k, n5), dn_p = Q(j + 1, k, n5) - q5;
+    R dxp = dmxh_p * Mx(S.xx, j, k) + dmyh_p * Mx(S.xy, j, k);
+    R dxm = dmxh_m * Mx(S.xx, j, k) + dmyh_m * Mx(S.xy, j, k);
+    R c2 = c2c * (n0 + q5);
+    R dcp = dxp * (chp_p - c2), dcm = dxm * (chp_m - c2);
+    R ax = fmax2(dcm, (R)0.0), cx = fmax2(dcp, (R)0.0);
+    sj = sj - ax * dn_m + cx * dn_p;
+    aj = aj - ax; cj = cj - cx; bj = bj + ax + cx;
+  }
+  {
+    R dmxh_m = (R)0.5 * (Mx(S.yx, j, k - 1) + Mx(S.yx, j, k)), dmyh_m = (R)0.5 * (Mx(S.yy, j, k - 1) + Mx(S.yy, j, k));
+    R dmxh_p = (R)0.5 * (Mx(S.yx, j, k) + Mx(S.yx, j, k + 1)), dmyh_p = (R)0.5 * (Mx(S.yy, j, k) + Mx(S.yy, j, k + 1));
+    R n0 = nul(j, k), nm = nul(j, k - 1), np = nul(j, k + 1);
+    R chp_m = chpc * ((R)0.5 * (nm + n0) + (R)0.5 * (Q(j, k - 1, n5) + q5));
+    R chp_p = chpc * ((R)0.5 * (n0 + np) + (R)0.5 * (q5 + Q(j, k + 1, n5)));
+    R dn_m = q5 - Q(j, k - 1, n5), dn_p = Q(j, k + 1, n5) - q5;
+    R dyp = dmxh_p * Mx(S.yx, j, k) + dmyh_p * Mx(S.yy, j, k);
+    R dym = dmxh_m * Mx(S.yx, j, k) + dmyh_m * Mx(S.yy, j, k);
+    R c2 = c2c * (n0 + q5);
+    R dcp = dyp * (chp_p - c2), dcm = dym * (chp_m - c2);
+    R ay = fmax2(dcm, (R)0.0), cy = fmax2(dcp, (R)0.0);
+    sj = sj - ay * dn_m + cy * dn_p;
+    ak = ak - ay; ck = ck - cy; bk = bk + ay + cy;
+  }
+  // ---- source (isour = 0, fturf = 0, no transition)
+  {
+    const R cb1 = (R)SAc::cb1, akt = (R)SAc::akt, cw1 = (R)SAc::cw1, cw2 = (R)SAc::cw2, cw3 = (R)SAc::cw3;
+    const R cv1 = (R)SAc::cv1, ct3 = (R)SAc::ct3, ct4 = (R)SAc::ct4;
+    const R d2min = (R)1.e-12, rmax = (R)10.0, stilim = (R)1.e-12, fturf = (R)0.0;
+    R vort = (R)0.0, d = (R)1.e10;
+    if (bodyflag) {
+      const R dx2 = (R)0.5, dy2 = (R)0.5;
+      R ux = (W(W_U, j + 1, k) - W(W_U, j - 1, k)) * dx2, vx = (W(W_V, j + 1, k) - W(W_V, j - 1, k)) * dx2;
+      R uy = (W(W_U, j, k + 1) - W(W_U, j, k - 1)) * dy2, vy = (W(W_V, j, k + 1) - W(W_V, j, k - 1)) * dy2;
+      R tx = Mx(S.xy, j, k) * ux - Mx(S.xx, j, k) * vx + Mx(S.yy, j, k) * uy - Mx(S.yx, j, k) * vy;
+      vort = fabs(tx);
+      d = S.sn[o];
+    }
+    R vnul = W(W_VMUL, j, k) / Q(j, k, 1) / Q(j, k, nq);
+    R chi = q5 / vnul;
+    chi = fmax2(chi, (R)1.e-12);
+    R fv1 = (cube(chi)) / (cube(chi) + cube(cv1));
+    R fv2 = (R)1. - chi / ((R)1. + chi * fv1);
+    R fv3 = (R)1.0;
+    R ft2 = fturf * ct3 * exp((R)-1. * ct4 * chi * chi);
+    R dchi = (R)1. / vnul;
+    R dfv1 = ((R)3. * cube(cv1)) * (sq(chi)) * dchi * sq((R)1. / (cube(chi) + cube(cv1)));
+    R dfv2 = (fv2 - (R)1.) / chi / vnul + ((R)1. - fv2) * ((R)1 - fv2) * (dfv1 + fv1 / chi / vnul);
+    R dfv3 = (R)0.0;
+    R dft2 = ((R)-2. * ct4) * chi * dchi * ft2;
+    R d2 = fmax2(sq(d), d2min);
+    R stilda = vort * fv3 + vnul / (d2 * akt * akt * rey) * chi * fv2;
+    stilda = fmax2(stilda, stilim);
+    R r = q5 / (d2 * akt * akt * rey) / stilda;
+    r = fmin2(r, rmax);
+    R g = r + cw2 * (pow6(r) - r);
+    R fw = ((R)1. + pow6(cw3)) / (pow6(g) + pow6(cw3));
+    fw = g * (pow(fw, (R)(1. / 6.)));
+    R dstild = vort * dfv3 + vnul * (dchi * fv2 + chi * dfv2) / (d2 * akt * akt * rey);
+    R dr = vnul * (dchi - chi * dstild / stilda) / stilda / (d2 * akt * akt * rey);
+    R dg = dr * ((R)1. + cw2 * ((R)6. * pow(r, (R)5.) - (R)1.));
+    R dfw = pow(((R)1. + pow6(cw3)) / (pow6(g) + pow6(cw3)), (R)(1. / 6.));
+    dfw = dfw * dg * ((R)1. - pow6(g) / (pow6(g) + pow6(cw3)));
+    R pro = cb1 * stilda * ((R)1. - ft2);
+    R des = (cw1 * fw - cb1 / (akt * akt) * ft2) / d2 / rey;
+    R prod = cb1 * stilda * ((R)1. - ft2) * q5;
+    R dest = (cw1 * fw - cb1 / (akt * akt) * ft2) * q5 * q5 / d2 / rey;
+    R dpro = pro * dstild / stilda - cb1 * stilda * dft2;
+    R ddes = (cw1 * dfw - cb1 / (akt * akt) * dft2) / d2 / rey * vnul * chi;
+    ddes = ddes + des;
+    ddes = ddes * q5;
+    dpro = dpro * q5;
+    sj = sj + prod - dest;
+    R tk1 = fmax2(des * q5 - pro, (R)0.0);
+    R tk2 = fmax2(ddes - dpro, (R)0.0);
+    bk = bk + tk1 + tk2;
+  }
+  // ---- time scaling (vmu_sa, samodel2d.f:104-134)
+  R tscal = S.tscale[o];
+  int ibi = S.iblank[o];
+  if (p.cfltur > 1 && p.idual_turb == 1) {
+    R dtp = (R)p.cfltur / (bj + bk);
+    tscal = dtp * (R)ibi;
+    tscal = tscal / ((R)1. + tscal / (R)p.h);
+  }
+  if (p.timeac == 1) {
+    R ib = (R)(ibi > 0 ? ibi : 0);
+    R J = Q(j, k, nq);
+    tscal = ib * ((R)1.0 + (R)0.002 * sqrt(J)) / ((R)1. + sqrt(J));
+    tscal = tscal * (R)1.0;
+    tscal = tscal / ((R)1. + tscal / (R)p.h);
+  }
+  S.w[W_SJ * ws + o] = sj * tscal;
+  S.w[W_AJ * ws + o] = aj * tscal;
+  S.w[W_CJ * ws + o] = cj * tscal;
+  S.w[W_AK * ws + o] = ak * tscal;
+  S.w[W_CK * ws + o] = ck * tscal;
+  S.w[W_BJ * ws + o] = (R)1. + (bj + bk) * tscal;
+}
+
+// lsolvej (samodel2d.f:1306-1344) on one k-line, then s1 = x,
+// sjmat = (s1 - s2)*bjmat with s2 = 0 (samodel2d.f:150-153)
+template <class R>
+__device__ void sa_lsolvej_line(const Slice<R>& S, const ot2d_params& p, int k) {
+  const int jd = S.jd; const int64_t ws = S.wstride;
+  R* a = S.w + W_AJ * ws; R* c = S.w + W_CJ * ws; R* s = S.w + W_SJ * ws; const R* b = S.w + W_BJ * ws;
+  const int js = p.jbeg, je = p.jend;
+  int64_t o = at(jd, js, k);
+  R bb = (R)1. / b[o];
+  R sp = s[o] * bb, cp = c[o] * bb;
+  s[o] = sp; c[o] = cp;
+  for (int j = js + 1; j <= je; ++j) {
+    o = at(jd, j, k);
+    bb = (R)1. / (b[o] - a[o] * cp);
+    sp = (s[o] - a[o] * sp) * bb;
+    cp = c[o] * bb;
+    s[o] = sp; c[o] = cp;
+  }
+  R snext = sp;
+  s[o] = ((snext + (R)0.) - (R)0.) * b[o];
+  for (int j = je - 1; j >= js; --j) {
+    o = at(jd, j, k);
+    R x = s[o] - c[o] * snext;
+    snext = x;
+    s[o] = ((x + (R)0.) - (R)0.) * b[o];
+  }
+}
+
+// lsolvek (samodel2d.f:1347-1385) on one j-line, then s2 = x and the
+// update q5 = max(q5 + x*max(iblank,0), 1e-20) (samodel2d.f:184-188) in FP64
+template <class R>
+__device__ void sa_lsolvek_line(const Slice<R>& S, const ot2d_params& p, int j) {
+  const int jd = S.jd; const int64_t ws = S.wstride, qs = S.qs;
+  R* a = S.w + W_AK * ws; R* c = S.w + W_CK * ws; R* s = S.w + W_SJ * ws; const R* b = S.w + W_BJ * ws;
+  const int ks = p.kbeg, ke = p.kend, n5 = p.nmv + 1;
+  int64_t o = at(jd, j, ks);
+  R bb = (R)1. / b[o];
+  R sp = s[o] * bb, cp = c[o] * bb;
+  s[o] = sp; c[o] = cp;
+  for (int k = ks + 1; k <= ke; ++k) {
+    o = at(jd, j, k);
+    bb = (R)1. / (b[o] - a[o] * cp);
+    sp = (s[o] - a[o] * sp) * bb;
+    cp = c[o] * bb;
+    s[o] = sp; c[o] = cp;
+  }
+  auto upd = [&](int64_t oo, R x) {
+    R x2 = (R)0. + x;            // s2 = s2 + sjmat, s2 = 0 on entry
+    R relx = (R)1.0 * x2;        // relfac * sjmat
+    s[oo] = relx;
+    int ibi = S.iblank[oo];
+    double ib = (double)(ibi > 0 ? ibi : 0);
+    double v = S.q64[(int64_t)(n5 - 1) * qs + oo] + (double)relx * ib;
+    v = (1.0e-20 > v) ? 1.0e-20 : v;
+    S.q64[(int64_t)(n5 - 1) * qs + oo] = v;
+    if constexpr (sizeof(R) != sizeof(double)) S.q[(int64_t)(n5 - 1) * qs + oo] = (R)v;
+  };
+  R snext = sp;
+  upd(o, snext);
+  for (int k = ke - 1; k >= ks; --k) {
+    o = at(jd, j, k);
+    R x = s[o] - c[o] * snext;
+    snext = x;
+    upd(o, x);
+  }
+}
+
+// c_turm, samodel2d.f:372-399 (all cells)
+template <class R>
+__device__ __forceinline__ void sa_turm_cell(const Slice<R>& S, const ot2d_params& p, int j, int k) {
+  const int64_t o = at(S.jd, j, k), qs = S.qs, ws = S.wstride;
+  const R cv1 = (R)SAc::cv1;
+  R rhoJ = S.q[o] * S.q[(p.nq - 1) * qs + o];
+  R vnul = S.w[W_VMUL * ws + o] / rhoJ;
+  R q5 = S.q[(int64_t)p.nmv * qs + o];
+  R chi = q5 / vnul;
+  R fv1 = cube(chi) / (cube(chi) + cube(cv1));
+  S.turmu[o] = rhoJ * q5 * fv1;
+}
+
+}  // namespace ot2d

@@ -1,0 +1,376 @@
+// kernels.cuh -- __global__ entry points over a ragged batch of slices.
+// Included by one translation unit per arithmetic type (kernels_fp64.cu,
+// kernels_fp32.cu) which instantiates the launchers.
+#pragma once
+#include "dev_common.cuh"
+#include "k_bc.cuh"
+#include "k_rhs.cuh"
+#include "k_lusgs.cuh"
+#include "k_sa.cuh"
+#include "k_misc.cuh"
+#include "launch.h"
+
+namespace ot2d {
+
+// Cell-parallel mapping: slice i owns blocks [first[i], first[i+1]) of
+// CELL_BS threads each, covering its jd*kd cells.
+#define OT2D_CELL_MAP()                                                      \
+  const int si = find_slice(first, nslice, blockIdx.x);                      \
+  const Slice<R>& S = sl[si];                                                \
+  const int cid = (blockIdx.x - first[si]) * blockDim.x + threadIdx.x;       \
+  const int j = cid % S.jd + 1, k = cid / S.jd + 1;                          \
+  const bool inside = cid < S.jd * S.kd;
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_time_step(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                       int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  const ot2d_params& p = *S.P;
+  int istep = S.ist ? S.ist[1] + 1 : p.istep;
+  R oat = (R)1.0;
+  if (p.ntac >= 2 && istep > 1) oat = (R)(2. / 3.);
+  if (p.ntac == 3 && istep > 2) oat = (R)(6. / 11.);
+  time_step_cell(S, j, k, oat);
+}
+
+template <class R>
+__global__ void k_bc(const Slice<R>* __restrict__ sl, int advance) {
+  const Slice<R>& S = sl[blockIdx.x];
+  if (S.ist && advance) {
+    __syncthreads();
+    if (threadIdx.x == 0) { S.ist[0] += 1; S.ist[1] += 1; }
+    __syncthreads();
+  }
+  const int istep0 = S.ist ? S.ist[0] : S.P->istep0;
+  bc_slice(S, nullptr, istep0);
+  shadow_ring(S, 1, 4);
+}
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_faces(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                   int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  const ot2d_params& p = *S.P;
+  R* F = S.w + 0 * S.wstride;
+  R* G = S.w + 4 * S.wstride;
+  if (k >= p.kbeg && k <= p.kend && j >= p.jbeg - 1 && j <= p.jend) xi_face(S, j, k, F);
+  if (j >= p.jbeg && j <= p.jend && k >= p.kbeg - 1 && k <= p.kend) eta_face(S, j, k, G);
+}
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_visc(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                  int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  const ot2d_params& p = *S.P;
+  if (p.invisc) return;
+  if (j >= p.jbeg && j <= p.jend && k <= S.kd - 1) visc_eta_face(S, j, k, S.w + 8 * S.wstride);
+  if (k >= p.kbeg && k <= p.kend && j <= S.jd - 1) visc_xi_face(S, j, k, S.w + 14 * S.wstride);
+}
+
+// Residual assembly.  flags: AS_ACC start from the incoming s and leave
+// halo cells alone (the drop-in rhsup / visrhs / timespectralrhs, which add
+// into s); otherwise start from 0 on every cell (step.f:41).  AS_INV adds the
+// inviscid face fluxes, AS_VISC the viscous ones (slices with invisc skip
+// them), AS_TS the time-spectral term, AS_NORM the per-block norm partials.
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_assemble(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                      int nslice, int flags, NormPart* __restrict__ part) {
+  OT2D_CELL_MAP();
+  __shared__ NormPart sh[CELL_BS];
+  NormPart np{0.0, 0.0, 0.0, 0x7fffffffffffffffLL};
+  if (inside) {
+    const ot2d_params& p = *S.P;
+    const int64_t o = at(S.jd, j, k);
+    const int nv = p.nv;
+    const bool acc = flags & AS_ACC;
+    R s[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) s[n] = (R)0.0;
+    const bool interior = j >= p.jbeg && j <= p.jend && k >= p.kbeg && k <= p.kend;
+    if (interior) {
+      if (acc)
+        for (int n = 1; n <= nv; ++n) s[n - 1] = S.s[(int64_t)(n - 1) * S.qs + o];
+      const bool visc = (flags & AS_VISC) && !p.invisc;
+      const R* F = (flags & AS_INV) ? S.w + 0 * S.wstride : nullptr;
+      const R* G = (flags & AS_INV) ? S.w + 4 * S.wstride : nullptr;
+      const R* VE = visc ? S.w + 8 * S.wstride : nullptr;
+      const R* VX = visc ? S.w + 14 * S.wstride : nullptr;
+      assemble_cell(S, j, k, F, G, VE, VX, s);
+      if ((flags & AS_TS) && p.timespectral && S.Ds) ts_cell(S, p, S.Ds, j, k, s, nv);
+      if (flags & AS_NORM) {
+        // norms (step.f:67-88)
+        int ibi = S.iblank[o];
+        double m = (double)(ibi > 0 ? ibi : 0);
+        for (int n = 1; n <= p.nmv; ++n) {
+          double smrs = fabs((double)s[n - 1]) * m;
+          long long key = ((long long)(k - 1) * (p.nmv + 1) + n) * (long long)S.jd + (j - 1);
+          if (smrs > np.resmax || (smrs == np.resmax && key < np.key)) { np.resmax = smrs; np.key = key; }
+        }
+        double s1 = (double)s[0] * m, s2 = (double)s[1] * m, s3 = (double)s[2] * m, s4 = (double)s[3] * m;
+        np.resrho = (double)s[0] * (double)s[0];
+        np.rsum = s1 * s1 + s2 * s2 + s3 * s3 + s4 * s4;
+      }
+    }
+    if (interior || !acc)
+      for (int n = 1; n <= nv; ++n) S.s[(int64_t)(n - 1) * S.qs + o] = s[n - 1];
+  }
+  if (!(flags & AS_NORM)) return;
+  // deterministic block reduction
+  sh[threadIdx.x] = np;
+  __syncthreads();
+  for (int st = CELL_BS / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sh[threadIdx.x] = norm_combine(sh[threadIdx.x], sh[threadIdx.x + st]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// Per-slice norms from the block partials (fixed order): red[0..3] =
+// rsum, resrho, resmax, key; status word on blow-up (step.f:105-110).
+template <class R>
+__global__ void k_norm_final(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first, int nslice,
+                             const NormPart* __restrict__ part) {
+  const int si = blockIdx.x;
+  const Slice<R>& S = sl[si];
+  if (threadIdx.x != 0) return;
+  NormPart acc{0.0, 0.0, 0.0, 0x7fffffffffffffffLL};
+  for (int b = first[si]; b < first[si + 1]; ++b) acc = norm_combine(acc, part[b]);
+  double volum = (double)(S.jd * S.kd);
+  double rsum = sqrt(acc.rsum / volum), resrho = sqrt(acc.resrho / volum);
+  S.red[0] = rsum; S.red[1] = resrho; S.red[2] = acc.resmax; S.red[3] = (double)acc.key;
+  if (S.ist) {
+    const int it = S.ist[1];
+    if (!(rsum <= 1000.0)) S.ist[2] |= 1;         // L2 norm out of bounds (step.f:105-110)
+    if (it == 1) S.red[4] = rsum;                 // first-iteration norm
+    S.red[5] = rsum;
+    if (rsum > S.red[6]) S.red[6] = rsum;         // running peak
+    if (S.ist[3] == 0 && it > 1 && rsum <= S.red[6] * S.red[7]) S.ist[3] = it;  // converged at `it`
+  }
+}
+
+template <class R>
+__global__ void k_rbc(const Slice<R>* __restrict__ sl) {
+  const Slice<R>& S = sl[blockIdx.x];
+  rbc_slice(S);
+}
+
+// s *= tscale on all cells (step.f:141-148), then ilu2d (lhs.f:470-814)
+template <class R>
+__global__ void k_lusgs(const Slice<R>* __restrict__ sl, int scale) {
+  __shared__ R xbuf[64][4];
+  const Slice<R>& S = sl[blockIdx.x];
+  const ot2d_params& p = *S.P;
+  const int64_t n2 = (int64_t)S.jd * S.kd;
+  for (int64_t i = threadIdx.x; scale && i < n2; i += blockDim.x) {
+    R t = S.tscale[i];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) S.s[n * S.qs + i] = S.s[n * S.qs + i] * t;
+  }
+  __syncthreads();
+  const R eps2 = (R)(p.epse * 2.), epsv = (R)1. + eps2;
+  lu_halo_scale(S, p, epsv);
+  __syncthreads();
+  lu_sweep<R, true>(S, xbuf);
+  __syncthreads();
+  lu_sweep<R, false>(S, xbuf);
+  __syncthreads();
+  lu_roundtrip(S, p);
+}
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_sa_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                     int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  if (S.P->lamin || S.P->iturb != 1) return;
+  sa_prep_cell(S, *S.P, j, k);
+}
+
+template <class R>
+__global__ void k_turbc(const Slice<R>* __restrict__ sl, int final_pass) {
+  const Slice<R>& S = sl[blockIdx.x];
+  const ot2d_params& p = *S.P;
+  if (p.lamin || p.iturb != 1) return;
+  turbc_slice(S, S.w + W_U * S.wstride, S.w + W_V * S.wstride);
+  shadow_ring(S, p.nmv + 1, p.nmv + 1);
+  if (final_pass) {
+    __syncthreads();
+    const int n2 = S.jd * S.kd;
+    for (int i = threadIdx.x; i < n2; i += blockDim.x) sa_turm_cell(S, p, i % S.jd + 1, i / S.jd + 1);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_sa_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                    int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  const ot2d_params& p = *S.P;
+  if (p.lamin || p.iturb != 1) return;
+  if (j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) return;
+  bool bodyflag = false;
+  for (int ib = 0; ib < p.nbc; ++ib) if (p.ibtyp[ib] == 5) bodyflag = true;
+  sa_rhs_cell(S, p, j, k, bodyflag);
+}
+
+// line solves: slice i owns lines [lfirst[i], lfirst[i+1]) (one thread each)
+template <class R>
+__global__ void k_sa_lsolve(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst, int nslice, int dir) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= lfirst[nslice]) return;
+  int lo = 0, hi = nslice - 1;
+  while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (lfirst[mid] <= gid) lo = mid; else hi = mid - 1; }
+  const Slice<R>& S = sl[lo];
+  const ot2d_params& p = *S.P;
+  if (p.lamin || p.iturb != 1) return;
+  const int line = gid - lfirst[lo];
+  if (dir == 0) { int k = p.kbeg + line; if (k <= p.kend) sa_lsolvej_line(S, p, k); }
+  else { int j = p.jbeg + line; if (j <= p.jend) sa_lsolvek_line(S, p, j); }
+}
+
+// q(1:4) += s*max(iblank,0) on interior cells (step.f:203-213), FP64 state
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                    int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  const ot2d_params& p = *S.P;
+  if (j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) return;
+  const int64_t o = at(S.jd, j, k);
+  int ibi = S.iblank[o];
+  double m = (double)(ibi > 0 ? ibi : 0);
+#pragma unroll
+  for (int n = 0; n < 4; ++n) {
+    double v = S.q64[n * S.qs + o] + (double)S.s[n * S.qs + o] * m;
+    S.q64[n * S.qs + o] = v;
+    if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = (R)v;
+  }
+}
+
+// monitor (step.f:356-370) on the FP64 state: count of cells with a^2 <=
+// 0.002 or a non-finite a^2 -> status bit 2
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_monitor(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                     int nslice) {
+  OT2D_CELL_MAP();
+  bool bad = false;
+  if (inside) {
+    const ot2d_params& p = *S.P;
+    const int64_t o = at(S.jd, j, k);
+    double rho = S.q64[o];
+    double qq = sq(S.q64[S.qs + o]) + sq(S.q64[2 * S.qs + o]);
+    double asq = p.ggm1 * (S.q64[3 * S.qs + o] - .5 * qq / rho) / rho;
+    bad = (asq <= 0.002) || (asq + 1 == asq) || (asq != asq);
+  }
+  bad = __syncthreads_or(bad);
+  if (bad && threadIdx.x == 0 && S.ist) atomicOr(&S.ist[2], 2);
+}
+
+// FP64 wall forces of one slice (forces.f:130-398); one CTA per slice,
+// integrands in parallel, sums by thread 0 in the reference's j order.
+// out[0..3] = cfx, cfy, cm0, cpower
+template <class R>
+__global__ void k_forces(const Slice<R>* __restrict__ sl, const double* const* __restrict__ xv,
+                         const double* const* __restrict__ yv, double* __restrict__ out) {
+  extern __shared__ double fsh[];
+  const Slice<R>& S = sl[blockIdx.x];
+  const ot2d_params& p = *S.P;
+  const int jd = S.jd, nq = p.nq, jmax = p.jmax;
+  const double* q = S.q64; const int64_t qs = S.qs;
+  auto Q = [&](int j, int k, int n) { return q[(int64_t)(n - 1) * qs + at(jd, j, k)]; };
+  auto XV = [&](int j, int k) { return xv[blockIdx.x][(int64_t)(k - 1) * jmax + (j - 1)]; };
+  auto YV = [&](int j, int k) { return yv[blockIdx.x][(int64_t)(k - 1) * jmax + (j - 1)]; };
+  const int k = p.kbeg, k2 = k + 1, k3 = k2 + 1, j1 = p.jtail1, j2 = p.jtail2, nw = j2 - j1 + 1;
+  double* zz = fsh; double* sxx = fsh + nw; double* syy = fsh + 2 * nw;
+  const double fmm = (p.fsmach != 0) ? p.fsmach : ((p.fmtip != 0) ? p.fmtip : 1.0);
+  const double gm1 = p.gm1, gamma = p.gamma;
+  for (int j = j1 + threadIdx.x; j <= j2; j += blockDim.x) {
+    double rr = 1. / Q(j, k, 1), rho = Q(j, k, 1) * Q(j, k, nq);
+    double u = Q(j, k, 2) * rr, v = Q(j, k, 3) * rr, e = Q(j, k, 4) * Q(j, k, nq);
+    double vsq = u * u + v * v, pp = gm1 * (e - rho * vsq / 2.), pp1 = pp / p.pinf;
+    double cp = 2. * (pp1 - 1.) / (gamma * sq(fmm));
+    double z = cp;
+    rr = 1. / Q(j, k - 1, 1); rho = Q(j, k - 1, 1) * Q(j, k - 1, nq);
+    u = Q(j, k - 1, 2) * rr; v = Q(j, k - 1, 3) * rr; e = Q(j, k - 1, 4) * Q(j, k - 1, nq);
+    vsq = u * u + v * v; pp = gm1 * (e - rho * vsq / 2.); pp1 = pp / p.pinf;
+    cp = 2. * (pp1 - 1.) / (gamma * sq(fmm));
+    zz[j - j1] = 0.5 * (z + cp);
+  }
+  __syncthreads();
+  double cn = 0., cc = 0., cmle = 0., cpinv = 0.;
+  if (threadIdx.x == 0) {
+    for (int j = j1; j <= j2; ++j) {
+      int jv = j - p.nhalo, kv = k - p.nhalo;
+      double z = zz[j - j1];
+      cn = cn - z * (XV(jv + 1, kv) - XV(jv, kv));
+      cc = cc + z * (YV(jv + 1, kv) - YV(jv, kv));
+      cmle = cmle + z * (0.5 * (XV(jv + 1, kv) + XV(jv, kv)) * (XV(jv + 1, kv) - XV(jv, kv)) +
+                         0.5 * (YV(jv + 1, kv) + YV(jv, kv)) * (YV(jv + 1, kv) - YV(jv, kv)));
+      double u = Q(j, k, 2) / Q(j, k, 1), v = Q(j, k, 3) / Q(j, k, 1);
+      double um = Q(j, k - 1, 2) / Q(j, k - 1, 1), vm = Q(j, k - 1, 3) / Q(j, k - 1, 1);
+      cpinv = cpinv + 0.5 * (u + um) * z * (YV(jv + 1, kv) - YV(jv, kv)) - 0.5 * (v + vm) * z * (XV(jv + 1, kv) - XV(jv, kv));
+    }
+    double half = (double)p.half;
+    cn = cn - half * cn; cmle = cmle - half * cmle; cc = cc + half * cc;
+  }
+  __syncthreads();
+  double cnv = 0., ccv = 0., cmlev = 0., cpv = 0.;
+  if (!p.invisc) {
+    const double amu = p.rinf * 1. / p.rey, uinf2 = sq(fmm);
+    const double *xx = S.xx64, *xy = S.xy64, *yx = S.yx64, *yy = S.yy64;
+    for (int j = j1 + threadIdx.x; j <= j2; j += blockDim.x) {
+      double uxi, vxi;
+      if (j == j1) {
+        uxi = Q(j + 1, k, 2) / Q(j + 1, k, 1) - Q(j, k, 2) / Q(j, k, 1);
+        vxi = Q(j + 1, k, 3) / Q(j + 1, k, 1) - Q(j, k, 3) / Q(j, k, 1);
+      } else if (j == j2) {
+        uxi = Q(j, k, 2) / Q(j, k, 1) - Q(j - 1, k, 2) / Q(j - 1, k, 1);
+        vxi = Q(j, k, 3) / Q(j, k, 1) - Q(j - 1, k, 3) / Q(j - 1, k, 1);
+      } else {
+        uxi = .5 * (Q(j + 1, k, 2) / Q(j + 1, k, 1) - Q(j - 1, k, 2) / Q(j - 1, k, 1));
+        vxi = .5 * (Q(j + 1, k, 3) / Q(j + 1, k, 1) - Q(j - 1, k, 3) / Q(j - 1, k, 1));
+      }
+      double ueta = -1.5 * Q(j, k, 2) / Q(j, k, 1) + 2. * Q(j, k2, 2) / Q(j, k2, 1) - .5 * Q(j, k3, 2) / Q(j, k3, 1);
+      double veta = -1.5 * Q(j, k, 3) / Q(j, k, 1) + 2. * Q(j, k2, 3) / Q(j, k2, 1) - .5 * Q(j, k3, 3) / Q(j, k3, 1);
+      const int64_t o = at(jd, j, k);
+      double xix = xx[o], xiy = xy[o], etax = yx[o], etay = yy[o];
+      double sfdiv = 2. / 3 * (uxi * xix + ueta * etax + vxi * xiy + veta * etay);
+      double a = amu * (2. * (uxi * xix + ueta * etax) - sfdiv);
+      double b = amu * (2. * (vxi * xiy + veta * etay) - sfdiv);
+      double tauw = amu * ((uxi * xiy + ueta * etay) + (vxi * xix + veta * etax));
+      sxx[j - j1] = a / (.5 * p.rinf * uinf2);
+      syy[j - j1] = b / (.5 * p.rinf * uinf2);
+      zz[j - j1] = tauw / (.5 * p.rinf * uinf2);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int j = j1; j <= j2; ++j) {
+        int jv = j - p.nhalo, kv = k - p.nhalo;
+        double z = zz[j - j1], sx = sxx[j - j1], sy = syy[j - j1];
+        ccv = ccv + z * (XV(jv + 1, kv) - XV(jv, kv)) - sx * (YV(jv + 1, kv) - YV(jv, kv));
+        cnv = cnv - z * (YV(jv + 1, kv) - YV(jv, kv)) + sy * (XV(jv + 1, kv) - XV(jv, kv));
+        cmlev = cmlev + z * (0.5 * (XV(jv + 1, kv) + XV(jv, kv)) * (YV(jv + 1, kv) - YV(jv, kv)) +
+                             0.5 * (YV(jv + 1, kv) + YV(jv, kv)) * (XV(jv + 1, kv) - XV(jv, kv))) -
+                0.5 * (XV(jv + 1, kv) + XV(jv, kv)) * (XV(jv + 1, kv) - XV(jv, kv)) * sy -
+                0.5 * (YV(jv + 1, kv) + YV(jv, kv)) * (YV(jv + 1, kv) - YV(jv, kv)) * sx;
+        double u = Q(j, k, 2) / Q(j, k, 1), v = Q(j, k, 3) / Q(j, k, 1);
+        double um = Q(j, k - 1, 2) / Q(j, k - 1, 1), vm = Q(j, k - 1, 3) / Q(j, k - 1, 1);
+        cpv = cpv + 0.5 * (u + um) * z * (XV(jv + 1, kv) - XV(jv, kv)) - 0.5 * (u + um) * sx * (YV(jv + 1, kv) - YV(jv, kv)) -
+              0.5 * (v + vm) * z * (YV(jv + 1, kv) - YV(jv, kv)) + 0.5 * (v + vm) * sy * (XV(jv + 1, kv) - XV(jv, kv));
+      }
+      double half = (double)p.half;
+      cnv = cnv - half * cnv; cmlev = cmlev - half * cmlev; ccv = ccv + half * ccv;
+    }
+  }
+  if (threadIdx.x == 0) {
+    out[4 * blockIdx.x + 0] = cc + ccv;
+    out[4 * blockIdx.x + 1] = cn + cnv;
+    out[4 * blockIdx.x + 2] = cmle + cmlev;
+    out[4 * blockIdx.x + 3] = (cpinv + cpv) / fmm;
+  }
+}
+
+}  // namespace ot2d

@@ -1,0 +1,50 @@
+// launch.h -- host-side launchers of the batched kernels.  Each launcher
+// covers every slice of a batch with one kernel launch on `st`.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ot2d {
+
+template <class R> struct Slice;
+struct NormPart;
+
+constexpr int CELL_BS = 256;
+
+struct Batch {
+  int nslice = 0;          // slices in the batch
+  int cell_blocks = 0;     // blocks of the cell-parallel kernels
+  int max_lu_warps = 1;    // warps per CTA of the LU-SGS kernel
+  int max_wall = 1;        // most wall cells of one slice (force kernel smem)
+  int jlines = 0, klines = 0;  // total k-lines / j-lines (SA line solves)
+  const int32_t* d_first = nullptr;   // [nslice+1] first cell block of each slice
+  const int32_t* d_jfirst = nullptr;  // [nslice+1] first k-line (lsolvej) of each slice
+  const int32_t* d_kfirst = nullptr;  // [nslice+1] first j-line (lsolvek) of each slice
+  NormPart* d_part = nullptr;         // [cell_blocks] norm partials
+};
+
+// One full iteration of step.f for every slice of the batch:
+// time_step, bc, rhsup (+visrhs, +time-spectral), norms, rbc, ilu2d,
+// vmu_sa (when `turb`), update, monitor.
+template <class R>
+cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, cudaStream_t st);
+
+// Individual phases (the drop-in routines call these on a batch of one).
+template <class R> cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st);
+template <class R> cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st);
+template <class R> cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+// scale = 1: multiply s by tscale first (step.f:141-148); 0: s already scaled
+template <class R> cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st);
+template <class R> cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b, int inviscid, int viscous, cudaStream_t st);
+// assembly flags: see AS_* in kernels.cuh
+enum { AS_ACC = 1, AS_INV = 2, AS_VISC = 4, AS_TS = 8, AS_NORM = 16 };
+template <class R> cudaError_t launch_assemble(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st);
+template <class R> cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+template <class R> cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+template <class R> cudaError_t launch_monitor(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+template <class R>
+cudaError_t launch_forces(const Slice<R>* d_sl, const Batch& b, const double* const* d_xv, const double* const* d_yv,
+                          double* d_out, cudaStream_t st);
+
+}  // namespace ot2d

@@ -1,0 +1,103 @@
+// launchers.cuh -- launcher bodies, instantiated once per arithmetic type.
+#pragma once
+#include "kernels.cuh"
+
+namespace ot2d {
+
+template <class R>
+cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_time_step<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st) {
+  k_bc<R><<<b.nslice, 128, 0, st>>>(d_sl, advance);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st) {
+  k_faces<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  if (viscous) k_visc<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  const int flags = AS_INV | AS_TS | AS_NORM | (viscous ? AS_VISC : 0);
+  k_assemble<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, flags, b.d_part);
+  k_norm_final<R><<<b.nslice, 32, 0, st>>>(d_sl, b.d_first, b.nslice, b.d_part);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b, int inviscid, int viscous, cudaStream_t st) {
+  if (inviscid) k_faces<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  if (viscous) k_visc<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_assemble(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st) {
+  k_assemble<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, flags, b.d_part);
+  if (flags & AS_NORM) k_norm_final<R><<<b.nslice, 32, 0, st>>>(d_sl, b.d_first, b.nslice, b.d_part);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_rbc<R><<<b.nslice, 128, 0, st>>>(d_sl);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st) {
+  k_lusgs<R><<<b.nslice, 32 * b.max_lu_warps, 0, st>>>(d_sl, scale);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_sa_prep<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  k_turbc<R><<<b.nslice, 256, 0, st>>>(d_sl, 0);
+  k_sa_rhs<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  k_sa_lsolve<R><<<(b.jlines + 63) / 64, 64, 0, st>>>(d_sl, b.d_jfirst, b.nslice, 0);
+  k_sa_lsolve<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice, 1);
+  k_turbc<R><<<b.nslice, 256, 0, st>>>(d_sl, 1);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_update<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_monitor(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_monitor<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_forces(const Slice<R>* d_sl, const Batch& b, const double* const* d_xv, const double* const* d_yv,
+                          double* d_out, cudaStream_t st) {
+  size_t smem = sizeof(double) * 3 * (size_t)b.max_wall;
+  k_forces<R><<<b.nslice, 128, smem, st>>>(d_sl, d_xv, d_yv, d_out);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, cudaStream_t st) {
+  cudaError_t e;
+  if ((e = launch_time_step(d_sl, b, st)) != cudaSuccess) return e;
+  if ((e = launch_bc(d_sl, b, 1, st)) != cudaSuccess) return e;
+  if ((e = launch_residual(d_sl, b, viscous, st)) != cudaSuccess) return e;
+  if ((e = launch_rbc(d_sl, b, st)) != cudaSuccess) return e;
+  if ((e = launch_lusgs(d_sl, b, 1, st)) != cudaSuccess) return e;
+  if (turb && (e = launch_sa(d_sl, b, st)) != cudaSuccess) return e;
+  if ((e = launch_update(d_sl, b, st)) != cudaSuccess) return e;
+  return launch_monitor(d_sl, b, st);
+}
+
+#define OT2D_INSTANTIATE(R)                                                                              \
+  template cudaError_t launch_iteration<R>(const Slice<R>*, const Batch&, int, int, cudaStream_t);      \
+  template cudaError_t launch_time_step<R>(const Slice<R>*, const Batch&, cudaStream_t);                \
+  template cudaError_t launch_bc<R>(const Slice<R>*, const Batch&, int, cudaStream_t);                  \
+  template cudaError_t launch_residual<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
+  template cudaError_t launch_rbc<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
+  template cudaError_t launch_lusgs<R>(const Slice<R>*, const Batch&, int, cudaStream_t);               \
+  template cudaError_t launch_faces<R>(const Slice<R>*, const Batch&, int, int, cudaStream_t);          \
+  template cudaError_t launch_assemble<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
+  template cudaError_t launch_sa<R>(const Slice<R>*, const Batch&, cudaStream_t);                       \
+  template cudaError_t launch_update<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
+  template cudaError_t launch_monitor<R>(const Slice<R>*, const Batch&, cudaStream_t);                  \
+  template cudaError_t launch_forces<R>(const Slice<R>*, const Batch&, const double* const*,            \
+                                        const double* const*, double*, cudaStream_t);
+
+}  // namespace ot2d

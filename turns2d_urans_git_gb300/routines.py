@@ -1,0 +1,151 @@
+"""The reference's hot-path subroutines, by their reference names.
+
+Each function forwards to the drop-in C-ABI routine that replaces the
+Fortran subroutine of the same name (declared in include/ot2d.h) with the
+reference's argument order.  Arrays are flat float64 / int32 buffers in the
+reference's column-major layout: numpy arrays (host memory, copied in and
+out by the library) or CUDA tensors / any object exposing
+``data_ptr()`` (device memory, used in place).  Scalars are passed by
+reference as the Fortran callers do.  A non-zero status raises
+``RoutineError``.
+"""
+import ctypes as C
+
+import numpy as np
+
+from .abi import Params
+from .api import lib
+
+_i = C.c_int32
+
+
+class RoutineError(RuntimeError):
+    def __init__(self, name, code):
+        super().__init__("%s returned status %d" % (name, code))
+        self.code = code
+
+
+def _p(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    if isinstance(a, np.ndarray):
+        if not (a.flags["C_CONTIGUOUS"] or a.flags["F_CONTIGUOUS"]):
+            raise ValueError("arrays must be contiguous")
+        if a.dtype not in (np.float64, np.int32):
+            raise TypeError("arrays must be float64 or int32, got %s" % a.dtype)
+        return C.c_void_p(a.ctypes.data)
+    raise TypeError(type(a))
+
+
+def _ref(v):
+    return C.byref(_i(int(v)))
+
+
+def _call(name, *args):
+    f = getattr(lib(), name)
+    f.restype = C.c_int
+    rc = f(*args)
+    if rc != 0:
+        raise RoutineError(name, rc)
+    return rc
+
+
+def set_params(p: Params):
+    """params_global of the current mesh (replaces set_pointers_globals)."""
+    _call("ot2d_set_params", C.byref(p))
+
+
+def rhsup(q, s, xx, xy, yx, yy, x, y, xv, yv, xold, yold, xole, yole, iblank, ugv, vgv, jd, kd, nei, im, bt):
+    """src/eulerrhs.f:2 -- s -= inviscid flux differences."""
+    _call("ot2d_rhsup", _p(q), _p(s), _p(xx), _p(xy), _p(yx), _p(yy), _p(x), _p(y), _p(xv), _p(yv), _p(xold),
+          _p(yold), _p(xole), _p(yole), _p(iblank), _p(ugv), _p(vgv), _ref(jd), _ref(kd), _ref(nei), _ref(im), _p(bt))
+
+
+def visrhs(turmu, q, s, xx, xy, yx, yy, ug, vg, tscale, iblank, jd, kd):
+    """src/visrhs.f:2 -- s += viscous flux differences."""
+    _call("ot2d_visrhs", _p(turmu), _p(q), _p(s), _p(xx), _p(xy), _p(yx), _p(yy), _p(ug), _p(vg), _p(tscale),
+          _p(iblank), _ref(jd), _ref(kd))
+
+
+def bc(q, x, y, xx, xy, yx, yy, ug, vg, im, jd, kd, bt):
+    """src/bc.f:2 -- halo cells of q."""
+    _call("ot2d_bc", _p(q), _p(x), _p(y), _p(xx), _p(xy), _p(yx), _p(yy), _p(ug), _p(vg), _ref(im), _ref(jd),
+          _ref(kd), _p(bt))
+
+
+def rbc(q, s, x, y, xx, xy, yx, yy, ug, vg, im, jd, kd, bt):
+    """src/bc.f:88 -- halo cells of the residual."""
+    _call("ot2d_rbc", _p(q), _p(s), _p(x), _p(y), _p(xx), _p(xy), _p(yx), _p(yy), _p(ug), _p(vg), _ref(im),
+          _ref(jd), _ref(kd), _p(bt))
+
+
+def time_step(q, xx, xy, yx, yy, ug, vg, tscale, bt, iblank, jd, kd):
+    """src/time.f:2 -- local time step."""
+    _call("ot2d_time_step", _p(q), _p(xx), _p(xy), _p(yx), _p(yy), _p(ug), _p(vg), _p(tscale), _p(bt), _p(iblank),
+          _ref(jd), _ref(kd))
+
+
+def ilu2d(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, tscale):
+    """src/lhs.f:470 -- LU-SGS implicit operator (s already times tscale)."""
+    _call("ot2d_ilu2d", _p(q), _p(s), _ref(jd), _ref(kd), _ref(js), _ref(je), _ref(ks), _ref(ke), _p(xx), _p(xy),
+          _p(yx), _p(yy), _p(ug), _p(vg), _p(turmu), _p(tscale))
+
+
+def vmu_sa(q, s, turmu, x, y, xv, yv, xx, xy, yx, yy, ug, vg, jd, kd, tscale, iblank, im, nsp):
+    """src/samodel2d.f:2 -- one Spalart-Allmaras update of q(:,:,5) and turmu."""
+    _call("ot2d_vmu_sa", _p(q), _p(s), _p(turmu), _p(x), _p(y), _p(xv), _p(yv), _p(xx), _p(xy), _p(yx), _p(yy),
+          _p(ug), _p(vg), _ref(jd), _ref(kd), _p(tscale), _p(iblank), _ref(im), _ref(nsp))
+
+
+def timespectralrhs(q, s, Ds, jd, kd, nsp):
+    """src/sources.f:2 -- time-spectral coupling term of instance nsp."""
+    _call("ot2d_timespectralrhs", _p(q), _p(s), _p(Ds), _ref(jd), _ref(kd), _ref(nsp))
+
+
+def step(q, qtn, qtnm1, qnewt, s, x, y, xv, yv, iblank, xx, xy, yx, yy, ug, vg, ugv, vgv, xold, yold, xole, yole,
+         turmu, tscale, bt, Ds, im, jd, kd):
+    """src/step.f:2 -- one iteration of every time instance; returns the
+    (rsum, resrho, resmax) norms of each instance."""
+    f = lib().ot2d_step
+    f.restype = C.c_int
+    rc = f(_p(q), _p(qtn), _p(qtnm1), _p(qnewt), _p(s), _p(x), _p(y), _p(xv), _p(yv), _p(iblank), _p(xx), _p(xy),
+           _p(yx), _p(yy), _p(ug), _p(vg), _p(ugv), _p(vgv), _p(xold), _p(yold), _p(xole), _p(yole), _p(turmu),
+           _p(tscale), _p(bt), _p(Ds), _ref(im), _ref(jd), _ref(kd))
+    norms = last_norms(64)
+    if rc != 0:
+        raise RoutineError("ot2d_step", rc)
+    return norms
+
+
+def last_norms(n):
+    out = np.zeros(3 * n)
+    lib().ot2d_last_norms(C.c_void_p(out.ctypes.data), 3 * n)
+    return out
+
+
+def monitor(q, jd, kd):
+    """src/step.f:332 -- returns mstop (1 on a non-positive a^2 or NaN)."""
+    mstop = _i(0)
+    _call("ot2d_monitor", C.byref(mstop), _p(q), _ref(jd), _ref(kd))
+    return mstop.value
+
+
+def force2d(jd, kd, x, y, xv, yv, q, xx, xy, yx, yy, nsp=1):
+    """src/forces.f:130 -- (cfx, cfy, cm0, cpower)."""
+    out = [C.c_double(0) for _ in range(4)]
+    _call("ot2d_force2d", _ref(jd), _ref(kd), _p(x), _p(y), _p(xv), _p(yv), _p(q), _p(xx), _p(xy), _p(yx), _p(yy),
+          C.byref(out[0]), C.byref(out[1]), C.byref(out[2]), C.byref(out[3]), _ref(nsp))
+    return tuple(o.value for o in out)
+
+
+def find_cellcenter(x, y, xv, yv, jd, kd, im=1):
+    """src/setup.f:111."""
+    _call("ot2d_find_cellcenter", _p(x), _p(y), _p(xv), _p(yv), _ref(jd), _ref(kd), _ref(im))
+
+
+def metfv(q, x, y, xv, yv, xx, xy, yx, yy, jd, kd, im=1):
+    """src/setup.f:440 -- J into q(:,:,nq) and the J-scaled metrics."""
+    _call("ot2d_metfv", _p(q), _p(x), _p(y), _p(xv), _p(yv), _p(xx), _p(xy), _p(yx), _p(yy), _ref(jd), _ref(kd),
+          _ref(im))
