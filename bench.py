@@ -1,0 +1,320 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 OVERTURNS-2D hot path.
+
+Workload (the configuration the headline metric is quoted on): viscous
+RANS-SA, NACA 0012 C-mesh 513x129 (first wall spacing 1e-6 chords), M=0.15,
+alpha=10 deg, Re=6e6 per chord, MUSCL kappa=1/3 + Roe, LU-SGS, local CFL 50
+-- run as a batch of B independent requests (alpha varied, seeded) resident
+in HBM.  A "step" is one iteration of the reference's step.f loop
+(time_step, bc, rhsup + visrhs, norms, rbc, ilu2d, vmu_sa, update, monitor)
+over the whole batch.  The meshes are generated algebraically from a seed
+(no dataset exists); flow fields start from freestream.
+
+  value   FP32-mixed batched cell-updates/s, device-resident (kernel path)
+  e2e     the same through the host-buffer C-ABI path: every step copies the
+          state of every request host->device and back (pinned buffers)
+  fp64    the plain FP64 path on the same batch (reported beside it)
+
+--impl reference times the reference's algorithm on the host cores: the
+CPU FP64 oracle (a line-by-line C++ restatement of the Fortran; the
+Fortran itself cannot be compiled here -- no Fortran compiler), one request
+per thread.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s & converged solves/s (FP32-mixed batched vs FP64 plain) + p50/p99"
+UNIT = "cell-updates/s"
+JMAX, KMAX = 513, 129
+WORKLOAD = "RANS-SA NACA0012 C-mesh 513x129, M0.15 a10 Re6e6, MUSCL+Roe, LU-SGS CFL50"
+
+# algorithmic bytes per interior cell per launch of each kernel family of
+# the FP32-mixed path (compulsory array traffic)
+ALG_BYTES_F32 = {0: 44, 1: 0, 2: 72, 3: 88, 4: 104, 5: 0, 6: 188, 7: 200, 8: 96}
+PHASES = ["time_step", "bc", "faces", "visc_faces", "assemble", "rbc", "lusgs", "sa", "update"]
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def batch_cases(n, seed=0, jmax=JMAX, kmax=KMAX):
+    from turns2d_urans_git_gb300 import api
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        alfa = 10.0 if i == 0 else float(rng.uniform(0.0, 10.0))
+        out.append(api.config_c2(jmax=jmax, kmax=kmax, alfa=alfa))
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock, power and throttle reasons during the
+    timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev, self.proc, self.path = dev, None, None
+
+    def start(self):
+        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(cases, max_threads=None, target_s=12.0):
+    """The reference algorithm (CPU FP64 oracle) on the host cores: one
+    request per thread, each a bounded number of iterations.  Returns
+    (cell-updates/s, threads, sample description)."""
+    from tests import oracle_binding as ob
+    ob.lib()
+    ncores = os.cpu_count() or 1
+    nthr = min(max_threads or ncores, ncores, len(cases))
+    # size the sample from one short probe
+    _, prm, xv, yv = cases[0]
+    t0 = time.perf_counter()
+    ob.solve(prm, xv.ravel(), yv.ravel(), 2)
+    per_it = (time.perf_counter() - t0) / 2
+    iters = max(2, int(target_s / max(per_it, 1e-6)))
+    cells = (prm.jmax - 1) * (prm.kmax - 1)
+    results = [None] * nthr
+
+    def work(i):
+        _, p, x, y = cases[i % len(cases)]
+        t = time.perf_counter()
+        n, _, _, _ = ob.solve(p, x.ravel(), y.ravel(), iters)
+        results[i] = (abs(n), time.perf_counter() - t)
+
+    th = [threading.Thread(target=work, args=(i,)) for i in range(nthr)]
+    t0 = time.perf_counter()
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    wall = time.perf_counter() - t0
+    done = sum(r[0] for r in results)
+    value = done * cells / wall
+    sample = "%d requests x %d iterations of the 513x129 SA case on %d threads (%.1f s wall)" % (nthr, iters, nthr, wall)
+    return value, nthr, sample
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    cases = batch_cases(max(args.batch, os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    vals = []
+    for _ in range(args.warmup):
+        pass  # the oracle has no warm state
+    per_step = max(1.0, min(args.ref_seconds, 150.0 / max(args.steps, 1)))
+    for _ in range(args.steps):
+        v, thr, sample = cpu_reference(cases, target_s=per_step)
+        vals.append(v)
+    value = float(np.median(vals))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded algebraic C-meshes)",
+            "config": {"workload": WORKLOAD, "batch": len(cases), "per_step": "bounded sample, see cpu_baseline"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    from turns2d_urans_git_gb300 import api
+    from turns2d_urans_git_gb300.abi import OT2D_FP32_MIXED, OT2D_FP64
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    cases = batch_cases(args.batch, seed=1000 * rank)
+    cells = (JMAX - 1) * (KMAX - 1)
+    B = len(cases)
+
+    def make(precision):
+        sv = api.Solver(precision, device=local, check_every=10 ** 8)
+        ids = [sv.add(prm, xv, yv, orders=0.0, max_iters=10 ** 8) for (_, prm, xv, yv) in cases]
+        return sv, ids
+
+    def timed(sv, steps):
+        stream = torch.cuda.ExternalStream(sv.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sv.iterate(steps)
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # ---- FP32-mixed batched, device resident (value)
+    sv, ids = make(OT2D_FP32_MIXED)
+    resident = sv.device_bytes()
+    sv.iterate(args.warmup)
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    ms = timed(sv, args.steps)
+    clocks = clk.stop()
+    value = world * B * cells * args.steps / (ms / 1e3)
+    # phase timers of the same batch -> dominant kernel + roofline
+    prof = (C.c_double * 9)()
+    api.lib().ot2d_solver_profile.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int32]
+    rc = api.lib().ot2d_solver_profile(sv._h, 5, prof, 9)
+    phase_ms = {PHASES[i]: prof[i] for i in range(9)} if rc == 0 else {}
+    dom = max(range(9), key=lambda i: prof[i]) if rc == 0 else 6
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    alg = ALG_BYTES_F32[dom] * B * cells
+    achieved = alg / (prof[dom] * 1e-3) / 1e9 if rc == 0 and prof[dom] > 0 else None
+    # ---- e2e through the host-buffer ABI path
+    qh = [np.zeros(prm.jd * prm.kd * prm.nspec * prm.nq) for (_, prm, _, _) in cases]
+    for iid, (_, prm, _, _), q in zip(ids, cases, qh):
+        q[:] = sv.get_q(iid, prm)
+    pinned = []
+    for q in qh:
+        t = torch.from_numpy(q).pin_memory()
+        pinned.append(t)
+    ptrs = (C.POINTER(C.c_double) * B)(*[C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)) for t in pinned])
+    idarr = (C.c_int32 * B)(*ids)
+    L = api.lib()
+    L.ot2d_solver_iterate_host.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
+                                           C.POINTER(C.POINTER(C.c_double)), C.c_int32]
+    e2e_steps = max(3, args.steps // 2)
+    L.ot2d_solver_iterate_host(sv._h, B, idarr, ptrs, 1)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc2 = L.ot2d_solver_iterate_host(sv._h, B, idarr, ptrs, e2e_steps)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    qbytes = sum(q.nbytes for q in qh)
+    e2e = world * B * cells * e2e_steps / e2e_s if rc2 == 0 else None
+    sv.close()
+    # ---- plain FP64 on the same batch (reported beside the headline)
+    fp64 = None
+    if not args.skip_fp64:
+        sv64, _ = make(OT2D_FP64)
+        sv64.iterate(1)
+        torch.cuda.synchronize()
+        k64 = max(2, args.fp64_steps)
+        ms64 = timed(sv64, k64)
+        fp64 = world * B * cells * k64 / (ms64 / 1e3)
+        sv64.close()
+    # ---- CPU baseline (rank 0, N=1 only): the oracle on the host cores
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        v, thr, sample = cpu_reference(batch_cases(os.cpu_count() or 1), target_s=args.ref_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port", "sample": sample}
+    if rank == 0:
+        launches_per_step = 14 + 6  # kernels per iteration (+6 SA kernels)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 (f64 state update, norms, forces)",
+                "data": "synthetic (seeded algebraic NACA0012 C-meshes, freestream start)",
+                "config": {"workload": WORKLOAD, "batch_per_gpu": B, "interior_cells": cells,
+                           "parallelism": "replicas x%d" % world, "precision": "fp32-mixed",
+                           "l2": "inputs larger than L2: %.0f MB resident per GPU (L2 129 MB)" % (resident / 1e6)},
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes},
+                "fp64_plain": {"value": fp64, "unit": UNIT},
+                "gpu_launches": launches_per_step * args.steps,
+                "phase_ms": phase_ms,
+                "roofline": {"bound": "hbm", "kernel": PHASES[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": (achieved / peak) if achieved else None, "traffic": None,
+                             "peak_source": "measured" if peaks else "fallback"},
+                "clocks": clocks}
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

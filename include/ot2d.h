@@ -151,6 +151,16 @@ int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value);
 int ot2d_solver_sync(ot2d_solver* s);
 /* the CUDA stream (cudaStream_t) the solver launches on */
 void* ot2d_solver_stream(ot2d_solver* s);
+/* Phase timers: runs `iters` iterations phase by phase with CUDA events
+ * between the kernel families and returns the mean milliseconds per phase:
+ * 0 time_step, 1 bc, 2 inviscid faces, 3 viscous faces, 4 assembly + norms,
+ * 5 rbc, 6 LU-SGS, 7 SA, 8 update + monitor. */
+#define OT2D_NPHASE 9
+int ot2d_solver_profile(ot2d_solver* s, int32_t iters, double* ms, int32_t nphase);
+/* Host-resident state, as a Fortran caller that owns q: every iteration
+ * copies q(jd,kd,nspec,nq) of the listed live instances host->device, runs
+ * one batched iteration and copies q back (the host arrays are updated). */
+int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, double* const* q_host, int32_t iters);
 /* Admit one solve: params + vertex grid of time instance 1 (jmax*kmax).
  * Returns the instance id (>= 0) or -status.  `orders` = target L2 drop in
  * decades; max_iters caps the iterations. */

@@ -32,6 +32,7 @@ struct Ctx {
   ot2d_params* dP = nullptr;
   double* dwork = nullptr; size_t wcap = 0;      // scratch arrays of one slice (or nspec slices)
   double* dred = nullptr; int32_t* dist = nullptr;
+  int nslice = 1;
   DevBatch<double> batch;
   std::vector<Staged> staged;
   std::vector<void*> pool;                         // staging buffers of this call
@@ -121,7 +122,9 @@ int prepare(int nslice, int& err) {
   if ((err = ensure_stream())) return err;
   if (!g_ctx.has) return err = OT2D_ERR_NOPARAMS;
   const size_t n2 = (size_t)g_ctx.P.jd * g_ctx.P.kd, ws = (n2 + 63) / 64 * 64;
-  const size_t need = ws * 20 * nslice + 8 * ws;
+  const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd);
+  const size_t need = ws * 20 * nslice + 8 * ws + rec * nslice;
+  g_ctx.nslice = nslice;
   if (need > g_ctx.wcap) {
     if (g_ctx.dwork) cudaFree(g_ctx.dwork);
     if (cudaMalloc(&g_ctx.dwork, need * sizeof(double)) != cudaSuccess) { g_ctx.dwork = nullptr; g_ctx.wcap = 0; return err = OT2D_ERR_NOMEM; }
@@ -141,6 +144,7 @@ Slice<double> base_slice(int nsp, int nspec, int64_t qs) {
   const size_t n2 = (size_t)p.jd * p.kd, ws = (n2 + 63) / 64 * 64;
   S.w = g_ctx.dwork + (size_t)(nsp - 1) * ws * 20;
   S.wstride = (int64_t)ws;
+  S.lurec = g_ctx.dwork + ws * 20 * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = g_ctx.dred + (size_t)RED_N * (nsp - 1);
   S.ist = nullptr;
   return S;

@@ -69,6 +69,7 @@ size_t plan(const ot2d_params& p, int precision, F&& assign) {
   assign("turmu", L.take(rb * n2 * nspec));
   assign("sn", L.take(rb * n2 * nspec));
   assign("w", L.take(rb * ws * NSCRATCH * nspec));
+  assign("lurec", L.take(rb * (size_t)lu_rec_elems(p.jd, p.kd) * nspec));
   return L.total;
 }
 
@@ -137,6 +138,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     else if (n == "turmu") d.turmu = ptr;
     else if (n == "sn") d.sn = ptr;
     else if (n == "w") d.w = ptr;
+    else if (n == "lurec") d.lurec = ptr;
   }
   const bool mixed = precision == OT2D_FP32_MIXED;
   if (!mixed) { d.q = d.q64; d.xx = d.xx64; d.xy = d.xy64; d.yx = d.yx64; d.yy = d.yy64; d.ug = d.ug64; d.vg = d.vg64; }
@@ -242,6 +244,7 @@ Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
   S.sn = R_(d.sn);
   S.w = (R*)d.w + (size_t)(nsp - 1) * d.wstride * NSCRATCH;
   S.wstride = (int64_t)d.wstride;
+  S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = red; S.ist = ist;
   S.Ds = p.timespectral ? d.Ds : nullptr;
   S.xx64 = D_(d.xx64); S.xy64 = D_(d.xy64); S.yx64 = D_(d.yx64); S.yy64 = D_(d.yy64);
@@ -254,27 +257,26 @@ template Slice<float> make_slice<float>(const DevSolve&, int, double*, int32_t*)
 template <class R>
 int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   const int n = (int)sl.size();
-  std::vector<int32_t> idx(3 * (n + 1));
-  std::vector<ot2d_params> hp;  // not needed: params live on the device
-  int cells = 0, jl = 0, kl = 0, maxw = 1, maxwall = 1;
-  // host copies of the dims come from the slices themselves (jd, kd); the
-  // interior extents follow from nhalo = 1
+  // four prefix tables of n+1 entries: cell blocks, k-lines, j-lines, LU record blocks
+  std::vector<int32_t> idx(4 * (n + 1));
+  int cells = 0, jl = 0, kl = 0, lub = 0, maxw = 1, maxwall = 1;
   for (int i = 0; i < n; ++i) {
-    idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl;
+    idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl; idx[3 * (n + 1) + i] = lub;
     const int jd = sl[i].jd, kd = sl[i].kd;
     cells += (jd * kd + CELL_BS - 1) / CELL_BS;
     jl += kd - 2;   // k-lines solved along j
     kl += jd - 2;   // j-lines solved along k
-    maxw = std::max(maxw, (kd - 2 + 31) / 32);
+    lub += (lu_nband(kd) * lu_nstep(jd) * 32 + CELL_BS - 1) / CELL_BS;
+    maxw = std::max(maxw, lu_nband(kd));
     maxwall = std::max(maxwall, jd);
   }
-  idx[n] = cells; idx[2 * (n + 1) - 1] = jl; idx[3 * (n + 1) - 1] = kl;
+  idx[n] = cells; idx[2 * (n + 1) - 1] = jl; idx[3 * (n + 1) - 1] = kl; idx[4 * (n + 1) - 1] = lub;
   if ((size_t)n > cap_sl) {
     if (d_sl) cudaFree(d_sl);
     if (d_idx) cudaFree(d_idx);
     cap_sl = std::max((size_t)n, (size_t)2 * cap_sl);
     if (cudaMalloc(&d_sl, cap_sl * sizeof(Slice<R>)) != cudaSuccess) return OT2D_ERR_NOMEM;
-    if (cudaMalloc(&d_idx, 3 * (cap_sl + 1) * sizeof(int32_t)) != cudaSuccess) return OT2D_ERR_NOMEM;
+    if (cudaMalloc(&d_idx, 4 * (cap_sl + 1) * sizeof(int32_t)) != cudaSuccess) return OT2D_ERR_NOMEM;
   }
   if ((size_t)cells > cap_part) {
     if (d_part) cudaFree(d_part);
@@ -290,7 +292,8 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   b.max_lu_warps = maxw;
   b.max_wall = maxwall;
   b.jlines = jl; b.klines = kl;
-  b.d_first = d_idx; b.d_jfirst = d_idx + (n + 1); b.d_kfirst = d_idx + 2 * (n + 1);
+  b.lu_blocks = lub;
+  b.d_first = d_idx; b.d_jfirst = d_idx + (n + 1); b.d_kfirst = d_idx + 2 * (n + 1); b.d_lfirst = d_idx + 3 * (n + 1);
   b.d_part = d_part;
   return OT2D_OK;
 }

@@ -7,6 +7,7 @@
 #include "ot2d.h"
 #include "../kernels/dev_common.cuh"
 #include "../kernels/k_misc.cuh"
+#include "../kernels/k_lusgs.cuh"
 #include "../kernels/launch.h"
 
 namespace ot2d {
@@ -34,6 +35,7 @@ struct DevSolve {
   void *q = nullptr, *s = nullptr, *xx = nullptr, *xy = nullptr, *yx = nullptr, *yy = nullptr;
   void *fxa = nullptr, *fya = nullptr, *gxa = nullptr, *gya = nullptr, *ftj = nullptr, *gtj = nullptr;
   void *ug = nullptr, *vg = nullptr, *tscale = nullptr, *bt = nullptr, *turmu = nullptr, *sn = nullptr, *w = nullptr;
+  void* lurec = nullptr;
 };
 
 // bytes one solve needs on the device

@@ -187,6 +187,42 @@ int forces_t(ot2d_solver* s, const std::vector<int>& ids, DevBatch<R>& tmp) {
   return OT2D_OK;
 }
 
+// Phase timing of the iteration (events between the kernel families on the
+// solver stream); advances the live requests by `iters` iterations.
+template <class R>
+int profile_t(ot2d_solver* s, DevBatch<R>& B, int iters, double* ms) {
+  cudaEvent_t ev[OT2D_NPHASE + 1];
+  for (auto& e : ev) cudaEventCreate(&e);
+  for (int p = 0; p < OT2D_NPHASE; ++p) ms[p] = 0.0;
+  const int visc = s->any_viscous ? 1 : 0, turb = s->any_turb ? 1 : 0;
+  int err = OT2D_OK;
+  for (int it = 0; it < iters && !err; ++it) {
+    cudaError_t e = cudaSuccess;
+    auto rec = [&](int i) { cudaEventRecord(ev[i], s->st); };
+    rec(0);
+    e = launch_time_step<R>(B.d_sl, B.b, s->st); rec(1);
+    if (!e) e = launch_bc<R>(B.d_sl, B.b, 1, s->st); rec(2);
+    if (!e) e = launch_faces<R>(B.d_sl, B.b, 1, 0, s->st); rec(3);
+    if (!e) e = launch_faces<R>(B.d_sl, B.b, 0, visc, s->st); rec(4);
+    if (!e) e = launch_assemble<R>(B.d_sl, B.b, AS_INV | AS_TS | AS_NORM | (visc ? AS_VISC : 0), s->st); rec(5);
+    if (!e) e = launch_rbc<R>(B.d_sl, B.b, s->st); rec(6);
+    if (!e) e = launch_lusgs<R>(B.d_sl, B.b, 1, s->st); rec(7);
+    if (!e && turb) e = launch_sa<R>(B.d_sl, B.b, s->st); rec(8);
+    if (!e) e = launch_update<R>(B.d_sl, B.b, s->st);
+    if (!e) e = launch_monitor<R>(B.d_sl, B.b, s->st); rec(9);
+    if (e != cudaSuccess || cudaEventSynchronize(ev[9]) != cudaSuccess) { err = OT2D_ERR_CUDA; break; }
+    for (int p = 0; p < OT2D_NPHASE; ++p) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[p], ev[p + 1]);
+      ms[p] += t;
+    }
+    ++s->since_check;
+  }
+  for (int p = 0; p < OT2D_NPHASE; ++p) ms[p] /= iters;
+  for (auto& e : ev) cudaEventDestroy(e);
+  return err;
+}
+
 int check(ot2d_solver* s) {
   s->since_check = 0;
   if (s->live.empty()) return OT2D_OK;
@@ -359,5 +395,41 @@ size_t ot2d_solver_device_bytes(const ot2d_solver* s) {
 size_t ot2d_instance_bytes(const ot2d_params* p, int32_t precision) { return p ? solve_bytes(*p, precision) : 0; }
 
 void* ot2d_solver_stream(ot2d_solver* s) { return s ? (void*)s->st : nullptr; }
+
+int ot2d_solver_profile(ot2d_solver* s, int32_t iters, double* ms, int32_t nphase) {
+  if (!s || !ms || iters < 1 || nphase < OT2D_NPHASE) return OT2D_ERR_ARG;
+  cudaSetDevice(s->device);
+  if (s->dirty) { int e = rebuild(s); if (e) return e; }
+  if (s->live.empty()) return OT2D_ERR_ARG;
+  return s->precision == OT2D_FP64 ? profile_t<double>(s, s->b64, iters, ms) : profile_t<float>(s, s->b32, iters, ms);
+}
+
+int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, double* const* q_host, int32_t iters) {
+  if (!s || n < 0 || (n && (!ids || !q_host)) || iters < 0) return OT2D_ERR_ARG;
+  cudaSetDevice(s->device);
+  if (s->dirty) { int e = rebuild(s); if (e) return e; }
+  std::vector<Rec*> rs;
+  for (int i = 0; i < n; ++i) {
+    auto it = s->recs.find(ids[i]);
+    if (it == s->recs.end() || !it->second.live) return OT2D_ERR_ARG;
+    rs.push_back(&it->second);
+  }
+  for (int it = 0; it < iters; ++it) {
+    for (int i = 0; i < n; ++i) {
+      const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
+      if (cudaMemcpyAsync(rs[i]->d.q64, q_host[i], bytes, cudaMemcpyHostToDevice, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+    }
+    if (s->precision == OT2D_FP32_MIXED && launch_shadow<float>(s->b32.d_sl, s->b32.b, s->st) != cudaSuccess)
+      return OT2D_ERR_CUDA;
+    if (cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+    for (int i = 0; i < n; ++i) {
+      const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
+      if (cudaMemcpyAsync(q_host[i], rs[i]->d.q64, bytes, cudaMemcpyDeviceToHost, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+    }
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+    if (++s->since_check >= s->check_every) { int e = check(s); if (e) return e; }
+  }
+  return OT2D_OK;
+}
 
 }  // extern "C"

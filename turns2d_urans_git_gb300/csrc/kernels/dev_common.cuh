@@ -30,6 +30,7 @@ struct Slice {
   const int32_t* iblank;
   const R* sn;                       // SA wall distance (static geometry)
   R* w;                              // scratch of this slice (phase dependent)
+  R* lurec;                          // LU-SGS sweep records (skewed bands)
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)
   double* red;                       // per-slice reduction output
   int32_t* ist;                      // per-slice counters: istep0, istep, status bits

@@ -2,18 +2,52 @@
 //
 // The reference sweeps i+j hyperplanes; cell (j,k) of the forward sweep
 // needs the already-updated s(j-1,k) and s(j,k-1) (backward: j+1, k+1).
-// Here one CTA owns one slice; warp w owns rows k = ks+32w .. ks+32w+31
-// (lane l -> one row) and all warps advance in a skewed lockstep: at global
-// step t lane l of warp w updates column j = js + t - 32w - l.  The (j-1,k)
-// contribution stays in the lane's registers, the (j,k-1) contribution
-// arrives from lane l-1 by __shfl_up_sync, and across warps through a
-// double-buffered shared-memory slot.  Every cell sees exactly the operands
-// of the reference's hyperplane order, so the result equals the sequential
-// sweep operation for operation.
+// GB300 design:
+//  1. k_lu_prep (fully parallel): every interior cell computes what the
+//     sweeps need from it -- its scaled residual, tscale/2, the diagonal d
+//     and the primitive / metric / spectral-radius factors of its outgoing
+//     contributions (lhs.f:524-563, :626-653) -- and stores them in a
+//     "skewed band" record: rows are grouped in bands of 32 (one warp, one
+//     row per lane) and the record of step t of a band holds, for every
+//     lane l, the cell at column t-l.  One wavefront step of a warp is then
+//     one contiguous chunk (24 fields x 32 lanes).
+//  2. k_lu_edges: point-Jacobi scaling of the halo residuals (lhs.f:567-598),
+//     their contributions to the first/last interior row and column, and
+//     (FP64) the reference's conservative->primitive->conservative round trip
+//     of q (lhs.f:524-531, :805-811).
+//  3. k_lu_sweep<FWD> (one CTA per slice, warp w = band w): the warps
+//     advance in a skewed lockstep; each warp streams its chunks into a
+//     shared-memory ring with cp.async.bulk (TMA) completing on mbarriers,
+//     the (j-1,k) contribution stays in registers, the (j,k-1) one arrives
+//     from the neighbouring lane by shuffle and across bands through a
+//     double-buffered shared slot.  Every cell sees exactly the operands of
+//     the reference's hyperplane order, so the sweep equals the sequential
+//     one operation for operation.
 #pragma once
 #include "dev_common.cuh"
 
 namespace ot2d {
+
+constexpr int LU_NF = 24;                 // fields per cell record
+constexpr int LU_CHUNK = LU_NF * 32;      // elements per (band, step) chunk
+
+// record fields
+enum {
+  LF_S = 0,    // 0..3: residual (forward input, then forward result)
+  LF_SV = 4, LF_D = 5, LF_UU = 6, LF_VV = 7, LF_UV2 = 8, LF_GE = 9,
+  LF_RI1 = 10, LF_RI2 = 11, LF_RK1 = 12, LF_RK2 = 13, LF_QX = 14, LF_QY = 15,
+  LF_FCX = 16, LF_FSX = 17, LF_FCY = 18, LF_FSY = 19,  // forward chk / spec (xi, eta)
+  LF_BCX = 20, LF_BSX = 21, LF_BCY = 22, LF_BSY = 23   // backward chk / spec
+};
+
+__host__ __device__ __forceinline__ int lu_nrow(int kd) { return kd - 2; }
+__host__ __device__ __forceinline__ int lu_ncol(int jd) { return jd - 2; }
+__host__ __device__ __forceinline__ int lu_nband(int kd) { return (kd - 2 + 31) / 32; }
+__host__ __device__ __forceinline__ int lu_nstep(int jd) { return jd - 2 + 31; }
+// elements of one slice's record: chunks + 4 halo-contribution arrays
+__host__ __device__ __forceinline__ int64_t lu_rec_elems(int jd, int kd) {
+  return (int64_t)lu_nband(kd) * lu_nstep(jd) * LU_CHUNK + 8 * (int64_t)(lu_nrow(kd) + lu_ncol(jd)) + 64;
+}
 
 template <class R>
 struct LuCell {
@@ -49,15 +83,13 @@ __device__ __forceinline__ LuCell<R> lu_cell(const Slice<R>& S, const ot2d_param
   return c;
 }
 
-// Contribution of cell c with correction s to its neighbour, lhs.f:626-653
-// (xi, forward), :656-683 (eta, forward), :725-752 / :755-782 (backward).
+// chk / spec of one direction (lhs.f:636-640, :667-671, :735-739, :765-769)
 template <class R, bool XI, bool FWD>
-__device__ __forceinline__ void lu_contrib(const LuCell<R>& c, const R* s, R gm1, R eps2, R* a) {
+__device__ __forceinline__ void lu_chkspec(const LuCell<R>& c, R eps2, R& chk, R& spec) {
   R ri1 = XI ? c.ri1 : c.rk1, ri2 = XI ? c.ri2 : c.rk2, qq = XI ? c.qx : c.qy, cc = XI ? c.cx : c.cy;
   R qqn = -ri1 * c.ugc - ri2 * c.vgc + qq;
   R sp1 = fabs(qqn) + cc;
   R sm2 = eps2 * sp1;
-  R chk, spec;
   if (FWD) {
     chk = (R)0.5 + fsign((R)0.5, qqn + cc);
     spec = XI ? chk * (qqn + sp1) + sm2 : chk * (qqn + sp1) + c.vn + sm2;
@@ -65,130 +97,270 @@ __device__ __forceinline__ void lu_contrib(const LuCell<R>& c, const R* s, R gm1
     chk = (R)0.5 - fsign((R)0.5, qqn - cc);
     spec = XI ? chk * (qqn - sp1) - sm2 : chk * (qqn - sp1) - c.vn - sm2;
   }
-  R s1 = s[0], s2 = s[1], s3 = s[2], s4 = s[3];
-  R a4 = chk * (ri1 * s2 + ri2 * s3 - qq * s1);
-  R a2 = chk * gm1 * (c.uv2 * s1 - (c.uu * s2 + c.vv * s3) + s4);
-  a[0] = a4 + spec * s1;
-  a[1] = ri1 * a2 + c.uu * a4 + spec * s2;
-  a[2] = ri2 * a2 + c.vv * a4 + spec * s3;
-  a[3] = qq * a2 + c.ge * a4 + spec * s4;
 }
 
-// Point-Jacobi scaling of the four halo edges (lhs.f:567-598); all threads
-// of the CTA.
+// contribution of a cell with correction s to its neighbour (lhs.f:643-653)
 template <class R>
-__device__ void lu_halo_scale(const Slice<R>& S, const ot2d_params& p, R epsv) {
-  const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
-  const int nk = ke - ks + 1, nj = je - js + 1;
-  const int tot = 2 * nk + 2 * nj;
-  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-    int j, k;
-    if (i < nk) { j = js - 1; k = ks + i; }
-    else if (i < 2 * nk) { j = je + 1; k = ks + i - nk; }
-    else if (i < 2 * nk + nj) { j = js + i - 2 * nk; k = ks - 1; }
-    else { j = js + i - 2 * nk - nj; k = ke + 1; }
-    LuCell<R> c = lu_cell(S, p, j, k, epsv);
-    const int64_t o = at(S.jd, j, k);
+__device__ __forceinline__ void lu_apply(R chk, R spec, R ri1, R ri2, R qq, R uu, R vv, R uv2, R ge, R gm1,
+                                         const R* s, R* a) {
+  R s1 = s[0], s2 = s[1], s3 = s[2], s4 = s[3];
+  R a4 = chk * (ri1 * s2 + ri2 * s3 - qq * s1);
+  R a2 = chk * gm1 * (uv2 * s1 - (uu * s2 + vv * s3) + s4);
+  a[0] = a4 + spec * s1;
+  a[1] = ri1 * a2 + uu * a4 + spec * s2;
+  a[2] = ri2 * a2 + vv * a4 + spec * s3;
+  a[3] = qq * a2 + ge * a4 + spec * s4;
+}
+
+template <class R, bool XI, bool FWD>
+__device__ __forceinline__ void lu_contrib(const LuCell<R>& c, const R* s, R gm1, R eps2, R* a) {
+  R chk, spec;
+  lu_chkspec<R, XI, FWD>(c, eps2, chk, spec);
+  lu_apply(chk, spec, XI ? c.ri1 : c.rk1, XI ? c.ri2 : c.rk2, XI ? c.qx : c.qy, c.uu, c.vv, c.uv2, c.ge, gm1, s, a);
+}
+
+// ---- kernel 1: records of the interior cells (one thread per (band, step, lane))
+template <class R>
+__device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_params& p, int band, int t, int l, int scale) {
+  const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nst = lu_nstep(S.jd);
+  const int r = 32 * band + l, c = t - l;
+  R* ch = S.lurec + ((int64_t)band * nst + t) * LU_CHUNK;
+  if (r >= nrow || c < 0 || c >= ncol) {
 #pragma unroll
-    for (int n = 0; n < 4; ++n) S.s[n * S.qs + o] = S.s[n * S.qs + o] * c.d;
+    for (int f = 0; f < LU_NF; ++f) ch[f * 32 + l] = (R)0;
+    return;
+  }
+  const int j = p.jbeg + c, k = p.kbeg + r;
+  const R eps2 = (R)(p.epse * 2.), epsv = (R)1. + eps2;
+  const int64_t o = at(S.jd, j, k);
+  LuCell<R> cl = lu_cell(S, p, j, k, epsv);
+  const R ts = S.tscale[o];
+#pragma unroll
+  for (int n = 0; n < 4; ++n) {
+    R v = S.s[n * S.qs + o];
+    ch[(LF_S + n) * 32 + l] = scale ? v * ts : v;
+  }
+  ch[LF_SV * 32 + l] = ts * (R)0.5;
+  ch[LF_D * 32 + l] = cl.d;
+  ch[LF_UU * 32 + l] = cl.uu; ch[LF_VV * 32 + l] = cl.vv; ch[LF_UV2 * 32 + l] = cl.uv2; ch[LF_GE * 32 + l] = cl.ge;
+  ch[LF_RI1 * 32 + l] = cl.ri1; ch[LF_RI2 * 32 + l] = cl.ri2; ch[LF_RK1 * 32 + l] = cl.rk1; ch[LF_RK2 * 32 + l] = cl.rk2;
+  ch[LF_QX * 32 + l] = cl.qx; ch[LF_QY * 32 + l] = cl.qy;
+  R a, b;
+  lu_chkspec<R, true, true>(cl, eps2, a, b);   ch[LF_FCX * 32 + l] = a; ch[LF_FSX * 32 + l] = b;
+  lu_chkspec<R, false, true>(cl, eps2, a, b);  ch[LF_FCY * 32 + l] = a; ch[LF_FSY * 32 + l] = b;
+  lu_chkspec<R, true, false>(cl, eps2, a, b);  ch[LF_BCX * 32 + l] = a; ch[LF_BSX * 32 + l] = b;
+  lu_chkspec<R, false, false>(cl, eps2, a, b); ch[LF_BCY * 32 + l] = a; ch[LF_BSY * 32 + l] = b;
+}
+
+// halo-contribution arrays after the chunks: A forward [nrow][4], A backward,
+// B forward [ncol][4], B backward
+template <class R>
+__device__ __forceinline__ R* lu_halo(const Slice<R>& S, int which) {
+  const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd);
+  R* base = S.lurec + (int64_t)lu_nband(S.kd) * lu_nstep(S.jd) * LU_CHUNK;
+  switch (which) {
+    case 0: return base;
+    case 1: return base + 4 * nrow;
+    case 2: return base + 8 * nrow;
+    default: return base + 8 * nrow + 4 * ncol;
   }
 }
 
-// One sweep of one slice.  FWD: lhs.f:611-714, else :716-800.
-template <class R, bool FWD>
-__device__ void lu_sweep(const Slice<R>& S, R (*xbuf)[4]) {
-  const ot2d_params& p = *S.P;
+// ---- kernel 2: halo edges (one thread per cell of the slice)
+template <class R>
+__device__ __forceinline__ void lu_edge_cell(const Slice<R>& S, const ot2d_params& p, int j, int k, int scale) {
   const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
-  const int ncol = je - js + 1, nrow = ke - ks + 1;
-  const int nw = (nrow + 31) >> 5;
+  const bool ij = j >= js && j <= je, ik = k >= ks && k <= ke;
+  const int64_t o = at(S.jd, j, k);
   const R eps2 = (R)(p.epse * 2.), epsv = (R)1. + eps2, gm1 = (R)p.gm1;
+  if (!(ij && ik)) {
+    R sv[4];
+    const R ts = S.tscale[o];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) sv[n] = scale ? S.s[n * S.qs + o] * ts : S.s[n * S.qs + o];
+    const bool edge = (ik && (j == js - 1 || j == je + 1)) || (ij && (k == ks - 1 || k == ke + 1));
+    if (edge) {
+      LuCell<R> c = lu_cell(S, p, j, k, epsv);
+#pragma unroll
+      for (int n = 0; n < 4; ++n) sv[n] = sv[n] * c.d;
+      R a[4];
+      R* dst = nullptr;
+      if (j == js - 1) { lu_contrib<R, true, true>(c, sv, gm1, eps2, a); dst = lu_halo(S, 0) + 4 * (k - ks); }
+      else if (j == je + 1) { lu_contrib<R, true, false>(c, sv, gm1, eps2, a); dst = lu_halo(S, 1) + 4 * (k - ks); }
+      else if (k == ks - 1) { lu_contrib<R, false, true>(c, sv, gm1, eps2, a); dst = lu_halo(S, 2) + 4 * (j - js); }
+      else { lu_contrib<R, false, false>(c, sv, gm1, eps2, a); dst = lu_halo(S, 3) + 4 * (j - js); }
+#pragma unroll
+      for (int n = 0; n < 4; ++n) dst[n] = a[n];
+    }
+#pragma unroll
+    for (int n = 0; n < 4; ++n) S.s[n * S.qs + o] = sv[n];
+  }
+  // FP64 plain path: q leaves ilu2d round-tripped (lhs.f:524-531, :805-811)
+  if constexpr (sizeof(R) == sizeof(double)) {
+    const int64_t qs = S.qs;
+    double q1 = S.q[o], J = S.q[(p.nq - 1) * qs + o];
+    double dj = 1.0 / q1;
+    double u = S.q[qs + o] * dj, v = S.q[2 * qs + o] * dj, e = S.q[3 * qs + o] * dj;
+    double q1n = (q1 * J) / J;
+    S.q[o] = q1n;
+    S.q[qs + o] = u * q1n;
+    S.q[2 * qs + o] = v * q1n;
+    S.q[3 * qs + o] = e * q1n;
+  }
+}
+
+// ---- kernel 3: the sweeps --------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Bounded wait on a ring slot; false after ~2^22 polls (the status word of
+// the slice records the timeout).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 22); ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Shared memory of the sweep kernel: nwarp rings of dq chunks, then the
+// barriers, then the cross-band slots.
+template <class R>
+__host__ __device__ __forceinline__ size_t lu_smem_bytes(int nwarp, int dq) {
+  return (size_t)nwarp * dq * LU_CHUNK * sizeof(R) + (size_t)nwarp * dq * sizeof(uint64_t) + (size_t)nwarp * 2 * 4 * sizeof(R);
+}
+
+template <class R, bool FWD>
+__device__ void lu_sweep_slice(const Slice<R>& S, int dq, int nwarp, unsigned char* smem) {
+  const ot2d_params& p = *S.P;
+  const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nb = lu_nband(S.kd), nst = lu_nstep(S.jd);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  const int r = 32 * w + l;                       // row offset from the sweep start
-  const bool rowok = (w < nw) && (r < nrow);
-  const int k = FWD ? ks + r : ke - r;
-  const int T = ncol + 31 + 32 * (nw - 1);
-  R aprev[4] = {0, 0, 0, 0};                      // contribution of (j-+1, k) for this lane
-  R bout[4] = {0, 0, 0, 0};                       // this lane's last contribution to row k+-1
-  const int64_t qs = S.qs;
+  const R gm1 = (R)p.gm1;
+  R* rings = (R*)smem;
+  uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * dq * LU_CHUNK * sizeof(R));
+  R* xb = (R*)(bars + (size_t)nwarp * dq);           // [nwarp][2][4]
+  R* ring = rings + (size_t)w * dq * LU_CHUNK;
+  uint64_t* bar = bars + (size_t)w * dq;
+  const bool wok = w < nb;
+  R* rec = S.lurec + (int64_t)w * nst * LU_CHUNK;
+  const uint32_t cbytes = LU_CHUNK * sizeof(R);
+  auto chunk_of = [&](int tl) -> int { return FWD ? tl : nst - 1 - tl; };
+  if (wok && l == 0)
+    for (int s = 0; s < dq; ++s) mbar_init(&bar[s], 1);
+  __syncthreads();
+  if (wok && l == 0) {
+    fence_proxy_async_smem();
+    for (int s = 0; s < dq && s < nst; ++s) {
+      mbar_expect_tx(&bar[s], cbytes);
+      bulk_g2s(ring + (size_t)s * LU_CHUNK, rec + (int64_t)chunk_of(s) * LU_CHUNK, cbytes, &bar[s]);
+    }
+  }
+  const R* Ah = lu_halo(S, FWD ? 0 : 1);
+  const R* Bh = lu_halo(S, FWD ? 2 : 3);
+  const int off = FWD ? 32 * w : 32 * (nb - 1 - w);
+  const int T = nst + 32 * (nb - 1);
+  const int r = 32 * w + l;
+  R aprev[4] = {0, 0, 0, 0}, bout[4] = {0, 0, 0, 0};
+  bool failed = false;
+  int tfail = 0;
   for (int t = 0; t < T; ++t) {
-    // contribution from the row below (FWD) / above, computed one step ago
     R bin[4];
 #pragma unroll
-    for (int n = 0; n < 4; ++n) bin[n] = __shfl_up_sync(0xffffffffu, bout[n], 1);
-    const int tl = t - 32 * w;
-    const int jo = tl - l;                        // column offset from the sweep start
-    const bool act = rowok && jo >= 0 && jo < ncol;
-    if (act) {
-      const int j = FWD ? js + jo : je - jo;
-      if (l == 0) {
-        if (w == 0) {
-          // neighbour is the halo row ks-1 (FWD) / ke+1 (backward)
-          const int kh = FWD ? ks - 1 : ke + 1;
-          LuCell<R> hc = lu_cell(S, p, j, kh, epsv);
-          R sh[4];
-          const int64_t oh = at(S.jd, j, kh);
+    for (int n = 0; n < 4; ++n)
+      bin[n] = FWD ? __shfl_up_sync(0xffffffffu, bout[n], 1) : __shfl_down_sync(0xffffffffu, bout[n], 1);
+    const int tl = t - off;
+    const bool wact = wok && tl >= 0 && tl < nst && !failed;  // warp-uniform
+    if (wact) {
+      const int slot = tl % dq;
+      const bool ok = mbar_wait_bounded(&bar[slot], (uint32_t)((tl / dq) & 1));
+      if (__any_sync(0xffffffffu, !ok)) { failed = true; tfail = tl; }
+      const R* ch = ring + (size_t)slot * LU_CHUNK;
+      const int c = FWD ? tl - l : ncol - 1 - (tl - (31 - l));
+      const bool act = !failed && r < nrow && c >= 0 && c < ncol;
+      if (act) {
+        if (FWD ? c == 0 : c == ncol - 1) {
 #pragma unroll
-          for (int n = 0; n < 4; ++n) sh[n] = S.s[n * qs + oh];
-          lu_contrib<R, false, FWD>(hc, sh, gm1, eps2, bin);
+          for (int n = 0; n < 4; ++n) aprev[n] = Ah[4 * r + n];
+        }
+        if (FWD) {
+          if (l == 0) {
+            if (w == 0) {
+#pragma unroll
+              for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
+            } else {
+#pragma unroll
+              for (int n = 0; n < 4; ++n) bin[n] = xb[((w - 1) * 2 + ((t - 1) & 1)) * 4 + n];
+            }
+          }
         } else {
+          if (r == nrow - 1) {
 #pragma unroll
-          for (int n = 0; n < 4; ++n) bin[n] = xbuf[2 * (w - 1) + ((t - 1) & 1)][n];
+            for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
+          } else if (l == 31) {
+#pragma unroll
+            for (int n = 0; n < 4; ++n) bin[n] = xb[((w + 1) * 2 + ((t - 1) & 1)) * 4 + n];
+          }
+        }
+        const R sv = ch[LF_SV * 32 + l], di = ch[LF_D * 32 + l];
+        R sn[4];
+#pragma unroll
+        for (int n = 0; n < 4; ++n) {
+          const R st = ch[(LF_S + n) * 32 + l];
+          sn[n] = FWD ? (st + sv * (aprev[n] + bin[n])) * di : st - sv * (aprev[n] + bin[n]) * di;
+        }
+        if (FWD) {
+          R* g = rec + (int64_t)chunk_of(tl) * LU_CHUNK;
+#pragma unroll
+          for (int n = 0; n < 4; ++n) g[(LF_S + n) * 32 + l] = sn[n];
+        } else {
+          const int64_t o = at(S.jd, p.jbeg + c, p.kbeg + r);
+#pragma unroll
+          for (int n = 0; n < 4; ++n) S.s[n * S.qs + o] = sn[n];
+        }
+        const R uu = ch[LF_UU * 32 + l], vv = ch[LF_VV * 32 + l], uv2 = ch[LF_UV2 * 32 + l], ge = ch[LF_GE * 32 + l];
+        lu_apply(ch[(FWD ? LF_FCX : LF_BCX) * 32 + l], ch[(FWD ? LF_FSX : LF_BSX) * 32 + l], ch[LF_RI1 * 32 + l],
+                 ch[LF_RI2 * 32 + l], ch[LF_QX * 32 + l], uu, vv, uv2, ge, gm1, sn, aprev);
+        lu_apply(ch[(FWD ? LF_FCY : LF_BCY) * 32 + l], ch[(FWD ? LF_FSY : LF_BSY) * 32 + l], ch[LF_RK1 * 32 + l],
+                 ch[LF_RK2 * 32 + l], ch[LF_QY * 32 + l], uu, vv, uv2, ge, gm1, sn, bout);
+        if (FWD ? (l == 31 && w + 1 < nb) : (l == 0 && w > 0)) {
+#pragma unroll
+          for (int n = 0; n < 4; ++n) xb[(w * 2 + (t & 1)) * 4 + n] = bout[n];
         }
       }
-      if (jo == 0) {
-        const int jh = FWD ? js - 1 : je + 1;
-        LuCell<R> hc = lu_cell(S, p, jh, k, epsv);
-        R sh[4];
-        const int64_t oh = at(S.jd, jh, k);
-#pragma unroll
-        for (int n = 0; n < 4; ++n) sh[n] = S.s[n * qs + oh];
-        lu_contrib<R, true, FWD>(hc, sh, gm1, eps2, aprev);
-      }
-      LuCell<R> c = lu_cell(S, p, j, k, epsv);
-      const int64_t o = at(S.jd, j, k);
-      const R sv = S.tscale[o] * (R)0.5, di = c.d;
-      R sn[4];
-#pragma unroll
-      for (int n = 0; n < 4; ++n) {
-        R st = S.s[n * qs + o];
-        sn[n] = FWD ? (st + sv * (aprev[n] + bin[n])) * di : st - sv * (aprev[n] + bin[n]) * di;
-        S.s[n * qs + o] = sn[n];
-      }
-      lu_contrib<R, true, FWD>(c, sn, gm1, eps2, aprev);
-      lu_contrib<R, false, FWD>(c, sn, gm1, eps2, bout);
-      if (l == 31 && w + 1 < nw) {
-#pragma unroll
-        for (int n = 0; n < 4; ++n) xbuf[2 * w + (t & 1)][n] = bout[n];
+      __syncwarp();
+      if (l == 0 && !failed && tl + dq < nst) {
+        fence_proxy_async_smem();
+        mbar_expect_tx(&bar[slot], cbytes);
+        bulk_g2s(ring + (size_t)slot * LU_CHUNK, rec + (int64_t)chunk_of(tl + dq) * LU_CHUNK, cbytes, &bar[slot]);
       }
     }
     __syncthreads();
   }
-}
-
-// FP64 plain path: the reference leaves q round-tripped through
-// (rho*J, u, v, e) and back (lhs.f:524-531, :805-811); reproduce it.
-template <class R>
-__device__ void lu_roundtrip(const Slice<R>& S, const ot2d_params& p) {
-  if constexpr (sizeof(R) != sizeof(double)) {
-    return;
-  } else {
-    const int jd = p.jd, kd = p.kd; const int64_t qs = S.qs;
-    const int js = p.jbeg - 1, je = p.jend + 1, ks = p.kbeg - 1, ke = p.kend + 1;
-    const int nj = je - js + 1, tot = nj * (ke - ks + 1);
-    (void)jd; (void)kd;
-    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      int j = js + i % nj, k = ks + i / nj;
-      const int64_t o = at(S.jd, j, k);
-      double q1 = S.q[o], J = S.q[(p.nq - 1) * qs + o];
-      double dj = 1.0 / q1;
-      double u = S.q[qs + o] * dj, v = S.q[2 * qs + o] * dj, e = S.q[3 * qs + o] * dj;
-      double r = q1 * J;
-      double q1n = r / J;
-      S.q[o] = q1n;
-      S.q[qs + o] = u * q1n;
-      S.q[2 * qs + o] = v * q1n;
-      S.q[3 * qs + o] = e * q1n;
-    }
+  if (failed && l == 0) {
+    // copies for steps tfail .. tfail+dq-1 were issued and not consumed:
+    // wait (bounded) for them before the CTA's shared memory goes away,
+    // then flag the slice
+    for (int u = tfail; u < tfail + dq && u < nst; ++u) mbar_wait_bounded(&bar[u % dq], (uint32_t)((u / dq) & 1));
+    if (S.ist) atomicOr(&S.ist[2], 4);
   }
 }
 

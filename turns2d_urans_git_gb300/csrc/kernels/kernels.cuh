@@ -157,27 +157,33 @@ __global__ void k_rbc(const Slice<R>* __restrict__ sl) {
   rbc_slice(S);
 }
 
-// s *= tscale on all cells (step.f:141-148), then ilu2d (lhs.f:470-814)
+// ilu2d (lhs.f:470-814), preceded by s *= tscale on all cells when `scale`
+// (step.f:141-148).  Records of the interior cells; one thread per
+// (band, step, lane) of every slice (prefix table lfirst).
 template <class R>
-__global__ void k_lusgs(const Slice<R>* __restrict__ sl, int scale) {
-  __shared__ R xbuf[64][4];
-  const Slice<R>& S = sl[blockIdx.x];
-  const ot2d_params& p = *S.P;
-  const int64_t n2 = (int64_t)S.jd * S.kd;
-  for (int64_t i = threadIdx.x; scale && i < n2; i += blockDim.x) {
-    R t = S.tscale[i];
-#pragma unroll
-    for (int n = 0; n < 4; ++n) S.s[n * S.qs + i] = S.s[n * S.qs + i] * t;
-  }
-  __syncthreads();
-  const R eps2 = (R)(p.epse * 2.), epsv = (R)1. + eps2;
-  lu_halo_scale(S, p, epsv);
-  __syncthreads();
-  lu_sweep<R, true>(S, xbuf);
-  __syncthreads();
-  lu_sweep<R, false>(S, xbuf);
-  __syncthreads();
-  lu_roundtrip(S, p);
+__global__ void __launch_bounds__(CELL_BS) k_lu_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst,
+                                                     int nslice, int scale) {
+  const int si = find_slice(lfirst, nslice, blockIdx.x);
+  const Slice<R>& S = sl[si];
+  const int g = (blockIdx.x - lfirst[si]) * blockDim.x + threadIdx.x;
+  const int nst = lu_nstep(S.jd), nb = lu_nband(S.kd);
+  const int l = g & 31, t = (g >> 5) % nst, band = (g >> 5) / nst;
+  if (band >= nb) return;
+  lu_prep_cell(S, *S.P, band, t, l, scale);
+}
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_lu_edges(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                      int nslice, int scale) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  lu_edge_cell(S, *S.P, j, k, scale);
+}
+
+template <class R, bool FWD>
+__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int dq) {
+  extern __shared__ __align__(128) unsigned char lu_smem[];
+  lu_sweep_slice<R, FWD>(sl[blockIdx.x], dq, blockDim.x >> 5, lu_smem);
 }
 
 template <class R>
@@ -247,6 +253,21 @@ __global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__
     double v = S.q64[n * S.qs + o] + (double)S.s[n * S.qs + o] * m;
     S.q64[n * S.qs + o] = v;
     if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = (R)v;
+  }
+}
+
+// compute copy of the whole state from the FP64 master (after the host
+// replaced q64); a no-op on the plain FP64 path where they are one array
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_shadow(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                    int nslice) {
+  if constexpr (sizeof(R) == sizeof(double)) {
+    return;
+  } else {
+    OT2D_CELL_MAP();
+    if (!inside) return;
+    const int64_t o = at(S.jd, j, k);
+    for (int n = 0; n < S.P->nq; ++n) S.q[n * S.qs + o] = (R)S.q64[n * S.qs + o];
   }
 }
 

@@ -20,6 +20,8 @@ struct Batch {
   const int32_t* d_first = nullptr;   // [nslice+1] first cell block of each slice
   const int32_t* d_jfirst = nullptr;  // [nslice+1] first k-line (lsolvej) of each slice
   const int32_t* d_kfirst = nullptr;  // [nslice+1] first j-line (lsolvek) of each slice
+  const int32_t* d_lfirst = nullptr;  // [nslice+1] first LU-SGS record block of each slice
+  int lu_blocks = 0;                  // blocks of the LU-SGS record kernel
   NormPart* d_part = nullptr;         // [cell_blocks] norm partials
 };
 
@@ -43,6 +45,8 @@ template <class R> cudaError_t launch_assemble(const Slice<R>* d_sl, const Batch
 template <class R> cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_monitor(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+// refresh the compute copy of q from q64 on every cell (mixed path)
+template <class R> cudaError_t launch_shadow(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R>
 cudaError_t launch_forces(const Slice<R>* d_sl, const Batch& b, const double* const* d_xv, const double* const* d_yv,
                           double* d_out, cudaStream_t st);

@@ -42,7 +42,21 @@ cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
 }
 template <class R>
 cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st) {
-  k_lusgs<R><<<b.nslice, 32 * b.max_lu_warps, 0, st>>>(d_sl, scale);
+  k_lu_prep<R><<<b.lu_blocks, CELL_BS, 0, st>>>(d_sl, b.d_lfirst, b.nslice, scale);
+  k_lu_edges<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale);
+  const int nw = b.max_lu_warps;
+  // ring depth: as deep as ~200 KB of shared memory allows (2..8 chunks)
+  int dq = 8;
+  while (dq > 2 && lu_smem_bytes<R>(nw, dq) > 200 * 1024) --dq;
+  const size_t smem = lu_smem_bytes<R>(nw, dq);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_lu_sweep<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_lu_sweep<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  k_lu_sweep<R, true><<<b.nslice, 32 * nw, smem, st>>>(d_sl, dq);
+  k_lu_sweep<R, false><<<b.nslice, 32 * nw, smem, st>>>(d_sl, dq);
   return cudaGetLastError();
 }
 template <class R>
@@ -58,6 +72,11 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
 template <class R>
 cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_update<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_shadow(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  if (sizeof(R) != sizeof(double)) k_shadow<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
 }
 template <class R>
@@ -97,6 +116,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   template cudaError_t launch_sa<R>(const Slice<R>*, const Batch&, cudaStream_t);                       \
   template cudaError_t launch_update<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
   template cudaError_t launch_monitor<R>(const Slice<R>*, const Batch&, cudaStream_t);                  \
+  template cudaError_t launch_shadow<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
   template cudaError_t launch_forces<R>(const Slice<R>*, const Batch&, const double* const*,            \
                                         const double* const*, double*, cudaStream_t);
 
