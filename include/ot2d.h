@@ -153,9 +153,9 @@ int ot2d_solver_sync(ot2d_solver* s);
 void* ot2d_solver_stream(ot2d_solver* s);
 /* Phase timers: runs `iters` iterations phase by phase with CUDA events
  * between the kernel families and returns the mean milliseconds per phase:
- * 0 time_step, 1 bc, 2 inviscid faces, 3 viscous faces, 4 assembly + norms,
- * 5 rbc, 6 LU-SGS, 7 SA, 8 update + monitor. */
-#define OT2D_NPHASE 9
+ * 0 time_step, 1 bc, 2 residual (inviscid + viscous fluxes, assembly and
+ * norms in one tiled kernel), 3 rbc, 4 LU-SGS, 5 SA, 6 update + monitor. */
+#define OT2D_NPHASE 7
 int ot2d_solver_profile(ot2d_solver* s, int32_t iters, double* ms, int32_t nphase);
 /* Host-resident state, as a Fortran caller that owns q: every iteration
  * copies q(jd,kd,nspec,nq) of the listed live instances host->device, runs

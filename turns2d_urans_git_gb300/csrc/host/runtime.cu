@@ -257,30 +257,36 @@ template Slice<float> make_slice<float>(const DevSolve&, int, double*, int32_t*)
 template <class R>
 int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   const int n = (int)sl.size();
-  // four prefix tables of n+1 entries: cell blocks, k-lines, j-lines, LU record blocks
-  std::vector<int32_t> idx(4 * (n + 1));
-  int cells = 0, jl = 0, kl = 0, lub = 0, maxw = 1, maxwall = 1;
+  // six prefix tables of n+1 entries: cell blocks, k-lines, j-lines, LU
+  // record blocks, 32-line groups, residual tiles
+  std::vector<int32_t> idx(6 * (n + 1));
+  int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1;
   for (int i = 0; i < n; ++i) {
     idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl; idx[3 * (n + 1) + i] = lub;
+    idx[4 * (n + 1) + i] = grp; idx[5 * (n + 1) + i] = tiles;
     const int jd = sl[i].jd, kd = sl[i].kd;
     cells += (jd * kd + CELL_BS - 1) / CELL_BS;
     jl += kd - 2;   // k-lines solved along j
     kl += jd - 2;   // j-lines solved along k
     lub += (lu_nband(kd) * lu_nstep(jd) * 32 + CELL_BS - 1) / CELL_BS;
+    grp += lu_nband(kd);
+    tiles += ((jd - 2 + RT_TJ - 1) / RT_TJ) * ((kd - 2 + RT_TK - 1) / RT_TK);
     maxw = std::max(maxw, lu_nband(kd));
     maxwall = std::max(maxwall, jd);
   }
   idx[n] = cells; idx[2 * (n + 1) - 1] = jl; idx[3 * (n + 1) - 1] = kl; idx[4 * (n + 1) - 1] = lub;
+  idx[5 * (n + 1) - 1] = grp; idx[6 * (n + 1) - 1] = tiles;
   if ((size_t)n > cap_sl) {
     if (d_sl) cudaFree(d_sl);
     if (d_idx) cudaFree(d_idx);
     cap_sl = std::max((size_t)n, (size_t)2 * cap_sl);
     if (cudaMalloc(&d_sl, cap_sl * sizeof(Slice<R>)) != cudaSuccess) return OT2D_ERR_NOMEM;
-    if (cudaMalloc(&d_idx, 4 * (cap_sl + 1) * sizeof(int32_t)) != cudaSuccess) return OT2D_ERR_NOMEM;
+    if (cudaMalloc(&d_idx, 6 * (cap_sl + 1) * sizeof(int32_t)) != cudaSuccess) return OT2D_ERR_NOMEM;
   }
-  if ((size_t)cells > cap_part) {
+  const size_t nparts = (size_t)std::max(cells, tiles);
+  if (nparts > cap_part) {
     if (d_part) cudaFree(d_part);
-    cap_part = std::max((size_t)cells, (size_t)2 * cap_part);
+    cap_part = std::max(nparts, (size_t)2 * cap_part);
     if (cudaMalloc(&d_part, cap_part * sizeof(NormPart)) != cudaSuccess) return OT2D_ERR_NOMEM;
   }
   if (cudaMemcpyAsync(d_sl, sl.data(), n * sizeof(Slice<R>), cudaMemcpyHostToDevice, st) != cudaSuccess) return OT2D_ERR_CUDA;
@@ -293,6 +299,10 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   b.max_wall = maxwall;
   b.jlines = jl; b.klines = kl;
   b.lu_blocks = lub;
+  b.jgroups = grp;
+  b.d_gfirst = d_idx + 4 * (n + 1);
+  b.d_tfirst = d_idx + 5 * (n + 1);
+  b.tile_blocks = tiles;
   b.d_first = d_idx; b.d_jfirst = d_idx + (n + 1); b.d_kfirst = d_idx + 2 * (n + 1); b.d_lfirst = d_idx + 3 * (n + 1);
   b.d_part = d_part;
   return OT2D_OK;

@@ -202,15 +202,13 @@ int profile_t(ot2d_solver* s, DevBatch<R>& B, int iters, double* ms) {
     rec(0);
     e = launch_time_step<R>(B.d_sl, B.b, s->st); rec(1);
     if (!e) e = launch_bc<R>(B.d_sl, B.b, 1, s->st); rec(2);
-    if (!e) e = launch_faces<R>(B.d_sl, B.b, 1, 0, s->st); rec(3);
-    if (!e) e = launch_faces<R>(B.d_sl, B.b, 0, visc, s->st); rec(4);
-    if (!e) e = launch_assemble<R>(B.d_sl, B.b, AS_INV | AS_TS | AS_NORM | (visc ? AS_VISC : 0), s->st); rec(5);
-    if (!e) e = launch_rbc<R>(B.d_sl, B.b, s->st); rec(6);
-    if (!e) e = launch_lusgs<R>(B.d_sl, B.b, 1, s->st); rec(7);
-    if (!e && turb) e = launch_sa<R>(B.d_sl, B.b, s->st); rec(8);
+    if (!e) e = launch_residual<R>(B.d_sl, B.b, visc, s->st); rec(3);
+    if (!e) e = launch_rbc<R>(B.d_sl, B.b, s->st); rec(4);
+    if (!e) e = launch_lusgs<R>(B.d_sl, B.b, 1, s->st); rec(5);
+    if (!e && turb) e = launch_sa<R>(B.d_sl, B.b, s->st); rec(6);
     if (!e) e = launch_update<R>(B.d_sl, B.b, s->st);
-    if (!e) e = launch_monitor<R>(B.d_sl, B.b, s->st); rec(9);
-    if (e != cudaSuccess || cudaEventSynchronize(ev[9]) != cudaSuccess) { err = OT2D_ERR_CUDA; break; }
+    rec(7);
+    if (e != cudaSuccess || cudaEventSynchronize(ev[7]) != cudaSuccess) { err = OT2D_ERR_CUDA; break; }
     for (int p = 0; p < OT2D_NPHASE; ++p) {
       float t = 0.f;
       cudaEventElapsedTime(&t, ev[p], ev[p + 1]);

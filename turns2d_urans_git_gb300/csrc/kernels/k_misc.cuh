@@ -40,6 +40,19 @@ __device__ __forceinline__ NormPart norm_combine(NormPart a, NormPart b) {
   return r;
 }
 
+// fixed shuffle tree over the 32 lanes of a warp; lane 0 gets the result
+__device__ __forceinline__ NormPart warp_norm_reduce(NormPart a) {
+  for (int off = 16; off > 0; off >>= 1) {
+    NormPart o;
+    o.rsum = __shfl_down_sync(0xffffffffu, a.rsum, off);
+    o.resrho = __shfl_down_sync(0xffffffffu, a.resrho, off);
+    o.resmax = __shfl_down_sync(0xffffffffu, a.resmax, off);
+    o.key = __shfl_down_sync(0xffffffffu, a.key, off);
+    if ((threadIdx.x & 31) < off) a = norm_combine(a, o);
+  }
+  return a;
+}
+
 // Wall force integrands of one wall cell (forces.f:168-205, :269-379)
 struct ForceCell { double zz, sxx, syy; };
 

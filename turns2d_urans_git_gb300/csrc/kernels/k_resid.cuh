@@ -1,0 +1,412 @@
+// k_resid.cuh -- the fused residual: rhsup (src/eulerrhs.f:2-280) +
+// visrhs (src/visrhs.f:2-287) + timespectralrhs (src/sources.f:2-27) + the
+// L2 / max norms of step.f:58-93, one CTA per tile of RT_TJ x RT_TK
+// interior cells.
+//
+// A tile stages its cells plus a 3-cell halo in shared memory once
+// (primitive variables, viscous cell factors, metrics), computes every
+// inviscid and viscous face flux of the tile exactly once, and assembles the
+// residual in the reference's accumulation order.  Per face and per cell the
+// arithmetic is the same as the reference's, so the FP64 path reproduces the
+// oracle bit for bit.
+#pragma once
+#include "dev_common.cuh"
+#include "k_rhs.cuh"
+#include "k_misc.cuh"
+#include "launch.h"
+
+namespace ot2d {
+
+constexpr int RT_H = 3;   // staged halo width (tile size RT_TJ x RT_TK: launch.h)
+constexpr int RT_RW = RT_TJ + 2 * RT_H, RT_RH = RT_TK + 2 * RT_H;   // staged region
+constexpr int RT_NR = RT_RW * RT_RH;
+constexpr int RT_BS = 256;
+// staged per-cell arrays
+enum { RS_RHO = 0, RS_U, RS_V, RS_P, RS_E, RS_VNU, RS_GKAP, RS_RJ, RS_UD, RS_VD, RS_ED, RS_XX, RS_XY, RS_YX, RS_YY, RS_N };
+// face arrays
+constexpr int RT_NF = 4 * RT_TK * (RT_TJ + 1);             // F: xi faces j0-1..j1, rows k0..k1
+constexpr int RT_NG = 4 * (RT_TK + 1) * RT_TJ;             // G: eta faces k0-1..k1, columns j0..j1
+constexpr int RT_VEH = RT_TK + 3, RT_VXW = RT_TJ + 3;
+constexpr int RT_NVE = 6 * RT_VEH * RT_TJ;                 // eta viscous, k0-2..k1+1
+constexpr int RT_NVX = 6 * RT_TK * RT_VXW;                 // xi viscous, j0-2..j1+1
+
+template <class R>
+__host__ __device__ constexpr size_t rt_smem_bytes() {
+  return ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) + sizeof(int) * RT_NR + 15) / 16) *
+             16 +
+         sizeof(NormPart) * RT_BS;
+}
+
+template <class R>
+struct RtSmem {
+  R* c;          // [RS_N][RT_NR]
+  R *F, *G, *VE, *VX;
+  int* iba;      // [RT_NR]
+  NormPart* red; // [RT_BS]
+  __device__ RtSmem(unsigned char* base) {
+    c = (R*)base;
+    F = c + (size_t)RS_N * RT_NR;
+    G = F + RT_NF;
+    VE = G + RT_NG;
+    VX = VE + RT_NVE;
+    iba = (int*)(VX + RT_NVX);
+    red = (NormPart*)(base + ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) +
+                               sizeof(int) * RT_NR + 15) / 16) * 16);
+  }
+  __device__ __forceinline__ R& at(int a, int r) const { return c[(size_t)a * RT_NR + r]; }
+};
+
+// Stage A: cell (j,k) of the staged region -> primitive f of rhsup
+// (eulerrhs.f:55-61, :71-79), viscous cell factors of visrhs
+// (visrhs.f:48-60), the q2/q1-style divided velocities of its cross terms
+// (visrhs.f:77-89), metrics and |iblank|.
+template <class R>
+__device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_params& p, const RtSmem<R>& sm, int r,
+                                              int j, int k, bool visc) {
+  const int64_t o = at(S.jd, j, k), qs = S.qs;
+  const R q1 = S.q[o], q2 = S.q[qs + o], q3 = S.q[2 * qs + o], q4 = S.q[3 * qs + o], J = S.q[(p.nq - 1) * qs + o];
+  const R gm1 = (R)p.gm1;
+  const R rhoi = (R)1.0 / q1;
+  sm.at(RS_RHO, r) = q1 * J;
+  const R u = q2 * rhoi, v = q3 * rhoi;
+  sm.at(RS_U, r) = u;
+  sm.at(RS_V, r) = v;
+  const R ppp = gm1 * (q4 - (R)0.5 * (sq(q2) + sq(q3)) / q1);
+  sm.at(RS_P, r) = ppp * J;
+  if (visc) {
+    const R c2b = (R)(198.6 / p.tinf), c2bp = c2b + (R)1., prtr = (R)(p.pr / 0.9);
+    const R e = q4 * rhoi - (R).5 * (sq(u) + sq(v));
+    const R tt = (R)p.ggm1 * e;
+    const R vmue = c2bp * tt * sqrt(tt) / (c2b + tt);
+    const R turm = S.turmu[o];
+    sm.at(RS_E, r) = e;
+    sm.at(RS_VNU, r) = vmue + turm;
+    sm.at(RS_GKAP, r) = vmue + prtr * turm;
+    sm.at(RS_RJ, r) = (R)1. / J;
+    const R ud = q2 / q1, vd = q3 / q1;
+    sm.at(RS_UD, r) = ud;
+    sm.at(RS_VD, r) = vd;
+    sm.at(RS_ED, r) = q4 / q1 - (R).5 * (sq(ud) + sq(vd));
+    sm.at(RS_XX, r) = S.xx[o]; sm.at(RS_XY, r) = S.xy[o]; sm.at(RS_YX, r) = S.yx[o]; sm.at(RS_YY, r) = S.yy[o];
+  }
+  const int ib = S.iblank[o];
+  sm.iba[r] = ib < 0 ? -ib : ib;
+}
+
+// A grid line read from the staged region: line position c sits at region
+// index o0 + c*stride; positions outside [lo, hi] were not staged (and are
+// never read by the reconstruction that uses them).
+template <class R>
+struct RtLine {
+  const RtSmem<R>* sm; int o0, stride, lo, hi; R gm1;
+  __device__ __forceinline__ void f4(int c, R* out) const {
+    if (c < lo || c > hi) { out[0] = out[1] = out[2] = out[3] = (R)0; return; }
+    const int r = o0 + c * stride;
+    out[0] = sm->at(RS_RHO, r); out[1] = sm->at(RS_U, r); out[2] = sm->at(RS_V, r); out[3] = sm->at(RS_P, r);
+  }
+  __device__ __forceinline__ int iba(int c) const { return (c < lo || c > hi) ? 0 : sm->iba[o0 + c * stride]; }
+};
+
+// eta-direction viscous quantities at column j, index k (visrhs.f:46-131):
+// face k+1/2 (f2, f3, f4) and cell k (f2v, f3v, f4v); r = region index of
+// (j,k); the cell above is r + RT_RW, the side neighbours r -+ 1.
+template <class R>
+__device__ __forceinline__ void rt_visc_eta(const RtSmem<R>& sm, int r, R gkpr, R dre, R* out) {
+  R bv[2][4], uu[2], vv[2], ee[2];
+  for (int m = 0; m < 2; ++m) {
+    const int rr = r + m * RT_RW;
+    const R rj = sm.at(RS_RJ, rr), vnu = sm.at(RS_VNU, rr), gkap = sm.at(RS_GKAP, rr);
+    uu[m] = sm.at(RS_U, rr); vv[m] = sm.at(RS_V, rr); ee[m] = sm.at(RS_E, rr);
+    const R yx = sm.at(RS_YX, rr), yy = sm.at(RS_YY, rr);
+    const R b4 = (sq(yx) + sq(yy)) * rj;
+    bv[m][0] = (b4 + sq(yx) / (R)3. * rj) * vnu * dre;
+    bv[m][1] = (b4 + sq(yy) / (R)3. * rj) * vnu * dre;
+    bv[m][3] = (yx * yy / (R)3. * rj) * vnu * dre;
+    bv[m][2] = b4 * gkpr * gkap * dre;
+  }
+  const int rm = r - 1, rp = r + 1;
+  const R vnu = sm.at(RS_VNU, r), gkap = sm.at(RS_GKAP, r);
+  const R rjm = sm.at(RS_RJ, rm), rjp = sm.at(RS_RJ, rp);
+  const R xxm = sm.at(RS_XX, rm), xym = sm.at(RS_XY, rm), yxm = sm.at(RS_YX, rm), yym = sm.at(RS_YY, rm);
+  const R xxp = sm.at(RS_XX, rp), xyp = sm.at(RS_XY, rp), yxp = sm.at(RS_YX, rp), yyp = sm.at(RS_YY, rp);
+  R d1 = ((R)(4. / 3.) * xxm * yxm + xym * yym) * rjm;
+  d1 = d1 + ((R)(4. / 3.) * xxp * yxp + xyp * yyp) * rjp;
+  d1 = vnu * dre * d1;
+  R d2 = ((R)(4. / 3.) * xym * yym + xxm * yxm) * rjm;
+  d2 = d2 + ((R)(4. / 3.) * xyp * yyp + xxp * yxp) * rjp;
+  d2 = vnu * dre * d2;
+  R d4 = (xym * yym + xxm * yxm) * rjm;
+  d4 = d4 + (xyp * yyp + xxp * yxp) * rjp;
+  d4 = d4 * gkpr * gkap * dre;
+  R d5 = ((R)(-2. / 3.) * xym * yxm + xxm * yym) * rjm;
+  d5 = d5 + ((R)(-2. / 3.) * xyp * yxp + xxp * yyp) * rjp;
+  d5 = vnu * dre * d5;
+  R d7 = ((R)(-2. / 3.) * xxm * yym + xym * yxm) * rjm;
+  d7 = d7 + ((R)(-2. / 3.) * xxp * yyp + xyp * yxp) * rjp;
+  d7 = vnu * dre * d7;
+  const R b1 = bv[1][0] + bv[0][0], b2 = bv[1][1] + bv[0][1], b5 = bv[1][3] + bv[0][3];
+  const R ujp1 = sm.at(RS_UD, rp), ujm1 = sm.at(RS_UD, rm);
+  const R duj = (R)0.5 * (ujp1 - ujm1);
+  const R vjp1 = sm.at(RS_VD, rp), vjm1 = sm.at(RS_VD, rm);
+  const R dvj = (R)0.5 * (vjp1 - vjm1);
+  const R dej = (R)0.5 * (sm.at(RS_ED, rp) - sm.at(RS_ED, rm));
+  const R t4 = uu[1] * bv[1][0] + uu[0] * bv[0][0];
+  const R t5 = vv[1] * bv[1][1] + vv[0] * bv[0][1];
+  const R t6 = uu[1] * bv[1][3] + uu[0] * bv[0][3];
+  const R t7 = vv[1] * bv[1][3] + vv[0] * bv[0][3];
+  const R t8 = bv[1][2] + bv[0][2];
+  const R du = uu[1] - uu[0], dv = vv[1] - vv[0], dei = ee[1] - ee[0];
+  out[0] = b1 * du + b5 * dv;
+  out[1] = b5 * du + b2 * dv;
+  out[2] = (t4 + t7) * du + (t5 + t6) * dv + t8 * dei;
+  out[3] = d1 * duj + d5 * dvj;
+  out[4] = d7 * duj + d2 * dvj;
+  R f4v = (R)0.5 * d1 * (R)0.5 * (sq(ujp1) - sq(ujm1));
+  f4v = f4v + (R)0.5 * d2 * (R)0.5 * (sq(vjp1) - sq(vjm1));
+  f4v = f4v + d5 * (R)0.5 * (ujp1 + ujm1) * dvj;
+  f4v = f4v + d7 * (R)0.5 * (vjp1 + vjm1) * duj;
+  f4v = f4v + d4 * dej;
+  out[5] = f4v;
+}
+
+// xi-direction viscous quantities at row k, index j (visrhs.f:166-251):
+// face j+1/2 and cell j; the cell to the right is r + 1, the neighbours
+// below / above r -+ RT_RW.
+template <class R>
+__device__ __forceinline__ void rt_visc_xi(const RtSmem<R>& sm, int r, R gkpr, R dre, R* out) {
+  R av[2][4], uu[2], vv[2], ee[2];
+  for (int m = 0; m < 2; ++m) {
+    const int rr = r + m;
+    const R rj = sm.at(RS_RJ, rr), vnu = sm.at(RS_VNU, rr), gkap = sm.at(RS_GKAP, rr);
+    uu[m] = sm.at(RS_U, rr); vv[m] = sm.at(RS_V, rr); ee[m] = sm.at(RS_E, rr);
+    const R xx = sm.at(RS_XX, rr), xy = sm.at(RS_XY, rr);
+    const R a4 = (sq(xx) + sq(xy)) * rj;
+    av[m][0] = (a4 + sq(xx) / (R)3. * rj) * vnu * dre;
+    av[m][1] = (a4 + sq(xy) / (R)3. * rj) * vnu * dre;
+    av[m][3] = (xx * xy / (R)3. * rj) * vnu * dre;
+    av[m][2] = a4 * gkpr * gkap * dre;
+  }
+  const int rm = r - RT_RW, rp = r + RT_RW;
+  const R vnu = sm.at(RS_VNU, r), gkap = sm.at(RS_GKAP, r);
+  const R rkm = sm.at(RS_RJ, rm), rkp = sm.at(RS_RJ, rp);
+  const R xxm = sm.at(RS_XX, rm), xym = sm.at(RS_XY, rm), yxm = sm.at(RS_YX, rm), yym = sm.at(RS_YY, rm);
+  const R xxp = sm.at(RS_XX, rp), xyp = sm.at(RS_XY, rp), yxp = sm.at(RS_YX, rp), yyp = sm.at(RS_YY, rp);
+  R d1 = ((R)(4. / 3.) * xxm * yxm + xym * yym) * rkm;
+  d1 = d1 + ((R)(4. / 3.) * xxp * yxp + xyp * yyp) * rkp;
+  d1 = vnu * dre * d1;
+  R d2 = ((R)(4. / 3.) * xym * yym + xxm * yxm) * rkm;
+  d2 = d2 + ((R)(4. / 3.) * xyp * yyp + xxp * yxp) * rkp;
+  d2 = vnu * dre * d2;
+  R d4 = (xym * yym + xxm * yxm) * rkm;
+  d4 = d4 + (xyp * yyp + xxp * yxp) * rkp;
+  d4 = d4 * gkpr * gkap * dre;
+  R d5 = ((R)(-2. / 3.) * xym * yxm + xxm * yym) * rkm;
+  d5 = d5 + ((R)(-2. / 3.) * xyp * yxp + xxp * yyp) * rkp;
+  d5 = vnu * dre * d5;
+  R d7 = ((R)(-2. / 3.) * xxm * yym + xym * yxm) * rkm;
+  d7 = d7 + ((R)(-2. / 3.) * xxp * yyp + xyp * yxp) * rkp;
+  d7 = vnu * dre * d7;
+  const R a1 = av[1][0] + av[0][0], a2 = av[1][1] + av[0][1], a5 = av[1][3] + av[0][3];
+  const R ukp1 = sm.at(RS_UD, rp), ukm1 = sm.at(RS_UD, rm);
+  const R duk = (R)0.5 * (ukp1 - ukm1);
+  const R vkp1 = sm.at(RS_VD, rp), vkm1 = sm.at(RS_VD, rm);
+  const R dvk = (R)0.5 * (vkp1 - vkm1);
+  const R dek = (R)0.5 * (sm.at(RS_ED, rp) - sm.at(RS_ED, rm));
+  const R t4 = uu[1] * av[1][0] + uu[0] * av[0][0];
+  const R t5 = vv[1] * av[1][1] + vv[0] * av[0][1];
+  const R t6 = uu[1] * av[1][3] + uu[0] * av[0][3];
+  const R t7 = vv[1] * av[1][3] + vv[0] * av[0][3];
+  const R t8 = av[1][2] + av[0][2];
+  const R du = uu[1] - uu[0], dv = vv[1] - vv[0], dei = ee[1] - ee[0];
+  out[0] = a1 * du + a5 * dv;
+  out[1] = a5 * du + a2 * dv;
+  out[2] = (t4 + t7) * du + (t5 + t6) * dv + t8 * dei;
+  out[3] = d1 * duk + d7 * dvk;
+  out[4] = d5 * duk + d2 * dvk;
+  R f4v = (R)0.5 * d1 * (R)0.5 * (sq(ukp1) - sq(ukm1));
+  f4v = f4v + (R)0.5 * d2 * (R)0.5 * (sq(vkp1) - sq(vkm1));
+  f4v = f4v + d5 * (R)0.5 * (vkp1 + vkm1) * duk;
+  f4v = f4v + d7 * (R)0.5 * (ukp1 + ukm1) * dvk;
+  f4v = f4v + d4 * dek;
+  out[5] = f4v;
+}
+
+// One tile of the residual (step.f:41-93 for the cells of the tile): tile
+// `tile` of the slice covers interior cells j0..j1 x k0..k1.  flags as for
+// the cell-parallel assembly (AS_*).  Without AS_ACC the tile also zeroes s
+// on the halo cells next to it (step.f:41 zeroes s everywhere).  np receives
+// the thread's norm partial.
+template <class R>
+__device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int flags, NormPart& np) {
+  const ot2d_params& p = *S.P;
+  const int jd = S.jd, kd = S.kd, t = threadIdx.x;
+  const int ntj = (p.jend - p.jbeg + RT_TJ) / RT_TJ;
+  const int j0 = p.jbeg + (tile % ntj) * RT_TJ, k0 = p.kbeg + (tile / ntj) * RT_TK;
+  const int j1 = min(j0 + RT_TJ - 1, p.jend), k1 = min(k0 + RT_TK - 1, p.kend);
+  const int jr = j0 - RT_H, kr = k0 - RT_H;
+  const bool visc = (flags & AS_VISC) && !p.invisc;
+  const bool inv = flags & AS_INV;
+  const R gm1 = (R)p.gm1;
+  // A: stage the region
+  for (int r = t; r < RT_NR; r += RT_BS) {
+    const int j = jr + r % RT_RW, k = kr + r / RT_RW;
+    if (j >= 1 && j <= jd && k >= 1 && k <= kd) rt_stage_cell(S, p, sm, r, j, k, visc);
+  }
+  __syncthreads();
+  // B-D: every face quantity of the tile, as one work list so that the
+  // threads stay busy across the four kinds
+  const int nB = inv ? RT_TK * (RT_TJ + 1) : 0, nC = inv ? (RT_TK + 1) * RT_TJ : 0;
+  const int nD1 = visc ? RT_VEH * RT_TJ : 0, nD2 = visc ? RT_TK * RT_VXW : 0;
+  const int ntot = nB + nC + nD1 + nD2;
+  const R gkpr = (R)(p.gamma / p.pr), dre = (R)(.5 / p.rey);
+  for (int w = t; w < ntot; w += RT_BS) {
+    if (w < nB) {
+      // B: xi face j+1/2 of row k, j in j0-1..j1 (eulerrhs.f:69-167)
+      const int f = w;
+      const int kk = f / (RT_TJ + 1), jf = f % (RT_TJ + 1);
+      const int j = j0 - 1 + jf, k = k0 + kk;
+      if (j > j1 || k > k1) continue;
+      const RtLine<R> L{&sm, (k - kr) * RT_RW - jr, 1, max(1, jr), min(jd, jr + RT_RW - 1), gm1};
+      const int64_t o = at(jd, j, k);
+      R fl[4];
+      face_flux(L, make_recon<R>(p, 0), j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sm.F[v * (RT_TK * (RT_TJ + 1)) + f] = fl[v];
+    } else if (w < nB + nC) {
+      // C: eta face k+1/2 of column j, k in k0-1..k1 (eulerrhs.f:170-268)
+      const int f = w - nB;
+      const int kf = f / RT_TJ, jj = f % RT_TJ;
+      const int j = j0 + jj, k = k0 - 1 + kf;
+      if (j > j1 || k > k1) continue;
+      const RtLine<R> L{&sm, (j - jr) - kr * RT_RW, RT_RW, max(1, kr), min(kd, kr + RT_RH - 1), gm1};
+      const int64_t o = at(jd, j, k);
+      R fl[4];
+      face_flux(L, make_recon<R>(p, 1), k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sm.G[v * ((RT_TK + 1) * RT_TJ) + f] = fl[v];
+    } else if (w < nB + nC + nD1) {
+      // D1: eta viscous terms at k0-2..k1+1 of columns j0..j1
+      const int f = w - nB - nC;
+      const int kf = f / RT_TJ, jj = f % RT_TJ;
+      const int j = j0 + jj, k = k0 - 2 + kf;
+      if (j > j1 || k < 1 || k > kd - 1 || k > k1 + 1) continue;
+      R out[6];
+      rt_visc_eta(sm, (k - kr) * RT_RW + (j - jr), gkpr, dre, out);
+#pragma unroll
+      for (int v = 0; v < 6; ++v) sm.VE[v * (RT_VEH * RT_TJ) + f] = out[v];
+    } else {
+      // D2: xi viscous terms at j0-2..j1+1 of rows k0..k1
+      const int f = w - nB - nC - nD1;
+      const int kk = f / RT_VXW, jf = f % RT_VXW;
+      const int j = j0 - 2 + jf, k = k0 + kk;
+      if (k > k1 || j < 1 || j > jd - 1 || j > j1 + 1) continue;
+      R out[6];
+      rt_visc_xi(sm, (k - kr) * RT_RW + (j - jr), gkpr, dre, out);
+#pragma unroll
+      for (int v = 0; v < 6; ++v) sm.VX[v * (RT_TK * RT_VXW) + f] = out[v];
+    }
+  }
+  __syncthreads();
+  // E: per-cell assembly in the reference's order, then the time-spectral
+  // term, the norm partial and the store
+  const int jj = t % RT_TJ, kk = t / RT_TJ;
+  const int j = j0 + jj, k = k0 + kk;
+  const int nv = p.nv;
+  const bool acc = flags & AS_ACC;
+  if (j <= j1 && k <= k1) {
+    const int64_t o = at(jd, j, k);
+    R s[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) s[n] = (R)0.0;
+    if (acc) {
+#pragma unroll
+      for (int n = 0; n < 8; ++n)
+        if (n < nv) s[n] = S.s[(int64_t)n * S.qs + o];
+    }
+    if (inv) {
+      const R* F = sm.F + kk * (RT_TJ + 1) + jj;
+      const R* G = sm.G + kk * RT_TJ + jj;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) s[v] = s[v] - (F[v * (RT_TK * (RT_TJ + 1)) + 1] - F[v * (RT_TK * (RT_TJ + 1))]);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) s[v] = s[v] - (G[v * ((RT_TK + 1) * RT_TJ) + RT_TJ] - G[v * ((RT_TK + 1) * RT_TJ)]);
+    }
+    if (visc) {
+      // VE row of cell k is kk+2; VX column of cell j is jj+2
+      const R* VE = sm.VE + (kk + 2) * RT_TJ + jj;
+      for (int v = 0; v < 3; ++v) {
+        const R* a0 = VE + v * (RT_VEH * RT_TJ);
+        const R* b0 = VE + (v + 3) * (RT_VEH * RT_TJ);
+        const R a = a0[0] - a0[-RT_TJ];
+        R b;
+        if (k == p.kend) b = (R)0.5 * (b0[-2 * RT_TJ] - (R)4. * b0[-RT_TJ] + (R)3 * b0[0]);
+        else b = (R)0.5 * (b0[RT_TJ] - b0[-RT_TJ]);
+        s[v + 1] = s[v + 1] + a + b;
+      }
+      const R* VX = sm.VX + kk * RT_VXW + jj + 2;
+      for (int v = 0; v < 3; ++v) {
+        const R* a0 = VX + v * (RT_TK * RT_VXW);
+        const R* b0 = VX + (v + 3) * (RT_TK * RT_VXW);
+        const R a = a0[0] - a0[-1];
+        R b;
+        if (j == p.jend) b = (R)0.5 * (b0[-2] - (R)4. * b0[-1] + (R)3 * b0[0]);
+        else b = (R)0.5 * (b0[1] - b0[-1]);
+        s[v + 1] = s[v + 1] + a + b;
+      }
+    }
+    if ((flags & AS_TS) && p.timespectral && S.Ds) {
+      // timespectralrhs (sources.f:16-24): s(n) -= rotf*Ds(nsp,m)*q(m)
+      const int64_t n2 = (int64_t)jd * kd;
+      const R rotf = (R)p.rotf;
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        if (n >= nv) continue;
+        R a = s[n];
+        for (int m = 1; m <= S.nspec; ++m) {
+          const R dsn = (R)S.Ds[(int64_t)(m - 1) * S.nspec + (S.nsp - 1)];
+          const R qm = S.q[(int64_t)n * S.qs + (int64_t)(m - S.nsp) * n2 + o];
+          a = a - rotf * dsn * qm;
+        }
+        s[n] = a;
+      }
+    }
+    if (flags & AS_NORM) {
+      // norms (step.f:67-88): the per-cell terms in R, the reduction in f64.
+      // The first variable of the cell's maximum |s| carries the smallest
+      // loop-order key, as in the reference's scan.
+      const int ibi = S.iblank[o];
+      const R m = (R)(ibi > 0 ? ibi : 0);
+      R best = (R)-1;
+      int bn = 1;
+#pragma unroll
+      for (int n = 1; n <= 8; ++n) {
+        if (n > p.nmv) continue;
+        const R smrs = fabs(s[n - 1]) * m;
+        if (smrs > best) { best = smrs; bn = n; }
+      }
+      np.resmax = (double)best;
+      np.key = ((long long)(k - 1) * (p.nmv + 1) + bn) * (long long)jd + (j - 1);
+      const R s1 = s[0] * m, s2 = s[1] * m, s3 = s[2] * m, s4 = s[3] * m;
+      np.resrho = (double)(s[0] * s[0]);
+      np.rsum = (double)(s1 * s1 + s2 * s2 + s3 * s3 + s4 * s4);
+    }
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+      if (n < nv) S.s[(int64_t)n * S.qs + o] = s[n];
+  }
+  if (!acc) {
+    // halo cells bordering the tile
+    const int jlo = (j0 == p.jbeg) ? 1 : j0, jhi = (j1 == p.jend) ? jd : j1;
+    const int klo = (k0 == p.kbeg) ? 1 : k0, khi = (k1 == p.kend) ? kd : k1;
+    const int nw = jhi - jlo + 1, nbox = nw * (khi - klo + 1);
+    if (nbox > (j1 - j0 + 1) * (k1 - k0 + 1))
+      for (int i = t; i < nbox; i += RT_BS) {
+        const int hj = jlo + i % nw, hk = klo + i / nw;
+        if (hj >= p.jbeg && hj <= p.jend && hk >= p.kbeg && hk <= p.kend) continue;
+        const int64_t o = at(jd, hj, hk);
+        for (int n = 1; n <= nv; ++n) S.s[(int64_t)(n - 1) * S.qs + o] = (R)0.0;
+      }
+  }
+}
+
+}  // namespace ot2d

@@ -241,9 +241,10 @@ __device__ __forceinline__ void roe(R gm1, const R* L, const R* Rr, R ri1, R ri2
   f[3] = aj * (eplft * uulft + eprht * uurht - r3 * plar - aq4) - fssub * z;
 }
 
-// Inviscid flux through one face between cells i and i+1 of a line.
-template <class R>
-__device__ __forceinline__ void face_flux(const LineRd<R>& L, const Recon<R>& rc, int i, int n, R ri1, R ri2, R ri3,
+// Inviscid flux through one face between cells i and i+1 of a line.  L
+// supplies f4(c, out) (the primitive f of cell c) and iba(c).
+template <class R, class Line>
+__device__ __forceinline__ void face_flux(const Line& L, const Recon<R>& rc, int i, int n, R ri1, R ri2, R ri3,
                                           R* fout) {
   R wl[4][7], ql[4], qr[4];
   int ibw[7];

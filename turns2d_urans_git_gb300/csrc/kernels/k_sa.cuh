@@ -215,42 +215,208 @@ __device__ void sa_lsolvej_line(const Slice<R>& S, const ot2d_params& p, int k) 
   }
 }
 
+// lsolvej for 32 consecutive k-lines by one warp (lane l <-> line kline0+l).
+// The lines run along j, the fast index of the arrays, so the warp stages
+// 32 x 32 tiles through shared memory (one row of a tile per load, then one
+// line per lane); the arithmetic per line is sa_lsolvej_line's, in its
+// order.  The tiles are fetched with cp.async into two buffers, the next
+// tile in flight while the current one is eliminated.
+// smem: LJ_SMEM elements of R.
+constexpr int LJ_TILE = 32 * 33;
+constexpr int LJ_SMEM = 2 * 4 * LJ_TILE;
+
+template <class R>
+__device__ __forceinline__ void lj_cp_async(R* dst, const R* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src), "n"((int)sizeof(R)));
+}
+__device__ __forceinline__ void lj_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void lj_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <class R>
+__device__ void sa_lsolvej_group(const Slice<R>& S, const ot2d_params& p, int kline0, R* sm) {
+  const int lane = threadIdx.x & 31;
+  const int jd = S.jd; const int64_t ws = S.wstride;
+  const R* ga = S.w + W_AJ * ws; R* gc = S.w + W_CJ * ws; R* gs = S.w + W_SJ * ws; const R* gb = S.w + W_BJ * ws;
+  const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
+  const int ntile = (je - js + 1 + 31) / 32;
+  const bool mine = ks + kline0 + lane <= ke;
+  // buffer b of array m: sm + (b*4 + m)*LJ_TILE; element (row r, column c) at r*33 + c
+  auto buf = [&](int b, int m) { return sm + (b * 4 + m) * LJ_TILE; };
+  // fetch tile t (columns j0..j0+31) of arrays m0..m0+nm-1 of {a, b, c, s}
+  auto fetch = [&](int t, int b, bool fwd) {
+    const int j = js + 32 * t + lane;
+    for (int r = 0; r < 32; ++r) {
+      const int kr = ks + kline0 + r;
+      if (kr <= ke && j <= je) {
+        const int64_t o = at(jd, j, kr);
+        if (fwd) lj_cp_async(buf(b, 0) + r * 33 + lane, ga + o);
+        lj_cp_async(buf(b, 1) + r * 33 + lane, gb + o);
+        lj_cp_async(buf(b, 2) + r * 33 + lane, gc + o);
+        lj_cp_async(buf(b, 3) + r * 33 + lane, gs + o);
+      }
+    }
+    lj_commit();
+  };
+  R cp = (R)0, sp = (R)0;
+  // forward elimination
+  fetch(0, 0, true);
+  for (int t = 0; t < ntile; ++t) {
+    const int b = t & 1;
+    if (t + 1 < ntile) { fetch(t + 1, b ^ 1, true); lj_wait<1>(); }
+    else lj_wait<0>();
+    __syncwarp();
+    const R *A = buf(b, 0), *B = buf(b, 1);
+    R *Cm = buf(b, 2), *Sm = buf(b, 3);
+    const int j0 = js + 32 * t, j = j0 + lane;
+    if (mine) {
+      for (int jj = 0; jj < 32 && j0 + jj <= je; ++jj) {
+        const int i = lane * 33 + jj;
+        R bb;
+        if (j0 + jj == js) { bb = (R)1. / B[i]; sp = Sm[i] * bb; cp = Cm[i] * bb; }
+        else { bb = (R)1. / (B[i] - A[i] * cp); sp = (Sm[i] - A[i] * sp) * bb; cp = Cm[i] * bb; }
+        Sm[i] = sp; Cm[i] = cp;
+      }
+    }
+    __syncwarp();
+    for (int r = 0; r < 32; ++r) {
+      const int kr = ks + kline0 + r;
+      if (kr <= ke && j <= je) {
+        const int64_t o = at(jd, j, kr);
+        gc[o] = Cm[r * 33 + lane]; gs[o] = Sm[r * 33 + lane];
+      }
+    }
+    __syncwarp();
+  }
+  // the stores above are read back below by the same lanes (same element
+  // -> lane mapping); order them before the asynchronous copies
+  __threadfence_block();
+  // back substitution; output x * bjmat (samodel2d.f:150-153)
+  R snext = sp;
+  fetch(ntile - 1, 0, false);
+  for (int t = ntile - 1, n = 0; t >= 0; --t, ++n) {
+    const int b = n & 1;
+    if (t > 0) { fetch(t - 1, b ^ 1, false); lj_wait<1>(); }
+    else lj_wait<0>();
+    __syncwarp();
+    const R *B = buf(b, 1), *Cm = buf(b, 2);
+    R* Sm = buf(b, 3);
+    const int j0 = js + 32 * t, j = j0 + lane;
+    if (mine) {
+      const int jjmax = (je - j0 < 31) ? je - j0 : 31;
+      for (int jj = jjmax; jj >= 0; --jj) {
+        const int i = lane * 33 + jj;
+        R x = (j0 + jj == je) ? Sm[i] : Sm[i] - Cm[i] * snext;
+        snext = x;
+        Sm[i] = ((x + (R)0.) - (R)0.) * B[i];
+      }
+    }
+    __syncwarp();
+    for (int r = 0; r < 32; ++r) {
+      const int kr = ks + kline0 + r;
+      if (kr <= ke && j <= je) gs[at(jd, j, kr)] = Sm[r * 33 + lane];
+    }
+    __syncwarp();
+  }
+}
+
 // lsolvek (samodel2d.f:1347-1385) on one j-line, then s2 = x and the
 // update q5 = max(q5 + x*max(iblank,0), 1e-20) (samodel2d.f:184-188) in FP64
+// and c_turm of the cell (samodel2d.f:193; the second turbc only changes
+// halo cells, so mu_t here equals the reference's).  The line is walked in
+// chunks of LK_U cells whose loads are issued one chunk ahead, before the
+// stores of the current chunk, so the recurrence does not wait on memory.
 template <class R>
 __device__ void sa_lsolvek_line(const Slice<R>& S, const ot2d_params& p, int j) {
+  constexpr int LK_U = sizeof(R) == 4 ? 8 : 4;
   const int jd = S.jd; const int64_t ws = S.wstride, qs = S.qs;
   R* a = S.w + W_AK * ws; R* c = S.w + W_CK * ws; R* s = S.w + W_SJ * ws; const R* b = S.w + W_BJ * ws;
+  const R* vmul = S.w + W_VMUL * ws;
   const int ks = p.kbeg, ke = p.kend, n5 = p.nmv + 1;
+  const R cv1 = (R)SAc::cv1;
   int64_t o = at(jd, j, ks);
   R bb = (R)1. / b[o];
   R sp = s[o] * bb, cp = c[o] * bb;
   s[o] = sp; c[o] = cp;
-  for (int k = ks + 1; k <= ke; ++k) {
-    o = at(jd, j, k);
-    bb = (R)1. / (b[o] - a[o] * cp);
-    sp = (s[o] - a[o] * sp) * bb;
-    cp = c[o] * bb;
-    s[o] = sp; c[o] = cp;
+  // forward elimination
+  {
+    R na[LK_U], nb[LK_U], nc[LK_U], ns[LK_U];
+    auto load = [&](int k0) {
+#pragma unroll
+      for (int u = 0; u < LK_U; ++u)
+        if (k0 + u <= ke) { const int64_t ou = at(jd, j, k0 + u); na[u] = a[ou]; nb[u] = b[ou]; nc[u] = c[ou]; ns[u] = s[ou]; }
+    };
+    load(ks + 1);
+    for (int k0 = ks + 1; k0 <= ke; k0 += LK_U) {
+      R ra[LK_U], rb[LK_U], rc[LK_U], rs[LK_U];
+#pragma unroll
+      for (int u = 0; u < LK_U; ++u) { ra[u] = na[u]; rb[u] = nb[u]; rc[u] = nc[u]; rs[u] = ns[u]; }
+      if (k0 + LK_U <= ke) load(k0 + LK_U);
+#pragma unroll
+      for (int u = 0; u < LK_U; ++u) {
+        if (k0 + u <= ke) {
+          o = at(jd, j, k0 + u);
+          bb = (R)1. / (rb[u] - ra[u] * cp);
+          sp = (rs[u] - ra[u] * sp) * bb;
+          cp = rc[u] * bb;
+          s[o] = sp; c[o] = cp;
+        }
+      }
+    }
   }
-  auto upd = [&](int64_t oo, R x) {
+  // back substitution + update + mu_t
+  double* q5 = S.q64 + (int64_t)(n5 - 1) * qs;
+  R nc[LK_U], ns[LK_U], nq1[LK_U], nJ[LK_U], nvm[LK_U];
+  double nq5[LK_U];
+  int nib[LK_U];
+  auto load = [&](int k0) {  // cells k0, k0-1, ..., k0-LK_U+1
+#pragma unroll
+    for (int u = 0; u < LK_U; ++u)
+      if (k0 - u >= ks) {
+        const int64_t ou = at(jd, j, k0 - u);
+        nc[u] = c[ou]; ns[u] = s[ou]; nq1[u] = S.q[ou]; nJ[u] = S.q[(int64_t)(p.nq - 1) * qs + ou];
+        nvm[u] = vmul[ou]; nq5[u] = q5[ou]; nib[u] = S.iblank[ou];
+      }
+  };
+  auto upd = [&](int64_t oo, R x, double q5o, int ibi, R q1, R J, R vm) {
     R x2 = (R)0. + x;            // s2 = s2 + sjmat, s2 = 0 on entry
     R relx = (R)1.0 * x2;        // relfac * sjmat
     s[oo] = relx;
-    int ibi = S.iblank[oo];
     double ib = (double)(ibi > 0 ? ibi : 0);
-    double v = S.q64[(int64_t)(n5 - 1) * qs + oo] + (double)relx * ib;
+    double v = q5o + (double)relx * ib;
     v = (1.0e-20 > v) ? 1.0e-20 : v;
-    S.q64[(int64_t)(n5 - 1) * qs + oo] = v;
+    q5[oo] = v;
     if constexpr (sizeof(R) != sizeof(double)) S.q[(int64_t)(n5 - 1) * qs + oo] = (R)v;
+    // c_turm (samodel2d.f:372-399) with q5 as just stored
+    const R rhoJ = q1 * J;
+    const R vnul = vm / rhoJ;
+    const R qv = (R)v;
+    const R chi = qv / vnul;
+    const R fv1 = cube(chi) / (cube(chi) + cube(cv1));
+    S.turmu[oo] = rhoJ * qv * fv1;
   };
   R snext = sp;
-  upd(o, snext);
-  for (int k = ke - 1; k >= ks; --k) {
-    o = at(jd, j, k);
-    R x = s[o] - c[o] * snext;
-    snext = x;
-    upd(o, x);
+  load(ke);
+  for (int k0 = ke; k0 >= ks; k0 -= LK_U) {
+    R rc[LK_U], rs[LK_U], rq1[LK_U], rJ[LK_U], rvm[LK_U];
+    double rq5[LK_U];
+    int rib[LK_U];
+#pragma unroll
+    for (int u = 0; u < LK_U; ++u) {
+      rc[u] = nc[u]; rs[u] = ns[u]; rq1[u] = nq1[u]; rJ[u] = nJ[u]; rvm[u] = nvm[u]; rq5[u] = nq5[u]; rib[u] = nib[u];
+    }
+    if (k0 - LK_U >= ks) load(k0 - LK_U);
+#pragma unroll
+    for (int u = 0; u < LK_U; ++u) {
+      const int k = k0 - u;
+      if (k >= ks) {
+        o = at(jd, j, k);
+        const R x = (k == ke) ? snext : rs[u] - rc[u] * snext;
+        snext = x;
+        upd(o, x, rq5[u], rib[u], rq1[u], rJ[u], rvm[u]);
+      }
+    }
   }
 }
 

@@ -9,8 +9,17 @@
 #include "k_sa.cuh"
 #include "k_misc.cuh"
 #include "launch.h"
+#include "k_resid.cuh"
 
 namespace ot2d {
+
+// true when the speed of sound squared of state q (Q/J, 4 variables) is at
+// or below 0.002 or not finite (the reference's mstop, step.f:366-368)
+__device__ __forceinline__ bool monitor_bad(double ggm1, const double* q) {
+  const double q1 = q[0], qq = q[1] * q[1] + q[2] * q[2];
+  const double lhs = ggm1 * (q[3] * q1 - 0.5 * qq), rhs = 0.002 * q1 * q1;
+  return !(q1 > 0.0) || !(lhs > rhs) || !isfinite(lhs);
+}
 
 // Cell-parallel mapping: slice i owns blocks [first[i], first[i+1]) of
 // CELL_BS threads each, covering its jd*kd cells.
@@ -45,6 +54,22 @@ __global__ void k_bc(const Slice<R>* __restrict__ sl, int advance) {
   const int istep0 = S.ist ? S.ist[0] : S.P->istep0;
   bc_slice(S, nullptr, istep0);
   shadow_ring(S, 1, 4);
+  // monitor of the halo ring just set (the interior is checked by k_update)
+  if (S.ist && advance) {
+    const int jd = S.jd, kd = S.kd, nring = 2 * jd + 2 * (kd - 2);
+    bool bad = false;
+    for (int i = threadIdx.x; i < nring; i += blockDim.x) {
+      int j, k;
+      if (i < jd) { j = i + 1; k = 1; }
+      else if (i < 2 * jd) { j = i - jd + 1; k = kd; }
+      else if (i < 2 * jd + kd - 2) { j = 1; k = i - 2 * jd + 2; }
+      else { j = jd; k = i - (2 * jd + kd - 2) + 2; }
+      const int64_t o = at(jd, j, k);
+      double qh[4] = {S.q64[o], S.q64[S.qs + o], S.q64[2 * S.qs + o], S.q64[3 * S.qs + o]};
+      bad = bad || monitor_bad(S.P->ggm1, qh);
+    }
+    if (bad) atomicOr(&S.ist[2], 2);
+  }
 }
 
 template <class R>
@@ -128,6 +153,32 @@ __global__ void __launch_bounds__(CELL_BS) k_assemble(const Slice<R>* __restrict
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
+// Fused residual over tiles of RT_TJ x RT_TK interior cells: slice i owns
+// tiles [tfirst[i], tfirst[i+1]).  Dynamic shared memory: rt_smem_bytes<R>().
+template <class R>
+__global__ void __launch_bounds__(RT_BS) k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst,
+                                                  int nslice, int flags, NormPart* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char rt_raw[];
+  const int si = find_slice(tfirst, nslice, blockIdx.x);
+  const Slice<R>& S = sl[si];
+  RtSmem<R> sm(rt_raw);
+  NormPart np{0.0, 0.0, 0.0, 0x7fffffffffffffffLL};
+  resid_tile(S, sm, blockIdx.x - tfirst[si], flags, np);
+  if (!(flags & AS_NORM)) return;
+  // deterministic block reduction: a fixed shuffle tree per warp, then the
+  // warp partials in warp order
+  np = warp_norm_reduce(np);
+  NormPart* sh = sm.red;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = np;
+  __syncthreads();
+  if (wid == 0) {
+    np = lane < RT_BS / 32 ? sh[lane] : NormPart{0.0, 0.0, 0.0, 0x7fffffffffffffffLL};
+    np = warp_norm_reduce(np);
+    if (lane == 0) part[blockIdx.x] = np;
+  }
+}
+
 // Per-slice norms from the block partials (fixed order): red[0..3] =
 // rsum, resrho, resmax, key; status word on blow-up (step.f:105-110).
 template <class R>
@@ -135,9 +186,13 @@ __global__ void k_norm_final(const Slice<R>* __restrict__ sl, const int32_t* __r
                              const NormPart* __restrict__ part) {
   const int si = blockIdx.x;
   const Slice<R>& S = sl[si];
-  if (threadIdx.x != 0) return;
+  // one warp: lane l combines partials l, l+32, ... in order, then a fixed
+  // shuffle tree over the lanes (the same order on every run)
+  const int lane = threadIdx.x & 31;
   NormPart acc{0.0, 0.0, 0.0, 0x7fffffffffffffffLL};
-  for (int b = first[si]; b < first[si + 1]; ++b) acc = norm_combine(acc, part[b]);
+  for (int b = first[si] + lane; b < first[si + 1]; b += 32) acc = norm_combine(acc, part[b]);
+  acc = warp_norm_reduce(acc);
+  if (lane != 0) return;
   double volum = (double)(S.jd * S.kd);
   double rsum = sqrt(acc.rsum / volum), resrho = sqrt(acc.resrho / volum);
   S.red[0] = rsum; S.red[1] = resrho; S.red[2] = acc.resmax; S.red[3] = (double)acc.key;
@@ -203,9 +258,18 @@ __global__ void k_turbc(const Slice<R>* __restrict__ sl, int final_pass) {
   turbc_slice(S, S.w + W_U * S.wstride, S.w + W_V * S.wstride);
   shadow_ring(S, p.nmv + 1, p.nmv + 1);
   if (final_pass) {
+    // c_turm on the halo ring (the interior was done by the k-line solve
+    // right after its update; turbc leaves interior cells unchanged)
     __syncthreads();
-    const int n2 = S.jd * S.kd;
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) sa_turm_cell(S, p, i % S.jd + 1, i / S.jd + 1);
+    const int jd = S.jd, kd = S.kd, nring = 2 * jd + 2 * (kd - 2);
+    for (int i = threadIdx.x; i < nring; i += blockDim.x) {
+      int j, k;
+      if (i < jd) { j = i + 1; k = 1; }
+      else if (i < 2 * jd) { j = i - jd + 1; k = kd; }
+      else if (i < 2 * jd + kd - 2) { j = 1; k = i - 2 * jd + 2; }
+      else { j = jd; k = i - (2 * jd + kd - 2) + 2; }
+      sa_turm_cell(S, p, j, k);
+    }
   }
 }
 
@@ -237,6 +301,20 @@ __global__ void k_sa_lsolve(const Slice<R>* __restrict__ sl, const int32_t* __re
   else { int j = p.jbeg + line; if (j <= p.jend) sa_lsolvek_line(S, p, j); }
 }
 
+// lsolvej by warps of 32 k-lines (one warp per CTA); slice i owns groups
+// [gfirst[i], gfirst[i+1])
+template <class R>
+__global__ void __launch_bounds__(32) k_sa_lsolvej(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ gfirst,
+                                                   int nslice) {
+  extern __shared__ __align__(16) unsigned char lj_raw[];
+  R* sm = (R*)lj_raw;   // LJ_SMEM elements
+  const int si = find_slice(gfirst, nslice, blockIdx.x);
+  const Slice<R>& S = sl[si];
+  const ot2d_params& p = *S.P;
+  if (p.lamin || p.iturb != 1) return;
+  sa_lsolvej_group(S, p, 32 * (blockIdx.x - gfirst[si]), sm);
+}
+
 // q(1:4) += s*max(iblank,0) on interior cells (step.f:203-213), FP64 state
 template <class R>
 __global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
@@ -248,12 +326,17 @@ __global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__
   const int64_t o = at(S.jd, j, k);
   int ibi = S.iblank[o];
   double m = (double)(ibi > 0 ? ibi : 0);
+  double qn[4];
 #pragma unroll
   for (int n = 0; n < 4; ++n) {
     double v = S.q64[n * S.qs + o] + (double)S.s[n * S.qs + o] * m;
+    qn[n] = v;
     S.q64[n * S.qs + o] = v;
     if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = (R)v;
   }
+  // monitor of the updated cell (step.f:356-370), free of divisions:
+  // a^2 <= 0.002  <=>  ggm1*(q4*q1 - qq/2) <= 0.002*q1^2 for q1 > 0
+  if (S.ist && monitor_bad(p.ggm1, qn)) atomicOr(&S.ist[2], 2);
 }
 
 // compute copy of the whole state from the FP64 master (after the host

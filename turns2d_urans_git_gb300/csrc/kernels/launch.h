@@ -10,6 +10,8 @@ template <class R> struct Slice;
 struct NormPart;
 
 constexpr int CELL_BS = 256;
+// residual tile: RT_TJ x RT_TK interior cells per CTA
+constexpr int RT_TJ = 32, RT_TK = 8;
 
 struct Batch {
   int nslice = 0;          // slices in the batch
@@ -22,7 +24,11 @@ struct Batch {
   const int32_t* d_kfirst = nullptr;  // [nslice+1] first j-line (lsolvek) of each slice
   const int32_t* d_lfirst = nullptr;  // [nslice+1] first LU-SGS record block of each slice
   int lu_blocks = 0;                  // blocks of the LU-SGS record kernel
-  NormPart* d_part = nullptr;         // [cell_blocks] norm partials
+  const int32_t* d_gfirst = nullptr;  // [nslice+1] first 32-line group (lsolvej) of each slice
+  int jgroups = 0;                    // 32-line groups over the batch
+  const int32_t* d_tfirst = nullptr;  // [nslice+1] first residual tile of each slice
+  int tile_blocks = 0;                // residual tiles over the batch
+  NormPart* d_part = nullptr;         // [max(cell_blocks, tile_blocks)] norm partials
 };
 
 // One full iteration of step.f for every slice of the batch:

@@ -11,16 +11,21 @@ cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t 
 }
 template <class R>
 cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st) {
-  k_bc<R><<<b.nslice, 128, 0, st>>>(d_sl, advance);
+  k_bc<R><<<b.nslice, 256, 0, st>>>(d_sl, advance);
   return cudaGetLastError();
 }
 template <class R>
 cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st) {
-  k_faces<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
-  if (viscous) k_visc<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   const int flags = AS_INV | AS_TS | AS_NORM | (viscous ? AS_VISC : 0);
-  k_assemble<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, flags, b.d_part);
-  k_norm_final<R><<<b.nslice, 32, 0, st>>>(d_sl, b.d_first, b.nslice, b.d_part);
+  constexpr size_t smem = rt_smem_bytes<R>();
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k_resid<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  k_resid<R><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
+  k_norm_final<R><<<b.nslice, 32, 0, st>>>(d_sl, b.d_tfirst, b.nslice, b.d_part);
   return cudaGetLastError();
 }
 template <class R>
@@ -64,7 +69,14 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_sa_prep<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   k_turbc<R><<<b.nslice, 256, 0, st>>>(d_sl, 0);
   k_sa_rhs<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
-  k_sa_lsolve<R><<<(b.jlines + 63) / 64, 64, 0, st>>>(d_sl, b.d_jfirst, b.nslice, 0);
+  constexpr size_t lj_smem = sizeof(R) * LJ_SMEM;
+  static bool lj_attr = false;
+  if (!lj_attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_sa_lsolvej<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lj_smem);
+    if (e != cudaSuccess) return e;
+    lj_attr = true;
+  }
+  k_sa_lsolvej<R><<<b.jgroups, 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sa_lsolve<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice, 1);
   k_turbc<R><<<b.nslice, 256, 0, st>>>(d_sl, 1);
   return cudaGetLastError();
@@ -101,7 +113,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   if ((e = launch_lusgs(d_sl, b, 1, st)) != cudaSuccess) return e;
   if (turb && (e = launch_sa(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_update(d_sl, b, st)) != cudaSuccess) return e;
-  return launch_monitor(d_sl, b, st);
+  return cudaSuccess;  // the monitor runs inside k_update and k_bc
 }
 
 #define OT2D_INSTANTIATE(R)                                                                              \
