@@ -126,6 +126,26 @@ int ot2d_find_cellcenter(double* x, double* y, double* xv, double* yv, int32_t* 
 int ot2d_metfv(double* q, double* x, double* y, double* xv, double* yv, double* xx, double* xy, double* yx,
                double* yy, int32_t* jd, int32_t* kd, int32_t* im);
 
+/* Residual norms of step.f:58-93 -- rsum, resrho, resmax -- of one
+ * instance's residual s(jd,kd,nmv) already in device memory (double),
+ * computed without allocating device memory.  No counterpart in the
+ * reference (step.f computes these inline).  For callers that cannot
+ * allocate during their iteration loop (a driver whose device memory is all
+ * in its own pool, a loop that must not take cudaMalloc's implicit device
+ * synchronisation): the per-block partials live in a fixed static device
+ * array, which limits jd*kd to OT2D_NOALLOC_MAX_CELLS (larger: OT2D_ERR_ARG,
+ * nothing launched).  The first call on a device looks the array up with
+ * that device current; make it before any stream capture.  Calls share the
+ * array: calls that overlap in time race, so serialise them.  s, iblank:
+ * device pointers; js..ke: the interior (jbeg..jend, kbeg..kend); nmv >= 4;
+ * out (host, 6 doubles): rsum, resrho, resmax and the j, k, n of resmax
+ * (1-based; 0 when there is no interior cell).  stream: a cudaStream_t
+ * (null = the default stream); the call returns after the stream has
+ * finished the work. */
+#define OT2D_NOALLOC_MAX_CELLS 1048576
+int ot2d_norms_noalloc(const double* s, const int32_t* iblank, int32_t jd, int32_t kd, int32_t js, int32_t je,
+                       int32_t ks, int32_t ke, int32_t nmv, double* out, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* batched solver (host runtime over device-resident meshes)               */
 /* ---------------------------------------------------------------------- */

@@ -34,6 +34,7 @@ UNITS = [
     ("host/runtime.cu", ["-fmad=false"]),
     ("host/solver.cu", ["-fmad=false"]),
     ("host/dropin.cu", ["-fmad=false"]),
+    ("host/noalloc.cu", ["-fmad=false"]),
     ("host/geom.cpp", None),
     ("host/setup_host.cpp", None),
 ]
