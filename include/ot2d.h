@@ -105,6 +105,10 @@ int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int3
 int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
                 double* xy, double* yx, double* yy, double* ug, double* vg, int32_t* jd, int32_t* kd,
                 double* tscale, int32_t* iblank, int32_t* im, int32_t* nsp);
+/* src/komegasst.f:2-3 (no transition model: itrans = 0) */
+int ot2d_komegasst(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
+                   double* xy, double* yx, double* yy, double* ug, double* vg, int32_t* jd, int32_t* kd,
+                   double* tscale, int32_t* iblank, int32_t* im);
 /* src/sources.f:2 (q, s: full (jd,kd,nspec,nv) arrays) */
 int ot2d_timespectralrhs(double* q, double* s, double* Ds, int32_t* jd, int32_t* kd, int32_t* nsp);
 /* src/step.f:2-7 (full arrays over nspec; norms of the last call via

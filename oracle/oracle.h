@@ -39,6 +39,15 @@ void visrhs(const P& p, A2 turmu, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy);
 void time_step(const P& p, A3 q, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 tscale, A2 bt, I2 iblank);
 /* lhs.f:470-814 */
 void ilu2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, A2 tscale);
+/* lhs.f:817-1057 (ilhs = 2: lhsinv + pentadag) */
+void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, I2 iblank, A2 tscale, A2 bt);
+/* samodel2d.f:200-240 */
+void lamvis(const P& p, A3 q, A2 vmul);
+/* samodel2d.f:243-293 */
+void dist(const P& p, A2 sn, A2 x, A2 y, const double* xv, const double* yv);
+/* komegasst.f:2-187 (no transition model); res_out (optional) = {restke, restomega} */
+void komegasst(const P& p, A3 q, A3 s, A2 turmu, A2 x, A2 y, const double* xv, const double* yv,
+               A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 tscale, I2 iblank, double* res_out);
 /* samodel2d.f:2-197 */
 void vmu_sa(const P& p, A3 q, A3 s, A2 turmu, A2 x, A2 y, const double* xv, const double* yv,
             A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 tscale, I2 iblank, double* resl2_out);

@@ -9,8 +9,8 @@
  * Parity status: the reference ships no golden vectors, test data or sample
  * inputs, and no Fortran compiler exists on either machine, so the oracle is
  * "parity unpinned" against the reference itself.  It is pinned instead by
- * the invariants the tests check (freestream preservation, symmetry, Thomas
- * vs dense solve, Ds antisymmetry) and by golden fixtures it generated.
+ * the invariants the tests check (freestream preservation, residual mirror
+ * symmetry, Ds antisymmetry) and by golden fixtures it generated.
  *
  * Fortran semantics kept throughout (the reference is compiled with -r8 /
  * -fdefault-real-8, configure.ac:27-33):

@@ -1,7 +1,9 @@
 /*
  * oracle_implicit.cpp -- TEST INFRASTRUCTURE ONLY (see oracle_common.h).
- * FP64 restatement of the local time step (src/time.f) and the LU-SGS
- * hyperplane operator ilu2d (src/lhs.f:470-814).
+ * FP64 restatement of the local time step (src/time.f), the LU-SGS
+ * hyperplane operator ilu2d (src/lhs.f:470-814) and the diagonalised ADI
+ * operator arc2d with its pentadiagonal line inversions (src/lhs.f:817-1057,
+ * lhsinv :1536-1816, pentadag :1819-1873; ilhs = 2).
  */
 #include <cstdio>
 #include <cstdlib>
@@ -201,6 +203,291 @@ void ilu2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
       q(j, k, 3) = q(j, k, 3) * q(j, k, 1);
       q(j, k, 4) = q(j, k, 4) * q(j, k, 1);
     }
+}
+
+/* lhs.f:1819-1873 (1-based a..f of length N) */
+static void pentadag(double* a, double* b, double* c, double* d, double* e, double* f, int N) {
+  auto A = [&](int i) -> double& { return a[i - 1]; };
+  auto B = [&](int i) -> double& { return b[i - 1]; };
+  auto Cc = [&](int i) -> double& { return c[i - 1]; };
+  auto D = [&](int i) -> double& { return d[i - 1]; };
+  auto E = [&](int i) -> double& { return e[i - 1]; };
+  auto F = [&](int i) -> double& { return f[i - 1]; };
+  int i = 1;
+  double d0 = 1.0 / Cc(i);
+  D(i + 1) = D(i + 1) * d0;
+  E(i + 2) = E(i + 2) * d0;
+  F(i) = F(i) * d0;
+  i = 2;
+  double d1 = B(i - 1);
+  d0 = 1.0 / (Cc(i) - d1 * D(i));
+  F(i) = (F(i) - d1 * F(i - 1)) * d0;
+  D(i + 1) = (D(i + 1) - d1 * E(i + 1)) * d0;
+  E(i + 2) = E(i + 2) * d0;
+  for (i = 3; i <= N; ++i) {
+    d1 = A(i - 2);
+    double d2 = (B(i - 1) - A(i - 2) * D(i - 1));
+    d0 = 1. / (Cc(i) - d2 * D(i) - d1 * E(i));
+    F(i) = (F(i) - d2 * F(i - 1) - d1 * F(i - 2)) * d0;
+    if (i <= N - 1) {
+      D(i + 1) = (D(i + 1) - d2 * E(i + 1)) * d0;
+      if (i <= N - 2) E(i + 2) = (E(i + 2)) * d0;
+    }
+  }
+  i = N - 1;
+  d1 = D(i + 1);
+  F(i) = F(i) - d1 * F(i + 1);
+  for (i = N - 2; i >= 1; --i) {
+    d1 = D(i + 1);
+    double d2 = E(i + 2);
+    F(i) = F(i) - d1 * F(i + 1) - d2 * F(i + 2);
+  }
+}
+
+/* lhs.f:1536-1816: pentadiagonal inversion along direction idir (1: j
+ * lines, m = j, n = k; 2: k lines, m = k, n = j) over m = ms..me, n = ns..ne */
+static void lhsinv(const P& p, A3 q, A3 s, A2 qn, A2 cn, A2 d2p, int ms, int me, int ns, int ne, int idir, A2 xn,
+                   A2 yn, A2 vnu, I2 iblank, A2 tscale, A2 bt) {
+  const int nq = p.nq, nmv = p.nmv;
+  const size_t L = (size_t)me + 3;
+  std::vector<double> jcbn(L), tscal(L), v1(L), v2(L), v3(L), g(L), atmp(L), btmp(L), ctmp(L), dtmp(L), etmp(L);
+  std::vector<double> a(L), b(L), c(L), d(L), e(L), f(L), a1(L), b1(L), c1(L), d1(L), e1(L), f1(L);
+  std::vector<double> diag(L * (nq + 1));
+  auto DG = [&](int m, int i) -> double& { return diag[(size_t)m * (nq + 1) + i]; };
+  const double dis2 = 10.0, dis4 = 0.1, Mp = p.Mp;
+  auto Q = [&](int m, int n, int v) -> double& { return idir == 1 ? q(m, n, v) : q(n, m, v); };
+  auto S = [&](int m, int n, int v) -> double& { return idir == 1 ? s(m, n, v) : s(n, m, v); };
+  auto X2 = [&](A2 a2, int m, int n) -> double& { return idir == 1 ? a2(m, n) : a2(n, m); };
+  auto IB = [&](int m, int n) { return idir == 1 ? iblank(m, n) : iblank(n, m); };
+  for (int n = ns; n <= ne; ++n) {
+    for (int m = ms; m <= me; ++m) {
+      jcbn[m] = Q(m, n, nq);
+      tscal[m] = X2(tscale, m, n);
+      g[m] = X2(d2p, m, n);
+      (void)IB(m, n);
+      const double btv = X2(bt, m, n);
+      const double bSq = (Mp * Mp) / (btv - (Mp * Mp) * (btv - 1));
+      const double qv = X2(qn, m, n), cv = X2(cn, m, n);
+      const double X = std::sqrt(((1. - bSq) * qv) * ((1. - bSq) * qv) + 4. * bSq * cv * cv);
+      DG(m, 1) = qv;
+      DG(m, 2) = qv;
+      DG(m, 3) = 0.5 * ((bSq + 1.) * qv + X);
+      DG(m, 4) = 0.5 * ((bSq + 1.) * qv - X);
+      DG(m, nq) = 0.5 * ((bSq + 1.) * std::fabs(qv) + X) / Q(m, n, nq);
+    }
+    for (int m = ms + 1; m <= me - 1; ++m) {
+      v1[m] = (X2(xn, m, n) * X2(xn, m, n) + X2(yn, m, n) * X2(yn, m, n)) / Q(m, n, nq);
+      v1[m] = v1[m] + (X2(xn, m + 1, n) * X2(xn, m + 1, n) + X2(yn, m + 1, n) * X2(yn, m + 1, n)) / Q(m + 1, n, nq);
+      v1[m] = v1[m] * Q(m, n, nq) * X2(vnu, m, n);
+      v3[m] = (X2(xn, m, n) * X2(xn, m, n) + X2(yn, m, n) * X2(yn, m, n)) / Q(m, n, nq);
+      v3[m] = v3[m] + (X2(xn, m - 1, n) * X2(xn, m - 1, n) + X2(yn, m - 1, n) * X2(yn, m - 1, n)) / Q(m - 1, n, nq);
+      v3[m] = v3[m] * Q(m, n, nq) * X2(vnu, m, n);
+      v2[m] = 0.5 * (v1[m] + v3[m]);
+    }
+    v1[ms] = v2[ms] = v3[ms] = 0;
+    v1[me] = v2[me] = v3[me] = 0;
+    auto dn = [&](int m) { return DG(m, nq); };
+    for (int m = ms + 3; m <= me - 3; ++m) {
+      const double c2 = 0.5 * ((g[m] + g[m + 1])) * dis2, c2m = 0.5 * ((g[m] + g[m - 1])) * dis2;
+      const double c4p = (dis4 - fmin2(dis4, .5 * dis2 * (g[m + 2] + g[m + 1])));
+      const double c4 = (dis4 - fmin2(dis4, 1. * c2)), c4m = (dis4 - fmin2(dis4, 1. * c2m));
+      const double c4m2 = (dis4 - fmin2(dis4, .5 * dis2 * (g[m - 2] + g[m - 1])));
+      atmp[m] = (dn(m + 1) + dn(m + 2)) * c4p;
+      btmp[m] = -((dn(m + 2) + dn(m + 1)) * c4p + (dn(m + 1) + dn(m)) * (3. * c4 + c2));
+      ctmp[m] = +((dn(m - 1) + dn(m)) * (3. * c4m + c2m) + (dn(m + 1) + dn(m)) * (3. * c4 + c2));
+      dtmp[m] = -((dn(m - 2) + dn(m - 1)) * c4m2 + (dn(m) + dn(m - 1)) * (3. * c4m + c2m));
+      etmp[m] = (dn(m - 1) + dn(m - 2)) * c4m2;
+    }
+    {
+      const int m = ms + 2;
+      const double c2 = 0.5 * ((g[m] + g[m + 1])) * dis2, c2m = 0.5 * ((g[m] + g[m - 1])) * dis2;
+      const double c4p = (dis4 - fmin2(dis4, .5 * dis2 * (g[m + 2] + g[m + 1])));
+      const double c4 = (dis4 - 1. * fmin2(dis4, c2)), c4m = (dis4 - fmin2(dis4, 1. * c2m));
+      const double c4m2 = (dis4 - fmin2(dis4, 1. * dis2 * (g[m - 1])));
+      atmp[m] = (dn(m + 1) + dn(m + 2)) * c4p;
+      btmp[m] = -((dn(m + 2) + dn(m + 1)) * c4p + (dn(m + 1) + dn(m)) * (3. * c4 + c2));
+      ctmp[m] = ((dn(m - 1) + dn(m)) * (3. * c4m + c2m) + (dn(m + 1) + dn(m)) * (3. * c4 + c2));
+      dtmp[m] = -((2. * dn(m - 1)) * c4m2 + (dn(m) + dn(m - 1)) * (3. * c4m + c2m));
+    }
+    {
+      const int m = ms + 1;
+      const double c2 = 0.5 * ((g[m] + g[m + 1])) * dis2, c2m = ((g[m])) * dis2;
+      const double c4p = (dis4 - fmin2(dis4, .5 * dis2 * (g[m + 2] + g[m + 1])));
+      const double c4 = (dis4 - fmin2(dis4, 1. * c2)), c4m = (dis4 - fmin2(dis4, 1. * c2m));
+      atmp[m] = (dn(m + 1) + dn(m + 2)) * c4p;
+      btmp[m] = -((dn(m + 2) + dn(m + 1)) * c4p + (dn(m + 1) + dn(m)) * (3. * c4 + c2));
+      ctmp[m] = (2. * (dn(m)) * (2. * c4m + c2m) + (dn(m + 1) + dn(m)) * (3. * c4 + c2));
+    }
+    {
+      const int m = me - 2;
+      const double c2 = 0.5 * ((g[m] + g[m + 1])) * dis2, c2m = 0.5 * ((g[m] + g[m - 1])) * dis2;
+      const double c4p = (dis4 - fmin2(dis4, 1. * dis2 * (g[m + 1])));
+      const double c4 = (dis4 - fmin2(dis4, 1. * c2)), c4m = (dis4 - fmin2(dis4, 1. * c2m));
+      const double c4m2 = (dis4 - fmin2(dis4, .5 * dis2 * (g[m - 2] + g[m - 1])));
+      btmp[m] = -(2. * (dn(m + 1)) * c4p + (dn(m + 1) + dn(m)) * (3. * c4 + c2));
+      ctmp[m] = ((dn(m - 1) + dn(m)) * (3. * c4m + c2m) + (dn(m + 1) + dn(m)) * (2. * c4 + c2));
+      dtmp[m] = -((dn(m - 2) + dn(m - 1)) * c4m2 + (dn(m) + dn(m - 1)) * (3. * c4m + c2m));
+      etmp[m] = (dn(m - 1) + dn(m - 2)) * c4m2;
+    }
+    {
+      const int m = me - 1;
+      const double c2 = ((g[m])) * dis2, c2m = 0.5 * ((g[m] + g[m - 1])) * dis2;
+      const double c4 = (dis4 - fmin2(dis4, 1. * c2)), c4m = (dis4 - fmin2(dis4, 1. * c2m));
+      const double c4m2 = (dis4 - fmin2(dis4, .5 * dis2 * (g[m - 2] + g[m - 1])));
+      ctmp[m] = +((dn(m - 1) + dn(m)) * (3. * c4m + c2m) + 2. * (dn(m)) * (2. * c4 + c2));
+      dtmp[m] = -((dn(m - 2) + dn(m - 1)) * c4m2 + (dn(m) + dn(m - 1)) * (3. * c4m + c2m));
+      etmp[m] = (dn(m - 1) + dn(m - 2)) * c4m2;
+    }
+    for (int m = ms; m <= me; ++m) {
+      atmp[m] = atmp[m] * jcbn[m]; btmp[m] = btmp[m] * jcbn[m]; ctmp[m] = ctmp[m] * jcbn[m];
+      dtmp[m] = dtmp[m] * jcbn[m]; etmp[m] = etmp[m] * jcbn[m];
+    }
+    for (int i = 1; i <= nmv; ++i) {
+      for (int m = ms; m <= me; ++m) {
+        a1[m] = atmp[m]; b1[m] = btmp[m]; c1[m] = ctmp[m]; d1[m] = dtmp[m]; e1[m] = etmp[m];
+        f1[m] = S(m, n, i);
+        b1[m] = b1[m] - DG(m, i) * 0.5;
+        d1[m] = d1[m] + DG(m, i) * 0.5;
+        b1[m] = b1[m] - 0.5 * v1[m];
+        c1[m] = c1[m] + v2[m];
+        d1[m] = d1[m] - 0.5 * v3[m];
+        a1[m] = (m <= me - 2) ? a1[m] * tscal[m + 2] : a1[m] * tscal[m];
+        b1[m] = (m <= me - 1) ? b1[m] * tscal[m + 1] : b1[m] * tscal[m];
+        d1[m] = (m >= ms + 1) ? d1[m] * tscal[m - 1] : d1[m] * tscal[m];
+        e1[m] = (m >= ms + 2) ? e1[m] * tscal[m - 2] : e1[m] * tscal[m];
+        c1[m] = c1[m] * tscal[m] + 1.0;
+      }
+      for (int m = ms + 1; m <= me - 1; ++m) {
+        a[m - ms] = a1[m]; b[m - ms] = b1[m]; c[m - ms] = c1[m];
+        d[m - ms] = d1[m]; e[m - ms] = e1[m]; f[m - ms] = f1[m];
+      }
+      const int N = me - ms - 1;
+      f[1] = f[1] - b1[ms] * f1[ms] / c1[ms];
+      f[N] = f[N] - d1[me] * f1[me] / c1[me];
+      d[1] = 0; e[1] = 0; e[2] = 0;
+      b[N] = 0; a[N] = 0; a[N - 1] = 0;
+      pentadag(&a[1], &b[1], &c[1], &d[1], &e[1], &f[1], N);
+      for (int m = ms + 1; m <= me - 1; ++m) S(m, n, i) = f[m - ms];
+    }
+  }
+}
+
+/* lhs.f:817-1057 (ilhs = 2).  The tmp coefficient arrays of lhsinv at m = ms
+ * and m = me are never assigned by the reference and are read as 0 here
+ * (what a fresh allocation holds). */
+void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, I2 iblank, A2 tscale, A2 bt) {
+  const int jd = p.jd, kd = p.kd, nq = p.nq;
+  const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
+  const size_t n2 = (size_t)jd * kd;
+  std::vector<double> buf(n2 * 11, 0.0);
+  int slot = 0;
+  auto mk = [&]() { return A2{buf.data() + n2 * (slot++), jd}; };
+  A2 pr = mk(), d2px = mk(), d2py = mk(), uv = mk(), vn = mk(), ge = mk(), qx = mk(), qy = mk(), cx = mk(), cy = mk();
+  const double gm1 = p.gm1, ggm1 = p.ggm1;
+  /* :853-860 conservative -> primitive (rho, u, v, e) */
+  for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js - 1; j <= je + 1; ++j) {
+    double dj = 1.0 / q(j, k, 1);
+    q(j, k, 2) = q(j, k, 2) * dj;
+    q(j, k, 3) = q(j, k, 3) * dj;
+    q(j, k, 4) = q(j, k, 4) * dj;
+    q(j, k, 1) = q(j, k, 1) * q(j, k, nq);
+  }
+  /* :863-917 multiply by T_xi inverse */
+  for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js - 1; j <= je + 1; ++j) {
+    double uu = q(j, k, 2), vv = q(j, k, 3);
+    double uv2 = 0.5 * (uu * uu + vv * vv);
+    double cjkl = std::sqrt(ggm1 * (q(j, k, 4) - uv2));
+    double c2i = 1.0 / (cjkl * cjkl);
+    pr(j, k) = (q(j, k, 4) - uv2) * gm1 * q(j, k, 1);
+    double rj1 = xx(j, k), rj2 = xy(j, k);
+    double qq1 = rj1 * uu + rj2 * vv;
+    qx(j, k) = qq1 - (rj1 * ug(j, k) + rj2 * vg(j, k));
+    double rr1 = std::sqrt(p2(rj1) + p2(rj2));
+    rj1 = rj1 / rr1; rj2 = rj2 / rr1;
+    double rk1 = yx(j, k), rk2 = yy(j, k);
+    double qq2 = rk1 * uu + rk2 * vv;
+    qy(j, k) = qq2 - (rk1 * ug(j, k) + rk2 * vg(j, k));
+    double rr2 = std::sqrt(p2(rk1) + p2(rk2));
+    rk1 = rk1 / rr2; rk2 = rk2 / rr2;
+    double vnu = (p.rmue + turmu(j, k)) / (p.rey * q(j, k, 1));
+    uv(j, k) = uv2;
+    cx(j, k) = cjkl * rr1;
+    cy(j, k) = cjkl * rr2;
+    vn(j, k) = vnu;
+    ge(j, k) = p.gamma * q(j, k, 4) - gm1 * uv2;
+    double a1 = s(j, k, 2) * uu + s(j, k, 3) * vv - s(j, k, 4);
+    a1 = a1 * gm1 * c2i;
+    a1 = a1 + s(j, k, 1) * (1.0 - uv2 * gm1 * c2i);
+    double a2 = (rj1 * vv - rj2 * uu) * s(j, k, 1) + rj2 * s(j, k, 2) - rj1 * s(j, k, 3);
+    double a3 = uv2 * s(j, k, 1) - s(j, k, 2) * uu - s(j, k, 3) * vv + s(j, k, 4);
+    a3 = a3 * gm1 * c2i;
+    double a4 = qq1 * s(j, k, 1) / rr1 - rj1 * s(j, k, 2) - rj2 * s(j, k, 3);
+    s(j, k, 1) = a1;
+    s(j, k, 2) = a2;
+    s(j, k, 3) = 0.5 * (a3 - a4 / cjkl);
+    s(j, k, 4) = 0.5 * (a3 + a4 / cjkl);
+  }
+  /* :919-935 */
+  for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js; j <= je; ++j) {
+    d2px(j, k) = std::fabs(pr(j + 1, k) - 2. * pr(j, k) + pr(j - 1, k));
+    d2px(j, k) = d2px(j, k) / std::fabs(pr(j + 1, k) + 2. * pr(j, k) + pr(j - 1, k));
+  }
+  for (int k = ks - 1; k <= ke + 1; ++k) { d2px(js - 1, k) = 0; d2px(je + 1, k) = 0; }
+  lhsinv(p, q, s, qx, cx, d2px, js - 1, je + 1, ks - 1, ke + 1, 1, xx, xy, vn, iblank, tscale, bt);
+  /* :948-975 multiply by N inverse */
+  for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js - 1; j <= je + 1; ++j) {
+    double cjkl = std::sqrt(ggm1 * (q(j, k, 4) - uv(j, k)));
+    double rj1 = xx(j, k), rj2 = xy(j, k), rr1 = std::sqrt(rj1 * rj1 + rj2 * rj2);
+    double rk1 = yx(j, k), rk2 = yy(j, k), rr2 = std::sqrt(rk1 * rk1 + rk2 * rk2);
+    double a1 = (rj1 * rk1 + rj2 * rk2) / rr1 / rr2;
+    double a2 = (rj1 * rk2 - rj2 * rk1) / rr1 / rr2;
+    double a4 = a1 * s(j, k, 2) + (cjkl * s(j, k, 3) - cjkl * s(j, k, 4)) * a2;
+    double a5 = -0.5 * (a2 * s(j, k, 2) / cjkl - (a1 + 1) * s(j, k, 3) + (a1 - 1) * s(j, k, 4));
+    double a6 = 0.5 * (a2 * s(j, k, 2) / cjkl - (a1 - 1) * s(j, k, 3) + (a1 + 1) * s(j, k, 4));
+    s(j, k, 2) = a4;
+    s(j, k, 3) = a5;
+    s(j, k, 4) = a6;
+  }
+  /* :977-993 */
+  for (int k = ks; k <= ke; ++k) for (int j = js - 1; j <= je + 1; ++j) {
+    d2py(j, k) = std::fabs(pr(j, k + 1) - 2. * pr(j, k) + pr(j, k - 1));
+    d2py(j, k) = d2py(j, k) / std::fabs(pr(j, k + 1) + 2. * pr(j, k) + pr(j, k - 1));
+  }
+  for (int j = js - 1; j <= je + 1; ++j) { d2py(j, ks - 1) = 0; d2py(j, ke + 1) = 0; }
+  lhsinv(p, q, s, qy, cy, d2py, ks - 1, ke + 1, js - 1, je + 1, 2, yx, yy, vn, iblank, tscale, bt);
+  /* :1005-1034 multiply by T_eta */
+  for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js - 1; j <= je + 1; ++j) {
+    double uu = q(j, k, 2), vv = q(j, k, 3);
+    double cjkl = std::sqrt(ggm1 * (q(j, k, 4) - uv(j, k)));
+    double rk1 = yx(j, k), rk2 = yy(j, k);
+    double qq2 = qy(j, k) + (rk1 * ug(j, k) + rk2 * vg(j, k));
+    double rr2 = std::sqrt(rk1 * rk1 + rk2 * rk2);
+    rk1 = rk1 / rr2; rk2 = rk2 / rr2;
+    double a1 = s(j, k, 1) + s(j, k, 3) + s(j, k, 4);
+    double a2 = uu * s(j, k, 1) + rk2 * s(j, k, 2) + (uu + rk1 * cjkl) * s(j, k, 3);
+    a2 = a2 + (uu - rk1 * cjkl) * s(j, k, 4);
+    double a3 = vv * s(j, k, 1) - rk1 * s(j, k, 2) + (vv + rk2 * cjkl) * s(j, k, 3);
+    a3 = a3 + (vv - rk2 * cjkl) * s(j, k, 4);
+    double a4 = uv(j, k) * s(j, k, 1) + (rk2 * uu - rk1 * vv) * s(j, k, 2);
+    a4 = a4 + (ge(j, k) + cjkl * qq2 / rr2) * s(j, k, 3);
+    a4 = a4 + (ge(j, k) - cjkl * qq2 / rr2) * s(j, k, 4);
+    s(j, k, 1) = a1; s(j, k, 2) = a2; s(j, k, 3) = a3; s(j, k, 4) = a4;
+  }
+  if (p.iunst == 2) {
+    for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js - 1; j <= je + 1; ++j) {
+      double a2 = s(j, k, 2), a3 = s(j, k, 3);
+      double a4 = 1.0 + p2(tscale(j, k) * p.rotf);
+      s(j, k, 2) = (a2 + tscale(j, k) * p.rotf * a3) / a4;
+      s(j, k, 3) = (a3 - tscale(j, k) * p.rotf * a2) / a4;
+    }
+  }
+  /* :1047-1054 primitive -> conservative */
+  for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js - 1; j <= je + 1; ++j) {
+    q(j, k, 1) = q(j, k, 1) / q(j, k, nq);
+    q(j, k, 2) = q(j, k, 2) * q(j, k, 1);
+    q(j, k, 3) = q(j, k, 3) * q(j, k, 1);
+    q(j, k, 4) = q(j, k, 4) * q(j, k, 1);
+  }
 }
 
 }  // namespace oro

@@ -13,8 +13,8 @@ namespace oro {
 static const double cb1 = 0.1355, sigma = 0.6666667, cb2 = 0.622, akt = 0.41, cw1 = 3.2390678;
 static const double cw2 = 0.3, cw3 = 2., cv1 = 7.1, ct3 = 1.2, ct4 = 0.5;
 
-/* samodel2d.f:200-240 */
-static void lamvis(const P& p, A3 q, A2 vmul) {
+/* samodel2d.f:200-240 (also called by komegasst, komegasst.f:49) */
+void lamvis(const P& p, A3 q, A2 vmul) {
   double c2b = 198.6 / p.tinf, c2bp = c2b + 1.;
   for (int k = 1; k <= p.kd; ++k) for (int j = 1; j <= p.jd; ++j) {
     double ra = 1. / q(j, k, 1);
@@ -25,8 +25,8 @@ static void lamvis(const P& p, A3 q, A2 vmul) {
   }
 }
 
-/* samodel2d.f:243-293 */
-static void dist(const P& p, A2 sn, A2 x, A2 y, const double* xv_, const double* yv_) {
+/* samodel2d.f:243-293 (kwdist, komegasst.f:218-268, is the same computation) */
+void dist(const P& p, A2 sn, A2 x, A2 y, const double* xv_, const double* yv_) {
   const int jd = p.jd, kd = p.kd, jmax = p.jmax, nhalo = p.nhalo;
   auto xv = [&](int j, int k) { return xv_[(size_t)(k - 1) * jmax + (j - 1)]; };
   auto yv = [&](int j, int k) { return yv_[(size_t)(k - 1) * jmax + (j - 1)]; };

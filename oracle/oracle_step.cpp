@@ -192,6 +192,17 @@ double oro_vmu_sa(const P* p, double* q, double* s, double* turmu, double* x, do
          v2(p, ug), v2(p, vg), v2(p, tscale), I2{iblank, p->jd}, &r);
   return r;
 }
+void oro_komegasst(const P* p, double* q, double* s, double* turmu, double* x, double* y, const double* xv,
+                   const double* yv, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+                   double* tscale, const int32_t* iblank, double* res) {
+  komegasst(*p, v3(p, q), v3(p, s), v2(p, turmu), v2(p, x), v2(p, y), xv, yv, v2(p, xx), v2(p, xy), v2(p, yx),
+            v2(p, yy), v2(p, ug), v2(p, vg), v2(p, tscale), I2{iblank, p->jd}, res);
+}
+void oro_arc2d(const P* p, double* q, double* s, double* xx, double* xy, double* yx, double* yy, double* ug,
+               double* vg, double* turmu, const int32_t* iblank, double* tscale, double* bt) {
+  arc2d(*p, v3(p, q), v3(p, s), v2(p, xx), v2(p, xy), v2(p, yx), v2(p, yy), v2(p, ug), v2(p, vg), v2(p, turmu),
+        I2{iblank, p->jd}, v2(p, tscale), v2(p, bt));
+}
 int oro_monitor(const P* p, double* q) {
   int n = 0;
   size_t n2 = (size_t)p->jd * p->kd;
@@ -268,6 +279,9 @@ int oro_step(const P* pp, double* q, double* s, double* x, double* y, const doub
     if (p.ilhs == 1) {
       ilu2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
             v2(pp, turmu + o), ts);
+    } else if (p.ilhs == 2) {
+      arc2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
+            v2(pp, turmu + o), I2{iblank + o, jd}, ts, v2(pp, bt + o));
     } else {
       std::fprintf(stderr, "oracle: ilhs=%d not restated\n", p.ilhs); std::abort();
     }
@@ -279,6 +293,10 @@ int oro_step(const P* pp, double* q, double* s, double* x, double* y, const doub
         vmu_sa(p, v3(pp, q + o), v3(pp, s + o), v2(pp, turmu + o), v2(pp, x + o), v2(pp, y + o), xv + (nsp - 1) * nvert,
                yv + (nsp - 1) * nvert, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o),
                v2(pp, vg + o), v2(pp, tscale + o), I2{iblank + o, jd}, nullptr);
+      } else if (p.iturb == 2) {
+        komegasst(p, v3(pp, q + o), v3(pp, s + o), v2(pp, turmu + o), v2(pp, x + o), v2(pp, y + o),
+                  xv + (nsp - 1) * nvert, yv + (nsp - 1) * nvert, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o),
+                  v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o), v2(pp, tscale + o), I2{iblank + o, jd}, nullptr);
       } else {
         std::fprintf(stderr, "oracle: iturb=%d not restated\n", p.iturb); std::abort();
       }

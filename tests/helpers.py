@@ -12,12 +12,12 @@ class Case:
     """All arrays of one single-instance (nspec=1) case in reference layout."""
 
     def __init__(self, jmax=65, kmax=25, viscous=False, ilim=1, irhsy=-3, seed=0, naca=(0.0, 0.0, 0.12),
-                 perturb=0.02, alfa=2.0, fsmach=0.5, rey=1e6, ds_wall=None, n_wake=None, istep0=10):
+                 perturb=0.02, alfa=2.0, fsmach=0.5, rey=1e6, ds_wall=None, n_wake=None, istep0=10, iturb=1):
         if ds_wall is None:
             ds_wall = 2e-3 if not viscous else 1e-4
         kw = dict(irhsy=irhsy, ilim=ilim, ilhs=1, iconstant_cfl=1, fsmach=fsmach, alfa=alfa)
         if viscous:
-            kw.update(invisc=0, lamin=0, iturb=1, dt=50.0, rey=rey, vnuinf=3.0)
+            kw.update(invisc=0, lamin=0, iturb=iturb, dt=50.0, rey=rey, vnuinf=3.0)
         else:
             kw.update(invisc=1, lamin=1, dt=10.0)
         self.inp, _, xv, yv = api.cmesh_case(jmax, kmax, n_wake=n_wake, naca=naca, ds_wall=ds_wall, **kw)
@@ -64,8 +64,13 @@ class Case:
         q[1] = rho * u / J
         q[2] = rho * v / J
         q[3] = e / J
-        if p.iturb == 1:
+        if not p.lamin and p.iturb == 1:
             q[4] = p.vnuinf * (1.0 + 50.0 * rng.uniform(0, 1, n2))
+            self.turmu[:] = 0.1 * rng.uniform(0, 1, n2)
+        elif not p.lamin and p.iturb == 2:
+            # k and omega (times rho) spread over decades around freestream
+            q[4] = rho * p.tkeinf * 10.0 ** rng.uniform(0, 3, n2)
+            q[5] = rho * p.tomegainf * 10.0 ** rng.uniform(0, 3, n2)
             self.turmu[:] = 0.1 * rng.uniform(0, 1, n2)
         self.tscale[:] = 0.0
 

@@ -122,6 +122,43 @@ def test_vmu_sa():
     assert relerr(t, to) <= TOL
 
 
+def test_komegasst():
+    """komegasst (k-omega SST, komegasst.f:2-187) on a perturbed state,
+    drop-in against the oracle; the BC ramp is mid-way (istep0 = 10)."""
+    c = Case(viscous=True, seed=17, iturb=2)
+    L = ob.lib()
+    L.oro_time_step(_o(c), ob.ptr(c.q), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug),
+                    ob.ptr(c.vg), ob.ptr(c.tscale), ob.ptr(c.bt), ob.ptr(c.iblank))
+    so = np.random.default_rng(5).uniform(-1, 1, c.n2 * c.p.nv) * 1e-6
+    s = so.copy()
+    qo, q, to, t = c.q.copy(), c.q.copy(), c.turmu.copy(), c.turmu.copy()
+    L.oro_komegasst(_o(c), ob.ptr(qo), ob.ptr(so), ob.ptr(to), ob.ptr(c.x), ob.ptr(c.y), ob.ptr(c.xv), ob.ptr(c.yv),
+                    ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug), ob.ptr(c.vg),
+                    ob.ptr(c.tscale), ob.ptr(c.iblank), None)
+    rt.set_params(c.p)
+    rt.komegasst(q, s, t, c.x, c.y, c.xv, c.yv, c.xx, c.xy, c.yx, c.yy, c.ug, c.vg, c.jd, c.kd, c.tscale, c.iblank, 1)
+    kw = slice(4 * c.n2, 6 * c.n2)
+    assert not np.array_equal(qo[kw], c.q[kw])
+    assert relerr(q[kw], qo[kw]) <= TOL
+    assert relerr(t, to) <= TOL
+    assert relerr(s[kw], so[kw]) <= TOL
+
+
+def test_solver_sst_fp64_matches_oracle():
+    """The batched solver on a k-omega SST case (cambered NACA 2412, WENO +
+    Roe, LU-SGS), 40 iterations, FP64, against the oracle driver."""
+    _, prm, xv, yv = api.cmesh_case(97, 33, naca=(0.02, 0.4, 0.12), ds_wall=1e-3, invisc=0, lamin=0, iturb=2,
+                                    irhsy=-3, ilim=4, ilhs=1, iconstant_cfl=1, dt=20.0, fsmach=0.73, alfa=2.8,
+                                    rey=6.5e6)
+    r, q, hist, forces, q_o = _solver_vs_oracle(prm, xv, yv, 40, OT2D_FP64)
+    assert r.status == 0 and r.iterations == 40
+    assert abs(r.rsum_last - hist[-1, 0]) <= 1e-10 * hist[-1, 0]
+    assert relerr(q, q_o) <= 1e-10
+    f = forces[0]
+    for a, b in ((r.cl, f[0]), (r.cd, f[1]), (r.cm, f[2])):
+        assert abs(a - b) <= 1e-10 * max(abs(b), 1e-3)
+
+
 def _full_arrays(c):
     return dict(q=c.q.copy(), s=np.zeros(c.n2 * c.p.nv), turmu=c.turmu.copy(), tscale=np.zeros(c.n2),
                 bt=np.zeros(c.n2))

@@ -111,6 +111,15 @@ def config_c2(jmax=513, kmax=129, fsmach=0.15, alfa=10.0, rey=6e6, naca=(0.0, 0.
                       rey=rey, vnuinf=3.0)
 
 
+def wall_spacing(kmax, r_far=20.0, ratio=1.2, floor=1e-6):
+    """First-cell wall spacing of a C-mesh with kmax points across: the
+    spacing whose geometric stretching at `ratio` reaches the far field, but
+    not below `floor` (1e-6 chords, y+ < 1 at Re ~ 1e7).  Coarse meshes with
+    a 1e-6 spacing would need stretching ratios above 1.3, on which the SA
+    solve diverges (the oracle does the same)."""
+    return max(floor, r_far * (ratio - 1.0) / (ratio ** (kmax - 1) - 1.0))
+
+
 def config_c4_sample(rng, sizes=((129, 33), (257, 65), (385, 97), (513, 129), (769, 193))):
     """One seeded batched-SA request: NACA m in U[0,0.06], p in U[0.2,0.6],
     t in U[0.08,0.18]; size from `sizes`; M in U[0.3,0.85], alpha in U[-2,8],
@@ -118,7 +127,7 @@ def config_c4_sample(rng, sizes=((129, 33), (257, 65), (385, 97), (513, 129), (7
     jmax, kmax = sizes[int(rng.integers(len(sizes)))]
     m, pp, t = rng.uniform(0, 0.06), rng.uniform(0.2, 0.6), rng.uniform(0.08, 0.18)
     M, a, Re = rng.uniform(0.3, 0.85), rng.uniform(-2.0, 8.0), rng.uniform(1e6, 1e7)
-    return config_c2(jmax, kmax, fsmach=M, alfa=a, rey=Re, naca=(m, pp, t), ds_wall=1e-6)
+    return config_c2(jmax, kmax, fsmach=M, alfa=a, rey=Re, naca=(m, pp, t), ds_wall=wall_spacing(kmax))
 
 
 def config_c5_ts(rng, nspec=None):
@@ -128,7 +137,7 @@ def config_c5_ts(rng, nspec=None):
     if nspec is None:
         nspec = int(rng.choice([3, 5, 7]))
     a0, k = rng.uniform(0.0, 10.0), rng.uniform(0.05, 0.15)
-    return cmesh_case(257, 65, naca=(0.0, 0.0, 0.12), ds_wall=1e-6, invisc=0, lamin=0, iturb=1,
+    return cmesh_case(257, 65, naca=(0.0, 0.0, 0.12), ds_wall=wall_spacing(65), invisc=0, lamin=0, iturb=1,
                       irhsy=-3, ilim=1, ilhs=1, iconstant_cfl=1, dt=50.0, fsmach=0.3, alfa=a0, rey=6e6,
                       vnuinf=3.0, timespectral=1, nspec=nspec, rf=k, angmax=5.0, xac=0.25, motiontype=1)
 

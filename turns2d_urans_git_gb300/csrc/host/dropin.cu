@@ -24,6 +24,10 @@ std::map<uintptr_t, Reg> g_reg;
 
 struct Staged { void* host; void* dev; size_t bytes; bool out; };
 
+// scratch arrays per slice of a drop-in call (the k-omega SST solve is the
+// largest user: SST_NSCRATCH)
+constexpr size_t DW_SLOTS = SST_NSCRATCH + 1;
+
 struct Ctx {
   ot2d_params P{};
   bool has = false;
@@ -123,7 +127,7 @@ int prepare(int nslice, int& err) {
   if (!g_ctx.has) return err = OT2D_ERR_NOPARAMS;
   const size_t n2 = (size_t)g_ctx.P.jd * g_ctx.P.kd, ws = (n2 + 63) / 64 * 64;
   const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd);
-  const size_t need = ws * 20 * nslice + 8 * ws + rec * nslice;
+  const size_t need = ws * DW_SLOTS * nslice + 8 * ws + rec * nslice;
   g_ctx.nslice = nslice;
   if (need > g_ctx.wcap) {
     if (g_ctx.dwork) cudaFree(g_ctx.dwork);
@@ -136,15 +140,31 @@ int prepare(int nslice, int& err) {
 }
 
 // A slice over caller arrays (one time instance, variable stride qs).
+bool sst_params(const ot2d_params& p) { return !p.lamin && p.iturb == 2; }
+
+// k-omega SST geometry of one instance: sn = 1e10 on meshes without a wall
+// (kwdist runs only with one, komegasst.f:67), and the wall term dely2
+// uploaded to d_wd2
+void sst_geometry(const ot2d_params& p, const double* x, const double* y, const double* xv, const double* yv,
+                  double* sn, double* d_wd2, int& err) {
+  const size_t n2 = (size_t)p.jd * p.kd;
+  bool body = false;
+  for (int ib = 0; ib < p.nbc; ++ib) if (p.ibtyp[ib] == 5) body = true;
+  if (!body) for (size_t i = 0; i < n2; ++i) sn[i] = 1.e10;
+  std::vector<double> wd2(n2);
+  sst_wall_d2(p, x, y, xv, yv, wd2.data());
+  if (!err && cudaMemcpy(d_wd2, wd2.data(), n2 * 8, cudaMemcpyHostToDevice) != cudaSuccess) err = OT2D_ERR_CUDA;
+}
+
 Slice<double> base_slice(int nsp, int nspec, int64_t qs) {
   Slice<double> S{};
   const ot2d_params& p = g_ctx.P;
   S.P = g_ctx.dP;
   S.jd = p.jd; S.kd = p.kd; S.nsp = nsp; S.nspec = nspec; S.qs = qs;
   const size_t n2 = (size_t)p.jd * p.kd, ws = (n2 + 63) / 64 * 64;
-  S.w = g_ctx.dwork + (size_t)(nsp - 1) * ws * 20;
+  S.w = g_ctx.dwork + (size_t)(nsp - 1) * ws * DW_SLOTS;
   S.wstride = (int64_t)ws;
-  S.lurec = g_ctx.dwork + ws * 20 * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
+  S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = g_ctx.dred + (size_t)RED_N * (nsp - 1);
   S.ist = nullptr;
   return S;
@@ -248,7 +268,7 @@ int ot2d_rhsup(double* q, double* s, double* xx, double* xy, double* yx, double*
   const size_t n2 = (size_t)p.jd * p.kd;
   Slice<double> S = base_slice(1, 1, (int64_t)n2);
   const size_t ws = (size_t)S.wstride;
-  double* faces = g_ctx.dwork + ws * 20;           // 4 face-normal arrays
+  double* faces = g_ctx.dwork + ws * DW_SLOTS;           // 4 face-normal arrays
   double* tjs = faces + 4 * ws;                     // 2 face-speed arrays
   faces_upload(faces, tjs, xv, yv, ugv, vgv, ws, err);
   S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, false, err);
@@ -391,7 +411,7 @@ int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, doubl
   const size_t n2 = (size_t)p.jd * p.kd, nv = (size_t)p.jmax * p.kmax;
   Slice<double> S = base_slice(1, 1, (int64_t)n2);
   const size_t ws = (size_t)S.wstride;
-  double* dsn = g_ctx.dwork + ws * 20;
+  double* dsn = g_ctx.dwork + ws * DW_SLOTS;
   {
     std::vector<double> hx = host_copy(x, n2), hy = host_copy(y, n2), hxv = host_copy(xv, nv), hyv = host_copy(yv, nv);
     std::vector<double> sn(n2);
@@ -413,6 +433,47 @@ int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, doubl
   std::vector<Slice<double>> sl{S};
   run_batch(sl, err);
   if (!err && launch_sa<double>(g_ctx.batch.d_sl, g_ctx.batch.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_komegasst(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
+                   double* xy, double* yx, double* yy, double* ug, double* vg, int32_t* jd, int32_t* kd,
+                   double* tscale, int32_t* iblank, int32_t* im) {
+  (void)im;
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !sst_params(p) || p.itrans != 0 || !q || !s || !turmu || !x || !y || !xv || !yv || !tscale ||
+      !iblank)
+    return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, nv = (size_t)p.jmax * p.kmax;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  const size_t ws = (size_t)S.wstride;
+  double* dsn = g_ctx.dwork + ws * DW_SLOTS;
+  double* dwd2 = dsn + ws;
+  {
+    std::vector<double> hx = host_copy(x, n2), hy = host_copy(y, n2), hxv = host_copy(xv, nv), hyv = host_copy(yv, nv);
+    std::vector<double> sn(n2);
+    wall_distance(p, hx.data(), hy.data(), hxv.data(), hyv.data(), sn.data());
+    sst_geometry(p, hx.data(), hy.data(), hxv.data(), hyv.data(), sn.data(), dwd2, err);
+    if (!err && cudaMemcpy(dsn, sn.data(), n2 * 8, cudaMemcpyHostToDevice) != cudaSuccess) err = OT2D_ERR_CUDA;
+  }
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
+  S.turmu = (double*)resolve(turmu, n2 * 8, true, true, err);
+  S.xx = S.xx64 = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = S.xy64 = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = S.yx64 = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = S.yy64 = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug = S.ug64 = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg = S.vg64 = (double*)resolve(vg, n2 * 8, true, false, err);
+  S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
+  S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
+  S.sn = dsn;
+  S.wd2 = dwd2;
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_sst<double>(g_ctx.batch.d_sl, g_ctx.batch.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   return finish(err);
 }
 
@@ -445,7 +506,8 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   int err = 0;
   if (prepare(nspec, err)) return fail(err);
   const ot2d_params& p = g_ctx.P;
-  if (!dims_ok(jd, kd) || p.ilhs != 1 || p.itnmax > 1 || (!p.lamin && p.iturb != 1)) return fail(OT2D_ERR_ARG);
+  if (!dims_ok(jd, kd) || p.ilhs != 1 || p.itnmax > 1 || (!p.lamin && p.iturb != 1 && p.iturb != 2) || p.itrans != 0)
+    return fail(OT2D_ERR_ARG);
   if (!q || !s || !x || !y || !xv || !yv || !iblank || !xx || !xy || !yx || !yy || !turmu || !tscale) return fail(OT2D_ERR_ARG);
   if (p.timespectral && (!ugv || !vgv || !ug || !vg || !Ds)) return fail(OT2D_ERR_ARG);
   const size_t n2 = (size_t)p.jd * p.kd, ns = (size_t)nspec, nv = (size_t)p.jmax * p.kmax, qs = n2 * ns;
@@ -464,17 +526,20 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   // per-instance face normals and wall distance from the host grid
   const size_t ws = (n2 + 63) / 64 * 64;
   double* extra = nullptr;
-  if (!err && cudaMalloc(&extra, sizeof(double) * ws * 7 * ns) != cudaSuccess) err = OT2D_ERR_NOMEM;
+  if (!err && cudaMalloc(&extra, sizeof(double) * ws * 8 * ns) != cudaSuccess) err = OT2D_ERR_NOMEM;
   if (extra) g_ctx.pool.push_back(extra);
   std::vector<Slice<double>> sl;
   std::vector<double> hx = host_copy(x, qs), hy = host_copy(y, qs), hxv = host_copy(xv, nv * ns), hyv = host_copy(yv, nv * ns);
   for (int nsp = 1; nsp <= nspec && !err; ++nsp) {
-    double* e = extra + (size_t)(nsp - 1) * ws * 7;
+    double* e = extra + (size_t)(nsp - 1) * ws * 8;
     faces_upload(e, e + 4 * ws, xv + (nsp - 1) * nv, yv + (nsp - 1) * nv, ugv ? ugv + (nsp - 1) * nv : nullptr,
                  vgv ? vgv + (nsp - 1) * nv : nullptr, ws, err);
     std::vector<double> sn(n2);
     wall_distance(p, hx.data() + (nsp - 1) * n2, hy.data() + (nsp - 1) * n2, hxv.data() + (nsp - 1) * nv,
                   hyv.data() + (nsp - 1) * nv, sn.data());
+    if (sst_params(p))
+      sst_geometry(p, hx.data() + (nsp - 1) * n2, hy.data() + (nsp - 1) * n2, hxv.data() + (nsp - 1) * nv,
+                   hyv.data() + (nsp - 1) * nv, sn.data(), e + 7 * ws, err);
     if (cudaMemcpy(e + 6 * ws, sn.data(), n2 * 8, cudaMemcpyHostToDevice) != cudaSuccess) err = OT2D_ERR_CUDA;
     Slice<double> S = base_slice(nsp, nspec, (int64_t)qs);
     const size_t o = (size_t)(nsp - 1) * n2;
@@ -486,17 +551,19 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
     S.fxa = e; S.fya = e + ws; S.gxa = e + 2 * ws; S.gya = e + 3 * ws;
     S.ftj = p.timespectral ? e + 4 * ws : nullptr; S.gtj = p.timespectral ? e + 5 * ws : nullptr;
     S.sn = e + 6 * ws;
+    S.wd2 = sst_params(p) ? e + 7 * ws : nullptr;
     S.Ds = dDs;
     sl.push_back(S);
   }
   run_batch(sl, err);
   const auto& B = g_ctx.batch;
-  const int visc = p.invisc ? 0 : 1, turb = (!p.lamin && p.iturb == 1) ? 1 : 0;
+  const int visc = p.invisc ? 0 : 1, turb = (!p.lamin && p.iturb == 1) ? 1 : 0, sst = sst_params(p) ? 1 : 0;
   if (!err && launch_bc<double>(B.d_sl, B.b, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_residual<double>(B.d_sl, B.b, visc, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_rbc<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_lusgs<double>(B.d_sl, B.b, 1, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && turb && launch_sa<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && sst && launch_sst<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_update<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err) {
     std::vector<double> red((size_t)RED_N * nspec);

@@ -209,6 +209,39 @@ void wall_distance(const ot2d_params& p, const double* x_, const double* y_, con
   }
 }
 
+void sst_wall_d2(const ot2d_params& p, const double* x_, const double* y_, const double* xv_, const double* yv_,
+                 double* wd2_) {
+  const int jd = p.jd, kd = p.kd, nh = p.nhalo;
+  C2 wd2{wd2_, jd};
+  C2 x{const_cast<double*>(x_), jd}, y{const_cast<double*>(y_), jd};
+  V2 xv{xv_, p.jmax}, yv{yv_, p.jmax};
+  for (int k = 1; k <= kd; ++k)
+    for (int j = 1; j <= jd; ++j) wd2(j, k) = 0.0;
+  for (int ib = 0; ib < p.nbc; ++ib) {
+    if (p.ibtyp[ib] != 5) continue;
+    int js, je, ks, ke;
+    bc_cells(p, ib, js, je, ks, ke);
+    const int idir = p.ibdir[ib], iadd = isgn(idir), iadir = idir < 0 ? -idir : idir;
+    if (iadir == 1) {
+      const int j = (idir == 1) ? je : js, j1 = j + iadd, jv = j1 - nh;
+      for (int k = ks; k <= ke; ++k) {
+        const int kv = k - nh;
+        const double dx = x(j1, k) - 0.5 * (xv(jv, kv) + xv(jv, kv + 1));
+        const double dy = y(j1, k) - 0.5 * (yv(jv, kv) + yv(jv, kv + 1));
+        wd2(j, k) = dx * dx + dy * dy;
+      }
+    } else if (iadir == 2) {
+      const int k = (idir == 2) ? ke : ks, k1 = k + iadd, kv = k1 - nh;
+      for (int j = js; j <= je; ++j) {
+        const int jv = j - nh;
+        const double dx = x(j, k1) - 0.5 * (xv(jv, kv) + xv(jv + 1, kv));
+        const double dy = y(j, k1) - 0.5 * (yv(jv, kv) + yv(jv + 1, kv));
+        wd2(j, k) = dx * dx + dy * dy;
+      }
+    }
+  }
+}
+
 void face_normals(const ot2d_params& p, const double* xv_, const double* yv_, const double* ugv_, const double* vgv_,
                   double* fxa_, double* fya_, double* gxa_, double* gya_, double* ftj_, double* gtj_) {
   const int jd = p.jd, nh = p.nhalo;

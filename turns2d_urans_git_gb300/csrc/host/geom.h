@@ -12,6 +12,11 @@ void cell_centres(const ot2d_params& p, const double* xv, const double* yv, doub
 int metrics(const ot2d_params& p, const double* xv, const double* yv, double* J, double* xx, double* xy, double* yx,
             double* yy);
 void wall_distance(const ot2d_params& p, const double* x, const double* y, const double* xv, const double* yv, double* sn);
+// dely2 of komegabc_wall (komegasst.f:1000-1007, :1042-1049) on every wall
+// halo cell (squared distance from the first interior cell centre to the
+// wall face midpoint); 0 elsewhere
+void sst_wall_d2(const ot2d_params& p, const double* x, const double* y, const double* xv, const double* yv,
+                 double* wd2);
 void face_normals(const ot2d_params& p, const double* xv, const double* yv, const double* ugv, const double* vgv,
                   double* fxa, double* fya, double* gxa, double* gya, double* ftj, double* gtj);
 void ts_pitch_grid(const ot2d_params& p, const double* xv1, const double* yv1, double tspec, double* xv, double* yv);

@@ -20,7 +20,10 @@ const char* cuda_err_name(cudaError_t e) { return cudaGetErrorName(e); }
 namespace {
 constexpr size_t ALIGN = 256;
 inline size_t al(size_t b) { return (b + ALIGN - 1) / ALIGN * ALIGN; }
-constexpr int NSCRATCH = 20;  // scratch arrays per slice (residual phase is the largest user)
+// scratch arrays per time instance: the SA bands (9) and the drop-in face
+// fluxes (20) fit in 20; the k-omega SST fields and two-equation bands take 27
+inline int nscratch(const ot2d_params& p) { return (!p.lamin && p.iturb == 2) ? SST_NSCRATCH + 1 : 20; }
+inline bool is_sst(const ot2d_params& p) { return !p.lamin && p.iturb == 2; }
 
 struct Layout {
   size_t total = 0;
@@ -68,7 +71,8 @@ size_t plan(const ot2d_params& p, int precision, F&& assign) {
   assign("bt", L.take(rb * n2 * nspec));
   assign("turmu", L.take(rb * n2 * nspec));
   assign("sn", L.take(rb * n2 * nspec));
-  assign("w", L.take(rb * ws * NSCRATCH * nspec));
+  assign("w", L.take(rb * ws * nscratch(p) * nspec));
+  if (is_sst(p)) assign("wd2", L.take(sizeof(double) * n2 * nspec));
   assign("lurec", L.take(rb * (size_t)lu_rec_elems(p.jd, p.kd) * nspec));
   return L.total;
 }
@@ -96,7 +100,8 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
   if (!xv1 || !yv1 || p.nspec < 1 || p.nhalo != 1 || p.jd != p.jmax + 1 || p.kd != p.kmax + 1) return OT2D_ERR_ARG;
   if (precision != OT2D_FP64 && precision != OT2D_FP32_MIXED) return OT2D_ERR_ARG;
   if (p.ilhs != 1) return OT2D_ERR_ARG;            // ADI operator: not in this build
-  if (!p.lamin && p.iturb != 1) return OT2D_ERR_ARG;  // SA only
+  if (!p.lamin && p.iturb != 1 && p.iturb != 2) return OT2D_ERR_ARG;  // SA or k-omega SST
+  if (p.itrans != 0) return OT2D_ERR_ARG;                            // no transition model
   d = DevSolve{};
   d.P = p; d.precision = precision; d.nspec = p.nspec;
   d.n2 = (size_t)p.jd * p.kd; d.nvert = (size_t)p.jmax * p.kmax; d.wstride = (d.n2 + 63) / 64 * 64;
@@ -139,6 +144,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     else if (n == "sn") d.sn = ptr;
     else if (n == "w") d.w = ptr;
     else if (n == "lurec") d.lurec = ptr;
+    else if (n == "wd2") d.wd2 = (double*)ptr;
   }
   const bool mixed = precision == OT2D_FP32_MIXED;
   if (!mixed) { d.q = d.q64; d.xx = d.xx64; d.xy = d.xy64; d.yx = d.yx64; d.yy = d.yy64; d.ug = d.ug64; d.vg = d.vg64; }
@@ -148,7 +154,10 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
   std::vector<double> q(qs * p.nq, 0.0), xx(qs), xy(qs), yx(qs), yy(qs), ug(qs, 0.0), vg(qs, 0.0);
   std::vector<double> xv(nv * ns), yv(nv * ns), ugv(nv * ns, 0.0), vgv(nv * ns, 0.0);
   std::vector<double> x(n2), y(n2), sn(qs), fxa(qs), fya(qs), gxa(qs), gya(qs), ftj(qs, 0.0), gtj(qs, 0.0);
-  std::vector<double> Ds(ns * ns, 0.0);
+  std::vector<double> Ds(ns * ns, 0.0), wd2(is_sst(p) ? qs : 0);
+  d.nscratch = nscratch(p);
+  bool body = false;
+  for (int ib = 0; ib < p.nbc; ++ib) if (p.ibtyp[ib] == 5) body = true;
   const double pi = 4.0 * std::atan(1.0);
   if (p.timespectral) ts_operator(p.nspec, Ds.data());
   for (int nsp = 1; nsp <= p.nspec; ++nsp) {
@@ -170,6 +179,11 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
                     vgv.data() + (nsp - 1) * nv);
     freestream(p, q.data() + o, qs);
     wall_distance(p, x.data(), y.data(), xvn, yvn, sn.data() + o);
+    if (is_sst(p)) {
+      // kwdist runs only for meshes with a wall (komegasst.f:67); 1e10 otherwise
+      if (!body) for (size_t i = 0; i < n2; ++i) sn[o + i] = 1.e10;
+      sst_wall_d2(p, x.data(), y.data(), xvn, yvn, wd2.data() + o);
+    }
     face_normals(p, xvn, yvn, ugv.data() + (nsp - 1) * nv, vgv.data() + (nsp - 1) * nv, fxa.data() + o, fya.data() + o,
                  gxa.data() + o, gya.data() + o, p.timespectral ? ftj.data() + o : nullptr,
                  p.timespectral ? gtj.data() + o : nullptr);
@@ -187,6 +201,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     chk(cudaMemcpyAsync(d.vg64, vg.data(), qs * 8, cudaMemcpyHostToDevice, st));
     chk(cudaMemcpyAsync(d.Ds, Ds.data(), ns * ns * 8, cudaMemcpyHostToDevice, st));
   }
+  if (d.wd2) chk(cudaMemcpyAsync(d.wd2, wd2.data(), qs * 8, cudaMemcpyHostToDevice, st));
   chk(cudaMemcpyAsync(d.xv, xv.data(), xv.size() * 8, cudaMemcpyHostToDevice, st));
   chk(cudaMemcpyAsync(d.yv, yv.data(), yv.size() * 8, cudaMemcpyHostToDevice, st));
   std::vector<int32_t> ib(qs, 1);
@@ -242,7 +257,8 @@ Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
   S.tscale = R_(d.tscale); S.bt = R_(d.bt); S.turmu = R_(d.turmu);
   S.iblank = d.iblank + o;
   S.sn = R_(d.sn);
-  S.w = (R*)d.w + (size_t)(nsp - 1) * d.wstride * NSCRATCH;
+  S.w = (R*)d.w + (size_t)(nsp - 1) * d.wstride * d.nscratch;
+  S.wd2 = D_(d.wd2);
   S.wstride = (int64_t)d.wstride;
   S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = red; S.ist = ist;

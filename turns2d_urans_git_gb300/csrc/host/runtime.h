@@ -36,6 +36,8 @@ struct DevSolve {
   void *fxa = nullptr, *fya = nullptr, *gxa = nullptr, *gya = nullptr, *ftj = nullptr, *gtj = nullptr;
   void *ug = nullptr, *vg = nullptr, *tscale = nullptr, *bt = nullptr, *turmu = nullptr, *sn = nullptr, *w = nullptr;
   void* lurec = nullptr;
+  double* wd2 = nullptr;   // SST wall term (k-omega SST instances only)
+  int nscratch = 0;        // scratch arrays per time instance
 };
 
 // bytes one solve needs on the device

@@ -57,7 +57,8 @@ struct ot2d_solver {
   int check_every = 25;
   int keep_q = 0;
   int since_check = 0;
-  bool any_viscous = false, any_turb = false;
+  bool any_viscous = false;
+  int turb_bits = 0;   // 1: some SA instance, 2: some SST instance
   double* d_forces = nullptr; size_t forces_cap = 0;
   DevBatch<double> f64;
   DevBatch<float> f32;
@@ -111,21 +112,22 @@ template <class R>
 int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   drop_graph(s);
   std::vector<Slice<R>> sl;
-  s->any_viscous = false; s->any_turb = false;
+  s->any_viscous = false; s->turb_bits = 0;
   for (int id : s->live) {
     const Rec& r = s->recs[id];
     slices_of<R>(s, r, sl);
     if (!r.d.P.invisc) s->any_viscous = true;
-    if (!r.d.P.lamin && r.d.P.iturb == 1) s->any_turb = true;
+    if (!r.d.P.lamin && r.d.P.iturb == 1) s->turb_bits |= 1;
+    if (!r.d.P.lamin && r.d.P.iturb == 2) s->turb_bits |= 2;
   }
   s->dirty = false;
   if (sl.empty()) return OT2D_OK;
   int e = B.build(sl, s->st);
   if (e) return e;
-  // The kernels branch on each slice's own params, so inviscid, laminar and
-  // SA requests can share one batch.
+  // The kernels branch on each slice's own params, so inviscid, laminar,
+  // SA and SST requests can share one batch.
   if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
-  cudaError_t le = launch_iteration<R>(B.d_sl, B.b, s->any_viscous ? 1 : 0, s->any_turb ? 1 : 0, s->st);
+  cudaError_t le = launch_iteration<R>(B.d_sl, B.b, s->any_viscous ? 1 : 0, s->turb_bits, s->st);
   cudaError_t ce = cudaStreamEndCapture(s->st, &s->graph);
   if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
   if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
@@ -194,7 +196,7 @@ int profile_t(ot2d_solver* s, DevBatch<R>& B, int iters, double* ms) {
   cudaEvent_t ev[OT2D_NPHASE + 1];
   for (auto& e : ev) cudaEventCreate(&e);
   for (int p = 0; p < OT2D_NPHASE; ++p) ms[p] = 0.0;
-  const int visc = s->any_viscous ? 1 : 0, turb = s->any_turb ? 1 : 0;
+  const int visc = s->any_viscous ? 1 : 0, turb = s->turb_bits;
   int err = OT2D_OK;
   for (int it = 0; it < iters && !err; ++it) {
     cudaError_t e = cudaSuccess;
@@ -205,7 +207,9 @@ int profile_t(ot2d_solver* s, DevBatch<R>& B, int iters, double* ms) {
     if (!e) e = launch_residual<R>(B.d_sl, B.b, visc, s->st); rec(3);
     if (!e) e = launch_rbc<R>(B.d_sl, B.b, s->st); rec(4);
     if (!e) e = launch_lusgs<R>(B.d_sl, B.b, 1, s->st); rec(5);
-    if (!e && turb) e = launch_sa<R>(B.d_sl, B.b, s->st); rec(6);
+    if (!e && (turb & 1)) e = launch_sa<R>(B.d_sl, B.b, s->st);
+    if (!e && (turb & 2)) e = launch_sst<R>(B.d_sl, B.b, s->st);
+    rec(6);
     if (!e) e = launch_update<R>(B.d_sl, B.b, s->st);
     rec(7);
     if (e != cudaSuccess || cudaEventSynchronize(ev[7]) != cudaSuccess) { err = OT2D_ERR_CUDA; break; }

@@ -28,7 +28,8 @@ struct Slice {
   const R *ug, *vg;                  // cell grid velocities, null if steady
   R *tscale, *bt, *turmu;
   const int32_t* iblank;
-  const R* sn;                       // SA wall distance (static geometry)
+  const R* sn;                       // SA / SST wall distance (static geometry)
+  const double* wd2;                 // SST wall term dely2 on the wall halo cells (null unless SST)
   R* w;                              // scratch of this slice (phase dependent)
   R* lurec;                          // LU-SGS sweep records (skewed bands)
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)

@@ -242,125 +242,183 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
-// Shared memory of the sweep kernel: nwarp rings of dq chunks, then the
-// barriers, then the cross-band slots.
-template <class R>
-__host__ __device__ __forceinline__ size_t lu_smem_bytes(int nwarp, int dq) {
-  return (size_t)nwarp * dq * LU_CHUNK * sizeof(R) + (size_t)nwarp * dq * sizeof(uint64_t) + (size_t)nwarp * 2 * 4 * sizeof(R);
+// Bounded spin on a shared-memory progress counter: true once *cnt >= need.
+__device__ __forceinline__ bool lu_spin_ge(const volatile int* cnt, int need) {
+  for (uint32_t it = 0; it < (1u << 22); ++it)
+    if (*cnt >= need) return true;
+  return false;
 }
 
+// Cross-band ring: the boundary lane of band w hands its outgoing (j,k-1)
+// contribution of local step t to the next band in sweep order through
+// slot t % LU_XB; the consumer reads it at its step t - 31.
+constexpr int LU_XB = 128;
+
+// Shared memory of the sweep kernel: per warp a ring of two groups of G
+// chunks, its two barriers, its cross-band ring and its progress counter;
+// then the first-row halo contributions of the slice (4 per column, at most
+// maxcol columns).
+template <class R>
+__host__ __device__ __forceinline__ size_t lu_smem_bytes(int nwarp, int G, int maxcol) {
+  return (size_t)nwarp * 2 * G * LU_CHUNK * sizeof(R) + (size_t)nwarp * 2 * sizeof(uint64_t) +
+         (size_t)nwarp * LU_XB * 4 * sizeof(R) + (size_t)nwarp * sizeof(int) + 16 +
+         (size_t)4 * maxcol * sizeof(R);
+}
+
+// One sweep of one slice.  Warp w owns band w (rows 32w..32w+31, lane l ->
+// row 32w+l) and walks its nst local steps; at local step t lane l is on
+// column t-l (forward) or ncol-1-(t-(31-l)) (backward), so the lanes of a
+// warp are on 32 consecutive hyperplanes and the in-band dependency (the
+// neighbouring row) arrives by shuffle from the previous step.  The
+// dependency across bands -- lane 31 of band w-1 feeds lane 0 of band w
+// 31 steps later (backward: lane 0 of band w+1 feeds lane 31 of band w) --
+// goes through the cross-band ring guarded by per-warp progress counters,
+// so the warps run without block-wide barriers.  The records stream in
+// through cp.async.bulk, G chunks per copy, double-buffered.
 template <class R, bool FWD>
-__device__ void lu_sweep_slice(const Slice<R>& S, int dq, int nwarp, unsigned char* smem) {
+__device__ void lu_sweep_slice(const Slice<R>& S, int G, int nwarp, unsigned char* smem) {
   const ot2d_params& p = *S.P;
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nb = lu_nband(S.kd), nst = lu_nstep(S.jd);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   const R gm1 = (R)p.gm1;
   R* rings = (R*)smem;
-  uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * dq * LU_CHUNK * sizeof(R));
-  R* xb = (R*)(bars + (size_t)nwarp * dq);           // [nwarp][2][4]
-  R* ring = rings + (size_t)w * dq * LU_CHUNK;
-  uint64_t* bar = bars + (size_t)w * dq;
+  uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * 2 * G * LU_CHUNK * sizeof(R));
+  R* xrings = (R*)(bars + (size_t)nwarp * 2);
+  volatile int* prog = (volatile int*)(xrings + (size_t)nwarp * LU_XB * 4);
+  // halo contributions into the first (forward) / last (backward) row,
+  // read once per step by one lane: staged in shared memory
+  R* bhs = (R*)(((uintptr_t)(prog + nwarp) + 15) & ~(uintptr_t)15);
+  R* ring = rings + (size_t)w * 2 * G * LU_CHUNK;
+  uint64_t* bar = bars + (size_t)w * 2;
   const bool wok = w < nb;
-  R* rec = S.lurec + (int64_t)w * nst * LU_CHUNK;
-  const uint32_t cbytes = LU_CHUNK * sizeof(R);
-  auto chunk_of = [&](int tl) -> int { return FWD ? tl : nst - 1 - tl; };
-  if (wok && l == 0)
-    for (int s = 0; s < dq; ++s) mbar_init(&bar[s], 1);
-  __syncthreads();
-  if (wok && l == 0) {
+  const R* rec_w = S.lurec + (int64_t)w * nst * LU_CHUNK;
+  R* recw = S.lurec + (int64_t)w * nst * LU_CHUNK;
+  const int ngrp = (nst + G - 1) / G;
+  // group g of the sweep covers local steps g*G .. g*G+G-1; its chunks are
+  // contiguous in memory starting at chunk c0(g) (ascending)
+  auto c0 = [&](int g) -> int { return FWD ? g * G : max(0, nst - (g + 1) * G); };
+  auto gsize = [&](int g) -> int { return min(G, nst - g * G); };
+  auto issue = [&](int g) {
+    const uint32_t bytes = (uint32_t)gsize(g) * LU_CHUNK * sizeof(R);
     fence_proxy_async_smem();
-    for (int s = 0; s < dq && s < nst; ++s) {
-      mbar_expect_tx(&bar[s], cbytes);
-      bulk_g2s(ring + (size_t)s * LU_CHUNK, rec + (int64_t)chunk_of(s) * LU_CHUNK, cbytes, &bar[s]);
-    }
+    mbar_expect_tx(&bar[g & 1], bytes);
+    bulk_g2s(ring + (size_t)(g & 1) * G * LU_CHUNK, rec_w + (int64_t)c0(g) * LU_CHUNK, bytes, &bar[g & 1]);
+  };
+  if (l == 0) {
+    if (wok) { mbar_init(&bar[0], 1); mbar_init(&bar[1], 1); }
+    prog[w] = 0;
+  }
+  {
+    const R* Bg = lu_halo(S, FWD ? 2 : 3);
+    for (int i = threadIdx.x; i < 4 * ncol; i += blockDim.x) bhs[i] = Bg[i];
+  }
+  __syncthreads();
+  if (!wok) return;
+  if (l == 0) {
+    issue(0);
+    if (ngrp > 1) issue(1);
   }
   const R* Ah = lu_halo(S, FWD ? 0 : 1);
-  const R* Bh = lu_halo(S, FWD ? 2 : 3);
-  const int off = FWD ? 32 * w : 32 * (nb - 1 - w);
-  const int T = nst + 32 * (nb - 1);
+  const R* Bh = bhs;
+  // neighbouring bands in sweep order and the boundary lanes
+  const int wprev = FWD ? w - 1 : w + 1, wnext = FWD ? w + 1 : w - 1;
+  const bool has_prev = FWD ? w > 0 : w + 1 < nb, has_next = FWD ? w + 1 < nb : w > 0;
+  const int lin = FWD ? 0 : 31, lout = FWD ? 31 : 0;
+  R* xout = xrings + (size_t)w * LU_XB * 4;
+  const R* xin = xrings + (size_t)(has_prev ? wprev : w) * LU_XB * 4;
   const int r = 32 * w + l;
   R aprev[4] = {0, 0, 0, 0}, bout[4] = {0, 0, 0, 0};
   bool failed = false;
-  int tfail = 0;
-  for (int t = 0; t < T; ++t) {
+  int gfail = -1;
+  for (int tl = 0; tl < nst; ++tl) {
+    const int g = tl / G;
+    if (tl % G == 0) {
+      const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+      if (__any_sync(0xffffffffu, !ok)) { failed = true; gfail = g; break; }
+    }
+    const int pos = FWD ? tl - c0(g) : (nst - 1 - tl) - c0(g);
+    const R* ch = ring + ((size_t)(g & 1) * G + pos) * LU_CHUNK;
     R bin[4];
 #pragma unroll
     for (int n = 0; n < 4; ++n)
       bin[n] = FWD ? __shfl_up_sync(0xffffffffu, bout[n], 1) : __shfl_down_sync(0xffffffffu, bout[n], 1);
-    const int tl = t - off;
-    const bool wact = wok && tl >= 0 && tl < nst && !failed;  // warp-uniform
-    if (wact) {
-      const int slot = tl % dq;
-      const bool ok = mbar_wait_bounded(&bar[slot], (uint32_t)((tl / dq) & 1));
-      if (__any_sync(0xffffffffu, !ok)) { failed = true; tfail = tl; }
-      const R* ch = ring + (size_t)slot * LU_CHUNK;
-      const int c = FWD ? tl - l : ncol - 1 - (tl - (31 - l));
-      const bool act = !failed && r < nrow && c >= 0 && c < ncol;
-      if (act) {
-        if (FWD ? c == 0 : c == ncol - 1) {
+    const int c = FWD ? tl - l : ncol - 1 - (tl - (31 - l));
+    const bool act = r < nrow && c >= 0 && c < ncol;
+    bool bad = false;
+    if (act) {
+      if (FWD ? c == 0 : c == ncol - 1) {
 #pragma unroll
-          for (int n = 0; n < 4; ++n) aprev[n] = Ah[4 * r + n];
-        }
-        if (FWD) {
-          if (l == 0) {
-            if (w == 0) {
+        for (int n = 0; n < 4; ++n) aprev[n] = Ah[4 * r + n];
+      }
+      // the (j,k-1) / (j,k+1) neighbour from outside the band
+      if (FWD ? l == 0 : (l == 31 || r == nrow - 1)) {
+        if (!has_prev || (!FWD && r == nrow - 1)) {
 #pragma unroll
-              for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
-            } else {
-#pragma unroll
-              for (int n = 0; n < 4; ++n) bin[n] = xb[((w - 1) * 2 + ((t - 1) & 1)) * 4 + n];
-            }
-          }
+          for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
         } else {
-          if (r == nrow - 1) {
+          // produced by band wprev at its step tl + 31
+          if (lu_spin_ge(&prog[wprev], tl + 32)) {
+            __threadfence_block();
+            const R* x = xin + (size_t)((tl + 31) % LU_XB) * 4;
 #pragma unroll
-            for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
-          } else if (l == 31) {
-#pragma unroll
-            for (int n = 0; n < 4; ++n) bin[n] = xb[((w + 1) * 2 + ((t - 1) & 1)) * 4 + n];
+            for (int n = 0; n < 4; ++n) bin[n] = x[n];
+          } else {
+            bad = true;
           }
         }
-        const R sv = ch[LF_SV * 32 + l], di = ch[LF_D * 32 + l];
-        R sn[4];
-#pragma unroll
-        for (int n = 0; n < 4; ++n) {
-          const R st = ch[(LF_S + n) * 32 + l];
-          sn[n] = FWD ? (st + sv * (aprev[n] + bin[n])) * di : st - sv * (aprev[n] + bin[n]) * di;
-        }
-        if (FWD) {
-          R* g = rec + (int64_t)chunk_of(tl) * LU_CHUNK;
-#pragma unroll
-          for (int n = 0; n < 4; ++n) g[(LF_S + n) * 32 + l] = sn[n];
-        } else {
-          const int64_t o = at(S.jd, p.jbeg + c, p.kbeg + r);
-#pragma unroll
-          for (int n = 0; n < 4; ++n) S.s[n * S.qs + o] = sn[n];
-        }
-        const R uu = ch[LF_UU * 32 + l], vv = ch[LF_VV * 32 + l], uv2 = ch[LF_UV2 * 32 + l], ge = ch[LF_GE * 32 + l];
-        lu_apply(ch[(FWD ? LF_FCX : LF_BCX) * 32 + l], ch[(FWD ? LF_FSX : LF_BSX) * 32 + l], ch[LF_RI1 * 32 + l],
-                 ch[LF_RI2 * 32 + l], ch[LF_QX * 32 + l], uu, vv, uv2, ge, gm1, sn, aprev);
-        lu_apply(ch[(FWD ? LF_FCY : LF_BCY) * 32 + l], ch[(FWD ? LF_FSY : LF_BSY) * 32 + l], ch[LF_RK1 * 32 + l],
-                 ch[LF_RK2 * 32 + l], ch[LF_QY * 32 + l], uu, vv, uv2, ge, gm1, sn, bout);
-        if (FWD ? (l == 31 && w + 1 < nb) : (l == 0 && w > 0)) {
-#pragma unroll
-          for (int n = 0; n < 4; ++n) xb[(w * 2 + (t & 1)) * 4 + n] = bout[n];
-        }
       }
-      __syncwarp();
-      if (l == 0 && !failed && tl + dq < nst) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(&bar[slot], cbytes);
-        bulk_g2s(ring + (size_t)slot * LU_CHUNK, rec + (int64_t)chunk_of(tl + dq) * LU_CHUNK, cbytes, &bar[slot]);
+      const R sv = ch[LF_SV * 32 + l], di = ch[LF_D * 32 + l];
+      R sn[4];
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        const R st = ch[(LF_S + n) * 32 + l];
+        sn[n] = FWD ? (st + sv * (aprev[n] + bin[n])) * di : st - sv * (aprev[n] + bin[n]) * di;
       }
+      if (FWD) {
+        R* gch = recw + (int64_t)tl * LU_CHUNK;
+#pragma unroll
+        for (int n = 0; n < 4; ++n) gch[(LF_S + n) * 32 + l] = sn[n];
+      } else {
+        const int64_t o = at(S.jd, p.jbeg + c, p.kbeg + r);
+#pragma unroll
+        for (int n = 0; n < 4; ++n) S.s[n * S.qs + o] = sn[n];
+      }
+      const R uu = ch[LF_UU * 32 + l], vv = ch[LF_VV * 32 + l], uv2 = ch[LF_UV2 * 32 + l], ge = ch[LF_GE * 32 + l];
+      lu_apply(ch[(FWD ? LF_FCX : LF_BCX) * 32 + l], ch[(FWD ? LF_FSX : LF_BSX) * 32 + l], ch[LF_RI1 * 32 + l],
+               ch[LF_RI2 * 32 + l], ch[LF_QX * 32 + l], uu, vv, uv2, ge, gm1, sn, aprev);
+      lu_apply(ch[(FWD ? LF_FCY : LF_BCY) * 32 + l], ch[(FWD ? LF_FSY : LF_BSY) * 32 + l], ch[LF_RK1 * 32 + l],
+               ch[LF_RK2 * 32 + l], ch[LF_QY * 32 + l], uu, vv, uv2, ge, gm1, sn, bout);
     }
-    __syncthreads();
+    // hand the boundary contribution to the next band (its slot must have
+    // been read: the consumer is at least at step tl - LU_XB + 32)
+    if (l == lout) {
+      if (act && has_next) {
+        if (lu_spin_ge(&prog[wnext], tl - LU_XB + 32)) {
+          R* x = xout + (size_t)(tl % LU_XB) * 4;
+#pragma unroll
+          for (int n = 0; n < 4; ++n) x[n] = bout[n];
+        } else {
+          bad = true;
+        }
+      }
+      __threadfence_block();
+      prog[w] = tl + 1;
+    }
+    if (__any_sync(0xffffffffu, bad)) { failed = true; gfail = g; break; }
+    // group done: refill its buffer with group g + 2
+    if (tl % G == G - 1 || tl == nst - 1) {
+      __syncwarp();
+      if (l == 0 && g + 2 < ngrp) issue(g + 2);
+    }
   }
-  if (failed && l == 0) {
-    // copies for steps tfail .. tfail+dq-1 were issued and not consumed:
-    // wait (bounded) for them before the CTA's shared memory goes away,
-    // then flag the slice
-    for (int u = tfail; u < tfail + dq && u < nst; ++u) mbar_wait_bounded(&bar[u % dq], (uint32_t)((u / dq) & 1));
-    if (S.ist) atomicOr(&S.ist[2], 4);
+  if (failed) {
+    if (l == lout) prog[w] = 1 << 30;  // release a waiting neighbour (it gives up on its own bound otherwise)
+    if (l == 0) {
+      // copies issued and not consumed: groups gfail .. gfail+1; wait
+      // (bounded) before the CTA's shared memory goes away, then flag
+      for (int g = gfail; g < gfail + 2 && g < ngrp; ++g) mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+      if (S.ist) atomicOr(&S.ist[2], 4);
+    }
   }
 }
 

@@ -30,28 +30,29 @@ constexpr int RT_VEH = RT_TK + 3, RT_VXW = RT_TJ + 3;
 constexpr int RT_NVE = 6 * RT_VEH * RT_TJ;                 // eta viscous, k0-2..k1+1
 constexpr int RT_NVX = 6 * RT_TK * RT_VXW;                 // xi viscous, j0-2..j1+1
 
+// |iblank| of the staged cells is kept as one byte (values above 255 are
+// clamped; the reference's blanking values are -1, 0 and 1)
 template <class R>
 __host__ __device__ constexpr size_t rt_smem_bytes() {
-  return ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) + sizeof(int) * RT_NR + 15) / 16) *
-             16 +
-         sizeof(NormPart) * RT_BS;
+  return ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) + RT_NR + 15) / 16) * 16 +
+         sizeof(NormPart) * (RT_BS / 32);
 }
 
 template <class R>
 struct RtSmem {
   R* c;          // [RS_N][RT_NR]
   R *F, *G, *VE, *VX;
-  int* iba;      // [RT_NR]
-  NormPart* red; // [RT_BS]
+  uint8_t* iba;  // [RT_NR]
+  NormPart* red; // [RT_BS / 32] warp partials
   __device__ RtSmem(unsigned char* base) {
     c = (R*)base;
     F = c + (size_t)RS_N * RT_NR;
     G = F + RT_NF;
     VE = G + RT_NG;
     VX = VE + RT_NVE;
-    iba = (int*)(VX + RT_NVX);
-    red = (NormPart*)(base + ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) +
-                               sizeof(int) * RT_NR + 15) / 16) * 16);
+    iba = (uint8_t*)(VX + RT_NVX);
+    red = (NormPart*)(base + ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) + RT_NR + 15) /
+                              16) * 16);
   }
   __device__ __forceinline__ R& at(int a, int r) const { return c[(size_t)a * RT_NR + r]; }
 };
@@ -90,7 +91,8 @@ __device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_para
     sm.at(RS_XX, r) = S.xx[o]; sm.at(RS_XY, r) = S.xy[o]; sm.at(RS_YX, r) = S.yx[o]; sm.at(RS_YY, r) = S.yy[o];
   }
   const int ib = S.iblank[o];
-  sm.iba[r] = ib < 0 ? -ib : ib;
+  const int ia = ib < 0 ? -ib : ib;
+  sm.iba[r] = (uint8_t)(ia > 255 ? 255 : ia);
 }
 
 // A grid line read from the staged region: line position c sits at region

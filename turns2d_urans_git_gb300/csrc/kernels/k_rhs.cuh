@@ -106,30 +106,33 @@ template <class R> __device__ __forceinline__ R weno5(R a, R b, R c, R d, R e) {
 
 // Left / right states at cell i of a line of n cells, for one variable,
 // following the limiter the reference dispatches (eulerrhs.f:85-97):
-// ilim 0 -> iflux, |ilim| 1 -> muscld_new, ilim 4 -> weno.
-// w[0..6] = f(i-3..i+3) (entries outside 1..n are not read).
+// ilim 0 -> iflux, |ilim| 1 -> muscld_new, ilim 4 -> weno.  The WENO
+// forms take a window w[0..6] = f(i-3..i+3) (entries outside 1..n are not
+// read).
 template <class R>
 struct Recon {
   int ilim; R th, qt, epsl;
-  // muscld_new, eulerrhs.f:855-873 ; is=1, imax=n, im=n-1
-  __device__ __forceinline__ void muscl(const R* w, int i, int n, int ibm, int ib0, int ibp, R& ql, R& qr) const {
-    if (qt == (R)0.0 || i == 1 || i == n) { ql = w[3]; qr = w[3]; return; }
+  // muscld_new, eulerrhs.f:855-873 (is=1, imax=n, im=n-1) on the cells
+  // i-1, i, i+1 of the line
+  __device__ __forceinline__ void muscl3(R wm, R w0, R wp, int i, int n, int ibm, int ib0, int ibp, R& ql,
+                                         R& qr) const {
+    if (qt == (R)0.0 || i == 1 || i == n) { ql = w0; qr = w0; return; }
     R thm = (R)1.0 - th, thp = (R)1.0 + th;
-    R f2i = w[4] - w[3], f2i1 = w[3] - w[2];
+    R f2i = wp - w0, f2i1 = w0 - wm;
     R a1 = (R)3.0 * (f2i * f2i1 + epsl);
     R a2 = (R)2.0 * sq(f2i - f2i1) + a1;
     R f3i = a1 / a2;
     R f3qt = qt * f3i * (R)ib0 * (R)ibp * (R)ibm;
-    ql = w[3] + f3qt * (thm * f2i1 + thp * f2i);
-    qr = w[3] - f3qt * (thp * f2i1 + thm * f2i);
+    ql = w0 + f3qt * (thm * f2i1 + thp * f2i);
+    qr = w0 - f3qt * (thp * f2i1 + thm * f2i);
   }
   // iflux, eulerrhs.f:650-659
-  __device__ __forceinline__ void central(const R* w, int i, int n, R& ql, R& qr) const {
-    if (qt == (R)0.0 || i == 1 || i == n) { ql = w[3]; qr = w[3]; return; }
-    R s1 = w[3] - w[2], s2 = w[4] - w[3];
+  __device__ __forceinline__ void central3(R wm, R w0, R wp, int i, int n, R& ql, R& qr) const {
+    if (qt == (R)0.0 || i == 1 || i == n) { ql = w0; qr = w0; return; }
+    R s1 = w0 - wm, s2 = wp - w0;
     R slope = (s1 + s2) / (R)2;
-    ql = w[3] + (R)0.5 * slope;
-    qr = w[3] - (R)0.5 * slope;
+    ql = w0 + (R)0.5 * slope;
+    qr = w0 - (R)0.5 * slope;
   }
   // weno, eulerrhs.f:1046-1189.  f1(i) = f(i+1)-f(i); f2 with the
   // extrapolated end values; f2m(i) = ammd(f2(i), f2(i+1)).
@@ -242,29 +245,25 @@ __device__ __forceinline__ void roe(R gm1, const R* L, const R* Rr, R ri1, R ri2
 }
 
 // Inviscid flux through one face between cells i and i+1 of a line.  L
-// supplies f4(c, out) (the primitive f of cell c) and iba(c).
-template <class R, class Line>
-__device__ __forceinline__ void face_flux(const Line& L, const Recon<R>& rc, int i, int n, R ri1, R ri2, R ri3,
-                                          R* fout) {
-  R wl[4][7], ql[4], qr[4];
-  int ibw[7];
-  // window cells i-3 .. i+4 (two overlapping 7-point windows for i and i+1)
-  R w8[4][8];
+// supplies f4(c, out) (the primitive f of cell c) and iba(c).  LIM is the
+// limiter family (0 central, 1 MUSCL, 4 WENO) so that the central and MUSCL
+// forms index their window with constants only (the window stays in
+// registers); face_flux() dispatches on rc.ilim.
+template <int LIM, class R, class Line>
+__device__ __forceinline__ void face_flux_t(const Line& L, const Recon<R>& rc, int i, int n, R ri1, R ri2, R ri3,
+                                            R* fout) {
+  R ql[4], qr[4];
+  if constexpr (LIM == 4) {
+    // window cells i-3 .. i+4 (two overlapping 7-point windows for i and i+1)
+    R w8[4][8];
 #pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    int c = i - 3 + m;
-    if (c >= 1 && c <= n) {
-      R t[4]; L.f4(c, t);
+    for (int m = 0; m < 8; ++m) {
+      const int c = i - 3 + m;
+      R t[4] = {(R)0, (R)0, (R)0, (R)0};
+      if (c >= 1 && c <= n) L.f4(c, t);
 #pragma unroll
       for (int v = 0; v < 4; ++v) w8[v][m] = t[v];
-    } else {
-#pragma unroll
-      for (int v = 0; v < 4; ++v) w8[v][m] = (R)0;
     }
-  }
-  (void)wl; (void)ibw;
-  int ilm = rc.ilim < 0 ? -rc.ilim : rc.ilim;
-  if (rc.ilim == 4) {
     int blank_l = 1, blank_r = 1;
     if (i >= 3 && i + 2 <= n) blank_l = L.iba(i) * L.iba(i - 1) * L.iba(i + 1) * L.iba(i - 2) * L.iba(i + 2);
     if (i + 1 >= 3 && i + 3 <= n) blank_r = L.iba(i + 1) * L.iba(i) * L.iba(i + 2) * L.iba(i - 1) * L.iba(i + 3);
@@ -273,24 +272,46 @@ __device__ __forceinline__ void face_flux(const Line& L, const Recon<R>& rc, int
       ql[v] = rc.weno_l(&w8[v][0], i, n, blank_l);
       qr[v] = rc.weno_r(&w8[v][1], i + 1, n, blank_r);
     }
-  } else if (ilm == 1) {
-    int bm = (i - 1 >= 1) ? L.iba(i - 1) : 0, b0 = L.iba(i), bp = L.iba(i + 1);
-    int bp2 = (i + 2 <= n) ? L.iba(i + 2) : 0;
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      R dummy;
-      rc.muscl(&w8[v][0], i, n, bm, b0, bp, ql[v], dummy);
-      rc.muscl(&w8[v][1], i + 1, n, b0, bp, bp2, dummy, qr[v]);
-    }
   } else {
+    // cells i-1 .. i+2 (w4[m] = f(i-1+m)); MUSCL / central read only these
+    R w4[4][4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      R dummy;
-      rc.central(&w8[v][0], i, n, ql[v], dummy);
-      rc.central(&w8[v][1], i + 1, n, dummy, qr[v]);
+    for (int m = 0; m < 4; ++m) {
+      const int c = i - 1 + m;
+      R t[4] = {(R)0, (R)0, (R)0, (R)0};
+      if (c >= 1 && c <= n) L.f4(c, t);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) w4[v][m] = t[v];
+    }
+    if constexpr (LIM == 1) {
+      const int bm = (i - 1 >= 1) ? L.iba(i - 1) : 0, b0 = L.iba(i), bp = L.iba(i + 1);
+      const int bp2 = (i + 2 <= n) ? L.iba(i + 2) : 0;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        R dummy;
+        // muscl reads w[2..4] around its cell: cell i -> w4[v][0..2], cell i+1 -> w4[v][1..3]
+        rc.muscl3(w4[v][0], w4[v][1], w4[v][2], i, n, bm, b0, bp, ql[v], dummy);
+        rc.muscl3(w4[v][1], w4[v][2], w4[v][3], i + 1, n, b0, bp, bp2, dummy, qr[v]);
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        R dummy;
+        rc.central3(w4[v][0], w4[v][1], w4[v][2], i, n, ql[v], dummy);
+        rc.central3(w4[v][1], w4[v][2], w4[v][3], i + 1, n, dummy, qr[v]);
+      }
     }
   }
   roe(L.gm1, ql, qr, ri1, ri2, ri3, fout);
+}
+
+template <class R, class Line>
+__device__ __forceinline__ void face_flux(const Line& L, const Recon<R>& rc, int i, int n, R ri1, R ri2, R ri3,
+                                          R* fout) {
+  const int ilm = rc.ilim < 0 ? -rc.ilim : rc.ilim;
+  if (rc.ilim == 4) face_flux_t<4>(L, rc, i, n, ri1, ri2, ri3, fout);
+  else if (ilm == 1) face_flux_t<1>(L, rc, i, n, ri1, ri2, ri3, fout);
+  else face_flux_t<0>(L, rc, i, n, ri1, ri2, ri3, fout);
 }
 
 template <class R>

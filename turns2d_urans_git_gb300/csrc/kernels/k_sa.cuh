@@ -234,11 +234,15 @@ __device__ __forceinline__ void lj_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void lj_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-template <class R>
-__device__ void sa_lsolvej_group(const Slice<R>& S, const ot2d_params& p, int kline0, R* sm) {
+// The bands are the scratch slots sa, sb, sc, ss.  SAOUT: the result is
+// ((x + 0) - 0) * b as vmu_sa forms it (samodel2d.f:150-153); otherwise
+// x * b as komegasst does (komegasst.f:134-139).
+template <class R, bool SAOUT = true>
+__device__ void sa_lsolvej_group(const Slice<R>& S, const ot2d_params& p, int kline0, R* sm, int sa = W_AJ,
+                                 int sb = W_BJ, int sc = W_CJ, int ss = W_SJ) {
   const int lane = threadIdx.x & 31;
   const int jd = S.jd; const int64_t ws = S.wstride;
-  const R* ga = S.w + W_AJ * ws; R* gc = S.w + W_CJ * ws; R* gs = S.w + W_SJ * ws; const R* gb = S.w + W_BJ * ws;
+  const R* ga = S.w + sa * ws; R* gc = S.w + sc * ws; R* gs = S.w + ss * ws; const R* gb = S.w + sb * ws;
   const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
   const int ntile = (je - js + 1 + 31) / 32;
   const bool mine = ks + kline0 + lane <= ke;
@@ -309,7 +313,8 @@ __device__ void sa_lsolvej_group(const Slice<R>& S, const ot2d_params& p, int kl
         const int i = lane * 33 + jj;
         R x = (j0 + jj == je) ? Sm[i] : Sm[i] - Cm[i] * snext;
         snext = x;
-        Sm[i] = ((x + (R)0.) - (R)0.) * B[i];
+        if constexpr (SAOUT) Sm[i] = ((x + (R)0.) - (R)0.) * B[i];
+        else Sm[i] = x * B[i];
       }
     }
     __syncwarp();

@@ -7,6 +7,7 @@
 #include "k_rhs.cuh"
 #include "k_lusgs.cuh"
 #include "k_sa.cuh"
+#include "k_sst.cuh"
 #include "k_misc.cuh"
 #include "launch.h"
 #include "k_resid.cuh"
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(CELL_BS) k_assemble(const Slice<R>* __restrict
 // Fused residual over tiles of RT_TJ x RT_TK interior cells: slice i owns
 // tiles [tfirst[i], tfirst[i+1]).  Dynamic shared memory: rt_smem_bytes<R>().
 template <class R>
-__global__ void __launch_bounds__(RT_BS) k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst,
+__global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 1) k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst,
                                                   int nslice, int flags, NormPart* __restrict__ part) {
   extern __shared__ __align__(16) unsigned char rt_raw[];
   const int si = find_slice(tfirst, nslice, blockIdx.x);
@@ -236,9 +237,9 @@ __global__ void __launch_bounds__(CELL_BS) k_lu_edges(const Slice<R>* __restrict
 }
 
 template <class R, bool FWD>
-__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int dq) {
+__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int G) {
   extern __shared__ __align__(128) unsigned char lu_smem[];
-  lu_sweep_slice<R, FWD>(sl[blockIdx.x], dq, blockDim.x >> 5, lu_smem);
+  lu_sweep_slice<R, FWD>(sl[blockIdx.x], G, blockDim.x >> 5, lu_smem);
 }
 
 template <class R>
@@ -313,6 +314,95 @@ __global__ void __launch_bounds__(32) k_sa_lsolvej(const Slice<R>* __restrict__ 
   const ot2d_params& p = *S.P;
   if (p.lamin || p.iturb != 1) return;
   sa_lsolvej_group(S, p, 32 * (blockIdx.x - gfirst[si]), sm);
+}
+
+// ---- k-omega SST (komegasst.f:2-187) ---------------------------------------
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_sst_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                      int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside || !sst_slice(*S.P)) return;
+  sst_prep_cell(S, *S.P, j, k);
+}
+
+// komegabc on one CTA per slice; final pass: the second komegabc followed by
+// findturm on the halo ring (the interior was done by the k-line solve)
+template <class R>
+__global__ void k_sst_bc(const Slice<R>* __restrict__ sl, int final_pass) {
+  const Slice<R>& S = sl[blockIdx.x];
+  const ot2d_params& p = *S.P;
+  if (!sst_slice(p)) return;
+  sst_bc_slice(S, S.wd2);
+  shadow_ring(S, p.nmv + 1, p.nmv + 2);
+  if (final_pass) {
+    __syncthreads();
+    const int jd = S.jd, kd = S.kd, nring = 2 * jd + 2 * (kd - 2);
+    for (int i = threadIdx.x; i < nring; i += blockDim.x) {
+      int j, k;
+      if (i < jd) { j = i + 1; k = 1; }
+      else if (i < 2 * jd) { j = i - jd + 1; k = kd; }
+      else if (i < 2 * jd + kd - 2) { j = 1; k = i - 2 * jd + 2; }
+      else { j = jd; k = i - (2 * jd + kd - 2) + 2; }
+      sst_turm_cell(S, p, j, k);
+    }
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_sst_fields(const Slice<R>* __restrict__ sl,
+                                                        const int32_t* __restrict__ first, int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  const ot2d_params& p = *S.P;
+  if (!sst_slice(p) || j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) return;
+  sst_fields_cell(S, p, j, k);
+}
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_sst_turm(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                      int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside || !sst_slice(*S.P)) return;
+  sst_turm_cell(S, *S.P, j, k);
+}
+
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_sst_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                     int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  const ot2d_params& p = *S.P;
+  if (!sst_slice(p) || j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) return;
+  sst_rhs_cell(S, p, j, k);
+}
+
+// lsolvej2 of equation blockIdx.y by warps of 32 k-lines; output x * bjmat
+template <class R>
+__global__ void __launch_bounds__(32) k_sst_lsolvej(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ gfirst,
+                                                    int nslice) {
+  extern __shared__ __align__(16) unsigned char lj_raw[];
+  R* sm = (R*)lj_raw;   // LJ_SMEM elements
+  const int si = find_slice(gfirst, nslice, blockIdx.x);
+  const Slice<R>& S = sl[si];
+  const ot2d_params& p = *S.P;
+  if (!sst_slice(p)) return;
+  const int n = blockIdx.y;
+  sa_lsolvej_group<R, false>(S, p, 32 * (blockIdx.x - gfirst[si]), sm, kband(KB_AJ, n), kband(KB_BJ, n),
+                             kband(KB_CJ, n), kband(KB_SJ, n));
+}
+
+// lsolvek2 + update + findturm, one thread per j-line
+template <class R>
+__global__ void k_sst_lsolvek(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst, int nslice) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= lfirst[nslice]) return;
+  int lo = 0, hi = nslice - 1;
+  while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (lfirst[mid] <= gid) lo = mid; else hi = mid - 1; }
+  const Slice<R>& S = sl[lo];
+  const ot2d_params& p = *S.P;
+  if (!sst_slice(p)) return;
+  const int j = p.jbeg + gid - lfirst[lo];
+  if (j <= p.jend) sst_lsolvek_line(S, p, j);
 }
 
 // q(1:4) += s*max(iblank,0) on interior cells (step.f:203-213), FP64 state

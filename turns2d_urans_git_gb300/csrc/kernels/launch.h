@@ -12,6 +12,8 @@ struct NormPart;
 constexpr int CELL_BS = 256;
 // residual tile: RT_TJ x RT_TK interior cells per CTA
 constexpr int RT_TJ = 32, RT_TK = 8;
+// scratch arrays per slice of the k-omega SST solve (k_sst.cuh: SSTw)
+constexpr int SST_NSCRATCH = 27;
 
 struct Batch {
   int nslice = 0;          // slices in the batch
@@ -33,7 +35,7 @@ struct Batch {
 
 // One full iteration of step.f for every slice of the batch:
 // time_step, bc, rhsup (+visrhs, +time-spectral), norms, rbc, ilu2d,
-// vmu_sa (when `turb`), update, monitor.
+// vmu_sa (turb bit 1), komegasst (turb bit 2), update, monitor.
 template <class R>
 cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, cudaStream_t st);
 
@@ -49,6 +51,7 @@ template <class R> cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b
 enum { AS_ACC = 1, AS_INV = 2, AS_VISC = 4, AS_TS = 8, AS_NORM = 16 };
 template <class R> cudaError_t launch_assemble(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st);
 template <class R> cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+template <class R> cudaError_t launch_sst(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_monitor(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 // refresh the compute copy of q from q64 on every cell (mixed path)

@@ -50,18 +50,19 @@ cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaSt
   k_lu_prep<R><<<b.lu_blocks, CELL_BS, 0, st>>>(d_sl, b.d_lfirst, b.nslice, scale);
   k_lu_edges<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale);
   const int nw = b.max_lu_warps;
-  // ring depth: as deep as ~200 KB of shared memory allows (2..8 chunks)
-  int dq = 8;
-  while (dq > 2 && lu_smem_bytes<R>(nw, dq) > 200 * 1024) --dq;
-  const size_t smem = lu_smem_bytes<R>(nw, dq);
+  // chunks per bulk copy: as many as ~200 KB of shared memory allows (1..8)
+  const int maxcol = b.max_wall;   // >= jd - 2 of every slice
+  int G = 8;
+  while (G > 1 && lu_smem_bytes<R>(nw, G, maxcol) > 200 * 1024) G >>= 1;
+  const size_t smem = lu_smem_bytes<R>(nw, G, maxcol);
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_lu_sweep<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_lu_sweep<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr_set = true;
   }
-  k_lu_sweep<R, true><<<b.nslice, 32 * nw, smem, st>>>(d_sl, dq);
-  k_lu_sweep<R, false><<<b.nslice, 32 * nw, smem, st>>>(d_sl, dq);
+  k_lu_sweep<R, true><<<b.nslice, 32 * nw, smem, st>>>(d_sl, G);
+  k_lu_sweep<R, false><<<b.nslice, 32 * nw, smem, st>>>(d_sl, G);
   return cudaGetLastError();
 }
 template <class R>
@@ -79,6 +80,26 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_sa_lsolvej<R><<<b.jgroups, 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sa_lsolve<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice, 1);
   k_turbc<R><<<b.nslice, 256, 0, st>>>(d_sl, 1);
+  return cudaGetLastError();
+}
+// komegasst (komegasst.f:2-187) for the SST slices of the batch
+template <class R>
+cudaError_t launch_sst(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_sst_prep<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  k_sst_bc<R><<<b.nslice, 256, 0, st>>>(d_sl, 0);
+  k_sst_fields<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  k_sst_turm<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  k_sst_rhs<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  constexpr size_t lj_smem = sizeof(R) * LJ_SMEM;
+  static bool lj_attr = false;
+  if (!lj_attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_sst_lsolvej<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lj_smem);
+    if (e != cudaSuccess) return e;
+    lj_attr = true;
+  }
+  k_sst_lsolvej<R><<<dim3(b.jgroups, 2), 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
+  k_sst_lsolvek<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice);
+  k_sst_bc<R><<<b.nslice, 256, 0, st>>>(d_sl, 1);
   return cudaGetLastError();
 }
 template <class R>
@@ -111,7 +132,8 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   if ((e = launch_residual(d_sl, b, viscous, st)) != cudaSuccess) return e;
   if ((e = launch_rbc(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_lusgs(d_sl, b, 1, st)) != cudaSuccess) return e;
-  if (turb && (e = launch_sa(d_sl, b, st)) != cudaSuccess) return e;
+  if ((turb & 1) && (e = launch_sa(d_sl, b, st)) != cudaSuccess) return e;
+  if ((turb & 2) && (e = launch_sst(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_update(d_sl, b, st)) != cudaSuccess) return e;
   return cudaSuccess;  // the monitor runs inside k_update and k_bc
 }
@@ -126,6 +148,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   template cudaError_t launch_faces<R>(const Slice<R>*, const Batch&, int, int, cudaStream_t);          \
   template cudaError_t launch_assemble<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
   template cudaError_t launch_sa<R>(const Slice<R>*, const Batch&, cudaStream_t);                       \
+  template cudaError_t launch_sst<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
   template cudaError_t launch_update<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
   template cudaError_t launch_monitor<R>(const Slice<R>*, const Batch&, cudaStream_t);                  \
   template cudaError_t launch_shadow<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \

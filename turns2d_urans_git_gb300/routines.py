@@ -99,6 +99,12 @@ def vmu_sa(q, s, turmu, x, y, xv, yv, xx, xy, yx, yy, ug, vg, jd, kd, tscale, ib
           _p(ug), _p(vg), _ref(jd), _ref(kd), _p(tscale), _p(iblank), _ref(im), _ref(nsp))
 
 
+def komegasst(q, s, turmu, x, y, xv, yv, xx, xy, yx, yy, ug, vg, jd, kd, tscale, iblank, im):
+    """src/komegasst.f:2 -- one k-omega SST update of q(:,:,5:6) and turmu."""
+    _call("ot2d_komegasst", _p(q), _p(s), _p(turmu), _p(x), _p(y), _p(xv), _p(yv), _p(xx), _p(xy), _p(yx), _p(yy),
+          _p(ug), _p(vg), _ref(jd), _ref(kd), _p(tscale), _p(iblank), _ref(im))
+
+
 def timespectralrhs(q, s, Ds, jd, kd, nsp):
     """src/sources.f:2 -- time-spectral coupling term of instance nsp."""
     _call("ot2d_timespectralrhs", _p(q), _p(s), _p(Ds), _ref(jd), _ref(kd), _ref(nsp))
