@@ -101,6 +101,10 @@ int ot2d_time_step(double* q, double* xx, double* xy, double* yx, double* yy, do
 int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
                double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu,
                double* tscale);
+/* src/lhs.f:817-818 (ilhs = 2: pentadiagonal lhsinv, lhs.f:1536-1816) */
+int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+               double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu, int32_t* iblank,
+               double* tscale, double* bt);
 /* src/samodel2d.f:2-3 */
 int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
                 double* xy, double* yx, double* yy, double* ug, double* vg, int32_t* jd, int32_t* kd,

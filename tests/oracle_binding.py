@@ -51,6 +51,7 @@ def lib():
         L.oro_vmu_sa.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
         L.oro_vmu_sa.restype = C.c_double
         L.oro_komegasst.argtypes = [_P] + [_dp] * 14 + [_ip, _dp]
+        L.oro_arc2d.argtypes = [_P] + [_dp] * 9 + [_ip, _dp, _dp]
         L.oro_monitor.argtypes = [_P, _dp]
         L.oro_monitor.restype = C.c_int
         L.oro_force2d.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]

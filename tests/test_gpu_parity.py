@@ -159,6 +159,44 @@ def test_solver_sst_fp64_matches_oracle():
         assert abs(a - b) <= 1e-10 * max(abs(b), 1e-3)
 
 
+@pytest.mark.parametrize("visc", [False, True])
+def test_arc2d(visc):
+    """arc2d (diagonalised ADI with pentadiagonal line inversions,
+    lhs.f:817-1057) on a perturbed state and a random right-hand side."""
+    c = Case(viscous=visc, seed=19)
+    L = ob.lib()
+    L.oro_time_step(_o(c), ob.ptr(c.q), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug),
+                    ob.ptr(c.vg), ob.ptr(c.tscale), ob.ptr(c.bt), ob.ptr(c.iblank))
+    so = np.random.default_rng(23).uniform(-1, 1, c.n2 * c.p.nv) * 1e-4
+    s = so.copy()
+    qo, q = c.q.copy(), c.q.copy()
+    L.oro_arc2d(_o(c), ob.ptr(qo), ob.ptr(so), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug),
+                ob.ptr(c.vg), ob.ptr(c.turmu), ob.ptr(c.iblank), ob.ptr(c.tscale), ob.ptr(c.bt))
+    rt.set_params(c.p)
+    p = c.p
+    rt.arc2d(q, s, c.jd, c.kd, p.jbeg, p.jend, p.kbeg, p.kend, c.xx, c.xy, c.yx, c.yy, c.ug, c.vg, c.turmu, c.iblank,
+             c.tscale, c.bt)
+    assert relerr(s[:4 * c.n2], so[:4 * c.n2]) <= TOL
+    assert relerr(q, qo) <= TOL
+
+
+@pytest.mark.parametrize("kind", ["euler", "sst_weno"])
+def test_solver_adi_fp64_matches_oracle(kind):
+    """The batched solver with the ADI operator (ilhs = 2), FP64, against the
+    oracle driver: an inviscid case and a k-omega SST + WENO case."""
+    if kind == "euler":
+        _, prm, xv, yv = api.cmesh_case(97, 25, ds_wall=2e-3, invisc=1, lamin=1, irhsy=-3, ilim=1, ilhs=2,
+                                        iconstant_cfl=1, dt=2.0, fsmach=0.8, alfa=1.25)
+    else:
+        _, prm, xv, yv = api.cmesh_case(97, 33, naca=(0.02, 0.4, 0.12), ds_wall=1e-3, invisc=0, lamin=0, iturb=2,
+                                        irhsy=-3, ilim=4, ilhs=2, iconstant_cfl=1, dt=2.0, fsmach=0.73, alfa=2.8,
+                                        rey=6.5e6)
+    r, q, hist, forces, q_o = _solver_vs_oracle(prm, xv, yv, 40, OT2D_FP64)
+    assert r.status == 0 and r.iterations == 40
+    assert abs(r.rsum_last - hist[-1, 0]) <= 1e-10 * hist[-1, 0]
+    assert relerr(q, q_o) <= 1e-10
+
+
 def _full_arrays(c):
     return dict(q=c.q.copy(), s=np.zeros(c.n2 * c.p.nv), turmu=c.turmu.copy(), tscale=np.zeros(c.n2),
                 bt=np.zeros(c.n2))

@@ -395,7 +395,37 @@ int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int3
   S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
   std::vector<Slice<double>> sl{S};
   run_batch(sl, err);
-  if (!err && launch_lusgs<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && launch_lusgs<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+               double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu, int32_t* iblank,
+               double* tscale, double* bt) {
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !js || !je || !ks || !ke || *js != p.jbeg || *je != p.jend || *ks != p.kbeg || *ke != p.kend)
+    return fail(OT2D_ERR_ARG);
+  if (!q || !s || !xx || !xy || !yx || !yy || !turmu || !tscale || !iblank || p.jd < 10 || p.kd < 10)
+    return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
+  S.xx = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg = (double*)resolve(vg, n2 * 8, true, false, err);
+  S.turmu = (double*)resolve(turmu, n2 * 8, true, false, err);
+  S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
+  S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
+  S.bt = bt ? (double*)resolve(bt, n2 * 8, true, false, err) : nullptr;
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_adi<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
   return finish(err);
 }
 
@@ -506,7 +536,8 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   int err = 0;
   if (prepare(nspec, err)) return fail(err);
   const ot2d_params& p = g_ctx.P;
-  if (!dims_ok(jd, kd) || p.ilhs != 1 || p.itnmax > 1 || (!p.lamin && p.iturb != 1 && p.iturb != 2) || p.itrans != 0)
+  if (!dims_ok(jd, kd) || (p.ilhs != 1 && p.ilhs != 2) || p.itnmax > 1 || (!p.lamin && p.iturb != 1 && p.iturb != 2) ||
+      p.itrans != 0)
     return fail(OT2D_ERR_ARG);
   if (!q || !s || !x || !y || !xv || !yv || !iblank || !xx || !xy || !yx || !yy || !turmu || !tscale) return fail(OT2D_ERR_ARG);
   if (p.timespectral && (!ugv || !vgv || !ug || !vg || !Ds)) return fail(OT2D_ERR_ARG);
@@ -561,7 +592,8 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   if (!err && launch_bc<double>(B.d_sl, B.b, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_residual<double>(B.d_sl, B.b, visc, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_rbc<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
-  if (!err && launch_lusgs<double>(B.d_sl, B.b, 1, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && p.ilhs == 1 && launch_lusgs<double>(B.d_sl, B.b, 1, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && p.ilhs == 2 && launch_adi<double>(B.d_sl, B.b, 1, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && turb && launch_sa<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && sst && launch_sst<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_update<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;

@@ -22,7 +22,10 @@ constexpr size_t ALIGN = 256;
 inline size_t al(size_t b) { return (b + ALIGN - 1) / ALIGN * ALIGN; }
 // scratch arrays per time instance: the SA bands (9) and the drop-in face
 // fluxes (20) fit in 20; the k-omega SST fields and two-equation bands take 27
-inline int nscratch(const ot2d_params& p) { return (!p.lamin && p.iturb == 2) ? SST_NSCRATCH + 1 : 20; }
+inline int nscratch(const ot2d_params& p) {
+  return ((!p.lamin && p.iturb == 2) || p.ilhs == 2) ? (SST_NSCRATCH > ADI_NSCRATCH ? SST_NSCRATCH : ADI_NSCRATCH) + 1
+                                                     : 20;
+}
 inline bool is_sst(const ot2d_params& p) { return !p.lamin && p.iturb == 2; }
 
 struct Layout {
@@ -99,7 +102,8 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
                  cudaStream_t st) {
   if (!xv1 || !yv1 || p.nspec < 1 || p.nhalo != 1 || p.jd != p.jmax + 1 || p.kd != p.kmax + 1) return OT2D_ERR_ARG;
   if (precision != OT2D_FP64 && precision != OT2D_FP32_MIXED) return OT2D_ERR_ARG;
-  if (p.ilhs != 1) return OT2D_ERR_ARG;            // ADI operator: not in this build
+  if (p.ilhs != 1 && p.ilhs != 2) return OT2D_ERR_ARG;      // LU-SGS or ADI (pentadiagonal)
+  if (p.ilhs == 2 && (p.jd < 10 || p.kd < 10)) return OT2D_ERR_ARG;  // ADI lines of >= 8 points
   if (!p.lamin && p.iturb != 1 && p.iturb != 2) return OT2D_ERR_ARG;  // SA or k-omega SST
   if (p.itrans != 0) return OT2D_ERR_ARG;                            // no transition model
   d = DevSolve{};
@@ -276,7 +280,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   // six prefix tables of n+1 entries: cell blocks, k-lines, j-lines, LU
   // record blocks, 32-line groups, residual tiles
   std::vector<int32_t> idx(6 * (n + 1));
-  int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1;
+  int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1, maxkd = 1;
   for (int i = 0; i < n; ++i) {
     idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl; idx[3 * (n + 1) + i] = lub;
     idx[4 * (n + 1) + i] = grp; idx[5 * (n + 1) + i] = tiles;
@@ -289,6 +293,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
     tiles += ((jd - 2 + RT_TJ - 1) / RT_TJ) * ((kd - 2 + RT_TK - 1) / RT_TK);
     maxw = std::max(maxw, lu_nband(kd));
     maxwall = std::max(maxwall, jd);
+    maxkd = std::max(maxkd, kd);
   }
   idx[n] = cells; idx[2 * (n + 1) - 1] = jl; idx[3 * (n + 1) - 1] = kl; idx[4 * (n + 1) - 1] = lub;
   idx[5 * (n + 1) - 1] = grp; idx[6 * (n + 1) - 1] = tiles;
@@ -313,6 +318,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   b.cell_blocks = cells;
   b.max_lu_warps = maxw;
   b.max_wall = maxwall;
+  b.max_kd = maxkd;
   b.jlines = jl; b.klines = kl;
   b.lu_blocks = lub;
   b.jgroups = grp;

@@ -59,6 +59,7 @@ struct ot2d_solver {
   int since_check = 0;
   bool any_viscous = false;
   int turb_bits = 0;   // 1: some SA instance, 2: some SST instance
+  int lhs_bits = 0;    // 1: some LU-SGS instance, 2: some ADI instance
   double* d_forces = nullptr; size_t forces_cap = 0;
   DevBatch<double> f64;
   DevBatch<float> f32;
@@ -112,13 +113,14 @@ template <class R>
 int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   drop_graph(s);
   std::vector<Slice<R>> sl;
-  s->any_viscous = false; s->turb_bits = 0;
+  s->any_viscous = false; s->turb_bits = 0; s->lhs_bits = 0;
   for (int id : s->live) {
     const Rec& r = s->recs[id];
     slices_of<R>(s, r, sl);
     if (!r.d.P.invisc) s->any_viscous = true;
     if (!r.d.P.lamin && r.d.P.iturb == 1) s->turb_bits |= 1;
     if (!r.d.P.lamin && r.d.P.iturb == 2) s->turb_bits |= 2;
+    s->lhs_bits |= (r.d.P.ilhs == 2) ? 2 : 1;
   }
   s->dirty = false;
   if (sl.empty()) return OT2D_OK;
@@ -127,7 +129,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   // The kernels branch on each slice's own params, so inviscid, laminar,
   // SA and SST requests can share one batch.
   if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
-  cudaError_t le = launch_iteration<R>(B.d_sl, B.b, s->any_viscous ? 1 : 0, s->turb_bits, s->st);
+  cudaError_t le = launch_iteration<R>(B.d_sl, B.b, s->any_viscous ? 1 : 0, s->turb_bits, s->lhs_bits, s->st);
   cudaError_t ce = cudaStreamEndCapture(s->st, &s->graph);
   if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
   if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
@@ -206,7 +208,9 @@ int profile_t(ot2d_solver* s, DevBatch<R>& B, int iters, double* ms) {
     if (!e) e = launch_bc<R>(B.d_sl, B.b, 1, s->st); rec(2);
     if (!e) e = launch_residual<R>(B.d_sl, B.b, visc, s->st); rec(3);
     if (!e) e = launch_rbc<R>(B.d_sl, B.b, s->st); rec(4);
-    if (!e) e = launch_lusgs<R>(B.d_sl, B.b, 1, s->st); rec(5);
+    if (!e && (s->lhs_bits & 1)) e = launch_lusgs<R>(B.d_sl, B.b, 1, s->st, 1);
+    if (!e && (s->lhs_bits & 2)) e = launch_adi<R>(B.d_sl, B.b, 1, s->st, 1);
+    rec(5);
     if (!e && (turb & 1)) e = launch_sa<R>(B.d_sl, B.b, s->st);
     if (!e && (turb & 2)) e = launch_sst<R>(B.d_sl, B.b, s->st);
     rec(6);

@@ -8,6 +8,7 @@
 #include "k_lusgs.cuh"
 #include "k_sa.cuh"
 #include "k_sst.cuh"
+#include "k_adi.cuh"
 #include "k_misc.cuh"
 #include "launch.h"
 #include "k_resid.cuh"
@@ -218,27 +219,28 @@ __global__ void k_rbc(const Slice<R>* __restrict__ sl) {
 // (band, step, lane) of every slice (prefix table lfirst).
 template <class R>
 __global__ void __launch_bounds__(CELL_BS) k_lu_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst,
-                                                     int nslice, int scale) {
+                                                     int nslice, int scale, int only_lu) {
   const int si = find_slice(lfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];
   const int g = (blockIdx.x - lfirst[si]) * blockDim.x + threadIdx.x;
   const int nst = lu_nstep(S.jd), nb = lu_nband(S.kd);
   const int l = g & 31, t = (g >> 5) % nst, band = (g >> 5) / nst;
-  if (band >= nb) return;
+  if (band >= nb || (only_lu && S.P->ilhs != 1)) return;
   lu_prep_cell(S, *S.P, band, t, l, scale);
 }
 
 template <class R>
 __global__ void __launch_bounds__(CELL_BS) k_lu_edges(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
-                                                      int nslice, int scale) {
+                                                      int nslice, int scale, int only_lu) {
   OT2D_CELL_MAP();
-  if (!inside) return;
+  if (!inside || (only_lu && S.P->ilhs != 1)) return;
   lu_edge_cell(S, *S.P, j, k, scale);
 }
 
 template <class R, bool FWD>
-__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int G) {
+__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int G, int only_lu) {
   extern __shared__ __align__(128) unsigned char lu_smem[];
+  if (only_lu && sl[blockIdx.x].P->ilhs != 1) return;
   lu_sweep_slice<R, FWD>(sl[blockIdx.x], G, blockDim.x >> 5, lu_smem);
 }
 
@@ -403,6 +405,56 @@ __global__ void k_sst_lsolvek(const Slice<R>* __restrict__ sl, const int32_t* __
   if (!sst_slice(p)) return;
   const int j = p.jbeg + gid - lfirst[lo];
   if (j <= p.jend) sst_lsolvek_line(S, p, j);
+}
+
+// ---- ADI operator arc2d (lhs.f:817-1057), ilhs = 2 ------------------------
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_adi_txi(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                     int nslice, int scale, int only) {
+  OT2D_CELL_MAP();
+  if (!inside || (only && !adi_slice(*S.P))) return;
+  adi_txi_cell(S, *S.P, j, k, scale);
+}
+// line direction dir over all cells: d2p (what = 0) or the coefficients (1)
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_adi_line_cells(const Slice<R>* __restrict__ sl,
+                                                            const int32_t* __restrict__ first, int nslice, int dir,
+                                                            int what, int only) {
+  OT2D_CELL_MAP();
+  if (!inside) return;
+  const ot2d_params& p = *S.P;
+  if (only && !adi_slice(p)) return;
+  const int m = dir == 0 ? j : k, n = dir == 0 ? k : j;
+  const int ms = dir == 0 ? p.jbeg - 1 : p.kbeg - 1, me = dir == 0 ? p.jend + 1 : p.kend + 1;
+  if (what == 0) adi_d2p_cell(S, dir, m, n, ms, me);
+  else adi_coef_cell(S, p, dir, m, n, ms, me);
+}
+// one thread per (line, variable); blockIdx.y = slice
+template <class R>
+__global__ void k_adi_solve(const Slice<R>* __restrict__ sl, int dir, int only) {
+  const Slice<R>& S = sl[blockIdx.y];
+  const ot2d_params& p = *S.P;
+  if (only && !adi_slice(p)) return;
+  const int nlines = dir == 0 ? S.kd : S.jd;   // n = ks-1..ke+1 / js-1..je+1
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4 * nlines) return;
+  const int n = 1 + t % nlines, i = 1 + t / nlines;
+  const int ms = dir == 0 ? p.jbeg - 1 : p.kbeg - 1, me = dir == 0 ? p.jend + 1 : p.kend + 1;
+  adi_solve_line(S, p, dir, i, n, ms, me);
+}
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_adi_ninv(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                      int nslice, int only) {
+  OT2D_CELL_MAP();
+  if (!inside || (only && !adi_slice(*S.P))) return;
+  adi_ninv_cell(S, *S.P, j, k);
+}
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_adi_teta(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                      int nslice, int only) {
+  OT2D_CELL_MAP();
+  if (!inside || (only && !adi_slice(*S.P))) return;
+  adi_teta_cell(S, *S.P, j, k);
 }
 
 // q(1:4) += s*max(iblank,0) on interior cells (step.f:203-213), FP64 state

@@ -14,12 +14,15 @@ constexpr int CELL_BS = 256;
 constexpr int RT_TJ = 32, RT_TK = 8;
 // scratch arrays per slice of the k-omega SST solve (k_sst.cuh: SSTw)
 constexpr int SST_NSCRATCH = 27;
+// scratch arrays per slice of the ADI operator (k_adi.cuh: ADIw)
+constexpr int ADI_NSCRATCH = 25;
 
 struct Batch {
   int nslice = 0;          // slices in the batch
   int cell_blocks = 0;     // blocks of the cell-parallel kernels
   int max_lu_warps = 1;    // warps per CTA of the LU-SGS kernel
-  int max_wall = 1;        // most wall cells of one slice (force kernel smem)
+  int max_wall = 1;        // most wall cells of one slice (force kernel smem); also max jd
+  int max_kd = 1;          // largest kd of the batch
   int jlines = 0, klines = 0;  // total k-lines / j-lines (SA line solves)
   const int32_t* d_first = nullptr;   // [nslice+1] first cell block of each slice
   const int32_t* d_jfirst = nullptr;  // [nslice+1] first k-line (lsolvej) of each slice
@@ -35,23 +38,30 @@ struct Batch {
 
 // One full iteration of step.f for every slice of the batch:
 // time_step, bc, rhsup (+visrhs, +time-spectral), norms, rbc, ilu2d,
-// vmu_sa (turb bit 1), komegasst (turb bit 2), update, monitor.
+// vmu_sa (turb bit 1), komegasst (turb bit 2), update, monitor.  lhs bit 1:
+// some slice uses LU-SGS (ilhs = 1), bit 2: some slice uses ADI (ilhs = 2).
 template <class R>
-cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, cudaStream_t st);
+cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st);
 
 // Individual phases (the drop-in routines call these on a batch of one).
 template <class R> cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st);
 template <class R> cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st);
 template <class R> cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
-// scale = 1: multiply s by tscale first (step.f:141-148); 0: s already scaled
-template <class R> cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st);
+// scale = 1: multiply s by tscale first (step.f:141-148); 0: s already scaled.
+// only_lu = 1: skip slices whose ilhs is not 1 (mixed batches); 0: every slice
+template <class R> cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st,
+                                            int only_lu);
 template <class R> cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b, int inviscid, int viscous, cudaStream_t st);
 // assembly flags: see AS_* in kernels.cuh
 enum { AS_ACC = 1, AS_INV = 2, AS_VISC = 4, AS_TS = 8, AS_NORM = 16 };
 template <class R> cudaError_t launch_assemble(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st);
 template <class R> cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_sst(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+// arc2d (ilhs = 2); scale = 1: preceded by s *= tscale on all cells
+// (step.f:141-148).  only_adi = 1: skip slices whose ilhs is not 2
+template <class R> cudaError_t launch_adi(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st,
+                                          int only_adi);
 template <class R> cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_monitor(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 // refresh the compute copy of q from q64 on every cell (mixed path)

@@ -46,9 +46,9 @@ cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   return cudaGetLastError();
 }
 template <class R>
-cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st) {
-  k_lu_prep<R><<<b.lu_blocks, CELL_BS, 0, st>>>(d_sl, b.d_lfirst, b.nslice, scale);
-  k_lu_edges<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale);
+cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
+  k_lu_prep<R><<<b.lu_blocks, CELL_BS, 0, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
+  k_lu_edges<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
   const int nw = b.max_lu_warps;
   // chunks per bulk copy: as many as ~200 KB of shared memory allows (1..8)
   const int maxcol = b.max_wall;   // >= jd - 2 of every slice
@@ -61,8 +61,8 @@ cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaSt
     cudaFuncSetAttribute(k_lu_sweep<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr_set = true;
   }
-  k_lu_sweep<R, true><<<b.nslice, 32 * nw, smem, st>>>(d_sl, G);
-  k_lu_sweep<R, false><<<b.nslice, 32 * nw, smem, st>>>(d_sl, G);
+  k_lu_sweep<R, true><<<b.nslice, 32 * nw, smem, st>>>(d_sl, G, only_lu);
+  k_lu_sweep<R, false><<<b.nslice, 32 * nw, smem, st>>>(d_sl, G, only_lu);
   return cudaGetLastError();
 }
 template <class R>
@@ -103,6 +103,19 @@ cudaError_t launch_sst(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   return cudaGetLastError();
 }
 template <class R>
+cudaError_t launch_adi(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_adi) {
+  k_adi_txi<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_adi);
+  for (int dir = 0; dir < 2; ++dir) {
+    if (dir == 1) k_adi_ninv<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, only_adi);
+    k_adi_line_cells<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, dir, 0, only_adi);
+    k_adi_line_cells<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, dir, 1, only_adi);
+    const int nl = 4 * (dir == 0 ? b.max_kd : b.max_wall);
+    k_adi_solve<R><<<dim3((nl + 63) / 64, b.nslice), 64, 0, st>>>(d_sl, dir, only_adi);
+  }
+  k_adi_teta<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, only_adi);
+  return cudaGetLastError();
+}
+template <class R>
 cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_update<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
@@ -125,13 +138,14 @@ cudaError_t launch_forces(const Slice<R>* d_sl, const Batch& b, const double* co
   return cudaGetLastError();
 }
 template <class R>
-cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, cudaStream_t st) {
+cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st) {
   cudaError_t e;
   if ((e = launch_time_step(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_bc(d_sl, b, 1, st)) != cudaSuccess) return e;
   if ((e = launch_residual(d_sl, b, viscous, st)) != cudaSuccess) return e;
   if ((e = launch_rbc(d_sl, b, st)) != cudaSuccess) return e;
-  if ((e = launch_lusgs(d_sl, b, 1, st)) != cudaSuccess) return e;
+  if ((lhs & 1) && (e = launch_lusgs(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
+  if ((lhs & 2) && (e = launch_adi(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
   if ((turb & 1) && (e = launch_sa(d_sl, b, st)) != cudaSuccess) return e;
   if ((turb & 2) && (e = launch_sst(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_update(d_sl, b, st)) != cudaSuccess) return e;
@@ -139,16 +153,17 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
 }
 
 #define OT2D_INSTANTIATE(R)                                                                              \
-  template cudaError_t launch_iteration<R>(const Slice<R>*, const Batch&, int, int, cudaStream_t);      \
+  template cudaError_t launch_iteration<R>(const Slice<R>*, const Batch&, int, int, int, cudaStream_t); \
   template cudaError_t launch_time_step<R>(const Slice<R>*, const Batch&, cudaStream_t);                \
   template cudaError_t launch_bc<R>(const Slice<R>*, const Batch&, int, cudaStream_t);                  \
   template cudaError_t launch_residual<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
   template cudaError_t launch_rbc<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
-  template cudaError_t launch_lusgs<R>(const Slice<R>*, const Batch&, int, cudaStream_t);               \
+  template cudaError_t launch_lusgs<R>(const Slice<R>*, const Batch&, int, cudaStream_t, int);          \
   template cudaError_t launch_faces<R>(const Slice<R>*, const Batch&, int, int, cudaStream_t);          \
   template cudaError_t launch_assemble<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
   template cudaError_t launch_sa<R>(const Slice<R>*, const Batch&, cudaStream_t);                       \
   template cudaError_t launch_sst<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
+  template cudaError_t launch_adi<R>(const Slice<R>*, const Batch&, int, cudaStream_t, int);            \
   template cudaError_t launch_update<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
   template cudaError_t launch_monitor<R>(const Slice<R>*, const Batch&, cudaStream_t);                  \
   template cudaError_t launch_shadow<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
