@@ -44,6 +44,10 @@ WORKLOAD = "RANS-SA NACA0012 C-mesh 513x129, M0.15 a10 Re6e6, MUSCL+Roe, LU-SGS 
 # the FP32-mixed path (compulsory array traffic)
 ALG_BYTES_F32 = {0: 44, 1: 0, 2: 80, 3: 0, 4: 188, 5: 200, 6: 96}
 PHASES = ["time_step", "bc", "residual", "rbc", "lusgs", "sa", "update"]
+# DRAM bytes per interior cell per launch measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of the batch-8 capture, 0.52 M cells, summarised in
+# profiles/top_kernels_rans_sa_513x129_b8_fp32mixed.md), scaled to the batch
+TRAFFIC_PER_CELL = {"residual": (40.559104e6 + 0.576256e6) / (8 * 65536)}
 NPH = len(PHASES)
 
 
@@ -140,6 +144,79 @@ def cpu_reference(cases, max_threads=None, target_s=12.0):
     value = done * cells / wall
     sample = "%d requests x %d iterations of the 513x129 SA case on %d threads (%.1f s wall)" % (nthr, iters, nthr, wall)
     return value, nthr, sample
+
+
+def serve_stream(precision, reqs, arrivals, orders, max_iters, check_every, device, cap_s):
+    """Continuous-batching service of a request stream: requests are
+    admitted at the first status check after their arrival time and retired
+    when converged (L2 norm `orders` decades below its running peak), failed
+    or capped.  Returns per-request (arrival, done, result) and the makespan
+    (s); stops admitting and gives up after cap_s seconds."""
+    from turns2d_urans_git_gb300 import api
+    sv = api.Solver(precision, device=device, check_every=check_every)
+    t0 = time.perf_counter()
+    pending = sorted(zip(arrivals, range(len(reqs))))
+    admitted = {}
+    while True:
+        now = time.perf_counter() - t0
+        while pending and pending[0][0] <= now:
+            ta, i = pending.pop(0)
+            _, prm, xv, yv = reqs[i]
+            admitted[sv.add(prm, xv, yv, orders=orders, max_iters=max_iters)] = (i, ta, now)
+        if sv.live() == 0:
+            if not pending or now > cap_s:
+                break
+            time.sleep(max(0.0, min(pending[0][0] - now, 0.05)))
+            continue
+        if now > cap_s:
+            break
+        sv.iterate(check_every)
+        sv.sync()
+    sv.sync()
+    t_end = time.perf_counter() - t0
+    out = []
+    for iid, (i, ta, tadm) in admitted.items():
+        r = sv.result(iid)
+        out.append((i, ta, r))
+    # the solver clock starts at creation, the same origin as t0 up to the
+    # constructor's duration (t_done in its own seconds)
+    sv.close()
+    return out, t_end
+
+
+def serving_section(args, device):
+    """FP32-mixed vs FP64 on the same seeded request stream: converged
+    solves/s and p50/p99 time to a converged solution."""
+    from turns2d_urans_git_gb300 import api
+    from turns2d_urans_git_gb300.abi import OT2D_FP32_MIXED, OT2D_FP64
+    rng = np.random.default_rng(7)
+    sizes = ((129, 33), (257, 65))
+    reqs = [api.config_c4_sample(rng, sizes=sizes) for _ in range(args.serve_requests)]
+    gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
+    arrivals = np.cumsum(gaps) - gaps[0]
+    res = {}
+    for name, prec in (("fp32_mixed", OT2D_FP32_MIXED), ("fp64", OT2D_FP64)):
+        out, t_end = serve_stream(prec, reqs, arrivals, args.serve_orders, args.serve_max_iters, 25, device,
+                                  args.serve_seconds)
+        lat = [r.t_done - ta for (i, ta, r) in out if r.converged]
+        conv = len(lat)
+        res[name] = {"requests": len(reqs), "admitted": len(out), "converged": conv,
+                     "solves_per_s": conv / t_end if t_end > 0 else None,
+                     "p50_s": float(np.percentile(lat, 50)) if lat else None,
+                     "p99_s": float(np.percentile(lat, 99)) if lat else None,
+                     "makespan_s": t_end,
+                     "forces": {i: (r.cl, r.cd, r.cm) for (i, ta, r) in out if r.converged}}
+    a, b = res["fp32_mixed"].pop("forces"), res["fp64"].pop("forces")
+    both = sorted(set(a) & set(b))
+    dcl = max((abs(a[i][0] - b[i][0]) for i in both), default=None)
+    dcd = max((abs(a[i][1] - b[i][1]) for i in both), default=None)
+    sm, sd = res["fp32_mixed"]["solves_per_s"], res["fp64"]["solves_per_s"]
+    return {"workload": "%d seeded RANS-SA requests (NACA 4-digit m,p,t; M 0.3-0.85; a -2..8 deg; Re 1e6-1e7; "
+                        "meshes %s), Poisson arrivals %.1f/s, converged = %.1f decades below the running peak"
+                        % (len(reqs), "/".join("%dx%d" % s_ for s_ in sizes), args.serve_rate, args.serve_orders),
+            "fp32_mixed": res["fp32_mixed"], "fp64": res["fp64"],
+            "speedup_solves_per_s": (sm / sd) if sm and sd else None,
+            "max_abs_dcl_vs_fp64": dcl, "max_abs_dcd_vs_fp64": dcd, "compared": len(both)}
 
 
 def run_reference(args):
@@ -268,6 +345,10 @@ def run_ours(args):
         ms64 = timed(sv64, k64)
         fp64 = world * B * cells * k64 / (ms64 / 1e3)
         sv64.close()
+    # ---- served request stream (rank 0 only): converged solves/s, p50/p99
+    serve = None
+    if rank == 0 and not args.skip_serve:
+        serve = serving_section(args, local)
     # ---- CPU baseline (rank 0, N=1 only): the oracle on the host cores
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
@@ -289,11 +370,16 @@ def run_ours(args):
                 "gpu_launches": launches_per_step * args.steps,
                 "phase_ms": phase_ms,
                 "roofline": {"bound": "hbm", "kernel": PHASES[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": (achieved / peak) if achieved else None, "traffic": None,
+                             "frac": (achieved / peak) if achieved else None,
+                             "traffic": (TRAFFIC_PER_CELL[PHASES[dom]] * B * cells
+                                         if PHASES[dom] in TRAFFIC_PER_CELL else None),
+                             "traffic_note": "bytes per launch, ncu batch-8 capture scaled by cells",
                              "peak_source": "measured" if peaks else "fallback"},
                 "clocks": clocks}
         if cpu:
             line["cpu_baseline"] = cpu
+        if serve:
+            line["serving"] = serve
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -311,6 +397,12 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-rate", type=float, default=8.0)
+    ap.add_argument("--serve-orders", type=float, default=2.0)
+    ap.add_argument("--serve-max-iters", type=int, default=20000)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--skip-serve", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

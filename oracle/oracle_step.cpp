@@ -155,6 +155,9 @@ int oro_metfv(const P* p, double* q, const double* xv, const double* yv, double*
 void oro_qzero(const P* p, double* q) { qzero(*p, v3(p, q)); }
 void oro_qdivj(const P* p, double* q) { qdivj(*p, v3(p, q)); }
 void oro_computeTScoefs(int n, double* Ds) { computeTScoefs(n, Ds); }
+void oro_timespectralrhs(const P* p, const double* q, double* s, const double* Ds, int nsp) {
+  timespectralrhs(*p, q, s, Ds, nsp);
+}
 void oro_find_coord_TS_orig(const P* p, double* xv, double* yv, const double* xv1, const double* yv1, double tspec) {
   find_coord_TS_orig(*p, xv, yv, xv1, yv1, tspec);
 }

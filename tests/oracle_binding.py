@@ -40,6 +40,7 @@ def lib():
         L.oro_qzero.argtypes = [_P, _dp]
         L.oro_qdivj.argtypes = [_P, _dp]
         L.oro_computeTScoefs.argtypes = [C.c_int, _dp]
+        L.oro_timespectralrhs.argtypes = [_P, _dp, _dp, _dp, C.c_int]
         L.oro_find_coord_TS_orig.argtypes = [_P, _dp, _dp, _dp, _dp, C.c_double]
         L.oro_find_timemetrics_TS_orig.argtypes = [_P, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp]
         L.oro_bc.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]

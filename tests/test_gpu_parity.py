@@ -197,6 +197,43 @@ def test_solver_adi_fp64_matches_oracle(kind):
     assert relerr(q, q_o) <= 1e-10
 
 
+@pytest.mark.parametrize("nspec", [3, 5])
+def test_timespectralrhs(nspec):
+    """sources.f:2-27: s(nsp) -= rotf * sum_m Ds(m,nsp) q(m), every instance."""
+    _, p, _, _ = api.cmesh_case(65, 25, invisc=1, lamin=1, timespectral=1, nspec=nspec, rf=0.1, angmax=5.0,
+                                xac=0.25, motiontype=1, fsmach=0.3)
+    rng = np.random.default_rng(nspec)
+    n2 = p.jd * p.kd
+    q = rng.uniform(0.5, 1.5, n2 * nspec * p.nq)
+    s0 = rng.uniform(-1, 1, n2 * nspec * p.nv) * 1e-3
+    Ds = np.zeros(nspec * nspec)
+    ob.lib().oro_computeTScoefs(nspec, ob.ptr(Ds))
+    rt.set_params(p)
+    for nsp in range(1, nspec + 1):
+        so, s = s0.copy(), s0.copy()
+        ob.lib().oro_timespectralrhs(C.byref(p), ob.ptr(q), ob.ptr(so), ob.ptr(Ds), nsp)
+        rt.timespectralrhs(q, s, Ds, p.jd, p.kd, nsp)
+        assert not np.array_equal(so, s0)
+        assert relerr(s, so) <= TOL
+
+
+@pytest.mark.parametrize("visc", [False, True])
+def test_solver_ts_fp64_matches_oracle(visc):
+    """A time-spectral pitching-airfoil request (3 instances coupled through
+    Ds, pitching grids and grid speeds) through the batched solver, FP64,
+    against the oracle driver."""
+    kw = dict(timespectral=1, nspec=3, rf=0.1, angmax=5.0, xac=0.25, motiontype=1, fsmach=0.3, alfa=2.0,
+              irhsy=-3, ilim=1, ilhs=1, iconstant_cfl=1)
+    if visc:
+        _, prm, xv, yv = api.cmesh_case(97, 33, ds_wall=1e-3, invisc=0, lamin=0, iturb=1, dt=20.0, rey=2e6,
+                                        vnuinf=3.0, **kw)
+    else:
+        _, prm, xv, yv = api.cmesh_case(97, 25, ds_wall=2e-3, invisc=1, lamin=1, dt=10.0, **kw)
+    r, q, hist, forces, q_o = _solver_vs_oracle(prm, xv, yv, 30, OT2D_FP64)
+    assert r.status == 0 and r.iterations == 30
+    assert relerr(q, q_o) <= 1e-10
+
+
 def _full_arrays(c):
     return dict(q=c.q.copy(), s=np.zeros(c.n2 * c.p.nv), turmu=c.turmu.copy(), tscale=np.zeros(c.n2),
                 bt=np.zeros(c.n2))

@@ -76,6 +76,7 @@ size_t plan(const ot2d_params& p, int precision, F&& assign) {
   assign("sn", L.take(rb * n2 * nspec));
   assign("w", L.take(rb * ws * nscratch(p) * nspec));
   if (is_sst(p)) assign("wd2", L.take(sizeof(double) * n2 * nspec));
+  if (mixed) assign("sinf", L.take(rb * n2 * nspec * 4));
   assign("lurec", L.take(rb * (size_t)lu_rec_elems(p.jd, p.kd) * nspec));
   return L.total;
 }
@@ -96,6 +97,29 @@ size_t solve_bytes(const ot2d_params& p, int precision) {
 void solve_destroy(DevSolve& d) {
   if (d.mem) cudaFree(d.mem);
   d = DevSolve{};
+}
+
+// Mixed path: the f32 residual (inviscid + viscous, no BCs) of the uniform
+// freestream state just uploaded, kept in d.sinf and subtracted by the
+// residual kernel every iteration.  In real arithmetic it is 0.
+int freestream_residual_f32(DevSolve& d, cudaStream_t st) {
+  std::vector<Slice<float>> sl;
+  for (int nsp = 1; nsp <= d.P.nspec; ++nsp) {
+    Slice<float> S = make_slice<float>(d, nsp, nullptr, nullptr);
+    S.sinf = nullptr;
+    sl.push_back(S);
+  }
+  DevBatch<float> B;
+  int e = B.build(sl, st);
+  if (e) { B.release(); return e; }
+  const int flags = AS_INV | (d.P.invisc ? 0 : AS_VISC);
+  const size_t qs = d.n2 * (size_t)d.P.nspec;
+  bool bad = launch_resid_tiles<float>(B.d_sl, B.b, flags, st) != cudaSuccess;
+  if (!bad && cudaMemcpyAsync(d.sinf, d.s, qs * 4 * sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess) bad = true;
+  if (!bad && cudaMemsetAsync(d.s, 0, qs * (size_t)d.P.nv * sizeof(float), st) != cudaSuccess) bad = true;
+  if (!bad && cudaStreamSynchronize(st) != cudaSuccess) bad = true;
+  B.release();
+  return bad ? OT2D_ERR_CUDA : OT2D_OK;
 }
 
 int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double* xv1, const double* yv1,
@@ -149,6 +173,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     else if (n == "w") d.w = ptr;
     else if (n == "lurec") d.lurec = ptr;
     else if (n == "wd2") d.wd2 = (double*)ptr;
+    else if (n == "sinf") d.sinf = ptr;
   }
   const bool mixed = precision == OT2D_FP32_MIXED;
   if (!mixed) { d.q = d.q64; d.xx = d.xx64; d.xy = d.xy64; d.yx = d.yx64; d.yy = d.yy64; d.ug = d.ug64; d.vg = d.vg64; }
@@ -226,6 +251,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     chk(upload_as<float>(d.sn, sn.data(), qs, st, t14));
     chk(cudaMemsetAsync(d.turmu, 0, qs * sizeof(float), st));
     chk(cudaStreamSynchronize(st));
+    if (!bad && freestream_residual_f32(d, st) != OT2D_OK) bad = true;
   } else {
     chk(cudaMemcpyAsync(d.fxa, fxa.data(), qs * 8, cudaMemcpyHostToDevice, st));
     chk(cudaMemcpyAsync(d.fya, fya.data(), qs * 8, cudaMemcpyHostToDevice, st));
@@ -263,6 +289,7 @@ Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
   S.sn = R_(d.sn);
   S.w = (R*)d.w + (size_t)(nsp - 1) * d.wstride * d.nscratch;
   S.wd2 = D_(d.wd2);
+  S.sinf = R_(d.sinf);
   S.wstride = (int64_t)d.wstride;
   S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = red; S.ist = ist;

@@ -37,6 +37,7 @@ struct DevSolve {
   void *ug = nullptr, *vg = nullptr, *tscale = nullptr, *bt = nullptr, *turmu = nullptr, *sn = nullptr, *w = nullptr;
   void* lurec = nullptr;
   double* wd2 = nullptr;   // SST wall term (k-omega SST instances only)
+  void* sinf = nullptr;    // f32 freestream residual (mixed path only)
   int nscratch = 0;        // scratch arrays per time instance
 };
 

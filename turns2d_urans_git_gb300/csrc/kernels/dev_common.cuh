@@ -30,6 +30,7 @@ struct Slice {
   const int32_t* iblank;
   const R* sn;                       // SA / SST wall distance (static geometry)
   const double* wd2;                 // SST wall term dely2 on the wall halo cells (null unless SST)
+  const R* sinf;                     // mixed path: f32 residual of the uniform freestream (4 vars), or null
   R* w;                              // scratch of this slice (phase dependent)
   R* lurec;                          // LU-SGS sweep records (skewed bands)
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)

@@ -242,17 +242,32 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
-// Bounded spin on a shared-memory progress counter: true once *cnt >= need.
-__device__ __forceinline__ bool lu_spin_ge(const volatile int* cnt, int need) {
-  for (uint32_t it = 0; it < (1u << 22); ++it)
-    if (*cnt >= need) return true;
+// Progress counters in shared memory: the producer publishes with a release
+// store, the consumer reads with an acquire load (CTA scope), so the data
+// written before the store is visible after the load.
+__device__ __forceinline__ int lu_ld_acquire(const int* cnt) {
+  int v;
+  asm volatile("ld.acquire.cta.shared::cta.s32 %0, [%1];" : "=r"(v) : "r"(smem_u32(cnt)) : "memory");
+  return v;
+}
+__device__ __forceinline__ void lu_st_release(int* cnt, int v) {
+  asm volatile("st.release.cta.shared::cta.s32 [%0], %1;" ::"r"(smem_u32(cnt)), "r"(v) : "memory");
+}
+// Bounded wait until *cnt >= need; `seen` caches the last value read, so a
+// counter already known to be far enough ahead is not read again.
+__device__ __forceinline__ bool lu_wait_ge(const int* cnt, int need, int& seen) {
+  if (seen >= need) return true;
+  for (uint32_t it = 0; it < (1u << 22); ++it) {
+    seen = lu_ld_acquire(cnt);
+    if (seen >= need) return true;
+  }
   return false;
 }
 
 // Cross-band ring: the boundary lane of band w hands its outgoing (j,k-1)
 // contribution of local step t to the next band in sweep order through
 // slot t % LU_XB; the consumer reads it at its step t - 31.
-constexpr int LU_XB = 128;
+constexpr int LU_XB = 128;   // a power of two
 
 // Shared memory of the sweep kernel: per warp a ring of two groups of G
 // chunks, its two barriers, its cross-band ring and its progress counter;
@@ -275,8 +290,8 @@ __host__ __device__ __forceinline__ size_t lu_smem_bytes(int nwarp, int G, int m
 // goes through the cross-band ring guarded by per-warp progress counters,
 // so the warps run without block-wide barriers.  The records stream in
 // through cp.async.bulk, G chunks per copy, double-buffered.
-template <class R, bool FWD>
-__device__ void lu_sweep_slice(const Slice<R>& S, int G, int nwarp, unsigned char* smem) {
+template <class R, bool FWD, int G>
+__device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem) {
   const ot2d_params& p = *S.P;
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nb = lu_nband(S.kd), nst = lu_nstep(S.jd);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -284,7 +299,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int G, int nwarp, unsigned cha
   R* rings = (R*)smem;
   uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * 2 * G * LU_CHUNK * sizeof(R));
   R* xrings = (R*)(bars + (size_t)nwarp * 2);
-  volatile int* prog = (volatile int*)(xrings + (size_t)nwarp * LU_XB * 4);
+  int* prog = (int*)(xrings + (size_t)nwarp * LU_XB * 4);
   // halo contributions into the first (forward) / last (backward) row,
   // read once per step by one lane: staged in shared memory
   R* bhs = (R*)(((uintptr_t)(prog + nwarp) + 15) & ~(uintptr_t)15);
@@ -323,96 +338,94 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int G, int nwarp, unsigned cha
   // neighbouring bands in sweep order and the boundary lanes
   const int wprev = FWD ? w - 1 : w + 1, wnext = FWD ? w + 1 : w - 1;
   const bool has_prev = FWD ? w > 0 : w + 1 < nb, has_next = FWD ? w + 1 < nb : w > 0;
-  const int lin = FWD ? 0 : 31, lout = FWD ? 31 : 0;
+  const int lout = FWD ? 31 : 0;
   R* xout = xrings + (size_t)w * LU_XB * 4;
   const R* xin = xrings + (size_t)(has_prev ? wprev : w) * LU_XB * 4;
   const int r = 32 * w + l;
+  // this lane's row of s (backward sweep output), indexed by column
+  R* srow = S.s + (int64_t)(p.kbeg + r - 1) * S.jd + (p.jbeg - 1);
   R aprev[4] = {0, 0, 0, 0}, bout[4] = {0, 0, 0, 0};
-  bool failed = false;
+  int seen_prev = 0, seen_next = 0;   // cached progress of the neighbouring bands
+  bool bad = false;
   int gfail = -1;
-  for (int tl = 0; tl < nst; ++tl) {
-    const int g = tl / G;
-    if (tl % G == 0) {
-      const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
-      if (__any_sync(0xffffffffu, !ok)) { failed = true; gfail = g; break; }
-    }
-    const int pos = FWD ? tl - c0(g) : (nst - 1 - tl) - c0(g);
-    const R* ch = ring + ((size_t)(g & 1) * G + pos) * LU_CHUNK;
-    R bin[4];
+  for (int g = 0; g < ngrp; ++g) {
+    const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+    if (__any_sync(0xffffffffu, !ok || bad)) { gfail = g; break; }
+    const int gs = gsize(g);
+    const R* gring = ring + (size_t)(g & 1) * G * LU_CHUNK;
+#pragma unroll 1
+    for (int u = 0; u < gs; ++u) {
+      const int tl = g * G + u;
+      const R* ch = gring + (FWD ? u : gs - 1 - u) * LU_CHUNK;
+      R bin[4];
 #pragma unroll
-    for (int n = 0; n < 4; ++n)
-      bin[n] = FWD ? __shfl_up_sync(0xffffffffu, bout[n], 1) : __shfl_down_sync(0xffffffffu, bout[n], 1);
-    const int c = FWD ? tl - l : ncol - 1 - (tl - (31 - l));
-    const bool act = r < nrow && c >= 0 && c < ncol;
-    bool bad = false;
-    if (act) {
-      if (FWD ? c == 0 : c == ncol - 1) {
+      for (int n = 0; n < 4; ++n)
+        bin[n] = FWD ? __shfl_up_sync(0xffffffffu, bout[n], 1) : __shfl_down_sync(0xffffffffu, bout[n], 1);
+      const int c = FWD ? tl - l : ncol - 1 - (tl - (31 - l));
+      const bool act = r < nrow && c >= 0 && c < ncol;
+      if (act) {
+        if (FWD ? c == 0 : c == ncol - 1) {
 #pragma unroll
-        for (int n = 0; n < 4; ++n) aprev[n] = Ah[4 * r + n];
-      }
-      // the (j,k-1) / (j,k+1) neighbour from outside the band
-      if (FWD ? l == 0 : (l == 31 || r == nrow - 1)) {
-        if (!has_prev || (!FWD && r == nrow - 1)) {
+          for (int n = 0; n < 4; ++n) aprev[n] = Ah[4 * r + n];
+        }
+        // the (j,k-1) / (j,k+1) neighbour from outside the band
+        if (FWD ? l == 0 : (l == 31 || r == nrow - 1)) {
+          if (!has_prev || (!FWD && r == nrow - 1)) {
 #pragma unroll
-          for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
-        } else {
-          // produced by band wprev at its step tl + 31
-          if (lu_spin_ge(&prog[wprev], tl + 32)) {
-            __threadfence_block();
-            const R* x = xin + (size_t)((tl + 31) % LU_XB) * 4;
+            for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
+          } else if (lu_wait_ge(&prog[wprev], tl + 32, seen_prev)) {
+            // produced by band wprev at its step tl + 31
+            const R* x = xin + ((tl + 31) & (LU_XB - 1)) * 4;
 #pragma unroll
             for (int n = 0; n < 4; ++n) bin[n] = x[n];
           } else {
             bad = true;
           }
         }
-      }
-      const R sv = ch[LF_SV * 32 + l], di = ch[LF_D * 32 + l];
-      R sn[4];
+        const R sv = ch[LF_SV * 32 + l], di = ch[LF_D * 32 + l];
+        R sn[4];
 #pragma unroll
-      for (int n = 0; n < 4; ++n) {
-        const R st = ch[(LF_S + n) * 32 + l];
-        sn[n] = FWD ? (st + sv * (aprev[n] + bin[n])) * di : st - sv * (aprev[n] + bin[n]) * di;
-      }
-      if (FWD) {
-        R* gch = recw + (int64_t)tl * LU_CHUNK;
-#pragma unroll
-        for (int n = 0; n < 4; ++n) gch[(LF_S + n) * 32 + l] = sn[n];
-      } else {
-        const int64_t o = at(S.jd, p.jbeg + c, p.kbeg + r);
-#pragma unroll
-        for (int n = 0; n < 4; ++n) S.s[n * S.qs + o] = sn[n];
-      }
-      const R uu = ch[LF_UU * 32 + l], vv = ch[LF_VV * 32 + l], uv2 = ch[LF_UV2 * 32 + l], ge = ch[LF_GE * 32 + l];
-      lu_apply(ch[(FWD ? LF_FCX : LF_BCX) * 32 + l], ch[(FWD ? LF_FSX : LF_BSX) * 32 + l], ch[LF_RI1 * 32 + l],
-               ch[LF_RI2 * 32 + l], ch[LF_QX * 32 + l], uu, vv, uv2, ge, gm1, sn, aprev);
-      lu_apply(ch[(FWD ? LF_FCY : LF_BCY) * 32 + l], ch[(FWD ? LF_FSY : LF_BSY) * 32 + l], ch[LF_RK1 * 32 + l],
-               ch[LF_RK2 * 32 + l], ch[LF_QY * 32 + l], uu, vv, uv2, ge, gm1, sn, bout);
-    }
-    // hand the boundary contribution to the next band (its slot must have
-    // been read: the consumer is at least at step tl - LU_XB + 32)
-    if (l == lout) {
-      if (act && has_next) {
-        if (lu_spin_ge(&prog[wnext], tl - LU_XB + 32)) {
-          R* x = xout + (size_t)(tl % LU_XB) * 4;
-#pragma unroll
-          for (int n = 0; n < 4; ++n) x[n] = bout[n];
-        } else {
-          bad = true;
+        for (int n = 0; n < 4; ++n) {
+          const R st = ch[(LF_S + n) * 32 + l];
+          sn[n] = FWD ? (st + sv * (aprev[n] + bin[n])) * di : st - sv * (aprev[n] + bin[n]) * di;
         }
+        if (FWD) {
+          R* gch = recw + (int64_t)tl * LU_CHUNK;
+#pragma unroll
+          for (int n = 0; n < 4; ++n) gch[(LF_S + n) * 32 + l] = sn[n];
+        } else {
+#pragma unroll
+          for (int n = 0; n < 4; ++n) srow[n * S.qs + c] = sn[n];
+        }
+        const R uu = ch[LF_UU * 32 + l], vv = ch[LF_VV * 32 + l], uv2 = ch[LF_UV2 * 32 + l], ge = ch[LF_GE * 32 + l];
+        lu_apply(ch[(FWD ? LF_FCX : LF_BCX) * 32 + l], ch[(FWD ? LF_FSX : LF_BSX) * 32 + l], ch[LF_RI1 * 32 + l],
+                 ch[LF_RI2 * 32 + l], ch[LF_QX * 32 + l], uu, vv, uv2, ge, gm1, sn, aprev);
+        lu_apply(ch[(FWD ? LF_FCY : LF_BCY) * 32 + l], ch[(FWD ? LF_FSY : LF_BSY) * 32 + l], ch[LF_RK1 * 32 + l],
+                 ch[LF_RK2 * 32 + l], ch[LF_QY * 32 + l], uu, vv, uv2, ge, gm1, sn, bout);
       }
-      __threadfence_block();
-      prog[w] = tl + 1;
+      // hand the boundary contribution to the next band (its slot must have
+      // been read: the consumer is at least at step tl - LU_XB + 32), then
+      // publish this band's progress
+      if (l == lout) {
+        if (act && has_next) {
+          if (lu_wait_ge(&prog[wnext], tl - LU_XB + 32, seen_next)) {
+            R* x = xout + (tl & (LU_XB - 1)) * 4;
+#pragma unroll
+            for (int n = 0; n < 4; ++n) x[n] = bout[n];
+          } else {
+            bad = true;
+          }
+        }
+        lu_st_release(&prog[w], tl + 1);
+      }
     }
-    if (__any_sync(0xffffffffu, bad)) { failed = true; gfail = g; break; }
     // group done: refill its buffer with group g + 2
-    if (tl % G == G - 1 || tl == nst - 1) {
-      __syncwarp();
-      if (l == 0 && g + 2 < ngrp) issue(g + 2);
-    }
+    __syncwarp();
+    if (l == 0 && g + 2 < ngrp) issue(g + 2);
   }
-  if (failed) {
-    if (l == lout) prog[w] = 1 << 30;  // release a waiting neighbour (it gives up on its own bound otherwise)
+  if (__any_sync(0xffffffffu, bad) && gfail < 0) gfail = ngrp;
+  if (gfail >= 0) {
+    if (l == lout) lu_st_release(&prog[w], 1 << 30);  // release a waiting neighbour
     if (l == 0) {
       // copies issued and not consumed: groups gfail .. gfail+1; wait
       // (bounded) before the CTA's shared memory goes away, then flag

@@ -356,6 +356,14 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
         s[v + 1] = s[v + 1] + a + b;
       }
     }
+    if (S.sinf) {
+      // f32 path: remove the f32 residual of the uniform freestream on this
+      // mesh (exactly 0 in real arithmetic: closed cells, uniform state);
+      // what remains of it in f32 is metric / state rounding that would
+      // otherwise set the floor of the residual
+#pragma unroll
+      for (int v = 0; v < 4; ++v) s[v] = s[v] - S.sinf[(int64_t)v * S.qs + o];
+    }
     if ((flags & AS_TS) && p.timespectral && S.Ds) {
       // timespectralrhs (sources.f:16-24): s(n) -= rotf*Ds(nsp,m)*q(m)
       const int64_t n2 = (int64_t)jd * kd;

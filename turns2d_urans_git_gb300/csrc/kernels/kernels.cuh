@@ -16,11 +16,13 @@
 namespace ot2d {
 
 // true when the speed of sound squared of state q (Q/J, 4 variables) is at
-// or below 0.002 or not finite (the reference's mstop, step.f:366-368)
-__device__ __forceinline__ bool monitor_bad(double ggm1, const double* q) {
-  const double q1 = q[0], qq = q[1] * q[1] + q[2] * q[2];
-  const double lhs = ggm1 * (q[3] * q1 - 0.5 * qq), rhs = 0.002 * q1 * q1;
-  return !(q1 > 0.0) || !(lhs > rhs) || !isfinite(lhs);
+// or below 0.002 or not finite (the reference's mstop, step.f:366-368);
+// evaluated in T (the mixed path checks its f32 copy of the updated state)
+template <class T>
+__device__ __forceinline__ bool monitor_bad(T ggm1, const T* q) {
+  const T q1 = q[0], qq = q[1] * q[1] + q[2] * q[2];
+  const T lhs = ggm1 * (q[3] * q1 - (T)0.5 * qq), rhs = (T)0.002 * q1 * q1;
+  return !(q1 > (T)0) || !(lhs > rhs) || !isfinite(lhs);
 }
 
 // Cell-parallel mapping: slice i owns blocks [first[i], first[i+1]) of
@@ -68,7 +70,7 @@ __global__ void k_bc(const Slice<R>* __restrict__ sl, int advance) {
       else { j = jd; k = i - (2 * jd + kd - 2) + 2; }
       const int64_t o = at(jd, j, k);
       double qh[4] = {S.q64[o], S.q64[S.qs + o], S.q64[2 * S.qs + o], S.q64[3 * S.qs + o]};
-      bad = bad || monitor_bad(S.P->ggm1, qh);
+      bad = bad || monitor_bad<double>(S.P->ggm1, qh);
     }
     if (bad) atomicOr(&S.ist[2], 2);
   }
@@ -237,11 +239,11 @@ __global__ void __launch_bounds__(CELL_BS) k_lu_edges(const Slice<R>* __restrict
   lu_edge_cell(S, *S.P, j, k, scale);
 }
 
-template <class R, bool FWD>
-__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int G, int only_lu) {
+template <class R, bool FWD, int G>
+__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int only_lu) {
   extern __shared__ __align__(128) unsigned char lu_smem[];
   if (only_lu && sl[blockIdx.x].P->ilhs != 1) return;
-  lu_sweep_slice<R, FWD>(sl[blockIdx.x], G, blockDim.x >> 5, lu_smem);
+  lu_sweep_slice<R, FWD, G>(sl[blockIdx.x], blockDim.x >> 5, lu_smem);
 }
 
 template <class R>
@@ -468,17 +470,17 @@ __global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__
   const int64_t o = at(S.jd, j, k);
   int ibi = S.iblank[o];
   double m = (double)(ibi > 0 ? ibi : 0);
-  double qn[4];
+  R qn[4];
 #pragma unroll
   for (int n = 0; n < 4; ++n) {
     double v = S.q64[n * S.qs + o] + (double)S.s[n * S.qs + o] * m;
-    qn[n] = v;
     S.q64[n * S.qs + o] = v;
-    if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = (R)v;
+    qn[n] = (R)v;
+    if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = qn[n];
   }
   // monitor of the updated cell (step.f:356-370), free of divisions:
   // a^2 <= 0.002  <=>  ggm1*(q4*q1 - qq/2) <= 0.002*q1^2 for q1 > 0
-  if (S.ist && monitor_bad(p.ggm1, qn)) atomicOr(&S.ist[2], 2);
+  if (S.ist && monitor_bad<R>((R)p.ggm1, qn)) atomicOr(&S.ist[2], 2);
 }
 
 // compute copy of the whole state from the FP64 master (after the host

@@ -52,6 +52,8 @@ template <class R> cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, 
 // only_lu = 1: skip slices whose ilhs is not 1 (mixed batches); 0: every slice
 template <class R> cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st,
                                             int only_lu);
+// the tiled residual alone with assembly flags AS_* (no norms)
+template <class R> cudaError_t launch_resid_tiles(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st);
 template <class R> cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b, int inviscid, int viscous, cudaStream_t st);
 // assembly flags: see AS_* in kernels.cuh
 enum { AS_ACC = 1, AS_INV = 2, AS_VISC = 4, AS_TS = 8, AS_NORM = 16 };

@@ -29,6 +29,14 @@ cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, c
   return cudaGetLastError();
 }
 template <class R>
+cudaError_t launch_resid_tiles(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st) {
+  constexpr size_t smem = rt_smem_bytes<R>();
+  cudaError_t e = cudaFuncSetAttribute(k_resid<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_resid<R><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags & ~AS_NORM, b.d_part);
+  return cudaGetLastError();
+}
+template <class R>
 cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b, int inviscid, int viscous, cudaStream_t st) {
   if (inviscid) k_faces<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   if (viscous) k_visc<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
@@ -57,12 +65,29 @@ cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaSt
   const size_t smem = lu_smem_bytes<R>(nw, G, maxcol);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_lu_sweep<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_lu_sweep<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    const void* ks[] = {(const void*)k_lu_sweep<R, true, 8>, (const void*)k_lu_sweep<R, false, 8>,
+                        (const void*)k_lu_sweep<R, true, 4>, (const void*)k_lu_sweep<R, false, 4>,
+                        (const void*)k_lu_sweep<R, true, 2>, (const void*)k_lu_sweep<R, false, 2>,
+                        (const void*)k_lu_sweep<R, true, 1>, (const void*)k_lu_sweep<R, false, 1>};
+    for (const void* k : ks) {
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      if (e != cudaSuccess) return e;
+    }
     attr_set = true;
   }
-  k_lu_sweep<R, true><<<b.nslice, 32 * nw, smem, st>>>(d_sl, G, only_lu);
-  k_lu_sweep<R, false><<<b.nslice, 32 * nw, smem, st>>>(d_sl, G, only_lu);
+  auto run = [&](auto fwd, auto bwd) -> cudaError_t {
+    fwd<<<b.nslice, 32 * nw, smem, st>>>(d_sl, only_lu);
+    bwd<<<b.nslice, 32 * nw, smem, st>>>(d_sl, only_lu);
+    return cudaSuccess;
+  };
+  cudaError_t e;
+  switch (G) {
+    case 8: e = run(k_lu_sweep<R, true, 8>, k_lu_sweep<R, false, 8>); break;
+    case 4: e = run(k_lu_sweep<R, true, 4>, k_lu_sweep<R, false, 4>); break;
+    case 2: e = run(k_lu_sweep<R, true, 2>, k_lu_sweep<R, false, 2>); break;
+    default: e = run(k_lu_sweep<R, true, 1>, k_lu_sweep<R, false, 1>); break;
+  }
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 template <class R>
@@ -160,6 +185,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   template cudaError_t launch_rbc<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
   template cudaError_t launch_lusgs<R>(const Slice<R>*, const Batch&, int, cudaStream_t, int);          \
   template cudaError_t launch_faces<R>(const Slice<R>*, const Batch&, int, int, cudaStream_t);          \
+  template cudaError_t launch_resid_tiles<R>(const Slice<R>*, const Batch&, int, cudaStream_t);         \
   template cudaError_t launch_assemble<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
   template cudaError_t launch_sa<R>(const Slice<R>*, const Batch&, cudaStream_t);                       \
   template cudaError_t launch_sst<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
