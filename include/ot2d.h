@@ -101,7 +101,8 @@ int ot2d_time_step(double* q, double* xx, double* xy, double* yx, double* yy, do
 int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
                double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu,
                double* tscale);
-/* src/lhs.f:817-818 (ilhs = 2: pentadiagonal lhsinv, lhs.f:1536-1816) */
+/* src/lhs.f:817-818: pentadiagonal lhsinv (lhs.f:1536-1816), or the
+ * upwind-split lhsinv_up (lhs.f:1333-1533) when params ilhs = 3 */
 int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
                double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu, int32_t* iblank,
                double* tscale, double* bt);
@@ -175,6 +176,11 @@ typedef struct ot2d_result {
 ot2d_solver* ot2d_solver_create(int32_t device, int32_t precision);
 void ot2d_solver_destroy(ot2d_solver* s);
 int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value);
+/* Also count an instance as converged once its CL and CD stayed within a
+ * band of width dcl / dcd over the last 8 status checks and its L2 norm is a
+ * decade below its peak (0, 0: residual criterion only, the default).  The
+ * forces of running instances are then evaluated at every check. */
+int ot2d_solver_set_force_tol(ot2d_solver* s, double dcl, double dcd);
 /* read the device status table now and retire finished instances */
 int ot2d_solver_sync(ot2d_solver* s);
 /* the CUDA stream (cudaStream_t) the solver launches on */

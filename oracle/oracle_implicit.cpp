@@ -372,7 +372,75 @@ static void lhsinv(const P& p, A3 q, A3 s, A2 qn, A2 cn, A2 d2p, int ms, int me,
   }
 }
 
-/* lhs.f:817-1057 (ilhs = 2).  The tmp coefficient arrays of lhsinv at m = ms
+/* lhs.f:1333-1533: the upwind-split line inversion of ilhs = 3 (a
+ * tridiagonal system solved with pentadag) */
+static void lhsinv_up(const P& p, A3 q, A3 s, A2 qn, A2 cn, int ms, int me, int ns, int ne, int idir, A2 xn, A2 yn,
+                      A2 vnu, A2 tscale, A2 bt) {
+  const int nq = p.nq, nmv = p.nmv;
+  const size_t L = (size_t)me + 3;
+  std::vector<double> tscal(L), v1(L), v2(L), v3(L);
+  std::vector<double> a(L), b(L), c(L), d(L), e(L), f(L), a1(L), b1(L), c1(L), d1(L), e1(L), f1(L);
+  std::vector<double> dp(L * 5), dm(L * 5);
+  const double epsval = 0.05, fac = 1.05, Mp = p.Mp;
+  auto Q = [&](int m, int n, int v) -> double& { return idir == 1 ? q(m, n, v) : q(n, m, v); };
+  auto S = [&](int m, int n, int v) -> double& { return idir == 1 ? s(m, n, v) : s(n, m, v); };
+  auto X2 = [&](A2 a2, int m, int n) -> double& { return idir == 1 ? a2(m, n) : a2(n, m); };
+  for (int n = ns; n <= ne; ++n) {
+    for (int m = ms; m <= me; ++m) {
+      tscal[m] = X2(tscale, m, n);
+      const double btv = X2(bt, m, n);
+      const double bSq = (Mp * Mp) / (btv - (Mp * Mp) * (btv - 1));
+      const double qv = X2(qn, m, n), cv = X2(cn, m, n);
+      const double X = std::sqrt(((1. - bSq) * qv) * ((1. - bSq) * qv) + 4. * bSq * cv * cv);
+      const double eig1 = qv, eig2 = 0.5 * ((bSq + 1.) * qv + X), eig3 = 0.5 * ((bSq + 1.) * qv - X);
+      const double eps = epsval * std::sqrt(p2(X2(xn, m, n)) + p2(X2(yn, m, n)));
+      const double eg[5] = {0, eig1, eig1, eig2, eig3};
+      for (int i = 1; i <= 4; ++i) {
+        dp[(size_t)m * 5 + i] = 0.5 * (eg[i] + fac * std::sqrt(p2(eg[i]) + p2(eps)));
+        dm[(size_t)m * 5 + i] = 0.5 * (eg[i] - fac * std::sqrt(p2(eg[i]) + p2(eps)));
+      }
+    }
+    for (int m = ms + 1; m <= me - 1; ++m) {
+      v1[m] = (X2(xn, m, n) * X2(xn, m, n) + X2(yn, m, n) * X2(yn, m, n)) / Q(m, n, nq);
+      v1[m] = v1[m] + (X2(xn, m + 1, n) * X2(xn, m + 1, n) + X2(yn, m + 1, n) * X2(yn, m + 1, n)) / Q(m + 1, n, nq);
+      v1[m] = v1[m] * Q(m, n, nq) * X2(vnu, m, n);
+      v3[m] = (X2(xn, m, n) * X2(xn, m, n) + X2(yn, m, n) * X2(yn, m, n)) / Q(m, n, nq);
+      v3[m] = v3[m] + (X2(xn, m - 1, n) * X2(xn, m - 1, n) + X2(yn, m - 1, n) * X2(yn, m - 1, n)) / Q(m - 1, n, nq);
+      v3[m] = v3[m] * Q(m, n, nq) * X2(vnu, m, n);
+      v2[m] = 0.5 * (v1[m] + v3[m]);
+    }
+    v1[ms] = v2[ms] = v3[ms] = 0;
+    v1[me] = v2[me] = v3[me] = 0;
+    for (int i = 1; i <= nmv; ++i) {
+      for (int m = ms; m <= me; ++m) {
+        a1[m] = 0.; b1[m] = 0.; c1[m] = 0.; d1[m] = 0.; e1[m] = 0.;
+        f1[m] = S(m, n, i);
+        b1[m] = b1[m] - dp[(size_t)m * 5 + i];
+        d1[m] = d1[m] + dm[(size_t)m * 5 + i];
+        c1[m] = c1[m] + dp[(size_t)m * 5 + i] - dm[(size_t)m * 5 + i];
+        b1[m] = b1[m] - 0.5 * v1[m];
+        c1[m] = c1[m] + v2[m];
+        d1[m] = d1[m] - 0.5 * v3[m];
+        b1[m] = (m <= me - 1) ? b1[m] * tscal[m + 1] : b1[m] * tscal[m];
+        d1[m] = (m >= ms + 1) ? d1[m] * tscal[m - 1] : d1[m] * tscal[m];
+        c1[m] = c1[m] * tscal[m] + 1.0;
+      }
+      for (int m = ms + 1; m <= me - 1; ++m) {
+        a[m - ms] = a1[m]; b[m - ms] = b1[m]; c[m - ms] = c1[m];
+        d[m - ms] = d1[m]; e[m - ms] = e1[m]; f[m - ms] = f1[m];
+      }
+      const int N = me - ms - 1;
+      f[1] = f[1] - b1[ms] * f1[ms] / c1[ms];
+      f[N] = f[N] - d1[me] * f1[me] / c1[me];
+      d[1] = 0; e[1] = 0; e[2] = 0;
+      b[N] = 0; a[N] = 0; a[N - 1] = 0;
+      pentadag(&a[1], &b[1], &c[1], &d[1], &e[1], &f[1], N);
+      for (int m = ms + 1; m <= me - 1; ++m) S(m, n, i) = f[m - ms];
+    }
+  }
+}
+
+/* lhs.f:817-1057 (ilhs = 2, or 3 with lhsinv_up).  The tmp coefficient arrays of lhsinv at m = ms
  * and m = me are never assigned by the reference and are read as 0 here
  * (what a fresh allocation holds). */
 void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, I2 iblank, A2 tscale, A2 bt) {
@@ -433,7 +501,8 @@ void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
     d2px(j, k) = d2px(j, k) / std::fabs(pr(j + 1, k) + 2. * pr(j, k) + pr(j - 1, k));
   }
   for (int k = ks - 1; k <= ke + 1; ++k) { d2px(js - 1, k) = 0; d2px(je + 1, k) = 0; }
-  lhsinv(p, q, s, qx, cx, d2px, js - 1, je + 1, ks - 1, ke + 1, 1, xx, xy, vn, iblank, tscale, bt);
+  if (p.ilhs == 3) lhsinv_up(p, q, s, qx, cx, js - 1, je + 1, ks - 1, ke + 1, 1, xx, xy, vn, tscale, bt);
+  else lhsinv(p, q, s, qx, cx, d2px, js - 1, je + 1, ks - 1, ke + 1, 1, xx, xy, vn, iblank, tscale, bt);
   /* :948-975 multiply by N inverse */
   for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js - 1; j <= je + 1; ++j) {
     double cjkl = std::sqrt(ggm1 * (q(j, k, 4) - uv(j, k)));
@@ -454,7 +523,8 @@ void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
     d2py(j, k) = d2py(j, k) / std::fabs(pr(j, k + 1) + 2. * pr(j, k) + pr(j, k - 1));
   }
   for (int j = js - 1; j <= je + 1; ++j) { d2py(j, ks - 1) = 0; d2py(j, ke + 1) = 0; }
-  lhsinv(p, q, s, qy, cy, d2py, ks - 1, ke + 1, js - 1, je + 1, 2, yx, yy, vn, iblank, tscale, bt);
+  if (p.ilhs == 3) lhsinv_up(p, q, s, qy, cy, ks - 1, ke + 1, js - 1, je + 1, 2, yx, yy, vn, tscale, bt);
+  else lhsinv(p, q, s, qy, cy, d2py, ks - 1, ke + 1, js - 1, je + 1, 2, yx, yy, vn, iblank, tscale, bt);
   /* :1005-1034 multiply by T_eta */
   for (int k = ks - 1; k <= ke + 1; ++k) for (int j = js - 1; j <= je + 1; ++j) {
     double uu = q(j, k, 2), vv = q(j, k, 3);

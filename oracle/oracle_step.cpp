@@ -282,7 +282,7 @@ int oro_step(const P* pp, double* q, double* s, double* x, double* y, const doub
     if (p.ilhs == 1) {
       ilu2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
             v2(pp, turmu + o), ts);
-    } else if (p.ilhs == 2) {
+    } else if (p.ilhs == 2 || p.ilhs == 3) {
       arc2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
             v2(pp, turmu + o), I2{iblank + o, jd}, ts, v2(pp, bt + o));
     } else {

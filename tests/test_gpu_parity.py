@@ -159,11 +159,13 @@ def test_solver_sst_fp64_matches_oracle():
         assert abs(a - b) <= 1e-10 * max(abs(b), 1e-3)
 
 
-@pytest.mark.parametrize("visc", [False, True])
-def test_arc2d(visc):
-    """arc2d (diagonalised ADI with pentadiagonal line inversions,
-    lhs.f:817-1057) on a perturbed state and a random right-hand side."""
+@pytest.mark.parametrize("visc,ilhs", [(False, 2), (True, 2), (True, 3)])
+def test_arc2d(visc, ilhs):
+    """arc2d (diagonalised ADI, lhs.f:817-1057) with the pentadiagonal
+    (ilhs 2) or upwind tridiagonal (ilhs 3) line inversions, on a perturbed
+    state and a random right-hand side."""
     c = Case(viscous=visc, seed=19)
+    c.p.ilhs = ilhs
     L = ob.lib()
     L.oro_time_step(_o(c), ob.ptr(c.q), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug),
                     ob.ptr(c.vg), ob.ptr(c.tscale), ob.ptr(c.bt), ob.ptr(c.iblank))
@@ -180,13 +182,15 @@ def test_arc2d(visc):
     assert relerr(q, qo) <= TOL
 
 
-@pytest.mark.parametrize("kind", ["euler", "sst_weno"])
+@pytest.mark.parametrize("kind", ["euler", "euler_up", "sst_weno"])
 def test_solver_adi_fp64_matches_oracle(kind):
-    """The batched solver with the ADI operator (ilhs = 2), FP64, against the
-    oracle driver: an inviscid case and a k-omega SST + WENO case."""
-    if kind == "euler":
-        _, prm, xv, yv = api.cmesh_case(97, 25, ds_wall=2e-3, invisc=1, lamin=1, irhsy=-3, ilim=1, ilhs=2,
-                                        iconstant_cfl=1, dt=2.0, fsmach=0.8, alfa=1.25)
+    """The batched solver with the ADI operator (ilhs = 2, or 3 for the
+    upwind variant), FP64, against the oracle driver: inviscid cases and a
+    k-omega SST + WENO case."""
+    if kind.startswith("euler"):
+        _, prm, xv, yv = api.cmesh_case(97, 25, ds_wall=2e-3, invisc=1, lamin=1, irhsy=-3, ilim=1,
+                                        ilhs=3 if kind == "euler_up" else 2, iconstant_cfl=1, dt=2.0, fsmach=0.8,
+                                        alfa=1.25)
     else:
         _, prm, xv, yv = api.cmesh_case(97, 33, naca=(0.02, 0.4, 0.12), ds_wall=1e-3, invisc=0, lamin=0, iturb=2,
                                         irhsy=-3, ilim=4, ilhs=2, iconstant_cfl=1, dt=2.0, fsmach=0.73, alfa=2.8,

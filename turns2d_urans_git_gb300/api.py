@@ -154,6 +154,14 @@ class Solver:
         L.ot2d_solver_set_option(self._h, 2, 1 if keep_q else 0)
         self.precision = precision
 
+    def set_force_tol(self, dcl, dcd):
+        """Converge also on stable forces (see ot2d_solver_set_force_tol)."""
+        f = lib().ot2d_solver_set_force_tol
+        f.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        rc = f(self._h, float(dcl), float(dcd))
+        if rc != 0:
+            raise RuntimeError("ot2d_solver_set_force_tol failed (%d)" % rc)
+
     def close(self):
         if self._h:
             lib().ot2d_solver_destroy(self._h)

@@ -167,6 +167,7 @@ Slice<double> base_slice(int nsp, int nspec, int64_t qs) {
   S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = g_ctx.dred + (size_t)RED_N * (nsp - 1);
   S.ist = nullptr;
+  slice_consts(S, p);
   return S;
 }
 
@@ -536,7 +537,7 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   int err = 0;
   if (prepare(nspec, err)) return fail(err);
   const ot2d_params& p = g_ctx.P;
-  if (!dims_ok(jd, kd) || (p.ilhs != 1 && p.ilhs != 2) || p.itnmax > 1 || (!p.lamin && p.iturb != 1 && p.iturb != 2) ||
+  if (!dims_ok(jd, kd) || p.ilhs < 1 || p.ilhs > 3 || p.itnmax > 1 || (!p.lamin && p.iturb != 1 && p.iturb != 2) ||
       p.itrans != 0)
     return fail(OT2D_ERR_ARG);
   if (!q || !s || !x || !y || !xv || !yv || !iblank || !xx || !xy || !yx || !yy || !turmu || !tscale) return fail(OT2D_ERR_ARG);
@@ -593,7 +594,7 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   if (!err && launch_residual<double>(B.d_sl, B.b, visc, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_rbc<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && p.ilhs == 1 && launch_lusgs<double>(B.d_sl, B.b, 1, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
-  if (!err && p.ilhs == 2 && launch_adi<double>(B.d_sl, B.b, 1, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
+  if (!err && p.ilhs != 1 && launch_adi<double>(B.d_sl, B.b, 1, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && turb && launch_sa<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && sst && launch_sst<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   if (!err && launch_update<double>(B.d_sl, B.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;

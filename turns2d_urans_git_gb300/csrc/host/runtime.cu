@@ -23,7 +23,7 @@ inline size_t al(size_t b) { return (b + ALIGN - 1) / ALIGN * ALIGN; }
 // scratch arrays per time instance: the SA bands (9) and the drop-in face
 // fluxes (20) fit in 20; the k-omega SST fields and two-equation bands take 27
 inline int nscratch(const ot2d_params& p) {
-  return ((!p.lamin && p.iturb == 2) || p.ilhs == 2) ? (SST_NSCRATCH > ADI_NSCRATCH ? SST_NSCRATCH : ADI_NSCRATCH) + 1
+  return ((!p.lamin && p.iturb == 2) || p.ilhs != 1) ? (SST_NSCRATCH > ADI_NSCRATCH ? SST_NSCRATCH : ADI_NSCRATCH) + 1
                                                      : 20;
 }
 inline bool is_sst(const ot2d_params& p) { return !p.lamin && p.iturb == 2; }
@@ -126,8 +126,8 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
                  cudaStream_t st) {
   if (!xv1 || !yv1 || p.nspec < 1 || p.nhalo != 1 || p.jd != p.jmax + 1 || p.kd != p.kmax + 1) return OT2D_ERR_ARG;
   if (precision != OT2D_FP64 && precision != OT2D_FP32_MIXED) return OT2D_ERR_ARG;
-  if (p.ilhs != 1 && p.ilhs != 2) return OT2D_ERR_ARG;      // LU-SGS or ADI (pentadiagonal)
-  if (p.ilhs == 2 && (p.jd < 10 || p.kd < 10)) return OT2D_ERR_ARG;  // ADI lines of >= 8 points
+  if (p.ilhs < 1 || p.ilhs > 3) return OT2D_ERR_ARG;        // LU-SGS or ADI (pentadiagonal / upwind)
+  if (p.ilhs != 1 && (p.jd < 10 || p.kd < 10)) return OT2D_ERR_ARG;  // ADI lines of >= 8 points
   if (!p.lamin && p.iturb != 1 && p.iturb != 2) return OT2D_ERR_ARG;  // SA or k-omega SST
   if (p.itrans != 0) return OT2D_ERR_ARG;                            // no transition model
   d = DevSolve{};
@@ -290,6 +290,7 @@ Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
   S.w = (R*)d.w + (size_t)(nsp - 1) * d.wstride * d.nscratch;
   S.wd2 = D_(d.wd2);
   S.sinf = R_(d.sinf);
+  slice_consts(S, p);
   S.wstride = (int64_t)d.wstride;
   S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = red; S.ist = ist;

@@ -6,6 +6,7 @@
 // Convergence, blow-up and monitor flags are raised on the device; the host
 // reads the small status table every `check_every` iterations and retires
 // finished requests (forces in FP64, slot and memory freed).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -26,7 +27,12 @@ struct Rec {
   bool live = false;
   ot2d_result res{};
   std::vector<double> qkeep;
+  // force-stability convergence (ot2d_solver_set_force_tol): CL, CD of
+  // the last FORCE_WIN status checks
+  double win_cl[8] = {0}, win_cd[8] = {0};
+  int nwin = 0;
 };
+constexpr int FORCE_WIN = 8;
 
 double now_s() {
   using namespace std::chrono;
@@ -55,6 +61,7 @@ struct ot2d_solver {
   int next_id = 0;
   double t0 = 0;
   int check_every = 25;
+  double force_dcl = 0, force_dcd = 0;   // > 0: also converge on stable forces
   int keep_q = 0;
   int since_check = 0;
   bool any_viscous = false;
@@ -120,7 +127,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
     if (!r.d.P.invisc) s->any_viscous = true;
     if (!r.d.P.lamin && r.d.P.iturb == 1) s->turb_bits |= 1;
     if (!r.d.P.lamin && r.d.P.iturb == 2) s->turb_bits |= 2;
-    s->lhs_bits |= (r.d.P.ilhs == 2) ? 2 : 1;
+    s->lhs_bits |= (r.d.P.ilhs == 1) ? 1 : 2;
   }
   s->dirty = false;
   if (sl.empty()) return OT2D_OK;
@@ -255,6 +262,32 @@ int check(ot2d_solver* s) {
     r.res.converged = (conv && !status) ? 1 : 0;
     if (status || conv || its >= r.max_iters) done.push_back(id);
   }
+  if (s->force_dcl > 0 || s->force_dcd > 0) {
+    // forces of the instances still running; converged once CL and CD stayed
+    // within the tolerances over the last FORCE_WIN checks and the L2 norm
+    // is a decade below its peak
+    std::vector<int> run;
+    for (int id : s->live)
+      if (std::find(done.begin(), done.end(), id) == done.end()) run.push_back(id);
+    if (!run.empty()) {
+      int fe = (s->precision == OT2D_FP64) ? forces_t<double>(s, run, s->f64) : forces_t<float>(s, run, s->f32);
+      if (fe) return fe;
+      for (int id : run) {
+        Rec& r = s->recs[id];
+        const double* red = s->h_red + (size_t)RED_N * r.slots[0];
+        r.win_cl[r.nwin % FORCE_WIN] = r.res.cl;
+        r.win_cd[r.nwin % FORCE_WIN] = r.res.cd;
+        ++r.nwin;
+        if (r.nwin < FORCE_WIN || !(red[5] <= 0.1 * red[6])) continue;
+        double lo_l = r.win_cl[0], hi_l = lo_l, lo_d = r.win_cd[0], hi_d = lo_d;
+        for (int i = 1; i < FORCE_WIN; ++i) {
+          lo_l = std::min(lo_l, r.win_cl[i]); hi_l = std::max(hi_l, r.win_cl[i]);
+          lo_d = std::min(lo_d, r.win_cd[i]); hi_d = std::max(hi_d, r.win_cd[i]);
+        }
+        if (hi_l - lo_l <= s->force_dcl && hi_d - lo_d <= s->force_dcd) { r.res.converged = 1; done.push_back(id); }
+      }
+    }
+  }
   if (done.empty()) return OT2D_OK;
   int e = (s->precision == OT2D_FP64) ? forces_t<double>(s, done, s->f64) : forces_t<float>(s, done, s->f32);
   const double t = now_s() - s->t0;
@@ -312,6 +345,12 @@ int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value) {
   if (key == OT2D_OPT_CHECK_EVERY && value >= 1) { s->check_every = value; return OT2D_OK; }
   if (key == OT2D_OPT_KEEP_Q) { s->keep_q = value ? 1 : 0; return OT2D_OK; }
   return OT2D_ERR_ARG;
+}
+
+int ot2d_solver_set_force_tol(ot2d_solver* s, double dcl, double dcd) {
+  if (!s || dcl < 0 || dcd < 0) return OT2D_ERR_ARG;
+  s->force_dcl = dcl; s->force_dcd = dcd;
+  return OT2D_OK;
 }
 
 int ot2d_solver_add(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv, double orders,

@@ -31,6 +31,10 @@ struct Slice {
   const R* sn;                       // SA / SST wall distance (static geometry)
   const double* wd2;                 // SST wall term dely2 on the wall halo cells (null unless SST)
   const R* sinf;                     // mixed path: f32 residual of the uniform freestream (4 vars), or null
+  // constants of the residual derived from the double parameters once, on
+  // the host (slice_consts): reconstruction (eulerrhs.f:40-53), Sutherland
+  // and Prandtl factors (visrhs.f:36-44)
+  R k_th, k_qt, k_epsl_x, k_epsl_y, k_c2b, k_c2bp, k_prtr, k_gkpr, k_dre, k_gm1, k_ggm1;
   R* w;                              // scratch of this slice (phase dependent)
   R* lurec;                          // LU-SGS sweep records (skewed bands)
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)
@@ -40,6 +44,25 @@ struct Slice {
   // FP64 geometry kept for FP64-only work (forces, BC metrics in mixed mode)
   const double *xx64, *xy64, *yx64, *yy64, *ug64, *vg64;
 };
+
+// Fill the residual constants of a slice from its parameters (host side;
+// the same double expressions the kernels would evaluate).
+template <class R>
+inline void slice_consts(Slice<R>& S, const ot2d_params& p) {
+  const int irhs = p.irhsy < 0 ? -p.irhsy : p.irhsy;
+  S.k_th = (R)((double)(irhs - 2) / (double)irhs);
+  S.k_qt = (irhs == 1) ? (R)0.0 : (R)0.25;
+  const double ex = 10. / (double)p.jmax, ey = 10. / (double)p.kmax;
+  S.k_epsl_x = (R)((ex * ex) * ex);
+  S.k_epsl_y = (R)((ey * ey) * ey);
+  S.k_c2b = (R)(198.6 / p.tinf);
+  S.k_c2bp = S.k_c2b + (R)1.;
+  S.k_prtr = (R)(p.pr / 0.9);
+  S.k_gkpr = (R)(p.gamma / p.pr);
+  S.k_dre = (R)(.5 / p.rey);
+  S.k_gm1 = (R)p.gm1;
+  S.k_ggm1 = (R)p.ggm1;
+}
 
 // Fortran SIGN(a,b): |a| with the IEEE sign of b (gfortran semantics).
 template <class R> __device__ __forceinline__ R fsign(R a, R b) { return copysign(fabs(a), b); }

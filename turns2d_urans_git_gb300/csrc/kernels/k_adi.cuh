@@ -1,6 +1,7 @@
 // k_adi.cuh -- the diagonalised ADI operator arc2d with pentadiagonal line
 // inversions (src/lhs.f:817-1057 with lhsinv :1536-1816 and pentadag
-// :1819-1873; ilhs = 2).
+// :1819-1873; ilhs = 2) or the upwind-split tridiagonal ones (lhsinv_up
+// :1333-1533; ilhs = 3).
 //
 // The reference converts q to primitive variables in place, multiplies s by
 // T_xi^-1, inverts a scalar pentadiagonal system per j-line and variable,
@@ -24,7 +25,7 @@ enum ADIw { A_P = 0, A_QX, A_QY, A_CX, A_CY, A_UV, A_VN, A_GE, A_U, A_V, A_E, A_
             A_DM, A_EM = A_DM + 4, A_N = A_EM + 4 };
 static_assert(A_N <= ADI_NSCRATCH, "ADI scratch layout");
 
-__device__ __forceinline__ bool adi_slice(const ot2d_params& p) { return p.ilhs == 2; }
+__device__ __forceinline__ bool adi_slice(const ot2d_params& p) { return p.ilhs == 2 || p.ilhs == 3; }
 
 // line view of direction dir (0: j lines, m = j, n = k; 1: k lines, m = k, n = j)
 __device__ __forceinline__ int64_t adi_at(int jd, int dir, int m, int n) { return dir == 0 ? at(jd, m, n) : at(jd, n, m); }
@@ -211,6 +212,27 @@ __device__ __forceinline__ AdiRow<R> adi_row(const Slice<R>& S, const ot2d_param
     v2 = (R)0.5 * (v1 + v3);
   }
   AdiRow<R> r;
+  auto T = [&](int mm) { return ts[adi_at(jd, dir, mm, n)]; };
+  if (p.ilhs == 3) {
+    // lhsinv_up (lhs.f:1387-1501): upwind split eigenvalues, tridiagonal
+    const R* xn = dir == 0 ? S.xx : S.yx;
+    const R* yn = dir == 0 ? S.xy : S.yy;
+    const R eps = (R)0.05 * sqrt(sq(xn[o]) + sq(yn[o]));
+    const R fac = (R)1.05;
+    const R dpl = (R)0.5 * (di + fac * sqrt(sq(di) + sq(eps)));
+    const R dmi = (R)0.5 * (di - fac * sqrt(sq(di) + sq(eps)));
+    r.a = (R)0.; r.b = (R)0.; r.c = (R)0.; r.d = (R)0.; r.e = (R)0.;
+    r.b = r.b - dpl;
+    r.d = r.d + dmi;
+    r.c = r.c + dpl - dmi;
+    r.b = r.b - (R)0.5 * v1;
+    r.c = r.c + v2;
+    r.d = r.d - (R)0.5 * v3;
+    r.b = (m <= me - 1) ? r.b * T(m + 1) : r.b * T(m);
+    r.d = (m >= ms + 1) ? r.d * T(m - 1) : r.d * T(m);
+    r.c = r.c * T(m) + (R)1.0;
+    return r;
+  }
   r.a = S.w[A_AT * ws + o]; r.b = S.w[A_BT * ws + o]; r.c = S.w[A_CT * ws + o];
   r.d = S.w[A_DT * ws + o]; r.e = S.w[A_ET * ws + o];
   r.b = r.b - di * (R)0.5;
@@ -218,7 +240,6 @@ __device__ __forceinline__ AdiRow<R> adi_row(const Slice<R>& S, const ot2d_param
   r.b = r.b - (R)0.5 * v1;
   r.c = r.c + v2;
   r.d = r.d - (R)0.5 * v3;
-  auto T = [&](int mm) { return ts[adi_at(jd, dir, mm, n)]; };
   r.a = (m <= me - 2) ? r.a * T(m + 2) : r.a * T(m);
   r.b = (m <= me - 1) ? r.b * T(m + 1) : r.b * T(m);
   r.d = (m >= ms + 1) ? r.d * T(m - 1) : r.d * T(m);

@@ -66,7 +66,7 @@ __device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_para
                                               int j, int k, bool visc) {
   const int64_t o = at(S.jd, j, k), qs = S.qs;
   const R q1 = S.q[o], q2 = S.q[qs + o], q3 = S.q[2 * qs + o], q4 = S.q[3 * qs + o], J = S.q[(p.nq - 1) * qs + o];
-  const R gm1 = (R)p.gm1;
+  const R gm1 = S.k_gm1;
   const R rhoi = (R)1.0 / q1;
   sm.at(RS_RHO, r) = q1 * J;
   const R u = q2 * rhoi, v = q3 * rhoi;
@@ -75,9 +75,9 @@ __device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_para
   const R ppp = gm1 * (q4 - (R)0.5 * (sq(q2) + sq(q3)) / q1);
   sm.at(RS_P, r) = ppp * J;
   if (visc) {
-    const R c2b = (R)(198.6 / p.tinf), c2bp = c2b + (R)1., prtr = (R)(p.pr / 0.9);
+    const R c2b = S.k_c2b, c2bp = S.k_c2bp, prtr = S.k_prtr;
     const R e = q4 * rhoi - (R).5 * (sq(u) + sq(v));
-    const R tt = (R)p.ggm1 * e;
+    const R tt = S.k_ggm1 * e;
     const R vmue = c2bp * tt * sqrt(tt) / (c2b + tt);
     const R turm = S.turmu[o];
     sm.at(RS_E, r) = e;
@@ -248,7 +248,8 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
   const int jr = j0 - RT_H, kr = k0 - RT_H;
   const bool visc = (flags & AS_VISC) && !p.invisc;
   const bool inv = flags & AS_INV;
-  const R gm1 = (R)p.gm1;
+  const R gm1 = S.k_gm1;
+  const Recon<R> rx{p.ilim, S.k_th, S.k_qt, S.k_epsl_x}, ry{p.ilim, S.k_th, S.k_qt, S.k_epsl_y};
   // A: stage the region
   for (int r = t; r < RT_NR; r += RT_BS) {
     const int j = jr + r % RT_RW, k = kr + r / RT_RW;
@@ -260,7 +261,7 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
   const int nB = inv ? RT_TK * (RT_TJ + 1) : 0, nC = inv ? (RT_TK + 1) * RT_TJ : 0;
   const int nD1 = visc ? RT_VEH * RT_TJ : 0, nD2 = visc ? RT_TK * RT_VXW : 0;
   const int ntot = nB + nC + nD1 + nD2;
-  const R gkpr = (R)(p.gamma / p.pr), dre = (R)(.5 / p.rey);
+  const R gkpr = S.k_gkpr, dre = S.k_dre;
   for (int w = t; w < ntot; w += RT_BS) {
     if (w < nB) {
       // B: xi face j+1/2 of row k, j in j0-1..j1 (eulerrhs.f:69-167)
@@ -271,7 +272,7 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
       const RtLine<R> L{&sm, (k - kr) * RT_RW - jr, 1, max(1, jr), min(jd, jr + RT_RW - 1), gm1};
       const int64_t o = at(jd, j, k);
       R fl[4];
-      face_flux(L, make_recon<R>(p, 0), j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
+      face_flux(L, rx, j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sm.F[v * (RT_TK * (RT_TJ + 1)) + f] = fl[v];
     } else if (w < nB + nC) {
@@ -283,7 +284,7 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
       const RtLine<R> L{&sm, (j - jr) - kr * RT_RW, RT_RW, max(1, kr), min(kd, kr + RT_RH - 1), gm1};
       const int64_t o = at(jd, j, k);
       R fl[4];
-      face_flux(L, make_recon<R>(p, 1), k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
+      face_flux(L, ry, k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sm.G[v * ((RT_TK + 1) * RT_TJ) + f] = fl[v];
     } else if (w < nB + nC + nD1) {

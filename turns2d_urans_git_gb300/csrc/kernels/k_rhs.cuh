@@ -361,7 +361,7 @@ struct ViscCell { R u, v, e, vnu, gkap, rj; };
 template <class R>
 __device__ __forceinline__ ViscCell<R> visc_cell(const Slice<R>& S, const ot2d_params& p, int j, int k) {
   const int64_t o = at(S.jd, j, k), qs = S.qs;
-  const R c2b = (R)(198.6 / p.tinf), c2bp = c2b + (R)1., prtr = (R)(p.pr / 0.9);
+  const R c2b = S.k_c2b, c2bp = S.k_c2bp, prtr = S.k_prtr;
   ViscCell<R> c;
   R ra = (R)1. / S.q[o];
   c.u = S.q[qs + o] * ra; c.v = S.q[2 * qs + o] * ra;
@@ -380,7 +380,7 @@ template <class R>
 __device__ void visc_eta_face(const Slice<R>& S, int j, int k, R* V) {
   const ot2d_params& p = *S.P;
   const int jd = S.jd; const int64_t qs = S.qs;
-  const R gkpr = (R)(p.gamma / p.pr), dre = (R)(.5 / p.rey);
+  const R gkpr = S.k_gkpr, dre = S.k_dre;
   auto M = [&](const R* a, int jj, int kk) { return a[at(jd, jj, kk)]; };
   R bv[2][4], uu[2], vv[2], ee[2];
   R d1 = 0, d2 = 0, d4 = 0, d5 = 0, d7 = 0;
@@ -450,7 +450,7 @@ template <class R>
 __device__ void visc_xi_face(const Slice<R>& S, int j, int k, R* V) {
   const ot2d_params& p = *S.P;
   const int jd = S.jd; const int64_t qs = S.qs;
-  const R gkpr = (R)(p.gamma / p.pr), dre = (R)(.5 / p.rey);
+  const R gkpr = S.k_gkpr, dre = S.k_dre;
   auto M = [&](const R* a, int jj, int kk) { return a[at(jd, jj, kk)]; };
   R av[2][4], uu[2], vv[2], ee[2];
   R d1 = 0, d2 = 0, d4 = 0, d5 = 0, d7 = 0;

@@ -41,7 +41,7 @@ __device__ __forceinline__ bool sst_slice(const ot2d_params& p) { return !p.lami
 template <class R>
 __device__ __forceinline__ void sst_prep_cell(const Slice<R>& S, const ot2d_params& p, int j, int k) {
   const int64_t o = at(S.jd, j, k), qs = S.qs, ws = S.wstride;
-  const R c2b = (R)(198.6 / p.tinf), c2bp = c2b + (R)1.;
+  const R c2b = S.k_c2b, c2bp = S.k_c2bp;
   const R q1 = S.q[o], q2 = S.q[qs + o], q3 = S.q[2 * qs + o], q4 = S.q[3 * qs + o], J = S.q[(p.nq - 1) * qs + o];
   const R ra = (R)1. / q1;
   const R uvel = q2 * ra, vvel = q3 * ra;

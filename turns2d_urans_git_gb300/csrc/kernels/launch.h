@@ -39,7 +39,7 @@ struct Batch {
 // One full iteration of step.f for every slice of the batch:
 // time_step, bc, rhsup (+visrhs, +time-spectral), norms, rbc, ilu2d,
 // vmu_sa (turb bit 1), komegasst (turb bit 2), update, monitor.  lhs bit 1:
-// some slice uses LU-SGS (ilhs = 1), bit 2: some slice uses ADI (ilhs = 2).
+// some slice uses LU-SGS (ilhs = 1), bit 2: some slice uses ADI (ilhs = 2, 3).
 template <class R>
 cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st);
 
@@ -60,8 +60,9 @@ enum { AS_ACC = 1, AS_INV = 2, AS_VISC = 4, AS_TS = 8, AS_NORM = 16 };
 template <class R> cudaError_t launch_assemble(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st);
 template <class R> cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_sst(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
-// arc2d (ilhs = 2); scale = 1: preceded by s *= tscale on all cells
-// (step.f:141-148).  only_adi = 1: skip slices whose ilhs is not 2
+// arc2d (ilhs = 2 pentadiagonal, 3 upwind tridiagonal); scale = 1: preceded
+// by s *= tscale on all cells (step.f:141-148).  only_adi = 1: skip slices
+// whose ilhs is not 2 or 3
 template <class R> cudaError_t launch_adi(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st,
                                           int only_adi);
 template <class R> cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
