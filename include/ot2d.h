@@ -43,6 +43,8 @@ extern "C" {
 #define OT2D_ERR_NOPARAMS  5   /* no ot2d_set_params() before a drop-in routine      */
 #define OT2D_ERR_NOMEM     6   /* device allocation failed                           */
 #define OT2D_ERR_TIMEOUT   7   /* a bounded device wait gave up                      */
+#define OT2D_ERR_IO        8   /* a file could not be opened / read / written, or a
+                                  record is shorter than the data it should hold      */
 
 /* precision modes of the solver and of the drop-in routines */
 #define OT2D_FP64          0   /* plain FP64, operation order of the reference       */
@@ -156,6 +158,51 @@ int ot2d_norms_noalloc(const double* s, const int32_t* iblank, int32_t jd, int32
                        int32_t ks, int32_t ke, int32_t nmv, double* out, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* solution / restart files (src/io.f, src/init.f:138-206)                 */
+/* ---------------------------------------------------------------------- */
+/* Files are Fortran sequential unformatted files (4-byte record markers,
+ * 8-byte reals, 4-byte integers) in the record layout the reference writes
+ * and reads; Tecplot files use its '(3F22.13)' / '(3I10)' formats.  The
+ * library keeps its own table of Fortran unit numbers: the unit-level
+ * routines below read and write units opened with ot2d_unit_open, in the
+ * place of the reference's `open(unit=..., form=...)`.  Only itrans = 0 and
+ * num_grids = 1 grid reads are supported (OT2D_ERR_ARG otherwise). */
+/* open(unit, file=path, form='unformatted'|'formatted'), status 'unknown'
+ * (created / truncated) for writing, 'old' for reading */
+int ot2d_unit_open(int32_t unit, const char* path, int32_t formatted, int32_t for_write);
+int ot2d_unit_close(int32_t unit);
+/* one record of n integers (the mesh-size header of astore / init, istep0) */
+int ot2d_unit_write_ints(int32_t unit, const int32_t* v, int32_t n);
+/* the first n integers of the next record (the rest of the record is skipped) */
+int ot2d_unit_read_ints(int32_t unit, int32_t* v, int32_t n);
+/* src/io.f:2-170: writes fort.9 / fort.8 (fort_TS<n>.9 / .8 when ts) and
+ * SA.dat / komega.dat (SA_TS<n>.dat, komega_TS<n>.dat) in the current
+ * directory for the nmesh meshes of x, y, iblank (igrd) and q (iqdim) at the
+ * 1-based offsets ipointer(nmesh,5); jd, kd are set to the last mesh's
+ * sizes as set_pointers_globals does.  q(1:4) of every mesh goes through the
+ * (Q/J)*J -> /J round trip of store on the device, as in the reference. */
+int ot2d_astore(double* x, double* y, int32_t* iblank, double* q, int32_t* iturb, int32_t* itrans, int32_t* jgmx,
+                int32_t* kgmx, int32_t* nmesh, int32_t* ipointer, int32_t* igrd, int32_t* iqdim, int32_t* jd,
+                int32_t* kd, int32_t* istep0, int32_t* ts, int32_t* nspec);
+/* src/io.f:278-340: q(jd,kd,nspec,nq), x, y, iblank (jd,kd,nspec); lg, lq:
+ * nspec unit numbers (unformatted, open for writing) */
+int ot2d_store(double* q, double* x, double* y, int32_t* iblank, int32_t* jd, int32_t* kd, int32_t* lg, int32_t* lq);
+/* src/io.f:173-215 and :218-275: ltur formatted units, lq unformatted
+ * (storekomega writes q(5:nv) to lq once more, io.f:253) */
+int ot2d_storevnu(double* x, double* y, int32_t* iblank, double* q, int32_t* jd, int32_t* kd, int32_t* lq,
+                  int32_t* ltur);
+int ot2d_storekomega(double* x, double* y, int32_t* iblank, double* q, int32_t* jd, int32_t* kd, int32_t* lq,
+                     int32_t* ltur);
+/* src/io.f:343-380: xv, yv (jmax,kmax) from unit logg; iblank(jd,kd) = 1 */
+int ot2d_grid(double* xv, double* yv, int32_t* iblank, int32_t* jd, int32_t* kd, int32_t* logg);
+/* src/io.f:383-405 (q: one instance q(jd,kd,nq); sets totime of the
+ * current parameters) and src/io.f:408-425 */
+int ot2d_restr2(double* q, int32_t* jd, int32_t* kd, int32_t* logq);
+int ot2d_restr_turb(double* q, int32_t* jd, int32_t* kd, int32_t* logq);
+/* src/init.f:180-206: q(jd,kd,nq) of one instance, q(1:4) /= q(nq) */
+int ot2d_qdivj(double* q, int32_t* jd, int32_t* kd);
+
+/* ---------------------------------------------------------------------- */
 /* batched solver (host runtime over device-resident meshes)               */
 /* ---------------------------------------------------------------------- */
 
@@ -214,6 +261,22 @@ int ot2d_solver_get_q(ot2d_solver* s, int32_t id, double* q_out);
 size_t ot2d_solver_device_bytes(const ot2d_solver* s);
 /* device bytes one instance with these params would take */
 size_t ot2d_instance_bytes(const ot2d_params* p, int32_t precision);
+/* Snapshot of a live instance into the files astore writes (src/io.f:2-170)
+ * in directory dir: fort.8 / fort.9 (fort_TS<n>.*) and SA.dat / komega.dat.
+ * The conversion runs on the device over the resident state, including the
+ * (Q/J)*J -> /J round trip store applies to q; istep0 is the instance's
+ * step counter. */
+int ot2d_solver_store(ot2d_solver* s, int32_t id, const char* dir);
+/* store instance `id` into dir when it retires (converged, failed or capped),
+ * before its device memory is freed; dir = NULL cancels */
+int ot2d_solver_store_on_retire(ot2d_solver* s, int32_t id, const char* dir);
+/* Admit one solve that starts from the restart file dir/fort.3 (fort_TS<n>.3)
+ * as init.f:138-170 reads it with iread > 0: header, restr2, restr_turb and
+ * istep0 records, q(1:4)/J on the device; totime and istep0 come from the
+ * file, and the instance runs with iread = 1 as a reference restart does.
+ * Returns the instance id or -status. */
+int ot2d_solver_add_restart(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv,
+                            const char* dir, double orders, int32_t max_iters);
 
 #ifdef __cplusplus
 }

@@ -324,8 +324,20 @@ int oro_step(const P* pp, double* q, double* s, double* x, double* y, const doub
  * hist[it*nspec+nsp] = rsum; forces[5*nsp+{0..4}] = cl,cd,cm,cpower,- and
  * q_out (jd,kd,nspec,nq) the final state.  Returns the number of iterations
  * run, or the negative iteration count on a monitor / norm stop. */
+// The Turns_overset.f time loop from freestream (q_init = nullptr) or, as
+// init.f:138-170 does with iread > 0, from a restart state: q_init holds
+// q(1:nv) of every instance already divided by J (jd,kd,nspec,nv), and the
+// step counter istep0 continues from istep0_init.
+int oro_solve_from(const P* pin, const double* xv1, const double* yv1, int nsteps, double orders,
+                   const double* q_init, int istep0_init, double* hist, double* forces, double* q_out);
+
 int oro_solve(const P* pin, const double* xv1, const double* yv1, int nsteps, double orders,
               double* hist, double* forces, double* q_out) {
+  return oro_solve_from(pin, xv1, yv1, nsteps, orders, nullptr, 0, hist, forces, q_out);
+}
+
+int oro_solve_from(const P* pin, const double* xv1, const double* yv1, int nsteps, double orders,
+                   const double* q_init, int istep0_init, double* hist, double* forces, double* q_out) {
   P p = *pin;
   const int jd = p.jd, kd = p.kd, nspec = p.nspec, jmax = p.jmax, kmax = p.kmax;
   size_t n2 = (size_t)jd * kd, nv2 = n2 * nspec, nvert = (size_t)jmax * kmax;
@@ -356,9 +368,11 @@ int oro_solve(const P* pin, const double* xv1, const double* yv1, int nsteps, do
     qzero(p, qn);
     qdivj(p, qn);
   }
+  if (q_init)
+    for (int n = 0; n < p.nv; ++n) std::memcpy(q.data() + (size_t)n * nv2, q_init + (size_t)n * nv2, sizeof(double) * nv2);
   std::vector<double> norms(3 * nspec), first(nspec, 0.0);
   std::vector<int32_t> loc(3 * nspec);
-  p.istep0 = 0;
+  p.istep0 = q_init ? istep0_init : 0;
   int it = 0, stopped = 0;
   for (int istep = 1; istep <= nsteps; ++istep) {
     p.istep0 += 1; p.istep = istep;

@@ -60,6 +60,8 @@ def lib():
         L.oro_step.restype = C.c_int
         L.oro_solve.argtypes = [_P, _dp, _dp, C.c_int, C.c_double, _dp, _dp, _dp]
         L.oro_solve.restype = C.c_int
+        L.oro_solve_from.argtypes = [_P, _dp, _dp, C.c_int, C.c_double, _dp, C.c_int, _dp, _dp, _dp]
+        L.oro_solve_from.restype = C.c_int
         _lib = L
     return _lib
 
@@ -92,3 +94,32 @@ def solve(p, xv, yv, nsteps, orders=0.0):
                         ptr(np.ascontiguousarray(yv, dtype=np.float64)), nsteps, orders,
                         ptr(hist), ptr(forces), ptr(q))
     return n, hist[:abs(n)], forces, q
+
+
+def solve_from(p, xv, yv, nsteps, q_init, istep0, orders=0.0):
+    """The oracle driver from a restart state q_init (q(1:nv) / J, flat
+    (jd,kd,nspec,nv) or the full (jd,kd,nspec,nq) array) continuing at istep0."""
+    nsp = p.nspec
+    hist = np.zeros((nsteps, nsp))
+    forces = np.zeros((nsp, 5))
+    q = np.zeros(p.jd * p.kd * nsp * p.nq)
+    qi = np.ascontiguousarray(q_init, dtype=np.float64)
+    n = lib().oro_solve_from(C.byref(p), ptr(np.ascontiguousarray(xv, dtype=np.float64)),
+                             ptr(np.ascontiguousarray(yv, dtype=np.float64)), nsteps, orders, ptr(qi), int(istep0),
+                             ptr(hist), ptr(forces), ptr(q))
+    return n, hist[:abs(n)], forces, q
+
+
+_io = None
+
+
+def oracle_io():
+    """The numpy restatement of the solution / restart files (oracle/oracle_io.py)."""
+    global _io
+    if _io is None:
+        import importlib.util
+        path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "oracle_io.py")
+        spec = importlib.util.spec_from_file_location("oracle_io", path)
+        _io = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(_io)
+    return _io

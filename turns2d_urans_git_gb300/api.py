@@ -211,6 +211,34 @@ class Solver:
     def device_bytes(self):
         return lib().ot2d_solver_device_bytes(self._h)
 
+    def store(self, iid, directory):
+        """Write fort.8 / fort.9 (and SA.dat / komega.dat) of a live instance
+        into `directory` (ot2d_solver_store, the astore record layout)."""
+        f = lib().ot2d_solver_store
+        f.argtypes = [C.c_void_p, C.c_int32, C.c_char_p]
+        rc = f(self._h, int(iid), os.fsencode(directory))
+        if rc != 0:
+            raise RuntimeError("ot2d_solver_store failed (%d)" % rc)
+
+    def store_on_retire(self, iid, directory):
+        """Store the instance into `directory` when it retires (None cancels)."""
+        f = lib().ot2d_solver_store_on_retire
+        f.argtypes = [C.c_void_p, C.c_int32, C.c_char_p]
+        rc = f(self._h, int(iid), None if directory is None else os.fsencode(directory))
+        if rc != 0:
+            raise RuntimeError("ot2d_solver_store_on_retire failed (%d)" % rc)
+
+    def add_restart(self, prm, xv, yv, directory, orders=10.0, max_iters=2000):
+        """Admit a solve that starts from `directory`/fort.3 (fort_TS<n>.3)."""
+        xv = np.ascontiguousarray(xv, dtype=np.float64)
+        yv = np.ascontiguousarray(yv, dtype=np.float64)
+        f = lib().ot2d_solver_add_restart
+        f.argtypes = [C.c_void_p, C.POINTER(Params), _dp, _dp, C.c_char_p, C.c_double, C.c_int32]
+        rc = f(self._h, C.byref(prm), dptr(xv), dptr(yv), os.fsencode(directory), float(orders), int(max_iters))
+        if rc < 0:
+            raise RuntimeError("ot2d_solver_add_restart failed (%d)" % -rc)
+        return rc
+
     def stream(self):
         return lib().ot2d_solver_stream(self._h)
 

@@ -35,6 +35,7 @@ UNITS = [
     ("host/solver.cu", ["-fmad=false"]),
     ("host/dropin.cu", ["-fmad=false"]),
     ("host/noalloc.cu", ["-fmad=false"]),
+    ("host/io.cu", ["-fmad=false"]),
     ("host/geom.cpp", None),
     ("host/setup_host.cpp", None),
 ]

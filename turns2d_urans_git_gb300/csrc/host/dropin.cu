@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "geom.h"
+#include "io.h"
 #include "runtime.h"
 
 namespace ot2d {
@@ -203,6 +204,144 @@ int faces_upload(double* dst4, double* dst2, const double* xv, const double* yv,
   return err;
 }
 
+
+// Device view of an argument without staging: the pointer itself for device
+// memory, the registered mirror for registered host memory, else nullptr.
+void* device_view(const void* p, size_t bytes) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) == cudaSuccess &&
+      (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged))
+    return const_cast<void*>(p);
+  cudaGetLastError();
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  auto it = g_reg.upper_bound((uintptr_t)p);
+  if (it == g_reg.begin()) return nullptr;
+  --it;
+  const uintptr_t base = it->first;
+  if ((uintptr_t)p + bytes <= base + it->second.bytes) return (char*)it->second.dev + ((uintptr_t)p - base);
+  return nullptr;
+}
+
+// Read an argument as the library sees it (device data for device or
+// registered memory, else the host array).
+int fetch(const void* p, size_t bytes, void* dst) {
+  if (!bytes) return OT2D_OK;
+  if (void* d = device_view(p, bytes))
+    return cudaMemcpy(dst, d, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? OT2D_OK : OT2D_ERR_CUDA;
+  std::memcpy(dst, p, bytes);
+  return OT2D_OK;
+}
+
+// Write into an argument: device memory in place; host memory and, when it is
+// registered, its device mirror too.
+int put(void* p, const void* src, size_t bytes) {
+  if (!bytes) return OT2D_OK;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) == cudaSuccess &&
+      (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged))
+    return cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess ? OT2D_OK : OT2D_ERR_CUDA;
+  cudaGetLastError();
+  std::memcpy(p, src, bytes);
+  if (void* d = device_view(p, bytes))
+    return cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess ? OT2D_OK : OT2D_ERR_CUDA;
+  return OT2D_OK;
+}
+
+// store, io.f:278-340, for one mesh: q(jd,kd,nspec,nq) goes through the
+// device pack (Q = (Q/J)*J written, Q/J restored in place); lg / lq: nspec
+// unformatted units; iblank is written to the grid file when num_grids > 1.
+int store_impl(double* q, const double* x, const double* y, const int32_t* iblank, int jd, int kd,
+               const int32_t* lg, const int32_t* lq, int num_grids) {
+  int err = ensure_stream();
+  if (err) return err;
+  if (!g_ctx.has) return OT2D_ERR_NOPARAMS;
+  const ot2d_params& p = g_ctx.P;
+  if (jd < 1 || kd < 1 || !q || !x || !y || !lg || !lq || (num_grids > 1 && !iblank) || p.nv < 4) return OT2D_ERR_ARG;
+  const size_t n2 = (size_t)jd * kd, ns = (size_t)p.nspec, nv = (size_t)p.nv;
+  const bool turb = p.iturb == 1 || p.iturb == 2;
+  double* dq = (double*)resolve(q, n2 * ns * p.nq * 8, true, true, err);
+  double* rec = nullptr;
+  if (!err && cudaMalloc(&rec, ns * nv * n2 * 8) != cudaSuccess) err = OT2D_ERR_NOMEM;
+  if (rec) g_ctx.pool.push_back(rec);
+  if (!err && io_pack(dq, nullptr, rec, nullptr, n2, p.nspec, p.nq, p.nv, IO_REC, g_ctx.st) != cudaSuccess)
+    err = OT2D_ERR_CUDA;
+  std::vector<double> h(ns * nv * n2);
+  if (!err && cudaMemcpyAsync(h.data(), rec, h.size() * 8, cudaMemcpyDeviceToHost, g_ctx.st) != cudaSuccess)
+    err = OT2D_ERR_CUDA;
+  if ((err = finish(err))) return err;
+  std::vector<double> hx(n2 * ns), hy(n2 * ns);
+  std::vector<int32_t> hib(num_grids > 1 ? n2 * ns : 0);
+  if ((err = fetch(x, hx.size() * 8, hx.data())) || (err = fetch(y, hy.size() * 8, hy.data())) ||
+      (err = fetch(iblank, hib.size() * 4, hib.data())))
+    return err;
+  const double hdr[4] = {p.fsmach, p.alfa, p.rey * p.fsmach, p.totime};   // fstip, alfa, reypr, totime
+  for (size_t s = 0; s < ns && !err; ++s) {
+    FILE* fq = unit_file(lq[s], false, true);
+    FILE* fg = unit_file(lg[s], false, true);
+    if (!fq || !fg) return OT2D_ERR_IO;
+    const double* r = h.data() + s * nv * n2;
+    Seg sh{hdr, sizeof(hdr)}, sq{r, 4 * n2 * 8}, st{r + 4 * n2, (nv - 4) * n2 * 8};
+    Seg sg[3] = {{hx.data() + s * n2, n2 * 8}, {hy.data() + s * n2, n2 * 8},
+                 {hib.empty() ? nullptr : hib.data() + s * n2, hib.empty() ? 0 : n2 * 4}};
+    err = rec_write(fq, &sh, 1);
+    if (!err) err = rec_write(fq, &sq, 1);
+    if (!err && turb) err = rec_write(fq, &st, 1);
+    if (!err) err = rec_write(fg, sg, num_grids > 1 ? 3 : 2);
+  }
+  return err;
+}
+
+// storevnu (io.f:173-215) and storekomega (io.f:218-275) for one mesh
+int storeturb_impl(const double* x, const double* y, const int32_t* iblank, double* q, int jd, int kd,
+                   const int32_t* lq, const int32_t* ltur, bool sst) {
+  int err = ensure_stream();
+  if (err) return err;
+  if (!g_ctx.has) return OT2D_ERR_NOPARAMS;
+  const ot2d_params& p = g_ctx.P;
+  if (jd < 1 || kd < 1 || !q || !x || !y || !iblank || !ltur || (sst && !lq) || p.itrans != 0 ||
+      p.nv < (sst ? 6 : 5))
+    return OT2D_ERR_ARG;
+  const size_t n2 = (size_t)jd * kd, ns = (size_t)p.nspec, nv = (size_t)p.nv, qs = n2 * ns;
+  std::vector<double> tec(sst ? ns * 2 * n2 : 0), turbv(ns * (nv - 4) * n2);
+  if (sst) {
+    // k = q(5)/rho, omega = q(6)/rho with rho = q(1)*J, on the device
+    double* dq = (double*)resolve(q, qs * p.nq * 8, true, false, err);
+    double* dt = nullptr;
+    if (!err && cudaMalloc(&dt, tec.size() * 8) != cudaSuccess) err = OT2D_ERR_NOMEM;
+    if (dt) g_ctx.pool.push_back(dt);
+    if (!err && io_pack(dq, nullptr, nullptr, dt, n2, p.nspec, p.nq, p.nv, IO_TEC, g_ctx.st) != cudaSuccess)
+      err = OT2D_ERR_CUDA;
+    if (!err && cudaMemcpyAsync(tec.data(), dt, tec.size() * 8, cudaMemcpyDeviceToHost, g_ctx.st) != cudaSuccess)
+      err = OT2D_ERR_CUDA;
+    if ((err = finish(err))) return err;
+  }
+  for (size_t s = 0; s < ns && !err; ++s)
+    for (size_t n = 4; n < nv && !err; ++n)
+      err = fetch(q + n * qs + s * n2, n2 * 8, turbv.data() + (s * (nv - 4) + (n - 4)) * n2);
+  std::vector<double> hx(n2 * ns), hy(n2 * ns);
+  std::vector<int32_t> hib(n2 * ns);
+  if (!err) err = fetch(x, hx.size() * 8, hx.data());
+  if (!err) err = fetch(y, hy.size() * 8, hy.data());
+  if (!err) err = fetch(iblank, hib.size() * 4, hib.data());
+  for (size_t s = 0; s < ns && !err; ++s) {
+    FILE* ft = unit_file(ltur[s], true, true);
+    if (!ft) return OT2D_ERR_IO;
+    const double* tv = turbv.data() + s * (nv - 4) * n2;
+    if (sst) {
+      Seg sg{tv, (nv - 4) * n2 * 8};
+      err = rec_write(unit_file(lq[s], false, true), &sg, 1);
+    }
+    if (!err) err = tec_zone(ft, jd, kd);
+    if (!err) err = tec_reals(ft, hx.data() + s * n2, n2);
+    if (!err) err = tec_reals(ft, hy.data() + s * n2, n2);
+    if (!err) err = tec_ints(ft, hib.data() + s * n2, n2);
+    if (!err && !sst) err = tec_reals(ft, tv, n2);
+    if (!err && sst) err = tec_reals(ft, tec.data() + s * 2 * n2, n2);
+    if (!err && sst) err = tec_reals(ft, tec.data() + s * 2 * n2 + n2, n2);
+  }
+  return err;
+}
 }  // namespace
 }  // namespace ot2d
 
@@ -705,6 +844,136 @@ int ot2d_metfv(double* q, double* x, double* y, double* xv, double* yv, double* 
   host_store(xx, a.data(), n2); host_store(xy, b.data(), n2);
   host_store(yx, c.data(), n2); host_store(yy, d.data(), n2);
   return nneg ? fail(OT2D_ERR_ARG) : OT2D_OK;
+}
+
+int ot2d_store(double* q, double* x, double* y, int32_t* iblank, int32_t* jd, int32_t* kd, int32_t* lg,
+               int32_t* lq) {
+  if (!jd || !kd) return fail(OT2D_ERR_ARG);
+  return fail(store_impl(q, x, y, iblank, *jd, *kd, lg, lq, 1));
+}
+
+int ot2d_storevnu(double* x, double* y, int32_t* iblank, double* q, int32_t* jd, int32_t* kd, int32_t* lq,
+                  int32_t* ltur) {
+  if (!jd || !kd) return fail(OT2D_ERR_ARG);
+  return fail(storeturb_impl(x, y, iblank, q, *jd, *kd, lq, ltur, false));
+}
+
+int ot2d_storekomega(double* x, double* y, int32_t* iblank, double* q, int32_t* jd, int32_t* kd, int32_t* lq,
+                     int32_t* ltur) {
+  if (!jd || !kd) return fail(OT2D_ERR_ARG);
+  return fail(storeturb_impl(x, y, iblank, q, *jd, *kd, lq, ltur, true));
+}
+
+int ot2d_astore(double* x, double* y, int32_t* iblank, double* q, int32_t* iturb, int32_t* itrans, int32_t* jgmx,
+                int32_t* kgmx, int32_t* nmesh, int32_t* ipointer, int32_t* igrd, int32_t* iqdim, int32_t* jd,
+                int32_t* kd, int32_t* istep0, int32_t* ts, int32_t* nspec) {
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  const ot2d_params& p = g_ctx.P;
+  if (!x || !y || !iblank || !q || !iturb || !itrans || !jgmx || !kgmx || !nmesh || !ipointer || !igrd || !iqdim ||
+      !jd || !kd || !istep0 || !ts || !nspec)
+    return fail(OT2D_ERR_ARG);
+  const int nm = *nmesh, ns = *nspec, it = *iturb;
+  if (nm < 1 || ns != p.nspec || *itrans != 0 || it != p.iturb) return fail(OT2D_ERR_ARG);
+  const bool tsf = *ts != 0, turb = it == 1 || it == 2;
+  // meshes must lie inside x / y / iblank (igrd) and q (iqdim)
+  for (int im = 0; im < nm; ++im) {
+    const int64_t n2 = (int64_t)jgmx[im] * kgmx[im];
+    const int64_t ig = ipointer[im], igq = ipointer[nm + im];
+    if (jgmx[im] < 1 || kgmx[im] < 1 || ig < 1 || igq < 1 || ig - 1 + n2 * ns > *igrd ||
+        igq - 1 + n2 * ns * p.nq > *iqdim)
+      return fail(OT2D_ERR_ARG);
+  }
+  std::vector<int32_t> lg(ns), lq(ns), lt(ns);
+  std::vector<int32_t> dims(2 * (size_t)nm);
+  for (int im = 0; im < nm; ++im) { dims[2 * im] = jgmx[im]; dims[2 * im + 1] = kgmx[im]; }
+  int err = 0;
+  // io.f:38-71: open the grid / solution files, mesh-count and size records
+  for (int s = 0; s < ns && !err; ++s) {
+    lg[s] = 1000 * (s + 1) + 9; lq[s] = 1000 * (s + 1) + 8; lt[s] = 1000 * (s + 1) + 10;
+    err = unit_open(lg[s], sol_file("", tsf, s + 1, 'g', it).c_str(), false, true);
+    if (!err) err = unit_open(lq[s], sol_file("", tsf, s + 1, 'q', it).c_str(), false, true);
+    const int32_t n1 = nm;
+    for (int32_t u : {lg[s], lq[s]}) {
+      Seg sm{&n1, 4}, sd{dims.data(), dims.size() * 4};
+      if (!err && nm > 1) err = rec_write(unit_file(u, false, true), &sm, 1);
+      if (!err) err = rec_write(unit_file(u, false, true), &sd, 1);
+    }
+  }
+  // io.f:75-80: store every mesh
+  for (int im = 0; im < nm && !err; ++im) {
+    *jd = jgmx[im]; *kd = kgmx[im];
+    const int64_t ig = ipointer[im] - 1, igq = ipointer[nm + im] - 1;
+    err = store_impl(q + igq, x + ig, y + ig, iblank + ig, *jd, *kd, lg.data(), lq.data(), nm);
+  }
+  // io.f:84-158: the turbulence files
+  for (int s = 0; s < ns && !err && turb; ++s) {
+    err = unit_open(lt[s], sol_file("", tsf, s + 1, 't', it).c_str(), true, true);
+    if (!err) err = tec_title(unit_file(lt[s], true, true), it);
+  }
+  for (int im = 0; im < nm && !err && turb; ++im) {
+    *jd = jgmx[im]; *kd = kgmx[im];
+    const int64_t ig = ipointer[im] - 1, igq = ipointer[nm + im] - 1;
+    err = storeturb_impl(x + ig, y + ig, iblank + ig, q + igq, *jd, *kd, lq.data(), lt.data(), it == 2);
+  }
+  // io.f:162-168: istep0 and close
+  for (int s = 0; s < ns; ++s) {
+    if (!err) {
+      Seg si{istep0, 4};
+      err = rec_write(unit_file(lq[s], false, true), &si, 1);
+    }
+    int e1 = unit_close(lg[s]), e2 = unit_close(lq[s]), e3 = turb ? unit_close(lt[s]) : 0;
+    if (!err) err = e1 ? e1 : (e2 ? e2 : e3);
+  }
+  return fail(err);
+}
+
+int ot2d_grid(double* xv, double* yv, int32_t* iblank, int32_t* jd, int32_t* kd, int32_t* logg) {
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  if (!xv || !yv || !iblank || !jd || !kd || !logg || *jd < 1 || *kd < 1) return fail(OT2D_ERR_ARG);
+  const int jmax = *jd - g_ctx.P.nadd, kmax = *kd - g_ctx.P.nadd;
+  if (jmax < 1 || kmax < 1) return fail(OT2D_ERR_ARG);
+  const size_t nv = (size_t)jmax * kmax, n2 = (size_t)*jd * *kd;
+  std::vector<double> h(2 * nv);
+  int err = rec_read(unit_file(*logg, false, false), h.data(), h.size() * 8);
+  if (!err) err = put(xv, h.data(), nv * 8);
+  if (!err) err = put(yv, h.data() + nv, nv * 8);
+  std::vector<int32_t> one(n2, 1);   // num_grids = 1
+  if (!err) err = put(iblank, one.data(), n2 * 4);
+  return fail(err);
+}
+
+int ot2d_restr2(double* q, int32_t* jd, int32_t* kd, int32_t* logq) {
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  if (!q || !jd || !kd || !logq || *jd < 1 || *kd < 1) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)*jd * *kd;
+  FILE* f = unit_file(*logq, false, false);
+  double hdr[4];
+  std::vector<double> h(4 * n2);
+  int err = rec_read(f, hdr, sizeof(hdr));   // fstip, alf, reypr, totime
+  if (!err) err = rec_read(f, h.data(), h.size() * 8);
+  if (!err) { g_ctx.P.totime = hdr[3]; err = put(q, h.data(), h.size() * 8); }
+  return fail(err);
+}
+
+int ot2d_restr_turb(double* q, int32_t* jd, int32_t* kd, int32_t* logq) {
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  if (!q || !jd || !kd || !logq || *jd < 1 || *kd < 1 || g_ctx.P.nv < 4) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)*jd * *kd, nt = (size_t)g_ctx.P.nv - 4;
+  std::vector<double> h(nt * n2);
+  int err = rec_read(unit_file(*logq, false, false), h.data(), h.size() * 8);
+  if (!err) err = put(q + 4 * n2, h.data(), h.size() * 8);
+  return fail(err);
+}
+
+int ot2d_qdivj(double* q, int32_t* jd, int32_t* kd) {
+  int err = ensure_stream();
+  if (err) return fail(err);
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  if (!q || !jd || !kd || *jd < 1 || *kd < 1) return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)*jd * *kd;
+  double* dq = (double*)resolve(q, n2 * g_ctx.P.nq * 8, true, true, err);
+  if (!err && io_unpack(dq, dq, nullptr, n2, 1, g_ctx.P.nq, 4, 1, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
 }
 
 }  // extern "C"

@@ -9,10 +9,14 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <map>
+#include <string>
 #include <vector>
 
+#include "geom.h"
+#include "io.h"
 #include "runtime.h"
 
 namespace ot2d {
@@ -31,6 +35,7 @@ struct Rec {
   // the last FORCE_WIN status checks
   double win_cl[8] = {0}, win_cd[8] = {0};
   int nwin = 0;
+  std::string store_dir;   // ot2d_solver_store_on_retire: written when retired
 };
 constexpr int FORCE_WIN = 8;
 
@@ -236,6 +241,28 @@ int profile_t(ot2d_solver* s, DevBatch<R>& B, int iters, double* ms) {
   return err;
 }
 
+// astore (io.f:2-170) of one live instance: the device pack converts and
+// round-trips q; cell centres come from the device vertex grids through the
+// set-up routine find_cellcenter; istep0 is the instance's step counter.
+int store_rec(ot2d_solver* s, Rec& r, const std::string& dir) {
+  const ot2d_params& p = r.d.P;
+  const size_t n2 = r.d.n2, nv = r.d.nvert, ns = (size_t)p.nspec;
+  int32_t ist[IST_N];
+  std::vector<double> xv(nv * ns), yv(nv * ns), x(n2 * ns), y(n2 * ns);
+  std::vector<int32_t> ib(n2 * ns);
+  if (cudaMemcpyAsync(ist, s->d_ist + (size_t)IST_N * r.slots[0], sizeof(ist), cudaMemcpyDeviceToHost, s->st) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(xv.data(), r.d.xv, xv.size() * 8, cudaMemcpyDeviceToHost, s->st) != cudaSuccess ||
+      cudaMemcpyAsync(yv.data(), r.d.yv, yv.size() * 8, cudaMemcpyDeviceToHost, s->st) != cudaSuccess ||
+      cudaMemcpyAsync(ib.data(), r.d.iblank, ib.size() * 4, cudaMemcpyDeviceToHost, s->st) != cudaSuccess ||
+      cudaStreamSynchronize(s->st) != cudaSuccess)
+    return OT2D_ERR_CUDA;
+  for (size_t k = 0; k < ns; ++k)
+    cell_centres(p, xv.data() + k * nv, yv.data() + k * nv, x.data() + k * n2, y.data() + k * n2);
+  float* qc = s->precision == OT2D_FP32_MIXED ? (float*)r.d.q : nullptr;
+  return write_solution(dir, p, r.d.q64, qc, x.data(), y.data(), ib.data(), ist[0], s->st);
+}
+
 int check(ot2d_solver* s) {
   s->since_check = 0;
   if (s->live.empty()) return OT2D_OK;
@@ -294,6 +321,10 @@ int check(ot2d_solver* s) {
   for (int id : done) {
     Rec& r = s->recs[id];
     r.res.t_done = t;
+    if (!r.store_dir.empty()) {
+      const int se = store_rec(s, r, r.store_dir);
+      if (se && !e) e = se;
+    }
     if (s->keep_q) {
       r.qkeep.resize((size_t)r.d.n2 * r.d.nspec * r.d.P.nq);
       cudaMemcpy(r.qkeep.data(), r.d.q64, r.qkeep.size() * sizeof(double), cudaMemcpyDeviceToHost);
@@ -475,6 +506,61 @@ int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, doub
     if (++s->since_check >= s->check_every) { int e = check(s); if (e) return e; }
   }
   return OT2D_OK;
+}
+
+int ot2d_solver_store(ot2d_solver* s, int32_t id, const char* dir) {
+  if (!s || !dir) return OT2D_ERR_ARG;
+  auto it = s->recs.find(id);
+  if (it == s->recs.end() || !it->second.live) return OT2D_ERR_ARG;
+  cudaSetDevice(s->device);
+  return store_rec(s, it->second, dir);
+}
+
+int ot2d_solver_store_on_retire(ot2d_solver* s, int32_t id, const char* dir) {
+  if (!s) return OT2D_ERR_ARG;
+  auto it = s->recs.find(id);
+  if (it == s->recs.end() || !it->second.live) return OT2D_ERR_ARG;
+  it->second.store_dir = dir ? dir : "";
+  return OT2D_OK;
+}
+
+int ot2d_solver_add_restart(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv,
+                            const char* dir, double orders, int32_t max_iters) {
+  if (!s || !p || !dir) return -OT2D_ERR_ARG;
+  const int id = ot2d_solver_add(s, p, xv, yv, orders, max_iters);
+  if (id < 0) return id;
+  Rec& r = s->recs[id];
+  double totime = 0.0;
+  int istep0 = 0;
+  float* qc = s->precision == OT2D_FP32_MIXED ? (float*)r.d.q : nullptr;
+  int e = read_restart(dir, r.d.P, r.d.q64, qc, &totime, &istep0, s->st);
+  if (!e) {
+    // init.f:165 (istep0) and io.f:400 (totime) of the restart file; the
+    // instance runs as a reference restart does, with iread = 1 (the wall
+    // start-up ramps of bc.f / komegasst.f are then off)
+    r.d.P.totime = totime;
+    if (r.d.P.iread < 1) r.d.P.iread = 1;
+    const int32_t i0 = istep0;
+    if (cudaMemcpyAsync((char*)r.d.dP + offsetof(ot2d_params, totime), &r.d.P.totime, sizeof(double),
+                        cudaMemcpyHostToDevice, s->st) != cudaSuccess ||
+        cudaMemcpyAsync((char*)r.d.dP + offsetof(ot2d_params, iread), &r.d.P.iread, sizeof(int32_t),
+                        cudaMemcpyHostToDevice, s->st) != cudaSuccess)
+      e = OT2D_ERR_CUDA;
+    for (int sl : r.slots)
+      if (!e && cudaMemcpyAsync(s->d_ist + (size_t)IST_N * sl, &i0, sizeof(i0), cudaMemcpyHostToDevice, s->st) !=
+                    cudaSuccess)
+        e = OT2D_ERR_CUDA;
+    if (!e && cudaStreamSynchronize(s->st) != cudaSuccess) e = OT2D_ERR_CUDA;
+  }
+  if (e) {
+    for (int sl : r.slots) s->free_slots.push_back(sl);
+    solve_destroy(r.d);
+    s->recs.erase(id);
+    s->live.erase(std::remove(s->live.begin(), s->live.end(), id), s->live.end());
+    s->dirty = true;
+    return -e;
+  }
+  return id;
 }
 
 }  // extern "C"

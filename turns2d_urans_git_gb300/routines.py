@@ -161,3 +161,83 @@ def metfv(q, x, y, xv, yv, xx, xy, yx, yy, jd, kd, im=1):
     """src/setup.f:440 -- J into q(:,:,nq) and the J-scaled metrics."""
     _call("ot2d_metfv", _p(q), _p(x), _p(y), _p(xv), _p(yv), _p(xx), _p(xy), _p(yx), _p(yy), _ref(jd), _ref(kd),
           _ref(im))
+
+
+# ---- solution / restart files (src/io.f, src/init.f) ----------------------
+# Fortran unit numbers refer to the library's own unit table: open them with
+# unit_open() where the reference has `open(unit=...)`.
+
+def unit_open(unit, path, formatted=False, for_write=True):
+    """open(unit, file=path, form='formatted'|'unformatted')."""
+    f = lib().ot2d_unit_open
+    f.argtypes = [_i, C.c_char_p, _i, _i]
+    _call("ot2d_unit_open", _i(unit), str(path).encode(), _i(1 if formatted else 0), _i(1 if for_write else 0))
+
+
+def unit_close(unit):
+    _call("ot2d_unit_close", _i(unit))
+
+
+def unit_write_ints(unit, values):
+    v = np.ascontiguousarray(values, dtype=np.int32)
+    _call("ot2d_unit_write_ints", _i(unit), C.c_void_p(v.ctypes.data), _i(v.size))
+
+
+def unit_read_ints(unit, n):
+    v = np.zeros(n, dtype=np.int32)
+    _call("ot2d_unit_read_ints", _i(unit), C.c_void_p(v.ctypes.data), _i(n))
+    return v
+
+
+def astore(x, y, iblank, q, iturb, itrans, jgmx, kgmx, nmesh, ipointer, igrd, iqdim, istep0, ts, nspec):
+    """src/io.f:2 -- writes the solution files into the current directory;
+    returns the (jd, kd) of the last mesh."""
+    jd, kd = _i(0), _i(0)
+    jg = np.ascontiguousarray(jgmx, dtype=np.int32)
+    kg = np.ascontiguousarray(kgmx, dtype=np.int32)
+    ip = np.asfortranarray(np.asarray(ipointer, dtype=np.int32).reshape(nmesh, 5, order="F"))
+    _call("ot2d_astore", _p(x), _p(y), _p(iblank), _p(q), _ref(iturb), _ref(itrans), _p(jg), _p(kg), _ref(nmesh),
+          C.c_void_p(ip.ctypes.data), _ref(igrd), _ref(iqdim), C.byref(jd), C.byref(kd), _ref(istep0),
+          _ref(1 if ts else 0), _ref(nspec))
+    return jd.value, kd.value
+
+
+def store(q, x, y, iblank, jd, kd, lg, lq):
+    """src/io.f:278 (lg, lq: one unit per time instance)."""
+    lg = np.ascontiguousarray(lg, dtype=np.int32)
+    lq = np.ascontiguousarray(lq, dtype=np.int32)
+    _call("ot2d_store", _p(q), _p(x), _p(y), _p(iblank), _ref(jd), _ref(kd), _p(lg), _p(lq))
+
+
+def storevnu(x, y, iblank, q, jd, kd, lq, ltur):
+    """src/io.f:173."""
+    lq = np.ascontiguousarray(lq, dtype=np.int32)
+    lt = np.ascontiguousarray(ltur, dtype=np.int32)
+    _call("ot2d_storevnu", _p(x), _p(y), _p(iblank), _p(q), _ref(jd), _ref(kd), _p(lq), _p(lt))
+
+
+def storekomega(x, y, iblank, q, jd, kd, lq, ltur):
+    """src/io.f:218."""
+    lq = np.ascontiguousarray(lq, dtype=np.int32)
+    lt = np.ascontiguousarray(ltur, dtype=np.int32)
+    _call("ot2d_storekomega", _p(x), _p(y), _p(iblank), _p(q), _ref(jd), _ref(kd), _p(lq), _p(lt))
+
+
+def grid(xv, yv, iblank, jd, kd, logg):
+    """src/io.f:343."""
+    _call("ot2d_grid", _p(xv), _p(yv), _p(iblank), _ref(jd), _ref(kd), _ref(logg))
+
+
+def restr2(q, jd, kd, logq):
+    """src/io.f:383 (q: one time instance, q(jd,kd,nq))."""
+    _call("ot2d_restr2", _p(q), _ref(jd), _ref(kd), _ref(logq))
+
+
+def restr_turb(q, jd, kd, logq):
+    """src/io.f:408."""
+    _call("ot2d_restr_turb", _p(q), _ref(jd), _ref(kd), _ref(logq))
+
+
+def qdivj(q, jd, kd):
+    """src/init.f:180."""
+    _call("ot2d_qdivj", _p(q), _ref(jd), _ref(kd))
