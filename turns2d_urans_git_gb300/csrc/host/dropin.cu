@@ -127,7 +127,7 @@ int prepare(int nslice, int& err) {
   if ((err = ensure_stream())) return err;
   if (!g_ctx.has) return err = OT2D_ERR_NOPARAMS;
   const size_t n2 = (size_t)g_ctx.P.jd * g_ctx.P.kd, ws = (n2 + 63) / 64 * 64;
-  const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd);
+  const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd, 8);
   const size_t need = ws * DW_SLOTS * nslice + 8 * ws + rec * nslice;
   g_ctx.nslice = nslice;
   if (need > g_ctx.wcap) {
@@ -165,7 +165,7 @@ Slice<double> base_slice(int nsp, int nspec, int64_t qs) {
   const size_t n2 = (size_t)p.jd * p.kd, ws = (n2 + 63) / 64 * 64;
   S.w = g_ctx.dwork + (size_t)(nsp - 1) * ws * DW_SLOTS;
   S.wstride = (int64_t)ws;
-  S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
+  S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd, 8);
   S.red = g_ctx.dred + (size_t)RED_N * (nsp - 1);
   S.ist = nullptr;
   slice_consts(S, p);

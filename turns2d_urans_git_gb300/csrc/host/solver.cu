@@ -52,6 +52,9 @@ using namespace ot2d;
 struct ot2d_solver {
   int device = 0, precision = OT2D_FP64;
   cudaStream_t st = nullptr;
+  cudaStream_t st_d2h = nullptr;          // downloads of ot2d_solver_iterate_host
+  std::vector<cudaEvent_t> ev_d2h;        // per instance: its download finished
+  cudaEvent_t ev_step = nullptr;          // the iteration's kernels finished
   int cap = 0;
   double* d_red = nullptr; int32_t* d_ist = nullptr;
   double* h_red = nullptr; int32_t* h_ist = nullptr;
@@ -140,6 +143,8 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   if (e) return e;
   // The kernels branch on each slice's own params, so inviscid, laminar,
   // SA and SST requests can share one batch.
+  Branch* br = nullptr;   // the turbulence branch's stream, created outside the capture
+  if (branch_of_device(br) != cudaSuccess) return OT2D_ERR_CUDA;
   if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
   cudaError_t le = launch_iteration<R>(B.d_sl, B.b, s->any_viscous ? 1 : 0, s->turb_bits, s->lhs_bits, s->st);
   cudaError_t ce = cudaStreamEndCapture(s->st, &s->graph);
@@ -358,8 +363,12 @@ ot2d_solver* ot2d_solver_create(int32_t device, int32_t precision) {
 void ot2d_solver_destroy(ot2d_solver* s) {
   if (!s) return;
   cudaStreamSynchronize(s->st);
+  if (s->st_d2h) cudaStreamSynchronize(s->st_d2h);
   drop_graph(s);
   for (auto& kv : s->recs) solve_destroy(kv.second.d);
+  for (cudaEvent_t e : s->ev_d2h) cudaEventDestroy(e);
+  if (s->ev_step) cudaEventDestroy(s->ev_step);
+  if (s->st_d2h) cudaStreamDestroy(s->st_d2h);
   s->b64.release(); s->b32.release(); s->f64.release(); s->f32.release();
   if (s->d_red) cudaFree(s->d_red);
   if (s->d_ist) cudaFree(s->d_ist);
@@ -490,22 +499,52 @@ int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, doub
     if (it == s->recs.end() || !it->second.live) return OT2D_ERR_ARG;
     rs.push_back(&it->second);
   }
-  for (int it = 0; it < iters; ++it) {
-    for (int i = 0; i < n; ++i) {
-      const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
-      if (cudaMemcpyAsync(rs[i]->d.q64, q_host[i], bytes, cudaMemcpyHostToDevice, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
-    }
-    if (s->precision == OT2D_FP32_MIXED && launch_shadow<float>(s->b32.d_sl, s->b32.b, s->st) != cudaSuccess)
-      return OT2D_ERR_CUDA;
-    if (cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
-    for (int i = 0; i < n; ++i) {
-      const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
-      if (cudaMemcpyAsync(q_host[i], rs[i]->d.q64, bytes, cudaMemcpyDeviceToHost, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
-    }
-    if (cudaStreamSynchronize(s->st) != cudaSuccess) return OT2D_ERR_CUDA;
-    if (++s->since_check >= s->check_every) { int e = check(s); if (e) return e; }
+  // Downloads run on their own stream: instance i's upload for the next
+  // iteration waits only for its own download, so the uploads of early
+  // instances overlap the downloads of later ones (both copy directions).
+  if (!s->st_d2h && cudaStreamCreateWithFlags(&s->st_d2h, cudaStreamNonBlocking) != cudaSuccess) return OT2D_ERR_CUDA;
+  if (!s->ev_step && cudaEventCreateWithFlags(&s->ev_step, cudaEventDisableTiming) != cudaSuccess) return OT2D_ERR_CUDA;
+  while ((int)s->ev_d2h.size() < n) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return OT2D_ERR_CUDA;
+    s->ev_d2h.push_back(e);
   }
-  return OT2D_OK;
+  int err = OT2D_OK;
+  for (int it = 0; it < iters && !err; ++it) {
+    for (int i = 0; i < n && !err; ++i) {
+      const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
+      if ((it > 0 && cudaStreamWaitEvent(s->st, s->ev_d2h[i], 0) != cudaSuccess) ||
+          cudaMemcpyAsync(rs[i]->d.q64, q_host[i], bytes, cudaMemcpyHostToDevice, s->st) != cudaSuccess)
+        err = OT2D_ERR_CUDA;
+    }
+    if (!err && s->precision == OT2D_FP32_MIXED && launch_shadow<float>(s->b32.d_sl, s->b32.b, s->st) != cudaSuccess)
+      err = OT2D_ERR_CUDA;
+    if (!err && cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) err = OT2D_ERR_CUDA;
+    if (!err && (cudaEventRecord(s->ev_step, s->st) != cudaSuccess ||
+                 cudaStreamWaitEvent(s->st_d2h, s->ev_step, 0) != cudaSuccess))
+      err = OT2D_ERR_CUDA;
+    for (int i = 0; i < n && !err; ++i) {
+      const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
+      if (cudaMemcpyAsync(q_host[i], rs[i]->d.q64, bytes, cudaMemcpyDeviceToHost, s->st_d2h) != cudaSuccess ||
+          cudaEventRecord(s->ev_d2h[i], s->st_d2h) != cudaSuccess)
+        err = OT2D_ERR_CUDA;
+    }
+    if (!err && ++s->since_check >= s->check_every) {
+      // the status read must not see the next iteration's uploads in flight
+      if (cudaStreamSynchronize(s->st_d2h) != cudaSuccess) err = OT2D_ERR_CUDA;
+      else err = check(s);
+      if (!err && s->dirty) {
+        // instances retired: the caller's list no longer matches the batch
+        for (int i = 0; i < n; ++i)
+          if (!rs[i]->live) { err = OT2D_ERR_ARG; break; }
+        if (!err) err = rebuild(s);
+      }
+    }
+  }
+  // every download has landed in the caller's buffers
+  if (cudaStreamSynchronize(s->st_d2h) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
+  if (cudaStreamSynchronize(s->st) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
+  return err;
 }
 
 int ot2d_solver_store(ot2d_solver* s, int32_t id, const char* dir) {

@@ -29,7 +29,16 @@
 namespace ot2d {
 
 constexpr int LU_NF = 24;                 // fields per cell record
-constexpr int LU_CHUNK = LU_NF * 32;      // elements per (band, step) chunk
+// A (band, step) chunk holds the records of the band's 32 lanes one after
+// another (lane-major): lane l's 24 fields are contiguous, so a lane reads
+// its record with 16-byte shared-memory loads.  Each record is padded to LS
+// elements so that the eight lanes of one load phase hit disjoint banks
+// (f32: 112-byte stride, f64: 208-byte stride).
+template <class R>
+struct LuLay {
+  static constexpr int LS = sizeof(R) == 4 ? 28 : 26;   // elements per lane record
+  static constexpr int CH = 32 * LS;                    // elements per chunk
+};
 
 // record fields
 enum {
@@ -44,9 +53,31 @@ __host__ __device__ __forceinline__ int lu_nrow(int kd) { return kd - 2; }
 __host__ __device__ __forceinline__ int lu_ncol(int jd) { return jd - 2; }
 __host__ __device__ __forceinline__ int lu_nband(int kd) { return (kd - 2 + 31) / 32; }
 __host__ __device__ __forceinline__ int lu_nstep(int jd) { return jd - 2 + 31; }
-// elements of one slice's record: chunks + 4 halo-contribution arrays
-__host__ __device__ __forceinline__ int64_t lu_rec_elems(int jd, int kd) {
-  return (int64_t)lu_nband(kd) * lu_nstep(jd) * LU_CHUNK + 8 * (int64_t)(lu_nrow(kd) + lu_ncol(jd)) + 64;
+// elements of one slice's record (element size esize bytes): chunks + 4
+// halo-contribution arrays
+__host__ __device__ __forceinline__ int64_t lu_rec_elems(int jd, int kd, int esize) {
+  const int ch = esize == 4 ? LuLay<float>::CH : LuLay<double>::CH;
+  return (int64_t)lu_nband(kd) * lu_nstep(jd) * ch + 8 * (int64_t)(lu_nrow(kd) + lu_ncol(jd)) + 64;
+}
+
+// four consecutive record fields (16-byte aligned) as one or two vector
+// accesses
+template <class R>
+struct Lu4 { R x, y, z, w; };
+__device__ __forceinline__ Lu4<float> lu_ld4(const float* p) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Lu4<double> lu_ld4(const double* p) {
+  const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+  return {a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void lu_st4(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void lu_st4(double* p, double a, double b, double c, double d) {
+  *reinterpret_cast<double2*>(p) = make_double2(a, b);
+  *reinterpret_cast<double2*>(p + 2) = make_double2(c, d);
 }
 
 template <class R>
@@ -124,10 +155,11 @@ template <class R>
 __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_params& p, int band, int t, int l, int scale) {
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nst = lu_nstep(S.jd);
   const int r = 32 * band + l, c = t - l;
-  R* ch = S.lurec + ((int64_t)band * nst + t) * LU_CHUNK;
+  R* rr = S.lurec + ((int64_t)band * nst + t) * LuLay<R>::CH + l * LuLay<R>::LS;
   if (r >= nrow || c < 0 || c >= ncol) {
+    const R z = (R)0;
 #pragma unroll
-    for (int f = 0; f < LU_NF; ++f) ch[f * 32 + l] = (R)0;
+    for (int f = 0; f < LU_NF; f += 4) lu_st4(rr + f, z, z, z, z);
     return;
   }
   const int j = p.jbeg + c, k = p.kbeg + r;
@@ -135,21 +167,23 @@ __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_param
   const int64_t o = at(S.jd, j, k);
   LuCell<R> cl = lu_cell(S, p, j, k, epsv);
   const R ts = S.tscale[o];
+  R sv[4];
 #pragma unroll
   for (int n = 0; n < 4; ++n) {
     R v = S.s[n * S.qs + o];
-    ch[(LF_S + n) * 32 + l] = scale ? v * ts : v;
+    sv[n] = scale ? v * ts : v;
   }
-  ch[LF_SV * 32 + l] = ts * (R)0.5;
-  ch[LF_D * 32 + l] = cl.d;
-  ch[LF_UU * 32 + l] = cl.uu; ch[LF_VV * 32 + l] = cl.vv; ch[LF_UV2 * 32 + l] = cl.uv2; ch[LF_GE * 32 + l] = cl.ge;
-  ch[LF_RI1 * 32 + l] = cl.ri1; ch[LF_RI2 * 32 + l] = cl.ri2; ch[LF_RK1 * 32 + l] = cl.rk1; ch[LF_RK2 * 32 + l] = cl.rk2;
-  ch[LF_QX * 32 + l] = cl.qx; ch[LF_QY * 32 + l] = cl.qy;
-  R a, b;
-  lu_chkspec<R, true, true>(cl, eps2, a, b);   ch[LF_FCX * 32 + l] = a; ch[LF_FSX * 32 + l] = b;
-  lu_chkspec<R, false, true>(cl, eps2, a, b);  ch[LF_FCY * 32 + l] = a; ch[LF_FSY * 32 + l] = b;
-  lu_chkspec<R, true, false>(cl, eps2, a, b);  ch[LF_BCX * 32 + l] = a; ch[LF_BSX * 32 + l] = b;
-  lu_chkspec<R, false, false>(cl, eps2, a, b); ch[LF_BCY * 32 + l] = a; ch[LF_BSY * 32 + l] = b;
+  lu_st4(rr + LF_S, sv[0], sv[1], sv[2], sv[3]);
+  lu_st4(rr + LF_SV, ts * (R)0.5, cl.d, cl.uu, cl.vv);
+  lu_st4(rr + LF_UV2, cl.uv2, cl.ge, cl.ri1, cl.ri2);
+  lu_st4(rr + LF_RK1, cl.rk1, cl.rk2, cl.qx, cl.qy);
+  R a, b, a2, b2;
+  lu_chkspec<R, true, true>(cl, eps2, a, b);
+  lu_chkspec<R, false, true>(cl, eps2, a2, b2);
+  lu_st4(rr + LF_FCX, a, b, a2, b2);
+  lu_chkspec<R, true, false>(cl, eps2, a, b);
+  lu_chkspec<R, false, false>(cl, eps2, a2, b2);
+  lu_st4(rr + LF_BCX, a, b, a2, b2);
 }
 
 // halo-contribution arrays after the chunks: A forward [nrow][4], A backward,
@@ -157,7 +191,7 @@ __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_param
 template <class R>
 __device__ __forceinline__ R* lu_halo(const Slice<R>& S, int which) {
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd);
-  R* base = S.lurec + (int64_t)lu_nband(S.kd) * lu_nstep(S.jd) * LU_CHUNK;
+  R* base = S.lurec + (int64_t)lu_nband(S.kd) * lu_nstep(S.jd) * LuLay<R>::CH;
   switch (which) {
     case 0: return base;
     case 1: return base + 4 * nrow;
@@ -275,7 +309,7 @@ constexpr int LU_XB = 128;   // a power of two
 // maxcol columns).
 template <class R>
 __host__ __device__ __forceinline__ size_t lu_smem_bytes(int nwarp, int G, int maxcol) {
-  return (size_t)nwarp * 2 * G * LU_CHUNK * sizeof(R) + (size_t)nwarp * 2 * sizeof(uint64_t) +
+  return (size_t)nwarp * 2 * G * LuLay<R>::CH * sizeof(R) + (size_t)nwarp * 2 * sizeof(uint64_t) +
          (size_t)nwarp * LU_XB * 4 * sizeof(R) + (size_t)nwarp * sizeof(int) + 16 +
          (size_t)4 * maxcol * sizeof(R);
 }
@@ -297,27 +331,28 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   const R gm1 = (R)p.gm1;
   R* rings = (R*)smem;
-  uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * 2 * G * LU_CHUNK * sizeof(R));
+  constexpr int CH = LuLay<R>::CH, LS = LuLay<R>::LS;
+  uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * 2 * G * CH * sizeof(R));
   R* xrings = (R*)(bars + (size_t)nwarp * 2);
   int* prog = (int*)(xrings + (size_t)nwarp * LU_XB * 4);
   // halo contributions into the first (forward) / last (backward) row,
   // read once per step by one lane: staged in shared memory
   R* bhs = (R*)(((uintptr_t)(prog + nwarp) + 15) & ~(uintptr_t)15);
-  R* ring = rings + (size_t)w * 2 * G * LU_CHUNK;
+  R* ring = rings + (size_t)w * 2 * G * CH;
   uint64_t* bar = bars + (size_t)w * 2;
   const bool wok = w < nb;
-  const R* rec_w = S.lurec + (int64_t)w * nst * LU_CHUNK;
-  R* recw = S.lurec + (int64_t)w * nst * LU_CHUNK;
+  const R* rec_w = S.lurec + (int64_t)w * nst * CH;
+  R* recw = S.lurec + (int64_t)w * nst * CH;
   const int ngrp = (nst + G - 1) / G;
   // group g of the sweep covers local steps g*G .. g*G+G-1; its chunks are
   // contiguous in memory starting at chunk c0(g) (ascending)
   auto c0 = [&](int g) -> int { return FWD ? g * G : max(0, nst - (g + 1) * G); };
   auto gsize = [&](int g) -> int { return min(G, nst - g * G); };
   auto issue = [&](int g) {
-    const uint32_t bytes = (uint32_t)gsize(g) * LU_CHUNK * sizeof(R);
+    const uint32_t bytes = (uint32_t)gsize(g) * CH * sizeof(R);
     fence_proxy_async_smem();
     mbar_expect_tx(&bar[g & 1], bytes);
-    bulk_g2s(ring + (size_t)(g & 1) * G * LU_CHUNK, rec_w + (int64_t)c0(g) * LU_CHUNK, bytes, &bar[g & 1]);
+    bulk_g2s(ring + (size_t)(g & 1) * G * CH, rec_w + (int64_t)c0(g) * CH, bytes, &bar[g & 1]);
   };
   if (l == 0) {
     if (wok) { mbar_init(&bar[0], 1); mbar_init(&bar[1], 1); }
@@ -352,11 +387,15 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
     const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
     if (__any_sync(0xffffffffu, !ok || bad)) { gfail = g; break; }
     const int gs = gsize(g);
-    const R* gring = ring + (size_t)(g & 1) * G * LU_CHUNK;
+    const R* gring = ring + (size_t)(g & 1) * G * CH;
 #pragma unroll 1
     for (int u = 0; u < gs; ++u) {
       const int tl = g * G + u;
-      const R* ch = gring + (FWD ? u : gs - 1 - u) * LU_CHUNK;
+      // this lane's record: residual, (tscale/2, d, u, v), (uv2, ge, xi
+      // metrics), (eta metrics, qx, qy), this sweep's (chk, spec) pairs
+      const R* rr = gring + (FWD ? u : gs - 1 - u) * CH + l * LS;
+      const Lu4<R> r0 = lu_ld4(rr + LF_S), r1 = lu_ld4(rr + LF_SV), r2 = lu_ld4(rr + LF_UV2),
+                   r3 = lu_ld4(rr + LF_RK1), r4 = lu_ld4(rr + (FWD ? LF_FCX : LF_BCX));
       R bin[4];
 #pragma unroll
       for (int n = 0; n < 4; ++n)
@@ -382,26 +421,22 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
             bad = true;
           }
         }
-        const R sv = ch[LF_SV * 32 + l], di = ch[LF_D * 32 + l];
+        const R sv = r1.x, di = r1.y;
+        const R st[4] = {r0.x, r0.y, r0.z, r0.w};
         R sn[4];
 #pragma unroll
-        for (int n = 0; n < 4; ++n) {
-          const R st = ch[(LF_S + n) * 32 + l];
-          sn[n] = FWD ? (st + sv * (aprev[n] + bin[n])) * di : st - sv * (aprev[n] + bin[n]) * di;
-        }
+        for (int n = 0; n < 4; ++n)
+          sn[n] = FWD ? (st[n] + sv * (aprev[n] + bin[n])) * di : st[n] - sv * (aprev[n] + bin[n]) * di;
         if (FWD) {
-          R* gch = recw + (int64_t)tl * LU_CHUNK;
-#pragma unroll
-          for (int n = 0; n < 4; ++n) gch[(LF_S + n) * 32 + l] = sn[n];
+          lu_st4(recw + (int64_t)tl * CH + l * LS + LF_S, sn[0], sn[1], sn[2], sn[3]);
         } else {
 #pragma unroll
           for (int n = 0; n < 4; ++n) srow[n * S.qs + c] = sn[n];
         }
-        const R uu = ch[LF_UU * 32 + l], vv = ch[LF_VV * 32 + l], uv2 = ch[LF_UV2 * 32 + l], ge = ch[LF_GE * 32 + l];
-        lu_apply(ch[(FWD ? LF_FCX : LF_BCX) * 32 + l], ch[(FWD ? LF_FSX : LF_BSX) * 32 + l], ch[LF_RI1 * 32 + l],
-                 ch[LF_RI2 * 32 + l], ch[LF_QX * 32 + l], uu, vv, uv2, ge, gm1, sn, aprev);
-        lu_apply(ch[(FWD ? LF_FCY : LF_BCY) * 32 + l], ch[(FWD ? LF_FSY : LF_BSY) * 32 + l], ch[LF_RK1 * 32 + l],
-                 ch[LF_RK2 * 32 + l], ch[LF_QY * 32 + l], uu, vv, uv2, ge, gm1, sn, bout);
+        // xi: (chk, spec) = r4.x, r4.y with ri1, ri2, qx; eta: r4.z, r4.w
+        // with rk1, rk2, qy; u, v, uv2, ge shared
+        lu_apply(r4.x, r4.y, r2.z, r2.w, r3.z, r1.z, r1.w, r2.x, r2.y, gm1, sn, aprev);
+        lu_apply(r4.z, r4.w, r3.x, r3.y, r3.w, r1.z, r1.w, r2.x, r2.y, gm1, sn, bout);
       }
       // hand the boundary contribution to the next band (its slot must have
       // been read: the consumer is at least at step tl - LU_XB + 32), then

@@ -470,10 +470,16 @@ __global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__
   const int64_t o = at(S.jd, j, k);
   int ibi = S.iblank[o];
   double m = (double)(ibi > 0 ? ibi : 0);
+  // every load before the first store (the state and the residual may not
+  // alias, but the compiler cannot know): eight independent loads in flight
+  double q0[4];
+  R sv[4];
+#pragma unroll
+  for (int n = 0; n < 4; ++n) { q0[n] = S.q64[n * S.qs + o]; sv[n] = S.s[n * S.qs + o]; }
   R qn[4];
 #pragma unroll
   for (int n = 0; n < 4; ++n) {
-    double v = S.q64[n * S.qs + o] + (double)S.s[n * S.qs + o] * m;
+    double v = q0[n] + (double)sv[n] * m;
     S.q64[n * S.qs + o] = v;
     qn[n] = (R)v;
     if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = qn[n];

@@ -43,6 +43,15 @@ struct Batch {
 template <class R>
 cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st);
 
+// The second stream of an iteration (one per device and host thread) and
+// the events of its fork and join; created on first use.  Call it once
+// before capturing an iteration into a graph.
+struct Branch {
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+cudaError_t branch_of_device(Branch*& out);
+
 // Individual phases (the drop-in routines call these on a batch of one).
 template <class R> cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st);

@@ -53,10 +53,19 @@ cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_rbc<R><<<b.nslice, 128, 0, st>>>(d_sl);
   return cudaGetLastError();
 }
+// ilu2d part 1: the sweep records and the halo edges (reads q, mu_t, tscale;
+// the FP64 path also round-trips q here)
 template <class R>
-cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
+cudaError_t launch_lusgs_prep(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
   k_lu_prep<R><<<b.lu_blocks, CELL_BS, 0, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
   k_lu_edges<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
+  return cudaGetLastError();
+}
+// ilu2d part 2: the forward and backward sweeps, launched at the device's
+// highest priority (they are the iteration's longest dependency chain and
+// run beside the turbulence branch)
+template <class R>
+cudaError_t launch_lusgs_sweeps(const Slice<R>* d_sl, const Batch& b, cudaStream_t st, int only_lu) {
   const int nw = b.max_lu_warps;
   // chunks per bulk copy: as many as ~200 KB of shared memory allows (1..8)
   const int maxcol = b.max_wall;   // >= jd - 2 of every slice
@@ -64,6 +73,7 @@ cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaSt
   while (G > 1 && lu_smem_bytes<R>(nw, G, maxcol) > 200 * 1024) G >>= 1;
   const size_t smem = lu_smem_bytes<R>(nw, G, maxcol);
   static bool attr_set = false;
+  static int prio = 0;
   if (!attr_set) {
     const void* ks[] = {(const void*)k_lu_sweep<R, true, 8>, (const void*)k_lu_sweep<R, false, 8>,
                         (const void*)k_lu_sweep<R, true, 4>, (const void*)k_lu_sweep<R, false, 4>,
@@ -73,12 +83,24 @@ cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaSt
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
       if (e != cudaSuccess) return e;
     }
+    int lo = 0, hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess) prio = hi;
     attr_set = true;
   }
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = prio;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(b.nslice);
+  cfg.blockDim = dim3(32 * nw);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
   auto run = [&](auto fwd, auto bwd) -> cudaError_t {
-    fwd<<<b.nslice, 32 * nw, smem, st>>>(d_sl, only_lu);
-    bwd<<<b.nslice, 32 * nw, smem, st>>>(d_sl, only_lu);
-    return cudaSuccess;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, fwd, d_sl, only_lu);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernelEx(&cfg, bwd, d_sl, only_lu);
   };
   cudaError_t e;
   switch (G) {
@@ -89,6 +111,12 @@ cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaSt
   }
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
+  cudaError_t e = launch_lusgs_prep(d_sl, b, scale, st, only_lu);
+  if (e != cudaSuccess) return e;
+  return launch_lusgs_sweeps(d_sl, b, st, only_lu);
 }
 template <class R>
 cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
@@ -169,10 +197,28 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   if ((e = launch_bc(d_sl, b, 1, st)) != cudaSuccess) return e;
   if ((e = launch_residual(d_sl, b, viscous, st)) != cudaSuccess) return e;
   if ((e = launch_rbc(d_sl, b, st)) != cudaSuccess) return e;
-  if ((lhs & 1) && (e = launch_lusgs(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
-  if ((lhs & 2) && (e = launch_adi(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
-  if ((turb & 1) && (e = launch_sa(d_sl, b, st)) != cudaSuccess) return e;
-  if ((turb & 2) && (e = launch_sst(d_sl, b, st)) != cudaSuccess) return e;
+  if (lhs == 1 && turb) {
+    // The turbulence solve (step.f:184-190) reads q, mu_t and tscale, which
+    // the LU-SGS sweeps do not write, and writes its own variables and mu_t,
+    // which the sweeps do not read once the records are built: after the
+    // record / edge kernels (mu_t read, FP64 q round trip done) it runs on
+    // a second stream beside the sweeps, joined before the update.
+    Branch* br = nullptr;
+    if ((e = branch_of_device(br)) != cudaSuccess) return e;
+    if ((e = launch_lusgs_prep(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(br->fork, st)) != cudaSuccess) return e;
+    if ((e = launch_lusgs_sweeps(d_sl, b, st, 1)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(br->st, br->fork, 0)) != cudaSuccess) return e;
+    if ((turb & 1) && (e = launch_sa(d_sl, b, br->st)) != cudaSuccess) return e;
+    if ((turb & 2) && (e = launch_sst(d_sl, b, br->st)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(br->join, br->st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, br->join, 0)) != cudaSuccess) return e;
+  } else {
+    if ((lhs & 1) && (e = launch_lusgs(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
+    if ((lhs & 2) && (e = launch_adi(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
+    if ((turb & 1) && (e = launch_sa(d_sl, b, st)) != cudaSuccess) return e;
+    if ((turb & 2) && (e = launch_sst(d_sl, b, st)) != cudaSuccess) return e;
+  }
   if ((e = launch_update(d_sl, b, st)) != cudaSuccess) return e;
   return cudaSuccess;  // the monitor runs inside k_update and k_bc
 }
