@@ -244,7 +244,12 @@ int ot2d_solver_profile(ot2d_solver* s, int32_t iters, double* ms, int32_t nphas
 int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, double* const* q_host, int32_t iters);
 /* Admit one solve: params + vertex grid of time instance 1 (jmax*kmax).
  * Returns the instance id (>= 0) or -status.  `orders` = target L2 drop in
- * decades; max_iters caps the iterations. */
+ * decades; max_iters caps the iterations.  A time-accurate solve (iunst = 1,
+ * motiontype = 1: the pitching grid of motion.f:546-632, dual time stepping
+ * with itnmax Newton iterations per physical step, Turns_overset.f:360-505)
+ * runs exactly max_iters physical steps, has no residual convergence test,
+ * and is retired after its last Newton iteration.  A steady solve runs at
+ * most max_iters iterations. */
 int ot2d_solver_add(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv, double orders,
                     int32_t max_iters);
 /* Run `iters` iterations over every live instance (one launch per kernel

@@ -30,9 +30,21 @@ void bc(const P& p, A3 q, A2 x, A2 y, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, 
 /* bc.f:88-177 */
 void rbc(const P& p, A3 q, A3 s);
 
-/* eulerrhs.f:2-280 (nei=1, iprecon=.false.) */
+/* eulerrhs.f:2-280 (nei=1, iprecon=.false.); xold..yole: the vertices of
+ * the two previous time levels, needed when iunst > 0 (face speeds from the
+ * swept areas, eulerrhs.f:118-140, :224-246) */
 void rhsup(const P& p, A3 q, A3 s, const double* xv, const double* yv, I2 iblank,
-           const double* ugv, const double* vgv);
+           const double* ugv, const double* vgv, const double* xold = nullptr, const double* yold = nullptr,
+           const double* xole = nullptr, const double* yole = nullptr);
+/* motion.f:546-632 (pitch, motiontype 1): rotates the cell centres and the
+ * vertices by the step's pitch increment about (xac, yac), sets the cell
+ * grid speeds, shifts the two previous vertex levels */
+void pitch(const P& p, A2 x, A2 y, double* xv, double* yv, double* xold, double* yold, double* xole, double* yole,
+           A2 ug, A2 vg);
+/* time.f:110-175 (all nspec instances; qtn, qtnm1, qnewt: (jd,kd,nspec,nv)) */
+void stqol(const P& p, const double* q, double* qtn, double* qtnm1, double* qnewt);
+/* time.f:178-210 for one instance: s -= (q - qnewt)/(oat*h) on the interior */
+void newton(const P& p, A3 q, const double* qnewt, A3 s);
 /* visrhs.f:2-287 */
 void visrhs(const P& p, A2 turmu, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy);
 /* time.f:2-108 (one time instance) */

@@ -231,9 +231,10 @@ static void reconstruct(const P& p, Line& L, int n, double th, double qt, double
   (void)eps;
 }
 
-/* eulerrhs.f:2-280 with nei=1, iprecon=.false., iunst=0 */
+/* eulerrhs.f:2-280 with nei=1, iprecon=.false. */
 void rhsup(const P& p, A3 q, A3 s, const double* xv_, const double* yv_, I2 iblank,
-           const double* ugv_, const double* vgv_) {
+           const double* ugv_, const double* vgv_, const double* xold_, const double* yold_,
+           const double* xole_, const double* yole_) {
   const int jd = p.jd, kd = p.kd, nq = p.nq, jmax = p.jmax, nhalo = p.nhalo;
   auto xv = [&](int j, int k) { return xv_[(size_t)(k - 1) * jmax + (j - 1)]; };
   auto yv = [&](int j, int k) { return yv_[(size_t)(k - 1) * jmax + (j - 1)]; };
@@ -251,7 +252,13 @@ void rhsup(const P& p, A3 q, A3 s, const double* xv_, const double* yv_, I2 ibla
       ppp(j, k) = p.gm1 * (q(j, k, 4) - 0.5 * (p2(q(j, k, 2)) + p2(q(j, k, 3))) / q(j, k, 1));
   int mdim = (jd > kd ? jd : kd);
   Line L(mdim);
-  if (p.iunst > 0) { std::fprintf(stderr, "oracle: iunst>0 not restated\n"); std::abort(); }
+  if (p.iunst > 0 && (!xold_ || !yold_ || !xole_ || !yole_)) {
+    std::fprintf(stderr, "oracle: iunst>0 needs the previous vertex levels\n"); std::abort();
+  }
+  auto xold = [&](int j, int k) { return xold_[(size_t)(k - 1) * jmax + (j - 1)]; };
+  auto yold = [&](int j, int k) { return yold_[(size_t)(k - 1) * jmax + (j - 1)]; };
+  auto xole = [&](int j, int k) { return xole_[(size_t)(k - 1) * jmax + (j - 1)]; };
+  auto yole = [&](int j, int k) { return yole_[(size_t)(k - 1) * jmax + (j - 1)]; };
   /* xi fluxes */
   for (int k = p.kbeg; k <= p.kend; ++k) {
     int kv = k - nhalo + 1;
@@ -269,7 +276,24 @@ void rhsup(const P& p, A3 q, A3 s, const double* xv_, const double* yv_, I2 ibla
       L.xa[j] = (yv(jv, kv) - yv(jv, kv - 1));
       L.ya[j] = -(xv(jv, kv) - xv(jv, kv - 1));
     }
-    if (p.timespectral) {
+    if (p.iunst > 0) {
+      /* eulerrhs.f:118-139: face speed from the area the face sweeps */
+      for (int j = p.jbeg - 1; j <= p.jend; ++j) {
+        int jv = j - nhalo + 1;
+        double dx1 = xv(jv, kv) - xold(jv, kv - 1), dy1 = yv(jv, kv) - yold(jv, kv - 1);
+        double dx2 = xold(jv, kv) - xv(jv, kv - 1), dy2 = yold(jv, kv) - yv(jv, kv - 1);
+        L.tj[j] = -(0.5 * (dx1 * dy2 - dx2 * dy1) / p.dt);
+      }
+      if (p.ntac == 2 && p.istep > 1) {
+        for (int j = p.jbeg - 1; j <= p.jend; ++j) {
+          int jv = j - nhalo + 1;
+          double dx1 = xold(jv, kv) - xole(jv, kv - 1), dy1 = yold(jv, kv) - yole(jv, kv - 1);
+          double dx2 = xole(jv, kv) - xold(jv, kv - 1), dy2 = yole(jv, kv) - yold(jv, kv - 1);
+          double temp = -(0.5 * (dx1 * dy2 - dx2 * dy1) / p.dt);
+          L.tj[j] = 1.5 * L.tj[j] - 0.5 * temp;
+        }
+      }
+    } else if (p.timespectral) {
       for (int j = p.jbeg - 1; j <= p.jend; ++j) {
         int jv = j - nhalo + 1;
         L.tj[j] = -0.5 * (ugv(jv, kv) + ugv(jv, kv - 1)) * L.xa[j] - 0.5 * (vgv(jv, kv) + vgv(jv, kv - 1)) * L.ya[j];
@@ -298,7 +322,24 @@ void rhsup(const P& p, A3 q, A3 s, const double* xv_, const double* yv_, I2 ibla
       L.xa[k] = -(yv(jv, kv) - yv(jv - 1, kv));
       L.ya[k] = (xv(jv, kv) - xv(jv - 1, kv));
     }
-    if (p.timespectral) {
+    if (p.iunst > 0) {
+      /* eulerrhs.f:224-246 */
+      for (int k = p.kbeg - 1; k <= p.kend; ++k) {
+        int kv = k - nhalo + 1;
+        double dx1 = xv(jv, kv) - xold(jv - 1, kv), dy1 = yv(jv, kv) - yold(jv - 1, kv);
+        double dx2 = xold(jv, kv) - xv(jv - 1, kv), dy2 = yold(jv, kv) - yv(jv - 1, kv);
+        L.tj[k] = 0.5 * (dx1 * dy2 - dx2 * dy1) / p.dt;
+      }
+      if (p.ntac == 2 && p.istep > 1) {
+        for (int k = p.kbeg - 1; k <= p.kend; ++k) {
+          int kv = k - nhalo + 1;
+          double dx1 = xold(jv, kv) - xole(jv - 1, kv), dy1 = yold(jv, kv) - yole(jv - 1, kv);
+          double dx2 = xole(jv, kv) - xold(jv - 1, kv), dy2 = yole(jv, kv) - yold(jv - 1, kv);
+          double temp = 0.5 * (dx1 * dy2 - dx2 * dy1) / p.dt;
+          L.tj[k] = 1.5 * L.tj[k] - 0.5 * temp;
+        }
+      }
+    } else if (p.timespectral) {
       for (int k = p.kbeg - 1; k <= p.kend; ++k) {
         int kv = k - nhalo + 1;
         L.tj[k] = -0.5 * (ugv(jv, kv) + ugv(jv - 1, kv)) * L.xa[k] - 0.5 * (vgv(jv, kv) + vgv(jv - 1, kv)) * L.ya[k];

@@ -222,10 +222,28 @@ void oro_force2d(const P* p, double* q, const double* xv, const double* yv, doub
  * arrays (jd,kd,nspec[,n]).  norms[3*nsp+{0,1,2}] = rsum, resrho, resmax;
  * loc[3*nsp+{0,1,2}] = j,k,n of resmax.  Returns 0, or 2 when the L2 norm
  * exceeds 1000 (the reference's `stop 'norm'`, step.f:105-110). */
+int oro_step_u(const P* pp, double* q, double* s, double* x, double* y, const double* xv, const double* yv,
+               const int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+               const double* ugv, const double* vgv, double* turmu, double* tscale, double* bt, const double* Ds,
+               double* norms, int32_t* loc, const double* qnewt, const double* xold, const double* yold,
+               const double* xole, const double* yole);
+
 int oro_step(const P* pp, double* q, double* s, double* x, double* y, const double* xv, const double* yv,
              const int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
              const double* ugv, const double* vgv, double* turmu, double* tscale, double* bt, const double* Ds,
              double* norms, int32_t* loc) {
+  return oro_step_u(pp, q, s, x, y, xv, yv, iblank, xx, xy, yx, yy, ug, vg, ugv, vgv, turmu, tscale, bt, Ds, norms,
+                    loc, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+/* step.f:2-218 with the time-accurate terms: qnewt (jd,kd,nspec,nv) is the
+ * Newton target of stqol (used when itnmax > 1, time.f:178-210), xold..yole
+ * the previous vertex levels (used when iunst > 0). */
+int oro_step_u(const P* pp, double* q, double* s, double* x, double* y, const double* xv, const double* yv,
+               const int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+               const double* ugv, const double* vgv, double* turmu, double* tscale, double* bt, const double* Ds,
+               double* norms, int32_t* loc, const double* qnewt, const double* xold, const double* yold,
+               const double* xole, const double* yole) {
   const P& p = *pp;
   const int jd = p.jd, kd = p.kd, nspec = p.nspec;
   size_t n2 = (size_t)jd * kd, nv2 = (size_t)jd * kd * nspec;
@@ -239,8 +257,14 @@ int oro_step(const P* pp, double* q, double* s, double* x, double* y, const doub
     A2 z{nullptr, jd};
     bc(p, qn, z, z, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
        v2(pp, bt + o));
-    rhsup(p, qn, sn, xv + (nsp - 1) * nvert, yv + (nsp - 1) * nvert, I2{iblank + o, jd}, ugv + (nsp - 1) * nvert,
-          vgv + (nsp - 1) * nvert);
+    const size_t ov = (size_t)(nsp - 1) * nvert;
+    rhsup(p, qn, sn, xv + ov, yv + ov, I2{iblank + o, jd}, ugv + ov, vgv + ov, xold ? xold + ov : nullptr,
+          yold ? yold + ov : nullptr, xole ? xole + ov : nullptr, yole ? yole + ov : nullptr);
+    // compute_residual, step.f:274-285 (time-spectral Newton terms are not restated)
+    if (p.itnmax > 1 && !p.timespectral) {
+      if (!qnewt) { std::fprintf(stderr, "oracle: itnmax>1 needs qnewt\n"); std::abort(); }
+      newton(p, qn, qnewt + o, sn);
+    }
     if (!p.invisc) visrhs(p, v2(pp, turmu + o), qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o));
     if (p.timespectral) timespectralrhs(p, q, s, Ds, nsp);
   }
@@ -372,10 +396,27 @@ int oro_solve_from(const P* pin, const double* xv1, const double* yv1, int nstep
     for (int n = 0; n < p.nv; ++n) std::memcpy(q.data() + (size_t)n * nv2, q_init + (size_t)n * nv2, sizeof(double) * nv2);
   std::vector<double> norms(3 * nspec), first(nspec, 0.0);
   std::vector<int32_t> loc(3 * nspec);
+  // time-accurate state: previous vertex levels (init.f:101-108) and the
+  // stqol levels (time.f:110-175)
+  const bool moving = p.iunst > 0 && p.motiontype == 1;
+  if (p.iunst > 0 && !moving) { std::fprintf(stderr, "oracle: only motiontype 1 (pitch) is restated\n"); std::abort(); }
+  std::vector<double> xold(xv), yold(yv), xole(xv), yole(yv);
+  std::vector<double> qtn(p.itnmax > 1 ? nv2 * p.nv : 0, 0.0), qtnm1(qtn), qnewt(qtn);
   p.istep0 = q_init ? istep0_init : 0;
   int it = 0, stopped = 0;
   for (int istep = 1; istep <= nsteps; ++istep) {
     p.istep0 += 1; p.istep = istep;
+    // Turns_overset.f:365-403
+    if (p.iunst != 0) p.totime += p.dt;
+    if (moving) {
+      pitch(p, A2{x.data(), jd}, A2{y.data(), jd}, xv.data(), yv.data(), xold.data(), yold.data(), xole.data(),
+            yole.data(), A2{ug.data(), jd}, A2{vg.data(), jd});
+      A3 qn{q.data(), jd, nv2};
+      if (metfv(p, qn, xv.data(), yv.data(), A2{xx.data(), jd}, A2{xy.data(), jd}, A2{yx.data(), jd},
+                A2{yy.data(), jd}) != 0)
+        return -istep;
+    }
+    if (p.itnmax > 1) stqol(p, q.data(), qtn.data(), qtnm1.data(), qnewt.data());
     for (int itn = 1; itn <= p.itnmax; ++itn) {
       p.itn = itn;
       for (int nsp = 1; nsp <= nspec; ++nsp) {
@@ -384,9 +425,12 @@ int oro_solve_from(const P* pin, const double* xv1, const double* yv1, int nstep
                   A2{yy.data() + o, jd}, A2{ug.data() + o, jd}, A2{vg.data() + o, jd}, A2{tscale.data() + o, jd},
                   A2{bt.data() + o, jd}, I2{iblank.data() + o, jd});
       }
-      int st = oro_step(&p, q.data(), s.data(), x.data(), y.data(), xv.data(), yv.data(), iblank.data(), xx.data(),
-                        xy.data(), yx.data(), yy.data(), ug.data(), vg.data(), ugv.data(), vgv.data(), turmu.data(),
-                        tscale.data(), bt.data(), Ds.data(), norms.data(), loc.data());
+      int st = oro_step_u(&p, q.data(), s.data(), x.data(), y.data(), xv.data(), yv.data(), iblank.data(),
+                          xx.data(), xy.data(), yx.data(), yy.data(), ug.data(), vg.data(), ugv.data(), vgv.data(),
+                          turmu.data(), tscale.data(), bt.data(), Ds.data(), norms.data(), loc.data(),
+                          p.itnmax > 1 ? qnewt.data() : nullptr, moving ? xold.data() : nullptr,
+                          moving ? yold.data() : nullptr, moving ? xole.data() : nullptr,
+                          moving ? yole.data() : nullptr);
       int bad = 0;
       for (int nsp = 0; nsp < nspec; ++nsp) bad += monitor(p, A3{q.data() + nsp * n2, jd, nv2});
       if (st != 0 || bad != 0) stopped = 1;

@@ -1,0 +1,88 @@
+"""GPU parity of the time-accurate path (iunst = 1, motiontype = 1): a
+pitching NACA 0012 advanced by dual time stepping -- per physical step the
+grid rotation, metrics, face speeds and wall distances on the device
+(motion.f pitch, setup.f metfv, eulerrhs.f swept-area face speeds,
+samodel2d.f dist), stqol, then itnmax Newton iterations with the physical-time
+term of newton -- through the batched solver, against the oracle driver
+running the same Turns_overset.f loop.
+
+Tolerance: 1e-12 relative on the state for Euler and SA (the FP64 path keeps
+the reference's operation order, including the geometry); 1e-10 for SST, as
+in the steady SST test (pow / exp of its source terms may differ by an ulp).
+"""
+import numpy as np
+import pytest
+
+from tests import oracle_binding as ob
+from tests.helpers import relerr
+from turns2d_urans_git_gb300 import api
+from turns2d_urans_git_gb300.abi import OT2D_FP64, OT2D_FP32_MIXED
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    # name: (config_pitching kwargs, physical steps, state tolerance)
+    "euler_ntac2": (dict(jmax=97, kmax=25, ntac=2, itnmax=4, dt=0.1, rf=0.5, angmax=2.0), 8, 1e-12),
+    "euler_ntac1": (dict(jmax=97, kmax=25, ntac=1, itnmax=3, dt=0.1, rf=0.5, angmax=2.0), 6, 1e-12),
+    "euler_ntac3": (dict(jmax=97, kmax=25, ntac=3, itnmax=3, dt=0.1, rf=0.5, angmax=2.0), 6, 1e-12),
+    "sa_ntac2": (dict(jmax=97, kmax=33, viscous=True, iturb=1, ntac=2, itnmax=3, dt=0.1, rf=0.5, angmax=2.0), 5,
+                 1e-12),
+    "sst_ntac2": (dict(jmax=97, kmax=33, viscous=True, iturb=2, ntac=2, itnmax=3, dt=0.1, rf=0.5, angmax=2.0), 5,
+                  1e-10),
+}
+
+
+@pytest.mark.parametrize("kind", sorted(CASES))
+def test_solver_pitching_fp64_matches_oracle(kind):
+    kw, nsteps, tol = CASES[kind]
+    _, prm, xv, yv = api.config_pitching(**kw)
+    n, hist, forces, q_o = ob.solve(prm, xv.ravel(), yv.ravel(), nsteps)
+    assert n == nsteps
+    # a status-check interval that does not divide the iteration count: the
+    # instance still stops after exactly nsteps physical steps
+    sv = api.Solver(OT2D_FP64, check_every=7, keep_q=True)
+    iid = sv.add(prm, xv, yv, orders=0.0, max_iters=nsteps)
+    sv.iterate(nsteps * prm.itnmax + 20)
+    assert sv.live() == 0
+    r = sv.result(iid)
+    q = sv.get_q(iid, prm)
+    sv.close()
+    assert r.status == 0 and r.iterations == nsteps, (r.status, r.iterations)
+    assert relerr(q, q_o) <= tol
+    assert abs(r.rsum_last - hist[-1, 0]) <= 1e-9 * hist[-1, 0]
+    f = forces[0]
+    for a, b in ((r.cl, f[0]), (r.cd, f[1]), (r.cm, f[2])):
+        assert abs(a - b) <= 100 * tol * max(abs(b), 1e-3)
+
+
+def test_solver_pitching_mixed_close_to_fp64():
+    """The FP32-mixed path on the same pitching Euler case: forces within
+    1e-4 of FP64 after 8 physical steps (the f32 residual has no freestream
+    correction on a moving grid)."""
+    _, prm, xv, yv = api.config_pitching(jmax=97, kmax=25, ntac=2, itnmax=4, dt=0.1, rf=0.5, angmax=2.0)
+    out = {}
+    for prec in (OT2D_FP64, OT2D_FP32_MIXED):
+        sv = api.Solver(prec, check_every=100)
+        iid = sv.add(prm, xv, yv, orders=0.0, max_iters=8)
+        sv.iterate(8 * prm.itnmax)
+        assert sv.live() == 0
+        out[prec] = sv.result(iid)
+        sv.close()
+    a, b = out[OT2D_FP32_MIXED], out[OT2D_FP64]
+    assert a.status == 0 and a.iterations == 8
+    assert abs(a.cl - b.cl) <= 1e-4 and abs(a.cd - b.cd) <= 1e-4
+
+
+def test_steady_instance_stops_exactly_at_its_cap():
+    """A steady instance whose cap is not a multiple of the status-check
+    interval runs exactly max_iters iterations."""
+    _, prm, xv, yv = api.config_c1(jmax=65, kmax=25)
+    n, hist, forces, q_o = ob.solve(prm, xv.ravel(), yv.ravel(), 30)
+    sv = api.Solver(OT2D_FP64, check_every=25, keep_q=True)
+    iid = sv.add(prm, xv, yv, orders=0.0, max_iters=30)
+    sv.iterate(100)
+    r = sv.result(iid)
+    q = sv.get_q(iid, prm)
+    sv.close()
+    assert r.iterations == 30
+    assert relerr(q, q_o) <= 1e-12

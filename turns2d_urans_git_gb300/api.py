@@ -103,6 +103,22 @@ def config_c1(jmax=257, kmax=65):
                       irhsy=-3, ilim=1, ilhs=1, iconstant_cfl=1, dt=10.0, fsmach=0.80, alfa=1.25)
 
 
+def config_pitching(jmax=129, kmax=33, viscous=False, iturb=1, ntac=2, itnmax=4, dt=0.05, rf=0.2, angmax=2.0,
+                    xac=0.25, fsmach=0.5, alfa=0.0, rey=1e6, ds_wall=None):
+    """Time-accurate pitching NACA 0012 (iunst=1, motiontype=1: alpha(t) =
+    alfa + angmax*(1 - cos(rf*t)) about (xac, 0)): dual time stepping with
+    itnmax Newton iterations per physical step dt at order ntac, MUSCL,
+    LU-SGS, pseudo-time CFL 1; Euler, or RANS (iturb 1 SA / 2 SST)."""
+    kw = dict(invisc=1, lamin=1)
+    if viscous:
+        kw = dict(invisc=0, lamin=0, iturb=iturb, rey=rey, vnuinf=3.0)
+    if ds_wall is None:
+        ds_wall = wall_spacing(kmax) if viscous else 1e-3
+    return cmesh_case(jmax, kmax, naca=(0.0, 0.0, 0.12), ds_wall=ds_wall, irhsy=-3, ilim=1, ilhs=1,
+                      iconstant_cfl=1, idual=1, iunst=1, motiontype=1, ntac=ntac, itnmax=itnmax, dt=dt, rf=rf,
+                      angmax=angmax, xac=xac, yac=0.0, fsmach=fsmach, alfa=alfa, **kw)
+
+
 def config_c2(jmax=513, kmax=129, fsmach=0.15, alfa=10.0, rey=6e6, naca=(0.0, 0.0, 0.12), ds_wall=1e-6):
     """Viscous RANS-SA NACA 0012, M=0.15, alpha=10, Re=6e6, MUSCL, LU-SGS,
     local CFL 50, nu_tilde_inf = 3 nu_inf."""

@@ -127,7 +127,7 @@ int prepare(int nslice, int& err) {
   if ((err = ensure_stream())) return err;
   if (!g_ctx.has) return err = OT2D_ERR_NOPARAMS;
   const size_t n2 = (size_t)g_ctx.P.jd * g_ctx.P.kd, ws = (n2 + 63) / 64 * 64;
-  const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd, 8);
+  const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd);
   const size_t need = ws * DW_SLOTS * nslice + 8 * ws + rec * nslice;
   g_ctx.nslice = nslice;
   if (need > g_ctx.wcap) {
@@ -165,7 +165,7 @@ Slice<double> base_slice(int nsp, int nspec, int64_t qs) {
   const size_t n2 = (size_t)p.jd * p.kd, ws = (n2 + 63) / 64 * 64;
   S.w = g_ctx.dwork + (size_t)(nsp - 1) * ws * DW_SLOTS;
   S.wstride = (int64_t)ws;
-  S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd, 8);
+  S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = g_ctx.dred + (size_t)RED_N * (nsp - 1);
   S.ist = nullptr;
   slice_consts(S, p);
@@ -533,10 +533,18 @@ int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int3
   S.vg = (double*)resolve(vg, n2 * 8, true, false, err);
   S.turmu = (double*)resolve(turmu, n2 * 8, true, false, err);
   S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
+  // status word for the sweeps' bounded waits (bit 4: a wait gave up)
+  S.ist = g_ctx.dist;
+  if (!err && cudaMemsetAsync(g_ctx.dist, 0, sizeof(int32_t) * IST_N, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
   std::vector<Slice<double>> sl{S};
   run_batch(sl, err);
   if (!err && launch_lusgs<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
-  return finish(err);
+  int32_t ist[IST_N] = {0};
+  if (!err && cudaMemcpyAsync(ist, g_ctx.dist, sizeof(ist), cudaMemcpyDeviceToHost, g_ctx.st) != cudaSuccess)
+    err = OT2D_ERR_CUDA;
+  err = finish(err);
+  if (!err && (ist[2] & 4)) err = fail(OT2D_ERR_TIMEOUT);
+  return err;
 }
 
 int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,

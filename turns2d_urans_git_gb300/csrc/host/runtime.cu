@@ -41,6 +41,8 @@ size_t plan(const ot2d_params& p, int precision, F&& assign) {
   const bool mixed = precision == OT2D_FP32_MIXED;
   const size_t rb = mixed ? sizeof(float) : sizeof(double);
   const bool ts = p.timespectral != 0;
+  const bool mv = p.iunst == 1;          // time-accurate pitching grid
+  const bool gs = ts || mv;              // grid speeds present
   Layout L;
   assign("P", L.take(sizeof(ot2d_params)));
   assign("q64", L.take(sizeof(double) * n2 * nspec * p.nq));
@@ -48,10 +50,23 @@ size_t plan(const ot2d_params& p, int precision, F&& assign) {
   assign("xy64", L.take(sizeof(double) * n2 * nspec));
   assign("yx64", L.take(sizeof(double) * n2 * nspec));
   assign("yy64", L.take(sizeof(double) * n2 * nspec));
-  if (ts) {
+  if (gs) {
     assign("ug64", L.take(sizeof(double) * n2 * nspec));
     assign("vg64", L.take(sizeof(double) * n2 * nspec));
-    assign("Ds", L.take(sizeof(double) * nspec * nspec));
+  }
+  if (ts) assign("Ds", L.take(sizeof(double) * nspec * nspec));
+  if (mv) {
+    assign("xc", L.take(sizeof(double) * n2 * nspec));
+    assign("yc", L.take(sizeof(double) * n2 * nspec));
+    assign("xold", L.take(sizeof(double) * nvert * nspec));
+    assign("yold", L.take(sizeof(double) * nvert * nspec));
+    assign("xole", L.take(sizeof(double) * nvert * nspec));
+    assign("yole", L.take(sizeof(double) * nvert * nspec));
+    if (p.itnmax > 1) {
+      assign("qtn", L.take(sizeof(double) * n2 * nspec * p.nv));
+      assign("qtnm1", L.take(sizeof(double) * n2 * nspec * p.nv));
+      assign("qnewt", L.take(sizeof(double) * n2 * nspec * p.nv));
+    }
   }
   assign("xv", L.take(sizeof(double) * nvert * nspec));
   assign("yv", L.take(sizeof(double) * nvert * nspec));
@@ -62,22 +77,23 @@ size_t plan(const ot2d_params& p, int precision, F&& assign) {
     assign("xy", L.take(rb * n2 * nspec));
     assign("yx", L.take(rb * n2 * nspec));
     assign("yy", L.take(rb * n2 * nspec));
-    if (ts) { assign("ug", L.take(rb * n2 * nspec)); assign("vg", L.take(rb * n2 * nspec)); }
+    if (gs) { assign("ug", L.take(rb * n2 * nspec)); assign("vg", L.take(rb * n2 * nspec)); }
   }
   assign("s", L.take(rb * n2 * nspec * p.nv));
   assign("fxa", L.take(rb * n2 * nspec));
   assign("fya", L.take(rb * n2 * nspec));
   assign("gxa", L.take(rb * n2 * nspec));
   assign("gya", L.take(rb * n2 * nspec));
-  if (ts) { assign("ftj", L.take(rb * n2 * nspec)); assign("gtj", L.take(rb * n2 * nspec)); }
+  if (gs) { assign("ftj", L.take(rb * n2 * nspec)); assign("gtj", L.take(rb * n2 * nspec)); }
   assign("tscale", L.take(rb * n2 * nspec));
   assign("bt", L.take(rb * n2 * nspec));
   assign("turmu", L.take(rb * n2 * nspec));
   assign("sn", L.take(rb * n2 * nspec));
   assign("w", L.take(rb * ws * nscratch(p) * nspec));
   if (is_sst(p)) assign("wd2", L.take(sizeof(double) * n2 * nspec));
-  if (mixed) assign("sinf", L.take(rb * n2 * nspec * 4));
-  assign("lurec", L.take(rb * (size_t)lu_rec_elems(p.jd, p.kd, (int)rb) * nspec));
+  // the freestream correction belongs to a fixed grid
+  if (mixed && !mv) assign("sinf", L.take(rb * n2 * nspec * 4));
+  assign("lurec", L.take(rb * (size_t)lu_rec_elems(p.jd, p.kd) * nspec));
   return L.total;
 }
 
@@ -96,7 +112,33 @@ size_t solve_bytes(const ot2d_params& p, int precision) {
 
 void solve_destroy(DevSolve& d) {
   if (d.mem) cudaFree(d.mem);
+  if (d.motion) cudaFree(d.motion);
   d = DevSolve{};
+}
+
+int solve_motion_table(DevSolve& d, int nsteps, cudaStream_t st) {
+  if (d.P.iunst != 1 || nsteps < 1) return OT2D_OK;
+  const ot2d_params& p = d.P;
+  const double pi = 4.0 * std::atan(1.0);
+  std::vector<double> t(4 * (size_t)nsteps);
+  for (int istep = 1; istep <= nsteps; ++istep) {
+    // motion.f:579-583
+    const double dtheta = -(p.angmax * (std::cos(p.rotf * (double)istep * p.dt) -
+                                        std::cos(p.rotf * (double)(istep - 1) * p.dt)));
+    double* m = t.data() + 4 * (size_t)(istep - 1);
+    m[0] = std::sin(dtheta * pi / 180.);
+    m[1] = std::cos(dtheta * pi / 180.);
+    m[2] = std::sin(-1. * dtheta * pi / 180.);
+    m[3] = std::cos(-1. * dtheta * pi / 180.);
+  }
+  if (d.motion) cudaFree(d.motion);
+  d.motion = nullptr; d.nmotion = 0;
+  if (cudaMalloc(&d.motion, t.size() * sizeof(double)) != cudaSuccess) { d.motion = nullptr; return OT2D_ERR_NOMEM; }
+  if (cudaMemcpyAsync(d.motion, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return OT2D_ERR_CUDA;
+  d.nmotion = nsteps;
+  return OT2D_OK;
 }
 
 // Mixed path: the f32 residual (inviscid + viscous, no BCs) of the uniform
@@ -130,6 +172,13 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
   if (p.ilhs != 1 && (p.jd < 10 || p.kd < 10)) return OT2D_ERR_ARG;  // ADI lines of >= 8 points
   if (!p.lamin && p.iturb != 1 && p.iturb != 2) return OT2D_ERR_ARG;  // SA or k-omega SST
   if (p.itrans != 0) return OT2D_ERR_ARG;                            // no transition model
+  // steady, or time accurate with the pitching grid (Turns_overset.f:372-403:
+  // iunst 1, motiontype 1) at first to third order; Newton iterations only
+  // in time-accurate runs; not together with the time-spectral form
+  if (p.iunst != 0 && !(p.iunst == 1 && p.motiontype == 1 && !p.timespectral && p.ntac >= 1 && p.ntac <= 3 &&
+                        p.dt > 0 && p.h > 0))
+    return OT2D_ERR_ARG;
+  if (p.itnmax < 1 || (p.itnmax > 1 && p.iunst != 1)) return OT2D_ERR_ARG;
   d = DevSolve{};
   d.P = p; d.precision = precision; d.nspec = p.nspec;
   d.n2 = (size_t)p.jd * p.kd; d.nvert = (size_t)p.jmax * p.kmax; d.wstride = (d.n2 + 63) / 64 * 64;
@@ -173,6 +222,15 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     else if (n == "w") d.w = ptr;
     else if (n == "lurec") d.lurec = ptr;
     else if (n == "wd2") d.wd2 = (double*)ptr;
+    else if (n == "xc") d.xc = (double*)ptr;
+    else if (n == "yc") d.yc = (double*)ptr;
+    else if (n == "xold") d.xold = (double*)ptr;
+    else if (n == "yold") d.yold = (double*)ptr;
+    else if (n == "xole") d.xole = (double*)ptr;
+    else if (n == "yole") d.yole = (double*)ptr;
+    else if (n == "qtn") d.qtn = (double*)ptr;
+    else if (n == "qtnm1") d.qtnm1 = (double*)ptr;
+    else if (n == "qnewt") d.qnewt = (double*)ptr;
     else if (n == "sinf") d.sinf = ptr;
   }
   const bool mixed = precision == OT2D_FP32_MIXED;
@@ -231,6 +289,23 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     chk(cudaMemcpyAsync(d.Ds, Ds.data(), ns * ns * 8, cudaMemcpyHostToDevice, st));
   }
   if (d.wd2) chk(cudaMemcpyAsync(d.wd2, wd2.data(), qs * 8, cudaMemcpyHostToDevice, st));
+  if (d.xc) {
+    // time-accurate grid at rest before its first step (init.f:101-108):
+    // centres of instance 1, both previous vertex levels = the grid, no
+    // grid speed; face speeds and stqol levels are set by the first step
+    chk(cudaMemcpyAsync(d.xc, x.data(), n2 * 8, cudaMemcpyHostToDevice, st));
+    chk(cudaMemcpyAsync(d.yc, y.data(), n2 * 8, cudaMemcpyHostToDevice, st));
+    for (double* dst : {d.xold, d.xole}) chk(cudaMemcpyAsync(dst, xv.data(), nv * 8, cudaMemcpyHostToDevice, st));
+    for (double* dst : {d.yold, d.yole}) chk(cudaMemcpyAsync(dst, yv.data(), nv * 8, cudaMemcpyHostToDevice, st));
+    chk(cudaMemsetAsync(d.ug64, 0, qs * 8, st));
+    chk(cudaMemsetAsync(d.vg64, 0, qs * 8, st));
+    const size_t rb = mixed ? sizeof(float) : sizeof(double);
+    if (mixed) { chk(cudaMemsetAsync(d.ug, 0, qs * rb, st)); chk(cudaMemsetAsync(d.vg, 0, qs * rb, st)); }
+    chk(cudaMemsetAsync(d.ftj, 0, qs * rb, st));
+    chk(cudaMemsetAsync(d.gtj, 0, qs * rb, st));
+    for (double* a : {d.qtn, d.qtnm1, d.qnewt})
+      if (a) chk(cudaMemsetAsync(a, 0, qs * (size_t)p.nv * 8, st));
+  }
   chk(cudaMemcpyAsync(d.xv, xv.data(), xv.size() * 8, cudaMemcpyHostToDevice, st));
   chk(cudaMemcpyAsync(d.yv, yv.data(), yv.size() * 8, cudaMemcpyHostToDevice, st));
   std::vector<int32_t> ib(qs, 1);
@@ -251,7 +326,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     chk(upload_as<float>(d.sn, sn.data(), qs, st, t14));
     chk(cudaMemsetAsync(d.turmu, 0, qs * sizeof(float), st));
     chk(cudaStreamSynchronize(st));
-    if (!bad && freestream_residual_f32(d, st) != OT2D_OK) bad = true;
+    if (!bad && d.sinf && freestream_residual_f32(d, st) != OT2D_OK) bad = true;
   } else {
     chk(cudaMemcpyAsync(d.fxa, fxa.data(), qs * 8, cudaMemcpyHostToDevice, st));
     chk(cudaMemcpyAsync(d.fya, fya.data(), qs * 8, cudaMemcpyHostToDevice, st));
@@ -282,8 +357,9 @@ Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
   S.q = R_(d.q); S.q64 = D_(d.q64); S.s = R_(d.s);
   S.xx = R_(d.xx); S.xy = R_(d.xy); S.yx = R_(d.yx); S.yy = R_(d.yy);
   S.fxa = R_(d.fxa); S.fya = R_(d.fya); S.gxa = R_(d.gxa); S.gya = R_(d.gya);
-  S.ftj = p.timespectral ? R_(d.ftj) : nullptr; S.gtj = p.timespectral ? R_(d.gtj) : nullptr;
-  S.ug = p.timespectral ? R_(d.ug) : nullptr; S.vg = p.timespectral ? R_(d.vg) : nullptr;
+  const bool gs = p.timespectral || d.xc;
+  S.ftj = gs ? R_(d.ftj) : nullptr; S.gtj = gs ? R_(d.gtj) : nullptr;
+  S.ug = gs ? R_(d.ug) : nullptr; S.vg = gs ? R_(d.vg) : nullptr;
   S.tscale = R_(d.tscale); S.bt = R_(d.bt); S.turmu = R_(d.turmu);
   S.iblank = d.iblank + o;
   S.sn = R_(d.sn);
@@ -292,11 +368,19 @@ Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
   S.sinf = R_(d.sinf);
   slice_consts(S, p);
   S.wstride = (int64_t)d.wstride;
-  S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd, (int)sizeof(R));
+  S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
   S.red = red; S.ist = ist;
   S.Ds = p.timespectral ? d.Ds : nullptr;
   S.xx64 = D_(d.xx64); S.xy64 = D_(d.xy64); S.yx64 = D_(d.yx64); S.yy64 = D_(d.yy64);
-  S.ug64 = p.timespectral ? D_(d.ug64) : nullptr; S.vg64 = p.timespectral ? D_(d.vg64) : nullptr;
+  S.ug64 = gs ? D_(d.ug64) : nullptr; S.vg64 = gs ? D_(d.vg64) : nullptr;
+  const size_t ov = (size_t)(nsp - 1) * d.nvert;
+  S.xv = d.xv + ov; S.yv = d.yv + ov;
+  if (d.xc) {
+    S.xc = D_(d.xc); S.yc = D_(d.yc);
+    S.xold = d.xold + ov; S.yold = d.yold + ov; S.xole = d.xole + ov; S.yole = d.yole + ov;
+    S.qtn = D_(d.qtn); S.qtnm1 = D_(d.qtnm1); S.qnewt = D_(d.qnewt);
+    S.motion = d.motion; S.nmotion = d.nmotion;
+  }
   return S;
 }
 template Slice<double> make_slice<double>(const DevSolve&, int, double*, int32_t*);
@@ -308,8 +392,9 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   // six prefix tables of n+1 entries: cell blocks, k-lines, j-lines, LU
   // record blocks, 32-line groups, residual tiles
   std::vector<int32_t> idx(6 * (n + 1));
-  int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1, maxkd = 1;
+  int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1, maxkd = 1, moving = 0;
   for (int i = 0; i < n; ++i) {
+    if (sl[i].xc) moving = 1;
     idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl; idx[3 * (n + 1) + i] = lub;
     idx[4 * (n + 1) + i] = grp; idx[5 * (n + 1) + i] = tiles;
     const int jd = sl[i].jd, kd = sl[i].kd;
@@ -343,6 +428,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
     return OT2D_ERR_CUDA;
   if (cudaStreamSynchronize(st) != cudaSuccess) return OT2D_ERR_CUDA;
   b.nslice = n;
+  b.moving = moving;
   b.cell_blocks = cells;
   b.max_lu_warps = maxw;
   b.max_wall = maxwall;

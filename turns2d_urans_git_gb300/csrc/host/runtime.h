@@ -12,10 +12,13 @@
 
 namespace ot2d {
 
-// reduction / status record of one slice (red: 8 doubles, ist: 4 ints)
-//  red: rsum, resrho, resmax, resmax key, rsum at it 1, rsum now, peak rsum, 10^-orders
-//  ist: istep0, istep, status bits (1 norm, 2 monitor), iteration of convergence
-constexpr int RED_N = 8, IST_N = 4;
+// reduction / status record of one slice (red: 9 doubles, ist: 6 ints)
+//  red: rsum, resrho, resmax, resmax key, rsum at it 1, rsum now, peak rsum, 10^-orders,
+//       1/(oat*h) of the physical-time term (time.f:195-200)
+//  ist: istep0, istep (physical steps), status bits (1 norm, 2 monitor, 4 sweep
+//       timeout, 8 no motion entry, 16 folded cell), iteration of convergence,
+//       Newton iteration within the physical step (1..itnmax), spare
+constexpr int RED_N = 9, IST_N = 6;
 
 // All device arrays of one solve (every time instance), carved from one
 // allocation.  FP64 arrays always exist; the compute-type arrays alias the
@@ -37,6 +40,12 @@ struct DevSolve {
   void *ug = nullptr, *vg = nullptr, *tscale = nullptr, *bt = nullptr, *turmu = nullptr, *sn = nullptr, *w = nullptr;
   void* lurec = nullptr;
   double* wd2 = nullptr;   // SST wall term (k-omega SST instances only)
+  // time-accurate moving grid (iunst = 1): centres, previous vertex levels,
+  // stqol levels (itnmax > 1) and the per-step pitch table (own allocation)
+  double *xc = nullptr, *yc = nullptr, *xold = nullptr, *yold = nullptr, *xole = nullptr, *yole = nullptr;
+  double *qtn = nullptr, *qtnm1 = nullptr, *qnewt = nullptr;
+  double* motion = nullptr;
+  int nmotion = 0;
   void* sinf = nullptr;    // f32 freestream residual (mixed path only)
   int nscratch = 0;        // scratch arrays per time instance
 };
@@ -49,6 +58,9 @@ size_t solve_bytes(const ot2d_params& p, int precision);
 int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double* xv1, const double* yv1,
                  cudaStream_t st);
 void solve_destroy(DevSolve& d);
+// Per physical step 1..nsteps of a pitching solve: sin and cos of the pitch
+// increment and of its negative (motion.f:576-583), uploaded to d.motion.
+int solve_motion_table(DevSolve& d, int nsteps, cudaStream_t st);
 
 // Slice view of time instance nsp (1-based) of a solve; red/ist point into
 // the caller's status table.

@@ -27,7 +27,8 @@ struct Rec {
   int id = -1;
   std::vector<int> slots;
   double orders = 10.0;
-  int max_iters = 0;
+  int max_iters = 0;        // iterations (steady) or physical time steps (time accurate)
+  long launched = 0;        // iterations run since admission
   bool live = false;
   ot2d_result res{};
   std::vector<double> qkeep;
@@ -38,6 +39,13 @@ struct Rec {
   std::string store_dir;   // ot2d_solver_store_on_retire: written when retired
 };
 constexpr int FORCE_WIN = 8;
+
+// iterations an instance runs before it retires: max_iters, or max_iters
+// physical steps of itnmax Newton iterations each
+long iter_cap(const Rec& r) {
+  const int itn = r.d.P.itnmax > 1 ? r.d.P.itnmax : 1;
+  return (long)r.max_iters * itn;
+}
 
 double now_s() {
   using namespace std::chrono;
@@ -221,7 +229,8 @@ int profile_t(ot2d_solver* s, DevBatch<R>& B, int iters, double* ms) {
     cudaError_t e = cudaSuccess;
     auto rec = [&](int i) { cudaEventRecord(ev[i], s->st); };
     rec(0);
-    e = launch_time_step<R>(B.d_sl, B.b, s->st); rec(1);
+    e = launch_iter_begin<R>(B.d_sl, B.b, s->st);
+    if (!e) e = launch_time_step<R>(B.d_sl, B.b, s->st); rec(1);
     if (!e) e = launch_bc<R>(B.d_sl, B.b, 1, s->st); rec(2);
     if (!e) e = launch_residual<R>(B.d_sl, B.b, visc, s->st); rec(3);
     if (!e) e = launch_rbc<R>(B.d_sl, B.b, s->st); rec(4);
@@ -265,7 +274,13 @@ int store_rec(ot2d_solver* s, Rec& r, const std::string& dir) {
   for (size_t k = 0; k < ns; ++k)
     cell_centres(p, xv.data() + k * nv, yv.data() + k * nv, x.data() + k * n2, y.data() + k * n2);
   float* qc = s->precision == OT2D_FP32_MIXED ? (float*)r.d.q : nullptr;
-  return write_solution(dir, p, r.d.q64, qc, x.data(), y.data(), ib.data(), ist[0], s->st);
+  // totime as the driver keeps it: 0 at the start of the run, + dt per
+  // physical step of a time-accurate run (Turns_overset.f:359, :365)
+  ot2d_params pw = p;
+  pw.totime = 0.0;
+  if (p.iunst != 0)
+    for (int i = 0; i < ist[1]; ++i) pw.totime = pw.totime + p.dt;
+  return write_solution(dir, pw, r.d.q64, qc, x.data(), y.data(), ib.data(), ist[0], s->st);
 }
 
 int check(ot2d_solver* s) {
@@ -281,7 +296,9 @@ int check(ot2d_solver* s) {
     for (int sl : r.slots) {
       const int32_t* ist = s->h_ist + (size_t)IST_N * sl;
       if (ist[2] & 1) status = OT2D_ERR_NORM;
-      else if ((ist[2] & 2) && !status) status = OT2D_ERR_MONITOR;
+      else if ((ist[2] & 18) && !status) status = OT2D_ERR_MONITOR;   // bad state / folded cell
+      else if ((ist[2] & 4) && !status) status = OT2D_ERR_TIMEOUT;    // a sweep wait gave up
+      else if ((ist[2] & 8) && !status) status = OT2D_ERR_ARG;        // step beyond the motion table
       if (ist[3] == 0) conv = false;
       conv_it = std::max(conv_it, (int)ist[3]);
       its = ist[1];
@@ -292,7 +309,7 @@ int check(ot2d_solver* s) {
     r.res.iterations = conv ? conv_it : its;
     r.res.status = status;
     r.res.converged = (conv && !status) ? 1 : 0;
-    if (status || conv || its >= r.max_iters) done.push_back(id);
+    if (status || conv || r.launched >= iter_cap(r)) done.push_back(id);
   }
   if (s->force_dcl > 0 || s->force_dcd > 0) {
     // forces of the instances still running; converged once CL and CD stayed
@@ -401,6 +418,13 @@ int ot2d_solver_add(ot2d_solver* s, const ot2d_params* p, const double* xv, cons
   Rec r;
   int e = solve_create(r.d, *p, s->precision, xv, yv, s->st);
   if (e) return -e;
+  if (p->iunst == 1) {
+    // time accurate: max_iters physical steps, the pitch table for them,
+    // no residual convergence test
+    e = solve_motion_table(r.d, max_iters, s->st);
+    if (e) { solve_destroy(r.d); return -e; }
+    orders = 0.0;
+  }
   r.id = s->next_id++;
   r.orders = orders; r.max_iters = max_iters; r.live = true;
   r.res.id = r.id;
@@ -431,11 +455,21 @@ int ot2d_solver_iterate(ot2d_solver* s, int32_t iters) {
     if (s->dirty) { int e = rebuild(s); if (e) return e; }
     if (s->live.empty()) break;
     int chunk = std::min(s->check_every - s->since_check, iters - done);
+    // no instance runs past its cap: stop the chunk at the first cap
+    long rem = chunk;
+    for (int id : s->live) rem = std::min(rem, iter_cap(s->recs[id]) - s->recs[id].launched);
+    chunk = (int)std::max(1L, rem);
     for (int i = 0; i < chunk; ++i)
       if (cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+    bool capped = false;
+    for (int id : s->live) {
+      Rec& r = s->recs[id];
+      r.launched += chunk;
+      if (r.launched >= iter_cap(r)) capped = true;
+    }
     s->since_check += chunk;
     done += chunk;
-    if (s->since_check >= s->check_every) { int e = check(s); if (e) return e; }
+    if (s->since_check >= s->check_every || capped) { int e = check(s); if (e) return e; }
   }
   return OT2D_OK;
 }
@@ -529,7 +563,12 @@ int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, doub
           cudaEventRecord(s->ev_d2h[i], s->st_d2h) != cudaSuccess)
         err = OT2D_ERR_CUDA;
     }
-    if (!err && ++s->since_check >= s->check_every) {
+    bool capped = false;
+    for (int id : s->live) {
+      Rec& r = s->recs[id];
+      if (++r.launched >= iter_cap(r)) capped = true;
+    }
+    if (!err && (++s->since_check >= s->check_every || capped)) {
       // the status read must not see the next iteration's uploads in flight
       if (cudaStreamSynchronize(s->st_d2h) != cudaSuccess) err = OT2D_ERR_CUDA;
       else err = check(s);
@@ -574,15 +613,14 @@ int ot2d_solver_add_restart(ot2d_solver* s, const ot2d_params* p, const double* 
   float* qc = s->precision == OT2D_FP32_MIXED ? (float*)r.d.q : nullptr;
   int e = read_restart(dir, r.d.P, r.d.q64, qc, &totime, &istep0, s->st);
   if (!e) {
-    // init.f:165 (istep0) and io.f:400 (totime) of the restart file; the
-    // instance runs as a reference restart does, with iread = 1 (the wall
-    // start-up ramps of bc.f / komegasst.f are then off)
-    r.d.P.totime = totime;
+    // init.f:165 (istep0) of the restart file; the instance runs as a
+    // reference restart does, with iread = 1 (the wall start-up ramps of
+    // bc.f / komegasst.f are then off).  The file's totime is not kept: the
+    // driver restarts it at 0 (Turns_overset.f:359).
+    (void)totime;
     if (r.d.P.iread < 1) r.d.P.iread = 1;
     const int32_t i0 = istep0;
-    if (cudaMemcpyAsync((char*)r.d.dP + offsetof(ot2d_params, totime), &r.d.P.totime, sizeof(double),
-                        cudaMemcpyHostToDevice, s->st) != cudaSuccess ||
-        cudaMemcpyAsync((char*)r.d.dP + offsetof(ot2d_params, iread), &r.d.P.iread, sizeof(int32_t),
+    if (cudaMemcpyAsync((char*)r.d.dP + offsetof(ot2d_params, iread), &r.d.P.iread, sizeof(int32_t),
                         cudaMemcpyHostToDevice, s->st) != cudaSuccess)
       e = OT2D_ERR_CUDA;
     for (int sl : r.slots)

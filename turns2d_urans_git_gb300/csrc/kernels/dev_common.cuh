@@ -39,10 +39,17 @@ struct Slice {
   R* lurec;                          // LU-SGS sweep records (skewed bands)
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)
   double* red;                       // per-slice reduction output
-  int32_t* ist;                      // per-slice counters: istep0, istep, status bits
+  int32_t* ist;                      // per-slice counters: istep0, istep, status bits, convergence
+                                     // iteration, Newton iteration of the physical step
   const double* Ds;                  // time-spectral operator Ds(nspec,nspec)
   // FP64 geometry kept for FP64-only work (forces, BC metrics in mixed mode)
   const double *xx64, *xy64, *yx64, *yy64, *ug64, *vg64;
+  // time-accurate moving grid (iunst = 1, motiontype = 1); null otherwise
+  double *xc, *yc;                        // cell centres, rotated every physical step
+  double *xv, *yv, *xold, *yold, *xole, *yole;   // vertices now and at the two previous levels
+  double *qtn, *qtnm1, *qnewt;            // stqol levels (itnmax > 1), (jd,kd,nspec,nv)
+  const double* motion;                   // per physical step: sin, cos of the pitch increment and of its negative
+  int32_t nmotion;                        // physical steps in the table
 };
 
 // Fill the residual constants of a slice from its parameters (host side;

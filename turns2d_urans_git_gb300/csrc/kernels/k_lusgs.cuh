@@ -29,17 +29,17 @@
 namespace ot2d {
 
 constexpr int LU_NF = 24;                 // fields per cell record
-// A (band, step) chunk holds the records of the band's 32 lanes one after
-// another (lane-major): lane l's 24 fields are contiguous, so a lane reads
-// its record with 16-byte shared-memory loads.  Each record is padded to LS
-// elements so that the eight lanes of one load phase hit disjoint banks
-// (f32: 112-byte stride, f64: 208-byte stride).
+// A (band, step) chunk holds the records of the band's 32 lanes as
+// 16-byte field groups interleaved over the lanes: [group][lane][GW fields]
+// with GW = 16 bytes of fields (4 f32 or 2 f64).  A lane reads four
+// consecutive fields with one (f32) or two (f64) 16-byte shared loads; the
+// eight lanes of a load phase read 128 contiguous bytes (no bank conflict)
+// and a warp writes a group of a chunk as 512 contiguous bytes.
 template <class R>
 struct LuLay {
-  static constexpr int LS = sizeof(R) == 4 ? 28 : 26;   // elements per lane record
-  static constexpr int CH = 32 * LS;                    // elements per chunk
+  static constexpr int GW = 16 / (int)sizeof(R);   // fields per 16-byte group
+  static constexpr int CH = 32 * LU_NF;            // elements per chunk
 };
-
 // record fields
 enum {
   LF_S = 0,    // 0..3: residual (forward input, then forward result)
@@ -48,36 +48,40 @@ enum {
   LF_FCX = 16, LF_FSX = 17, LF_FCY = 18, LF_FSY = 19,  // forward chk / spec (xi, eta)
   LF_BCX = 20, LF_BSX = 21, LF_BCY = 22, LF_BSY = 23   // backward chk / spec
 };
+// element offset of field f of lane l within a chunk
+template <class R>
+__host__ __device__ __forceinline__ int lu_idx(int f, int l) {
+  constexpr int GW = LuLay<R>::GW;
+  return ((f / GW) * 32 + l) * GW + (f % GW);
+}
 
 __host__ __device__ __forceinline__ int lu_nrow(int kd) { return kd - 2; }
 __host__ __device__ __forceinline__ int lu_ncol(int jd) { return jd - 2; }
 __host__ __device__ __forceinline__ int lu_nband(int kd) { return (kd - 2 + 31) / 32; }
 __host__ __device__ __forceinline__ int lu_nstep(int jd) { return jd - 2 + 31; }
-// elements of one slice's record (element size esize bytes): chunks + 4
-// halo-contribution arrays
-__host__ __device__ __forceinline__ int64_t lu_rec_elems(int jd, int kd, int esize) {
-  const int ch = esize == 4 ? LuLay<float>::CH : LuLay<double>::CH;
-  return (int64_t)lu_nband(kd) * lu_nstep(jd) * ch + 8 * (int64_t)(lu_nrow(kd) + lu_ncol(jd)) + 64;
+// elements of one slice's record: chunks + 4 halo-contribution arrays
+__host__ __device__ __forceinline__ int64_t lu_rec_elems(int jd, int kd) {
+  return (int64_t)lu_nband(kd) * lu_nstep(jd) * (32 * LU_NF) + 8 * (int64_t)(lu_nrow(kd) + lu_ncol(jd)) + 64;
 }
 
-// four consecutive record fields (16-byte aligned) as one or two vector
-// accesses
+// fields f..f+3 of lane l of a chunk (f a multiple of 4) as 16-byte accesses
 template <class R>
 struct Lu4 { R x, y, z, w; };
-__device__ __forceinline__ Lu4<float> lu_ld4(const float* p) {
-  const float4 v = *reinterpret_cast<const float4*>(p);
+__device__ __forceinline__ Lu4<float> lu_ld4(const float* ch, int f, int l) {
+  const float4 v = *reinterpret_cast<const float4*>(ch + lu_idx<float>(f, l));
   return {v.x, v.y, v.z, v.w};
 }
-__device__ __forceinline__ Lu4<double> lu_ld4(const double* p) {
-  const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+__device__ __forceinline__ Lu4<double> lu_ld4(const double* ch, int f, int l) {
+  const double2 a = *reinterpret_cast<const double2*>(ch + lu_idx<double>(f, l));
+  const double2 b = *reinterpret_cast<const double2*>(ch + lu_idx<double>(f + 2, l));
   return {a.x, a.y, b.x, b.y};
 }
-__device__ __forceinline__ void lu_st4(float* p, float a, float b, float c, float d) {
-  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+__device__ __forceinline__ void lu_st4(float* ch, int f, int l, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(ch + lu_idx<float>(f, l)) = make_float4(a, b, c, d);
 }
-__device__ __forceinline__ void lu_st4(double* p, double a, double b, double c, double d) {
-  *reinterpret_cast<double2*>(p) = make_double2(a, b);
-  *reinterpret_cast<double2*>(p + 2) = make_double2(c, d);
+__device__ __forceinline__ void lu_st4(double* ch, int f, int l, double a, double b, double c, double d) {
+  *reinterpret_cast<double2*>(ch + lu_idx<double>(f, l)) = make_double2(a, b);
+  *reinterpret_cast<double2*>(ch + lu_idx<double>(f + 2, l)) = make_double2(c, d);
 }
 
 template <class R>
@@ -151,15 +155,17 @@ __device__ __forceinline__ void lu_contrib(const LuCell<R>& c, const R* s, R gm1
 }
 
 // ---- kernel 1: records of the interior cells (one thread per (band, step, lane))
+// The record of lane l of chunk (band, t), written as six 16-byte field
+// groups (coalesced over the warp).
 template <class R>
 __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_params& p, int band, int t, int l, int scale) {
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nst = lu_nstep(S.jd);
   const int r = 32 * band + l, c = t - l;
-  R* rr = S.lurec + ((int64_t)band * nst + t) * LuLay<R>::CH + l * LuLay<R>::LS;
+  R* ch = S.lurec + ((int64_t)band * nst + t) * LuLay<R>::CH;
   if (r >= nrow || c < 0 || c >= ncol) {
     const R z = (R)0;
 #pragma unroll
-    for (int f = 0; f < LU_NF; f += 4) lu_st4(rr + f, z, z, z, z);
+    for (int f = 0; f < LU_NF; f += 4) lu_st4(ch, f, l, z, z, z, z);
     return;
   }
   const int j = p.jbeg + c, k = p.kbeg + r;
@@ -173,17 +179,17 @@ __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_param
     R v = S.s[n * S.qs + o];
     sv[n] = scale ? v * ts : v;
   }
-  lu_st4(rr + LF_S, sv[0], sv[1], sv[2], sv[3]);
-  lu_st4(rr + LF_SV, ts * (R)0.5, cl.d, cl.uu, cl.vv);
-  lu_st4(rr + LF_UV2, cl.uv2, cl.ge, cl.ri1, cl.ri2);
-  lu_st4(rr + LF_RK1, cl.rk1, cl.rk2, cl.qx, cl.qy);
+  lu_st4(ch, LF_S, l, sv[0], sv[1], sv[2], sv[3]);
+  lu_st4(ch, LF_SV, l, ts * (R)0.5, cl.d, cl.uu, cl.vv);
+  lu_st4(ch, LF_UV2, l, cl.uv2, cl.ge, cl.ri1, cl.ri2);
+  lu_st4(ch, LF_RK1, l, cl.rk1, cl.rk2, cl.qx, cl.qy);
   R a, b, a2, b2;
   lu_chkspec<R, true, true>(cl, eps2, a, b);
   lu_chkspec<R, false, true>(cl, eps2, a2, b2);
-  lu_st4(rr + LF_FCX, a, b, a2, b2);
+  lu_st4(ch, LF_FCX, l, a, b, a2, b2);
   lu_chkspec<R, true, false>(cl, eps2, a, b);
   lu_chkspec<R, false, false>(cl, eps2, a2, b2);
-  lu_st4(rr + LF_BCX, a, b, a2, b2);
+  lu_st4(ch, LF_BCX, l, a, b, a2, b2);
 }
 
 // halo-contribution arrays after the chunks: A forward [nrow][4], A backward,
@@ -331,7 +337,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   const R gm1 = (R)p.gm1;
   R* rings = (R*)smem;
-  constexpr int CH = LuLay<R>::CH, LS = LuLay<R>::LS;
+  constexpr int CH = LuLay<R>::CH;
   uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * 2 * G * CH * sizeof(R));
   R* xrings = (R*)(bars + (size_t)nwarp * 2);
   int* prog = (int*)(xrings + (size_t)nwarp * LU_XB * 4);
@@ -393,9 +399,9 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
       const int tl = g * G + u;
       // this lane's record: residual, (tscale/2, d, u, v), (uv2, ge, xi
       // metrics), (eta metrics, qx, qy), this sweep's (chk, spec) pairs
-      const R* rr = gring + (FWD ? u : gs - 1 - u) * CH + l * LS;
-      const Lu4<R> r0 = lu_ld4(rr + LF_S), r1 = lu_ld4(rr + LF_SV), r2 = lu_ld4(rr + LF_UV2),
-                   r3 = lu_ld4(rr + LF_RK1), r4 = lu_ld4(rr + (FWD ? LF_FCX : LF_BCX));
+      const R* ch = gring + (FWD ? u : gs - 1 - u) * CH;
+      const Lu4<R> r0 = lu_ld4(ch, LF_S, l), r1 = lu_ld4(ch, LF_SV, l), r2 = lu_ld4(ch, LF_UV2, l),
+                   r3 = lu_ld4(ch, LF_RK1, l), r4 = lu_ld4(ch, FWD ? LF_FCX : LF_BCX, l);
       R bin[4];
 #pragma unroll
       for (int n = 0; n < 4; ++n)
@@ -428,7 +434,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
         for (int n = 0; n < 4; ++n)
           sn[n] = FWD ? (st[n] + sv * (aprev[n] + bin[n])) * di : st[n] - sv * (aprev[n] + bin[n]) * di;
         if (FWD) {
-          lu_st4(recw + (int64_t)tl * CH + l * LS + LF_S, sn[0], sn[1], sn[2], sn[3]);
+          lu_st4(recw + (int64_t)tl * CH, LF_S, l, sn[0], sn[1], sn[2], sn[3]);
         } else {
 #pragma unroll
           for (int n = 0; n < 4; ++n) srow[n * S.qs + c] = sn[n];

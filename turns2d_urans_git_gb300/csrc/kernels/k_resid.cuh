@@ -334,6 +334,18 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
 #pragma unroll
       for (int v = 0; v < 4; ++v) s[v] = s[v] - (G[v * ((RT_TK + 1) * RT_TJ) + RT_TJ] - G[v * ((RT_TK + 1) * RT_TJ)]);
     }
+    if (S.qnewt) {
+      // newton (time.f:195-206): the physical-time term, added between the
+      // inviscid and the viscous parts as compute_residual does
+      // (step.f:274-285); 1/(oat*h) of this step in red[8]
+      const double tac = S.red[8];
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        if (n >= nv) continue;
+        const int64_t on = (int64_t)n * S.qs + o;
+        s[n] = s[n] - (R)((S.q64[on] - S.qnewt[on]) * tac);
+      }
+    }
     if (visc) {
       // VE row of cell k is kk+2; VX column of cell j is jj+2
       const R* VE = sm.VE + (kk + 2) * RT_TJ + jj;

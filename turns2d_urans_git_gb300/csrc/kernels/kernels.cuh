@@ -10,6 +10,7 @@
 #include "k_sst.cuh"
 #include "k_adi.cuh"
 #include "k_misc.cuh"
+#include "k_motion.cuh"
 #include "launch.h"
 #include "k_resid.cuh"
 
@@ -40,21 +41,68 @@ __global__ void __launch_bounds__(CELL_BS) k_time_step(const Slice<R>* __restric
   OT2D_CELL_MAP();
   if (!inside) return;
   const ot2d_params& p = *S.P;
-  int istep = S.ist ? S.ist[1] + 1 : p.istep;
+  int istep = S.ist ? S.ist[1] : p.istep;   // advanced by k_iter_begin
   R oat = (R)1.0;
   if (p.ntac >= 2 && istep > 1) oat = (R)(2. / 3.);
   if (p.ntac == 3 && istep > 2) oat = (R)(6. / 11.);
   time_step_cell(S, j, k, oat);
 }
 
+// Start of a solver iteration (one thread per slice): the step counters of
+// Turns_overset.f:362-364 -- advanced once per physical time step, i.e. at
+// the first of the itnmax Newton iterations (:472-474) -- and the
+// physical-time factor 1/(oat*h) of newton (time.f:195-200) in red[8].
+template <class R>
+__global__ void k_iter_begin(const Slice<R>* __restrict__ sl, int nslice) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nslice) return;
+  const Slice<R>& S = sl[i];
+  if (!S.ist) return;
+  const ot2d_params& p = *S.P;
+  int itn = 1;
+  if (p.itnmax > 1) itn = S.ist[4] % p.itnmax + 1;
+  S.ist[4] = itn;
+  if (itn == 1) { S.ist[0] += 1; S.ist[1] += 1; }
+  const int istep = S.ist[1];
+  double oat = 1.0;
+  if (p.ntac >= 2 && istep > 1) oat = 2. / 3.;
+  if (p.ntac == 3 && istep > 2) oat = 6. / 11.;
+  if (S.red) S.red[8] = 1. / (oat * p.h);
+}
+
+// Moving slices at the start of a physical step: pitch + stqol (one thread
+// per cell / vertex), then metrics, faces and wall distances (one thread per
+// cell), then the metric halo and the SST wall term (one CTA per slice).
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_mv_pitch(const Slice<R>* __restrict__ sl,
+                                                      const int32_t* __restrict__ first, int nslice) {
+  OT2D_CELL_MAP();
+  (void)j; (void)k;
+  if (!inside || !mv_new_step(S)) return;
+  mv_pitch_cell(S, cid);
+}
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_mv_geom(const Slice<R>* __restrict__ sl,
+                                                     const int32_t* __restrict__ first, int nslice) {
+  OT2D_CELL_MAP();
+  if (!inside || !mv_new_step(S)) return;
+  mv_geom_cell(S, j, k);
+}
+template <class R>
+__global__ void k_mv_halo(const Slice<R>* __restrict__ sl) {
+  const Slice<R>& S = sl[blockIdx.x];
+  if (!mv_new_step(S)) return;   // uniform over the CTA
+  const ot2d_params& p = *S.P;
+  if (!p.lamin && p.iturb == 2 && S.wd2)
+    for (int ib = 0; ib < p.nbc; ++ib)
+      if (p.ibtyp[ib] == 5)
+        for (int i = threadIdx.x; i < S.jd + S.kd; i += blockDim.x) mv_sst_wall(S, ib, i);
+  mv_metric_halo(S);
+}
+
 template <class R>
 __global__ void k_bc(const Slice<R>* __restrict__ sl, int advance) {
   const Slice<R>& S = sl[blockIdx.x];
-  if (S.ist && advance) {
-    __syncthreads();
-    if (threadIdx.x == 0) { S.ist[0] += 1; S.ist[1] += 1; }
-    __syncthreads();
-  }
   const int istep0 = S.ist ? S.ist[0] : S.P->istep0;
   bc_slice(S, nullptr, istep0);
   shadow_ring(S, 1, 4);

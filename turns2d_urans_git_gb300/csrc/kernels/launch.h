@@ -19,6 +19,7 @@ constexpr int ADI_NSCRATCH = 25;
 
 struct Batch {
   int nslice = 0;          // slices in the batch
+  int moving = 0;          // some slice is time accurate on a pitching grid
   int cell_blocks = 0;     // blocks of the cell-parallel kernels
   int max_lu_warps = 1;    // warps per CTA of the LU-SGS kernel
   int max_wall = 1;        // most wall cells of one slice (force kernel smem); also max jd
@@ -53,6 +54,10 @@ struct Branch {
 cudaError_t branch_of_device(Branch*& out);
 
 // Individual phases (the drop-in routines call these on a batch of one).
+// Start of an iteration: step counters and Newton iteration counter of every
+// slice, then (moving slices starting a physical step) pitch, stqol, metrics,
+// face speeds and wall distances.
+template <class R> cudaError_t launch_iter_begin(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st);
 template <class R> cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st);

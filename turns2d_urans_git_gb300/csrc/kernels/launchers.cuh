@@ -5,6 +5,16 @@
 namespace ot2d {
 
 template <class R>
+cudaError_t launch_iter_begin(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_iter_begin<R><<<(b.nslice + 127) / 128, 128, 0, st>>>(d_sl, b.nslice);
+  if (b.moving) {
+    k_mv_pitch<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+    k_mv_geom<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+    k_mv_halo<R><<<b.nslice, 256, 0, st>>>(d_sl);
+  }
+  return cudaGetLastError();
+}
+template <class R>
 cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_time_step<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
@@ -193,6 +203,7 @@ cudaError_t launch_forces(const Slice<R>* d_sl, const Batch& b, const double* co
 template <class R>
 cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st) {
   cudaError_t e;
+  if ((e = launch_iter_begin(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_time_step(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_bc(d_sl, b, 1, st)) != cudaSuccess) return e;
   if ((e = launch_residual(d_sl, b, viscous, st)) != cudaSuccess) return e;
@@ -226,6 +237,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
 #define OT2D_INSTANTIATE(R)                                                                              \
   template cudaError_t launch_iteration<R>(const Slice<R>*, const Batch&, int, int, int, cudaStream_t); \
   template cudaError_t launch_time_step<R>(const Slice<R>*, const Batch&, cudaStream_t);                \
+  template cudaError_t launch_iter_begin<R>(const Slice<R>*, const Batch&, cudaStream_t);               \
   template cudaError_t launch_bc<R>(const Slice<R>*, const Batch&, int, cudaStream_t);                  \
   template cudaError_t launch_residual<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
   template cudaError_t launch_rbc<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
