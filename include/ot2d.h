@@ -119,7 +119,9 @@ int ot2d_komegasst(double* q, double* s, double* turmu, double* x, double* y, do
 /* src/sources.f:2 (q, s: full (jd,kd,nspec,nv) arrays) */
 int ot2d_timespectralrhs(double* q, double* s, double* Ds, int32_t* jd, int32_t* kd, int32_t* nsp);
 /* src/step.f:2-7 (full arrays over nspec; norms of the last call via
- * ot2d_last_norms) */
+ * ot2d_last_norms).  Time accurate (iunst = 1): xold..yole give the
+ * swept-area face speeds and ug, vg the cell grid speeds; itnmax > 1: qnewt
+ * gives newton's physical-time term (time.f:178-210). */
 int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, double* x, double* y, double* xv,
               double* yv, int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
               double* ugv, double* vgv, double* xold, double* yold, double* xole, double* yole, double* turmu,
@@ -132,6 +134,14 @@ int ot2d_monitor(int32_t* mstop, double* q, int32_t* jd, int32_t* kd);
 int ot2d_force2d(int32_t* jd, int32_t* kd, double* x, double* y, double* xv, double* yv, double* q, double* xx,
                  double* xy, double* yx, double* yy, double* cfx, double* cfy, double* cm0, double* cpower,
                  int32_t* nsp);
+/* src/motion.f:546-632 (pitch, motiontype 1): rotates x, y (cell centres)
+ * and xv, yv by step istep's increment, shifts xold/xole, sets ug, vg; the
+ * step's sines and cosines are taken on the host, the rest runs on the
+ * device */
+int ot2d_pitch(int32_t* init, double* x, double* y, double* xv, double* yv, double* xold, double* yold, double* xole,
+               double* yole, double* ug, double* vg, int32_t* jd, int32_t* kd);
+/* src/time.f:110-175 (q(jd,kd,nspec,nq); qtn, qtnm1, qnewt (jd,kd,nspec,nv)) */
+int ot2d_stqol(double* q, double* qtn, double* qtnm1, double* qnewt, int32_t* jd, int32_t* kd);
 /* src/setup.f:111 and src/setup.f:440 (q: one instance, only q(:,:,nq) is written) */
 int ot2d_find_cellcenter(double* x, double* y, double* xv, double* yv, int32_t* jd, int32_t* kd, int32_t* im);
 int ot2d_metfv(double* q, double* x, double* y, double* xv, double* yv, double* xx, double* xy, double* yx,

@@ -86,3 +86,55 @@ def test_steady_instance_stops_exactly_at_its_cap():
     sv.close()
     assert r.iterations == 30
     assert relerr(q, q_o) <= 1e-12
+
+
+@pytest.mark.parametrize("kind", ["euler_ntac2", "sa_ntac2"])
+def test_dropin_time_loop_matches_oracle(kind):
+    """The Turns_overset.f:360-505 loop driven through the drop-in routines,
+    as a Fortran driver would call them: per physical step ot2d_pitch,
+    ot2d_metfv, ot2d_stqol, then itnmax x (ot2d_time_step, ot2d_step,
+    ot2d_monitor); the state equals the oracle driver's."""
+    import ctypes as C
+    from turns2d_urans_git_gb300 import routines as rt
+    kw, nsteps, tol = CASES[kind]
+    nsteps = min(nsteps, 4)
+    _, prm, xv0, yv0 = api.config_pitching(**kw)
+    n, hist, forces, q_o = ob.solve(prm, xv0.ravel(), yv0.ravel(), nsteps)
+    assert n == nsteps
+    p = type(prm).from_buffer_copy(prm)
+    jd, kd, n2, nvert = p.jd, p.kd, p.jd * p.kd, p.jmax * p.kmax
+    xv = np.ascontiguousarray(xv0.ravel(), dtype=np.float64)
+    yv = np.ascontiguousarray(yv0.ravel(), dtype=np.float64)
+    z = lambda m=1: np.zeros(n2 * m)
+    x, y, xx, xy, yx, yy, ug, vg = z(), z(), z(), z(), z(), z(), z(), z()
+    turmu, tscale, bt = z(), z(), z()
+    q, s = z(p.nq), z(p.nv)
+    qtn, qtnm1, qnewt = z(p.nv), z(p.nv), z(p.nv)
+    iblank = np.ones(n2, dtype=np.int32)
+    ugv, vgv = np.zeros(nvert), np.zeros(nvert)
+    Ds = np.zeros(1)
+    # initia (init.f): centres, metrics, freestream Q/J -- set up by the oracle
+    L, pp = ob.lib(), C.byref(p)
+    L.oro_find_cellcenter(pp, ob.ptr(x), ob.ptr(y), ob.ptr(xv), ob.ptr(yv))
+    assert L.oro_metfv(pp, ob.ptr(q), ob.ptr(xv), ob.ptr(yv), ob.ptr(xx), ob.ptr(xy), ob.ptr(yx), ob.ptr(yy)) == 0
+    L.oro_qzero(pp, ob.ptr(q))
+    L.oro_qdivj(pp, ob.ptr(q))
+    xold, yold, xole, yole = xv.copy(), yv.copy(), xv.copy(), yv.copy()
+    p.istep0 = 0
+    for istep in range(1, nsteps + 1):
+        p.istep0 += 1
+        p.istep = istep
+        p.totime += p.dt
+        rt.set_params(p)
+        rt.pitch(x, y, xv, yv, xold, yold, xole, yole, ug, vg, jd, kd)
+        rt.metfv(q, x, y, xv, yv, xx, xy, yx, yy, jd, kd)
+        if p.itnmax > 1:
+            rt.stqol(q, qtn, qtnm1, qnewt, jd, kd)
+        for itn in range(1, p.itnmax + 1):
+            p.itn = itn
+            rt.set_params(p)
+            rt.time_step(q, xx, xy, yx, yy, ug, vg, tscale, bt, iblank, jd, kd)
+            rt.step(q, qtn, qtnm1, qnewt, s, x, y, xv, yv, iblank, xx, xy, yx, yy, ug, vg, ugv, vgv, xold, yold,
+                    xole, yole, turmu, tscale, bt, Ds, 1, jd, kd)
+            assert rt.monitor(q, jd, kd) == 0
+    assert relerr(q, q_o) <= tol

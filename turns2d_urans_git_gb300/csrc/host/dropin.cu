@@ -127,7 +127,7 @@ int prepare(int nslice, int& err) {
   if ((err = ensure_stream())) return err;
   if (!g_ctx.has) return err = OT2D_ERR_NOPARAMS;
   const size_t n2 = (size_t)g_ctx.P.jd * g_ctx.P.kd, ws = (n2 + 63) / 64 * 64;
-  const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd);
+  const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd, 8);
   const size_t need = ws * DW_SLOTS * nslice + 8 * ws + rec * nslice;
   g_ctx.nslice = nslice;
   if (need > g_ctx.wcap) {
@@ -165,7 +165,7 @@ Slice<double> base_slice(int nsp, int nspec, int64_t qs) {
   const size_t n2 = (size_t)p.jd * p.kd, ws = (n2 + 63) / 64 * 64;
   S.w = g_ctx.dwork + (size_t)(nsp - 1) * ws * DW_SLOTS;
   S.wstride = (int64_t)ws;
-  S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
+  S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd, 8);
   S.red = g_ctx.dred + (size_t)RED_N * (nsp - 1);
   S.ist = nullptr;
   slice_consts(S, p);
@@ -183,20 +183,28 @@ bool dims_ok(const int32_t* jd, const int32_t* kd) {
 }
 
 // face normals (and time-spectral face speeds) from the vertex grid
+// (xold..yole: the previous vertex levels of a time-accurate moving grid,
+// or null)
 int faces_upload(double* dst4, double* dst2, const double* xv, const double* yv, const double* ugv, const double* vgv,
-                 size_t ws, int& err) {
+                 size_t ws, int& err, const double* xold = nullptr, const double* yold = nullptr,
+                 const double* xole = nullptr, const double* yole = nullptr) {
   const ot2d_params& p = g_ctx.P;
   const size_t nv = (size_t)p.jmax * p.kmax, n2 = (size_t)p.jd * p.kd;
   std::vector<double> hx = host_copy(xv, nv), hy = host_copy(yv, nv), hu, hvv;
   std::vector<double> f(4 * n2), t(2 * n2, 0.0);
-  const bool ts = p.timespectral && ugv && vgv;
+  const bool swept = p.iunst > 0 && xold && yold && xole && yole;
+  const bool ts = !swept && p.timespectral && ugv && vgv;
   if (ts) { hu = host_copy(ugv, nv); hvv = host_copy(vgv, nv); }
   face_normals(p, hx.data(), hy.data(), ts ? hu.data() : nullptr, ts ? hvv.data() : nullptr, f.data(), f.data() + n2,
                f.data() + 2 * n2, f.data() + 3 * n2, ts ? t.data() : nullptr, ts ? t.data() + n2 : nullptr);
+  if (swept) {
+    std::vector<double> a = host_copy(xold, nv), b = host_copy(yold, nv), c = host_copy(xole, nv), d = host_copy(yole, nv);
+    face_speeds_swept(p, hx.data(), hy.data(), a.data(), b.data(), c.data(), d.data(), t.data(), t.data() + n2);
+  }
   for (int a = 0; a < 4; ++a)
     if (cudaMemcpyAsync(dst4 + a * ws, f.data() + a * n2, n2 * 8, cudaMemcpyHostToDevice, g_ctx.st) != cudaSuccess)
       err = OT2D_ERR_CUDA;
-  if (ts && dst2)
+  if ((ts || swept) && dst2)
     for (int a = 0; a < 2; ++a)
       if (cudaMemcpyAsync(dst2 + a * ws, t.data() + a * n2, n2 * 8, cudaMemcpyHostToDevice, g_ctx.st) != cudaSuccess)
         err = OT2D_ERR_CUDA;
@@ -400,22 +408,25 @@ int ot2d_sync_to_device(void* h) {
 int ot2d_rhsup(double* q, double* s, double* xx, double* xy, double* yx, double* yy, double* x, double* y,
                double* xv, double* yv, double* xold, double* yold, double* xole, double* yole, int32_t* iblank,
                double* ugv, double* vgv, int32_t* jd, int32_t* kd, int32_t* nei, int32_t* im, double* bt) {
-  (void)xx; (void)xy; (void)yx; (void)yy; (void)x; (void)y; (void)xold; (void)yold; (void)xole; (void)yole; (void)im; (void)bt;
+  (void)xx; (void)xy; (void)yx; (void)yy; (void)x; (void)y; (void)im; (void)bt;
   int err = 0;
   if (prepare(1, err)) return fail(err);
   const ot2d_params& p = g_ctx.P;
-  if (!dims_ok(jd, kd) || !nei || *nei != 1 || p.iunst != 0 || !q || !s || !xv || !yv || !iblank) return fail(OT2D_ERR_ARG);
+  const bool swept = p.iunst == 1;   // time-accurate moving grid: face speeds from the swept areas
+  if (!dims_ok(jd, kd) || !nei || *nei != 1 || (p.iunst != 0 && !swept) || !q || !s || !xv || !yv || !iblank ||
+      (swept && (!xold || !yold || !xole || !yole)))
+    return fail(OT2D_ERR_ARG);
   const size_t n2 = (size_t)p.jd * p.kd;
   Slice<double> S = base_slice(1, 1, (int64_t)n2);
   const size_t ws = (size_t)S.wstride;
   double* faces = g_ctx.dwork + ws * DW_SLOTS;           // 4 face-normal arrays
   double* tjs = faces + 4 * ws;                     // 2 face-speed arrays
-  faces_upload(faces, tjs, xv, yv, ugv, vgv, ws, err);
+  faces_upload(faces, tjs, xv, yv, ugv, vgv, ws, err, xold, yold, xole, yole);
   S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, false, err);
   S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
   S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
   S.fxa = faces; S.fya = faces + ws; S.gxa = faces + 2 * ws; S.gya = faces + 3 * ws;
-  if (p.timespectral && ugv && vgv) { S.ftj = tjs; S.gtj = tjs + ws; }
+  if ((p.timespectral && ugv && vgv) || swept) { S.ftj = tjs; S.gtj = tjs + ws; }
   std::vector<Slice<double>> sl{S};
   run_batch(sl, err);
   if (!err && launch_faces<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 1, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
@@ -679,16 +690,19 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
               double* yv, int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
               double* ugv, double* vgv, double* xold, double* yold, double* xole, double* yole, double* turmu,
               double* tscale, double* bt, double* Ds, int32_t* im, int32_t* jd, int32_t* kd) {
-  (void)qtn; (void)qtnm1; (void)qnewt; (void)xold; (void)yold; (void)xole; (void)yole; (void)im; (void)bt;
+  (void)qtn; (void)qtnm1; (void)im; (void)bt;
   const int nspec = g_ctx.has ? g_ctx.P.nspec : 1;
   int err = 0;
   if (prepare(nspec, err)) return fail(err);
   const ot2d_params& p = g_ctx.P;
-  if (!dims_ok(jd, kd) || p.ilhs < 1 || p.ilhs > 3 || p.itnmax > 1 || (!p.lamin && p.iturb != 1 && p.iturb != 2) ||
-      p.itrans != 0)
+  const bool swept = p.iunst == 1, newton = p.itnmax > 1;
+  if (!dims_ok(jd, kd) || p.ilhs < 1 || p.ilhs > 3 || (p.iunst != 0 && !swept) || (newton && p.timespectral) ||
+      (!p.lamin && p.iturb != 1 && p.iturb != 2) || p.itrans != 0)
     return fail(OT2D_ERR_ARG);
   if (!q || !s || !x || !y || !xv || !yv || !iblank || !xx || !xy || !yx || !yy || !turmu || !tscale) return fail(OT2D_ERR_ARG);
   if (p.timespectral && (!ugv || !vgv || !ug || !vg || !Ds)) return fail(OT2D_ERR_ARG);
+  if (swept && (!xold || !yold || !xole || !yole || !ug || !vg)) return fail(OT2D_ERR_ARG);
+  if (newton && !qnewt) return fail(OT2D_ERR_ARG);
   const size_t n2 = (size_t)p.jd * p.kd, ns = (size_t)nspec, nv = (size_t)p.jmax * p.kmax, qs = n2 * ns;
   double* dq = (double*)resolve(q, qs * p.nq * 8, true, true, err);
   double* ds = (double*)resolve(s, qs * p.nv * 8, false, true, err);
@@ -697,8 +711,21 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   double* dxy = (double*)resolve(xy, qs * 8, true, false, err);
   double* dyx = (double*)resolve(yx, qs * 8, true, false, err);
   double* dyy = (double*)resolve(yy, qs * 8, true, false, err);
-  double* dug = p.timespectral ? (double*)resolve(ug, qs * 8, true, false, err) : nullptr;
-  double* dvg = p.timespectral ? (double*)resolve(vg, qs * 8, true, false, err) : nullptr;
+  double* dug = (p.timespectral || swept) ? (double*)resolve(ug, qs * 8, true, false, err) : nullptr;
+  double* dvg = (p.timespectral || swept) ? (double*)resolve(vg, qs * 8, true, false, err) : nullptr;
+  double* dqn = newton ? (double*)resolve(qnewt, qs * p.nv * 8, true, false, err) : nullptr;
+  if (newton && !err) {
+    // newton's 1/(oat*h) (time.f:195-200) for the residual kernel
+    double oat = 1.0;
+    if (p.ntac >= 2 && p.istep > 1) oat = 2. / 3.;
+    if (p.ntac == 3 && p.istep > 2) oat = 6. / 11.;
+    const double tac = 1. / (oat * p.h);
+    for (int nsp = 0; nsp < nspec && !err; ++nsp)
+      if (cudaMemcpyAsync(g_ctx.dred + (size_t)RED_N * nsp + 8, &tac, sizeof(double), cudaMemcpyHostToDevice,
+                          g_ctx.st) != cudaSuccess)
+        err = OT2D_ERR_CUDA;
+    cudaStreamSynchronize(g_ctx.st);
+  }
   double* dturmu = (double*)resolve(turmu, qs * 8, true, true, err);
   double* dts = (double*)resolve(tscale, qs * 8, true, false, err);
   double* dDs = p.timespectral ? (double*)resolve(Ds, ns * ns * 8, true, false, err) : nullptr;
@@ -712,7 +739,8 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   for (int nsp = 1; nsp <= nspec && !err; ++nsp) {
     double* e = extra + (size_t)(nsp - 1) * ws * 8;
     faces_upload(e, e + 4 * ws, xv + (nsp - 1) * nv, yv + (nsp - 1) * nv, ugv ? ugv + (nsp - 1) * nv : nullptr,
-                 vgv ? vgv + (nsp - 1) * nv : nullptr, ws, err);
+                 vgv ? vgv + (nsp - 1) * nv : nullptr, ws, err, swept ? xold : nullptr, swept ? yold : nullptr,
+                 swept ? xole : nullptr, swept ? yole : nullptr);
     std::vector<double> sn(n2);
     wall_distance(p, hx.data() + (nsp - 1) * n2, hy.data() + (nsp - 1) * n2, hxv.data() + (nsp - 1) * nv,
                   hyv.data() + (nsp - 1) * nv, sn.data());
@@ -728,7 +756,8 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
     S.turmu = dturmu + o; S.tscale = dts + o;
     S.bt = nullptr;  // bt is 1 on the non-preconditioned path
     S.fxa = e; S.fya = e + ws; S.gxa = e + 2 * ws; S.gya = e + 3 * ws;
-    S.ftj = p.timespectral ? e + 4 * ws : nullptr; S.gtj = p.timespectral ? e + 5 * ws : nullptr;
+    S.ftj = (p.timespectral || swept) ? e + 4 * ws : nullptr; S.gtj = (p.timespectral || swept) ? e + 5 * ws : nullptr;
+    S.qnewt = dqn ? dqn + o : nullptr;
     S.sn = e + 6 * ws;
     S.wd2 = sst_params(p) ? e + 7 * ws : nullptr;
     S.Ds = dDs;
@@ -981,6 +1010,64 @@ int ot2d_qdivj(double* q, int32_t* jd, int32_t* kd) {
   const size_t n2 = (size_t)*jd * *kd;
   double* dq = (double*)resolve(q, n2 * g_ctx.P.nq * 8, true, true, err);
   if (!err && io_unpack(dq, dq, nullptr, n2, 1, g_ctx.P.nq, 4, 1, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_pitch(int32_t* init, double* x, double* y, double* xv, double* yv, double* xold, double* yold, double* xole,
+               double* yole, double* ug, double* vg, int32_t* jd, int32_t* kd) {
+  (void)init;
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !x || !y || !xv || !yv || !xold || !yold || !xole || !yole || !ug || !vg ||
+      p.ntac < 1 || p.ntac > 3 || !(p.dt > 0))
+    return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd, nv = (size_t)p.jmax * p.kmax;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.xc = (double*)resolve(x, n2 * 8, true, true, err);
+  S.yc = (double*)resolve(y, n2 * 8, true, true, err);
+  S.xv = (double*)resolve(xv, nv * 8, true, true, err);
+  S.yv = (double*)resolve(yv, nv * 8, true, true, err);
+  S.xold = (double*)resolve(xold, nv * 8, true, true, err);
+  S.yold = (double*)resolve(yold, nv * 8, true, true, err);
+  S.xole = (double*)resolve(xole, nv * 8, true, true, err);
+  S.yole = (double*)resolve(yole, nv * 8, true, true, err);
+  S.ug = S.ug64 = (double*)resolve(ug, n2 * 8, true, true, err);
+  S.vg = S.vg64 = (double*)resolve(vg, n2 * 8, true, true, err);
+  // the increment of step istep (motion.f:576-583) as a one-entry table, and
+  // a status word that reads "first Newton iteration of step 1 of the table"
+  const double pi = 4.0 * std::atan(1.0);
+  const double dtheta = -(p.angmax * (std::cos(p.rotf * (double)p.istep * p.dt) -
+                                      std::cos(p.rotf * (double)(p.istep - 1) * p.dt)));
+  const double m[4] = {std::sin(dtheta * pi / 180.), std::cos(dtheta * pi / 180.), std::sin(-1. * dtheta * pi / 180.),
+                       std::cos(-1. * dtheta * pi / 180.)};
+  double* dm = nullptr;
+  if (!err && cudaMalloc(&dm, sizeof(m)) != cudaSuccess) err = OT2D_ERR_NOMEM;
+  if (dm) g_ctx.pool.push_back(dm);
+  if (!err && cudaMemcpyAsync(dm, m, sizeof(m), cudaMemcpyHostToDevice, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  const int32_t ist[IST_N] = {0, 1, 0, 0, 1, 0};
+  if (!err && cudaMemcpyAsync(g_ctx.dist, ist, sizeof(ist), cudaMemcpyHostToDevice, g_ctx.st) != cudaSuccess)
+    err = OT2D_ERR_CUDA;
+  S.motion = dm; S.nmotion = 1; S.ist = g_ctx.dist;
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_pitch<double>(g_ctx.batch.d_sl, g_ctx.batch.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_stqol(double* q, double* qtn, double* qtnm1, double* qnewt, int32_t* jd, int32_t* kd) {
+  int err = 0;
+  if ((err = ensure_stream())) return fail(err);
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !q || !qtn || !qtnm1 || !qnewt || p.nv < 4) return fail(OT2D_ERR_ARG);
+  const size_t qs = (size_t)p.jd * p.kd * p.nspec;
+  double* dq = (double*)resolve(q, qs * p.nq * 8, true, false, err);
+  double* d1 = (double*)resolve(qtn, qs * p.nv * 8, true, true, err);
+  double* d2 = (double*)resolve(qtnm1, qs * p.nv * 8, true, true, err);
+  double* d3 = (double*)resolve(qnewt, qs * p.nv * 8, false, true, err);
+  if (!err && launch_stqol(dq, d1, d2, d3, (int64_t)qs, p.nv, p.ntac, p.istep, g_ctx.st) != cudaSuccess)
+    err = OT2D_ERR_CUDA;
   return finish(err);
 }
 

@@ -5,6 +5,8 @@
  *   metrics, J        metfv             src/setup.f:440-724
  *   SA wall distance  dist              src/samodel2d.f:243-293
  *   face normals      rhsup             src/eulerrhs.f:102-116, :209-223
+ *   swept-area face speeds of a moving grid (drop-in path)
+ *                     rhsup             src/eulerrhs.f:118-139, :224-246
  *   time-spectral pitching grid and grid speeds (sine form)
  *                     find_coord_TS_orig / find_timemetrics_TS_orig
  *                     src/setup.f:396-438, :789-835; tj: eulerrhs.f:140-146
@@ -270,6 +272,43 @@ void face_normals(const ot2d_params& p, const double* xv_, const double* yv_, co
         C2 gtj{gtj_, jd};
         gtj(j, k) = -0.5 * (ugv(a, b) + ugv(a - 1, b)) * gxa(j, k) - 0.5 * (vgv(a, b) + vgv(a - 1, b)) * gya(j, k);
       }
+    }
+}
+
+void face_speeds_swept(const ot2d_params& p, const double* xv_, const double* yv_, const double* xold_,
+                       const double* yold_, const double* xole_, const double* yole_, double* ftj_, double* gtj_) {
+  const int jd = p.jd, nh = p.nhalo;
+  C2 ftj{ftj_, jd}, gtj{gtj_, jd};
+  V2 xv{xv_, p.jmax}, yv{yv_, p.jmax}, xo{xold_, p.jmax}, yo{yold_, p.jmax}, xe{xole_, p.jmax}, ye{yole_, p.jmax};
+  for (size_t i = 0; i < (size_t)jd * p.kd; ++i) { ftj_[i] = 0; gtj_[i] = 0; }
+  const bool second = p.ntac == 2 && p.istep > 1;
+  for (int k = p.kbeg; k <= p.kend; ++k)
+    for (int j = p.jbeg - 1; j <= p.jend; ++j) {
+      const int a = j - nh + 1, b = k - nh + 1;
+      double dx1 = xv(a, b) - xo(a, b - 1), dy1 = yv(a, b) - yo(a, b - 1);
+      double dx2 = xo(a, b) - xv(a, b - 1), dy2 = yo(a, b) - yv(a, b - 1);
+      double tj = -(0.5 * (dx1 * dy2 - dx2 * dy1) / p.dt);
+      if (second) {
+        dx1 = xo(a, b) - xe(a, b - 1); dy1 = yo(a, b) - ye(a, b - 1);
+        dx2 = xe(a, b) - xo(a, b - 1); dy2 = ye(a, b) - yo(a, b - 1);
+        const double temp = -(0.5 * (dx1 * dy2 - dx2 * dy1) / p.dt);
+        tj = 1.5 * tj - 0.5 * temp;
+      }
+      ftj(j, k) = tj;
+    }
+  for (int j = p.jbeg; j <= p.jend; ++j)
+    for (int k = p.kbeg - 1; k <= p.kend; ++k) {
+      const int a = j - nh + 1, b = k - nh + 1;
+      double dx1 = xv(a, b) - xo(a - 1, b), dy1 = yv(a, b) - yo(a - 1, b);
+      double dx2 = xo(a, b) - xv(a - 1, b), dy2 = yo(a, b) - yv(a - 1, b);
+      double tj = 0.5 * (dx1 * dy2 - dx2 * dy1) / p.dt;
+      if (second) {
+        dx1 = xo(a, b) - xe(a - 1, b); dy1 = yo(a, b) - ye(a - 1, b);
+        dx2 = xe(a, b) - xo(a - 1, b); dy2 = ye(a, b) - yo(a - 1, b);
+        const double temp = 0.5 * (dx1 * dy2 - dx2 * dy1) / p.dt;
+        tj = 1.5 * tj - 0.5 * temp;
+      }
+      gtj(j, k) = tj;
     }
 }
 

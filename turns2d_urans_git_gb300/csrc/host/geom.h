@@ -19,6 +19,11 @@ void sst_wall_d2(const ot2d_params& p, const double* x, const double* y, const d
                  double* wd2);
 void face_normals(const ot2d_params& p, const double* xv, const double* yv, const double* ugv, const double* vgv,
                   double* fxa, double* fya, double* gxa, double* gya, double* ftj, double* gtj);
+// time-accurate face speeds from the areas the faces sweep between the
+// vertex levels (eulerrhs.f:118-139, :224-246; second order when ntac = 2
+// and istep > 1); ftj / gtj on the xi / eta faces as face_normals indexes them
+void face_speeds_swept(const ot2d_params& p, const double* xv, const double* yv, const double* xold,
+                       const double* yold, const double* xole, const double* yole, double* ftj, double* gtj);
 void ts_pitch_grid(const ot2d_params& p, const double* xv1, const double* yv1, double tspec, double* xv, double* yv);
 void ts_grid_speed(const ot2d_params& p, const double* x, const double* y, const double* xv, const double* yv,
                    double tspec, double* ug, double* vg, double* ugv, double* vgv);

@@ -93,7 +93,7 @@ size_t plan(const ot2d_params& p, int precision, F&& assign) {
   if (is_sst(p)) assign("wd2", L.take(sizeof(double) * n2 * nspec));
   // the freestream correction belongs to a fixed grid
   if (mixed && !mv) assign("sinf", L.take(rb * n2 * nspec * 4));
-  assign("lurec", L.take(rb * (size_t)lu_rec_elems(p.jd, p.kd) * nspec));
+  assign("lurec", L.take(rb * (size_t)lu_rec_elems(p.jd, p.kd, (int)rb) * nspec));
   return L.total;
 }
 
@@ -368,7 +368,7 @@ Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
   S.sinf = R_(d.sinf);
   slice_consts(S, p);
   S.wstride = (int64_t)d.wstride;
-  S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd);
+  S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd, (int)sizeof(R));
   S.red = red; S.ist = ist;
   S.Ds = p.timespectral ? d.Ds : nullptr;
   S.xx64 = D_(d.xx64); S.xy64 = D_(d.xy64); S.yx64 = D_(d.yx64); S.yy64 = D_(d.yy64);

@@ -29,16 +29,17 @@
 namespace ot2d {
 
 constexpr int LU_NF = 24;                 // fields per cell record
-// A (band, step) chunk holds the records of the band's 32 lanes as
-// 16-byte field groups interleaved over the lanes: [group][lane][GW fields]
-// with GW = 16 bytes of fields (4 f32 or 2 f64).  A lane reads four
-// consecutive fields with one (f32) or two (f64) 16-byte shared loads; the
-// eight lanes of a load phase read 128 contiguous bytes (no bank conflict)
-// and a warp writes a group of a chunk as 512 contiguous bytes.
+// A (band, step) chunk holds the records of the band's 32 lanes one after
+// another (lane-major): lane l's 24 fields are contiguous, so a lane reads
+// four consecutive fields with one (f32) or two (f64) 16-byte shared loads.
+// Each record is padded to LS elements so that the eight lanes of a load
+// phase hit disjoint banks (f32: 112-byte stride, f64: 208-byte stride).
+// (Interleaving 16-byte field groups over the lanes instead was measured
+// slower in the backward sweep.)
 template <class R>
 struct LuLay {
-  static constexpr int GW = 16 / (int)sizeof(R);   // fields per 16-byte group
-  static constexpr int CH = 32 * LU_NF;            // elements per chunk
+  static constexpr int LS = sizeof(R) == 4 ? 28 : 26;   // elements per lane record
+  static constexpr int CH = 32 * LS;                    // elements per chunk
 };
 // record fields
 enum {
@@ -51,17 +52,18 @@ enum {
 // element offset of field f of lane l within a chunk
 template <class R>
 __host__ __device__ __forceinline__ int lu_idx(int f, int l) {
-  constexpr int GW = LuLay<R>::GW;
-  return ((f / GW) * 32 + l) * GW + (f % GW);
+  return l * LuLay<R>::LS + f;
 }
 
 __host__ __device__ __forceinline__ int lu_nrow(int kd) { return kd - 2; }
 __host__ __device__ __forceinline__ int lu_ncol(int jd) { return jd - 2; }
 __host__ __device__ __forceinline__ int lu_nband(int kd) { return (kd - 2 + 31) / 32; }
 __host__ __device__ __forceinline__ int lu_nstep(int jd) { return jd - 2 + 31; }
-// elements of one slice's record: chunks + 4 halo-contribution arrays
-__host__ __device__ __forceinline__ int64_t lu_rec_elems(int jd, int kd) {
-  return (int64_t)lu_nband(kd) * lu_nstep(jd) * (32 * LU_NF) + 8 * (int64_t)(lu_nrow(kd) + lu_ncol(jd)) + 64;
+// elements of one slice's record (element size esize bytes): chunks + 4
+// halo-contribution arrays
+__host__ __device__ __forceinline__ int64_t lu_rec_elems(int jd, int kd, int esize) {
+  const int ch = esize == 4 ? LuLay<float>::CH : LuLay<double>::CH;
+  return (int64_t)lu_nband(kd) * lu_nstep(jd) * ch + 8 * (int64_t)(lu_nrow(kd) + lu_ncol(jd)) + 64;
 }
 
 // fields f..f+3 of lane l of a chunk (f a multiple of 4) as 16-byte accesses
@@ -155,13 +157,14 @@ __device__ __forceinline__ void lu_contrib(const LuCell<R>& c, const R* s, R gm1
 }
 
 // ---- kernel 1: records of the interior cells (one thread per (band, step, lane))
-// The record of lane l of chunk (band, t), written as six 16-byte field
-// groups (coalesced over the warp).
+// The record of lane l of chunk (band, t) into ch, the chunk as the warp
+// stages it in shared memory (k_lu_prep stores the staged chunk with
+// contiguous 16-byte accesses).
 template <class R>
-__device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_params& p, int band, int t, int l, int scale) {
-  const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nst = lu_nstep(S.jd);
+__device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_params& p, int band, int t, int l, int scale,
+                                             R* ch) {
+  const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd);
   const int r = 32 * band + l, c = t - l;
-  R* ch = S.lurec + ((int64_t)band * nst + t) * LuLay<R>::CH;
   if (r >= nrow || c < 0 || c >= ncol) {
     const R z = (R)0;
 #pragma unroll

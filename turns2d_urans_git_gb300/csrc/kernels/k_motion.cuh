@@ -30,6 +30,20 @@ __device__ __forceinline__ bool mv_new_step(const Slice<R>& S) {
   return S.xc && S.ist && S.ist[4] == 1;
 }
 
+// stqol (time.f:128-168) for one element o of q / qtn / qtnm1 / qnewt
+__device__ __forceinline__ void mv_stqol_elem(const double* q, double* qtn, double* qtnm1, double* qnewt, int64_t o,
+                                              int ntac, int istep) {
+  const bool c1 = (ntac == 2 && istep > 1) || (ntac == 3 && istep == 2);
+  const bool c2 = ntac == 3 && istep > 2;
+  const double qv = q[o], qt = qtn[o];
+  double v = qv;
+  if (c1) v = v + (qv - qt) / 3.;
+  if (c2) v = v + 7. * (qv - qt) / 11. - 2. * (qt - qtnm1[o]) / 11.;
+  qnewt[o] = v;
+  qtnm1[o] = qt;
+  qtn[o] = qv;
+}
+
 // Phase A (one thread per cell of the slice; the first jmax*kmax threads
 // also own one vertex): pitch and stqol.
 template <class R>
@@ -66,21 +80,10 @@ __device__ void mv_pitch_cell(const Slice<R>& S, int cid) {
       const_cast<R*>(S.ug)[cid] = (R)ug;
       const_cast<R*>(S.vg)[cid] = (R)vg;
     }
-    // stqol (time.f:128-168), element by element
-    if (S.qnewt) {
-      const bool c1 = (p.ntac == 2 && istep > 1) || (p.ntac == 3 && istep == 2);
-      const bool c2 = p.ntac == 3 && istep > 2;
-      for (int n = 0; n < p.nv; ++n) {
-        const int64_t o = (int64_t)n * S.qs + cid;
-        const double q = S.q64[o], qt = S.qtn[o];
-        double v = q;
-        if (c1) v = v + (q - qt) / 3.;
-        if (c2) v = v + 7. * (q - qt) / 11. - 2. * (qt - S.qtnm1[o]) / 11.;
-        S.qnewt[o] = v;
-        S.qtnm1[o] = qt;
-        S.qtn[o] = q;
-      }
-    }
+    // stqol, element by element
+    if (S.qnewt)
+      for (int n = 0; n < p.nv; ++n)
+        mv_stqol_elem(S.q64, S.qtn, S.qtnm1, S.qnewt, (int64_t)n * S.qs + cid, p.ntac, istep);
   }
   if (cid < (int64_t)p.jmax * p.kmax) {
     // motion.f:607-624

@@ -101,7 +101,7 @@ __global__ void k_mv_halo(const Slice<R>* __restrict__ sl) {
 }
 
 template <class R>
-__global__ void k_bc(const Slice<R>* __restrict__ sl, int advance) {
+__global__ void __launch_bounds__(BC_BS) k_bc(const Slice<R>* __restrict__ sl, int advance) {
   const Slice<R>& S = sl[blockIdx.x];
   const int istep0 = S.ist ? S.ist[0] : S.P->istep0;
   bc_slice(S, nullptr, istep0);
@@ -267,16 +267,28 @@ __global__ void k_rbc(const Slice<R>* __restrict__ sl) {
 // ilu2d (lhs.f:470-814), preceded by s *= tscale on all cells when `scale`
 // (step.f:141-148).  Records of the interior cells; one thread per
 // (band, step, lane) of every slice (prefix table lfirst).
+// A warp builds one chunk: each lane writes its record into the warp's
+// shared-memory copy of the chunk, then the warp stores the chunk with
+// contiguous 16-byte accesses (full sectors; the lane-major records would
+// otherwise be written with a 112- / 208-byte stride).
 template <class R>
 __global__ void __launch_bounds__(CELL_BS) k_lu_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst,
                                                      int nslice, int scale, int only_lu) {
+  extern __shared__ __align__(16) unsigned char lp_smem[];
   const int si = find_slice(lfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];
   const int g = (blockIdx.x - lfirst[si]) * blockDim.x + threadIdx.x;
   const int nst = lu_nstep(S.jd), nb = lu_nband(S.kd);
   const int l = g & 31, t = (g >> 5) % nst, band = (g >> 5) / nst;
-  if (band >= nb || (only_lu && S.P->ilhs != 1)) return;
-  lu_prep_cell(S, *S.P, band, t, l, scale);
+  if (band >= nb || (only_lu && S.P->ilhs != 1)) return;   // uniform over the warp
+  constexpr int CH = LuLay<R>::CH;
+  R* stage = (R*)lp_smem + (threadIdx.x >> 5) * CH;
+  lu_prep_cell(S, *S.P, band, t, l, scale, stage);
+  __syncwarp();
+  int4* dst = reinterpret_cast<int4*>(S.lurec + ((int64_t)band * nst + t) * CH);
+  const int4* src = reinterpret_cast<const int4*>(stage);
+  constexpr int n16 = (int)(CH * sizeof(R) / 16);
+  for (int i = l; i < n16; i += 32) dst[i] = src[i];
 }
 
 template <class R>
@@ -304,7 +316,7 @@ __global__ void __launch_bounds__(CELL_BS) k_sa_prep(const Slice<R>* __restrict_
 }
 
 template <class R>
-__global__ void k_turbc(const Slice<R>* __restrict__ sl, int final_pass) {
+__global__ void __launch_bounds__(BC_BS) k_turbc(const Slice<R>* __restrict__ sl, int final_pass) {
   const Slice<R>& S = sl[blockIdx.x];
   const ot2d_params& p = *S.P;
   if (p.lamin || p.iturb != 1) return;
@@ -327,7 +339,7 @@ __global__ void k_turbc(const Slice<R>* __restrict__ sl, int final_pass) {
 }
 
 template <class R>
-__global__ void __launch_bounds__(CELL_BS) k_sa_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+__global__ void __launch_bounds__(CELL_BS, sizeof(R) == 4 ? 4 : 1) k_sa_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
                                                     int nslice) {
   OT2D_CELL_MAP();
   if (!inside) return;

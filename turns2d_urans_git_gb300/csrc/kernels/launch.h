@@ -10,6 +10,9 @@ template <class R> struct Slice;
 struct NormPart;
 
 constexpr int CELL_BS = 256;
+// threads of the one-CTA-per-slice boundary kernels (their loops run along
+// the boundary rows; more threads, fewer serial passes per row)
+constexpr int BC_BS = 512;
 // residual tile: RT_TJ x RT_TK interior cells per CTA
 constexpr int RT_TJ = 32, RT_TK = 8;
 // scratch arrays per slice of the k-omega SST solve (k_sst.cuh: SSTw)
@@ -59,6 +62,12 @@ cudaError_t branch_of_device(Branch*& out);
 // face speeds and wall distances.
 template <class R> cudaError_t launch_iter_begin(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+// pitch alone (the drop-in ot2d_pitch): slices with xc set and ist[4] == 1
+template <class R> cudaError_t launch_pitch(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+// stqol over n elements of each of nv variables (stride qs): q of the
+// current step, the stored levels and the Newton target (time.f:110-175)
+cudaError_t launch_stqol(const double* q, double* qtn, double* qtnm1, double* qnewt, int64_t qs, int nv, int ntac,
+                         int istep, cudaStream_t st);
 template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st);
 template <class R> cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st);
 template <class R> cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);

@@ -15,13 +15,18 @@ cudaError_t launch_iter_begin(const Slice<R>* d_sl, const Batch& b, cudaStream_t
   return cudaGetLastError();
 }
 template <class R>
+cudaError_t launch_pitch(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_mv_pitch<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  return cudaGetLastError();
+}
+template <class R>
 cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_time_step<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
 }
 template <class R>
 cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st) {
-  k_bc<R><<<b.nslice, 256, 0, st>>>(d_sl, advance);
+  k_bc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, advance);
   return cudaGetLastError();
 }
 template <class R>
@@ -67,7 +72,15 @@ cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
 // the FP64 path also round-trips q here)
 template <class R>
 cudaError_t launch_lusgs_prep(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
-  k_lu_prep<R><<<b.lu_blocks, CELL_BS, 0, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
+  // one staged chunk per warp (f32 28 KB, f64 53 KB per block)
+  constexpr size_t prep_smem = (size_t)(CELL_BS / 32) * LuLay<R>::CH * sizeof(R);
+  static bool prep_attr = false;
+  if (!prep_attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_lu_prep<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
+    if (e != cudaSuccess) return e;
+    prep_attr = true;
+  }
+  k_lu_prep<R><<<b.lu_blocks, CELL_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
   k_lu_edges<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
   return cudaGetLastError();
 }
@@ -131,7 +144,7 @@ cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaSt
 template <class R>
 cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_sa_prep<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
-  k_turbc<R><<<b.nslice, 256, 0, st>>>(d_sl, 0);
+  k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 0);
   k_sa_rhs<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   constexpr size_t lj_smem = sizeof(R) * LJ_SMEM;
   static bool lj_attr = false;
@@ -142,7 +155,7 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   }
   k_sa_lsolvej<R><<<b.jgroups, 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sa_lsolve<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice, 1);
-  k_turbc<R><<<b.nslice, 256, 0, st>>>(d_sl, 1);
+  k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 1);
   return cudaGetLastError();
 }
 // komegasst (komegasst.f:2-187) for the SST slices of the batch
@@ -238,6 +251,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   template cudaError_t launch_iteration<R>(const Slice<R>*, const Batch&, int, int, int, cudaStream_t); \
   template cudaError_t launch_time_step<R>(const Slice<R>*, const Batch&, cudaStream_t);                \
   template cudaError_t launch_iter_begin<R>(const Slice<R>*, const Batch&, cudaStream_t);               \
+  template cudaError_t launch_pitch<R>(const Slice<R>*, const Batch&, cudaStream_t);                    \
   template cudaError_t launch_bc<R>(const Slice<R>*, const Batch&, int, cudaStream_t);                  \
   template cudaError_t launch_residual<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
   template cudaError_t launch_rbc<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \

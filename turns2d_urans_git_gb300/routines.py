@@ -241,3 +241,16 @@ def restr_turb(q, jd, kd, logq):
 def qdivj(q, jd, kd):
     """src/init.f:180."""
     _call("ot2d_qdivj", _p(q), _ref(jd), _ref(kd))
+
+
+# ---- time-accurate pieces (src/motion.f, src/time.f) -------------------------
+
+def pitch(x, y, xv, yv, xold, yold, xole, yole, ug, vg, jd, kd, init=0):
+    """src/motion.f:546 -- step params.istep of the pitching motion."""
+    _call("ot2d_pitch", _ref(init), _p(x), _p(y), _p(xv), _p(yv), _p(xold), _p(yold), _p(xole), _p(yole), _p(ug),
+          _p(vg), _ref(jd), _ref(kd))
+
+
+def stqol(q, qtn, qtnm1, qnewt, jd, kd):
+    """src/time.f:110."""
+    _call("ot2d_stqol", _p(q), _p(qtn), _p(qtnm1), _p(qnewt), _ref(jd), _ref(kd))
