@@ -51,6 +51,9 @@ void visrhs(const P& p, A2 turmu, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy);
 void time_step(const P& p, A3 q, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 tscale, A2 bt, I2 iblank);
 /* lhs.f:470-814 */
 void ilu2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, A2 tscale);
+/* lhs.f:2-467 (Turkel-preconditioned LU-SGS) and sources.f:97-148 */
+void preilu2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, A2 tscale, A2 bt);
+void rhslom(const P& p, A3 q, A3 s, A2 bt);
 /* lhs.f:817-1057 (ilhs = 2: lhsinv + pentadag) */
 void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, I2 iblank, A2 tscale, A2 bt);
 /* samodel2d.f:200-240 */

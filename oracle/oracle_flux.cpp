@@ -222,6 +222,95 @@ static void roeflx(const P& p, Line& L, int is, int ie) {
   }
 }
 
+/* eulerrhs.f:450-625 (roetrklflx): the Roe flux with Turkel's low-Mach
+ * preconditioning; b = 1 on every face (eulerrhs.f:78, :185), so
+ * bSq = Mp**2 */
+static void roetrklflx(const P& p, Line& L, int is, int ie) {
+  const double gm1 = p.gm1, eps = 1.e-6;
+  const double bt = 1.0;
+  const double bSq = (p.Mp * p.Mp) / (bt - (p.Mp * p.Mp) * (bt - 1.));
+  for (int i = is; i <= ie; ++i) {
+    int i1 = i + 1;
+    double rlft = L.ql[1][i], ulft = L.ql[2][i], vlft = L.ql[3][i], plft = L.ql[4][i];
+    double rlfti = 1.0 / rlft;
+    double rulft = rlft * ulft, rvlft = rlft * vlft;
+    double uvl = 0.5 * (ulft * ulft + vlft * vlft);
+    double elft = plft / gm1 + rlft * uvl;
+    double hlft = (elft + plft) * rlfti;
+    double clft = std::sqrt(gm1 * (hlft - uvl));
+    double rrht = L.qr[1][i1], urht = L.qr[2][i1], vrht = L.qr[3][i1], prht = L.qr[4][i1];
+    double rrhti = 1.0 / rrht;
+    double rurht = rrht * urht, rvrht = rrht * vrht;
+    double uvr = 0.5 * (urht * urht + vrht * vrht);
+    double erht = prht / gm1 + rrht * uvr;
+    double hrht = (erht + prht) * rrhti;
+    double crht = std::sqrt(gm1 * (hrht - uvr));
+    double rat = std::sqrt(rrht * rlfti);
+    double rati = 1.0 / (rat + 1.);
+    double rav = rat * rlft;
+    double uav = (rat * urht + ulft) * rati;
+    double vav = (rat * vrht + vlft) * rati;
+    double hav = (rat * hrht + hlft) * rati;
+    double uv = 0.5 * (uav * uav + vav * vav);
+    double cav = std::sqrt(gm1 * (hav - uv));
+    double aq1 = rrht - rlft, aq2 = urht - ulft, aq3 = vrht - vlft, aq4 = prht - plft;
+    double ri1 = L.xa[i], ri2 = L.ya[i], ri3 = L.tj[i];
+    double rr2 = ri1 * ri1 + ri2 * ri2;
+    double rr = std::sqrt(rr2);
+    double r0 = 1.0 / rr;
+    double r1 = ri1 * r0, r2 = ri2 * r0, r3 = ri3 * r0;
+    double uumxt = r1 * uav + r2 * vav;
+    double uu = uumxt + r3;
+    double c2 = cav * cav;
+    double c2i = 1.0 / c2;
+    double X = std::sqrt((((1. - bSq) * uu) * (1. - bSq)) * uu + ((4. * bSq) * c2));
+    double auu = std::fabs(uu);
+    double aupc = 0.5 * std::fabs((1. + bSq) * uu + X);
+    double aumc = 0.5 * std::fabs((1. + bSq) * uu - X);
+    double uulft = r1 * ulft + r2 * vlft + r3;
+    double uurht = r1 * urht + r2 * vrht + r3;
+    X = std::sqrt(((1. - bSq) * uulft) * ((1. - bSq) * uulft) + ((4. * bSq) * clft) * clft);
+    double upclft = 0.5 * ((1. + bSq) * uulft + X);
+    double umclft = 0.5 * ((1. + bSq) * uulft - X);
+    X = std::sqrt(((1. - bSq) * uurht) * ((1. - bSq) * uurht) + ((4. * bSq) * crht) * crht);
+    double upcrht = 0.5 * ((1. + bSq) * uurht + X);
+    double umcrht = 0.5 * ((1. + bSq) * uurht - X);
+    double dauu = 4. * (uurht - uulft) + eps;
+    double dauus = fmax2(dauu, 0.0);
+    if (auu <= 0.5 * dauus) auu = auu * auu / dauu + 0.25 * dauu;
+    double daupc = 4. * (upcrht - upclft) + eps;
+    double daupcs = fmax2(daupc, 0.0);
+    if (aupc <= 0.5 * daupcs) aupc = aupc * aupc / daupc + 0.25 * daupc;
+    double daumc = 4. * (umcrht - umclft) + eps;
+    double daumcs = fmax2(daumc, 0.0);
+    if (aumc <= 0.5 * daumcs) aumc = aumc * aumc / daumc + 0.25 * daumc;
+    double aquu = uurht - uulft;
+    double ruuav = auu * rav;
+    X = std::sqrt(((1. - bSq) * uu) * ((1. - bSq) * uu) + ((4. * bSq) * c2));
+    double R = 0.5 * ((1. - bSq) * uu + X);
+    double S = 0.5 * ((1. - bSq) * uu - X);
+    double b1 = auu * (aq1 - c2i * aq4);
+    double b2 = aupc * (aq4 / R + rav * aquu) / X;
+    double b3 = aumc * (-(aq4 / S) - rav * aquu) / X;
+    double b4 = b1 + b2 + b3;
+    double b5 = (R * b2 + S * b3);
+    double b6 = ruuav * (aq2 - r1 * aquu);
+    double b7 = ruuav * (aq3 - r2 * aquu);
+    aq1 = b4;
+    aq2 = uav * b4 + r1 * b5 + b6;
+    aq3 = vav * b4 + r2 * b5 + b7;
+    aq4 = hav * b4 + uumxt * b5 + uav * b6 + vav * b7 - c2 * b1 / gm1;
+    double aj = 0.5 * rr;
+    double plar = plft + prht;
+    double eplft = elft + plft, eprht = erht + prht;
+    double fssub = 0.0;
+    L.f[1][i] = aj * (rlft * uulft + rrht * uurht - aq1) - fssub * p.rinf;
+    L.f[2][i] = aj * (rulft * uulft + rurht * uurht + r1 * plar - aq2) - fssub * p.rinf * p.uinf;
+    L.f[3][i] = aj * (rvlft * uulft + rvrht * uurht + r2 * plar - aq3) - fssub * p.rinf * p.vinf;
+    L.f[4][i] = aj * (eplft * uulft + eprht * uurht - r3 * plar - aq4) - fssub * p.einf;
+  }
+}
+
 static void reconstruct(const P& p, Line& L, int n, double th, double qt, double eps, double epsl) {
   int ilima = std::abs(p.ilim);
   if (ilima == 0) iflux(L, 1, n, qt);
@@ -231,7 +320,7 @@ static void reconstruct(const P& p, Line& L, int n, double th, double qt, double
   (void)eps;
 }
 
-/* eulerrhs.f:2-280 with nei=1, iprecon=.false. */
+/* eulerrhs.f:2-280 with nei=1 */
 void rhsup(const P& p, A3 q, A3 s, const double* xv_, const double* yv_, I2 iblank,
            const double* ugv_, const double* vgv_, const double* xold_, const double* yold_,
            const double* xole_, const double* yole_) {
@@ -301,7 +390,8 @@ void rhsup(const P& p, A3 q, A3 s, const double* xv_, const double* yv_, I2 ibla
     } else {
       for (int j = p.jbeg - 1; j <= p.jend; ++j) L.tj[j] = 0.0;
     }
-    roeflx(p, L, p.jbeg - 1, p.jend);
+    if (p.iprecon) roetrklflx(p, L, p.jbeg - 1, p.jend);
+    else roeflx(p, L, p.jbeg - 1, p.jend);
     for (int j = p.jbeg; j <= p.jend; ++j)
       for (int n = 1; n <= 4; ++n) s(j, k, n) = s(j, k, n) - (L.f[n][j] - L.f[n][j - 1]);
   }
@@ -347,7 +437,8 @@ void rhsup(const P& p, A3 q, A3 s, const double* xv_, const double* yv_, I2 ibla
     } else {
       for (int k = p.kbeg - 1; k <= p.kend; ++k) L.tj[k] = 0.;
     }
-    roeflx(p, L, p.kbeg - 1, p.kend);
+    if (p.iprecon) roetrklflx(p, L, p.kbeg - 1, p.kend);
+    else roeflx(p, L, p.kbeg - 1, p.kend);
     for (int k = p.kbeg; k <= p.kend; ++k)
       for (int n = 1; n <= 4; ++n) s(j, k, n) = s(j, k, n) - (L.f[n][k] - L.f[n][k - 1]);
   }

@@ -12,7 +12,10 @@
 namespace oro {
 
 /* time.f:2-108, one time instance (the reference loops nsp outside) */
-void time_step(const P& p, A3 q, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 tscale, A2 bt, I2 iblank) {
+void time_step(const P& pin, A3 q, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 tscale, A2 bt, I2 iblank) {
+  // time.f:30-35: time-accurate preconditioning switches to dual time
+  P p = pin;
+  if (p.iprecon && (p.timeac == 1 && !p.timespectral)) { p.idual = 1; p.idual_turb = 1; }
   const int jd = p.jd, kd = p.kd, nq = p.nq;
   double oat = 1.0;
   if (p.ntac >= 2 && p.istep > 1) oat = 2. / 3.;
@@ -31,6 +34,8 @@ void time_step(const P& p, A3 q, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 ts
       for (int k = 1; k <= kd; ++k) for (int j = 1; j <= jd; ++j) {
         double ib = (double)(iblank(j, k) > 0 ? iblank(j, k) : 0);
         tscale(j, k) = ib * (1.0 + jac_factor * std::sqrt(q(j, k, nq))) / (1.0 + std::sqrt(q(j, k, nq)));
+        if (p.iprecon)   // time.f:62-66
+          tscale(j, k) = 100. * ib * (1.0 + 0.005 * std::sqrt(q(j, k, nq))) / (1.0 + std::sqrt(q(j, k, nq)));
         tscale(j, k) = tscale(j, k) * p.dualtime;
         bt(j, k) = 1. / (1. + tscale(j, k) / h / oat);
         tscale(j, k) = tscale(j, k) / (1. + tscale(j, k) / h / oat);
@@ -202,6 +207,174 @@ void ilu2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
       q(j, k, 2) = q(j, k, 2) * q(j, k, 1);
       q(j, k, 3) = q(j, k, 3) * q(j, k, 1);
       q(j, k, 4) = q(j, k, 4) * q(j, k, 1);
+    }
+}
+
+/* lhs.f:2-467 (preilu2d): ilu2d with Turkel's low-Mach preconditioner --
+ * the preconditioned spectral radii in the diagonal and in the chk / spec
+ * split, and every neighbour contribution multiplied by the preconditioner
+ * (the same transform as rhslom) before its spec term */
+void preilu2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, A2 tscale, A2 bt) {
+  const int jd = p.jd, kd = p.kd, nq = p.nq;
+  const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
+  const double gamma = p.gamma, gm1 = p.gm1, ggm1 = p.ggm1, Mp2 = p.Mp * p.Mp;
+  size_t n2 = (size_t)jd * kd;
+  std::vector<double> d_(n2), uv_(n2), vn_(n2), ge_(n2), qx_(n2), qy_(n2), cx_(n2), cy_(n2), st_(n2 * 4);
+  A2 d{d_.data(), jd}, uv{uv_.data(), jd}, vn{vn_.data(), jd}, ge{ge_.data(), jd};
+  A2 qx{qx_.data(), jd}, qy{qy_.data(), jd}, cx{cx_.data(), jd}, cy{cy_.data(), jd};
+  A3 st{st_.data(), jd, n2};
+  int mdim = (jd > kd ? jd : kd) + 2;
+  std::vector<double> a_[5], b_[5];
+  for (int n = 1; n <= 4; ++n) { a_[n].assign(mdim, 0.); b_[n].assign(mdim, 0.); }
+  std::vector<int> ms(js + ks + je + ke + 2), me(js + ks + je + ke + 2);
+  double eps2 = p.epse * 2., epsv = 1. + eps2;
+  for (int m = js + ks; m <= je + ke; ++m) {
+    ms[m] = (js > m - ke) ? js : m - ke;
+    me[m] = (je < m - js) ? je : m - js;
+  }
+  auto bsq = [&](int j, int k) { return Mp2 / (bt(j, k) - Mp2 * (bt(j, k) - 1)); };
+  for (int k = ks - 1; k <= ke + 1; ++k)
+    for (int j = js - 1; j <= je + 1; ++j) {
+      double dj = 1.0 / q(j, k, 1);
+      q(j, k, 2) = q(j, k, 2) * dj;
+      q(j, k, 3) = q(j, k, 3) * dj;
+      q(j, k, 4) = q(j, k, 4) * dj;
+      q(j, k, 1) = q(j, k, 1) * q(j, k, nq);
+    }
+  for (int k = ks - 1; k <= ke + 1; ++k)
+    for (int j = js - 1; j <= je + 1; ++j) {
+      double uu = q(j, k, 2), vv = q(j, k, 3);
+      double uv2 = 0.5 * (uu * uu + vv * vv);
+      double cjkl = std::sqrt(ggm1 * (q(j, k, 4) - uv2));
+      double rj1 = xx(j, k), rj2 = xy(j, k);
+      double qq1 = rj1 * uu + rj2 * vv;
+      double qqx = std::fabs(-rj1 * ug(j, k) - rj2 * vg(j, k) + qq1);
+      double rr1 = std::sqrt(p2(rj1) + p2(rj2));
+      double rk1 = yx(j, k), rk2 = yy(j, k);
+      double qq2 = rk1 * uu + rk2 * vv;
+      double qqy = std::fabs(-rk1 * ug(j, k) - rk2 * vg(j, k) + qq2);
+      double rr2 = std::sqrt(p2(rk1) + p2(rk2));
+      double vnu = 2.0 * rr2 * rr2 * (p.rmue + turmu(j, k)) / (p.rey * q(j, k, 1));
+      double svt = tscale(j, k);
+      ge(j, k) = gamma * q(j, k, 4) - gm1 * uv2;
+      uv(j, k) = uv2; qx(j, k) = qq1; cx(j, k) = cjkl * rr1;
+      qy(j, k) = qq2; cy(j, k) = cjkl * rr2; vn(j, k) = vnu;
+      double bSq = bsq(j, k);
+      double X = std::sqrt(((1. - bSq) * qqx) * ((1. - bSq) * qqx) + ((4. * bSq) * cx(j, k)) * cx(j, k));
+      double term = 0.5 * ((bSq + 1.) * qqx + X);
+      double Y = std::sqrt(((1. - bSq) * qqy) * ((1. - bSq) * qqy) + ((4. * bSq) * cy(j, k)) * cy(j, k));
+      term = term + 0.5 * ((bSq + 1.) * qqy + Y);
+      d(j, k) = 1.0 / (1.0 + svt * (term * epsv + vnu));
+    }
+  for (int k = ks; k <= ke; ++k) for (int n = 1; n <= 4; ++n) s(js - 1, k, n) = s(js - 1, k, n) * d(js - 1, k);
+  for (int k = ks; k <= ke; ++k) for (int n = 1; n <= 4; ++n) s(je + 1, k, n) = s(je + 1, k, n) * d(je + 1, k);
+  for (int j = js; j <= je; ++j) for (int n = 1; n <= 4; ++n) s(j, ks - 1, n) = s(j, ks - 1, n) * d(j, ks - 1);
+  for (int j = js; j <= je; ++j) for (int n = 1; n <= 4; ++n) s(j, ke + 1, n) = s(j, ke + 1, n) * d(j, ke + 1);
+  for (int k = ks - 1; k <= ke + 1; ++k)
+    for (int j = js - 1; j <= je + 1; ++j)
+      for (int n = 1; n <= 4; ++n) st(j, k, n) = s(j, k, n);
+  if (p.iunst == 2) { std::fprintf(stderr, "oracle: preilu2d iunst=2 not restated\n"); std::abort(); }
+  // one neighbour's contribution (lhs.f:178-208): convective split, the
+  // preconditioner, then +/- spec * s
+  auto contrib = [&](int jn, int kn, double ri1, double ri2, double qq, double cc, const double* vnu, bool fwd,
+                     double* out) {
+    double uu = q(jn, kn, 2), vv = q(jn, kn, 3), uv2 = uv(jn, kn);
+    double qqn = -ri1 * ug(jn, kn) - ri2 * vg(jn, kn) + qq;
+    double bSq = bsq(jn, kn);
+    double X = std::sqrt(((1. - bSq) * qqn) * ((1. - bSq) * qqn) + ((4. * bSq) * cc) * cc);
+    double chk = fwd ? 0.5 + fsign(0.5, (bSq + 1.) * qqn + X) : 0.5 - fsign(0.5, (bSq + 1.) * qqn - X);
+    double sp1 = 0.5 * ((bSq + 1.) * std::fabs(qqn) + X);
+    double sm2 = eps2 * sp1;
+    double spec = vnu ? chk * sp1 + *vnu + sm2 : chk * sp1 + sm2;
+    double s1 = s(jn, kn, 1), s2 = s(jn, kn, 2), s3 = s(jn, kn, 3), s4 = s(jn, kn, 4);
+    double a4 = chk * (ri1 * s2 + ri2 * s3 - qq * s1);
+    double a2 = chk * gm1 * (uv2 * s1 - (uu * s2 + vv * s3) + s4);
+    double t[5];
+    t[1] = a4 + chk * qqn * s1;
+    t[2] = ri1 * a2 + uu * a4 + chk * qqn * s2;
+    t[3] = ri2 * a2 + vv * a4 + chk * qqn * s3;
+    t[4] = qq * a2 + ge(jn, kn) * a4 + chk * qqn * s4;
+    double r[5];
+    r[1] = uv(jn, kn) * t[1] - uu * t[2] - vv * t[3] + t[4];
+    r[2] = uu * r[1];
+    r[3] = vv * r[1];
+    r[4] = ge(jn, kn) * r[1];
+    double cjkl = std::sqrt(ggm1 * (q(jn, kn, 4) - uv(jn, kn)));
+    double term = gm1 * (bSq - 1.) / (cjkl * cjkl);
+    for (int n = 1; n <= 4; ++n) {
+      r[n] = r[n] * term;
+      r[n] = r[n] + t[n];
+    }
+    double sv4[5] = {0, s1, s2, s3, s4};
+    for (int n = 1; n <= 4; ++n) out[n] = fwd ? r[n] + spec * sv4[n] : r[n] - spec * sv4[n];
+  };
+  double c[5];
+  /* forward sweep */
+  for (int m = js + ks; m <= je + ke; ++m) {
+    for (int j = ms[m]; j <= me[m]; ++j) {
+      int k = m - j, j1 = j - 1;
+      contrib(j1, k, xx(j1, k), xy(j1, k), qx(j1, k), cx(j1, k), nullptr, true, c);
+      for (int n = 1; n <= 4; ++n) a_[n][j] = c[n];
+    }
+    for (int j = ms[m]; j <= me[m]; ++j) {
+      int k = m - j, k1 = k - 1;
+      contrib(j, k1, yx(j, k1), yy(j, k1), qy(j, k1), cy(j, k1), &vn(j, k1), true, c);
+      for (int n = 1; n <= 4; ++n) b_[n][j] = c[n];
+    }
+    for (int j = ms[m]; j <= me[m]; ++j) {
+      int k = m - j;
+      double svt = tscale(j, k), sv = svt * 0.5, di = d(j, k);
+      for (int n = 1; n <= 4; ++n) s(j, k, n) = (st(j, k, n) + sv * (a_[n][j] + b_[n][j])) * di;
+    }
+  }
+  /* backward sweep */
+  for (int m = je + ke; m >= js + ks; --m) {
+    for (int j = ms[m]; j <= me[m]; ++j) {
+      int k = m - j, j1 = j + 1;
+      contrib(j1, k, xx(j1, k), xy(j1, k), qx(j1, k), cx(j1, k), nullptr, false, c);
+      for (int n = 1; n <= 4; ++n) a_[n][j] = c[n];
+    }
+    for (int j = ms[m]; j <= me[m]; ++j) {
+      int k = m - j, k1 = k + 1;
+      contrib(j, k1, yx(j, k1), yy(j, k1), qy(j, k1), cy(j, k1), &vn(j, k1), false, c);
+      for (int n = 1; n <= 4; ++n) b_[n][j] = c[n];
+    }
+    for (int j = ms[m]; j <= me[m]; ++j) {
+      int k = m - j;
+      double svt = tscale(j, k), sv = svt * 0.5, di = d(j, k);
+      for (int n = 1; n <= 4; ++n) s(j, k, n) = s(j, k, n) - sv * (a_[n][j] + b_[n][j]) * di;
+    }
+  }
+  for (int k = ks - 1; k <= ke + 1; ++k)
+    for (int j = js - 1; j <= je + 1; ++j) {
+      q(j, k, 1) = q(j, k, 1) / q(j, k, nq);
+      q(j, k, 2) = q(j, k, 2) * q(j, k, 1);
+      q(j, k, 3) = q(j, k, 3) * q(j, k, 1);
+      q(j, k, 4) = q(j, k, 4) * q(j, k, 1);
+    }
+}
+
+/* sources.f:97-148 (rhslom): the residual multiplied by the low-Mach
+ * preconditioner on the interior */
+void rhslom(const P& p, A3 q, A3 s, A2 bt) {
+  const double gamma = p.gamma, gm1 = p.gm1, Mp2 = p.Mp * p.Mp;
+  for (int j = p.jbeg; j <= p.jend; ++j)
+    for (int k = p.kbeg; k <= p.kend; ++k) {
+      double u = q(j, k, 2) / q(j, k, 1);
+      double v = q(j, k, 3) / q(j, k, 1);
+      double phiSq = 0.5 * (u * u + v * v);
+      double ge = q(j, k, 4) / q(j, k, 1) * gamma - phiSq * gm1;
+      double aSq = (q(j, k, 4) / q(j, k, 1) - phiSq) * gm1 * gamma;
+      double tmp[5] = {0, s(j, k, 1), s(j, k, 2), s(j, k, 3), s(j, k, 4)};
+      s(j, k, 1) = phiSq * tmp[1] - u * tmp[2] - v * tmp[3] + tmp[4];
+      s(j, k, 2) = u * s(j, k, 1);
+      s(j, k, 3) = v * s(j, k, 1);
+      s(j, k, 4) = ge * s(j, k, 1);
+      double bSq = Mp2 / (bt(j, k) - Mp2 * (bt(j, k) - 1));
+      for (int n = 1; n <= 4; ++n) {
+        s(j, k, n) = s(j, k, n) * (gm1 * (bSq - 1.) / aSq);
+        s(j, k, n) = s(j, k, n) + tmp[n];
+      }
     }
 }
 

@@ -297,15 +297,21 @@ int oro_step_u(const P* pp, double* q, double* s, double* x, double* y, const do
   for (int nsp = 1; nsp <= nspec; ++nsp) {
     size_t o = (size_t)(nsp - 1) * n2;
     A3 qn = v3(pp, q + o), sn = v3(pp, s + o), ssn = v3(pp, ss.data() + o);
+    if (p.iprecon) rhslom(p, qn, sn, v2(pp, bt + o));   // step.f:121-123
     for (int k = p.kbeg; k <= p.kend; ++k) for (int j = p.jbeg; j <= p.jend; ++j)
       for (int n = 1; n <= p.nv; ++n) sn(j, k, n) = sn(j, k, n) + ssn(j, k, n);
     rbc(p, qn, sn);
     A2 ts = v2(pp, tscale + o);
     for (int k = 1; k <= kd; ++k) for (int j = 1; j <= jd; ++j)
       for (int n = 1; n <= 4; ++n) sn(j, k, n) = sn(j, k, n) * ts(j, k);
-    if (p.ilhs == 1) {
+    if (p.ilhs == 1 && p.iprecon) {
+      preilu2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o),
+               v2(pp, vg + o), v2(pp, turmu + o), ts, v2(pp, bt + o));
+    } else if (p.ilhs == 1) {
       ilu2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
             v2(pp, turmu + o), ts);
+    } else if ((p.ilhs == 2 || p.ilhs == 3) && p.iprecon) {
+      std::fprintf(stderr, "oracle: arc2d_precon not restated\n"); std::abort();
     } else if (p.ilhs == 2 || p.ilhs == 3) {
       arc2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
             v2(pp, turmu + o), I2{iblank + o, jd}, ts, v2(pp, bt + o));
@@ -363,6 +369,9 @@ int oro_solve(const P* pin, const double* xv1, const double* yv1, int nsteps, do
 int oro_solve_from(const P* pin, const double* xv1, const double* yv1, int nsteps, double orders,
                    const double* q_init, int istep0_init, double* hist, double* forces, double* q_out) {
   P p = *pin;
+  // time.f:30-35 sets idual / idual_turb in the module the first time the
+  // time step runs; the turbulence model sees them from then on
+  if (p.iprecon && (p.timeac == 1 && !p.timespectral)) { p.idual = 1; p.idual_turb = 1; }
   const int jd = p.jd, kd = p.kd, nspec = p.nspec, jmax = p.jmax, kmax = p.kmax;
   size_t n2 = (size_t)jd * kd, nv2 = n2 * nspec, nvert = (size_t)jmax * kmax;
   std::vector<double> q(nv2 * p.nq), s(nv2 * p.nv), x(nv2), y(nv2), xx(nv2), xy(nv2), yx(nv2), yy(nv2);

@@ -690,7 +690,7 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
               double* yv, int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
               double* ugv, double* vgv, double* xold, double* yold, double* xole, double* yole, double* turmu,
               double* tscale, double* bt, double* Ds, int32_t* im, int32_t* jd, int32_t* kd) {
-  (void)qtn; (void)qtnm1; (void)im; (void)bt;
+  (void)qtn; (void)qtnm1; (void)im;
   const int nspec = g_ctx.has ? g_ctx.P.nspec : 1;
   int err = 0;
   if (prepare(nspec, err)) return fail(err);
@@ -714,6 +714,8 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   double* dug = (p.timespectral || swept) ? (double*)resolve(ug, qs * 8, true, false, err) : nullptr;
   double* dvg = (p.timespectral || swept) ? (double*)resolve(vg, qs * 8, true, false, err) : nullptr;
   double* dqn = newton ? (double*)resolve(qnewt, qs * p.nv * 8, true, false, err) : nullptr;
+  // bt of time_step (far-field BC, preconditioner); 1 when not given
+  double* dbt = bt ? (double*)resolve(bt, qs * 8, true, false, err) : nullptr;
   if (newton && !err) {
     // newton's 1/(oat*h) (time.f:195-200) for the residual kernel
     double oat = 1.0;
@@ -754,7 +756,7 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
     S.xx = S.xx64 = dxx + o; S.xy = S.xy64 = dxy + o; S.yx = S.yx64 = dyx + o; S.yy = S.yy64 = dyy + o;
     S.ug = S.ug64 = dug ? dug + o : nullptr; S.vg = S.vg64 = dvg ? dvg + o : nullptr;
     S.turmu = dturmu + o; S.tscale = dts + o;
-    S.bt = nullptr;  // bt is 1 on the non-preconditioned path
+    S.bt = dbt ? dbt + o : nullptr;
     S.fxa = e; S.fya = e + ws; S.gxa = e + 2 * ws; S.gya = e + 3 * ws;
     S.ftj = (p.timespectral || swept) ? e + 4 * ws : nullptr; S.gtj = (p.timespectral || swept) ? e + 5 * ws : nullptr;
     S.qnewt = dqn ? dqn + o : nullptr;

@@ -179,8 +179,15 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
                         p.dt > 0 && p.h > 0))
     return OT2D_ERR_ARG;
   if (p.itnmax < 1 || (p.itnmax > 1 && p.iunst != 1)) return OT2D_ERR_ARG;
+  // Turkel preconditioning with the LU-SGS operator (preilu2d); the
+  // preconditioned ADI (arc2d_precon) is not built
+  if (p.iprecon && (p.ilhs != 1 || !(p.Mp > 0))) return OT2D_ERR_ARG;
   d = DevSolve{};
   d.P = p; d.precision = precision; d.nspec = p.nspec;
+  // time.f:30-35: with time-accurate low-Mach preconditioning the time step
+  // switches the module to dual time stepping (idual, idual_turb = 1) the
+  // first time it runs; every later routine sees the switched values
+  if (d.P.iprecon && d.P.timeac == 1 && !d.P.timespectral) { d.P.idual = 1; d.P.idual_turb = 1; }
   d.n2 = (size_t)p.jd * p.kd; d.nvert = (size_t)p.jmax * p.kmax; d.wstride = (d.n2 + 63) / 64 * 64;
   std::vector<std::pair<const char*, size_t>> offs;
   d.bytes = plan(p, precision, [&](const char* n, size_t o) { offs.emplace_back(n, o); });
@@ -277,7 +284,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
   }
   bool bad = false;
   auto chk = [&](cudaError_t e) { if (e != cudaSuccess) bad = true; };
-  chk(cudaMemcpyAsync(d.dP, &p, sizeof(p), cudaMemcpyHostToDevice, st));
+  chk(cudaMemcpyAsync(d.dP, &d.P, sizeof(d.P), cudaMemcpyHostToDevice, st));
   chk(cudaMemcpyAsync(d.q64, q.data(), q.size() * 8, cudaMemcpyHostToDevice, st));
   chk(cudaMemcpyAsync(d.xx64, xx.data(), qs * 8, cudaMemcpyHostToDevice, st));
   chk(cudaMemcpyAsync(d.xy64, xy.data(), qs * 8, cudaMemcpyHostToDevice, st));

@@ -157,13 +157,19 @@ static __device__ void trkl_cell(const ot2d_params& p, QV q, int j, int k, int j
 }
 
 // Apply the q boundary conditions of one slice.  Called by all threads of
-// one CTA; `bt` is the (FP64) time-step factor array (== 1 on the path).
+// one CTA; bt64: the time-step factor bt of time.f (FP64) given by the
+// caller, else the slice's own bt array, else 1 (bt enters the Turkel-form
+// far field through bSq = Mp**2/(bt - Mp**2*(bt-1)))
 template <class R>
 __device__ void bc_slice(const Slice<R>& S, const double* bt64, int istep0) {
   const ot2d_params& p = *S.P;
   const int jd = p.jd;
   QV q{S.q64, jd, S.qs};
   const double *xx = S.xx64, *xy = S.xy64, *yx = S.yx64, *yy = S.yy64, *ug = S.ug64, *vg = S.vg64;
+  auto btv = [&](int j, int k) -> double {
+    const int64_t o = at(jd, j, k);
+    return bt64 ? bt64[o] : (S.bt ? (double)S.bt[o] : 1.0);
+  };
   for (int ib = 0; ib < p.nbc; ++ib) {
     int js, je, ks, ke; bc_range(p, ib, js, je, ks, ke);
     const int idir = p.ibdir[ib], t = p.ibtyp[ib], iadd = isign1(idir), iadir = idir < 0 ? -idir : idir;
@@ -188,7 +194,7 @@ __device__ void bc_slice(const Slice<R>& S, const double* bt64, int istep0) {
         for (int k = ks + threadIdx.x; k <= ke; k += blockDim.x) {
           int j = (idir == 1) ? je : js, j1 = j + iadd, j2 = j1 + iadd;
           trkl_cell(p, q, j, k, j1, k, j2, k, xx[at(jd, j, k)], xy[at(jd, j, k)], ug ? ug[at(jd, j, k)] : 0.0,
-                    vg ? vg[at(jd, j, k)] : 0.0, bt64 ? bt64[at(jd, j, k)] : 1.0, iadd);
+                    vg ? vg[at(jd, j, k)] : 0.0, btv(j, k), iadd);
           for (int jc = 1; jc <= je - js; ++jc) {
             int jx = (idir == 1) ? je - jc : js + jc;
             extrap_prim(p, q, jx, k, jx + iadd, k, jx + 2 * iadd, k, 0.0);
@@ -198,7 +204,7 @@ __device__ void bc_slice(const Slice<R>& S, const double* bt64, int istep0) {
         for (int j = js + threadIdx.x; j <= je; j += blockDim.x) {
           int k = (idir == 2) ? ke : ks, k1 = k + iadd, k2 = k1 + iadd;
           trkl_cell(p, q, j, k, j, k1, j, k2, yx[at(jd, j, k)], yy[at(jd, j, k)], ug ? ug[at(jd, j, k)] : 0.0,
-                    vg ? vg[at(jd, j, k)] : 0.0, bt64 ? bt64[at(jd, j, k)] : 1.0, iadd);
+                    vg ? vg[at(jd, j, k)] : 0.0, btv(j, k), iadd);
           for (int kc = 1; kc <= ke - ks; ++kc) {
             int kx = (idir == 2) ? ke - kc : ks + kc;
             extrap_prim(p, q, j, kx, j, kx + iadd, j, kx + 2 * iadd, 0.0);

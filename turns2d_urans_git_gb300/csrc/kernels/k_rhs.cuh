@@ -24,6 +24,7 @@ __device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
       S.bt[o] = (R)1.;
     } else {
       R t = ib * ((R)1.0 + jac_factor * sqrt(J)) / ((R)1.0 + sqrt(J));
+      if (p.iprecon) t = (R)100. * ib * ((R)1.0 + (R)0.005 * sqrt(J)) / ((R)1.0 + sqrt(J));   // time.f:62-66
       t = t * (R)p.dualtime;
       S.bt[o] = (R)1. / ((R)1. + t / h / oat);
       S.tscale[o] = t / ((R)1. + t / h / oat);
