@@ -103,6 +103,16 @@ int ot2d_time_step(double* q, double* xx, double* xy, double* yx, double* yy, do
 int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
                double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu,
                double* tscale);
+/* src/lhs.f:2-3: ilu2d with Turkel's low-Mach preconditioner (bSq =
+ * Mp**2/(bt - Mp**2 (bt-1)) per cell, Mp from the params whatever iprecon
+ * says); bt as time_step wrote it */
+int ot2d_preilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+                  double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu,
+                  double* tscale, double* bt);
+/* src/sources.f:97: the residual s(1:4) of the interior cells multiplied by
+ * the low-Mach preconditioner */
+int ot2d_rhslom(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+                double* bt);
 /* src/lhs.f:817-818: pentadiagonal lhsinv (lhs.f:1536-1816), or the
  * upwind-split lhsinv_up (lhs.f:1333-1533) when params ilhs = 3 */
 int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
@@ -121,7 +131,9 @@ int ot2d_timespectralrhs(double* q, double* s, double* Ds, int32_t* jd, int32_t*
 /* src/step.f:2-7 (full arrays over nspec; norms of the last call via
  * ot2d_last_norms).  Time accurate (iunst = 1): xold..yole give the
  * swept-area face speeds and ug, vg the cell grid speeds; itnmax > 1: qnewt
- * gives newton's physical-time term (time.f:178-210). */
+ * gives newton's physical-time term (time.f:178-210).  iprecon (LU-SGS
+ * only): roetrklflx fluxes, rhslom after the norms and preilu2d, all reading
+ * bt, which must then be given. */
 int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, double* x, double* y, double* xv,
               double* yv, int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
               double* ugv, double* vgv, double* xold, double* yold, double* xole, double* yole, double* turmu,

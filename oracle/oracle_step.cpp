@@ -187,6 +187,12 @@ void oro_ilu2d(const P* p, double* q, double* s, double* xx, double* xy, double*
   ilu2d(*p, v3(p, q), v3(p, s), v2(p, xx), v2(p, xy), v2(p, yx), v2(p, yy), v2(p, ug), v2(p, vg), v2(p, turmu),
         v2(p, tscale));
 }
+void oro_preilu2d(const P* p, double* q, double* s, double* xx, double* xy, double* yx, double* yy, double* ug,
+                  double* vg, double* turmu, double* tscale, double* bt) {
+  preilu2d(*p, v3(p, q), v3(p, s), v2(p, xx), v2(p, xy), v2(p, yx), v2(p, yy), v2(p, ug), v2(p, vg), v2(p, turmu),
+           v2(p, tscale), v2(p, bt));
+}
+void oro_rhslom(const P* p, double* q, double* s, double* bt) { rhslom(*p, v3(p, q), v3(p, s), v2(p, bt)); }
 double oro_vmu_sa(const P* p, double* q, double* s, double* turmu, double* x, double* y, const double* xv, const double* yv,
                   double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* tscale,
                   const int32_t* iblank) {
@@ -372,6 +378,9 @@ int oro_solve_from(const P* pin, const double* xv1, const double* yv1, int nstep
   // time.f:30-35 sets idual / idual_turb in the module the first time the
   // time step runs; the turbulence model sees them from then on
   if (p.iprecon && (p.timeac == 1 && !p.timespectral)) { p.idual = 1; p.idual_turb = 1; }
+  // Turns_overset.f:481: without preconditioning Mp is 1 (the far-field BC
+  // reads it)
+  if (!p.iprecon) p.Mp = 1.0;
   const int jd = p.jd, kd = p.kd, nspec = p.nspec, jmax = p.jmax, kmax = p.kmax;
   size_t n2 = (size_t)jd * kd, nv2 = n2 * nspec, nvert = (size_t)jmax * kmax;
   std::vector<double> q(nv2 * p.nq), s(nv2 * p.nv), x(nv2), y(nv2), xx(nv2), xy(nv2), yx(nv2), yy(nv2);

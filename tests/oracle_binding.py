@@ -49,6 +49,8 @@ def lib():
         L.oro_visrhs.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.oro_time_step.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
         L.oro_ilu2d.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.oro_preilu2d.argtypes = [_P] + [_dp] * 11
+        L.oro_rhslom.argtypes = [_P, _dp, _dp, _dp]
         L.oro_vmu_sa.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
         L.oro_vmu_sa.restype = C.c_double
         L.oro_komegasst.argtypes = [_P] + [_dp] * 14 + [_ip, _dp]

@@ -153,3 +153,55 @@ def test_oracle_against_golden_history(name):
     assert relerr(hist[:, 0], g["hist"]) < 1e-12
     assert relerr(forces[0][:4], g["forces"]) < 1e-12
     assert relerr(q, g["q"]) < 1e-12
+
+
+def test_oracle_precon_reduces_to_plain_at_mp1():
+    """Turkel's preconditioner with Mp = 1 is the identity (bSq = 1): in
+    exact arithmetic roetrklflx is roeflx, rhslom leaves s as it is and
+    preilu2d is ilu2d.  The oracle's preconditioned routines and solve agree
+    with the plain ones to rounding -- a check of the restated eigenvalue
+    split, preconditioner transform and sweep signs."""
+    c = Case(viscous=True, seed=41, fsmach=0.2)
+    c.p.idual, c.p.Mp = 1, 1.0
+    L = ob.lib()
+    L.oro_time_step(C.byref(c.p), ob.ptr(c.q), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug),
+                    ob.ptr(c.vg), ob.ptr(c.tscale), ob.ptr(c.bt), ob.ptr(c.iblank))
+    s0 = np.random.default_rng(5).uniform(-1, 1, c.n2 * c.p.nv) * 1e-4
+    out = {}
+    for pre in (0, 1):
+        q, s = c.q.copy(), s0.copy()
+        args = [ob.ptr(q), ob.ptr(s), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug),
+                ob.ptr(c.vg), ob.ptr(c.turmu), ob.ptr(c.tscale)]
+        if pre:
+            L.oro_preilu2d(C.byref(c.p), *args, ob.ptr(c.bt))
+        else:
+            L.oro_ilu2d(C.byref(c.p), *args)
+        out[pre] = s
+    assert relerr(out[1], out[0]) <= 1e-12
+    s = s0.copy()
+    L.oro_rhslom(C.byref(c.p), ob.ptr(c.q), ob.ptr(s), ob.ptr(c.bt))
+    assert relerr(s, s0) <= 1e-12
+    _, prm, xv, yv = api.cmesh_case(97, 25, naca=(0.0, 0.0, 0.12), ds_wall=1e-3, invisc=1, lamin=1, irhsy=-3, ilim=1,
+                                    ilhs=1, iconstant_cfl=1, idual=1, dt=2.0, fsmach=0.1, alfa=2.0)
+    res = []
+    for pre in (0, 1):
+        prm.iprecon, prm.Mp = pre, 1.0
+        n, hist, forces, q = ob.solve(prm, xv.ravel(), yv.ravel(), 40)
+        assert n == 40
+        res.append(q)
+    assert relerr(res[1], res[0]) <= 1e-12
+
+
+def test_oracle_precon_changes_the_solution_below_mp1():
+    """With Mp < 1 the preconditioned solve runs (no blow-up over 60
+    iterations at M = 0.1) and differs from the plain one."""
+    _, prm, xv, yv = api.cmesh_case(97, 25, naca=(0.0, 0.0, 0.12), ds_wall=1e-3, invisc=1, lamin=1, irhsy=-3, ilim=1,
+                                    ilhs=1, iconstant_cfl=1, idual=1, dt=2.0, fsmach=0.1, alfa=2.0)
+    qs = []
+    for pre, mp in ((0, 1.0), (1, 0.3)):
+        prm.iprecon, prm.Mp = pre, mp
+        n, hist, forces, q = ob.solve(prm, xv.ravel(), yv.ravel(), 60)
+        assert n == 60 and np.all(np.isfinite(q))
+        qs.append(q)
+    n2 = prm.jd * prm.kd
+    assert relerr(qs[1][:4 * n2], qs[0][:4 * n2]) > 5e-7   # Q/J (J itself is the same grid)

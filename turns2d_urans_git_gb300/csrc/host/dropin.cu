@@ -350,6 +350,46 @@ int storeturb_impl(const double* x, const double* y, const int32_t* iblank, doub
   }
   return err;
 }
+// ilu2d (lhs.f:470-814) or, pre = true, preilu2d (lhs.f:2-467) on one time
+// instance: the routine is chosen by the call, not by params iprecon, as the
+// reference's step.f chooses it
+int lusgs_dropin(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+                 double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu, double* tscale,
+                 double* bt, bool pre) {
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !js || !je || !ks || !ke || *js != p.jbeg || *je != p.jend || *ks != p.kbeg || *ke != p.kend)
+    return fail(OT2D_ERR_ARG);
+  if (!q || !s || !xx || !xy || !yx || !yy || !turmu || !tscale || p.iunst == 2 || (pre && !bt))
+    return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.k_mp2 = pre ? p.Mp * p.Mp : -1.0;
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
+  S.xx = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg = (double*)resolve(vg, n2 * 8, true, false, err);
+  S.turmu = (double*)resolve(turmu, n2 * 8, true, false, err);
+  S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
+  if (pre) S.bt = (double*)resolve(bt, n2 * 8, true, false, err);
+  // status word for the sweeps' bounded waits (bit 4: a wait gave up)
+  S.ist = g_ctx.dist;
+  if (!err && cudaMemsetAsync(g_ctx.dist, 0, sizeof(int32_t) * IST_N, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_lusgs<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
+  int32_t ist[IST_N] = {0};
+  if (!err && cudaMemcpyAsync(ist, g_ctx.dist, sizeof(ist), cudaMemcpyDeviceToHost, g_ctx.st) != cudaSuccess)
+    err = OT2D_ERR_CUDA;
+  err = finish(err);
+  if (!err && (ist[2] & 4)) err = fail(OT2D_ERR_TIMEOUT);
+  return err;
+}
 }  // namespace
 }  // namespace ot2d
 
@@ -526,36 +566,33 @@ int ot2d_time_step(double* q, double* xx, double* xy, double* yx, double* yy, do
 int ot2d_ilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
                double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu,
                double* tscale) {
+  return lusgs_dropin(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, tscale, nullptr, false);
+}
+
+int ot2d_preilu2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+                  double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu,
+                  double* tscale, double* bt) {
+  return lusgs_dropin(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, tscale, bt, true);
+}
+
+int ot2d_rhslom(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+                double* bt) {
   int err = 0;
   if (prepare(1, err)) return fail(err);
   const ot2d_params& p = g_ctx.P;
   if (!dims_ok(jd, kd) || !js || !je || !ks || !ke || *js != p.jbeg || *je != p.jend || *ks != p.kbeg || *ke != p.kend)
     return fail(OT2D_ERR_ARG);
-  if (!q || !s || !xx || !xy || !yx || !yy || !turmu || !tscale || p.iunst == 2) return fail(OT2D_ERR_ARG);
+  if (!q || !s || !bt) return fail(OT2D_ERR_ARG);
   const size_t n2 = (size_t)p.jd * p.kd;
   Slice<double> S = base_slice(1, 1, (int64_t)n2);
-  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
+  S.k_mp2 = p.Mp * p.Mp;   // rhslom reads Mp whatever iprecon says
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, false, err);
   S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
-  S.xx = (double*)resolve(xx, n2 * 8, true, false, err);
-  S.xy = (double*)resolve(xy, n2 * 8, true, false, err);
-  S.yx = (double*)resolve(yx, n2 * 8, true, false, err);
-  S.yy = (double*)resolve(yy, n2 * 8, true, false, err);
-  S.ug = (double*)resolve(ug, n2 * 8, true, false, err);
-  S.vg = (double*)resolve(vg, n2 * 8, true, false, err);
-  S.turmu = (double*)resolve(turmu, n2 * 8, true, false, err);
-  S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
-  // status word for the sweeps' bounded waits (bit 4: a wait gave up)
-  S.ist = g_ctx.dist;
-  if (!err && cudaMemsetAsync(g_ctx.dist, 0, sizeof(int32_t) * IST_N, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  S.bt = (double*)resolve(bt, n2 * 8, true, false, err);
   std::vector<Slice<double>> sl{S};
   run_batch(sl, err);
-  if (!err && launch_lusgs<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
-  int32_t ist[IST_N] = {0};
-  if (!err && cudaMemcpyAsync(ist, g_ctx.dist, sizeof(ist), cudaMemcpyDeviceToHost, g_ctx.st) != cudaSuccess)
-    err = OT2D_ERR_CUDA;
-  err = finish(err);
-  if (!err && (ist[2] & 4)) err = fail(OT2D_ERR_TIMEOUT);
-  return err;
+  if (!err && launch_rhslom<double>(g_ctx.batch.d_sl, g_ctx.batch.b, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
 }
 
 int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
@@ -699,6 +736,9 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   if (!dims_ok(jd, kd) || p.ilhs < 1 || p.ilhs > 3 || (p.iunst != 0 && !swept) || (newton && p.timespectral) ||
       (!p.lamin && p.iturb != 1 && p.iturb != 2) || p.itrans != 0)
     return fail(OT2D_ERR_ARG);
+  // Turkel preconditioning: rhslom and preilu2d read bt; the preconditioned
+  // ADI operator (arc2d_precon) is not built
+  if (p.iprecon && (!bt || p.ilhs != 1)) return fail(OT2D_ERR_ARG);
   if (!q || !s || !x || !y || !xv || !yv || !iblank || !xx || !xy || !yx || !yy || !turmu || !tscale) return fail(OT2D_ERR_ARG);
   if (p.timespectral && (!ugv || !vgv || !ug || !vg || !Ds)) return fail(OT2D_ERR_ARG);
   if (swept && (!xold || !yold || !xole || !yole || !ug || !vg)) return fail(OT2D_ERR_ARG);

@@ -188,6 +188,9 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
   // switches the module to dual time stepping (idual, idual_turb = 1) the
   // first time it runs; every later routine sees the switched values
   if (d.P.iprecon && d.P.timeac == 1 && !d.P.timespectral) { d.P.idual = 1; d.P.idual_turb = 1; }
+  // Turns_overset.f:481: without preconditioning Mp is 1 (the far-field BC
+  // reads it)
+  if (!d.P.iprecon) d.P.Mp = 1.0;
   d.n2 = (size_t)p.jd * p.kd; d.nvert = (size_t)p.jmax * p.kmax; d.wstride = (d.n2 + 63) / 64 * 64;
   std::vector<std::pair<const char*, size_t>> offs;
   d.bytes = plan(p, precision, [&](const char* n, size_t o) { offs.emplace_back(n, o); });
@@ -399,9 +402,10 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   // six prefix tables of n+1 entries: cell blocks, k-lines, j-lines, LU
   // record blocks, 32-line groups, residual tiles
   std::vector<int32_t> idx(6 * (n + 1));
-  int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1, maxkd = 1, moving = 0;
+  int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1, maxkd = 1, moving = 0, precon = 0;
   for (int i = 0; i < n; ++i) {
     if (sl[i].xc) moving = 1;
+    if (sl[i].k_mp2 >= (R)0) precon = 1;
     idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl; idx[3 * (n + 1) + i] = lub;
     idx[4 * (n + 1) + i] = grp; idx[5 * (n + 1) + i] = tiles;
     const int jd = sl[i].jd, kd = sl[i].kd;
@@ -436,6 +440,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   if (cudaStreamSynchronize(st) != cudaSuccess) return OT2D_ERR_CUDA;
   b.nslice = n;
   b.moving = moving;
+  b.precon = precon;
   b.cell_blocks = cells;
   b.max_lu_warps = maxw;
   b.max_wall = maxwall;

@@ -35,6 +35,9 @@ struct Slice {
   // the host (slice_consts): reconstruction (eulerrhs.f:40-53), Sutherland
   // and Prandtl factors (visrhs.f:36-44)
   R k_th, k_qt, k_epsl_x, k_epsl_y, k_c2b, k_c2bp, k_prtr, k_gkpr, k_dre, k_gm1, k_ggm1;
+  // Turkel low-Mach preconditioning (iprecon): Mp**2, or -1 without it.
+  // A face has bt = 1 (eulerrhs.f:78, :185), so its bSq is Mp**2 itself.
+  R k_mp2;
   R* w;                              // scratch of this slice (phase dependent)
   R* lurec;                          // LU-SGS sweep records (skewed bands)
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)
@@ -69,6 +72,7 @@ inline void slice_consts(Slice<R>& S, const ot2d_params& p) {
   S.k_dre = (R)(.5 / p.rey);
   S.k_gm1 = (R)p.gm1;
   S.k_ggm1 = (R)p.ggm1;
+  S.k_mp2 = p.iprecon ? (R)(p.Mp * p.Mp) : (R)-1;
 }
 
 // Fortran SIGN(a,b): |a| with the IEEE sign of b (gfortran semantics).

@@ -28,18 +28,20 @@
 
 namespace ot2d {
 
-constexpr int LU_NF = 24;                 // fields per cell record
 // A (band, step) chunk holds the records of the band's 32 lanes one after
 // another (lane-major): lane l's 24 fields are contiguous, so a lane reads
 // four consecutive fields with one (f32) or two (f64) 16-byte shared loads.
 // Each record is padded to LS elements so that the eight lanes of a load
 // phase hit disjoint banks (f32: 112-byte stride, f64: 208-byte stride).
 // (Interleaving 16-byte field groups over the lanes instead was measured
-// slower in the backward sweep.)
-template <class R>
+// slower in the backward sweep.)  With Turkel preconditioning (PRE, the
+// preilu2d operator of lhs.f:2-467) a record carries 8 more fields: the
+// chk*qq products of both sweeps and the preconditioner factor.
+template <class R, bool PRE = false>
 struct LuLay {
-  static constexpr int LS = sizeof(R) == 4 ? 28 : 26;   // elements per lane record
-  static constexpr int CH = 32 * LS;                    // elements per chunk
+  static constexpr int NF = PRE ? 32 : 24;                                   // fields per record
+  static constexpr int LS = sizeof(R) == 4 ? (PRE ? 36 : 28) : (PRE ? 34 : 26);   // elements per lane record
+  static constexpr int CH = 32 * LS;                                         // elements per chunk
 };
 // record fields
 enum {
@@ -47,12 +49,15 @@ enum {
   LF_SV = 4, LF_D = 5, LF_UU = 6, LF_VV = 7, LF_UV2 = 8, LF_GE = 9,
   LF_RI1 = 10, LF_RI2 = 11, LF_RK1 = 12, LF_RK2 = 13, LF_QX = 14, LF_QY = 15,
   LF_FCX = 16, LF_FSX = 17, LF_FCY = 18, LF_FSY = 19,  // forward chk / spec (xi, eta)
-  LF_BCX = 20, LF_BSX = 21, LF_BCY = 22, LF_BSY = 23   // backward chk / spec
+  LF_BCX = 20, LF_BSX = 21, LF_BCY = 22, LF_BSY = 23,  // backward chk / spec
+  // preconditioned records only: chk*qq (xi, eta) and gm1 (bSq-1)/c**2 of
+  // the forward (24..27) and the backward (28..31) sweep
+  LF_PF = 24, LF_PB = 28
 };
 // element offset of field f of lane l within a chunk
-template <class R>
+template <class R, bool PRE = false>
 __host__ __device__ __forceinline__ int lu_idx(int f, int l) {
-  return l * LuLay<R>::LS + f;
+  return l * LuLay<R, PRE>::LS + f;
 }
 
 __host__ __device__ __forceinline__ int lu_nrow(int kd) { return kd - 2; }
@@ -60,39 +65,47 @@ __host__ __device__ __forceinline__ int lu_ncol(int jd) { return jd - 2; }
 __host__ __device__ __forceinline__ int lu_nband(int kd) { return (kd - 2 + 31) / 32; }
 __host__ __device__ __forceinline__ int lu_nstep(int jd) { return jd - 2 + 31; }
 // elements of one slice's record (element size esize bytes): chunks + 4
-// halo-contribution arrays
+// halo-contribution arrays, sized for the larger (preconditioned) layout so
+// that a slice can use either
 __host__ __device__ __forceinline__ int64_t lu_rec_elems(int jd, int kd, int esize) {
-  const int ch = esize == 4 ? LuLay<float>::CH : LuLay<double>::CH;
+  const int ch = esize == 4 ? LuLay<float, true>::CH : LuLay<double, true>::CH;
   return (int64_t)lu_nband(kd) * lu_nstep(jd) * ch + 8 * (int64_t)(lu_nrow(kd) + lu_ncol(jd)) + 64;
 }
 
 // fields f..f+3 of lane l of a chunk (f a multiple of 4) as 16-byte accesses
 template <class R>
 struct Lu4 { R x, y, z, w; };
+template <bool PRE = false>
 __device__ __forceinline__ Lu4<float> lu_ld4(const float* ch, int f, int l) {
-  const float4 v = *reinterpret_cast<const float4*>(ch + lu_idx<float>(f, l));
+  const float4 v = *reinterpret_cast<const float4*>(ch + lu_idx<float, PRE>(f, l));
   return {v.x, v.y, v.z, v.w};
 }
+template <bool PRE = false>
 __device__ __forceinline__ Lu4<double> lu_ld4(const double* ch, int f, int l) {
-  const double2 a = *reinterpret_cast<const double2*>(ch + lu_idx<double>(f, l));
-  const double2 b = *reinterpret_cast<const double2*>(ch + lu_idx<double>(f + 2, l));
+  const double2 a = *reinterpret_cast<const double2*>(ch + lu_idx<double, PRE>(f, l));
+  const double2 b = *reinterpret_cast<const double2*>(ch + lu_idx<double, PRE>(f + 2, l));
   return {a.x, a.y, b.x, b.y};
 }
+template <bool PRE = false>
 __device__ __forceinline__ void lu_st4(float* ch, int f, int l, float a, float b, float c, float d) {
-  *reinterpret_cast<float4*>(ch + lu_idx<float>(f, l)) = make_float4(a, b, c, d);
+  *reinterpret_cast<float4*>(ch + lu_idx<float, PRE>(f, l)) = make_float4(a, b, c, d);
 }
+template <bool PRE = false>
 __device__ __forceinline__ void lu_st4(double* ch, int f, int l, double a, double b, double c, double d) {
-  *reinterpret_cast<double2*>(ch + lu_idx<double>(f, l)) = make_double2(a, b);
-  *reinterpret_cast<double2*>(ch + lu_idx<double>(f + 2, l)) = make_double2(c, d);
+  *reinterpret_cast<double2*>(ch + lu_idx<double, PRE>(f, l)) = make_double2(a, b);
+  *reinterpret_cast<double2*>(ch + lu_idx<double, PRE>(f + 2, l)) = make_double2(c, d);
 }
 
 template <class R>
 struct LuCell {
   R uu, vv, uv2, ge, ri1, ri2, rk1, rk2, qx, cx, qy, cy, vn, ugc, vgc, d;
+  R bsq, term;   // preconditioned: bSq of the cell, gm1 (bSq-1)/c**2
 };
 
-// lhs.f:524-531 (conservative -> primitive) and :535-563 (diagonal)
-template <class R>
+// lhs.f:524-531 (conservative -> primitive) and :535-563 (diagonal); PRE:
+// preilu2d's diagonal (lhs.f:60-101) from the preconditioned spectral radii
+// 0.5 ((bSq+1)|qq| + sqrt(((1-bSq) qq)**2 + 4 bSq cc**2)) of both directions
+template <class R, bool PRE = false>
 __device__ __forceinline__ LuCell<R> lu_cell(const Slice<R>& S, const ot2d_params& p, int j, int k, R epsv) {
   const int64_t o = at(S.jd, j, k), qs = S.qs;
   LuCell<R> c;
@@ -114,9 +127,23 @@ __device__ __forceinline__ LuCell<R> lu_cell(const Slice<R>& S, const ot2d_param
   R rr2 = sqrt(sq(c.rk1) + sq(c.rk2));
   R vnu = (R)2.0 * rr2 * rr2 * ((R)p.rmue + S.turmu[o]) / ((R)p.rey * rho);
   R svt = S.tscale[o];
-  c.d = (R)1.0 / ((R)1.0 + svt * ((qqx + qqy + cjkl * (rr1 + rr2)) * epsv + vnu));
   c.qx = qq1; c.cx = cjkl * rr1; c.qy = qq2; c.cy = cjkl * rr2; c.vn = vnu;
   c.ge = (R)p.gamma * e - (R)p.gm1 * c.uv2;
+  if constexpr (PRE) {
+    const R btv = S.bt[o], mp2 = S.k_mp2;
+    const R bSq = mp2 / (btv - mp2 * (btv - (R)1));
+    const R omb = (R)1. - bSq, opb = bSq + (R)1., fb = (R)4. * bSq;
+    const R X = sqrt((omb * qqx) * (omb * qqx) + (fb * c.cx) * c.cx);
+    R term = (R)0.5 * (opb * qqx + X);
+    const R Y = sqrt((omb * qqy) * (omb * qqy) + (fb * c.cy) * c.cy);
+    term = term + (R)0.5 * (opb * qqy + Y);
+    c.d = (R)1.0 / ((R)1.0 + svt * (term * epsv + vnu));
+    c.bsq = bSq;
+    c.term = (R)p.gm1 * (bSq - (R)1.) / (cjkl * cjkl);
+  } else {
+    c.d = (R)1.0 / ((R)1.0 + svt * ((qqx + qqy + cjkl * (rr1 + rr2)) * epsv + vnu));
+    c.bsq = (R)0; c.term = (R)0;
+  }
   return c;
 }
 
@@ -149,18 +176,64 @@ __device__ __forceinline__ void lu_apply(R chk, R spec, R ri1, R ri2, R qq, R uu
   a[3] = qq * a2 + ge * a4 + spec * s4;
 }
 
+// preilu2d's chk / spec and chk*qq of one direction (lhs.f:160-179,
+// :221-241, :321-340, :382-402): the convective split of the preconditioned
+// eigenvalues (bSq+1) qq/2 +- X/2, X = sqrt(((1-bSq) qq)**2 + 4 bSq cc**2)
 template <class R, bool XI, bool FWD>
+__device__ __forceinline__ void lu_chkspec_pre(const LuCell<R>& c, R eps2, R& chk, R& cq, R& spec) {
+  R ri1 = XI ? c.ri1 : c.rk1, ri2 = XI ? c.ri2 : c.rk2, qq = XI ? c.qx : c.qy, cc = XI ? c.cx : c.cy;
+  R qqn = -ri1 * c.ugc - ri2 * c.vgc + qq;
+  const R bSq = c.bsq, omb = (R)1. - bSq, opb = bSq + (R)1.;
+  R X = sqrt((omb * qqn) * (omb * qqn) + (((R)4. * bSq) * cc) * cc);
+  if (FWD) chk = (R)0.5 + fsign((R)0.5, opb * qqn + X);
+  else chk = (R)0.5 - fsign((R)0.5, opb * qqn - X);
+  R sp1 = (R)0.5 * (opb * fabs(qqn) + X);
+  R sm2 = eps2 * sp1;
+  spec = XI ? chk * sp1 + sm2 : chk * sp1 + c.vn + sm2;
+  cq = chk * qqn;
+}
+
+// preconditioned contribution of a cell with correction s to its neighbour
+// (lhs.f:181-208): the split flux t, then t + term * [u,v,ge]^T
+// [uv2, -u, -v, 1] t (the preconditioner), then +- spec * s
+template <class R, bool FWD>
+__device__ __forceinline__ void lu_apply_pre(R chk, R cq, R spec, R term, R ri1, R ri2, R qq, R uu, R vv, R uv2,
+                                             R ge, R gm1, const R* s, R* a) {
+  R s1 = s[0], s2 = s[1], s3 = s[2], s4 = s[3];
+  R a4 = chk * (ri1 * s2 + ri2 * s3 - qq * s1);
+  R a2 = chk * gm1 * (uv2 * s1 - (uu * s2 + vv * s3) + s4);
+  const R t1 = a4 + cq * s1;
+  const R t2 = ri1 * a2 + uu * a4 + cq * s2;
+  const R t3 = ri2 * a2 + vv * a4 + cq * s3;
+  const R t4 = qq * a2 + ge * a4 + cq * s4;
+  const R r1 = uv2 * t1 - uu * t2 - vv * t3 + t4;
+  const R p1 = r1 * term + t1, p2 = (uu * r1) * term + t2, p3 = (vv * r1) * term + t3, p4 = (ge * r1) * term + t4;
+  if (FWD) {
+    a[0] = p1 + spec * s1; a[1] = p2 + spec * s2; a[2] = p3 + spec * s3; a[3] = p4 + spec * s4;
+  } else {
+    a[0] = p1 - spec * s1; a[1] = p2 - spec * s2; a[2] = p3 - spec * s3; a[3] = p4 - spec * s4;
+  }
+}
+
+template <class R, bool XI, bool FWD, bool PRE = false>
 __device__ __forceinline__ void lu_contrib(const LuCell<R>& c, const R* s, R gm1, R eps2, R* a) {
-  R chk, spec;
-  lu_chkspec<R, XI, FWD>(c, eps2, chk, spec);
-  lu_apply(chk, spec, XI ? c.ri1 : c.rk1, XI ? c.ri2 : c.rk2, XI ? c.qx : c.qy, c.uu, c.vv, c.uv2, c.ge, gm1, s, a);
+  if constexpr (PRE) {
+    R chk, cq, spec;
+    lu_chkspec_pre<R, XI, FWD>(c, eps2, chk, cq, spec);
+    lu_apply_pre<R, FWD>(chk, cq, spec, c.term, XI ? c.ri1 : c.rk1, XI ? c.ri2 : c.rk2, XI ? c.qx : c.qy, c.uu, c.vv,
+                         c.uv2, c.ge, gm1, s, a);
+  } else {
+    R chk, spec;
+    lu_chkspec<R, XI, FWD>(c, eps2, chk, spec);
+    lu_apply(chk, spec, XI ? c.ri1 : c.rk1, XI ? c.ri2 : c.rk2, XI ? c.qx : c.qy, c.uu, c.vv, c.uv2, c.ge, gm1, s, a);
+  }
 }
 
 // ---- kernel 1: records of the interior cells (one thread per (band, step, lane))
 // The record of lane l of chunk (band, t) into ch, the chunk as the warp
 // stages it in shared memory (k_lu_prep stores the staged chunk with
 // contiguous 16-byte accesses).
-template <class R>
+template <class R, bool PRE = false>
 __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_params& p, int band, int t, int l, int scale,
                                              R* ch) {
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd);
@@ -168,13 +241,13 @@ __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_param
   if (r >= nrow || c < 0 || c >= ncol) {
     const R z = (R)0;
 #pragma unroll
-    for (int f = 0; f < LU_NF; f += 4) lu_st4(ch, f, l, z, z, z, z);
+    for (int f = 0; f < LuLay<R, PRE>::NF; f += 4) lu_st4<PRE>(ch, f, l, z, z, z, z);
     return;
   }
   const int j = p.jbeg + c, k = p.kbeg + r;
   const R eps2 = (R)(p.epse * 2.), epsv = (R)1. + eps2;
   const int64_t o = at(S.jd, j, k);
-  LuCell<R> cl = lu_cell(S, p, j, k, epsv);
+  LuCell<R> cl = lu_cell<R, PRE>(S, p, j, k, epsv);
   const R ts = S.tscale[o];
   R sv[4];
 #pragma unroll
@@ -182,25 +255,37 @@ __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_param
     R v = S.s[n * S.qs + o];
     sv[n] = scale ? v * ts : v;
   }
-  lu_st4(ch, LF_S, l, sv[0], sv[1], sv[2], sv[3]);
-  lu_st4(ch, LF_SV, l, ts * (R)0.5, cl.d, cl.uu, cl.vv);
-  lu_st4(ch, LF_UV2, l, cl.uv2, cl.ge, cl.ri1, cl.ri2);
-  lu_st4(ch, LF_RK1, l, cl.rk1, cl.rk2, cl.qx, cl.qy);
+  lu_st4<PRE>(ch, LF_S, l, sv[0], sv[1], sv[2], sv[3]);
+  lu_st4<PRE>(ch, LF_SV, l, ts * (R)0.5, cl.d, cl.uu, cl.vv);
+  lu_st4<PRE>(ch, LF_UV2, l, cl.uv2, cl.ge, cl.ri1, cl.ri2);
+  lu_st4<PRE>(ch, LF_RK1, l, cl.rk1, cl.rk2, cl.qx, cl.qy);
   R a, b, a2, b2;
-  lu_chkspec<R, true, true>(cl, eps2, a, b);
-  lu_chkspec<R, false, true>(cl, eps2, a2, b2);
-  lu_st4(ch, LF_FCX, l, a, b, a2, b2);
-  lu_chkspec<R, true, false>(cl, eps2, a, b);
-  lu_chkspec<R, false, false>(cl, eps2, a2, b2);
-  lu_st4(ch, LF_BCX, l, a, b, a2, b2);
+  if constexpr (PRE) {
+    R q1, q2;
+    lu_chkspec_pre<R, true, true>(cl, eps2, a, q1, b);
+    lu_chkspec_pre<R, false, true>(cl, eps2, a2, q2, b2);
+    lu_st4<PRE>(ch, LF_FCX, l, a, b, a2, b2);
+    lu_st4<PRE>(ch, LF_PF, l, q1, q2, cl.term, (R)0);
+    lu_chkspec_pre<R, true, false>(cl, eps2, a, q1, b);
+    lu_chkspec_pre<R, false, false>(cl, eps2, a2, q2, b2);
+    lu_st4<PRE>(ch, LF_BCX, l, a, b, a2, b2);
+    lu_st4<PRE>(ch, LF_PB, l, q1, q2, cl.term, (R)0);
+  } else {
+    lu_chkspec<R, true, true>(cl, eps2, a, b);
+    lu_chkspec<R, false, true>(cl, eps2, a2, b2);
+    lu_st4(ch, LF_FCX, l, a, b, a2, b2);
+    lu_chkspec<R, true, false>(cl, eps2, a, b);
+    lu_chkspec<R, false, false>(cl, eps2, a2, b2);
+    lu_st4(ch, LF_BCX, l, a, b, a2, b2);
+  }
 }
 
 // halo-contribution arrays after the chunks: A forward [nrow][4], A backward,
 // B forward [ncol][4], B backward
-template <class R>
+template <class R, bool PRE = false>
 __device__ __forceinline__ R* lu_halo(const Slice<R>& S, int which) {
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd);
-  R* base = S.lurec + (int64_t)lu_nband(S.kd) * lu_nstep(S.jd) * LuLay<R>::CH;
+  R* base = S.lurec + (int64_t)lu_nband(S.kd) * lu_nstep(S.jd) * LuLay<R, PRE>::CH;
   switch (which) {
     case 0: return base;
     case 1: return base + 4 * nrow;
@@ -210,7 +295,7 @@ __device__ __forceinline__ R* lu_halo(const Slice<R>& S, int which) {
 }
 
 // ---- kernel 2: halo edges (one thread per cell of the slice)
-template <class R>
+template <class R, bool PRE = false>
 __device__ __forceinline__ void lu_edge_cell(const Slice<R>& S, const ot2d_params& p, int j, int k, int scale) {
   const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
   const bool ij = j >= js && j <= je, ik = k >= ks && k <= ke;
@@ -223,15 +308,15 @@ __device__ __forceinline__ void lu_edge_cell(const Slice<R>& S, const ot2d_param
     for (int n = 0; n < 4; ++n) sv[n] = scale ? S.s[n * S.qs + o] * ts : S.s[n * S.qs + o];
     const bool edge = (ik && (j == js - 1 || j == je + 1)) || (ij && (k == ks - 1 || k == ke + 1));
     if (edge) {
-      LuCell<R> c = lu_cell(S, p, j, k, epsv);
+      LuCell<R> c = lu_cell<R, PRE>(S, p, j, k, epsv);
 #pragma unroll
       for (int n = 0; n < 4; ++n) sv[n] = sv[n] * c.d;
       R a[4];
       R* dst = nullptr;
-      if (j == js - 1) { lu_contrib<R, true, true>(c, sv, gm1, eps2, a); dst = lu_halo(S, 0) + 4 * (k - ks); }
-      else if (j == je + 1) { lu_contrib<R, true, false>(c, sv, gm1, eps2, a); dst = lu_halo(S, 1) + 4 * (k - ks); }
-      else if (k == ks - 1) { lu_contrib<R, false, true>(c, sv, gm1, eps2, a); dst = lu_halo(S, 2) + 4 * (j - js); }
-      else { lu_contrib<R, false, false>(c, sv, gm1, eps2, a); dst = lu_halo(S, 3) + 4 * (j - js); }
+      if (j == js - 1) { lu_contrib<R, true, true, PRE>(c, sv, gm1, eps2, a); dst = lu_halo<R, PRE>(S, 0) + 4 * (k - ks); }
+      else if (j == je + 1) { lu_contrib<R, true, false, PRE>(c, sv, gm1, eps2, a); dst = lu_halo<R, PRE>(S, 1) + 4 * (k - ks); }
+      else if (k == ks - 1) { lu_contrib<R, false, true, PRE>(c, sv, gm1, eps2, a); dst = lu_halo<R, PRE>(S, 2) + 4 * (j - js); }
+      else { lu_contrib<R, false, false, PRE>(c, sv, gm1, eps2, a); dst = lu_halo<R, PRE>(S, 3) + 4 * (j - js); }
 #pragma unroll
       for (int n = 0; n < 4; ++n) dst[n] = a[n];
     }
@@ -316,9 +401,9 @@ constexpr int LU_XB = 128;   // a power of two
 // chunks, its two barriers, its cross-band ring and its progress counter;
 // then the first-row halo contributions of the slice (4 per column, at most
 // maxcol columns).
-template <class R>
+template <class R, bool PRE = false>
 __host__ __device__ __forceinline__ size_t lu_smem_bytes(int nwarp, int G, int maxcol) {
-  return (size_t)nwarp * 2 * G * LuLay<R>::CH * sizeof(R) + (size_t)nwarp * 2 * sizeof(uint64_t) +
+  return (size_t)nwarp * 2 * G * LuLay<R, PRE>::CH * sizeof(R) + (size_t)nwarp * 2 * sizeof(uint64_t) +
          (size_t)nwarp * LU_XB * 4 * sizeof(R) + (size_t)nwarp * sizeof(int) + 16 +
          (size_t)4 * maxcol * sizeof(R);
 }
@@ -333,14 +418,15 @@ __host__ __device__ __forceinline__ size_t lu_smem_bytes(int nwarp, int G, int m
 // goes through the cross-band ring guarded by per-warp progress counters,
 // so the warps run without block-wide barriers.  The records stream in
 // through cp.async.bulk, G chunks per copy, double-buffered.
-template <class R, bool FWD, int G>
+// PRE: the preilu2d records and contributions.
+template <class R, bool FWD, int G, bool PRE = false>
 __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem) {
   const ot2d_params& p = *S.P;
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nb = lu_nband(S.kd), nst = lu_nstep(S.jd);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   const R gm1 = (R)p.gm1;
   R* rings = (R*)smem;
-  constexpr int CH = LuLay<R>::CH;
+  constexpr int CH = LuLay<R, PRE>::CH;
   uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * 2 * G * CH * sizeof(R));
   R* xrings = (R*)(bars + (size_t)nwarp * 2);
   int* prog = (int*)(xrings + (size_t)nwarp * LU_XB * 4);
@@ -368,7 +454,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
     prog[w] = 0;
   }
   {
-    const R* Bg = lu_halo(S, FWD ? 2 : 3);
+    const R* Bg = lu_halo<R, PRE>(S, FWD ? 2 : 3);
     for (int i = threadIdx.x; i < 4 * ncol; i += blockDim.x) bhs[i] = Bg[i];
   }
   __syncthreads();
@@ -377,7 +463,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
     issue(0);
     if (ngrp > 1) issue(1);
   }
-  const R* Ah = lu_halo(S, FWD ? 0 : 1);
+  const R* Ah = lu_halo<R, PRE>(S, FWD ? 0 : 1);
   const R* Bh = bhs;
   // neighbouring bands in sweep order and the boundary lanes
   const int wprev = FWD ? w - 1 : w + 1, wnext = FWD ? w + 1 : w - 1;
@@ -403,8 +489,8 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
       // this lane's record: residual, (tscale/2, d, u, v), (uv2, ge, xi
       // metrics), (eta metrics, qx, qy), this sweep's (chk, spec) pairs
       const R* ch = gring + (FWD ? u : gs - 1 - u) * CH;
-      const Lu4<R> r0 = lu_ld4(ch, LF_S, l), r1 = lu_ld4(ch, LF_SV, l), r2 = lu_ld4(ch, LF_UV2, l),
-                   r3 = lu_ld4(ch, LF_RK1, l), r4 = lu_ld4(ch, FWD ? LF_FCX : LF_BCX, l);
+      const Lu4<R> r0 = lu_ld4<PRE>(ch, LF_S, l), r1 = lu_ld4<PRE>(ch, LF_SV, l), r2 = lu_ld4<PRE>(ch, LF_UV2, l),
+                   r3 = lu_ld4<PRE>(ch, LF_RK1, l), r4 = lu_ld4<PRE>(ch, FWD ? LF_FCX : LF_BCX, l);
       R bin[4];
 #pragma unroll
       for (int n = 0; n < 4; ++n)
@@ -437,15 +523,22 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
         for (int n = 0; n < 4; ++n)
           sn[n] = FWD ? (st[n] + sv * (aprev[n] + bin[n])) * di : st[n] - sv * (aprev[n] + bin[n]) * di;
         if (FWD) {
-          lu_st4(recw + (int64_t)tl * CH, LF_S, l, sn[0], sn[1], sn[2], sn[3]);
+          lu_st4<PRE>(recw + (int64_t)tl * CH, LF_S, l, sn[0], sn[1], sn[2], sn[3]);
         } else {
 #pragma unroll
           for (int n = 0; n < 4; ++n) srow[n * S.qs + c] = sn[n];
         }
         // xi: (chk, spec) = r4.x, r4.y with ri1, ri2, qx; eta: r4.z, r4.w
         // with rk1, rk2, qy; u, v, uv2, ge shared
-        lu_apply(r4.x, r4.y, r2.z, r2.w, r3.z, r1.z, r1.w, r2.x, r2.y, gm1, sn, aprev);
-        lu_apply(r4.z, r4.w, r3.x, r3.y, r3.w, r1.z, r1.w, r2.x, r2.y, gm1, sn, bout);
+        if constexpr (PRE) {
+          // (chk*qq xi, chk*qq eta, preconditioner factor)
+          const Lu4<R> r5 = lu_ld4<PRE>(ch, FWD ? LF_PF : LF_PB, l);
+          lu_apply_pre<R, FWD>(r4.x, r5.x, r4.y, r5.z, r2.z, r2.w, r3.z, r1.z, r1.w, r2.x, r2.y, gm1, sn, aprev);
+          lu_apply_pre<R, FWD>(r4.z, r5.y, r4.w, r5.z, r3.x, r3.y, r3.w, r1.z, r1.w, r2.x, r2.y, gm1, sn, bout);
+        } else {
+          lu_apply(r4.x, r4.y, r2.z, r2.w, r3.z, r1.z, r1.w, r2.x, r2.y, gm1, sn, aprev);
+          lu_apply(r4.z, r4.w, r3.x, r3.y, r3.w, r1.z, r1.w, r2.x, r2.y, gm1, sn, bout);
+        }
       }
       // hand the boundary contribution to the next band (its slot must have
       // been read: the consumer is at least at step tl - LU_XB + 32), then

@@ -233,12 +233,37 @@ __device__ __forceinline__ void rt_visc_xi(const RtSmem<R>& sm, int r, R gkpr, R
   out[5] = f4v;
 }
 
+// rhslom (sources.f:97-148) on one interior cell: s(1:4) times Turkel's
+// low-Mach preconditioner, (I + gm1 (bSq-1)/a**2 * [u,v,ge]^T
+// [phi**2, -u, -v, 1]) s, with bSq = Mp**2/(bt - Mp**2 (bt-1)) of the cell.
+template <class R>
+__device__ __forceinline__ void rhslom_cell(const Slice<R>& S, const ot2d_params& p, int64_t o, R* s) {
+  const int64_t qs = S.qs;
+  const R q1 = S.q[o], gm1 = S.k_gm1, gamma = (R)p.gamma, mp2 = S.k_mp2;
+  const R u = S.q[qs + o] / q1;
+  const R v = S.q[2 * qs + o] / q1;
+  const R phiSq = (R)0.5 * (u * u + v * v);
+  const R ge = S.q[3 * qs + o] / q1 * gamma - phiSq * gm1;
+  const R aSq = (S.q[3 * qs + o] / q1 - phiSq) * gm1 * gamma;
+  const R t1 = s[0], t2 = s[1], t3 = s[2], t4 = s[3];
+  const R a = phiSq * t1 - u * t2 - v * t3 + t4;
+  const R btv = S.bt[o];
+  const R bSq = mp2 / (btv - mp2 * (btv - (R)1));
+  const R f = gm1 * (bSq - (R)1.) / aSq;
+  s[0] = a * f + t1;
+  s[1] = (u * a) * f + t2;
+  s[2] = (v * a) * f + t3;
+  s[3] = (ge * a) * f + t4;
+}
+
 // One tile of the residual (step.f:41-93 for the cells of the tile): tile
 // `tile` of the slice covers interior cells j0..j1 x k0..k1.  flags as for
 // the cell-parallel assembly (AS_*).  Without AS_ACC the tile also zeroes s
 // on the halo cells next to it (step.f:41 zeroes s everywhere).  np receives
-// the thread's norm partial.
-template <class R>
+// the thread's norm partial.  PRE: the slice runs with Turkel's low-Mach
+// preconditioning -- roetrklflx fluxes, and in the full residual (AS_NORM)
+// rhslom applied to each cell after its norm terms (step.f:121-123).
+template <class R, bool PRE>
 __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int flags, NormPart& np) {
   const ot2d_params& p = *S.P;
   const int jd = S.jd, kd = S.kd, t = threadIdx.x;
@@ -249,7 +274,7 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
   const bool visc = (flags & AS_VISC) && !p.invisc;
   const bool inv = flags & AS_INV;
   const R gm1 = S.k_gm1;
-  const Recon<R> rx{p.ilim, S.k_th, S.k_qt, S.k_epsl_x}, ry{p.ilim, S.k_th, S.k_qt, S.k_epsl_y};
+  const Recon<R> rx{p.ilim, S.k_th, S.k_qt, S.k_epsl_x, S.k_mp2}, ry{p.ilim, S.k_th, S.k_qt, S.k_epsl_y, S.k_mp2};
   // A: stage the region
   for (int r = t; r < RT_NR; r += RT_BS) {
     const int j = jr + r % RT_RW, k = kr + r / RT_RW;
@@ -272,7 +297,7 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
       const RtLine<R> L{&sm, (k - kr) * RT_RW - jr, 1, max(1, jr), min(jd, jr + RT_RW - 1), gm1};
       const int64_t o = at(jd, j, k);
       R fl[4];
-      face_flux(L, rx, j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
+      face_flux_p<PRE>(L, rx, j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sm.F[v * (RT_TK * (RT_TJ + 1)) + f] = fl[v];
     } else if (w < nB + nC) {
@@ -284,7 +309,7 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
       const RtLine<R> L{&sm, (j - jr) - kr * RT_RW, RT_RW, max(1, kr), min(kd, kr + RT_RH - 1), gm1};
       const int64_t o = at(jd, j, k);
       R fl[4];
-      face_flux(L, ry, k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
+      face_flux_p<PRE>(L, ry, k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sm.G[v * ((RT_TK + 1) * RT_TJ) + f] = fl[v];
     } else if (w < nB + nC + nD1) {
@@ -412,6 +437,9 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
       const R s1 = s[0] * m, s2 = s[1] * m, s3 = s[2] * m, s4 = s[3] * m;
       np.resrho = (double)(s[0] * s[0]);
       np.rsum = (double)(s1 * s1 + s2 * s2 + s3 * s3 + s4 * s4);
+    }
+    if constexpr (PRE) {
+      if (flags & AS_NORM) rhslom_cell(S, p, o, s);
     }
 #pragma unroll
     for (int n = 0; n < 8; ++n)

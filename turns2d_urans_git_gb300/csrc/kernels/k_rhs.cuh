@@ -113,6 +113,7 @@ template <class R> __device__ __forceinline__ R weno5(R a, R b, R c, R d, R e) {
 template <class R>
 struct Recon {
   int ilim; R th, qt, epsl;
+  R bsq;   // bSq of the faces with Turkel preconditioning (Mp**2), < 0 without
   // muscld_new, eulerrhs.f:855-873 (is=1, imax=n, im=n-1) on the cells
   // i-1, i, i+1 of the line
   __device__ __forceinline__ void muscl3(R wm, R w0, R wp, int i, int n, int ibm, int ib0, int ibp, R& ql,
@@ -245,12 +246,99 @@ __device__ __forceinline__ void roe(R gm1, const R* L, const R* Rr, R ri1, R ri2
   f[3] = aj * (eplft * uulft + eprht * uurht - r3 * plar - aq4) - fssub * z;
 }
 
+// roetrklflx, eulerrhs.f:450-625 (fssub = 0): the Roe flux with Turkel's
+// low-Mach preconditioning.  bSq is the face's Mp**2/(bt - Mp**2*(bt-1))
+// with bt = 1, i.e. Mp**2; the eigenvalues (1+bSq)u/2 +- X/2 with
+// X = sqrt(((1-bSq)u)**2 + 4 bSq c**2) replace u +- c, in the same entropy
+// fix, and the acoustic waves are split with R and S = ((1-bSq)u +- X)/2.
+template <class R>
+__device__ __forceinline__ void roe_turkel(R gm1, R bSq, const R* L, const R* Rr, R ri1, R ri2, R ri3, R* f) {
+  const R eps = (R)1.e-6;
+  R rlft = L[0], ulft = L[1], vlft = L[2], plft = L[3];
+  R rlfti = (R)1.0 / rlft;
+  R rulft = rlft * ulft, rvlft = rlft * vlft;
+  R uvl = (R)0.5 * (ulft * ulft + vlft * vlft);
+  R elft = plft / gm1 + rlft * uvl;
+  R hlft = (elft + plft) * rlfti;
+  R clft = sqrt(gm1 * (hlft - uvl));
+  R rrht = Rr[0], urht = Rr[1], vrht = Rr[2], prht = Rr[3];
+  R rrhti = (R)1.0 / rrht;
+  R rurht = rrht * urht, rvrht = rrht * vrht;
+  R uvr = (R)0.5 * (urht * urht + vrht * vrht);
+  R erht = prht / gm1 + rrht * uvr;
+  R hrht = (erht + prht) * rrhti;
+  R crht = sqrt(gm1 * (hrht - uvr));
+  R rat = sqrt(rrht * rlfti);
+  R rati = (R)1.0 / (rat + (R)1.);
+  R rav = rat * rlft;
+  R uav = (rat * urht + ulft) * rati;
+  R vav = (rat * vrht + vlft) * rati;
+  R hav = (rat * hrht + hlft) * rati;
+  R uv = (R)0.5 * (uav * uav + vav * vav);
+  R cav = sqrt(gm1 * (hav - uv));
+  R aq1 = rrht - rlft, aq2 = urht - ulft, aq3 = vrht - vlft, aq4 = prht - plft;
+  R rr2 = ri1 * ri1 + ri2 * ri2;
+  R rr = sqrt(rr2);
+  R r0 = (R)1.0 / rr;
+  R r1 = ri1 * r0, r2 = ri2 * r0, r3 = ri3 * r0;
+  R uumxt = r1 * uav + r2 * vav;
+  R uu = uumxt + r3;
+  R c2 = cav * cav;
+  R c2i = (R)1.0 / c2;
+  const R omb = (R)1. - bSq, opb = (R)1. + bSq, fb = (R)4. * bSq;
+  R X = sqrt(((omb * uu) * omb) * uu + fb * c2);
+  R auu = fabs(uu);
+  R aupc = (R)0.5 * fabs(opb * uu + X);
+  R aumc = (R)0.5 * fabs(opb * uu - X);
+  R uulft = r1 * ulft + r2 * vlft + r3;
+  R uurht = r1 * urht + r2 * vrht + r3;
+  X = sqrt((omb * uulft) * (omb * uulft) + (fb * clft) * clft);
+  R upclft = (R)0.5 * (opb * uulft + X);
+  R umclft = (R)0.5 * (opb * uulft - X);
+  X = sqrt((omb * uurht) * (omb * uurht) + (fb * crht) * crht);
+  R upcrht = (R)0.5 * (opb * uurht + X);
+  R umcrht = (R)0.5 * (opb * uurht - X);
+  R dauu = (R)4. * (uurht - uulft) + eps;
+  R dauus = fmax2(dauu, (R)0.0);
+  if (auu <= (R)0.5 * dauus) auu = auu * auu / dauu + (R)0.25 * dauu;
+  R daupc = (R)4. * (upcrht - upclft) + eps;
+  R daupcs = fmax2(daupc, (R)0.0);
+  if (aupc <= (R)0.5 * daupcs) aupc = aupc * aupc / daupc + (R)0.25 * daupc;
+  R daumc = (R)4. * (umcrht - umclft) + eps;
+  R daumcs = fmax2(daumc, (R)0.0);
+  if (aumc <= (R)0.5 * daumcs) aumc = aumc * aumc / daumc + (R)0.25 * daumc;
+  R aquu = uurht - uulft;
+  R ruuav = auu * rav;
+  X = sqrt((omb * uu) * (omb * uu) + fb * c2);
+  R Rw = (R)0.5 * (omb * uu + X);
+  R Sw = (R)0.5 * (omb * uu - X);
+  R b1 = auu * (aq1 - c2i * aq4);
+  R b2 = aupc * (aq4 / Rw + rav * aquu) / X;
+  R b3 = aumc * (-(aq4 / Sw) - rav * aquu) / X;
+  R b4 = b1 + b2 + b3;
+  R b5 = (Rw * b2 + Sw * b3);
+  R b6 = ruuav * (aq2 - r1 * aquu);
+  R b7 = ruuav * (aq3 - r2 * aquu);
+  aq1 = b4;
+  aq2 = uav * b4 + r1 * b5 + b6;
+  aq3 = vav * b4 + r2 * b5 + b7;
+  aq4 = hav * b4 + uumxt * b5 + uav * b6 + vav * b7 - c2 * b1 / gm1;
+  R aj = (R)0.5 * rr;
+  R plar = plft + prht;
+  R eplft = elft + plft, eprht = erht + prht;
+  f[0] = aj * (rlft * uulft + rrht * uurht - aq1);
+  f[1] = aj * (rulft * uulft + rurht * uurht + r1 * plar - aq2);
+  f[2] = aj * (rvlft * uulft + rvrht * uurht + r2 * plar - aq3);
+  f[3] = aj * (eplft * uulft + eprht * uurht - r3 * plar - aq4);
+}
+
 // Inviscid flux through one face between cells i and i+1 of a line.  L
 // supplies f4(c, out) (the primitive f of cell c) and iba(c).  LIM is the
 // limiter family (0 central, 1 MUSCL, 4 WENO) so that the central and MUSCL
 // forms index their window with constants only (the window stays in
-// registers); face_flux() dispatches on rc.ilim.
-template <int LIM, class R, class Line>
+// registers); face_flux() dispatches on rc.ilim.  PRE: Turkel's
+// preconditioned flux (roetrklflx) in place of roeflx.
+template <int LIM, class R, class Line, bool PRE = false>
 __device__ __forceinline__ void face_flux_t(const Line& L, const Recon<R>& rc, int i, int n, R ri1, R ri2, R ri3,
                                             R* fout) {
   R ql[4], qr[4];
@@ -303,16 +391,27 @@ __device__ __forceinline__ void face_flux_t(const Line& L, const Recon<R>& rc, i
       }
     }
   }
-  roe(L.gm1, ql, qr, ri1, ri2, ri3, fout);
+  if constexpr (PRE) roe_turkel(L.gm1, rc.bsq, ql, qr, ri1, ri2, ri3, fout);
+  else roe(L.gm1, ql, qr, ri1, ri2, ri3, fout);
 }
 
+// the flux of one face with the limiter of rc.ilim; PRE fixed at compile
+// time (the fused residual is instantiated once per flux)
+template <bool PRE, class R, class Line>
+__device__ __forceinline__ void face_flux_p(const Line& L, const Recon<R>& rc, int i, int n, R ri1, R ri2, R ri3,
+                                            R* fout) {
+  const int ilm = rc.ilim < 0 ? -rc.ilim : rc.ilim;
+  if (rc.ilim == 4) face_flux_t<4, R, Line, PRE>(L, rc, i, n, ri1, ri2, ri3, fout);
+  else if (ilm == 1) face_flux_t<1, R, Line, PRE>(L, rc, i, n, ri1, ri2, ri3, fout);
+  else face_flux_t<0, R, Line, PRE>(L, rc, i, n, ri1, ri2, ri3, fout);
+}
+
+// eulerrhs.f:155-159, :263-267: roetrklflx with iprecon, roeflx without
 template <class R, class Line>
 __device__ __forceinline__ void face_flux(const Line& L, const Recon<R>& rc, int i, int n, R ri1, R ri2, R ri3,
                                           R* fout) {
-  const int ilm = rc.ilim < 0 ? -rc.ilim : rc.ilim;
-  if (rc.ilim == 4) face_flux_t<4>(L, rc, i, n, ri1, ri2, ri3, fout);
-  else if (ilm == 1) face_flux_t<1>(L, rc, i, n, ri1, ri2, ri3, fout);
-  else face_flux_t<0>(L, rc, i, n, ri1, ri2, ri3, fout);
+  if (rc.bsq >= (R)0) face_flux_p<true>(L, rc, i, n, ri1, ri2, ri3, fout);
+  else face_flux_p<false>(L, rc, i, n, ri1, ri2, ri3, fout);
 }
 
 template <class R>
@@ -324,6 +423,7 @@ __device__ __forceinline__ Recon<R> make_recon(const ot2d_params& p, int dir) {
   double ep = (dir == 0) ? 10. / (double)p.jmax : 10. / (double)p.kmax;
   rc.epsl = (R)((ep * ep) * ep);
   rc.ilim = p.ilim;
+  rc.bsq = p.iprecon ? (R)(p.Mp * p.Mp) : (R)-1;
   return rc;
 }
 

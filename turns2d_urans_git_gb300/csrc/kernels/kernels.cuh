@@ -207,15 +207,19 @@ __global__ void __launch_bounds__(CELL_BS) k_assemble(const Slice<R>* __restrict
 
 // Fused residual over tiles of RT_TJ x RT_TK interior cells: slice i owns
 // tiles [tfirst[i], tfirst[i+1]).  Dynamic shared memory: rt_smem_bytes<R>().
-template <class R>
+// PRE selects the preconditioned slices (k_mp2 >= 0); a batch that holds
+// both kinds launches both instantiations, each returning on the other's
+// tiles (a whole block returns, so every tile is done exactly once).
+template <class R, bool PRE>
 __global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 1) k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst,
                                                   int nslice, int flags, NormPart* __restrict__ part) {
   extern __shared__ __align__(16) unsigned char rt_raw[];
   const int si = find_slice(tfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];
+  if ((S.k_mp2 >= (R)0) != PRE) return;
   RtSmem<R> sm(rt_raw);
   NormPart np{0.0, 0.0, 0.0, 0x7fffffffffffffffLL};
-  resid_tile(S, sm, blockIdx.x - tfirst[si], flags, np);
+  resid_tile<R, PRE>(S, sm, blockIdx.x - tfirst[si], flags, np);
   if (!(flags & AS_NORM)) return;
   // deterministic block reduction: a fixed shuffle tree per warp, then the
   // warp partials in warp order
@@ -258,6 +262,22 @@ __global__ void k_norm_final(const Slice<R>* __restrict__ sl, const int32_t* __r
   }
 }
 
+// rhslom alone (sources.f:97-148): the drop-in routine's interior cells
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_rhslom(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+                                                    int nslice) {
+  OT2D_CELL_MAP();
+  const ot2d_params& p = *S.P;
+  if (!inside || j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) return;
+  const int64_t o = at(S.jd, j, k);
+  R s[4];
+#pragma unroll
+  for (int n = 0; n < 4; ++n) s[n] = S.s[(int64_t)n * S.qs + o];
+  rhslom_cell(S, p, o, s);
+#pragma unroll
+  for (int n = 0; n < 4; ++n) S.s[(int64_t)n * S.qs + o] = s[n];
+}
+
 template <class R>
 __global__ void k_rbc(const Slice<R>* __restrict__ sl) {
   const Slice<R>& S = sl[blockIdx.x];
@@ -270,20 +290,23 @@ __global__ void k_rbc(const Slice<R>* __restrict__ sl) {
 // A warp builds one chunk: each lane writes its record into the warp's
 // shared-memory copy of the chunk, then the warp stores the chunk with
 // contiguous 16-byte accesses (full sectors; the lane-major records would
-// otherwise be written with a 112- / 208-byte stride).
-template <class R>
+// otherwise be written with a 112- / 208-byte stride).  PRE: the
+// preconditioned (preilu2d) records of the slices with k_mp2 >= 0; each
+// instantiation returns on the other kind's slices.
+template <class R, bool PRE>
 __global__ void __launch_bounds__(CELL_BS) k_lu_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst,
                                                      int nslice, int scale, int only_lu) {
   extern __shared__ __align__(16) unsigned char lp_smem[];
   const int si = find_slice(lfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];
+  if ((S.k_mp2 >= (R)0) != PRE) return;   // uniform over the block
   const int g = (blockIdx.x - lfirst[si]) * blockDim.x + threadIdx.x;
   const int nst = lu_nstep(S.jd), nb = lu_nband(S.kd);
   const int l = g & 31, t = (g >> 5) % nst, band = (g >> 5) / nst;
   if (band >= nb || (only_lu && S.P->ilhs != 1)) return;   // uniform over the warp
-  constexpr int CH = LuLay<R>::CH;
+  constexpr int CH = LuLay<R, PRE>::CH;
   R* stage = (R*)lp_smem + (threadIdx.x >> 5) * CH;
-  lu_prep_cell(S, *S.P, band, t, l, scale, stage);
+  lu_prep_cell<R, PRE>(S, *S.P, band, t, l, scale, stage);
   __syncwarp();
   int4* dst = reinterpret_cast<int4*>(S.lurec + ((int64_t)band * nst + t) * CH);
   const int4* src = reinterpret_cast<const int4*>(stage);
@@ -291,19 +314,20 @@ __global__ void __launch_bounds__(CELL_BS) k_lu_prep(const Slice<R>* __restrict_
   for (int i = l; i < n16; i += 32) dst[i] = src[i];
 }
 
-template <class R>
+template <class R, bool PRE>
 __global__ void __launch_bounds__(CELL_BS) k_lu_edges(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
                                                       int nslice, int scale, int only_lu) {
   OT2D_CELL_MAP();
-  if (!inside || (only_lu && S.P->ilhs != 1)) return;
-  lu_edge_cell(S, *S.P, j, k, scale);
+  if (!inside || (only_lu && S.P->ilhs != 1) || (S.k_mp2 >= (R)0) != PRE) return;
+  lu_edge_cell<R, PRE>(S, *S.P, j, k, scale);
 }
 
-template <class R, bool FWD, int G>
+template <class R, bool FWD, int G, bool PRE>
 __global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int only_lu) {
   extern __shared__ __align__(128) unsigned char lu_smem[];
   if (only_lu && sl[blockIdx.x].P->ilhs != 1) return;
-  lu_sweep_slice<R, FWD, G>(sl[blockIdx.x], blockDim.x >> 5, lu_smem);
+  if ((sl[blockIdx.x].k_mp2 >= (R)0) != PRE) return;
+  lu_sweep_slice<R, FWD, G, PRE>(sl[blockIdx.x], blockDim.x >> 5, lu_smem);
 }
 
 template <class R>

@@ -23,6 +23,7 @@ constexpr int ADI_NSCRATCH = 25;
 struct Batch {
   int nslice = 0;          // slices in the batch
   int moving = 0;          // some slice is time accurate on a pitching grid
+  int precon = 0;          // some slice runs with Turkel preconditioning (k_mp2 >= 0)
   int cell_blocks = 0;     // blocks of the cell-parallel kernels
   int max_lu_warps = 1;    // warps per CTA of the LU-SGS kernel
   int max_wall = 1;        // most wall cells of one slice (force kernel smem); also max jd
@@ -71,6 +72,8 @@ cudaError_t launch_stqol(const double* q, double* qtn, double* qtnm1, double* qn
 template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st);
 template <class R> cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st);
 template <class R> cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+// rhslom alone (sources.f:97-148) on the interior cells of every slice
+template <class R> cudaError_t launch_rhslom(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 // scale = 1: multiply s by tscale first (step.f:141-148); 0: s already scaled.
 // only_lu = 1: skip slices whose ilhs is not 1 (mixed batches); 0: every slice
 template <class R> cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st,

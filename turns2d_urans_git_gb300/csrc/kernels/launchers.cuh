@@ -29,27 +29,34 @@ cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStr
   k_bc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, advance);
   return cudaGetLastError();
 }
+// the fused residual tiles: the plain instantiation always, the
+// preconditioned one when the batch holds a preconditioned slice
 template <class R>
-cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st) {
-  const int flags = AS_INV | AS_TS | AS_NORM | (viscous ? AS_VISC : 0);
+cudaError_t launch_resid_both(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st) {
   constexpr size_t smem = rt_smem_bytes<R>();
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_resid<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_resid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_resid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  k_resid<R><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
+  k_resid<R, false><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
+  if (b.precon) k_resid<R, true><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
+  return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st) {
+  const int flags = AS_INV | AS_TS | AS_NORM | (viscous ? AS_VISC : 0);
+  cudaError_t e = launch_resid_both(d_sl, b, flags, st);
+  if (e != cudaSuccess) return e;
   k_norm_final<R><<<b.nslice, 32, 0, st>>>(d_sl, b.d_tfirst, b.nslice, b.d_part);
   return cudaGetLastError();
 }
 template <class R>
 cudaError_t launch_resid_tiles(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st) {
-  constexpr size_t smem = rt_smem_bytes<R>();
-  cudaError_t e = cudaFuncSetAttribute(k_resid<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_resid<R><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags & ~AS_NORM, b.d_part);
-  return cudaGetLastError();
+  return launch_resid_both(d_sl, b, flags & ~AS_NORM, st);
 }
 template <class R>
 cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b, int inviscid, int viscous, cudaStream_t st) {
@@ -68,40 +75,52 @@ cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_rbc<R><<<b.nslice, 128, 0, st>>>(d_sl);
   return cudaGetLastError();
 }
-// ilu2d part 1: the sweep records and the halo edges (reads q, mu_t, tscale;
-// the FP64 path also round-trips q here)
 template <class R>
-cudaError_t launch_lusgs_prep(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
-  // one staged chunk per warp (f32 28 KB, f64 53 KB per block)
-  constexpr size_t prep_smem = (size_t)(CELL_BS / 32) * LuLay<R>::CH * sizeof(R);
+cudaError_t launch_rhslom(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  k_rhslom<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  return cudaGetLastError();
+}
+// ilu2d part 1: the sweep records and the halo edges (reads q, mu_t, tscale;
+// the FP64 path also round-trips q here).  PRE: the preilu2d records of the
+// preconditioned slices, launched only when the batch holds one.
+template <class R, bool PRE>
+cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
+  // one staged chunk per warp (f32 28 / 36 KB, f64 53 / 68 KB per block)
+  constexpr size_t prep_smem = (size_t)(CELL_BS / 32) * LuLay<R, PRE>::CH * sizeof(R);
   static bool prep_attr = false;
   if (!prep_attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_lu_prep<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
+    cudaError_t e = cudaFuncSetAttribute(k_lu_prep<R, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
     if (e != cudaSuccess) return e;
     prep_attr = true;
   }
-  k_lu_prep<R><<<b.lu_blocks, CELL_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
-  k_lu_edges<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
+  k_lu_prep<R, PRE><<<b.lu_blocks, CELL_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
+  k_lu_edges<R, PRE><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
   return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_lusgs_prep(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
+  cudaError_t e = launch_lusgs_prep_t<R, false>(d_sl, b, scale, st, only_lu);
+  if (e == cudaSuccess && b.precon) e = launch_lusgs_prep_t<R, true>(d_sl, b, scale, st, only_lu);
+  return e;
 }
 // ilu2d part 2: the forward and backward sweeps, launched at the device's
 // highest priority (they are the iteration's longest dependency chain and
 // run beside the turbulence branch)
-template <class R>
-cudaError_t launch_lusgs_sweeps(const Slice<R>* d_sl, const Batch& b, cudaStream_t st, int only_lu) {
+template <class R, bool PRE>
+cudaError_t launch_lusgs_sweeps_t(const Slice<R>* d_sl, const Batch& b, cudaStream_t st, int only_lu) {
   const int nw = b.max_lu_warps;
   // chunks per bulk copy: as many as ~200 KB of shared memory allows (1..8)
   const int maxcol = b.max_wall;   // >= jd - 2 of every slice
   int G = 8;
-  while (G > 1 && lu_smem_bytes<R>(nw, G, maxcol) > 200 * 1024) G >>= 1;
-  const size_t smem = lu_smem_bytes<R>(nw, G, maxcol);
+  while (G > 1 && lu_smem_bytes<R, PRE>(nw, G, maxcol) > 200 * 1024) G >>= 1;
+  const size_t smem = lu_smem_bytes<R, PRE>(nw, G, maxcol);
   static bool attr_set = false;
   static int prio = 0;
   if (!attr_set) {
-    const void* ks[] = {(const void*)k_lu_sweep<R, true, 8>, (const void*)k_lu_sweep<R, false, 8>,
-                        (const void*)k_lu_sweep<R, true, 4>, (const void*)k_lu_sweep<R, false, 4>,
-                        (const void*)k_lu_sweep<R, true, 2>, (const void*)k_lu_sweep<R, false, 2>,
-                        (const void*)k_lu_sweep<R, true, 1>, (const void*)k_lu_sweep<R, false, 1>};
+    const void* ks[] = {(const void*)k_lu_sweep<R, true, 8, PRE>, (const void*)k_lu_sweep<R, false, 8, PRE>,
+                        (const void*)k_lu_sweep<R, true, 4, PRE>, (const void*)k_lu_sweep<R, false, 4, PRE>,
+                        (const void*)k_lu_sweep<R, true, 2, PRE>, (const void*)k_lu_sweep<R, false, 2, PRE>,
+                        (const void*)k_lu_sweep<R, true, 1, PRE>, (const void*)k_lu_sweep<R, false, 1, PRE>};
     for (const void* k : ks) {
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
       if (e != cudaSuccess) return e;
@@ -127,13 +146,19 @@ cudaError_t launch_lusgs_sweeps(const Slice<R>* d_sl, const Batch& b, cudaStream
   };
   cudaError_t e;
   switch (G) {
-    case 8: e = run(k_lu_sweep<R, true, 8>, k_lu_sweep<R, false, 8>); break;
-    case 4: e = run(k_lu_sweep<R, true, 4>, k_lu_sweep<R, false, 4>); break;
-    case 2: e = run(k_lu_sweep<R, true, 2>, k_lu_sweep<R, false, 2>); break;
-    default: e = run(k_lu_sweep<R, true, 1>, k_lu_sweep<R, false, 1>); break;
+    case 8: e = run(k_lu_sweep<R, true, 8, PRE>, k_lu_sweep<R, false, 8, PRE>); break;
+    case 4: e = run(k_lu_sweep<R, true, 4, PRE>, k_lu_sweep<R, false, 4, PRE>); break;
+    case 2: e = run(k_lu_sweep<R, true, 2, PRE>, k_lu_sweep<R, false, 2, PRE>); break;
+    default: e = run(k_lu_sweep<R, true, 1, PRE>, k_lu_sweep<R, false, 1, PRE>); break;
   }
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
+}
+template <class R>
+cudaError_t launch_lusgs_sweeps(const Slice<R>* d_sl, const Batch& b, cudaStream_t st, int only_lu) {
+  cudaError_t e = launch_lusgs_sweeps_t<R, false>(d_sl, b, st, only_lu);
+  if (e == cudaSuccess && b.precon) e = launch_lusgs_sweeps_t<R, true>(d_sl, b, st, only_lu);
+  return e;
 }
 template <class R>
 cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
@@ -255,6 +280,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   template cudaError_t launch_bc<R>(const Slice<R>*, const Batch&, int, cudaStream_t);                  \
   template cudaError_t launch_residual<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
   template cudaError_t launch_rbc<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
+  template cudaError_t launch_rhslom<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
   template cudaError_t launch_lusgs<R>(const Slice<R>*, const Batch&, int, cudaStream_t, int);          \
   template cudaError_t launch_faces<R>(const Slice<R>*, const Batch&, int, int, cudaStream_t);          \
   template cudaError_t launch_resid_tiles<R>(const Slice<R>*, const Batch&, int, cudaStream_t);         \

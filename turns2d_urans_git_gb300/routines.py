@@ -93,6 +93,17 @@ def ilu2d(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, tscale):
           _p(yx), _p(yy), _p(ug), _p(vg), _p(turmu), _p(tscale))
 
 
+def preilu2d(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, tscale, bt):
+    """src/lhs.f:2 -- LU-SGS with Turkel's low-Mach preconditioner (bt of time_step)."""
+    _call("ot2d_preilu2d", _p(q), _p(s), _ref(jd), _ref(kd), _ref(js), _ref(je), _ref(ks), _ref(ke), _p(xx), _p(xy),
+          _p(yx), _p(yy), _p(ug), _p(vg), _p(turmu), _p(tscale), _p(bt))
+
+
+def rhslom(q, s, jd, kd, js, je, ks, ke, bt):
+    """src/sources.f:97 -- the interior residual times the low-Mach preconditioner."""
+    _call("ot2d_rhslom", _p(q), _p(s), _ref(jd), _ref(kd), _ref(js), _ref(je), _ref(ks), _ref(ke), _p(bt))
+
+
 def arc2d(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, iblank, tscale, bt):
     """src/lhs.f:817 -- diagonalised ADI (pentadiagonal line inversions)."""
     _call("ot2d_arc2d", _p(q), _p(s), _ref(jd), _ref(kd), _ref(js), _ref(je), _ref(ks), _ref(ke), _p(xx), _p(xy),
