@@ -205,3 +205,4 @@ def test_oracle_precon_changes_the_solution_below_mp1():
         qs.append(q)
     n2 = prm.jd * prm.kd
     assert relerr(qs[1][:4 * n2], qs[0][:4 * n2]) > 5e-7   # Q/J (J itself is the same grid)
+

@@ -38,6 +38,10 @@ struct Slice {
   // Turkel low-Mach preconditioning (iprecon): Mp**2, or -1 without it.
   // A face has bt = 1 (eulerrhs.f:78, :185), so its bSq is Mp**2 itself.
   R k_mp2;
+  // parameters the compute kernels read per cell, converted once (GB300's
+  // FP64 pipe is narrow: a double -> float conversion per cell and use
+  // costs more issue slots than the float arithmetic around it)
+  R k_gamma, k_rmue, k_rey, k_eps2, k_epsv, k_h, k_timeac, k_dualtime, k_cfltur;
   R* w;                              // scratch of this slice (phase dependent)
   R* lurec;                          // LU-SGS sweep records (skewed bands)
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)
@@ -73,6 +77,9 @@ inline void slice_consts(Slice<R>& S, const ot2d_params& p) {
   S.k_gm1 = (R)p.gm1;
   S.k_ggm1 = (R)p.ggm1;
   S.k_mp2 = p.iprecon ? (R)(p.Mp * p.Mp) : (R)-1;
+  S.k_gamma = (R)p.gamma; S.k_rmue = (R)p.rmue; S.k_rey = (R)p.rey;
+  S.k_eps2 = (R)(p.epse * 2.); S.k_epsv = (R)1. + S.k_eps2;
+  S.k_h = (R)p.h; S.k_timeac = (R)p.timeac; S.k_dualtime = (R)p.dualtime; S.k_cfltur = (R)p.cfltur;
 }
 
 // Fortran SIGN(a,b): |a| with the IEEE sign of b (gfortran semantics).
@@ -84,6 +91,10 @@ template <class R> __device__ __forceinline__ R sq(R x) { return x * x; }
 template <class R> __device__ __forceinline__ R cube(R x) { return (x * x) * x; }
 template <class R> __device__ __forceinline__ R pow6(R x) { R t = (x * x) * x; return t * t; }
 __device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
+
+// exact widening to double
+__device__ __forceinline__ double to_d(float x) { return (double)x; }
+__device__ __forceinline__ double to_d(double x) { return x; }
 
 // 1-based (j,k) -> linear offset inside one slice
 __device__ __forceinline__ int64_t at(int jd, int j, int k) { return (int64_t)(k - 1) * jd + (j - 1); }

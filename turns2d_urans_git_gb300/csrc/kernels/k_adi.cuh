@@ -36,7 +36,7 @@ __device__ __forceinline__ int64_t adi_at(int jd, int dir, int m, int n) { retur
 template <class R>
 __device__ void adi_txi_cell(const Slice<R>& S, const ot2d_params& p, int j, int k, int scale) {
   const int64_t o = at(S.jd, j, k), qs = S.qs, ws = S.wstride;
-  const R gm1 = (R)p.gm1, ggm1 = (R)p.ggm1;
+  const R gm1 = S.k_gm1, ggm1 = S.k_ggm1;
   const R q1 = S.q[o], J = S.q[(p.nq - 1) * qs + o];
   const R dj = (R)1.0 / q1;
   const R uu = S.q[qs + o] * dj, vv = S.q[2 * qs + o] * dj, e = S.q[3 * qs + o] * dj;
@@ -63,8 +63,8 @@ __device__ void adi_txi_cell(const Slice<R>& S, const ot2d_params& p, int j, int
   S.w[A_UV * ws + o] = uv2;
   S.w[A_CX * ws + o] = cjkl * rr1;
   S.w[A_CY * ws + o] = cjkl * rr2;
-  S.w[A_VN * ws + o] = ((R)p.rmue + S.turmu[o]) / ((R)p.rey * rho);
-  S.w[A_GE * ws + o] = (R)p.gamma * e - gm1 * uv2;
+  S.w[A_VN * ws + o] = (S.k_rmue + S.turmu[o]) / (S.k_rey * rho);
+  S.w[A_GE * ws + o] = S.k_gamma * e - gm1 * uv2;
   S.w[A_U * ws + o] = uu; S.w[A_V * ws + o] = vv; S.w[A_E * ws + o] = e;
   R a1 = s2 * uu + s3 * vv - s4;
   a1 = a1 * gm1 * c2i;
@@ -334,7 +334,7 @@ __device__ void adi_solve_line(const Slice<R>& S, const ot2d_params& p, int dir,
 template <class R>
 __device__ void adi_ninv_cell(const Slice<R>& S, const ot2d_params& p, int j, int k) {
   const int64_t o = at(S.jd, j, k), qs = S.qs, ws = S.wstride;
-  const R cjkl = sqrt((R)p.ggm1 * (S.w[A_E * ws + o] - S.w[A_UV * ws + o]));
+  const R cjkl = sqrt(S.k_ggm1 * (S.w[A_E * ws + o] - S.w[A_UV * ws + o]));
   const R rj1 = S.xx[o], rj2 = S.xy[o], rr1 = sqrt(rj1 * rj1 + rj2 * rj2);
   const R rk1 = S.yx[o], rk2 = S.yy[o], rr2 = sqrt(rk1 * rk1 + rk2 * rk2);
   const R a1 = (rj1 * rk1 + rj2 * rk2) / rr1 / rr2;
@@ -352,7 +352,7 @@ template <class R>
 __device__ void adi_teta_cell(const Slice<R>& S, const ot2d_params& p, int j, int k) {
   const int64_t o = at(S.jd, j, k), qs = S.qs, ws = S.wstride;
   const R uu = S.w[A_U * ws + o], vv = S.w[A_V * ws + o], uv = S.w[A_UV * ws + o], ge = S.w[A_GE * ws + o];
-  const R cjkl = sqrt((R)p.ggm1 * (S.w[A_E * ws + o] - uv));
+  const R cjkl = sqrt(S.k_ggm1 * (S.w[A_E * ws + o] - uv));
   R rk1 = S.yx[o], rk2 = S.yy[o];
   const R ugc = S.ug ? S.ug[o] : (R)0, vgc = S.vg ? S.vg[o] : (R)0;
   const R qq2 = S.w[A_QY * ws + o] + (rk1 * ugc + rk2 * vgc);

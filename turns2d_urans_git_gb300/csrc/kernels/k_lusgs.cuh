@@ -116,7 +116,7 @@ __device__ __forceinline__ LuCell<R> lu_cell(const Slice<R>& S, const ot2d_param
   R e = S.q[3 * qs + o] * dj;
   R rho = q1 * S.q[(p.nq - 1) * qs + o];
   c.uv2 = (R)0.5 * (c.uu * c.uu + c.vv * c.vv);
-  R cjkl = sqrt((R)p.ggm1 * (e - c.uv2));
+  R cjkl = sqrt(S.k_ggm1 * (e - c.uv2));
   c.ri1 = S.xx[o]; c.ri2 = S.xy[o]; c.rk1 = S.yx[o]; c.rk2 = S.yy[o];
   c.ugc = S.ug ? S.ug[o] : (R)0; c.vgc = S.vg ? S.vg[o] : (R)0;
   R qq1 = c.ri1 * c.uu + c.ri2 * c.vv;
@@ -125,10 +125,10 @@ __device__ __forceinline__ LuCell<R> lu_cell(const Slice<R>& S, const ot2d_param
   R qq2 = c.rk1 * c.uu + c.rk2 * c.vv;
   R qqy = fabs(-c.rk1 * c.ugc - c.rk2 * c.vgc + qq2);
   R rr2 = sqrt(sq(c.rk1) + sq(c.rk2));
-  R vnu = (R)2.0 * rr2 * rr2 * ((R)p.rmue + S.turmu[o]) / ((R)p.rey * rho);
+  R vnu = (R)2.0 * rr2 * rr2 * (S.k_rmue + S.turmu[o]) / (S.k_rey * rho);
   R svt = S.tscale[o];
   c.qx = qq1; c.cx = cjkl * rr1; c.qy = qq2; c.cy = cjkl * rr2; c.vn = vnu;
-  c.ge = (R)p.gamma * e - (R)p.gm1 * c.uv2;
+  c.ge = S.k_gamma * e - S.k_gm1 * c.uv2;
   if constexpr (PRE) {
     const R btv = S.bt[o], mp2 = S.k_mp2;
     const R bSq = mp2 / (btv - mp2 * (btv - (R)1));
@@ -139,7 +139,7 @@ __device__ __forceinline__ LuCell<R> lu_cell(const Slice<R>& S, const ot2d_param
     term = term + (R)0.5 * (opb * qqy + Y);
     c.d = (R)1.0 / ((R)1.0 + svt * (term * epsv + vnu));
     c.bsq = bSq;
-    c.term = (R)p.gm1 * (bSq - (R)1.) / (cjkl * cjkl);
+    c.term = S.k_gm1 * (bSq - (R)1.) / (cjkl * cjkl);
   } else {
     c.d = (R)1.0 / ((R)1.0 + svt * ((qqx + qqy + cjkl * (rr1 + rr2)) * epsv + vnu));
     c.bsq = (R)0; c.term = (R)0;
@@ -245,7 +245,7 @@ __device__ __forceinline__ void lu_prep_cell(const Slice<R>& S, const ot2d_param
     return;
   }
   const int j = p.jbeg + c, k = p.kbeg + r;
-  const R eps2 = (R)(p.epse * 2.), epsv = (R)1. + eps2;
+  const R eps2 = S.k_eps2, epsv = S.k_epsv;
   const int64_t o = at(S.jd, j, k);
   LuCell<R> cl = lu_cell<R, PRE>(S, p, j, k, epsv);
   const R ts = S.tscale[o];
@@ -300,7 +300,7 @@ __device__ __forceinline__ void lu_edge_cell(const Slice<R>& S, const ot2d_param
   const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
   const bool ij = j >= js && j <= je, ik = k >= ks && k <= ke;
   const int64_t o = at(S.jd, j, k);
-  const R eps2 = (R)(p.epse * 2.), epsv = (R)1. + eps2, gm1 = (R)p.gm1;
+  const R eps2 = S.k_eps2, epsv = S.k_epsv, gm1 = S.k_gm1;
   if (!(ij && ik)) {
     R sv[4];
     const R ts = S.tscale[o];
@@ -424,7 +424,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
   const ot2d_params& p = *S.P;
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nb = lu_nband(S.kd), nst = lu_nstep(S.jd);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  const R gm1 = (R)p.gm1;
+  const R gm1 = S.k_gm1;
   R* rings = (R*)smem;
   constexpr int CH = LuLay<R, PRE>::CH;
   uint64_t* bars = (uint64_t*)(smem + (size_t)nwarp * 2 * G * CH * sizeof(R));

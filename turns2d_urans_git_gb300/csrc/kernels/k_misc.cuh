@@ -53,6 +53,33 @@ __device__ __forceinline__ NormPart warp_norm_reduce(NormPart a) {
   return a;
 }
 
+// The same partial inside the residual kernel's warps: the maximum stays in
+// the compute type R (the maximum of floats, and its ties, are the same
+// taken in float or in double), so the float path's shuffle tree spends
+// the FP64 pipe on the two sums only.
+template <class R>
+struct NormPartR {
+  double rsum, resrho;
+  R resmax;
+  long long key;
+};
+template <class R>
+__device__ __forceinline__ NormPartR<R> warp_norm_reduce_r(NormPartR<R> a) {
+  for (int off = 16; off > 0; off >>= 1) {
+    NormPartR<R> o;
+    o.rsum = __shfl_down_sync(0xffffffffu, a.rsum, off);
+    o.resrho = __shfl_down_sync(0xffffffffu, a.resrho, off);
+    o.resmax = __shfl_down_sync(0xffffffffu, a.resmax, off);
+    o.key = __shfl_down_sync(0xffffffffu, a.key, off);
+    if ((threadIdx.x & 31) < off) {
+      a.rsum = a.rsum + o.rsum;
+      a.resrho = a.resrho + o.resrho;
+      if (o.resmax > a.resmax || (o.resmax == a.resmax && o.key < a.key)) { a.resmax = o.resmax; a.key = o.key; }
+    }
+  }
+  return a;
+}
+
 // Wall force integrands of one wall cell (forces.f:168-205, :269-379)
 struct ForceCell { double zz, sxx, syy; };
 

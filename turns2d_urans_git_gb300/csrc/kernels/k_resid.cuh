@@ -31,11 +31,11 @@ constexpr int RT_NVE = 6 * RT_VEH * RT_TJ;                 // eta viscous, k0-2.
 constexpr int RT_NVX = 6 * RT_TK * RT_VXW;                 // xi viscous, j0-2..j1+1
 
 // |iblank| of the staged cells is kept as one byte (values above 255 are
-// clamped; the reference's blanking values are -1, 0 and 1)
+// clamped; the reference's blanking values are -1, 0 and 1).  The norm
+// partials of the tile reuse the staged region at the end (k_resid).
 template <class R>
 __host__ __device__ constexpr size_t rt_smem_bytes() {
-  return ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) + RT_NR + 15) / 16) * 16 +
-         sizeof(NormPart) * (RT_BS / 32);
+  return ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) + RT_NR + 15) / 16) * 16;
 }
 
 template <class R>
@@ -43,7 +43,6 @@ struct RtSmem {
   R* c;          // [RS_N][RT_NR]
   R *F, *G, *VE, *VX;
   uint8_t* iba;  // [RT_NR]
-  NormPart* red; // [RT_BS / 32] warp partials
   __device__ RtSmem(unsigned char* base) {
     c = (R*)base;
     F = c + (size_t)RS_N * RT_NR;
@@ -51,8 +50,6 @@ struct RtSmem {
     VE = G + RT_NG;
     VX = VE + RT_NVE;
     iba = (uint8_t*)(VX + RT_NVX);
-    red = (NormPart*)(base + ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) + RT_NR + 15) /
-                              16) * 16);
   }
   __device__ __forceinline__ R& at(int a, int r) const { return c[(size_t)a * RT_NR + r]; }
 };
@@ -239,7 +236,7 @@ __device__ __forceinline__ void rt_visc_xi(const RtSmem<R>& sm, int r, R gkpr, R
 template <class R>
 __device__ __forceinline__ void rhslom_cell(const Slice<R>& S, const ot2d_params& p, int64_t o, R* s) {
   const int64_t qs = S.qs;
-  const R q1 = S.q[o], gm1 = S.k_gm1, gamma = (R)p.gamma, mp2 = S.k_mp2;
+  const R q1 = S.q[o], gm1 = S.k_gm1, gamma = S.k_gamma, mp2 = S.k_mp2;
   const R u = S.q[qs + o] / q1;
   const R v = S.q[2 * qs + o] / q1;
   const R phiSq = (R)0.5 * (u * u + v * v);
@@ -264,7 +261,7 @@ __device__ __forceinline__ void rhslom_cell(const Slice<R>& S, const ot2d_params
 // preconditioning -- roetrklflx fluxes, and in the full residual (AS_NORM)
 // rhslom applied to each cell after its norm terms (step.f:121-123).
 template <class R, bool PRE>
-__device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int flags, NormPart& np) {
+__device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int flags, NormPartR<R>& np) {
   const ot2d_params& p = *S.P;
   const int jd = S.jd, kd = S.kd, t = threadIdx.x;
   const int ntj = (p.jend - p.jbeg + RT_TJ) / RT_TJ;
@@ -432,11 +429,11 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
         const R smrs = fabs(s[n - 1]) * m;
         if (smrs > best) { best = smrs; bn = n; }
       }
-      np.resmax = (double)best;
+      np.resmax = best;
       np.key = ((long long)(k - 1) * (p.nmv + 1) + bn) * (long long)jd + (j - 1);
       const R s1 = s[0] * m, s2 = s[1] * m, s3 = s[2] * m, s4 = s[3] * m;
-      np.resrho = (double)(s[0] * s[0]);
-      np.rsum = (double)(s1 * s1 + s2 * s2 + s3 * s3 + s4 * s4);
+      np.resrho = to_d(s[0] * s[0]);
+      np.rsum = to_d(s1 * s1 + s2 * s2 + s3 * s3 + s4 * s4);
     }
     if constexpr (PRE) {
       if (flags & AS_NORM) rhslom_cell(S, p, o, s);

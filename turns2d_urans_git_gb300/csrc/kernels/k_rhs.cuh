@@ -14,7 +14,7 @@ __device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
   const ot2d_params& p = *S.P;
   const int jd = S.jd; const int64_t o = at(jd, j, k), qs = S.qs;
   const R* q = S.q;
-  const R h = (R)p.h, timeac = (R)p.timeac;
+  const R h = S.k_h, timeac = S.k_timeac;
   int ibi = S.iblank[o]; R ib = (R)(ibi > 0 ? ibi : 0);
   R jac_factor = p.invisc ? (R)0.01 : (R)0.002;
   if (p.iconstant_cfl == 0) {
@@ -25,7 +25,7 @@ __device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
     } else {
       R t = ib * ((R)1.0 + jac_factor * sqrt(J)) / ((R)1.0 + sqrt(J));
       if (p.iprecon) t = (R)100. * ib * ((R)1.0 + (R)0.005 * sqrt(J)) / ((R)1.0 + sqrt(J));   // time.f:62-66
-      t = t * (R)p.dualtime;
+      t = t * S.k_dualtime;
       S.bt[o] = (R)1. / ((R)1. + t / h / oat);
       S.tscale[o] = t / ((R)1. + t / h / oat);
     }
@@ -37,7 +37,7 @@ __device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
   R uu = (u - ugc) * xx + (v - vgc) * xy;
   R vv = (u - ugc) * yx + (v - vgc) * yy;
   R dxdx = sq(xx) + sq(xy), dydy = sq(yx) + sq(yy);
-  R asq = (R)p.ggm1 * (e - (R)0.5 * (sq(u) + sq(v)));
+  R asq = S.k_ggm1 * (e - (R)0.5 * (sq(u) + sq(v)));
   R lam_j = fabs(uu) + sqrt(asq * dxdx);
   R lam_k = fabs(vv) + sqrt(asq * dydy);
   if (p.idual == 0) {
@@ -45,7 +45,7 @@ __device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
     S.tscale[o] = t * ib;
     S.bt[o] = (R)1.;
   } else {
-    R hnew = (R)p.dualtime / (lam_j + lam_k);
+    R hnew = S.k_dualtime / (lam_j + lam_k);
     R t = hnew * ib;
     t = t / ((R)1. + t / h / oat);
     S.tscale[o] = t;
@@ -432,7 +432,7 @@ __device__ __forceinline__ Recon<R> make_recon(const ot2d_params& p, int dir) {
 template <class R>
 __device__ void xi_face(const Slice<R>& S, int j, int k, R* F) {
   const ot2d_params& p = *S.P;
-  LineRd<R> L{S.q, S.qs, S.jd, p.nq, k, 0, (R)p.gm1, S.iblank};
+  LineRd<R> L{S.q, S.qs, S.jd, p.nq, k, 0, S.k_gm1, S.iblank};
   Recon<R> rc = make_recon<R>(p, 0);
   int64_t o = at(S.jd, j, k);
   R f[4];
@@ -445,7 +445,7 @@ __device__ void xi_face(const Slice<R>& S, int j, int k, R* F) {
 template <class R>
 __device__ void eta_face(const Slice<R>& S, int j, int k, R* G) {
   const ot2d_params& p = *S.P;
-  LineRd<R> L{S.q, S.qs, S.jd, p.nq, j, 1, (R)p.gm1, S.iblank};
+  LineRd<R> L{S.q, S.qs, S.jd, p.nq, j, 1, S.k_gm1, S.iblank};
   Recon<R> rc = make_recon<R>(p, 1);
   int64_t o = at(S.jd, j, k);
   R f[4];
@@ -467,7 +467,7 @@ __device__ __forceinline__ ViscCell<R> visc_cell(const Slice<R>& S, const ot2d_p
   R ra = (R)1. / S.q[o];
   c.u = S.q[qs + o] * ra; c.v = S.q[2 * qs + o] * ra;
   c.e = S.q[3 * qs + o] * ra - (R).5 * (sq(c.u) + sq(c.v));
-  R tt = (R)p.ggm1 * c.e;
+  R tt = S.k_ggm1 * c.e;
   R vmue = c2bp * tt * sqrt(tt) / (c2b + tt);
   R turm = S.turmu[o];
   c.vnu = vmue + turm; c.gkap = vmue + prtr * turm;

@@ -43,7 +43,7 @@ __device__ __forceinline__ void sa_prep_cell(const Slice<R>& S, const ot2d_param
   R ra = (R)1. / q1;
   R uvel = q2 * ra, vvel = q3 * ra;
   R ei = q4 * ra - (R)0.5 * (sq(uvel) + sq(vvel));
-  R tt = (R)p.ggm1 * ei;
+  R tt = S.k_ggm1 * ei;
   S.w[W_VMUL * ws + o] = c2bp * tt * sqrt(tt) / (c2b + tt);
   S.w[W_U * ws + o] = q2 / q1;
   S.w[W_V * ws + o] = q3 / q1;
@@ -78,7 +78,7 @@ __device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int 
   auto W = [&](int a, int jj, int kk) { return S.w[a * ws + at(jd, jj, kk)]; };
   auto Mx = [&](const R* a, int jj, int kk) { return a[at(jd, jj, kk)]; };
   const int64_t o = at(jd, j, k);
-  const R rey = (R)p.rey;
+  const R rey = S.k_rey;
   // ---- convec
   SAnb<R> c0 = sa_split(S, j, k), cjm = sa_split(S, j - 1, k), cjp = sa_split(S, j + 1, k);
   SAnb<R> ckm = sa_split(S, j, k - 1), ckp = sa_split(S, j, k + 1);
@@ -185,16 +185,16 @@ __device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int 
   R tscal = S.tscale[o];
   int ibi = S.iblank[o];
   if (p.cfltur > 1 && p.idual_turb == 1) {
-    R dtp = (R)p.cfltur / (bj + bk);
+    R dtp = S.k_cfltur / (bj + bk);
     tscal = dtp * (R)ibi;
-    tscal = tscal / ((R)1. + tscal / (R)p.h);
+    tscal = tscal / ((R)1. + tscal / S.k_h);
   }
   if (p.timeac == 1) {
     R ib = (R)(ibi > 0 ? ibi : 0);
     R J = Q(j, k, nq);
     tscal = ib * ((R)1.0 + (R)0.002 * sqrt(J)) / ((R)1. + sqrt(J));
     tscal = tscal * (R)1.0;
-    tscal = tscal / ((R)1. + tscal / (R)p.h);
+    tscal = tscal / ((R)1. + tscal / S.k_h);
   }
   S.w[W_SJ * ws + o] = sj * tscal;
   S.w[W_AJ * ws + o] = aj * tscal;

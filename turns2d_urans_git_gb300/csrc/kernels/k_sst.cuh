@@ -46,7 +46,7 @@ __device__ __forceinline__ void sst_prep_cell(const Slice<R>& S, const ot2d_para
   const R ra = (R)1. / q1;
   const R uvel = q2 * ra, vvel = q3 * ra;
   const R ei = q4 * ra - (R)0.5 * (sq(uvel) + sq(vvel));
-  const R tt = (R)p.ggm1 * ei;
+  const R tt = S.k_ggm1 * ei;
   S.w[K_VMUL * ws + o] = c2bp * tt * sqrt(tt) / (c2b + tt);
   S.w[K_RHO * ws + o] = q1 * J;
   S.w[K_U * ws + o] = q2 / q1;
@@ -69,7 +69,7 @@ __device__ void sst_fields_cell(const Slice<R>& S, const ot2d_params& p, int j, 
   auto Q = [&](int jj, int kk, int n) { return S.q[(int64_t)(n - 1) * qs + at(jd, jj, kk)]; };
   const int64_t o = at(jd, j, k);
   const R xx = S.xx[o], xy = S.xy[o], yx = S.yx[o], yy = S.yy[o];
-  const R rei = (R)1. / (R)p.rey;
+  const R rei = (R)1. / S.k_rey;
   // kwvortic / turbstress share the velocity gradients
   const R usi = (R)0.5 * (W(K_U, j + 1, k) - W(K_U, j - 1, k)), vsi = (R)0.5 * (W(K_V, j + 1, k) - W(K_V, j - 1, k));
   const R ueta = (R)0.5 * (W(K_U, j, k + 1) - W(K_U, j, k - 1)), veta = (R)0.5 * (W(K_V, j, k + 1) - W(K_V, j, k - 1));
@@ -286,7 +286,7 @@ __device__ void sst_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int
   auto Q = [&](int jj, int kk, int n) { return S.q[(int64_t)(n - 1) * qs + at(jd, jj, kk)]; };
   auto X = [&](const R* a, int jj, int kk) { return a[at(jd, jj, kk)]; };
   const int64_t o = at(jd, j, k);
-  const R rey = (R)p.rey, rei = (R)1. / (R)p.rey;
+  const R rey = S.k_rey, rei = (R)1. / S.k_rey;
   // ---- convection: upwind split of this cell (:508-511, :546-549)
   const R ugc = S.ug ? S.ug[o] : (R)0, vgc = S.vg ? S.vg[o] : (R)0;
   const R u0 = W(K_U, j, k), v0 = W(K_V, j, k);
@@ -394,7 +394,7 @@ __device__ void sst_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int
     const R Jc = S.q[(int64_t)(nq - 1) * qs + o];
     tscal = ib * ((R)1.0 + (R)0.002 * sqrt(Jc)) / ((R)1. + sqrt(Jc));
     tscal = tscal * dtpseudo_turb;
-    tscal = tscal / ((R)1. + tscal / (R)p.h / oat);
+    tscal = tscal / ((R)1. + tscal / S.k_h / oat);
   }
   for (int n = 0; n < 2; ++n) {
     S.w[kband(KB_AJ, n) * ws + o] = aj[n] * tscal;

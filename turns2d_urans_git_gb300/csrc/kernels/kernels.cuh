@@ -218,20 +218,36 @@ __global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 1) k_resid(const S
   const Slice<R>& S = sl[si];
   if ((S.k_mp2 >= (R)0) != PRE) return;
   RtSmem<R> sm(rt_raw);
-  NormPart np{0.0, 0.0, 0.0, 0x7fffffffffffffffLL};
-  resid_tile<R, PRE>(S, sm, blockIdx.x - tfirst[si], flags, np);
+  NormPartR<R> npr{0.0, 0.0, (R)0, 0x7fffffffffffffffLL};
+  resid_tile<R, PRE>(S, sm, blockIdx.x - tfirst[si], flags, npr);
   if (!(flags & AS_NORM)) return;
-  // deterministic block reduction: a fixed shuffle tree per warp, then the
-  // warp partials in warp order
-  np = warp_norm_reduce(np);
-  NormPart* sh = sm.red;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) sh[wid] = np;
+  // Deterministic block reduction in a fixed order: every thread leaves its
+  // cell's terms in the staged region (only the face passes read it, and
+  // they are behind the tile's last barrier), then warp 0 sums the 8 values
+  // of each lane position in thread order and finishes with a shuffle tree.
+  // One warp does the FP64 additions of the whole tile.
+  static_assert(RT_BS == 256 && (size_t)RT_BS * (2 * sizeof(double) + sizeof(long long) + sizeof(R)) <=
+                                   sizeof(R) * (size_t)RS_N * RT_NR, "partials fit in the staged region");
+  double* prs = (double*)sm.c;
+  double* prr = prs + RT_BS;
+  long long* pky = (long long*)(prr + RT_BS);
+  R* pmx = (R*)(pky + RT_BS);
+  const int t = threadIdx.x, lane = t & 31;
+  prs[t] = npr.rsum; prr[t] = npr.resrho; pky[t] = npr.key; pmx[t] = npr.resmax;
   __syncthreads();
-  if (wid == 0) {
-    np = lane < RT_BS / 32 ? sh[lane] : NormPart{0.0, 0.0, 0.0, 0x7fffffffffffffffLL};
-    np = warp_norm_reduce(np);
-    if (lane == 0) part[blockIdx.x] = np;
+  if (t < 32) {
+    NormPartR<R> a{prs[lane], prr[lane], pmx[lane], pky[lane]};
+#pragma unroll
+    for (int i = 1; i < RT_BS / 32; ++i) {
+      const int u = lane + 32 * i;
+      a.rsum = a.rsum + prs[u];
+      a.resrho = a.resrho + prr[u];
+      const R m = pmx[u];
+      const long long ky = pky[u];
+      if (m > a.resmax || (m == a.resmax && ky < a.key)) { a.resmax = m; a.key = ky; }
+    }
+    a = warp_norm_reduce_r(a);
+    if (lane == 0) part[blockIdx.x] = NormPart{a.rsum, a.resrho, to_d(a.resmax), a.key};
   }
 }
 
@@ -285,31 +301,44 @@ __global__ void k_rbc(const Slice<R>* __restrict__ sl) {
 }
 
 // ilu2d (lhs.f:470-814), preceded by s *= tscale on all cells when `scale`
-// (step.f:141-148).  Records of the interior cells; one thread per
-// (band, step, lane) of every slice (prefix table lfirst).
-// A warp builds one chunk: each lane writes its record into the warp's
-// shared-memory copy of the chunk, then the warp stores the chunk with
-// contiguous 16-byte accesses (full sectors; the lane-major records would
-// otherwise be written with a 112- / 208-byte stride).  PRE: the
+// (step.f:141-148).  Records of the interior cells (prefix table lfirst):
+// a block of CELL_BS threads builds LU_PREP_CH consecutive chunks of the
+// band layout.  Lane l of chunk (band, t) is cell (row 32 band + l, column
+// t - l), so the chunks' lanes walk the grid diagonally; thread i computes
+// lane i / 8 of chunk i % 8 instead, which makes eight consecutive threads
+// read eight consecutive cells of one row (the lane-per-thread order would
+// touch a different row, and cache line, per thread).  The records go to
+// the block's shared-memory copy of its chunks (chunk stride padded by 16
+// bytes so the eight chunks of one row land in different banks), then each
+// warp stores one chunk with contiguous 16-byte accesses.  PRE: the
 // preconditioned (preilu2d) records of the slices with k_mp2 >= 0; each
 // instantiation returns on the other kind's slices.
+constexpr int LU_PREP_CH = CELL_BS / 32;   // chunks per block
+template <class R, bool PRE>
+__host__ __device__ constexpr int lu_prep_stride() { return LuLay<R, PRE>::CH + (int)(16 / sizeof(R)); }
 template <class R, bool PRE>
 __global__ void __launch_bounds__(CELL_BS) k_lu_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst,
                                                      int nslice, int scale, int only_lu) {
+  static_assert(CELL_BS == 256, "thread -> (chunk, lane) map assumes 8 chunks of 32 lanes");
   extern __shared__ __align__(16) unsigned char lp_smem[];
   const int si = find_slice(lfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];
-  if ((S.k_mp2 >= (R)0) != PRE) return;   // uniform over the block
-  const int g = (blockIdx.x - lfirst[si]) * blockDim.x + threadIdx.x;
+  if ((S.k_mp2 >= (R)0) != PRE) return;                    // uniform over the block
+  if (only_lu && S.P->ilhs != 1) return;                   // uniform over the block
   const int nst = lu_nstep(S.jd), nb = lu_nband(S.kd);
-  const int l = g & 31, t = (g >> 5) % nst, band = (g >> 5) / nst;
-  if (band >= nb || (only_lu && S.P->ilhs != 1)) return;   // uniform over the warp
-  constexpr int CH = LuLay<R, PRE>::CH;
-  R* stage = (R*)lp_smem + (threadIdx.x >> 5) * CH;
-  lu_prep_cell<R, PRE>(S, *S.P, band, t, l, scale, stage);
-  __syncwarp();
-  int4* dst = reinterpret_cast<int4*>(S.lurec + ((int64_t)band * nst + t) * CH);
-  const int4* src = reinterpret_cast<const int4*>(stage);
+  const int c0 = (blockIdx.x - lfirst[si]) * LU_PREP_CH;   // first chunk of the block
+  constexpr int CH = LuLay<R, PRE>::CH, CHS = lu_prep_stride<R, PRE>();
+  {
+    const int w = threadIdx.x & (LU_PREP_CH - 1), l = threadIdx.x / LU_PREP_CH;
+    const int c = c0 + w, band = c / nst, t = c - band * nst;
+    if (band < nb) lu_prep_cell<R, PRE>(S, *S.P, band, t, l, scale, (R*)lp_smem + w * CHS);
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int c = c0 + w, band = c / nst;
+  if (band >= nb) return;
+  int4* dst = reinterpret_cast<int4*>(S.lurec + (int64_t)c * CH);   // chunk (band, t) is chunk band*nst + t
+  const int4* src = reinterpret_cast<const int4*>((R*)lp_smem + w * CHS);
   constexpr int n16 = (int)(CH * sizeof(R) / 16);
   for (int i = l; i < n16; i += 32) dst[i] = src[i];
 }
@@ -570,7 +599,7 @@ __global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__
   }
   // monitor of the updated cell (step.f:356-370), free of divisions:
   // a^2 <= 0.002  <=>  ggm1*(q4*q1 - qq/2) <= 0.002*q1^2 for q1 > 0
-  if (S.ist && monitor_bad<R>((R)p.ggm1, qn)) atomicOr(&S.ist[2], 2);
+  if (S.ist && monitor_bad<R>(S.k_ggm1, qn)) atomicOr(&S.ist[2], 2);
 }
 
 // compute copy of the whole state from the FP64 master (after the host

@@ -86,7 +86,7 @@ cudaError_t launch_rhslom(const Slice<R>* d_sl, const Batch& b, cudaStream_t st)
 template <class R, bool PRE>
 cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
   // one staged chunk per warp (f32 28 / 36 KB, f64 53 / 68 KB per block)
-  constexpr size_t prep_smem = (size_t)(CELL_BS / 32) * LuLay<R, PRE>::CH * sizeof(R);
+  constexpr size_t prep_smem = (size_t)LU_PREP_CH * lu_prep_stride<R, PRE>() * sizeof(R);
   static bool prep_attr = false;
   if (!prep_attr) {
     cudaError_t e = cudaFuncSetAttribute(k_lu_prep<R, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
