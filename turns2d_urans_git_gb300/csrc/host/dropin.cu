@@ -502,7 +502,7 @@ int ot2d_visrhs(double* turmu, double* q, double* s, double* xx, double* xy, dou
 
 int ot2d_bc(double* q, double* x, double* y, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
             int32_t* im, int32_t* jd, int32_t* kd, double* bt) {
-  (void)x; (void)y; (void)im; (void)bt;
+  (void)x; (void)y; (void)im;
   int err = 0;
   if (prepare(1, err)) return fail(err);
   const ot2d_params& p = g_ctx.P;
@@ -510,12 +510,14 @@ int ot2d_bc(double* q, double* x, double* y, double* xx, double* xy, double* yx,
   const size_t n2 = (size_t)p.jd * p.kd;
   Slice<double> S = base_slice(1, 1, (int64_t)n2);
   S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
-  S.xx64 = (double*)resolve(xx, n2 * 8, true, false, err);
-  S.xy64 = (double*)resolve(xy, n2 * 8, true, false, err);
-  S.yx64 = (double*)resolve(yx, n2 * 8, true, false, err);
-  S.yy64 = (double*)resolve(yy, n2 * 8, true, false, err);
-  S.ug64 = (double*)resolve(ug, n2 * 8, true, false, err);
-  S.vg64 = (double*)resolve(vg, n2 * 8, true, false, err);
+  S.xx = S.xx64 = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = S.xy64 = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = S.yx64 = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = S.yy64 = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug = S.ug64 = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg = S.vg64 = (double*)resolve(vg, n2 * 8, true, false, err);
+  // bt of time_step enters the Turkel-form far field (bc.f:712-835); 1 when not given
+  S.bt = bt ? (double*)resolve(bt, n2 * 8, true, false, err) : nullptr;
   std::vector<Slice<double>> sl{S};
   run_batch(sl, err);
   if (!err && launch_bc<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st) != cudaSuccess) err = OT2D_ERR_CUDA;

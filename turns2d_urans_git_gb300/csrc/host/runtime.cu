@@ -403,9 +403,11 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   // record blocks, 32-line groups, residual tiles
   std::vector<int32_t> idx(6 * (n + 1));
   int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1, maxkd = 1, moving = 0, precon = 0;
+  int maxnbc = 0;
   for (int i = 0; i < n; ++i) {
     if (sl[i].xc) moving = 1;
     if (sl[i].k_mp2 >= (R)0) precon = 1;
+    maxnbc = std::max(maxnbc, (int)sl[i].nbc);
     idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl; idx[3 * (n + 1) + i] = lub;
     idx[4 * (n + 1) + i] = grp; idx[5 * (n + 1) + i] = tiles;
     const int jd = sl[i].jd, kd = sl[i].kd;
@@ -445,6 +447,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   b.max_lu_warps = maxw;
   b.max_wall = maxwall;
   b.max_kd = maxkd;
+  b.max_nbc = maxnbc;
   b.jlines = jl; b.klines = kl;
   b.lu_blocks = lub;
   b.jgroups = grp;

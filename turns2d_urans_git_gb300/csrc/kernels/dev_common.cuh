@@ -42,6 +42,7 @@ struct Slice {
   // FP64 pipe is narrow: a double -> float conversion per cell and use
   // costs more issue slots than the float arithmetic around it)
   R k_gamma, k_rmue, k_rey, k_eps2, k_epsv, k_h, k_timeac, k_dualtime, k_cfltur;
+  R k_mp, k_rinf, k_uinf, k_vinf, k_einf, k_pinf;     // the q boundary conditions
   R* w;                              // scratch of this slice (phase dependent)
   R* lurec;                          // LU-SGS sweep records (skewed bands)
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)
@@ -57,6 +58,7 @@ struct Slice {
   double *qtn, *qtnm1, *qnewt;            // stqol levels (itnmax > 1), (jd,kd,nspec,nv)
   const double* motion;                   // per physical step: sin, cos of the pitch increment and of its negative
   int32_t nmotion;                        // physical steps in the table
+  int32_t nbc;                            // &bcinp entries (params nbc)
 };
 
 // Fill the residual constants of a slice from its parameters (host side;
@@ -77,8 +79,11 @@ inline void slice_consts(Slice<R>& S, const ot2d_params& p) {
   S.k_gm1 = (R)p.gm1;
   S.k_ggm1 = (R)p.ggm1;
   S.k_mp2 = p.iprecon ? (R)(p.Mp * p.Mp) : (R)-1;
+  S.nbc = p.nbc;
   S.k_gamma = (R)p.gamma; S.k_rmue = (R)p.rmue; S.k_rey = (R)p.rey;
   S.k_eps2 = (R)(p.epse * 2.); S.k_epsv = (R)1. + S.k_eps2;
+  S.k_mp = (R)p.Mp; S.k_rinf = (R)p.rinf; S.k_uinf = (R)p.uinf; S.k_vinf = (R)p.vinf;
+  S.k_einf = (R)p.einf; S.k_pinf = (R)p.pinf;
   S.k_h = (R)p.h; S.k_timeac = (R)p.timeac; S.k_dualtime = (R)p.dualtime; S.k_cfltur = (R)p.cfltur;
 }
 

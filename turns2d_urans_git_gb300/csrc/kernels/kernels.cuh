@@ -100,12 +100,21 @@ __global__ void k_mv_halo(const Slice<R>* __restrict__ sl) {
   mv_metric_halo(S);
 }
 
+// bc.f:2-86, BC entry ib of every slice (grid: blockIdx.y = slice,
+// blockIdx.x = part of the entry's cells); slices with fewer entries return
+template <class R>
+__global__ void __launch_bounds__(BCE_BS) k_bc_entry(const Slice<R>* __restrict__ sl, int ib) {
+  const Slice<R>& S = sl[blockIdx.y];
+  if (ib >= S.nbc) return;
+  const int istep0 = S.ist ? S.ist[0] : S.P->istep0;
+  bc_entry(S, istep0, ib, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// after the entries: the compute copy of the halo ring and its monitor
 template <class R>
 __global__ void __launch_bounds__(BC_BS) k_bc(const Slice<R>* __restrict__ sl, int advance) {
   const Slice<R>& S = sl[blockIdx.x];
-  const int istep0 = S.ist ? S.ist[0] : S.P->istep0;
-  bc_slice(S, nullptr, istep0);
-  shadow_ring(S, 1, 4);
+  widen_ring(S, 1, 4);
   // monitor of the halo ring just set (the interior is checked by k_update)
   if (S.ist && advance) {
     const int jd = S.jd, kd = S.kd, nring = 2 * jd + 2 * (kd - 2);
@@ -117,8 +126,8 @@ __global__ void __launch_bounds__(BC_BS) k_bc(const Slice<R>* __restrict__ sl, i
       else if (i < 2 * jd + kd - 2) { j = 1; k = i - 2 * jd + 2; }
       else { j = jd; k = i - (2 * jd + kd - 2) + 2; }
       const int64_t o = at(jd, j, k);
-      double qh[4] = {S.q64[o], S.q64[S.qs + o], S.q64[2 * S.qs + o], S.q64[3 * S.qs + o]};
-      bad = bad || monitor_bad<double>(S.P->ggm1, qh);
+      const R qh[4] = {S.q[o], S.q[S.qs + o], S.q[2 * S.qs + o], S.q[3 * S.qs + o]};
+      bad = bad || monitor_bad<R>(S.k_ggm1, qh);
     }
     if (bad) atomicOr(&S.ist[2], 2);
   }

@@ -13,6 +13,8 @@ constexpr int CELL_BS = 256;
 // threads of the one-CTA-per-slice boundary kernels (their loops run along
 // the boundary rows; more threads, fewer serial passes per row)
 constexpr int BC_BS = 512;
+// threads of a CTA of one BC entry (several CTAs per slice)
+constexpr int BCE_BS = 128;
 // residual tile: RT_TJ x RT_TK interior cells per CTA
 constexpr int RT_TJ = 32, RT_TK = 8;
 // scratch arrays per slice of the k-omega SST solve (k_sst.cuh: SSTw)
@@ -28,6 +30,7 @@ struct Batch {
   int max_lu_warps = 1;    // warps per CTA of the LU-SGS kernel
   int max_wall = 1;        // most wall cells of one slice (force kernel smem); also max jd
   int max_kd = 1;          // largest kd of the batch
+  int max_nbc = 0;         // most &bcinp entries of one slice
   int jlines = 0, klines = 0;  // total k-lines / j-lines (SA line solves)
   const int32_t* d_first = nullptr;   // [nslice+1] first cell block of each slice
   const int32_t* d_jfirst = nullptr;  // [nslice+1] first k-line (lsolvej) of each slice
