@@ -118,6 +118,12 @@ int ot2d_rhslom(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int
 int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
                double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu, int32_t* iblank,
                double* tscale, double* bt);
+/* src/lhs.f:1060-1061: arc2d with Turkel's preconditioned eigenvectors in
+ * the T_xi^-1, N^-1 and T_eta transforms (bSq per cell from bt and the
+ * params' Mp whatever iprecon says); line inversions as ot2d_arc2d */
+int ot2d_arc2d_precon(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks,
+                      int32_t* ke, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+                      double* turmu, int32_t* iblank, double* tscale, double* bt);
 /* src/samodel2d.f:2-3 */
 int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
                 double* xy, double* yx, double* yy, double* ug, double* vg, int32_t* jd, int32_t* kd,
@@ -131,9 +137,9 @@ int ot2d_timespectralrhs(double* q, double* s, double* Ds, int32_t* jd, int32_t*
 /* src/step.f:2-7 (full arrays over nspec; norms of the last call via
  * ot2d_last_norms).  Time accurate (iunst = 1): xold..yole give the
  * swept-area face speeds and ug, vg the cell grid speeds; itnmax > 1: qnewt
- * gives newton's physical-time term (time.f:178-210).  iprecon (LU-SGS
- * only): roetrklflx fluxes, rhslom after the norms and preilu2d, all reading
- * bt, which must then be given. */
+ * gives newton's physical-time term (time.f:178-210).  iprecon:
+ * roetrklflx fluxes, rhslom after the norms and preilu2d or arc2d_precon,
+ * all reading bt, which must then be given. */
 int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, double* x, double* y, double* xv,
               double* yv, int32_t* iblank, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
               double* ugv, double* vgv, double* xold, double* yold, double* xole, double* yole, double* turmu,

@@ -55,7 +55,8 @@ void ilu2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
 void preilu2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, A2 tscale, A2 bt);
 void rhslom(const P& p, A3 q, A3 s, A2 bt);
 /* lhs.f:817-1057 (ilhs = 2: lhsinv + pentadag) */
-void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, I2 iblank, A2 tscale, A2 bt);
+void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, I2 iblank, A2 tscale, A2 bt,
+           bool pre = false);
 /* samodel2d.f:200-240 */
 void lamvis(const P& p, A3 q, A2 vmul);
 /* samodel2d.f:243-293 */

@@ -616,7 +616,12 @@ static void lhsinv_up(const P& p, A3 q, A3 s, A2 qn, A2 cn, int ms, int me, int 
 /* lhs.f:817-1057 (ilhs = 2, or 3 with lhsinv_up).  The tmp coefficient arrays of lhsinv at m = ms
  * and m = me are never assigned by the reference and are read as 0 here
  * (what a fresh allocation holds). */
-void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, I2 iblank, A2 tscale, A2 bt) {
+/* lhs.f:817-1057 (arc2d); pre: lhs.f:1060-1330 (arc2d_precon), the same
+ * ADI with Turkel's preconditioned eigenvectors in T_xi^-1, N^-1 and T_eta
+ * (bSq = Mp**2/(bt - Mp**2 (bt-1)) per cell) and the contravariant
+ * velocities taken relative to the grid before they are stored */
+void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 turmu, I2 iblank, A2 tscale, A2 bt,
+           bool pre) {
   const int jd = p.jd, kd = p.kd, nq = p.nq;
   const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
   const size_t n2 = (size_t)jd * kd;
@@ -641,13 +646,23 @@ void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
     double c2i = 1.0 / (cjkl * cjkl);
     pr(j, k) = (q(j, k, 4) - uv2) * gm1 * q(j, k, 1);
     double rj1 = xx(j, k), rj2 = xy(j, k);
-    double qq1 = rj1 * uu + rj2 * vv;
-    qx(j, k) = qq1 - (rj1 * ug(j, k) + rj2 * vg(j, k));
+    double qq1;
+    if (pre) {  /* :1116, :1134 */
+      qq1 = rj1 * (uu - ug(j, k)) + rj2 * (vv - vg(j, k));
+      qx(j, k) = qq1;
+    } else {
+      qq1 = rj1 * uu + rj2 * vv;
+      qx(j, k) = qq1 - (rj1 * ug(j, k) + rj2 * vg(j, k));
+    }
     double rr1 = std::sqrt(p2(rj1) + p2(rj2));
     rj1 = rj1 / rr1; rj2 = rj2 / rr1;
     double rk1 = yx(j, k), rk2 = yy(j, k);
-    double qq2 = rk1 * uu + rk2 * vv;
-    qy(j, k) = qq2 - (rk1 * ug(j, k) + rk2 * vg(j, k));
+    if (pre) {
+      qy(j, k) = rk1 * (uu - ug(j, k)) + rk2 * (vv - vg(j, k));
+    } else {
+      double qq2 = rk1 * uu + rk2 * vv;
+      qy(j, k) = qq2 - (rk1 * ug(j, k) + rk2 * vg(j, k));
+    }
     double rr2 = std::sqrt(p2(rk1) + p2(rk2));
     rk1 = rk1 / rr2; rk2 = rk2 / rr2;
     double vnu = (p.rmue + turmu(j, k)) / (p.rey * q(j, k, 1));
@@ -662,6 +677,20 @@ void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
     double a2 = (rj1 * vv - rj2 * uu) * s(j, k, 1) + rj2 * s(j, k, 2) - rj1 * s(j, k, 3);
     double a3 = uv2 * s(j, k, 1) - s(j, k, 2) * uu - s(j, k, 3) * vv + s(j, k, 4);
     a3 = a3 * gm1 * c2i;
+    if (pre) {  /* :1141-1164 */
+      double bSq = p.Mp * p.Mp / (bt(j, k) - p.Mp * p.Mp * (bt(j, k) - 1));
+      double X = std::sqrt(((1. - bSq) * qq1) * ((1. - bSq) * qq1) + 4. * bSq * cx(j, k) * cx(j, k)) / rr1;
+      double Y = 0.5 * ((1.0 - bSq) * qq1 / rr1 + X);
+      double Z = 0.5 * ((1.0 - bSq) * qq1 / rr1 - X);
+      double qqmxt = qq1 + ug(j, k) * rj1 * rr1 + vg(j, k) * rj2 * rr1;
+      double a4 = qqmxt * s(j, k, 1) / rr1 - rj1 * s(j, k, 2) - rj2 * s(j, k, 3);
+      a4 = a4 * bSq;
+      s(j, k, 1) = a1;
+      s(j, k, 2) = a2;
+      s(j, k, 3) = -(Z * a3 + a4) / X;
+      s(j, k, 4) = (Y * a3 + a4) / X;
+      continue;
+    }
     double a4 = qq1 * s(j, k, 1) / rr1 - rj1 * s(j, k, 2) - rj2 * s(j, k, 3);
     s(j, k, 1) = a1;
     s(j, k, 2) = a2;
@@ -683,6 +712,23 @@ void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
     double rk1 = yx(j, k), rk2 = yy(j, k), rr2 = std::sqrt(rk1 * rk1 + rk2 * rk2);
     double a1 = (rj1 * rk1 + rj2 * rk2) / rr1 / rr2;
     double a2 = (rj1 * rk2 - rj2 * rk1) / rr1 / rr2;
+    if (pre) {  /* :1207-1231 */
+      double bSq = p.Mp * p.Mp / (bt(j, k) - p.Mp * p.Mp * (bt(j, k) - 1));
+      double X = std::sqrt(((1.0 - bSq) * qx(j, k)) * ((1.0 - bSq) * qx(j, k)) + 4. * bSq * cx(j, k) * cx(j, k)) / rr1;
+      double Y = 0.5 * ((1.0 - bSq) * qx(j, k) / rr1 + X);
+      double Z = 0.5 * ((1.0 - bSq) * qx(j, k) / rr1 - X);
+      double X1 = std::sqrt(((1.0 - bSq) * qy(j, k)) * ((1.0 - bSq) * qy(j, k)) + 4. * bSq * cy(j, k) * cy(j, k)) / rr2;
+      double Y1 = 0.5 * ((1.0 - bSq) * qy(j, k) / rr2 + X1);
+      double Z1 = 0.5 * ((1.0 - bSq) * qy(j, k) / rr2 - X1);
+      double a4 = a1 * s(j, k, 2) + (Y * s(j, k, 3) + Z * s(j, k, 4)) * a2 / bSq;
+      double a5 = -(a2 * bSq * s(j, k, 2) - (Y * a1 - Z1) * s(j, k, 3) - (Z * a1 - Z1) * s(j, k, 4)) / X1;
+      double a6 = (a2 * bSq * s(j, k, 2) - (Y * a1 - Y1) * s(j, k, 3) - (Z * a1 - Y1) * s(j, k, 4)) / X1;
+      (void)cjkl;
+      s(j, k, 2) = a4;
+      s(j, k, 3) = a5;
+      s(j, k, 4) = a6;
+      continue;
+    }
     double a4 = a1 * s(j, k, 2) + (cjkl * s(j, k, 3) - cjkl * s(j, k, 4)) * a2;
     double a5 = -0.5 * (a2 * s(j, k, 2) / cjkl - (a1 + 1) * s(j, k, 3) + (a1 - 1) * s(j, k, 4));
     double a6 = 0.5 * (a2 * s(j, k, 2) / cjkl - (a1 - 1) * s(j, k, 3) + (a1 + 1) * s(j, k, 4));
@@ -703,6 +749,27 @@ void arc2d(const P& p, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy, A2 ug, A2 vg, A2 
     double uu = q(j, k, 2), vv = q(j, k, 3);
     double cjkl = std::sqrt(ggm1 * (q(j, k, 4) - uv(j, k)));
     double rk1 = yx(j, k), rk2 = yy(j, k);
+    if (pre) {  /* :1264-1298 */
+      double qq2 = qy(j, k);
+      double rr2 = std::sqrt(rk1 * rk1 + rk2 * rk2);
+      rk1 = rk1 / rr2; rk2 = rk2 / rr2;
+      double bSq = p.Mp * p.Mp / (bt(j, k) - p.Mp * p.Mp * (bt(j, k) - 1));
+      double X = std::sqrt(((1. - bSq) * qq2) * ((1. - bSq) * qq2) + 4. * bSq * cy(j, k) * cy(j, k)) / rr2;
+      double Y = 0.5 * ((1. - bSq) * qq2 / rr2 + X);
+      double Z = 0.5 * ((1. - bSq) * qq2 / rr2 - X);
+      double qqmxt = qq2 + ug(j, k) * rk1 * rr2 + vg(j, k) * rk2 * rr2;
+      double a1 = s(j, k, 1) + s(j, k, 3) + s(j, k, 4);
+      double a2 = uu * s(j, k, 1) + rk2 * s(j, k, 2) + (uu + rk1 * Y / bSq) * s(j, k, 3);
+      a2 = a2 + (uu + rk1 * Z / bSq) * s(j, k, 4);
+      double a3 = vv * s(j, k, 1) - rk1 * s(j, k, 2) + (vv + rk2 * Y / bSq) * s(j, k, 3);
+      a3 = a3 + (vv + rk2 * Z / bSq) * s(j, k, 4);
+      double a4 = uv(j, k) * s(j, k, 1) + (rk2 * uu - rk1 * vv) * s(j, k, 2);
+      a4 = a4 + (ge(j, k) + Y * qqmxt / rr2 / bSq) * s(j, k, 3);
+      a4 = a4 + (ge(j, k) + Z * qqmxt / rr2 / bSq) * s(j, k, 4);
+      (void)cjkl;
+      s(j, k, 1) = a1; s(j, k, 2) = a2; s(j, k, 3) = a3; s(j, k, 4) = a4;
+      continue;
+    }
     double qq2 = qy(j, k) + (rk1 * ug(j, k) + rk2 * vg(j, k));
     double rr2 = std::sqrt(rk1 * rk1 + rk2 * rk2);
     rk1 = rk1 / rr2; rk2 = rk2 / rr2;

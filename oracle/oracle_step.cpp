@@ -212,6 +212,11 @@ void oro_arc2d(const P* p, double* q, double* s, double* xx, double* xy, double*
   arc2d(*p, v3(p, q), v3(p, s), v2(p, xx), v2(p, xy), v2(p, yx), v2(p, yy), v2(p, ug), v2(p, vg), v2(p, turmu),
         I2{iblank, p->jd}, v2(p, tscale), v2(p, bt));
 }
+void oro_arc2d_precon(const P* p, double* q, double* s, double* xx, double* xy, double* yx, double* yy, double* ug,
+                      double* vg, double* turmu, const int32_t* iblank, double* tscale, double* bt) {
+  arc2d(*p, v3(p, q), v3(p, s), v2(p, xx), v2(p, xy), v2(p, yx), v2(p, yy), v2(p, ug), v2(p, vg), v2(p, turmu),
+        I2{iblank, p->jd}, v2(p, tscale), v2(p, bt), true);
+}
 int oro_monitor(const P* p, double* q) {
   int n = 0;
   size_t n2 = (size_t)p->jd * p->kd;
@@ -317,7 +322,8 @@ int oro_step_u(const P* pp, double* q, double* s, double* x, double* y, const do
       ilu2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
             v2(pp, turmu + o), ts);
     } else if ((p.ilhs == 2 || p.ilhs == 3) && p.iprecon) {
-      std::fprintf(stderr, "oracle: arc2d_precon not restated\n"); std::abort();
+      arc2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
+            v2(pp, turmu + o), I2{iblank + o, jd}, ts, v2(pp, bt + o), true);   // step.f:174-180
     } else if (p.ilhs == 2 || p.ilhs == 3) {
       arc2d(p, qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o), v2(pp, ug + o), v2(pp, vg + o),
             v2(pp, turmu + o), I2{iblank + o, jd}, ts, v2(pp, bt + o));

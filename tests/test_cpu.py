@@ -157,8 +157,8 @@ def test_oracle_against_golden_history(name):
 
 def test_oracle_precon_reduces_to_plain_at_mp1():
     """Turkel's preconditioner with Mp = 1 is the identity (bSq = 1): in
-    exact arithmetic roetrklflx is roeflx, rhslom leaves s as it is and
-    preilu2d is ilu2d.  The oracle's preconditioned routines and solve agree
+    exact arithmetic roetrklflx is roeflx, rhslom leaves s as it is,
+    preilu2d is ilu2d and arc2d_precon is arc2d.  The oracle's preconditioned routines and solve agree
     with the plain ones to rounding -- a check of the restated eigenvalue
     split, preconditioner transform and sweep signs."""
     c = Case(viscous=True, seed=41, fsmach=0.2)
@@ -178,6 +178,16 @@ def test_oracle_precon_reduces_to_plain_at_mp1():
             L.oro_ilu2d(C.byref(c.p), *args)
         out[pre] = s
     assert relerr(out[1], out[0]) <= 1e-12
+    for ilhs in (2, 3):   # arc2d_precon against arc2d
+        c.p.ilhs = ilhs
+        for pre in (0, 1):
+            q, s = c.q.copy(), s0.copy()
+            args = [ob.ptr(q), ob.ptr(s), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug),
+                    ob.ptr(c.vg), ob.ptr(c.turmu), ob.ptr(c.iblank), ob.ptr(c.tscale), ob.ptr(c.bt)]
+            (L.oro_arc2d_precon if pre else L.oro_arc2d)(C.byref(c.p), *args)
+            out[pre] = s[:4 * c.n2]
+        assert relerr(out[1], out[0]) <= 1e-12
+    c.p.ilhs = 1
     s = s0.copy()
     L.oro_rhslom(C.byref(c.p), ob.ptr(c.q), ob.ptr(s), ob.ptr(c.bt))
     assert relerr(s, s0) <= 1e-12
@@ -205,4 +215,3 @@ def test_oracle_precon_changes_the_solution_below_mp1():
         qs.append(q)
     n2 = prm.jd * prm.kd
     assert relerr(qs[1][:4 * n2], qs[0][:4 * n2]) > 5e-7   # Q/J (J itself is the same grid)
-

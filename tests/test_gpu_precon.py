@@ -1,8 +1,8 @@
 """GPU parity of Turkel's low-Mach preconditioning (iprecon, Mp) against the
 CPU FP64 oracle, through the C-ABI: the drop-in rhsup with roetrklflx
-(eulerrhs.f:450-625), rhslom (sources.f:97-148) and preilu2d (lhs.f:2-467),
-and the batched solver / drop-in step with all three in the iteration
-(step.f:121-123, :161-164; time.f:30-35, :62-66).
+(eulerrhs.f:450-625), rhslom (sources.f:97-148), preilu2d (lhs.f:2-467) and
+arc2d_precon (lhs.f:1060-1330), and the batched solver / drop-in step with
+them in the iteration (step.f:121-123, :154-180; time.f:30-35, :62-66).
 
 bt comes from a dual-time time step (idual = 1), so bSq = Mp**2/(bt -
 Mp**2 (bt-1)) differs from cell to cell.
@@ -112,6 +112,28 @@ def test_preilu2d(visc):
     assert relerr(s2, s) > 1e-6
 
 
+@pytest.mark.parametrize("visc,ilhs", [(False, 2), (True, 2), (True, 3)])
+def test_arc2d_precon(visc, ilhs):
+    c = _pcase(viscous=visc, seed=35)
+    c.p.ilhs = ilhs
+    L = ob.lib()
+    so = np.random.default_rng(23).uniform(-1, 1, c.n2 * c.p.nv) * 1e-4
+    s, qo, q = so.copy(), c.q.copy(), c.q.copy()
+    L.oro_arc2d_precon(_o(c), ob.ptr(qo), ob.ptr(so), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy),
+                       ob.ptr(c.ug), ob.ptr(c.vg), ob.ptr(c.turmu), ob.ptr(c.iblank), ob.ptr(c.tscale), ob.ptr(c.bt))
+    rt.set_params(c.p)
+    p = c.p
+    rt.arc2d_precon(q, s, c.jd, c.kd, p.jbeg, p.jend, p.kbeg, p.kend, c.xx, c.xy, c.yx, c.yy, c.ug, c.vg, c.turmu,
+                    c.iblank, c.tscale, c.bt)
+    assert relerr(s[:4 * c.n2], so[:4 * c.n2]) <= TOL
+    assert relerr(q, qo) <= TOL
+    # arc2d on the same input stays the plain operator
+    s2 = np.random.default_rng(23).uniform(-1, 1, c.n2 * c.p.nv) * 1e-4
+    rt.arc2d(c.q.copy(), s2, c.jd, c.kd, p.jbeg, p.jend, p.kbeg, p.kend, c.xx, c.xy, c.yx, c.yy, c.ug, c.vg,
+             c.turmu, c.iblank, c.tscale, c.bt)
+    assert relerr(s2[:4 * c.n2], s[:4 * c.n2]) > 1e-6
+
+
 def _precon_case(kind):
     if kind == "euler":
         _, prm, xv, yv = api.cmesh_case(97, 25, naca=(0.0, 0.0, 0.12), ds_wall=1e-3, invisc=1, lamin=1, irhsy=-3,
@@ -119,6 +141,13 @@ def _precon_case(kind):
     elif kind == "euler_weno":
         _, prm, xv, yv = api.cmesh_case(97, 25, naca=(0.0, 0.0, 0.12), ds_wall=1e-3, invisc=1, lamin=1, irhsy=-3,
                                         ilim=4, ilhs=1, iconstant_cfl=0, dt=2.0, fsmach=0.1, alfa=2.0)
+    elif kind == "euler_adi":
+        _, prm, xv, yv = api.cmesh_case(97, 25, naca=(0.0, 0.0, 0.12), ds_wall=1e-3, invisc=1, lamin=1, irhsy=-3,
+                                        ilim=1, ilhs=2, iconstant_cfl=1, dt=2.0, fsmach=0.1, alfa=2.0)
+    elif kind == "sa_adi_up":
+        _, prm, xv, yv = api.cmesh_case(97, 33, naca=(0.0, 0.0, 0.12), ds_wall=1e-3, invisc=0, lamin=0, iturb=1,
+                                        irhsy=-3, ilim=1, ilhs=3, iconstant_cfl=1, dt=5.0, fsmach=0.15, alfa=3.0,
+                                        rey=1e6, vnuinf=3.0)
     else:
         _, prm, xv, yv = api.cmesh_case(97, 33, naca=(0.0, 0.0, 0.12), ds_wall=1e-3, invisc=0, lamin=0, iturb=1,
                                         irhsy=-3, ilim=1, ilhs=1, iconstant_cfl=1, dt=5.0, fsmach=0.15, alfa=3.0,
@@ -127,7 +156,7 @@ def _precon_case(kind):
     return prm, xv, yv
 
 
-@pytest.mark.parametrize("kind", ["euler", "euler_weno", "sa"])
+@pytest.mark.parametrize("kind", ["euler", "euler_weno", "sa", "euler_adi", "sa_adi_up"])
 def test_solver_precon_fp64_matches_oracle(kind):
     """The batched solver with iprecon (roetrklflx, rhslom, preilu2d, the
     dual-time switch of time.f:30-35), FP64, against the oracle driver."""

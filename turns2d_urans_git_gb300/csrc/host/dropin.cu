@@ -390,6 +390,38 @@ int lusgs_dropin(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, in
   if (!err && (ist[2] & 4)) err = fail(OT2D_ERR_TIMEOUT);
   return err;
 }
+// arc2d (lhs.f:817-1057) or, pre = true, arc2d_precon (lhs.f:1060-1330) on
+// one time instance; as for the LU-SGS pair the call chooses the routine
+int adi_dropin(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
+               double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu, int32_t* iblank,
+               double* tscale, double* bt, bool pre) {
+  int err = 0;
+  if (prepare(1, err)) return fail(err);
+  const ot2d_params& p = g_ctx.P;
+  if (!dims_ok(jd, kd) || !js || !je || !ks || !ke || *js != p.jbeg || *je != p.jend || *ks != p.kbeg || *ke != p.kend)
+    return fail(OT2D_ERR_ARG);
+  if (!q || !s || !xx || !xy || !yx || !yy || !turmu || !tscale || !iblank || p.jd < 10 || p.kd < 10 || (pre && !bt))
+    return fail(OT2D_ERR_ARG);
+  const size_t n2 = (size_t)p.jd * p.kd;
+  Slice<double> S = base_slice(1, 1, (int64_t)n2);
+  S.k_mp2 = pre ? p.Mp * p.Mp : -1.0;
+  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
+  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
+  S.xx = (double*)resolve(xx, n2 * 8, true, false, err);
+  S.xy = (double*)resolve(xy, n2 * 8, true, false, err);
+  S.yx = (double*)resolve(yx, n2 * 8, true, false, err);
+  S.yy = (double*)resolve(yy, n2 * 8, true, false, err);
+  S.ug = (double*)resolve(ug, n2 * 8, true, false, err);
+  S.vg = (double*)resolve(vg, n2 * 8, true, false, err);
+  S.turmu = (double*)resolve(turmu, n2 * 8, true, false, err);
+  S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
+  S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
+  S.bt = bt ? (double*)resolve(bt, n2 * 8, true, false, err) : nullptr;
+  std::vector<Slice<double>> sl{S};
+  run_batch(sl, err);
+  if (!err && launch_adi<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
+  return finish(err);
+}
 }  // namespace
 }  // namespace ot2d
 
@@ -600,31 +632,13 @@ int ot2d_rhslom(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int
 int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks, int32_t* ke,
                double* xx, double* xy, double* yx, double* yy, double* ug, double* vg, double* turmu, int32_t* iblank,
                double* tscale, double* bt) {
-  int err = 0;
-  if (prepare(1, err)) return fail(err);
-  const ot2d_params& p = g_ctx.P;
-  if (!dims_ok(jd, kd) || !js || !je || !ks || !ke || *js != p.jbeg || *je != p.jend || *ks != p.kbeg || *ke != p.kend)
-    return fail(OT2D_ERR_ARG);
-  if (!q || !s || !xx || !xy || !yx || !yy || !turmu || !tscale || !iblank || p.jd < 10 || p.kd < 10)
-    return fail(OT2D_ERR_ARG);
-  const size_t n2 = (size_t)p.jd * p.kd;
-  Slice<double> S = base_slice(1, 1, (int64_t)n2);
-  S.q = S.q64 = (double*)resolve(q, n2 * p.nq * 8, true, true, err);
-  S.s = (double*)resolve(s, n2 * p.nv * 8, true, true, err);
-  S.xx = (double*)resolve(xx, n2 * 8, true, false, err);
-  S.xy = (double*)resolve(xy, n2 * 8, true, false, err);
-  S.yx = (double*)resolve(yx, n2 * 8, true, false, err);
-  S.yy = (double*)resolve(yy, n2 * 8, true, false, err);
-  S.ug = (double*)resolve(ug, n2 * 8, true, false, err);
-  S.vg = (double*)resolve(vg, n2 * 8, true, false, err);
-  S.turmu = (double*)resolve(turmu, n2 * 8, true, false, err);
-  S.iblank = (int32_t*)resolve(iblank, n2 * 4, true, false, err);
-  S.tscale = (double*)resolve(tscale, n2 * 8, true, false, err);
-  S.bt = bt ? (double*)resolve(bt, n2 * 8, true, false, err) : nullptr;
-  std::vector<Slice<double>> sl{S};
-  run_batch(sl, err);
-  if (!err && launch_adi<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
-  return finish(err);
+  return adi_dropin(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, iblank, tscale, bt, false);
+}
+
+int ot2d_arc2d_precon(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks,
+                      int32_t* ke, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
+                      double* turmu, int32_t* iblank, double* tscale, double* bt) {
+  return adi_dropin(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, iblank, tscale, bt, true);
 }
 
 int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
@@ -738,9 +752,8 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   if (!dims_ok(jd, kd) || p.ilhs < 1 || p.ilhs > 3 || (p.iunst != 0 && !swept) || (newton && p.timespectral) ||
       (!p.lamin && p.iturb != 1 && p.iturb != 2) || p.itrans != 0)
     return fail(OT2D_ERR_ARG);
-  // Turkel preconditioning: rhslom and preilu2d read bt; the preconditioned
-  // ADI operator (arc2d_precon) is not built
-  if (p.iprecon && (!bt || p.ilhs != 1)) return fail(OT2D_ERR_ARG);
+  // Turkel preconditioning: rhslom, preilu2d and arc2d_precon read bt
+  if (p.iprecon && !bt) return fail(OT2D_ERR_ARG);
   if (!q || !s || !x || !y || !xv || !yv || !iblank || !xx || !xy || !yx || !yy || !turmu || !tscale) return fail(OT2D_ERR_ARG);
   if (p.timespectral && (!ugv || !vgv || !ug || !vg || !Ds)) return fail(OT2D_ERR_ARG);
   if (swept && (!xold || !yold || !xole || !yole || !ug || !vg)) return fail(OT2D_ERR_ARG);

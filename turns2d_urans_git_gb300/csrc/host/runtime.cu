@@ -179,9 +179,8 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
                         p.dt > 0 && p.h > 0))
     return OT2D_ERR_ARG;
   if (p.itnmax < 1 || (p.itnmax > 1 && p.iunst != 1)) return OT2D_ERR_ARG;
-  // Turkel preconditioning with the LU-SGS operator (preilu2d); the
-  // preconditioned ADI (arc2d_precon) is not built
-  if (p.iprecon && (p.ilhs != 1 || !(p.Mp > 0))) return OT2D_ERR_ARG;
+  // Turkel preconditioning (preilu2d with LU-SGS, arc2d_precon with ADI)
+  if (p.iprecon && !(p.Mp > 0)) return OT2D_ERR_ARG;
   d = DevSolve{};
   d.P = p; d.precision = precision; d.nspec = p.nspec;
   // time.f:30-35: with time-accurate low-Mach preconditioning the time step

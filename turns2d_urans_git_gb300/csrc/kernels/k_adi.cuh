@@ -30,6 +30,13 @@ __device__ __forceinline__ bool adi_slice(const ot2d_params& p) { return p.ilhs 
 // line view of direction dir (0: j lines, m = j, n = k; 1: k lines, m = k, n = j)
 __device__ __forceinline__ int64_t adi_at(int jd, int dir, int m, int n) { return dir == 0 ? at(jd, m, n) : at(jd, n, m); }
 
+// bSq = Mp**2/(bt - Mp**2 (bt-1)) of cell o (arc2d_precon, lhsinv)
+template <class R>
+__device__ __forceinline__ R adi_bsq(const Slice<R>& S, int64_t o) {
+  const R btv = S.bt ? S.bt[o] : (R)1.;
+  return S.k_mp2 / (btv - S.k_mp2 * (btv - (R)1));
+}
+
 // s *= tscale when `scale` (step.f:141-148), primitive variables (:853-860) and the
 // T_xi^-1 multiplication with its per-cell factors (:863-917), on every
 // cell of js-1..je+1 x ks-1..ke+1
@@ -52,13 +59,20 @@ __device__ void adi_txi_cell(const Slice<R>& S, const ot2d_params& p, int j, int
   S.w[A_P * ws + o] = (e - uv2) * gm1 * rho;
   R rj1 = S.xx[o], rj2 = S.xy[o];
   const R ugc = S.ug ? S.ug[o] : (R)0, vgc = S.vg ? S.vg[o] : (R)0;
-  const R qq1 = rj1 * uu + rj2 * vv;
-  S.w[A_QX * ws + o] = qq1 - (rj1 * ugc + rj2 * vgc);
+  // arc2d_precon (:1116, :1125) takes the contravariant velocities relative
+  // to the grid before storing them; arc2d (:874-876) subtracts afterwards
+  const bool pre = S.k_mp2 >= (R)0;
+  const R qq1 = pre ? rj1 * (uu - ugc) + rj2 * (vv - vgc) : rj1 * uu + rj2 * vv;
+  S.w[A_QX * ws + o] = pre ? qq1 : qq1 - (rj1 * ugc + rj2 * vgc);
   const R rr1 = sqrt(sq(rj1) + sq(rj2));
   rj1 = rj1 / rr1; rj2 = rj2 / rr1;
   const R rk1 = S.yx[o], rk2 = S.yy[o];
-  const R qq2 = rk1 * uu + rk2 * vv;
-  S.w[A_QY * ws + o] = qq2 - (rk1 * ugc + rk2 * vgc);
+  if (pre) {
+    S.w[A_QY * ws + o] = rk1 * (uu - ugc) + rk2 * (vv - vgc);
+  } else {
+    const R qq2 = rk1 * uu + rk2 * vv;
+    S.w[A_QY * ws + o] = qq2 - (rk1 * ugc + rk2 * vgc);
+  }
   const R rr2 = sqrt(sq(rk1) + sq(rk2));
   S.w[A_UV * ws + o] = uv2;
   S.w[A_CX * ws + o] = cjkl * rr1;
@@ -72,9 +86,23 @@ __device__ void adi_txi_cell(const Slice<R>& S, const ot2d_params& p, int j, int
   const R a2 = (rj1 * vv - rj2 * uu) * s1 + rj2 * s2 - rj1 * s3;
   R a3 = uv2 * s1 - s2 * uu - s3 * vv + s4;
   a3 = a3 * gm1 * c2i;
-  const R a4 = qq1 * s1 / rr1 - rj1 * s2 - rj2 * s3;
   S.s[o] = a1;
   S.s[qs + o] = a2;
+  if (pre) {
+    // arc2d_precon :1141-1164: the preconditioned acoustic eigenvectors
+    const R bSq = adi_bsq(S, o), omb = (R)1. - bSq;
+    const R cx = cjkl * rr1;
+    const R X = sqrt((omb * qq1) * (omb * qq1) + (R)4. * bSq * cx * cx) / rr1;
+    const R Y = (R)0.5 * (omb * qq1 / rr1 + X);
+    const R Z = (R)0.5 * (omb * qq1 / rr1 - X);
+    const R qqmxt = qq1 + ugc * rj1 * rr1 + vgc * rj2 * rr1;
+    R a4 = qqmxt * s1 / rr1 - rj1 * s2 - rj2 * s3;
+    a4 = a4 * bSq;
+    S.s[2 * qs + o] = -(Z * a3 + a4) / X;
+    S.s[3 * qs + o] = (Y * a3 + a4) / X;
+    return;
+  }
+  const R a4 = qq1 * s1 / rr1 - rj1 * s2 - rj2 * s3;
   S.s[2 * qs + o] = (R)0.5 * (a3 - a4 / cjkl);
   S.s[3 * qs + o] = (R)0.5 * (a3 + a4 / cjkl);
 }
@@ -340,6 +368,21 @@ __device__ void adi_ninv_cell(const Slice<R>& S, const ot2d_params& p, int j, in
   const R a1 = (rj1 * rk1 + rj2 * rk2) / rr1 / rr2;
   const R a2 = (rj1 * rk2 - rj2 * rk1) / rr1 / rr2;
   const R s2 = S.s[qs + o], s3 = S.s[2 * qs + o], s4 = S.s[3 * qs + o];
+  if (S.k_mp2 >= (R)0) {
+    // arc2d_precon :1207-1231
+    const R bSq = adi_bsq(S, o), omb = (R)1.0 - bSq;
+    const R qx = S.w[A_QX * ws + o], qy = S.w[A_QY * ws + o], cx = S.w[A_CX * ws + o], cy = S.w[A_CY * ws + o];
+    const R X = sqrt((omb * qx) * (omb * qx) + (R)4. * bSq * cx * cx) / rr1;
+    const R Y = (R)0.5 * (omb * qx / rr1 + X);
+    const R Z = (R)0.5 * (omb * qx / rr1 - X);
+    const R X1 = sqrt((omb * qy) * (omb * qy) + (R)4. * bSq * cy * cy) / rr2;
+    const R Y1 = (R)0.5 * (omb * qy / rr2 + X1);
+    const R Z1 = (R)0.5 * (omb * qy / rr2 - X1);
+    S.s[qs + o] = a1 * s2 + (Y * s3 + Z * s4) * a2 / bSq;
+    S.s[2 * qs + o] = -(a2 * bSq * s2 - (Y * a1 - Z1) * s3 - (Z * a1 - Z1) * s4) / X1;
+    S.s[3 * qs + o] = (a2 * bSq * s2 - (Y * a1 - Y1) * s3 - (Z * a1 - Y1) * s4) / X1;
+    return;
+  }
   const R a4 = a1 * s2 + (cjkl * s3 - cjkl * s4) * a2;
   const R a5 = (R)-0.5 * (a2 * s2 / cjkl - (a1 + (R)1) * s3 + (a1 - (R)1) * s4);
   const R a6 = (R)0.5 * (a2 * s2 / cjkl - (a1 - (R)1) * s3 + (a1 + (R)1) * s4);
@@ -355,18 +398,36 @@ __device__ void adi_teta_cell(const Slice<R>& S, const ot2d_params& p, int j, in
   const R cjkl = sqrt(S.k_ggm1 * (S.w[A_E * ws + o] - uv));
   R rk1 = S.yx[o], rk2 = S.yy[o];
   const R ugc = S.ug ? S.ug[o] : (R)0, vgc = S.vg ? S.vg[o] : (R)0;
-  const R qq2 = S.w[A_QY * ws + o] + (rk1 * ugc + rk2 * vgc);
+  const bool pre = S.k_mp2 >= (R)0;
+  const R qq2 = pre ? S.w[A_QY * ws + o] : S.w[A_QY * ws + o] + (rk1 * ugc + rk2 * vgc);
   const R rr2 = sqrt(rk1 * rk1 + rk2 * rk2);
   rk1 = rk1 / rr2; rk2 = rk2 / rr2;
   const R s1 = S.s[o], s2 = S.s[qs + o], s3 = S.s[2 * qs + o], s4 = S.s[3 * qs + o];
   const R a1 = s1 + s3 + s4;
-  R a2 = uu * s1 + rk2 * s2 + (uu + rk1 * cjkl) * s3;
-  a2 = a2 + (uu - rk1 * cjkl) * s4;
-  R a3 = vv * s1 - rk1 * s2 + (vv + rk2 * cjkl) * s3;
-  a3 = a3 + (vv - rk2 * cjkl) * s4;
-  R a4 = uv * s1 + (rk2 * uu - rk1 * vv) * s2;
-  a4 = a4 + (ge + cjkl * qq2 / rr2) * s3;
-  a4 = a4 + (ge - cjkl * qq2 / rr2) * s4;
+  R a2, a3, a4;
+  if (pre) {
+    // arc2d_precon :1264-1298
+    const R bSq = adi_bsq(S, o), omb = (R)1. - bSq, cy = S.w[A_CY * ws + o];
+    const R X = sqrt((omb * qq2) * (omb * qq2) + (R)4. * bSq * cy * cy) / rr2;
+    const R Y = (R)0.5 * (omb * qq2 / rr2 + X);
+    const R Z = (R)0.5 * (omb * qq2 / rr2 - X);
+    const R qqmxt = qq2 + ugc * rk1 * rr2 + vgc * rk2 * rr2;
+    a2 = uu * s1 + rk2 * s2 + (uu + rk1 * Y / bSq) * s3;
+    a2 = a2 + (uu + rk1 * Z / bSq) * s4;
+    a3 = vv * s1 - rk1 * s2 + (vv + rk2 * Y / bSq) * s3;
+    a3 = a3 + (vv + rk2 * Z / bSq) * s4;
+    a4 = uv * s1 + (rk2 * uu - rk1 * vv) * s2;
+    a4 = a4 + (ge + Y * qqmxt / rr2 / bSq) * s3;
+    a4 = a4 + (ge + Z * qqmxt / rr2 / bSq) * s4;
+  } else {
+    a2 = uu * s1 + rk2 * s2 + (uu + rk1 * cjkl) * s3;
+    a2 = a2 + (uu - rk1 * cjkl) * s4;
+    a3 = vv * s1 - rk1 * s2 + (vv + rk2 * cjkl) * s3;
+    a3 = a3 + (vv - rk2 * cjkl) * s4;
+    a4 = uv * s1 + (rk2 * uu - rk1 * vv) * s2;
+    a4 = a4 + (ge + cjkl * qq2 / rr2) * s3;
+    a4 = a4 + (ge - cjkl * qq2 / rr2) * s4;
+  }
   R o2 = a2, o3 = a3;
   if (p.iunst == 2) {
     const R tsr = S.tscale[o] * (R)p.rotf;

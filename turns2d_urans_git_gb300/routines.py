@@ -110,6 +110,12 @@ def arc2d(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, iblank, t
           _p(yx), _p(yy), _p(ug), _p(vg), _p(turmu), _p(iblank), _p(tscale), _p(bt))
 
 
+def arc2d_precon(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, iblank, tscale, bt):
+    """src/lhs.f:1060 -- the ADI operator with Turkel's low-Mach preconditioner."""
+    _call("ot2d_arc2d_precon", _p(q), _p(s), _ref(jd), _ref(kd), _ref(js), _ref(je), _ref(ks), _ref(ke), _p(xx),
+          _p(xy), _p(yx), _p(yy), _p(ug), _p(vg), _p(turmu), _p(iblank), _p(tscale), _p(bt))
+
+
 def vmu_sa(q, s, turmu, x, y, xv, yv, xx, xy, yx, yy, ug, vg, jd, kd, tscale, iblank, im, nsp):
     """src/samodel2d.f:2 -- one Spalart-Allmaras update of q(:,:,5) and turmu."""
     _call("ot2d_vmu_sa", _p(q), _p(s), _p(turmu), _p(x), _p(y), _p(xv), _p(yv), _p(xx), _p(xy), _p(yx), _p(yy),
