@@ -124,6 +124,15 @@ int ot2d_arc2d(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int3
 int ot2d_arc2d_precon(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int32_t* je, int32_t* ks,
                       int32_t* ke, double* xx, double* xy, double* yx, double* yy, double* ug, double* vg,
                       double* turmu, int32_t* iblank, double* tscale, double* bt);
+/* src/connectivity.f:2-3: overset interpolation of q between the meshes of
+ * one grid system (the donor / fringe lists of the reference's connectivity,
+ * 1-based, Fortran-ordered; qg holds each mesh's q(jmx,kmx,nspec,nq) one
+ * after another).  Every donor is gathered before any fringe cell is
+ * written; a fringe cell listed twice takes its last entry.  Donor stencils
+ * must lie inside their mesh and rows inside qbc (OT2D_ERR_ARG otherwise). */
+int ot2d_do_interpolations(double* qg, int32_t* jmx, int32_t* kmx, int32_t* ibcg, int32_t* imeshg, int32_t* idonorg,
+                           double* fracg, int32_t* nfringeg, int32_t* ndonorg, int32_t* iisptrg, int32_t* iieptrg,
+                           int32_t* idsize, int32_t* qsize, int32_t* nmesh);
 /* src/samodel2d.f:2-3 */
 int ot2d_vmu_sa(double* q, double* s, double* turmu, double* x, double* y, double* xv, double* yv, double* xx,
                 double* xy, double* yx, double* yy, double* ug, double* vg, int32_t* jd, int32_t* kd,

@@ -56,6 +56,8 @@ def lib():
         L.oro_komegasst.argtypes = [_P] + [_dp] * 14 + [_ip, _dp]
         L.oro_arc2d.argtypes = [_P] + [_dp] * 9 + [_ip, _dp, _dp]
         L.oro_arc2d_precon.argtypes = [_P] + [_dp] * 9 + [_ip, _dp, _dp]
+        L.oro_do_interpolations.argtypes = [_P, _dp, _ip, _ip, _ip, _ip, _ip, _dp, _ip, _ip, _ip, _ip, C.c_int32,
+                                             C.c_int64, C.c_int32]
         L.oro_monitor.argtypes = [_P, _dp]
         L.oro_monitor.restype = C.c_int
         L.oro_force2d.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]

@@ -215,3 +215,43 @@ def test_oracle_precon_changes_the_solution_below_mp1():
         qs.append(q)
     n2 = prm.jd * prm.kd
     assert relerr(qs[1][:4 * n2], qs[0][:4 * n2]) > 5e-7   # Q/J (J itself is the same grid)
+
+
+@pytest.mark.parametrize("nspec", [1, 3])
+def test_oracle_overset_interpolation_is_exact_for_quadratics(nspec):
+    """do_interpolations' 9-point weights (connectivity.f:89-97) are the
+    tensor-product quadratic Lagrange basis at offsets (frac1, frac2) from the
+    donor cell: on a bi-quadratic field of q*J (mean flow) and q (turbulence)
+    every fringe cell receives the field's value at its donor point, and
+    cells that are not fringe cells keep their values."""
+    from tests.overset_case import make_params, make_system, oracle_interp
+    poly = lambda j, k: 1.5 + 0.2 * j - 0.1 * k + 0.03 * j * j + 0.02 * j * k - 0.05 * k * k + 0.001 * j * j * k * k
+    p = make_params(nspec)
+    sysd = make_system(p, 5, poly=poly, dup=False)
+    qg = oracle_interp(ob.lib(), ob.ptr, p, sysd)
+    off = 0
+    blocks = []
+    for jm, km in zip(sysd["jmx"], sysd["kmx"]):
+        n = jm * km * nspec * p.nq
+        blocks.append((qg[off:off + n].reshape((jm, km, nspec, p.nq), order="F"),
+                       sysd["qg"][off:off + n].reshape((jm, km, nspec, p.nq), order="F")))
+        off += n
+    for s in range(nspec):
+        # donor point of every qbc row
+        pts = {}
+        for im in range(sysd["nmesh"]):
+            for d in range(sysd["ndonorg"][im, s]):
+                row = sysd["iisptrg"][im, s] + d
+                pts[row] = (sysd["idonorg"][d, 0, im, s] + sysd["fracg"][d, 0, im, s],
+                            sysd["idonorg"][d, 1, im, s] + sysd["fracg"][d, 1, im, s])
+        for im, (new, old) in enumerate(blocks):
+            touched = np.zeros(new.shape[:2], dtype=bool)
+            for f in range(sysd["nfringeg"][im, s]):
+                ii, jj = sysd["imeshg"][f, 0, im, s], sysd["imeshg"][f, 1, im, s]
+                x, y = pts[sysd["ibcg"][f, im, s]]
+                touched[ii - 1, jj - 1] = True
+                for n in range(p.nv):
+                    want = poly(x, y) * (n + 1)
+                    got = new[ii - 1, jj - 1, s, n] * (new[ii - 1, jj - 1, s, p.nq - 1] if n < p.nmv else 1.0)
+                    assert abs(got - want) <= 1e-12 * abs(want)
+            assert np.array_equal(new[~touched][:, s, :], old[~touched][:, s, :])

@@ -422,6 +422,68 @@ int adi_dropin(double* q, double* s, int32_t* jd, int32_t* kd, int32_t* js, int3
   if (!err && launch_adi<double>(g_ctx.batch.d_sl, g_ctx.batch.b, 0, g_ctx.st, 0) != cudaSuccess) err = OT2D_ERR_CUDA;
   return finish(err);
 }
+// ---- overset interpolation (connectivity.f:2-190) ---------------------------
+// One donor: where its mesh's q block starts for its time instance, the
+// distance between variables, the mesh's jd, the donor cell, its offsets
+// and the qbc row it fills (qbc: per time instance a (bcdim, nv) block).
+struct OvsDon { int64_t qbase, vstride, boff; int32_t jm, ii, jj, bcdim, row, pad; double f1, f2; };
+// One fringe cell: the same addressing, the qbc row it takes.
+struct OvsFr { int64_t qbase, vstride, boff; int32_t jm, ii, jj, bcdim, row, pad; };
+
+// :69-128 -- 9-point quadratic Lagrange weights (exact power-of-two
+// scalings, so their grouping does not change a bit) on q*J (mean flow) and
+// q (turbulence variables)
+__global__ void k_ovs_gather(const OvsDon* __restrict__ dn, int nd, const double* __restrict__ qg,
+                             double* __restrict__ qbc, int nq, int nv, int nmv) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nd) return;
+  const OvsDon d = dn[e];
+  const double onefourth = 1. / 4;
+  const double djm1 = 1. + d.f1, dkm1 = 1. + d.f2, dj0 = d.f1, dk0 = d.f2, djp1 = 1. - d.f1, dkp1 = 1. - d.f2;
+  double w[9];
+  w[0] = (dj0 * djp1 * dk0 * dkp1) * onefourth;
+  w[1] = -(2 * (djm1 * djp1 * dk0 * dkp1) * onefourth);
+  w[2] = -((djm1 * dj0 * dk0 * dkp1) * onefourth);
+  w[3] = -(2 * (dj0 * djp1 * dkm1 * dkp1) * onefourth);
+  w[4] = 4 * (djm1 * djp1 * dkm1 * dkp1) * onefourth;
+  w[5] = 2 * (djm1 * dj0 * dkm1 * dkp1) * onefourth;
+  w[6] = -((dj0 * djp1 * dkm1 * dk0) * onefourth);
+  w[7] = 2 * (djm1 * djp1 * dkm1 * dk0) * onefourth;
+  w[8] = (djm1 * dj0 * dkm1 * dk0) * onefourth;
+  // stencil cells (ii-1..ii+1, jj-1..jj+1), j fastest, in the reference's term order
+  int64_t c[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) c[t] = d.qbase + (int64_t)(d.jj - 2 + t / 3) * d.jm + (d.ii - 2 + t % 3);
+  const double* J = qg + (int64_t)(nq - 1) * d.vstride;
+  for (int n = 1; n <= nv; ++n) {
+    const double* qn = qg + (int64_t)(n - 1) * d.vstride;
+    double a;
+    if (n <= nmv) {
+      a = w[0] * qn[c[0]] * J[c[0]];
+#pragma unroll
+      for (int t = 1; t < 9; ++t) a = a + w[t] * qn[c[t]] * J[c[t]];
+    } else {
+      a = w[0] * qn[c[0]];
+#pragma unroll
+      for (int t = 1; t < 9; ++t) a = a + w[t] * qn[c[t]];
+    }
+    qbc[d.boff + (int64_t)(n - 1) * d.bcdim + (d.row - 1)] = a;
+  }
+}
+
+// :154-167 -- fringe cells from qbc (mean flow divided by J)
+__global__ void k_ovs_scatter(const OvsFr* __restrict__ fr, int nf, double* __restrict__ qg,
+                              const double* __restrict__ qbc, int nq, int nv, int nmv) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nf) return;
+  const OvsFr f = fr[e];
+  const int64_t o = f.qbase + (int64_t)(f.jj - 1) * f.jm + (f.ii - 1);
+  const double J = qg[(int64_t)(nq - 1) * f.vstride + o];
+  for (int n = 1; n <= nv; ++n) {
+    const double v = qbc[f.boff + (int64_t)(n - 1) * f.bcdim + (f.row - 1)];
+    qg[(int64_t)(n - 1) * f.vstride + o] = n <= nmv ? v / J : v;
+  }
+}
 }  // namespace
 }  // namespace ot2d
 
@@ -1125,6 +1187,92 @@ int ot2d_stqol(double* q, double* qtn, double* qtnm1, double* qnewt, int32_t* jd
   double* d3 = (double*)resolve(qnewt, qs * p.nv * 8, false, true, err);
   if (!err && launch_stqol(dq, d1, d2, d3, (int64_t)qs, p.nv, p.ntac, p.istep, g_ctx.st) != cudaSuccess)
     err = OT2D_ERR_CUDA;
+  return finish(err);
+}
+
+int ot2d_do_interpolations(double* qg, int32_t* jmx, int32_t* kmx, int32_t* ibcg, int32_t* imeshg, int32_t* idonorg,
+                           double* fracg, int32_t* nfringeg, int32_t* ndonorg, int32_t* iisptrg, int32_t* iieptrg,
+                           int32_t* idsize, int32_t* qsize, int32_t* nmesh) {
+  int err = ensure_stream();
+  if (err) return fail(err);
+  if (!g_ctx.has) return fail(OT2D_ERR_NOPARAMS);
+  const ot2d_params& p = g_ctx.P;
+  if (!qg || !jmx || !kmx || !ibcg || !imeshg || !idonorg || !fracg || !nfringeg || !ndonorg || !iisptrg || !iieptrg ||
+      !idsize || !qsize || !nmesh || *nmesh < 1 || *idsize < 0 || *qsize < 0 || p.nspec < 1 || p.nv < p.nmv ||
+      p.nq <= p.nv)
+    return fail(OT2D_ERR_ARG);
+  const int nm = *nmesh, ns = p.nspec, ids = *idsize;
+  // the connectivity is read on the host (it is the caller's, possibly device memory)
+  std::vector<int32_t> hj(nm), hk(nm), nfr((size_t)nm * ns), ndo((size_t)nm * ns), iis((size_t)nm * ns),
+      iie((size_t)nm * ns);
+  const size_t nid = (size_t)ids * 2 * nm * ns;
+  std::vector<int32_t> hib((size_t)ids * nm * ns), hmesh(nid), hdon(nid);
+  std::vector<double> hfr(nid);
+  if ((err = fetch(jmx, nm * 4, hj.data())) || (err = fetch(kmx, nm * 4, hk.data())) ||
+      (err = fetch(nfringeg, nfr.size() * 4, nfr.data())) || (err = fetch(ndonorg, ndo.size() * 4, ndo.data())) ||
+      (err = fetch(iisptrg, iis.size() * 4, iis.data())) || (err = fetch(iieptrg, iie.size() * 4, iie.data())) ||
+      (err = fetch(ibcg, hib.size() * 4, hib.data())) || (err = fetch(imeshg, nid * 4, hmesh.data())) ||
+      (err = fetch(idonorg, nid * 4, hdon.data())) || (err = fetch(fracg, nid * 8, hfr.data())))
+    return fail(err);
+  // mesh blocks of qg (connectivity.f:57-65): q(jmx, kmx, nspec, nq) one after another
+  std::vector<int64_t> qoff(nm + 1, 0);
+  for (int im = 0; im < nm; ++im) {
+    if (hj[im] < 3 || hk[im] < 3) return fail(OT2D_ERR_ARG);
+    qoff[im + 1] = qoff[im] + (int64_t)hj[im] * hk[im] * ns * p.nq;
+  }
+  if (qoff[nm] > (int64_t)*qsize) return fail(OT2D_ERR_ARG);
+  std::vector<int64_t> boff(ns + 1, 0);
+  for (int s = 0; s < ns; ++s) {
+    const int bcdim = iie[(size_t)s * nm + (nm - 1)];
+    if (bcdim < 0) return fail(OT2D_ERR_ARG);
+    boff[s + 1] = boff[s] + (int64_t)bcdim * p.nv;
+  }
+  // every index is checked here, so the kernels read and write in bounds
+  std::vector<OvsDon> dons;
+  std::vector<OvsFr> frs;
+  std::map<int64_t, size_t> last;   // fringe cell -> its last entry (the reference's later write wins)
+  for (int s = 0; s < ns; ++s) {
+    const int bcdim = iie[(size_t)s * nm + (nm - 1)];
+    for (int im = 0; im < nm; ++im) {
+      const size_t mi = (size_t)s * nm + im;
+      const int jm = hj[im], km = hk[im];
+      const int64_t vstride = (int64_t)jm * km * ns, qbase = qoff[im] + (int64_t)jm * km * s;
+      if (ndo[mi] < 0 || ndo[mi] > ids || nfr[mi] < 0 || nfr[mi] > ids) return fail(OT2D_ERR_ARG);
+      for (int id = 0; id < ndo[mi]; ++id) {
+        OvsDon d{};
+        d.qbase = qbase; d.vstride = vstride; d.boff = boff[s]; d.jm = jm; d.bcdim = bcdim;
+        d.ii = hdon[(mi * 2 + 0) * ids + id]; d.jj = hdon[(mi * 2 + 1) * ids + id];
+        d.f1 = hfr[(mi * 2 + 0) * ids + id]; d.f2 = hfr[(mi * 2 + 1) * ids + id];
+        d.row = iis[mi] + id;
+        if (d.ii < 2 || d.ii > jm - 1 || d.jj < 2 || d.jj > km - 1 || d.row < 1 || d.row > bcdim)
+          return fail(OT2D_ERR_ARG);
+        dons.push_back(d);
+      }
+      for (int id = 0; id < nfr[mi]; ++id) {
+        OvsFr f{};
+        f.qbase = qbase; f.vstride = vstride; f.boff = boff[s]; f.jm = jm; f.bcdim = bcdim;
+        f.row = hib[mi * ids + id];
+        f.ii = hmesh[(mi * 2 + 0) * ids + id]; f.jj = hmesh[(mi * 2 + 1) * ids + id];
+        if (f.ii < 1 || f.ii > jm || f.jj < 1 || f.jj > km || f.row < 1 || f.row > bcdim) return fail(OT2D_ERR_ARG);
+        const int64_t cell = qbase + (int64_t)(f.jj - 1) * jm + (f.ii - 1);
+        auto it = last.find(cell);
+        if (it != last.end()) frs[it->second] = f;
+        else { last[cell] = frs.size(); frs.push_back(f); }
+      }
+    }
+  }
+  double* dq = (double*)resolve(qg, (size_t)qoff[nm] * 8, true, true, err);
+  OvsDon* ddn = dons.empty() ? nullptr : (OvsDon*)resolve(dons.data(), dons.size() * sizeof(OvsDon), true, false, err);
+  OvsFr* dfr = frs.empty() ? nullptr : (OvsFr*)resolve(frs.data(), frs.size() * sizeof(OvsFr), true, false, err);
+  double* dqbc = nullptr;
+  if (!err && boff[ns] > 0) {
+    if (cudaMalloc(&dqbc, (size_t)boff[ns] * 8) != cudaSuccess) err = OT2D_ERR_NOMEM;
+    else g_ctx.pool.push_back(dqbc);
+  }
+  const int nd = (int)dons.size(), nf = (int)frs.size();
+  if (!err && nd > 0) k_ovs_gather<<<(nd + 127) / 128, 128, 0, g_ctx.st>>>(ddn, nd, dq, dqbc, p.nq, p.nv, p.nmv);
+  if (!err && nf > 0) k_ovs_scatter<<<(nf + 127) / 128, 128, 0, g_ctx.st>>>(dfr, nf, dq, dqbc, p.nq, p.nv, p.nmv);
+  if (!err && cudaGetLastError() != cudaSuccess) err = OT2D_ERR_CUDA;
   return finish(err);
 }
 

@@ -116,6 +116,13 @@ def arc2d_precon(q, s, jd, kd, js, je, ks, ke, xx, xy, yx, yy, ug, vg, turmu, ib
           _p(xy), _p(yx), _p(yy), _p(ug), _p(vg), _p(turmu), _p(iblank), _p(tscale), _p(bt))
 
 
+def do_interpolations(qg, jmx, kmx, ibcg, imeshg, idonorg, fracg, nfringeg, ndonorg, iisptrg, iieptrg, idsize,
+                      qsize, nmesh):
+    """src/connectivity.f:2 -- overset interpolation: donors gathered, fringe cells overwritten."""
+    _call("ot2d_do_interpolations", _p(qg), _p(jmx), _p(kmx), _p(ibcg), _p(imeshg), _p(idonorg), _p(fracg),
+          _p(nfringeg), _p(ndonorg), _p(iisptrg), _p(iieptrg), _ref(idsize), _ref(qsize), _ref(nmesh))
+
+
 def vmu_sa(q, s, turmu, x, y, xv, yv, xx, xy, yx, yy, ug, vg, jd, kd, tscale, iblank, im, nsp):
     """src/samodel2d.f:2 -- one Spalart-Allmaras update of q(:,:,5) and turmu."""
     _call("ot2d_vmu_sa", _p(q), _p(s), _p(turmu), _p(x), _p(y), _p(xv), _p(yv), _p(xx), _p(xy), _p(yx), _p(yy),
