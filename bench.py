@@ -47,7 +47,10 @@ PHASES = ["time_step", "bc", "residual", "rbc", "lusgs", "sa", "update"]
 # DRAM bytes per interior cell per launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of the batch-8 capture, 0.52 M cells, summarised in
 # profiles/top_kernels_rans_sa_513x129_b8_fp32mixed.md), scaled to the batch
-TRAFFIC_PER_CELL = {"residual": (40.559104e6 + 0.576256e6) / (8 * 65536)}
+TRAFFIC_PER_CELL = {"residual": (40.552192e6 + 0.333312e6) / (8 * 65536),
+                    # k_lu_prep + both sweeps (k_lu_edges, ~1 % of the phase, not captured)
+                    "lusgs": (31.611648e6 + 9.395712e6 + 62.382336e6 + 2.520320e6 + 62.393856e6 + 1.144576e6)
+                    / (8 * 65536)}
 NPH = len(PHASES)
 
 
