@@ -58,6 +58,27 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def rank_max(x, dist, device):
+    """The slowest rank's value of x (a time): every rank gets the maximum."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput of replicas with the same per-rank work (weak
+    scaling): all ranks' units over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
+def rank_seed(rank):
+    """Each rank serves its own requests: seeds 1000 apart."""
+    return 1000 * rank
+
+
 def batch_cases(n, seed=0, jmax=JMAX, kmax=KMAX):
     from turns2d_urans_git_gb300 import api
     rng = np.random.default_rng(seed)
@@ -297,7 +318,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    cases = batch_cases(args.batch, seed=1000 * rank)
+    cases = batch_cases(args.batch, seed=rank_seed(rank))
     cells = (JMAX - 1) * (KMAX - 1)
     B = len(cases)
 
@@ -317,12 +338,7 @@ def run_ours(args):
         e1.record(stream)
         e1.synchronize()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return rank_max(e0.elapsed_time(e1), dist, "cuda")
 
     # ---- FP32-mixed batched, device resident (value)
     sv, ids = make(OT2D_FP32_MIXED)
@@ -333,7 +349,7 @@ def run_ours(args):
     clk.start()
     ms = timed(sv, args.steps)
     clocks = clk.stop()
-    value = world * B * cells * args.steps / (ms / 1e3)
+    value = whole_job_rate(B * cells * args.steps, world, ms / 1e3)
     # phase timers of the same batch -> dominant kernel + roofline
     prof = (C.c_double * NPH)()
     api.lib().ot2d_solver_profile.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int32]
@@ -369,13 +385,9 @@ def run_ours(args):
     t0 = time.perf_counter()
     rc2 = L.ot2d_solver_iterate_host(sv._h, B, idarr, ptrs, e2e_steps)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = rank_max(time.perf_counter() - t0, dist, "cuda")
     qbytes = sum(q.nbytes for q in qh)
-    e2e = world * B * cells * e2e_steps / e2e_s if rc2 == 0 else None
+    e2e = whole_job_rate(B * cells * e2e_steps, world, e2e_s) if rc2 == 0 else None
     sv.close()
     # ---- plain FP64 on the same batch (reported beside the headline)
     fp64 = None
@@ -385,7 +397,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         k64 = max(2, args.fp64_steps)
         ms64 = timed(sv64, k64)
-        fp64 = world * B * cells * k64 / (ms64 / 1e3)
+        fp64 = whole_job_rate(B * cells * k64, world, ms64 / 1e3)
         sv64.close()
     # ---- served request stream (rank 0 only): converged solves/s, p50/p99
     serve = None

@@ -1,0 +1,56 @@
+"""The multi-GPU path of bench.py is replicas only (no collective on the data
+path): each rank serves its own seeded requests and the whole-job figures
+are all ranks' work over the slowest rank's time.  These tests run that
+aggregation with world_size 2 on the CPU (gloo, 127.0.0.1).  No GPU."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, out):
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+    import bench
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        t_rank = [0.25, 0.75][rank]                  # this rank's time (s)
+        t = bench.rank_max(t_rank, dist, "cpu")
+        rate = bench.whole_job_rate(1000, world, t)
+        cases = bench.batch_cases(2, seed=bench.rank_seed(rank))
+        alfas = [float(c[1].alfa) for c in cases]
+        out.put((rank, t, rate, alfas))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replica_aggregation_gloo_world2():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=300) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (r0, t0, rate0, a0), (r1, t1, rate1, a1) = res
+    assert t0 == t1 == 0.75                 # both ranks see the slowest rank's time
+    assert rate0 == rate1 == 2 * 1000 / 0.75   # all ranks' units over that time
+    assert a0[1] != a1[1]                   # each rank serves its own seeded requests
