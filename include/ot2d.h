@@ -146,7 +146,9 @@ int ot2d_timespectralrhs(double* q, double* s, double* Ds, int32_t* jd, int32_t*
 /* src/step.f:2-7 (full arrays over nspec; norms of the last call via
  * ot2d_last_norms).  Time accurate (iunst = 1): xold..yole give the
  * swept-area face speeds and ug, vg the cell grid speeds; itnmax > 1: qnewt
- * gives newton's physical-time term (time.f:178-210).  iprecon:
+ * gives newton's physical-time term (time.f:178-210), or with the time-spectral
+ * form newtonTS's pseudo-time term (time.f:213-241, added after the norms).
+ * iprecon:
  * roetrklflx fluxes, rhslom after the norms and preilu2d or arc2d_precon,
  * all reading bt, which must then be given. */
 int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, double* x, double* y, double* xv,

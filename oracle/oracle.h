@@ -45,6 +45,7 @@ void pitch(const P& p, A2 x, A2 y, double* xv, double* yv, double* xold, double*
 void stqol(const P& p, const double* q, double* qtn, double* qtnm1, double* qnewt);
 /* time.f:178-210 for one instance: s -= (q - qnewt)/(oat*h) on the interior */
 void newton(const P& p, A3 q, const double* qnewt, A3 s);
+void newtonTS(const P& p, A3 q, const double* qnewt, A3 ss, A2 tscale);
 /* visrhs.f:2-287 */
 void visrhs(const P& p, A2 turmu, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy);
 /* time.f:2-108 (one time instance) */

@@ -80,4 +80,14 @@ void newton(const P& p, A3 q, const double* qnewt, A3 s) {
       for (int n = 1; n <= p.nv; ++n) s(j, k, n) = s(j, k, n) - (q(j, k, n) - qn(j, k, n)) * tac;
 }
 
+/* time.f:213-241 (newtonTS): the pseudo-time Newton term of a time-spectral
+ * run into ss (added to s after the norms) */
+void newtonTS(const P& p, A3 q, const double* qnewt, A3 ss, A2 tscale) {
+  A3 qn{const_cast<double*>(qnewt), q.jd, q.ns};
+  for (int k = p.kbeg; k <= p.kend; ++k)
+    for (int j = p.jbeg; j <= p.jend; ++j)
+      if (tscale(j, k) != 0)
+        for (int n = 1; n <= p.nv; ++n) ss(j, k, n) = ss(j, k, n) - (q(j, k, n) - qn(j, k, n)) / tscale(j, k);
+}
+
 }  // namespace oro

@@ -271,10 +271,12 @@ int oro_step_u(const P* pp, double* q, double* s, double* x, double* y, const do
     const size_t ov = (size_t)(nsp - 1) * nvert;
     rhsup(p, qn, sn, xv + ov, yv + ov, I2{iblank + o, jd}, ugv + ov, vgv + ov, xold ? xold + ov : nullptr,
           yold ? yold + ov : nullptr, xole ? xole + ov : nullptr, yole ? yole + ov : nullptr);
-    // compute_residual, step.f:274-285 (time-spectral Newton terms are not restated)
-    if (p.itnmax > 1 && !p.timespectral) {
+    // compute_residual, step.f:274-285: newton into s, or (time spectral)
+    // newtonTS into ss, which is added to s after the norms (step.f:125-131)
+    if (p.itnmax > 1) {
       if (!qnewt) { std::fprintf(stderr, "oracle: itnmax>1 needs qnewt\n"); std::abort(); }
-      newton(p, qn, qnewt + o, sn);
+      if (p.timespectral) newtonTS(p, qn, qnewt + o, v3(pp, ss.data() + o), v2(pp, tscale + o));
+      else newton(p, qn, qnewt + o, sn);
     }
     if (!p.invisc) visrhs(p, v2(pp, turmu + o), qn, sn, v2(pp, xx + o), v2(pp, xy + o), v2(pp, yx + o), v2(pp, yy + o));
     if (p.timespectral) timespectralrhs(p, q, s, Ds, nsp);

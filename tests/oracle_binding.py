@@ -62,6 +62,8 @@ def lib():
         L.oro_monitor.restype = C.c_int
         L.oro_force2d.argtypes = [_P, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.oro_step.argtypes = [_P] + [_dp] * 6 + [_ip] + [_dp] * 12 + [_dp, _ip]
+        L.oro_step_u.argtypes = [_P] + [_dp] * 6 + [_ip] + [_dp] * 12 + [_dp, _ip] + [_dp] * 5
+        L.oro_step_u.restype = C.c_int
         L.oro_step.restype = C.c_int
         L.oro_solve.argtypes = [_P, _dp, _dp, C.c_int, C.c_double, _dp, _dp, _dp]
         L.oro_solve.restype = C.c_int

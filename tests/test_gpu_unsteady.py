@@ -138,3 +138,66 @@ def test_dropin_time_loop_matches_oracle(kind):
                     xole, yole, turmu, tscale, bt, Ds, 1, jd, kd)
             assert rt.monitor(q, jd, kd) == 0
     assert relerr(q, q_o) <= tol
+
+
+@pytest.mark.parametrize("visc", [False, True])
+def test_step_newton_time_spectral_matches_oracle(visc):
+    """step.f with the time-spectral form and Newton sub-iterations (itnmax
+    > 1): newtonTS (time.f:213-241) gathers -(q - qnewt)/tscale in ss, which
+    is added to s after the norms (step.f:125-131), beside the
+    timespectralrhs coupling of the three instances.  Two consecutive
+    drop-in steps against the oracle's step."""
+    import ctypes as C
+    from tests.helpers import Case
+    from turns2d_urans_git_gb300 import routines as rt
+    ns = 3
+    c = Case(viscous=visc, seed=61, perturb=0.01)
+    p = type(c.p).from_buffer_copy(c.p)
+    p.timespectral, p.nspec, p.itnmax, p.rotf = 1, ns, 2, 0.1
+    n2 = c.n2
+    rng = np.random.default_rng(62)
+    rep = lambda a: np.ascontiguousarray(np.tile(a, ns))
+    x, y, xx, xy, yx, yy, ug, vg = (rep(a) for a in (c.x, c.y, c.xx, c.xy, c.yx, c.yy, c.ug, c.vg))
+    xv, yv, ugv, vgv = (rep(a) for a in (c.xv, c.yv, c.ugv, c.vgv))
+    iblank = rep(c.iblank)
+    qc = c.q.reshape(p.nq, n2)
+    q = np.concatenate([np.concatenate([qc[n] * (1.0 + 0.003 * i * rng.uniform(-1, 1, n2)) if n < p.nq - 1 else qc[n]
+                                        for i in range(ns)]) for n in range(p.nq)])
+    qnewt = q[:n2 * ns * p.nv] * (1.0 + 1e-3 * rng.uniform(-1, 1, n2 * ns * p.nv))
+    Ds = np.zeros(ns * ns)
+    ob.lib().oro_computeTScoefs(ns, ob.ptr(Ds))
+    arrs = {}
+    for who in ("oracle", "gpu"):
+        arrs[who] = dict(q=q.copy(), s=np.zeros(n2 * ns * p.nv), turmu=rep(c.turmu), tscale=np.zeros(n2 * ns),
+                         bt=np.zeros(n2 * ns))
+    L, pp = ob.lib(), C.byref(p)
+    for it in range(1, 3):
+        p.istep0 = p.istep = 1
+        p.itn = it
+        rt.set_params(p)
+        for who, a in arrs.items():
+            for nsp in range(ns):
+                sl = slice(nsp * n2, (nsp + 1) * n2)
+                qv = a["q"].reshape(p.nq, ns * n2)[:, sl].ravel()   # time_step of one instance
+                ts, bt = np.zeros(n2), np.zeros(n2)
+                p1 = type(p).from_buffer_copy(p)
+                p1.nspec = 1
+                L.oro_time_step(C.byref(p1), ob.ptr(np.ascontiguousarray(qv)), ob.ptr(c.xx), ob.ptr(c.xy),
+                                ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug), ob.ptr(c.vg), ob.ptr(ts), ob.ptr(bt),
+                                ob.ptr(c.iblank))
+                a["tscale"][sl], a["bt"][sl] = ts, bt
+            if who == "oracle":
+                norms, loc = np.zeros(3 * ns), np.zeros(3 * ns, dtype=np.int32)
+                st = L.oro_step_u(pp, ob.ptr(a["q"]), ob.ptr(a["s"]), ob.ptr(x), ob.ptr(y), ob.ptr(xv), ob.ptr(yv),
+                                  ob.ptr(iblank), ob.ptr(xx), ob.ptr(xy), ob.ptr(yx), ob.ptr(yy), ob.ptr(ug),
+                                  ob.ptr(vg), ob.ptr(ugv), ob.ptr(vgv), ob.ptr(a["turmu"]), ob.ptr(a["tscale"]),
+                                  ob.ptr(a["bt"]), ob.ptr(Ds), ob.ptr(norms), ob.ptr(loc), ob.ptr(qnewt), None, None,
+                                  None, None)
+                assert st == 0
+            else:
+                rt.step(a["q"], None, None, qnewt, a["s"], x, y, xv, yv, iblank, xx, xy, yx, yy, ug, vg, ugv, vgv,
+                        None, None, None, None, a["turmu"], a["tscale"], a["bt"], Ds, 1, p.jd, p.kd)
+        assert relerr(arrs["gpu"]["q"], arrs["oracle"]["q"]) <= 1e-12
+    # the Newton term changed the trajectory
+    p0 = type(p).from_buffer_copy(p)
+    assert not np.array_equal(arrs["gpu"]["q"], q)

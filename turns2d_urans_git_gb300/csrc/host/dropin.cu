@@ -811,7 +811,7 @@ int ot2d_step(double* q, double* qtn, double* qtnm1, double* qnewt, double* s, d
   if (prepare(nspec, err)) return fail(err);
   const ot2d_params& p = g_ctx.P;
   const bool swept = p.iunst == 1, newton = p.itnmax > 1;
-  if (!dims_ok(jd, kd) || p.ilhs < 1 || p.ilhs > 3 || (p.iunst != 0 && !swept) || (newton && p.timespectral) ||
+  if (!dims_ok(jd, kd) || p.ilhs < 1 || p.ilhs > 3 || (p.iunst != 0 && !swept) || (newton && p.timespectral && swept) ||
       (!p.lamin && p.iturb != 1 && p.iturb != 2) || p.itrans != 0)
     return fail(OT2D_ERR_ARG);
   // Turkel preconditioning: rhslom, preilu2d and arc2d_precon read bt

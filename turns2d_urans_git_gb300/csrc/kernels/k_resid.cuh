@@ -356,7 +356,7 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
 #pragma unroll
       for (int v = 0; v < 4; ++v) s[v] = s[v] - (G[v * ((RT_TK + 1) * RT_TJ) + RT_TJ] - G[v * ((RT_TK + 1) * RT_TJ)]);
     }
-    if (S.qnewt) {
+    if (S.qnewt && !p.timespectral) {
       // newton (time.f:195-206): the physical-time term, added between the
       // inviscid and the viscous parts as compute_residual does
       // (step.f:274-285); 1/(oat*h) of this step in red[8]
@@ -437,6 +437,21 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
     }
     if constexpr (PRE) {
       if (flags & AS_NORM) rhslom_cell(S, p, o, s);
+    }
+    if (S.qnewt && p.timespectral && (flags & AS_NORM)) {
+      // newtonTS (time.f:213-241): the pseudo-time Newton term of a
+      // time-spectral run, gathered in ss and added after the norms and
+      // rhslom (step.f:125-131)
+      const R ts = S.tscale[o];
+      if (ts != (R)0) {
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          if (n >= nv) continue;
+          const int64_t on = (int64_t)n * S.qs + o;
+          const double ssv = 0.0 - (S.q64[on] - S.qnewt[on]) / (double)ts;
+          s[n] = s[n] + (R)ssv;
+        }
+      }
     }
 #pragma unroll
     for (int n = 0; n < 8; ++n)
