@@ -360,6 +360,23 @@ __global__ void __launch_bounds__(CELL_BS) k_lu_edges(const Slice<R>* __restrict
   lu_edge_cell<R, PRE>(S, *S.P, j, k, scale);
 }
 
+// The same over the halo ring only (one halo layer): the f32 path has no
+// q round trip, so only the ring cells have work.  grid: (ring parts, slices)
+template <class R, bool PRE>
+__global__ void __launch_bounds__(128) k_lu_edges_ring(const Slice<R>* __restrict__ sl, int scale, int only_lu) {
+  const Slice<R>& S = sl[blockIdx.y];
+  if ((only_lu && S.P->ilhs != 1) || (S.k_mp2 >= (R)0) != PRE) return;
+  const int jd = S.jd, kd = S.kd, nring = 2 * jd + 2 * (kd - 2);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nring) return;
+  int j, k;
+  if (i < jd) { j = i + 1; k = 1; }
+  else if (i < 2 * jd) { j = i - jd + 1; k = kd; }
+  else if (i < 2 * jd + kd - 2) { j = 1; k = i - 2 * jd + 2; }
+  else { j = jd; k = i - (2 * jd + kd - 2) + 2; }
+  lu_edge_cell<R, PRE>(S, *S.P, j, k, scale);
+}
+
 template <class R, bool FWD, int G, bool PRE>
 __global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int only_lu) {
   extern __shared__ __align__(128) unsigned char lu_smem[];

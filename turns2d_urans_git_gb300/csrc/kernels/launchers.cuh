@@ -98,7 +98,13 @@ cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale,
     prep_attr = true;
   }
   k_lu_prep<R, PRE><<<b.lu_blocks, CELL_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
-  k_lu_edges<R, PRE><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
+  if constexpr (sizeof(R) == sizeof(double)) {
+    // every cell: the FP64 path also round-trips q (lhs.f:524-531, :805-811)
+    k_lu_edges<R, PRE><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
+  } else {
+    const int nring = 2 * b.max_wall + 2 * b.max_kd;   // >= the ring of every slice
+    k_lu_edges_ring<R, PRE><<<dim3((nring + 127) / 128, b.nslice), 128, 0, st>>>(d_sl, scale, only_lu);
+  }
   return cudaGetLastError();
 }
 template <class R>
