@@ -16,7 +16,7 @@ constexpr int BC_BS = 512;
 // threads of a CTA of one BC entry (several CTAs per slice)
 constexpr int BCE_BS = 128;
 // residual tile: RT_TJ x RT_TK interior cells per CTA
-constexpr int RT_TJ = 32, RT_TK = 8;
+constexpr int RT_TJ = 16, RT_TK = 16;
 // scratch arrays per slice of the k-omega SST solve (k_sst.cuh: SSTw)
 constexpr int SST_NSCRATCH = 27;
 // scratch arrays per slice of the ADI operator (k_adi.cuh: ADIw)
