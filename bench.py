@@ -41,7 +41,7 @@ JMAX, KMAX = 513, 129
 WORKLOAD = "RANS-SA NACA0012 C-mesh 513x129, M0.15 a10 Re6e6, MUSCL+Roe, LU-SGS CFL50"
 
 # algorithmic bytes per interior cell per launch of each kernel family of
-# the FP32-mixed path (compulsory array traffic)
+# the FP32-mixed path (the compulsory array traffic of each kernel family)
 ALG_BYTES_F32 = {0: 44, 1: 0, 2: 80, 3: 0, 4: 188, 5: 200, 6: 96}
 PHASES = ["time_step", "bc", "residual", "rbc", "lusgs", "sa", "update"]
 # DRAM bytes per interior cell per launch measured by ncu (dram__bytes_read.sum +
@@ -100,8 +100,8 @@ class ClockSampler:
         self.dev, self.proc, self.path = dev, None, None
 
     def start(self):
-        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        import tempfile
+        self.path = os.path.join(tempfile.gettempdir(), "ot2d_clocks_%d.csv" % os.getpid())
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
