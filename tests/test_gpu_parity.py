@@ -3,7 +3,7 @@ CPU FP64 oracle, through the C-ABI (numpy host arrays staged by the
 library, registered host arrays, and CUDA device pointers).
 
 Tolerance: the plain FP64 path must agree with the oracle to 1e-12 relative
-(the benchmark spec's bound); most routines are bit-exact because the FP64 kernels
+(the bound the path is specified to); most routines are bit-exact because the FP64 kernels
 keep the reference's operation order without fused multiply-adds and IEEE
 division / square root are correctly rounded on both sides.  pow/exp in the
 SA source term may differ by an ulp.
