@@ -43,6 +43,9 @@ WORKLOAD = "RANS-SA NACA0012 C-mesh 513x129, M0.15 a10 Re6e6, MUSCL+Roe, LU-SGS 
 # algorithmic bytes per interior cell per launch of each kernel family of
 # the FP32-mixed path (the compulsory array traffic of each kernel family)
 ALG_BYTES_F32 = {0: 44, 1: 0, 2: 80, 3: 0, 4: 188, 5: 200, 6: 96}
+# the same arrays in the plain FP64 path: 8 bytes per element (iblank 4);
+# the update has no f32 shadow to write
+ALG_BYTES_F64 = {0: 88, 1: 0, 2: 156, 3: 0, 4: 376, 5: 400, 6: 108}
 PHASES = ["time_step", "bc", "residual", "rbc", "lusgs", "sa", "update"]
 # DRAM bytes per interior cell per launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of the batch-8 capture, 0.52 M cells, summarised in
@@ -79,14 +82,37 @@ def rank_seed(rank):
     return 1000 * rank
 
 
-def batch_cases(n, seed=0, jmax=JMAX, kmax=KMAX):
-    from turns2d_urans_git_gb300 import api
+def batch_alfas(n, seed=0):
+    """Angles of attack of the batch: 10 deg, then seeded U[0, 10]."""
     rng = np.random.default_rng(seed)
+    return [10.0 if i == 0 else float(rng.uniform(0.0, 10.0)) for i in range(n)]
+
+
+def batch_cases(n, seed=0, jmax=JMAX, kmax=KMAX):
+    """The batch for the GPU arm, built by the library's own set-up calls."""
+    from turns2d_urans_git_gb300 import api
+    return [api.config_c2(jmax=jmax, kmax=kmax, alfa=a) for a in batch_alfas(n, seed)]
+
+
+def oracle_batch(n, seed=0, jmax=JMAX, kmax=KMAX):
+    """The same batch for the CPU legs, built without the product library:
+    the oracle's read_inputs over namelist inputs and the numpy restatement
+    of the mesh generator (bitwise the same meshes).  Returns (params, xv, yv)."""
+    from tests import oracle_binding as ob
+    oc = ob.oracle_cases()
     out = []
-    for i in range(n):
-        alfa = 10.0 if i == 0 else float(rng.uniform(0.0, 10.0))
-        out.append(api.config_c2(jmax=jmax, kmax=kmax, alfa=alfa))
+    for a in batch_alfas(n, seed):
+        inp, xv, yv = oc.c2_inputs(jmax, kmax, alfa=a)
+        out.append((ob.read_inputs(inp), xv, yv))
     return out
+
+
+def bench_config(batch, world):
+    """The workload description, the same dict for both arms."""
+    return {"workload": WORKLOAD, "batch_per_gpu": batch, "interior_cells": (JMAX - 1) * (KMAX - 1),
+            "parallelism": "replicas x%d" % world,
+            "l2": "inputs larger than L2: %d requests x %d cells, ~25 MB of state each (L2 129 MB)"
+                  % (batch, (JMAX - 1) * (KMAX - 1))}
 
 
 class ClockSampler:
@@ -134,61 +160,76 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_reference(cases, max_threads=None, target_s=12.0):
-    """The reference algorithm (CPU FP64 oracle) on the host cores: one
-    request per thread, each a bounded number of iterations.  Returns
-    (cell-updates/s, threads, sample description)."""
+def cpu_reference(cases, target_s=12.0, max_threads=None):
+    """The reference algorithm on the host cores: the -O3 build of the CPU
+    FP64 oracle (a line-by-line restatement of the Fortran, which cannot be
+    compiled here: no Fortran compiler), every request of the batch run for
+    the same bounded number of iterations on a pool of one thread per core.
+    Returns (cell-updates/s, threads, sample description)."""
     from tests import oracle_binding as ob
-    ob.lib()
+    ob.lib_fast()
     ncores = os.cpu_count() or 1
-    nthr = min(max_threads or ncores, ncores, len(cases))
-    # size the sample from one short probe
-    _, prm, xv, yv = cases[0]
+    nthr = max(1, min(max_threads or ncores, ncores, len(cases)))
+    prm, xv, yv = cases[0]
     t0 = time.perf_counter()
-    ob.solve(prm, xv.ravel(), yv.ravel(), 2)
+    ob.solve(prm, xv.ravel(), yv.ravel(), 2, fast=True)
     per_it = (time.perf_counter() - t0) / 2
-    iters = max(2, int(target_s / max(per_it, 1e-6)))
-    cells = (prm.jmax - 1) * (prm.kmax - 1)
-    results = [None] * nthr
+    # wall ~ (requests / threads) x iterations x per-iteration time
+    iters = max(2, int(target_s * nthr / (len(cases) * max(per_it, 1e-6))))
+    done = [0] * len(cases)
+    nxt = [0]
+    lock = threading.Lock()
 
-    def work(i):
-        _, p, x, y = cases[i % len(cases)]
-        t = time.perf_counter()
-        n, _, _, _ = ob.solve(p, x.ravel(), y.ravel(), iters)
-        results[i] = (abs(n), time.perf_counter() - t)
+    def work():
+        while True:
+            with lock:
+                i = nxt[0]
+                nxt[0] += 1
+            if i >= len(cases):
+                return
+            p, x, y = cases[i]
+            n, _, _, _ = ob.solve(p, x.ravel(), y.ravel(), iters, fast=True)
+            done[i] = abs(n) * (p.jmax - 1) * (p.kmax - 1)
 
-    th = [threading.Thread(target=work, args=(i,)) for i in range(nthr)]
+    th = [threading.Thread(target=work) for _ in range(nthr)]
     t0 = time.perf_counter()
     for t in th:
         t.start()
     for t in th:
         t.join()
     wall = time.perf_counter() - t0
-    done = sum(r[0] for r in results)
-    value = done * cells / wall
-    sample = "%d requests x %d iterations of the 513x129 SA case on %d threads (%.1f s wall)" % (nthr, iters, nthr, wall)
+    value = sum(done) / wall
+    sample = ("all %d requests of the batch x %d iterations each (513x129 RANS-SA, FP64 oracle -O3) on %d threads, "
+              "%.1f s wall" % (len(cases), iters, nthr, wall))
     return value, nthr, sample
 
 
-def serve_stream(precision, reqs, arrivals, orders, max_iters, check_every, device, cap_s, force_tol):
-    """Continuous-batching service of a request stream: requests are
-    admitted at the first status check after their arrival time and retired
-    when converged (L2 norm `orders` decades below its running peak), failed
-    or capped.  Returns per-request (arrival, done, result) and the makespan
-    (s); stops admitting and gives up after cap_s seconds."""
+def serve_stream(precision, reqs, arrivals, max_iters, check_every, device, cap_s, budget_mb=0):
+    """Continuous-batching service of a request stream: each request is
+    submitted at the first status check after its arrival time (admitted at
+    once when it fits the memory budget, queued otherwise) and retired when
+    converged -- FP64: its L2 norm `orders` decades below its peak; FP32-mixed:
+    the mixed rule (api.MIXED_RULE) -- failed or capped.  Stops submitting and
+    gives up after cap_s seconds.  Returns per-request (index, arrival,
+    result), the makespan (s) and the most requests ever queued."""
     from turns2d_urans_git_gb300 import api
+    from turns2d_urans_git_gb300.abi import OT2D_FP32_MIXED, OT2D_OPT_BUDGET_MB
     sv = api.Solver(precision, device=device, check_every=check_every)
-    if force_tol:
-        sv.set_force_tol(*force_tol)
+    if precision == OT2D_FP32_MIXED:
+        sv.set_mixed_rule()
+    if budget_mb:
+        sv.set_option(OT2D_OPT_BUDGET_MB, budget_mb)
     t0 = time.perf_counter()
     pending = sorted(zip(arrivals, range(len(reqs))))
-    admitted = {}
+    submitted = {}
+    max_queued = 0
     while True:
         now = time.perf_counter() - t0
-        while pending and pending[0][0] <= now:
+        while pending and pending[0][0] <= now and now <= cap_s:
             ta, i = pending.pop(0)
-            _, prm, xv, yv = reqs[i]
-            admitted[sv.add(prm, xv, yv, orders=orders, max_iters=max_iters)] = (i, ta, now)
+            (_, prm, xv, yv), orders = reqs[i]
+            submitted[sv.add(prm, xv, yv, orders=orders, max_iters=max_iters)] = (i, ta)
+        max_queued = max(max_queued, sv.queued())
         if sv.live() == 0:
             if not pending or now > cap_s:
                 break
@@ -197,17 +238,11 @@ def serve_stream(precision, reqs, arrivals, orders, max_iters, check_every, devi
         if now > cap_s:
             break
         sv.iterate(check_every)
-        sv.sync()
     sv.sync()
     t_end = time.perf_counter() - t0
-    out = []
-    for iid, (i, ta, tadm) in admitted.items():
-        r = sv.result(iid)
-        out.append((i, ta, r))
-    # the solver clock starts at creation, the same origin as t0 up to the
-    # constructor's duration (t_done in its own seconds)
+    out = [(i, ta, sv.result(iid)) for iid, (i, ta) in submitted.items()]
     sv.close()
-    return out, t_end
+    return out, t_end, max_queued
 
 
 def time_accurate_section(device, batch=64, nsteps=12, itnmax=4):
@@ -241,70 +276,150 @@ def time_accurate_section(device, batch=64, nsteps=12, itnmax=4):
             "cell_updates_per_s": batch * cells * its / (ms / 1e3)}
 
 
-def serving_section(args, device):
-    """FP32-mixed vs FP64 on the same seeded request stream: converged
-    solves/s and p50/p99 time to a converged solution."""
+def serve_requests(n, seed=7):
+    """The config-5 stream: 80 % steady RANS-SA requests drawn as the batched
+    configuration (NACA m, p, t; all five mesh sizes; M, alpha, Re), 20 %
+    time-spectral pitching NACA 0012 257x65 requests (N_ts in {3, 5, 7},
+    alpha0 in U[0, 10], k in U[0.05, 0.15], M 0.3); each with its own
+    tolerance, an L2 drop of 8, 9 or 10 decades."""
     from turns2d_urans_git_gb300 import api
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        case = api.config_c5_ts(rng) if rng.random() < 0.2 else api.config_c4_sample(rng)
+        out.append((case, float(rng.integers(8, 11))))
+    return out
+
+
+def serving_section(args, device):
+    """FP32-mixed vs FP64 on the same seeded Poisson request stream:
+    converged solves/s, p50/p99 time from submission to a converged
+    solution, and the force differences of the requests both converged."""
     from turns2d_urans_git_gb300.abi import OT2D_FP32_MIXED, OT2D_FP64
-    rng = np.random.default_rng(7)
-    sizes = ((129, 33), (257, 65))
-    reqs = [api.config_c4_sample(rng, sizes=sizes) for _ in range(args.serve_requests)]
+    reqs = serve_requests(args.serve_requests)
+    rng = np.random.default_rng(8)
     gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
     arrivals = np.cumsum(gaps) - gaps[0]
-    res = {}
+    res, forces = {}, {}
     for name, prec in (("fp32_mixed", OT2D_FP32_MIXED), ("fp64", OT2D_FP64)):
-        out, t_end = serve_stream(prec, reqs, arrivals, args.serve_orders, args.serve_max_iters, 25, device,
-                                  args.serve_seconds, (args.serve_dcl, args.serve_dcd))
-        lat = [r.t_done - ta for (i, ta, r) in out if r.converged]
-        conv = len(lat)
-        res[name] = {"requests": len(reqs), "admitted": len(out), "converged": conv,
-                     "solves_per_s": conv / t_end if t_end > 0 else None,
+        out, t_end, maxq = serve_stream(prec, reqs, arrivals, args.serve_max_iters, 25, device, args.serve_seconds,
+                                        args.serve_budget_mb)
+        conv = [(i, r) for (i, ta, r) in out if r.converged and r.status == 0]
+        lat = [r.t_done - r.t_submit for (i, r) in conv]
+        ts = sum(1 for (i, r) in conv if reqs[i][0][1].nspec > 1)
+        res[name] = {"requests": len(reqs), "submitted": len(out), "converged": len(conv),
+                     "converged_time_spectral": ts,
+                     "failed": sum(1 for (i, ta, r) in out if r.status != 0),
+                     "capped_or_unfinished": sum(1 for (i, ta, r) in out if r.status == 0 and not r.converged),
+                     "max_queued": maxq,
+                     "solves_per_s": len(conv) / t_end if t_end > 0 else None,
                      "p50_s": float(np.percentile(lat, 50)) if lat else None,
                      "p99_s": float(np.percentile(lat, 99)) if lat else None,
-                     "makespan_s": t_end,
-                     "forces": {i: (r.cl, r.cd, r.cm) for (i, ta, r) in out if r.converged}}
-    a, b = res["fp32_mixed"].pop("forces"), res["fp64"].pop("forces")
+                     "makespan_s": t_end}
+        forces[name] = {i: (r.cl, r.cd, r.cm) for (i, r) in conv}
+    a, b = forces["fp32_mixed"], forces["fp64"]
     both = sorted(set(a) & set(b))
-    dcls = sorted(abs(a[i][0] - b[i][0]) for i in both)
-    dcl = dcls[-1] if dcls else None
-    dcd = max((abs(a[i][1] - b[i][1]) for i in both), default=None)
+    d = np.array([[abs(a[i][k] - b[i][k]) for k in range(3)] for i in both]) if both else np.zeros((0, 3))
     sm, sd = res["fp32_mixed"]["solves_per_s"], res["fp64"]["solves_per_s"]
-    return {"workload": "%d seeded RANS-SA requests (NACA 4-digit m,p,t; M 0.3-0.85; a -2..8 deg; Re 1e6-1e7; "
-                        "meshes %s), Poisson arrivals %.1f/s; converged = L2 norm %.0f decades below its peak, or "
-                        "CL/CD within a band of %.0e/%.0e over 8 checks of 25 iterations with the norm a decade "
-                        "below its peak"
-                        % (len(reqs), "/".join("%dx%d" % s_ for s_ in sizes), args.serve_rate, args.serve_orders,
-                           args.serve_dcl, args.serve_dcd),
+    return {"workload": "%d seeded requests, Poisson arrivals %.2f/s: 80%% steady RANS-SA (NACA m,p,t; meshes "
+                        "129x33..769x193; M 0.3-0.85; a -2..8 deg; Re 1e6-1e7), 20%% time-spectral pitching NACA0012 "
+                        "257x65 (N_ts 3/5/7, M 0.3); per-request tolerance 8-10 decades; %d-iteration cap per "
+                        "request, %.0f s cap per precision"
+                        % (len(reqs), args.serve_rate, args.serve_max_iters, args.serve_seconds),
+            "convergence": {"fp64": "L2 norm (step.f:86-93) `orders` decades below its peak",
+                            "fp32_mixed": "f32 floor rule: norm 2 decades below its peak and CL, CD within 2e-6, "
+                                          "4e-7 over 8 samples 200 iterations apart"},
             "fp32_mixed": res["fp32_mixed"], "fp64": res["fp64"],
             "speedup_solves_per_s": (sm / sd) if sm and sd else None,
-            "max_abs_dcl_vs_fp64": dcl, "max_abs_dcd_vs_fp64": dcd, "compared": len(both),
-            "p50_abs_dcl_vs_fp64": float(np.percentile(dcls, 50)) if dcls else None,
-            "n_abs_dcl_over_1e-3": sum(1 for v in dcls if v > 1e-3)}
+            "compared": len(both),
+            "max_abs_dcl_vs_fp64": float(d[:, 0].max()) if both else None,
+            "max_abs_dcd_vs_fp64": float(d[:, 1].max()) if both else None,
+            "max_abs_dcm_vs_fp64": float(d[:, 2].max()) if both else None}
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the reference's algorithm restated in
+    C++; the Fortran itself cannot be built here) on the host cores over the
+    same 64-request batch as the GPU arm, built without the product library.
+    Rank 0 alone runs it; other ranks exit without work."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    cases = batch_cases(max(args.batch, os.cpu_count() or 1))
     t0 = time.perf_counter()
-    vals = []
-    for _ in range(args.warmup):
-        pass  # the oracle has no warm state
+    cases = oracle_batch(args.batch)
     per_step = max(1.0, min(args.ref_seconds, 150.0 / max(args.steps, 1)))
+    # warm-up: page in the library and the meshes (one short request)
+    from tests import oracle_binding as ob
+    for _ in range(min(args.warmup, 1)):
+        prm, xv, yv = cases[0]
+        ob.solve(prm, xv.ravel(), yv.ravel(), 1, fast=True)
+    vals = []
     for _ in range(args.steps):
         v, thr, sample = cpu_reference(cases, target_s=per_step)
         vals.append(v)
     value = float(np.median(vals))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded algebraic C-meshes)",
-            "config": {"workload": WORKLOAD, "batch": len(cases), "per_step": "bounded sample, see cpu_baseline"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": "port", "sample": sample},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded algebraic NACA0012 C-meshes, freestream start)",
+            "config": bench_config(len(cases), world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": "port",
+                             "sample": sample + "; median of %d such samples" % args.steps},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": time.perf_counter() - t0}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def e2e_rate(sv, ids, cases, steps, world, dist):
+    """Cell-updates/s through the host-buffer C-ABI path
+    (ot2d_solver_iterate_host): every step uploads every request's
+    q(jd,kd,nspec,nq) from pinned host memory, runs the iteration and reads q
+    back.  Returns (rate, bytes each way per step)."""
+    import torch
+    from turns2d_urans_git_gb300 import api
+    B = len(ids)
+    qh = [np.zeros(prm.jd * prm.kd * prm.nspec * prm.nq) for (_, prm, _, _) in cases]
+    for iid, (_, prm, _, _), q in zip(ids, cases, qh):
+        q[:] = sv.get_q(iid, prm)
+    pinned = [torch.from_numpy(q).pin_memory() for q in qh]
+    ptrs = (C.POINTER(C.c_double) * B)(*[C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)) for t in pinned])
+    idarr = (C.c_int32 * B)(*ids)
+    L = api.lib()
+    L.ot2d_solver_iterate_host.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
+                                           C.POINTER(C.POINTER(C.c_double)), C.c_int32]
+    L.ot2d_solver_iterate_host(sv._h, B, idarr, ptrs, 1)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = L.ot2d_solver_iterate_host(sv._h, B, idarr, ptrs, steps)
+    torch.cuda.synchronize()
+    secs = rank_max(time.perf_counter() - t0, dist, "cuda")
+    cells = sum((prm.jmax - 1) * (prm.kmax - 1) for (_, prm, _, _) in cases)
+    return (whole_job_rate(cells * steps, world, secs) if rc == 0 else None), sum(q.nbytes for q in qh)
+
+
+def phase_roofline(sv, alg_bytes, cells, peaks, traffic=None):
+    """Per-phase CUDA-event timers of the batch (ot2d_solver_profile) and the
+    HBM roofline of the dominant phase: algorithmic bytes of its arrays over
+    its measured time, against the measured copy bandwidth."""
+    from turns2d_urans_git_gb300 import api
+    prof = (C.c_double * NPH)()
+    api.lib().ot2d_solver_profile.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int32]
+    rc = api.lib().ot2d_solver_profile(sv._h, 5, prof, NPH)
+    if rc != 0:
+        return {}, None
+    phase_ms = {PHASES[i]: prof[i] for i in range(NPH)}
+    dom = max(range(NPH), key=lambda i: prof[i])
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg_bytes[dom] * cells / (prof[dom] * 1e-3) / 1e9 if prof[dom] > 0 else None
+    roof = {"bound": "hbm", "kernel": PHASES[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None,
+            "alg_bytes_per_cell": alg_bytes[dom],
+            "traffic": (traffic[PHASES[dom]] * cells if traffic and PHASES[dom] in traffic else None),
+            "traffic_note": "bytes per launch, ncu batch-8 capture scaled by cells",
+            "peak_source": "measured" if peaks else "fallback"}
+    return phase_ms, roof
 
 
 def run_ours(args):
@@ -321,6 +436,11 @@ def run_ours(args):
     cases = batch_cases(args.batch, seed=rank_seed(rank))
     cells = (JMAX - 1) * (KMAX - 1)
     B = len(cases)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
 
     def make(precision):
         sv = api.Solver(precision, device=local, check_every=10 ** 8)
@@ -342,7 +462,6 @@ def run_ours(args):
 
     # ---- FP32-mixed batched, device resident (value)
     sv, ids = make(OT2D_FP32_MIXED)
-    resident = sv.device_bytes()
     sv.iterate(args.warmup)
     torch.cuda.synchronize()
     clk = ClockSampler(local)
@@ -350,64 +469,32 @@ def run_ours(args):
     ms = timed(sv, args.steps)
     clocks = clk.stop()
     value = whole_job_rate(B * cells * args.steps, world, ms / 1e3)
-    # phase timers of the same batch -> dominant kernel + roofline
-    prof = (C.c_double * NPH)()
-    api.lib().ot2d_solver_profile.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int32]
-    rc = api.lib().ot2d_solver_profile(sv._h, 5, prof, NPH)
-    phase_ms = {PHASES[i]: prof[i] for i in range(NPH)} if rc == 0 else {}
-    dom = max(range(NPH), key=lambda i: prof[i]) if rc == 0 else 4
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    alg = ALG_BYTES_F32[dom] * B * cells
-    achieved = alg / (prof[dom] * 1e-3) / 1e9 if rc == 0 and prof[dom] > 0 else None
-    # ---- e2e through the host-buffer ABI path
-    qh = [np.zeros(prm.jd * prm.kd * prm.nspec * prm.nq) for (_, prm, _, _) in cases]
-    for iid, (_, prm, _, _), q in zip(ids, cases, qh):
-        q[:] = sv.get_q(iid, prm)
-    pinned = []
-    for q in qh:
-        t = torch.from_numpy(q).pin_memory()
-        pinned.append(t)
-    ptrs = (C.POINTER(C.c_double) * B)(*[C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)) for t in pinned])
-    idarr = (C.c_int32 * B)(*ids)
-    L = api.lib()
-    L.ot2d_solver_iterate_host.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
-                                           C.POINTER(C.POINTER(C.c_double)), C.c_int32]
-    e2e_steps = max(3, args.steps // 2)
-    L.ot2d_solver_iterate_host(sv._h, B, idarr, ptrs, 1)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rc2 = L.ot2d_solver_iterate_host(sv._h, B, idarr, ptrs, e2e_steps)
-    torch.cuda.synchronize()
-    e2e_s = rank_max(time.perf_counter() - t0, dist, "cuda")
-    qbytes = sum(q.nbytes for q in qh)
-    e2e = whole_job_rate(B * cells * e2e_steps, world, e2e_s) if rc2 == 0 else None
+    phase_ms, roof = phase_roofline(sv, ALG_BYTES_F32, B * cells, peaks, TRAFFIC_PER_CELL)
+    e2e, qbytes = e2e_rate(sv, ids, cases, max(3, args.steps // 2), world, dist)
     sv.close()
-    # ---- plain FP64 on the same batch (reported beside the headline)
+    # ---- plain FP64 on the same batch, with its own e2e and roofline
     fp64 = None
     if not args.skip_fp64:
-        sv64, _ = make(OT2D_FP64)
+        sv64, ids64 = make(OT2D_FP64)
         sv64.iterate(1)
         torch.cuda.synchronize()
         k64 = max(2, args.fp64_steps)
         ms64 = timed(sv64, k64)
-        fp64 = whole_job_rate(B * cells * k64, world, ms64 / 1e3)
+        ph64, roof64 = phase_roofline(sv64, ALG_BYTES_F64, B * cells, peaks)
+        e64, qb64 = e2e_rate(sv64, ids64, cases, 2, world, dist)
+        fp64 = {"value": whole_job_rate(B * cells * k64, world, ms64 / 1e3), "unit": UNIT, "steps": k64,
+                "ms_per_step": ms64 / k64, "phase_ms": ph64, "roofline": roof64,
+                "e2e": {"value": e64, "unit": UNIT, "h2d_bytes_per_step": qb64, "d2h_bytes_per_step": qb64}}
         sv64.close()
     # ---- served request stream (rank 0 only): converged solves/s, p50/p99
     serve = None
     if rank == 0 and not args.skip_serve:
         serve = serving_section(args, local)
-    unsteady = time_accurate_section(local) if rank == 0 else None
+    unsteady = time_accurate_section(local) if rank == 0 and not args.skip_serve else None
     # ---- CPU baseline (rank 0, N=1 only): the oracle on the host cores
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        v, thr, sample = cpu_reference(batch_cases(os.cpu_count() or 1), target_s=args.ref_seconds)
+        v, thr, sample = cpu_reference(oracle_batch(args.batch), target_s=args.ref_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port", "sample": sample}
     if rank == 0:
         # kernels per iteration: iter_begin, time_step, 5 BC entries + the
@@ -417,19 +504,13 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32 (f64 state update, norms, forces)",
                 "data": "synthetic (seeded algebraic NACA0012 C-meshes, freestream start)",
-                "config": {"workload": WORKLOAD, "batch_per_gpu": B, "interior_cells": cells,
-                           "parallelism": "replicas x%d" % world, "precision": "fp32-mixed",
-                           "l2": "inputs larger than L2: %.0f MB resident per GPU (L2 129 MB)" % (resident / 1e6)},
+                "config": bench_config(B, world),
+                "precision": "fp32-mixed",
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes},
-                "fp64_plain": {"value": fp64, "unit": UNIT},
+                "fp64_plain": fp64,
                 "gpu_launches": launches_per_step * args.steps,
                 "phase_ms": phase_ms,
-                "roofline": {"bound": "hbm", "kernel": PHASES[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": (achieved / peak) if achieved else None,
-                             "traffic": (TRAFFIC_PER_CELL[PHASES[dom]] * B * cells
-                                         if PHASES[dom] in TRAFFIC_PER_CELL else None),
-                             "traffic_note": "bytes per launch, ncu batch-8 capture scaled by cells",
-                             "peak_source": "measured" if peaks else "fallback"},
+                "roofline": roof,
                 "clocks": clocks}
         if cpu:
             line["cpu_baseline"] = cpu
@@ -443,6 +524,45 @@ def run_ours(args):
     return 0
 
 
+def run_replica_check(args):
+    """The replica launch and aggregation without a GPU (gloo): each rank
+    times one oracle iteration of the first request of its own seeded batch;
+    rank 0 prints the whole-job line (all ranks' cell-updates over the
+    slowest rank's time) and every rank's angles of attack."""
+    import torch.distributed as dist
+    rank, world, _ = env_rank()
+    dist.init_process_group("gloo")
+    from tests import oracle_binding as ob
+    cases = oracle_batch(args.batch, seed=rank_seed(rank), jmax=65, kmax=25)
+    prm, xv, yv = cases[0]
+    dist.barrier()
+    t0 = time.perf_counter()
+    ob.solve(prm, xv.ravel(), yv.ravel(), 1, fast=True)
+    secs = rank_max(time.perf_counter() - t0, dist, "cpu")
+    units = (prm.jmax - 1) * (prm.kmax - 1)
+    alfas = [None] * world
+    dist.all_gather_object(alfas, [float(p.alfa) for (p, _, _) in cases])
+    if rank == 0:
+        print(json.dumps({"n_gpus": world, "seconds": secs, "value": whole_job_rate(units, world, secs),
+                          "units_per_rank": units, "alfas": alfas}), flush=True)
+    dist.destroy_process_group()
+    return 0
+
+
+def spawn_replicas(n, argv):
+    """`bench.py --gpus N` outside torchrun: relaunch this script as N
+    replica processes, one per GPU, with the launcher the multi-GPU runs use
+    (torch.distributed.run, rendezvous on 127.0.0.1)."""
+    import socket
+    sk = socket.socket()
+    sk.bind(("127.0.0.1", 0))
+    port = sk.getsockname()[1]
+    sk.close()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + argv
+    return subprocess.call(cmd)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -454,17 +574,21 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
-    ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--serve-rate", type=float, default=8.0)
-    ap.add_argument("--serve-orders", type=float, default=10.0)
-    ap.add_argument("--serve-dcl", type=float, default=1e-5)
-    ap.add_argument("--serve-dcd", type=float, default=1e-6)
-    ap.add_argument("--serve-max-iters", type=int, default=20000)
-    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-requests", type=int, default=64)
+    ap.add_argument("--serve-rate", type=float, default=2.0)
+    ap.add_argument("--serve-max-iters", type=int, default=30000)
+    ap.add_argument("--serve-seconds", type=float, default=75.0)
+    ap.add_argument("--serve-budget-mb", type=int, default=0)
     ap.add_argument("--skip-serve", action="store_true")
+    # the replica launch and aggregation on CPU ranks (gloo); no GPU work
+    ap.add_argument("--cpu-replica-check", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return spawn_replicas(args.gpus, sys.argv[1:])
+    if args.cpu_replica_check:
+        return run_replica_check(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -184,9 +184,13 @@ int ot2d_metfv(double* q, double* x, double* y, double* xv, double* yv, double* 
  * in its own pool, a loop that must not take cudaMalloc's implicit device
  * synchronisation): the per-block partials live in a fixed static device
  * array, which limits jd*kd to OT2D_NOALLOC_MAX_CELLS (larger: OT2D_ERR_ARG,
- * nothing launched).  The first call on a device looks the array up with
- * that device current; make it before any stream capture.  Calls share the
- * array: calls that overlap in time race, so serialise them.  s, iblank:
+ * nothing launched).  The first call on a device looks the array's device
+ * address up with that device current and keeps it for the life of the
+ * process; after cudaDeviceReset that address is stale, so do not call this
+ * routine again in a process that has reset the device.  The call ends with a
+ * stream synchronisation and a copy to host memory, so it must not be made
+ * while its stream is being captured into a graph.  Calls share the array:
+ * calls that overlap in time race, so serialise them.  s, iblank:
  * device pointers; js..ke: the interior (jbeg..jend, kbeg..kend); nmv >= 4;
  * out (host, 6 doubles): rsum, resrho, resmax and the j, k, n of resmax
  * (1-based; 0 when there is no interior cell).  stream: a cudaStream_t
@@ -252,20 +256,36 @@ typedef struct ot2d_result {
   int32_t id, status, iterations, converged;
   double rsum_first, rsum_last;    /* L2 norm (step.f:86-93) at it 1 and last  */
   double cl, cd, cm, cpower;       /* compute_forces, FP64 (forces.f:2-127)     */
-  double t_admit, t_done;          /* seconds since solver creation             */
+  double t_admit, t_done;          /* seconds since solver creation: admitted to
+                                      the device, retired (t_admit < 0: queued)  */
+  double t_submit;                 /* seconds since solver creation: submitted  */
 } ot2d_result;
 
 /* solver options (ot2d_solver_set_option) */
-#define OT2D_OPT_CHECK_EVERY 1  /* iterations between host status reads (default 25) */
-#define OT2D_OPT_KEEP_Q      2  /* 1: keep q of retired instances for ot2d_solver_get_q */
+#define OT2D_OPT_CHECK_EVERY   1  /* iterations between host status reads (default 25) */
+#define OT2D_OPT_KEEP_Q        2  /* 1: keep q of retired instances for ot2d_solver_get_q */
+#define OT2D_OPT_FORCE_EVERY   3  /* force rule: iterations between the CL/CD samples of
+                                     its 8-sample window (default 0: every status check) */
+#define OT2D_OPT_FORCE_DECADES 4  /* force rule: decades the L2 norm must be below its peak
+                                     before the rule may retire an instance (default 1) */
+#define OT2D_OPT_BUDGET_MB     6  /* device memory the live instances may hold, MiB
+                                     (default 0: 90 % of the memory free when the solver
+                                     was created) */
+#define OT2D_OPT_POLL_LIMIT    5  /* polls a LU-SGS sweep wait makes before it gives up
+                                     (default 4194304).  An instance whose wait gave up
+                                     keeps its state and retires with OT2D_ERR_TIMEOUT;
+                                     small values make the waits run out on purpose */
 
 ot2d_solver* ot2d_solver_create(int32_t device, int32_t precision);
 void ot2d_solver_destroy(ot2d_solver* s);
 int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value);
 /* Also count an instance as converged once its CL and CD stayed within a
- * band of width dcl / dcd over the last 8 status checks and its L2 norm is a
- * decade below its peak (0, 0: residual criterion only, the default).  The
- * forces of running instances are then evaluated at every check. */
+ * band of width dcl / dcd over the last 8 force samples (one per status
+ * check, or one every OT2D_OPT_FORCE_EVERY iterations) and its L2 norm is
+ * OT2D_OPT_FORCE_DECADES (default 1) decades below its peak (0, 0: residual
+ * criterion only, the default).  This is the convergence rule of the
+ * FP32-mixed path, whose f32 residual has a floor a few decades below its
+ * peak and cannot show a 8-10 decade drop. */
 int ot2d_solver_set_force_tol(ot2d_solver* s, double dcl, double dcd);
 /* read the device status table now and retire finished instances */
 int ot2d_solver_sync(ot2d_solver* s);
@@ -281,9 +301,14 @@ int ot2d_solver_profile(ot2d_solver* s, int32_t iters, double* ms, int32_t nphas
  * copies q(jd,kd,nspec,nq) of the listed live instances host->device, runs
  * one batched iteration and copies q back (the host arrays are updated). */
 int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, double* const* q_host, int32_t iters);
-/* Admit one solve: params + vertex grid of time instance 1 (jmax*kmax).
+/* Submit one solve: params + vertex grid of time instance 1 (jmax*kmax).
  * Returns the instance id (>= 0) or -status.  `orders` = target L2 drop in
- * decades; max_iters caps the iterations.  A time-accurate solve (iunst = 1,
+ * decades; max_iters caps the iterations.  Admission is by device memory:
+ * a solve whose arrays (ot2d_instance_bytes) fit the memory budget next to
+ * the live instances is admitted at once; otherwise it waits in a FIFO
+ * queue and is admitted when retirements free enough memory (at a status
+ * check or at the next ot2d_solver_iterate); a solve larger than the whole
+ * budget is refused (-OT2D_ERR_NOMEM).  A time-accurate solve (iunst = 1,
  * motiontype = 1: the pitching grid of motion.f:546-632, dual time stepping
  * with itnmax Newton iterations per physical step, Turns_overset.f:360-505)
  * runs exactly max_iters physical steps, has no residual convergence test,
@@ -295,8 +320,10 @@ int ot2d_solver_add(ot2d_solver* s, const ot2d_params* p, const double* xv, cons
  * family per iteration).  Instances that converge, fail or reach their cap
  * are retired and their slot freed.  Returns OT2D_OK or a CUDA status. */
 int ot2d_solver_iterate(ot2d_solver* s, int32_t iters);
-/* number of live (not yet retired) instances */
+/* number of submitted, not yet retired instances (queued ones included) */
 int ot2d_solver_live(const ot2d_solver* s);
+/* number of submitted instances still waiting for device memory */
+int ot2d_solver_queued(const ot2d_solver* s);
 /* copy the result of instance `id` (valid once retired, or a live snapshot) */
 int ot2d_solver_result(ot2d_solver* s, int32_t id, ot2d_result* out);
 /* download q (jd,kd,nspec,nq) of a live or retired-but-kept instance */
@@ -321,6 +348,15 @@ int ot2d_solver_store_on_retire(ot2d_solver* s, int32_t id, const char* dir);
  * Returns the instance id or -status. */
 int ot2d_solver_add_restart(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv,
                             const char* dir, double orders, int32_t max_iters);
+
+/* Admit one solve that starts from the caller's state instead of the
+ * freestream: q(jd,kd,nspec,nq) in the reference layout (init.f:180-206:
+ * Q/J in 1..4, the turbulence variables in 5..nv); q(...,nq) is ignored, J
+ * comes from the grid (setup.f:440-724).  This is how a driver that owns q
+ * (Turns_overset.f:199-207) hands a state to the batched solver.  Returns
+ * the instance id or -status. */
+int ot2d_solver_add_state(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv,
+                          const double* q, double orders, int32_t max_iters);
 
 #ifdef __cplusplus
 }

@@ -406,3 +406,14 @@ void vmu_sa(const P& p, A3 q, A3 s, A2 turmu, A2 x, A2 y, const double* xv, cons
 }
 
 }  // namespace oro
+
+/* Test hook: the source terms of samodel2d.f:691-824 alone over the interior
+ * cells (jbeg..jend, kbeg..kend), so that a test can hold them against the
+ * published model.  q(jd,kd,nq) of one instance; sjmat and bk accumulate. */
+extern "C" void oro_sa_source(const oro::P* p, double* q, double* sn, double* vmul, double* vort, double* sjmat,
+                              double* bk) {
+  using namespace oro;
+  const A3 qq{q, p->jd, (size_t)p->jd * p->kd};
+  source(*p, qq, A2{sn, p->jd}, A2{sjmat, p->jd}, A2{vmul, p->jd}, A2{vort, p->jd}, A2{bk, p->jd}, p->jbeg,
+         p->jend, p->kbeg, p->kend);
+}

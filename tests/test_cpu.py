@@ -255,3 +255,93 @@ def test_oracle_overset_interpolation_is_exact_for_quadratics(nspec):
                     got = new[ii - 1, jj - 1, s, n] * (new[ii - 1, jj - 1, s, p.nq - 1] if n < p.nmv else 1.0)
                     assert abs(got - want) <= 1e-12 * abs(want)
             assert np.array_equal(new[~touched][:, s, :], old[~touched][:, s, :])
+
+
+def test_oracle_cases_match_the_library_setup():
+    """The benchmark's CPU legs build their cases without the product
+    library (oracle/oracle_cases.py + the oracle's read_inputs); those cases
+    are bitwise the ones the GPU arm builds with ot2d_mesh_naca4_cmesh,
+    ot2d_cmesh_bc_table and ot2d_params_from_inputs."""
+    oc = ob.oracle_cases()
+    rng = np.random.default_rng(4)
+    for (jm, km) in ((129, 33), (257, 65), (513, 129), (769, 193)):
+        for naca in ((0.0, 0.0, 0.12), (rng.uniform(0, 0.06), rng.uniform(0.2, 0.6), rng.uniform(0.08, 0.18))):
+            ds = oc.wall_spacing(km)
+            assert ds == api.wall_spacing(km)
+            alfa = float(rng.uniform(-2, 8))
+            inp, xv, yv = oc.c2_inputs(jm, km, fsmach=0.3, alfa=alfa, rey=5e6, naca=naca, ds_wall=ds)
+            _, prm, xv2, yv2 = api.config_c2(jm, km, fsmach=0.3, alfa=alfa, rey=5e6, naca=naca, ds_wall=ds)
+            assert np.array_equal(xv, xv2) and np.array_equal(yv, yv2), (jm, km, naca)
+            assert bytes(ob.read_inputs(inp)) == bytes(prm)
+
+
+def _sa_published(nut, nu, d, omega, rey):
+    """Production and destruction of the Spalart-Allmaras model as
+    published (Spalart & Allmaras, "A one-equation turbulence model for
+    aerodynamic flows", La Recherche Aerospatiale 1994(1):5-21; the standard
+    form without the trip and ft2 terms), in the reference's nondimensional
+    form (lengths in chords, 1/Re on the viscous terms).  The constants are
+    the paper's, with cw1 = cb1/kappa^2 + (1 + cb2)/sigma."""
+    cb1, sigma, cb2, kappa, cw2, cw3, cv1 = 0.1355, 2.0 / 3.0, 0.622, 0.41, 0.3, 2.0, 7.1
+    cw1 = cb1 / kappa ** 2 + (1.0 + cb2) / sigma
+    chi = nut / nu
+    fv1 = chi ** 3 / (chi ** 3 + cv1 ** 3)
+    fv2 = 1.0 - chi / (1.0 + chi * fv1)
+    st = omega + nut * fv2 / (kappa ** 2 * d ** 2 * rey)
+    r = np.minimum(nut / (st * kappa ** 2 * d ** 2 * rey), 10.0)
+    g = r + cw2 * (r ** 6 - r)
+    fw = g * ((1.0 + cw3 ** 6) / (g ** 6 + cw3 ** 6)) ** (1.0 / 6.0)
+    return cb1 * st * nut, cw1 * fw * (nut / d) ** 2 / rey
+
+
+def test_oracle_sa_source_matches_the_published_model():
+    """The oracle's SA source (samodel2d.f:691-824) at single cells against
+    an independent evaluation of the published model: the residual term
+    P - D, and the implicit diagonal it adds, max(D/nut - P/nut, 0) +
+    max(dD/dnut - D/nut - dP/dnut + P/nut, 0), with the derivatives taken by
+    central differences of the published formulas.  This catches a wrong
+    constant, sign or exponent in terms that vanish in freestream or on a
+    symmetric flow.  The reference writes its constants as decimals
+    (sigma = 0.6666667, cw1 = 3.2390678): they agree with the paper's to
+    ~1e-8, and the terms to 1e-7."""
+    _, p, _, _ = api.config_c2(jmax=33, kmax=17, ds_wall=1e-3)
+    jd, kd, n2 = p.jd, p.kd, p.jd * p.kd
+    rng = np.random.default_rng(17)
+    rho_over_j = rng.uniform(0.5e-3, 2e-3, n2)      # q(1) = rho / J
+    jac = rng.uniform(0.5e3, 2e3, n2)               # q(nq) = J
+    rho = rho_over_j * jac
+    vmul = rng.uniform(0.8, 1.2, n2)                # laminar viscosity (nondimensional)
+    nu = vmul / rho
+    chi = 10.0 ** rng.uniform(-1, 2.5, n2)          # nut / nu from the wall region to the outer layer
+    nut = chi * nu
+    d = 10.0 ** rng.uniform(-5, -1, n2)             # wall distance, chords
+    omega = 10.0 ** rng.uniform(-1, 3, n2)          # vorticity
+    q = np.zeros(n2 * p.nq)
+    q[:n2] = rho_over_j
+    q[(p.nmv) * n2:(p.nmv + 1) * n2] = nut          # q(nmv+1) = nu_tilde
+    q[(p.nq - 1) * n2:] = jac
+    sjmat, bk = np.zeros(n2), np.zeros(n2)
+    L = ob.lib()
+    L.oro_sa_source.argtypes = [C.POINTER(type(p))] + [C.POINTER(C.c_double)] * 6
+    L.oro_sa_source(C.byref(p), ob.ptr(q), ob.ptr(d), ob.ptr(vmul), ob.ptr(omega), ob.ptr(sjmat), ob.ptr(bk))
+    inner = np.zeros((kd, jd), bool)
+    inner[p.kbeg - 1:p.kend, p.jbeg - 1:p.jend] = True
+    inner = inner.ravel()
+    P, D = _sa_published(nut, nu, d, omega, p.rey)
+    # the published form has no clips: compare where the reference's clips
+    # of S~ (at 1e-12, fv2 < 0 makes S~ < vorticity) and of r (at 10) are
+    # inactive, with a margin for the central differences
+    fv2 = 1.0 - chi / (1.0 + chi * chi ** 3 / (chi ** 3 + 7.1 ** 3))
+    st = omega + nut * fv2 / (0.41 ** 2 * d ** 2 * p.rey)
+    r = nut / (st * 0.41 ** 2 * d ** 2 * p.rey)
+    sel = inner & (st > 0.1 * omega) & (r < 9.0)
+    assert sel.sum() > 100
+    assert np.max(np.abs(sjmat - (P - D))[sel] / np.maximum(np.abs(P), np.abs(D))[sel]) < 1e-7
+    h = 1e-6 * nut
+    Pp, Dp = _sa_published(nut + h, nu, d, omega, p.rey)
+    Pm, Dm = _sa_published(nut - h, nu, d, omega, p.rey)
+    dP, dD = (Pp - Pm) / (2 * h), (Dp - Dm) / (2 * h)
+    diag = np.maximum(D / nut - P / nut, 0.0) + np.maximum(dD - D / nut - dP + P / nut, 0.0)
+    scale = np.maximum.reduce([np.abs(P / nut), np.abs(D / nut), np.abs(dP), np.abs(dD)])
+    assert np.max(np.abs(bk - diag)[sel] / scale[sel]) < 1e-6
+    assert not bk[~inner].any() and not sjmat[~inner].any()

@@ -1,0 +1,63 @@
+"""The plain FP64 path on the benchmark's configurations at full size,
+against the oracle's fixtures (tests/golden/make_full_golden.py):
+
+  c1_full  inviscid 257x65, 2000 iterations (the configuration's count)
+  c2_full  RANS-SA 513x129 with 1e-6 wall spacing, 2000 iterations
+  c3_full  k-omega SST + WENO5 + ADI on 769x193 with 5e-7 wall spacing,
+           400 iterations at CFL 0.25
+
+Compared: the L2 norm of step.f:86-93 along the run, the final CL, CD, CM
+and cpower of forces.f, and checksums plus 1024 sample cells of the final
+state.  The bar is 1e-12 relative (the norms are tree reductions in another
+order, the state is bitwise the oracle's); the SST case is held to 1e-10:
+its model evaluates exp, tanh and real powers, whose last bit may differ
+between CUDA's and the host's libm, and 400 iterations carry that through
+the coupled solve."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.golden.make_full_golden import CASES, case, checksums
+from tests.helpers import relerr
+from turns2d_urans_git_gb300 import api
+from turns2d_urans_git_gb300.abi import OT2D_FP64
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = {"c1_full": 1e-12, "c2_full": 1e-12, "c3_full": 1e-10}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_full_size_fp64_matches_oracle_fixture(name):
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    kind, nsteps = CASES[name]
+    assert int(g["nsteps"]) == nsteps
+    _, prm, xv, yv = case(kind)
+    every = 1 if kind == "c1" else 20
+    sv = api.Solver(OT2D_FP64, check_every=every, keep_q=True)
+    iid = sv.add(prm, xv, yv, orders=0.0, max_iters=nsteps)
+    hist = []
+    done = 0
+    while done < nsteps:
+        sv.iterate(every)
+        done += every
+        r = sv.result(iid)
+        hist.append((min(done, nsteps), r.rsum_last))
+    sv.sync()
+    r = sv.result(iid)
+    q = sv.get_q(iid, prm)
+    sv.close()
+    tol = TOL[name]
+    assert r.status == 0 and r.iterations == nsteps
+    its = np.array([h[0] for h in hist]) - 1
+    assert relerr(np.array([h[1] for h in hist]), g["hist"][its]) <= tol
+    assert abs(r.rsum_first - g["hist"][0]) <= tol * g["hist"][0]
+    for a, b in zip((r.cl, r.cd, r.cm, r.cpower), g["forces"]):
+        assert abs(a - b) <= tol * max(abs(b), 1e-3), (name, a, b)
+    c = checksums(q, prm)
+    for k in ("qsum", "qsq", "qw"):
+        assert relerr(c[k], g[k]) <= tol, k
+    assert np.array_equal(c["cells"], g["cells"])
+    assert relerr(c["qcells"], g["qcells"]) <= tol

@@ -54,3 +54,26 @@ def test_replica_aggregation_gloo_world2():
     assert t0 == t1 == 0.75                 # both ranks see the slowest rank's time
     assert rate0 == rate1 == 2 * 1000 / 0.75   # all ranks' units over that time
     assert a0[1] != a1[1]                   # each rank serves its own seeded requests
+
+
+def test_bench_gpus2_spawns_two_replicas_gloo():
+    """`bench.py --gpus 2` outside a launcher starts two replica processes
+    itself (torch.distributed.run, 127.0.0.1); in the CPU check mode each
+    rank times its own seeded request over gloo and rank 0 prints the
+    whole-job line."""
+    import json
+    import subprocess
+    pytest.importorskip("torch")
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_ADDR",
+                                                            "MASTER_PORT")}
+    env["OMP_NUM_THREADS"] = "1"
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--batch", "2",
+                        "--cpu-replica-check"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = json.loads(lines[0])
+    assert line["n_gpus"] == 2
+    assert line["value"] == pytest.approx(2 * line["units_per_rank"] / line["seconds"])
+    a0, a1 = line["alfas"]
+    assert len(a0) == len(a1) == 2 and a0[1] != a1[1]     # each rank its own seeded requests

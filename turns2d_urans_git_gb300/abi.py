@@ -19,8 +19,18 @@ OT2D_ERR_NOPARAMS = 5
 OT2D_ERR_NOMEM = 6
 OT2D_ERR_TIMEOUT = 7
 
+OT2D_ERR_IO = 8
+
 OT2D_FP64 = 0
 OT2D_FP32_MIXED = 1
+
+# solver options (ot2d_solver_set_option)
+OT2D_OPT_CHECK_EVERY = 1
+OT2D_OPT_KEEP_Q = 2
+OT2D_OPT_FORCE_EVERY = 3
+OT2D_OPT_FORCE_DECADES = 4
+OT2D_OPT_POLL_LIMIT = 5
+OT2D_OPT_BUDGET_MB = 6
 
 _I = C.c_int32
 _D = C.c_double
@@ -65,7 +75,7 @@ class Inputs(C.Structure):
 class Result(C.Structure):
     _fields_ = [("id", _I), ("status", _I), ("iterations", _I), ("converged", _I),
                 ("rsum_first", _D), ("rsum_last", _D), ("cl", _D), ("cd", _D), ("cm", _D), ("cpower", _D),
-                ("t_admit", _D), ("t_done", _D)]
+                ("t_admit", _D), ("t_done", _D), ("t_submit", _D)]
 
 
 def default_inputs(**kw):

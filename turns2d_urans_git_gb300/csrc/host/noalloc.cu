@@ -13,8 +13,12 @@
 //    1025 x 1023 mesh); larger meshes are rejected with OT2D_ERR_ARG before
 //    anything is launched.
 //  * The first call on a device looks up the device address of the static
-//    scratch (cudaGetSymbolAddress, with that device current); make that
-//    first call before any stream capture on the device.
+//    scratch (cudaGetSymbolAddress, with that device current) and keeps it
+//    for the life of the process.  cudaDeviceReset unloads the module, so
+//    the kept address is stale afterwards: a process that resets the device
+//    must not call this routine again.
+//  * Every call ends with cudaStreamSynchronize and a copy into the caller's
+//    host buffer, so no call may be made while its stream is being captured.
 //  * The scratch is shared by every call on the device: two calls that
 //    overlap in time (different host threads, or different streams without
 //    an ordering between them) race on it.  Serialise them.

@@ -110,6 +110,17 @@ size_t solve_bytes(const ot2d_params& p, int precision) {
   return plan(p, precision, [](const char*, size_t) {});
 }
 
+bool batch_fits(int precision, bool precon, int kd_max, int jd_max) {
+  if (kd_max < 3 || jd_max < 3 || kd_max - 2 > 1024) return false;
+  const int nw = lu_nband(kd_max);
+  size_t lu;
+  if (precision == OT2D_FP32_MIXED)
+    lu = precon ? lu_smem_bytes<float, true>(nw, 1, jd_max) : lu_smem_bytes<float, false>(nw, 1, jd_max);
+  else
+    lu = precon ? lu_smem_bytes<double, true>(nw, 1, jd_max) : lu_smem_bytes<double, false>(nw, 1, jd_max);
+  return lu <= (size_t)SMEM_OPTIN_MAX && sizeof(double) * 3 * (size_t)jd_max <= (size_t)SMEM_OPTIN_MAX;
+}
+
 void solve_destroy(DevSolve& d) {
   if (d.mem) cudaFree(d.mem);
   if (d.motion) cudaFree(d.motion);
@@ -170,6 +181,8 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
   if (precision != OT2D_FP64 && precision != OT2D_FP32_MIXED) return OT2D_ERR_ARG;
   if (p.ilhs < 1 || p.ilhs > 3) return OT2D_ERR_ARG;        // LU-SGS or ADI (pentadiagonal / upwind)
   if (p.ilhs != 1 && (p.jd < 10 || p.kd < 10)) return OT2D_ERR_ARG;  // ADI lines of >= 8 points
+  // the sweep's CTA and shared memory, the force kernel's staging
+  if (!batch_fits(precision, p.iprecon != 0, p.kd, p.jd)) return OT2D_ERR_ARG;
   if (!p.lamin && p.iturb != 1 && p.iturb != 2) return OT2D_ERR_ARG;  // SA or k-omega SST
   if (p.itrans != 0) return OT2D_ERR_ARG;                            // no transition model
   // steady, or time accurate with the pitching grid (Turns_overset.f:372-403:
@@ -420,6 +433,9 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
     maxwall = std::max(maxwall, jd);
     maxkd = std::max(maxkd, kd);
   }
+  // a combination of meshes that fit alone may not fit together
+  if (n > 0 && !batch_fits(sizeof(R) == sizeof(float) ? OT2D_FP32_MIXED : OT2D_FP64, precon != 0, maxkd, maxwall))
+    return OT2D_ERR_ARG;
   idx[n] = cells; idx[2 * (n + 1) - 1] = jl; idx[3 * (n + 1) - 1] = kl; idx[4 * (n + 1) - 1] = lub;
   idx[5 * (n + 1) - 1] = grp; idx[6 * (n + 1) - 1] = tiles;
   if ((size_t)n > cap_sl) {

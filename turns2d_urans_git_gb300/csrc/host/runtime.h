@@ -52,6 +52,13 @@ struct DevSolve {
 
 // bytes one solve needs on the device
 size_t solve_bytes(const ot2d_params& p, int precision);
+// Launch limits of a batch whose tallest mesh has kd_max array rows and
+// whose widest has jd_max columns: the LU-SGS sweep runs one warp per 32
+// interior rows in one CTA (at most 1024 threads, kd - 2 <= 1024) with its
+// record ring, cross-band rings and first-row halo terms in shared memory
+// (at most 227 KB), and the force kernel stages 3 doubles per wall cell.
+// precon: the batch holds a preconditioned (preilu2d) mesh.
+bool batch_fits(int precision, bool precon, int kd_max, int jd_max);
 // allocate + fill the geometry and the freestream state of a solve from the
 // vertex grid of time instance 1 (xv1, yv1: jmax*kmax).  Returns OT2D_OK,
 // OT2D_ERR_ARG (bad grid / params) or OT2D_ERR_NOMEM / OT2D_ERR_CUDA.

@@ -11,6 +11,8 @@
 #include <cmath>
 #include <cstddef>
 #include <cstring>
+#include <deque>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -36,9 +38,27 @@ struct Rec {
   // the last FORCE_WIN status checks
   double win_cl[8] = {0}, win_cd[8] = {0};
   int nwin = 0;
+  long force_at = 0;       // iteration count of the last force sample
   std::string store_dir;   // ot2d_solver_store_on_retire: written when retired
+  bool queued = false;     // submitted, waiting for device memory
 };
 constexpr int FORCE_WIN = 8;
+
+// State set-up of a solve right after its admission (initial state from the
+// caller or from a restart file); returns an OT2D status.
+using InitFn = std::function<int(ot2d_solver*, Rec&)>;
+
+// A submitted solve waiting for device memory.
+struct Pending {
+  int id = -1;
+  ot2d_params p{};
+  std::vector<double> xv, yv;
+  double orders = 10.0;
+  int max_iters = 0;
+  size_t bytes = 0;
+  double t_submit = 0;
+  InitFn init;
+};
 
 // iterations an instance runs before it retires: max_iters, or max_iters
 // physical steps of itnmax Newton iterations each
@@ -69,6 +89,10 @@ struct ot2d_solver {
   std::vector<int> free_slots;
   std::map<int, Rec> recs;
   std::vector<int> live;
+  std::deque<Pending> queue;             // submitted, waiting for device memory (FIFO)
+  size_t budget_auto = 0;                // 90 % of the free memory at creation
+  size_t budget_set = 0;                 // OT2D_OPT_BUDGET_MB (0: the automatic budget)
+  size_t used = 0;                       // device bytes of the live instances
   DevBatch<double> b64;
   DevBatch<float> b32;
   bool dirty = true;
@@ -78,6 +102,9 @@ struct ot2d_solver {
   double t0 = 0;
   int check_every = 25;
   double force_dcl = 0, force_dcd = 0;   // > 0: also converge on stable forces
+  int force_every = 0;                   // iterations between force samples (0: every check)
+  int force_decades = 1;                 // norm drop below the peak the force rule needs
+  uint32_t poll_limit = 1u << 22;        // polls of a sweep wait (OT2D_OPT_POLL_LIMIT)
   int keep_q = 0;
   int since_check = 0;
   bool any_viscous = false;
@@ -149,6 +176,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   if (sl.empty()) return OT2D_OK;
   int e = B.build(sl, s->st);
   if (e) return e;
+  B.b.poll_limit = s->poll_limit;
   // The kernels branch on each slice's own params, so inviscid, laminar,
   // SA and SST requests can share one batch.
   Branch* br = nullptr;   // the turbulence branch's stream, created outside the capture
@@ -283,6 +311,131 @@ int store_rec(ot2d_solver* s, Rec& r, const std::string& dir) {
   return write_solution(dir, pw, r.d.q64, qc, x.data(), y.data(), ib.data(), ist[0], s->st);
 }
 
+size_t budget_of(const ot2d_solver* s) { return s->budget_set ? s->budget_set : s->budget_auto; }
+
+// The launches of the batch a new mesh would join must still fit.
+bool fits_with_live(ot2d_solver* s, const ot2d_params& p) {
+  int kdm = p.kd, jdm = p.jd;
+  bool pre = p.iprecon != 0;
+  for (int id : s->live) {
+    const ot2d_params& q = s->recs[id].d.P;
+    kdm = std::max(kdm, (int)q.kd); jdm = std::max(jdm, (int)q.jd); pre = pre || q.iprecon;
+  }
+  return batch_fits(s->precision, pre, kdm, jdm);
+}
+
+// Create the device state of a submitted solve and make it live.
+int admit(ot2d_solver* s, Pending& pd) {
+  if (grow_slots(s, pd.p.nspec) != OT2D_OK) return OT2D_ERR_NOMEM;
+  Rec r;
+  int e = solve_create(r.d, pd.p, s->precision, pd.xv.data(), pd.yv.data(), s->st);
+  if (e) return e;
+  double orders = pd.orders;
+  if (pd.p.iunst == 1) {
+    // time accurate: max_iters physical steps, the pitch table for them,
+    // no residual convergence test
+    e = solve_motion_table(r.d, pd.max_iters, s->st);
+    if (e) { solve_destroy(r.d); return e; }
+    orders = 0.0;
+  }
+  r.id = pd.id;
+  r.orders = orders; r.max_iters = pd.max_iters; r.live = true;
+  r.res.id = r.id;
+  r.res.t_submit = pd.t_submit;
+  r.res.t_admit = now_s() - s->t0;
+  std::vector<double> red(RED_N, 0.0);
+  std::vector<int32_t> ist(IST_N, 0);
+  red[7] = orders > 0 ? std::pow(10.0, -orders) : -1.0;
+  ist[0] = pd.p.istep0; ist[1] = 0;
+  for (int nsp = 0; nsp < pd.p.nspec; ++nsp) {
+    int sl = s->free_slots.back(); s->free_slots.pop_back();
+    r.slots.push_back(sl);
+    cudaMemcpyAsync(s->d_red + (size_t)RED_N * sl, red.data(), sizeof(double) * RED_N, cudaMemcpyHostToDevice, s->st);
+    cudaMemcpyAsync(s->d_ist + (size_t)IST_N * sl, ist.data(), sizeof(int32_t) * IST_N, cudaMemcpyHostToDevice, s->st);
+  }
+  if (cudaStreamSynchronize(s->st) != cudaSuccess) {
+    for (int sl : r.slots) s->free_slots.push_back(sl);
+    solve_destroy(r.d);
+    return OT2D_ERR_CUDA;
+  }
+  const int id = r.id;
+  s->used += r.d.bytes;
+  auto prev = s->recs.find(id);
+  if (prev != s->recs.end()) r.store_dir = prev->second.store_dir;   // set while it was queued
+  s->recs[id] = std::move(r);
+  s->live.push_back(id);
+  s->dirty = true;
+  if (pd.init) {
+    Rec& rr = s->recs[id];
+    e = pd.init(s, rr);
+    if (e) {
+      for (int sl : rr.slots) s->free_slots.push_back(sl);
+      rr.slots.clear();
+      s->used -= rr.d.bytes;
+      solve_destroy(rr.d);
+      rr.live = false;
+      s->live.erase(std::remove(s->live.begin(), s->live.end(), id), s->live.end());
+      return e;
+    }
+  }
+  return OT2D_OK;
+}
+
+// Admit queued solves in submission order while they fit the budget and the
+// batch launches; a failed admission retires that solve with its status.
+void admit_queued(ot2d_solver* s) {
+  while (!s->queue.empty()) {
+    Pending& head = s->queue.front();
+    if (s->used + head.bytes > budget_of(s) || !fits_with_live(s, head.p)) break;
+    Pending pd = std::move(head);
+    s->queue.pop_front();
+    const int e = admit(s, pd);
+    if (e) {
+      Rec& r = s->recs[pd.id];
+      r.live = false;
+      r.queued = false;
+      r.res.status = e;
+      r.res.t_done = now_s() - s->t0;
+    }
+  }
+}
+
+// Submit a solve: admitted now when it fits (and nothing is queued ahead of
+// it), queued otherwise.  Returns the id or -status.
+int submit(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv, double orders, int max_iters,
+           InitFn init) {
+  if (!s || !p || !xv || !yv || max_iters < 1) return -OT2D_ERR_ARG;
+  cudaSetDevice(s->device);
+  // a mesh that cannot launch even alone, or cannot fit the budget at all
+  if (!batch_fits(s->precision, p->iprecon != 0, p->kd, p->jd)) return -OT2D_ERR_ARG;
+  const size_t bytes = solve_bytes(*p, s->precision);
+  if (bytes > budget_of(s)) return -OT2D_ERR_NOMEM;
+  Pending pd;
+  pd.id = s->next_id++;
+  pd.p = *p;
+  const size_t nv = (size_t)p->jmax * p->kmax;
+  pd.xv.assign(xv, xv + nv);
+  pd.yv.assign(yv, yv + nv);
+  pd.orders = orders; pd.max_iters = max_iters; pd.bytes = bytes;
+  pd.t_submit = now_s() - s->t0;
+  pd.init = std::move(init);
+  if (s->queue.empty() && s->used + bytes <= budget_of(s) && fits_with_live(s, *p)) {
+    const int e = admit(s, pd);
+    return e ? -e : pd.id;
+  }
+  Rec r;
+  r.id = pd.id;
+  r.res.id = pd.id;
+  r.res.t_submit = pd.t_submit;
+  r.res.t_admit = -1.0;
+  r.max_iters = max_iters;
+  r.queued = true;
+  s->recs[pd.id] = std::move(r);
+  const int id = pd.id;
+  s->queue.push_back(std::move(pd));
+  return id;
+}
+
 int check(ot2d_solver* s) {
   s->since_check = 0;
   if (s->live.empty()) return OT2D_OK;
@@ -316,8 +469,12 @@ int check(ot2d_solver* s) {
     // within the tolerances over the last FORCE_WIN checks and the L2 norm
     // is a decade below its peak
     std::vector<int> run;
-    for (int id : s->live)
-      if (std::find(done.begin(), done.end(), id) == done.end()) run.push_back(id);
+    for (int id : s->live) {
+      const Rec& r = s->recs[id];
+      if (std::find(done.begin(), done.end(), id) != done.end()) continue;
+      if (s->force_every > 0 && r.nwin > 0 && r.launched - r.force_at < s->force_every) continue;
+      run.push_back(id);
+    }
     if (!run.empty()) {
       int fe = (s->precision == OT2D_FP64) ? forces_t<double>(s, run, s->f64) : forces_t<float>(s, run, s->f32);
       if (fe) return fe;
@@ -327,7 +484,8 @@ int check(ot2d_solver* s) {
         r.win_cl[r.nwin % FORCE_WIN] = r.res.cl;
         r.win_cd[r.nwin % FORCE_WIN] = r.res.cd;
         ++r.nwin;
-        if (r.nwin < FORCE_WIN || !(red[5] <= 0.1 * red[6])) continue;
+        r.force_at = r.launched;
+        if (r.nwin < FORCE_WIN || !(red[5] <= std::pow(10.0, -s->force_decades) * red[6])) continue;
         double lo_l = r.win_cl[0], hi_l = lo_l, lo_d = r.win_cd[0], hi_d = lo_d;
         for (int i = 1; i < FORCE_WIN; ++i) {
           lo_l = std::min(lo_l, r.win_cl[i]); hi_l = std::max(hi_l, r.win_cl[i]);
@@ -353,6 +511,7 @@ int check(ot2d_solver* s) {
     }
     for (int sl : r.slots) s->free_slots.push_back(sl);
     r.slots.clear();
+    s->used -= r.d.bytes;
     solve_destroy(r.d);
     r.live = false;
   }
@@ -360,6 +519,8 @@ int check(ot2d_solver* s) {
   for (int id : s->live) if (s->recs[id].live) nl.push_back(id);
   s->live.swap(nl);
   s->dirty = true;
+  // the memory just freed admits queued solves
+  admit_queued(s);
   return e;
 }
 
@@ -373,6 +534,8 @@ ot2d_solver* ot2d_solver_create(int32_t device, int32_t precision) {
   ot2d_solver* s = new ot2d_solver();
   s->device = device; s->precision = precision;
   if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) { delete s; return nullptr; }
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) s->budget_auto = fr / 10 * 9;
   s->t0 = now_s();
   return s;
 }
@@ -401,6 +564,14 @@ int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value) {
   if (!s) return OT2D_ERR_ARG;
   if (key == OT2D_OPT_CHECK_EVERY && value >= 1) { s->check_every = value; return OT2D_OK; }
   if (key == OT2D_OPT_KEEP_Q) { s->keep_q = value ? 1 : 0; return OT2D_OK; }
+  if (key == OT2D_OPT_FORCE_EVERY && value >= 0) { s->force_every = value; return OT2D_OK; }
+  if (key == OT2D_OPT_FORCE_DECADES && value >= 0) { s->force_decades = value; return OT2D_OK; }
+  if (key == OT2D_OPT_BUDGET_MB && value >= 0) { s->budget_set = (size_t)value << 20; return OT2D_OK; }
+  if (key == OT2D_OPT_POLL_LIMIT && value >= 1) {
+    s->poll_limit = (uint32_t)value;
+    s->dirty = true;   // the sweeps take the limit as a launch argument
+    return OT2D_OK;
+  }
   return OT2D_ERR_ARG;
 }
 
@@ -412,39 +583,7 @@ int ot2d_solver_set_force_tol(ot2d_solver* s, double dcl, double dcd) {
 
 int ot2d_solver_add(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv, double orders,
                     int32_t max_iters) {
-  if (!s || !p || !xv || !yv || max_iters < 1) return -OT2D_ERR_ARG;
-  cudaSetDevice(s->device);
-  if (grow_slots(s, p->nspec) != OT2D_OK) return -OT2D_ERR_NOMEM;
-  Rec r;
-  int e = solve_create(r.d, *p, s->precision, xv, yv, s->st);
-  if (e) return -e;
-  if (p->iunst == 1) {
-    // time accurate: max_iters physical steps, the pitch table for them,
-    // no residual convergence test
-    e = solve_motion_table(r.d, max_iters, s->st);
-    if (e) { solve_destroy(r.d); return -e; }
-    orders = 0.0;
-  }
-  r.id = s->next_id++;
-  r.orders = orders; r.max_iters = max_iters; r.live = true;
-  r.res.id = r.id;
-  r.res.t_admit = now_s() - s->t0;
-  std::vector<double> red(RED_N, 0.0);
-  std::vector<int32_t> ist(IST_N, 0);
-  red[7] = orders > 0 ? std::pow(10.0, -orders) : -1.0;
-  ist[0] = p->istep0; ist[1] = 0;
-  for (int nsp = 0; nsp < p->nspec; ++nsp) {
-    int sl = s->free_slots.back(); s->free_slots.pop_back();
-    r.slots.push_back(sl);
-    cudaMemcpyAsync(s->d_red + (size_t)RED_N * sl, red.data(), sizeof(double) * RED_N, cudaMemcpyHostToDevice, s->st);
-    cudaMemcpyAsync(s->d_ist + (size_t)IST_N * sl, ist.data(), sizeof(int32_t) * IST_N, cudaMemcpyHostToDevice, s->st);
-  }
-  cudaStreamSynchronize(s->st);
-  const int id = r.id;
-  s->recs[id] = std::move(r);
-  s->live.push_back(id);
-  s->dirty = true;
-  return id;
+  return submit(s, p, xv, yv, orders, max_iters, InitFn());
 }
 
 int ot2d_solver_iterate(ot2d_solver* s, int32_t iters) {
@@ -452,6 +591,7 @@ int ot2d_solver_iterate(ot2d_solver* s, int32_t iters) {
   cudaSetDevice(s->device);
   int done = 0;
   while (done < iters) {
+    admit_queued(s);
     if (s->dirty) { int e = rebuild(s); if (e) return e; }
     if (s->live.empty()) break;
     int chunk = std::min(s->check_every - s->since_check, iters - done);
@@ -479,7 +619,9 @@ int ot2d_solver_sync(ot2d_solver* s) {
   return check(s);
 }
 
-int ot2d_solver_live(const ot2d_solver* s) { return s ? (int)s->live.size() : 0; }
+int ot2d_solver_live(const ot2d_solver* s) { return s ? (int)(s->live.size() + s->queue.size()) : 0; }
+
+int ot2d_solver_queued(const ot2d_solver* s) { return s ? (int)s->queue.size() : 0; }
 
 int ot2d_solver_result(ot2d_solver* s, int32_t id, ot2d_result* out) {
   if (!s || !out) return OT2D_ERR_ARG;
@@ -597,7 +739,7 @@ int ot2d_solver_store(ot2d_solver* s, int32_t id, const char* dir) {
 int ot2d_solver_store_on_retire(ot2d_solver* s, int32_t id, const char* dir) {
   if (!s) return OT2D_ERR_ARG;
   auto it = s->recs.find(id);
-  if (it == s->recs.end() || !it->second.live) return OT2D_ERR_ARG;
+  if (it == s->recs.end() || !(it->second.live || it->second.queued)) return OT2D_ERR_ARG;
   it->second.store_dir = dir ? dir : "";
   return OT2D_OK;
 }
@@ -605,14 +747,13 @@ int ot2d_solver_store_on_retire(ot2d_solver* s, int32_t id, const char* dir) {
 int ot2d_solver_add_restart(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv,
                             const char* dir, double orders, int32_t max_iters) {
   if (!s || !p || !dir) return -OT2D_ERR_ARG;
-  const int id = ot2d_solver_add(s, p, xv, yv, orders, max_iters);
-  if (id < 0) return id;
-  Rec& r = s->recs[id];
-  double totime = 0.0;
-  int istep0 = 0;
-  float* qc = s->precision == OT2D_FP32_MIXED ? (float*)r.d.q : nullptr;
-  int e = read_restart(dir, r.d.P, r.d.q64, qc, &totime, &istep0, s->st);
-  if (!e) {
+  const std::string d = dir;
+  return submit(s, p, xv, yv, orders, max_iters, [d](ot2d_solver* s, Rec& r) -> int {
+    double totime = 0.0;
+    int istep0 = 0;
+    float* qc = s->precision == OT2D_FP32_MIXED ? (float*)r.d.q : nullptr;
+    int e = read_restart(d, r.d.P, r.d.q64, qc, &totime, &istep0, s->st);
+    if (e) return e;
     // init.f:165 (istep0) of the restart file; the instance runs as a
     // reference restart does, with iread = 1 (the wall start-up ramps of
     // bc.f / komegasst.f are then off).  The file's totime is not kept: the
@@ -622,22 +763,37 @@ int ot2d_solver_add_restart(ot2d_solver* s, const ot2d_params* p, const double* 
     const int32_t i0 = istep0;
     if (cudaMemcpyAsync((char*)r.d.dP + offsetof(ot2d_params, iread), &r.d.P.iread, sizeof(int32_t),
                         cudaMemcpyHostToDevice, s->st) != cudaSuccess)
-      e = OT2D_ERR_CUDA;
+      return OT2D_ERR_CUDA;
     for (int sl : r.slots)
-      if (!e && cudaMemcpyAsync(s->d_ist + (size_t)IST_N * sl, &i0, sizeof(i0), cudaMemcpyHostToDevice, s->st) !=
-                    cudaSuccess)
-        e = OT2D_ERR_CUDA;
-    if (!e && cudaStreamSynchronize(s->st) != cudaSuccess) e = OT2D_ERR_CUDA;
-  }
-  if (e) {
-    for (int sl : r.slots) s->free_slots.push_back(sl);
-    solve_destroy(r.d);
-    s->recs.erase(id);
-    s->live.erase(std::remove(s->live.begin(), s->live.end(), id), s->live.end());
-    s->dirty = true;
-    return -e;
-  }
-  return id;
+      if (cudaMemcpyAsync(s->d_ist + (size_t)IST_N * sl, &i0, sizeof(i0), cudaMemcpyHostToDevice, s->st) !=
+          cudaSuccess)
+        return OT2D_ERR_CUDA;
+    return cudaStreamSynchronize(s->st) == cudaSuccess ? OT2D_OK : OT2D_ERR_CUDA;
+  });
+}
+
+int ot2d_solver_add_state(ot2d_solver* s, const ot2d_params* p, const double* xv, const double* yv,
+                          const double* q, double orders, int32_t max_iters) {
+  if (!s || !p || !q) return -OT2D_ERR_ARG;
+  const size_t n2 = (size_t)p->jd * p->kd, ns = (size_t)p->nspec, nv = (size_t)p->nv;
+  // reference layout (n, s, cell) -> the unpack's record layout (s, n, cell)
+  std::vector<double> rec(ns * nv * n2);
+  for (size_t sp = 0; sp < ns; ++sp)
+    for (size_t n = 0; n < nv; ++n)
+      std::memcpy(rec.data() + (sp * nv + n) * n2, q + (n * ns + sp) * n2, n2 * sizeof(double));
+  return submit(s, p, xv, yv, orders, max_iters, [rec = std::move(rec)](ot2d_solver* s, Rec& r) -> int {
+    double* tmp = nullptr;
+    int e = OT2D_OK;
+    if (cudaMalloc(&tmp, rec.size() * sizeof(double)) != cudaSuccess) return OT2D_ERR_NOMEM;
+    float* qc = s->precision == OT2D_FP32_MIXED ? (float*)r.d.q : nullptr;
+    if (cudaMemcpyAsync(tmp, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice, s->st) !=
+            cudaSuccess ||
+        io_unpack(tmp, r.d.q64, qc, r.d.n2, r.d.nspec, r.d.P.nq, r.d.P.nv, 0, s->st) != cudaSuccess ||
+        cudaStreamSynchronize(s->st) != cudaSuccess)
+      e = OT2D_ERR_CUDA;
+    cudaFree(tmp);
+    return e;
+  });
 }
 
 }  // extern "C"

@@ -362,10 +362,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Bounded wait on a ring slot; false after ~2^22 polls (the status word of
-// the slice records the timeout).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 22); ++it)
+// Polls a sweep wait makes before it gives up (the status word of the slice
+// records the timeout).  The solver can lower it (OT2D_OPT_POLL_LIMIT) to
+// make the waits run out on purpose; the drain of copies still in flight
+// after a give-up always uses this default bound.
+constexpr uint32_t LU_POLL_DEFAULT = 1u << 22;
+
+// Bounded wait on a ring slot; false after `lim` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t lim = LU_POLL_DEFAULT) {
+  for (uint32_t it = 0; it < lim; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -383,9 +388,9 @@ __device__ __forceinline__ void lu_st_release(int* cnt, int v) {
 }
 // Bounded wait until *cnt >= need; `seen` caches the last value read, so a
 // counter already known to be far enough ahead is not read again.
-__device__ __forceinline__ bool lu_wait_ge(const int* cnt, int need, int& seen) {
+__device__ __forceinline__ bool lu_wait_ge(const int* cnt, int need, int& seen, uint32_t lim) {
   if (seen >= need) return true;
-  for (uint32_t it = 0; it < (1u << 22); ++it) {
+  for (uint32_t it = 0; it < lim; ++it) {
     seen = lu_ld_acquire(cnt);
     if (seen >= need) return true;
   }
@@ -420,7 +425,7 @@ __host__ __device__ __forceinline__ size_t lu_smem_bytes(int nwarp, int G, int m
 // through cp.async.bulk, G chunks per copy, double-buffered.
 // PRE: the preilu2d records and contributions.
 template <class R, bool FWD, int G, bool PRE = false>
-__device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem) {
+__device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem, uint32_t lim) {
   const ot2d_params& p = *S.P;
   const int nrow = lu_nrow(S.kd), ncol = lu_ncol(S.jd), nb = lu_nband(S.kd), nst = lu_nstep(S.jd);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -479,7 +484,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
   bool bad = false;
   int gfail = -1;
   for (int g = 0; g < ngrp; ++g) {
-    const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1));
+    const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1), lim);
     if (__any_sync(0xffffffffu, !ok || bad)) { gfail = g; break; }
     const int gs = gsize(g);
     const R* gring = ring + (size_t)(g & 1) * G * CH;
@@ -507,7 +512,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
           if (!has_prev || (!FWD && r == nrow - 1)) {
 #pragma unroll
             for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
-          } else if (lu_wait_ge(&prog[wprev], tl + 32, seen_prev)) {
+          } else if (lu_wait_ge(&prog[wprev], tl + 32, seen_prev, lim)) {
             // produced by band wprev at its step tl + 31
             const R* x = xin + ((tl + 31) & (LU_XB - 1)) * 4;
 #pragma unroll
@@ -545,7 +550,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
       // publish this band's progress
       if (l == lout) {
         if (act && has_next) {
-          if (lu_wait_ge(&prog[wnext], tl - LU_XB + 32, seen_next)) {
+          if (lu_wait_ge(&prog[wnext], tl - LU_XB + 32, seen_next, lim)) {
             R* x = xout + (tl & (LU_XB - 1)) * 4;
 #pragma unroll
             for (int n = 0; n < 4; ++n) x[n] = bout[n];

@@ -378,11 +378,11 @@ __global__ void __launch_bounds__(128) k_lu_edges_ring(const Slice<R>* __restric
 }
 
 template <class R, bool FWD, int G, bool PRE>
-__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int only_lu) {
+__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int only_lu, uint32_t poll_limit) {
   extern __shared__ __align__(128) unsigned char lu_smem[];
   if (only_lu && sl[blockIdx.x].P->ilhs != 1) return;
   if ((sl[blockIdx.x].k_mp2 >= (R)0) != PRE) return;
-  lu_sweep_slice<R, FWD, G, PRE>(sl[blockIdx.x], blockDim.x >> 5, lu_smem);
+  lu_sweep_slice<R, FWD, G, PRE>(sl[blockIdx.x], blockDim.x >> 5, lu_smem, poll_limit);
 }
 
 template <class R>
@@ -606,6 +606,9 @@ __global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__
   if (!inside) return;
   const ot2d_params& p = *S.P;
   if (j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) return;
+  // a sweep of this slice gave up (status bit 4): its correction is
+  // incomplete, so the state is left as it is until the slice is retired
+  if (S.ist && (__ldcg(&S.ist[2]) & 4)) return;
   const int64_t o = at(S.jd, j, k);
   int ibi = S.iblank[o];
   double m = (double)(ibi > 0 ? ibi : 0);

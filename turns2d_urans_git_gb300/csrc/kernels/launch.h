@@ -1,7 +1,9 @@
 // launch.h -- host-side launchers of the batched kernels.  Each launcher
 // covers every slice of a batch with one kernel launch on `st`.
 #pragma once
+#include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <cuda_runtime.h>
 
 namespace ot2d {
@@ -21,6 +23,40 @@ constexpr int RT_TJ = 16, RT_TK = 16;
 constexpr int SST_NSCRATCH = 27;
 // scratch arrays per slice of the ADI operator (k_adi.cuh: ADIw)
 constexpr int ADI_NSCRATCH = 25;
+
+// One-time set-up of a launch site per device (kernel attributes such as
+// the dynamic shared-memory limit, which CUDA keeps per device): run(f)
+// calls f once for the calling thread's current device and remembers its
+// success; concurrent callers on one device wait for the first.  One process
+// may drive several GPUs, so a single process-wide flag would leave the
+// other devices without the attribute.
+struct DeviceOnce {
+  static constexpr int MAXDEV = 64;
+  std::atomic<bool> done[MAXDEV] = {};
+  int value[MAXDEV] = {};   // a per-device value the set-up may record (a stream priority)
+  std::mutex mu;
+  template <class F>
+  cudaError_t run(F&& f, int* val = nullptr) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAXDEV) return cudaErrorInvalidDevice;
+    if (!done[dev].load(std::memory_order_acquire)) {
+      std::lock_guard<std::mutex> g(mu);
+      if (!done[dev].load(std::memory_order_relaxed)) {
+        int v = 0;
+        if ((e = f(v)) != cudaSuccess) return e;
+        value[dev] = v;
+        done[dev].store(true, std::memory_order_release);
+      }
+    }
+    if (val) *val = value[dev];
+    return cudaSuccess;
+  }
+};
+
+// Largest dynamic shared memory a CTA may opt in to on sm_103a (227 KB).
+constexpr int SMEM_OPTIN_MAX = 227 * 1024;
 
 struct Batch {
   int nslice = 0;          // slices in the batch
@@ -42,6 +78,7 @@ struct Batch {
   const int32_t* d_tfirst = nullptr;  // [nslice+1] first residual tile of each slice
   int tile_blocks = 0;                // residual tiles over the batch
   NormPart* d_part = nullptr;         // [max(cell_blocks, tile_blocks)] norm partials
+  uint32_t poll_limit = 1u << 22;     // polls of a LU-SGS sweep wait before it gives up
 };
 
 // One full iteration of step.f for every slice of the batch:

@@ -38,14 +38,14 @@ cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStr
 template <class R>
 cudaError_t launch_resid_both(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st) {
   constexpr size_t smem = rt_smem_bytes<R>();
-  static bool attr_set = false;
-  if (!attr_set) {
+  static DeviceOnce once;
+  cudaError_t ae = once.run([&](int&) {
     cudaError_t e = cudaFuncSetAttribute(k_resid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_resid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+    return e;
+  });
+  if (ae != cudaSuccess) return ae;
   k_resid<R, false><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
   if (b.precon) k_resid<R, true><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
   return cudaGetLastError();
@@ -91,12 +91,11 @@ template <class R, bool PRE>
 cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
   // one staged chunk per warp (f32 28 / 36 KB, f64 53 / 68 KB per block)
   constexpr size_t prep_smem = (size_t)LU_PREP_CH * lu_prep_stride<R, PRE>() * sizeof(R);
-  static bool prep_attr = false;
-  if (!prep_attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_lu_prep<R, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
-    if (e != cudaSuccess) return e;
-    prep_attr = true;
-  }
+  static DeviceOnce once;
+  cudaError_t ae = once.run([&](int&) {
+    return cudaFuncSetAttribute(k_lu_prep<R, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
+  });
+  if (ae != cudaSuccess) return ae;
   k_lu_prep<R, PRE><<<b.lu_blocks, CELL_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
   if constexpr (sizeof(R) == sizeof(double)) {
     // every cell: the FP64 path also round-trips q (lhs.f:524-531, :805-811)
@@ -124,21 +123,25 @@ cudaError_t launch_lusgs_sweeps_t(const Slice<R>* d_sl, const Batch& b, cudaStre
   int G = 8;
   while (G > 1 && lu_smem_bytes<R, PRE>(nw, G, maxcol) > 200 * 1024) G >>= 1;
   const size_t smem = lu_smem_bytes<R, PRE>(nw, G, maxcol);
-  static bool attr_set = false;
-  static int prio = 0;
-  if (!attr_set) {
-    const void* ks[] = {(const void*)k_lu_sweep<R, true, 8, PRE>, (const void*)k_lu_sweep<R, false, 8, PRE>,
-                        (const void*)k_lu_sweep<R, true, 4, PRE>, (const void*)k_lu_sweep<R, false, 4, PRE>,
-                        (const void*)k_lu_sweep<R, true, 2, PRE>, (const void*)k_lu_sweep<R, false, 2, PRE>,
-                        (const void*)k_lu_sweep<R, true, 1, PRE>, (const void*)k_lu_sweep<R, false, 1, PRE>};
-    for (const void* k : ks) {
-      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-      if (e != cudaSuccess) return e;
-    }
-    int lo = 0, hi = 0;
-    if (cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess) prio = hi;
-    attr_set = true;
-  }
+  if (32 * nw > 1024 || smem > (size_t)SMEM_OPTIN_MAX) return cudaErrorInvalidConfiguration;
+  static DeviceOnce once;
+  int prio = 0;
+  cudaError_t ae = once.run(
+      [&](int& hi_prio) {
+        const void* ks[] = {(const void*)k_lu_sweep<R, true, 8, PRE>, (const void*)k_lu_sweep<R, false, 8, PRE>,
+                            (const void*)k_lu_sweep<R, true, 4, PRE>, (const void*)k_lu_sweep<R, false, 4, PRE>,
+                            (const void*)k_lu_sweep<R, true, 2, PRE>, (const void*)k_lu_sweep<R, false, 2, PRE>,
+                            (const void*)k_lu_sweep<R, true, 1, PRE>, (const void*)k_lu_sweep<R, false, 1, PRE>};
+        for (const void* k : ks) {
+          cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_OPTIN_MAX);
+          if (e != cudaSuccess) return e;
+        }
+        int lo = 0, hi = 0;
+        if (cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess) hi_prio = hi;
+        return cudaSuccess;
+      },
+      &prio);
+  if (ae != cudaSuccess) return ae;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributePriority;
   at[0].val.priority = prio;
@@ -150,9 +153,9 @@ cudaError_t launch_lusgs_sweeps_t(const Slice<R>* d_sl, const Batch& b, cudaStre
   cfg.attrs = at;
   cfg.numAttrs = 1;
   auto run = [&](auto fwd, auto bwd) -> cudaError_t {
-    cudaError_t e = cudaLaunchKernelEx(&cfg, fwd, d_sl, only_lu);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, fwd, d_sl, only_lu, b.poll_limit);
     if (e != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, bwd, d_sl, only_lu);
+    return cudaLaunchKernelEx(&cfg, bwd, d_sl, only_lu, b.poll_limit);
   };
   cudaError_t e;
   switch (G) {
@@ -182,12 +185,11 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 0);
   k_sa_rhs<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   constexpr size_t lj_smem = sizeof(R) * LJ_SMEM;
-  static bool lj_attr = false;
-  if (!lj_attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_sa_lsolvej<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lj_smem);
-    if (e != cudaSuccess) return e;
-    lj_attr = true;
-  }
+  static DeviceOnce once;
+  cudaError_t ae = once.run([&](int&) {
+    return cudaFuncSetAttribute(k_sa_lsolvej<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lj_smem);
+  });
+  if (ae != cudaSuccess) return ae;
   k_sa_lsolvej<R><<<b.jgroups, 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sa_lsolve<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice, 1);
   k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 1);
@@ -202,12 +204,11 @@ cudaError_t launch_sst(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_sst_turm<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   k_sst_rhs<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   constexpr size_t lj_smem = sizeof(R) * LJ_SMEM;
-  static bool lj_attr = false;
-  if (!lj_attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_sst_lsolvej<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lj_smem);
-    if (e != cudaSuccess) return e;
-    lj_attr = true;
-  }
+  static DeviceOnce once;
+  cudaError_t ae = once.run([&](int&) {
+    return cudaFuncSetAttribute(k_sst_lsolvej<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lj_smem);
+  });
+  if (ae != cudaSuccess) return ae;
   k_sst_lsolvej<R><<<dim3(b.jgroups, 2), 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sst_lsolvek<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice);
   k_sst_bc<R><<<b.nslice, 256, 0, st>>>(d_sl, 1);
@@ -245,6 +246,12 @@ template <class R>
 cudaError_t launch_forces(const Slice<R>* d_sl, const Batch& b, const double* const* d_xv, const double* const* d_yv,
                           double* d_out, cudaStream_t st) {
   size_t smem = sizeof(double) * 3 * (size_t)b.max_wall;
+  if (smem > (size_t)SMEM_OPTIN_MAX) return cudaErrorInvalidConfiguration;
+  static DeviceOnce once;
+  cudaError_t ae = once.run([&](int&) {
+    return cudaFuncSetAttribute(k_forces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_OPTIN_MAX);
+  });
+  if (ae != cudaSuccess) return ae;
   k_forces<R><<<b.nslice, 128, smem, st>>>(d_sl, d_xv, d_yv, d_out);
   return cudaGetLastError();
 }
