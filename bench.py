@@ -112,7 +112,23 @@ def bench_config(batch, world):
     return {"workload": WORKLOAD, "batch_per_gpu": batch, "interior_cells": (JMAX - 1) * (KMAX - 1),
             "parallelism": "replicas x%d" % world,
             "l2": "inputs larger than L2: %d requests x %d cells, ~25 MB of state each (L2 129 MB)"
-                  % (batch, (JMAX - 1) * (KMAX - 1))}
+                  % (batch, (JMAX - 1) * (KMAX - 1)),
+            "launch_choices": "GPU arm: autotuned per mesh-size class (the line's `tuning`)"}
+
+
+def autotune(device, classes_fp32, classes_fp64):
+    """Launch choices of the GPU arm from the autotuner (cached per GPU,
+    precision and size class; searched on a miss)."""
+    import torch
+    from turns2d_urans_git_gb300 import tune
+    from turns2d_urans_git_gb300.abi import OT2D_FP32_MIXED, OT2D_FP64
+    gpu = torch.cuda.get_device_name(device)
+    t0 = time.perf_counter()
+    c32, _ = tune.tune(tune.gpu_measure_for_class(OT2D_FP32_MIXED, device=device), classes_fp32, gpu,
+                       OT2D_FP32_MIXED)
+    c64, _ = tune.tune(tune.gpu_measure_for_class(OT2D_FP64, batch=4, iters=3, device=device), classes_fp64, gpu,
+                       OT2D_FP64)
+    return c32, c64, time.perf_counter() - t0
 
 
 class ClockSampler:
@@ -204,7 +220,7 @@ def cpu_reference(cases, target_s=12.0, max_threads=None):
     return value, nthr, sample
 
 
-def serve_stream(precision, reqs, arrivals, max_iters, check_every, device, cap_s, budget_mb=0):
+def serve_stream(precision, reqs, arrivals, max_iters, check_every, device, cap_s, budget_mb=0, choices=None):
     """Continuous-batching service of a request stream: each request is
     submitted at the first status check after its arrival time (admitted at
     once when it fits the memory budget, queued otherwise) and retired when
@@ -215,6 +231,9 @@ def serve_stream(precision, reqs, arrivals, max_iters, check_every, device, cap_
     from turns2d_urans_git_gb300 import api
     from turns2d_urans_git_gb300.abi import OT2D_FP32_MIXED, OT2D_OPT_BUDGET_MB
     sv = api.Solver(precision, device=device, check_every=check_every)
+    if choices:
+        from turns2d_urans_git_gb300 import tune
+        tune.apply(sv, choices)
     if precision == OT2D_FP32_MIXED:
         sv.set_mixed_rule()
     if budget_mb:
@@ -291,7 +310,7 @@ def serve_requests(n, seed=7):
     return out
 
 
-def serving_section(args, device):
+def serving_section(args, device, choices=None):
     """FP32-mixed vs FP64 on the same seeded Poisson request stream:
     converged solves/s, p50/p99 time from submission to a converged
     solution, and the force differences of the requests both converged."""
@@ -303,7 +322,7 @@ def serving_section(args, device):
     res, forces = {}, {}
     for name, prec in (("fp32_mixed", OT2D_FP32_MIXED), ("fp64", OT2D_FP64)):
         out, t_end, maxq = serve_stream(prec, reqs, arrivals, args.serve_max_iters, 25, device, args.serve_seconds,
-                                        args.serve_budget_mb)
+                                        args.serve_budget_mb, (choices or {}).get(prec))
         conv = [(i, r) for (i, ta, r) in out if r.converged and r.status == 0]
         lat = [r.t_done - r.t_submit for (i, r) in conv]
         ts = sum(1 for (i, r) in conv if reqs[i][0][1].nspec > 1)
@@ -442,8 +461,13 @@ def run_ours(args):
     except (OSError, ValueError):
         pass
 
+    from turns2d_urans_git_gb300 import tune
+    c32, c64, tune_s = autotune(local, tune.SIZE_CLASSES, ((JMAX, KMAX),))
+    choices = {OT2D_FP32_MIXED: c32, OT2D_FP64: c64}
+
     def make(precision):
         sv = api.Solver(precision, device=local, check_every=10 ** 8)
+        tune.apply(sv, choices[precision])
         ids = [sv.add(prm, xv, yv, orders=0.0, max_iters=10 ** 8) for (_, prm, xv, yv) in cases]
         return sv, ids
 
@@ -489,7 +513,7 @@ def run_ours(args):
     # ---- served request stream (rank 0 only): converged solves/s, p50/p99
     serve = None
     if rank == 0 and not args.skip_serve:
-        serve = serving_section(args, local)
+        serve = serving_section(args, local, choices)
     unsteady = time_accurate_section(local) if rank == 0 and not args.skip_serve else None
     # ---- CPU baseline (rank 0, N=1 only): the oracle on the host cores
     cpu = None
@@ -506,6 +530,8 @@ def run_ours(args):
                 "data": "synthetic (seeded algebraic NACA0012 C-meshes, freestream start)",
                 "config": bench_config(B, world),
                 "precision": "fp32-mixed",
+                "tuning": {"fp32_mixed": tune.describe(c32), "fp64": tune.describe(c64),
+                           "search_s": tune_s, "cache": tune.default_cache_path()},
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes},
                 "fp64_plain": fp64,
                 "gpu_launches": launches_per_step * args.steps,
@@ -575,7 +601,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--serve-requests", type=int, default=64)
-    ap.add_argument("--serve-rate", type=float, default=2.0)
+    ap.add_argument("--serve-rate", type=float, default=16.0)
     ap.add_argument("--serve-max-iters", type=int, default=30000)
     ap.add_argument("--serve-seconds", type=float, default=75.0)
     ap.add_argument("--serve-budget-mb", type=int, default=0)

@@ -271,6 +271,11 @@ typedef struct ot2d_result {
 #define OT2D_OPT_BUDGET_MB     6  /* device memory the live instances may hold, MiB
                                      (default 0: 90 % of the memory free when the solver
                                      was created) */
+#define OT2D_OPT_LU_LAG        7  /* LU-SGS schedule: steps each 32-row band trails the
+                                     band it depends on beyond the minimum (default 0) */
+#define OT2D_OPT_LU_GROUP      8  /* LU-SGS records streamed per bulk copy: 1, 2, 4 or 8
+                                     (default 0: the largest the shared memory allows) */
+#define OT2D_OPT_RT_SHAPE      9  /* residual tile: 0 16x16 (default), 1 32x8, 2 8x32 cells */
 #define OT2D_OPT_POLL_LIMIT    5  /* polls a LU-SGS sweep wait makes before it gives up
                                      (default 4194304).  An instance whose wait gave up
                                      keeps its state and retires with OT2D_ERR_TIMEOUT;
@@ -287,6 +292,31 @@ int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value);
  * FP32-mixed path, whose f32 residual has a floor a few decades below its
  * peak and cannot show a 8-10 decade drop. */
 int ot2d_solver_set_force_tol(ot2d_solver* s, double dcl, double dcd);
+/* Launch choices for batches of one mesh-size class, as an autotuner
+ * measured them (turns2d_urans_git_gb300/tune.py).  When a batch is built,
+ * the first entry whose kd_max / jd_max bound the batch's largest mesh (the
+ * one with most cells) sets the residual tile shape, the LU-SGS copy group
+ * and the LU-SGS band lag; without a matching entry the OT2D_OPT_* values
+ * apply.  The choices change the launch geometry and schedule only: every
+ * variant gives the same results bit for bit. */
+typedef struct ot2d_tuning {
+  int32_t kd_max, jd_max;   /* class bound: kd <= kd_max and jd <= jd_max      */
+  int32_t rt_shape;         /* 0 16x16, 1 32x8, 2 8x32                          */
+  int32_t lu_group;         /* 0 (largest that fits), 1, 2, 4, 8                */
+  int32_t lu_lag;           /* 0..64                                            */
+  int32_t reserved;
+} ot2d_tuning;
+/* replace the tuning table (n entries, copied; n = 0 clears it) */
+int ot2d_solver_set_tuning(ot2d_solver* s, const ot2d_tuning* t, int32_t n);
+
+/* Append one JSON line per retired request to the file at path (id,
+ * status, convergence, iterations, precision, mesh and flow, first and last
+ * L2 norm, CL / CD / CM, submission / admission / retirement times); NULL
+ * stops logging.  The solver also marks admissions and retirements and
+ * brackets iterations and status checks with NVTX ranges, which cost
+ * nothing unless a profiler is attached. */
+int ot2d_solver_set_log(ot2d_solver* s, const char* path);
+
 /* read the device status table now and retire finished instances */
 int ot2d_solver_sync(ot2d_solver* s);
 /* the CUDA stream (cudaStream_t) the solver launches on */

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("precision", [OT2D_FP64, OT2D_FP32_MIXED])
-def test_footprint_admission_queues_and_matches_solo(precision):
+def test_footprint_admission_queues_and_matches_solo(precision, tmp_path):
     case = api.config_c2(jmax=129, kmax=33, fsmach=0.4, alfa=2.0, rey=2e6, ds_wall=1e-4)
     _, prm, xv, yv = case
     nbytes = api.instance_bytes(prm, precision)
@@ -32,6 +32,8 @@ def test_footprint_admission_queues_and_matches_solo(precision):
 
     sv = api.Solver(precision, check_every=10, keep_q=True)
     sv.set_option(OT2D_OPT_BUDGET_MB, mib)
+    log = str(tmp_path / "requests.jsonl")
+    sv.set_log(log)
     ids = [sv.add(prm, xv, yv, orders=0.0, max_iters=nsteps) for _ in range(5)]
     assert sv.queued() == 3
     assert sv.live() == 5
@@ -57,3 +59,11 @@ def test_footprint_admission_queues_and_matches_solo(precision):
         assert np.array_equal(sv.get_q(i, prm), q_solo)
         assert r.cl == r_solo.cl and r.cd == r_solo.cd
     sv.close()
+    # the per-request log: one JSON line per retired request
+    import json
+    recs = [json.loads(line) for line in open(log)]
+    assert sorted(x["id"] for x in recs) == sorted(ids)
+    for x in recs:
+        r = rs[ids.index(x["id"])]
+        assert x["status"] == 0 and x["iterations"] == nsteps and x["cl"] == r.cl
+        assert x["t_submit"] <= x["t_admit"] <= x["t_done"] and (x["jmax"], x["kmax"]) == (prm.jmax, prm.kmax)

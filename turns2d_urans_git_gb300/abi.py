@@ -31,6 +31,9 @@ OT2D_OPT_FORCE_EVERY = 3
 OT2D_OPT_FORCE_DECADES = 4
 OT2D_OPT_POLL_LIMIT = 5
 OT2D_OPT_BUDGET_MB = 6
+OT2D_OPT_LU_LAG = 7
+OT2D_OPT_LU_GROUP = 8
+OT2D_OPT_RT_SHAPE = 9
 
 _I = C.c_int32
 _D = C.c_double
@@ -70,6 +73,12 @@ class Inputs(C.Structure):
         ("nbc", _I), ("pad0", _I),
         ("ibtyp", _I * MAXBC), ("ibdir", _I * MAXBC), ("jbcs", _I * MAXBC), ("jbce", _I * MAXBC),
         ("kbcs", _I * MAXBC), ("kbce", _I * MAXBC)]
+
+
+class Tuning(C.Structure):
+    """ot2d_tuning: launch choices for batches of one mesh-size class."""
+    _fields_ = [("kd_max", _I), ("jd_max", _I), ("rt_shape", _I), ("lu_group", _I), ("lu_lag", _I),
+                ("reserved", _I)]
 
 
 class Result(C.Structure):

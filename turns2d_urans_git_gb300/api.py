@@ -305,6 +305,14 @@ class Solver:
             raise RuntimeError("ot2d_solver_add_state failed (%d)" % -rc)
         return rc
 
+    def set_log(self, path):
+        """Append one JSON line per retired request to `path` (None stops)."""
+        f = lib().ot2d_solver_set_log
+        f.argtypes = [C.c_void_p, C.c_char_p]
+        rc = f(self._h, None if path is None else os.fsencode(path))
+        if rc != 0:
+            raise RuntimeError("ot2d_solver_set_log failed (%d)" % rc)
+
     def set_option(self, key, value):
         rc = lib().ot2d_solver_set_option(self._h, int(key), int(value))
         if rc != 0:

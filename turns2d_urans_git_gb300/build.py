@@ -31,6 +31,14 @@ UNITS = [
     # (rcp / rsqrt based, <= 2 ulp) and flush-to-zero; its accuracy is stated
     # against the FP64 oracle, not bitwise
     ("kernels/kernels_fp32.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
+    # the fused residual, one unit per (precision, tile shape) so that its
+    # variants compile in parallel
+    ("kernels/resid_f32_16x16.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
+    ("kernels/resid_f32_32x8.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
+    ("kernels/resid_f32_8x32.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
+    ("kernels/resid_f64_16x16.cu", ["-fmad=false"]),
+    ("kernels/resid_f64_32x8.cu", ["-fmad=false"]),
+    ("kernels/resid_f64_8x32.cu", ["-fmad=false"]),
     ("host/runtime.cu", ["-fmad=false"]),
     ("host/solver.cu", ["-fmad=false"]),
     ("host/dropin.cu", ["-fmad=false"]),
@@ -59,7 +67,7 @@ def _compile(src, extra):
 def build(verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     units = [(s, e) for s, e in UNITS if os.path.exists(os.path.join(CSRC, s))]
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda u: _compile(*u), units))
     cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", OUT] + objs + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -415,11 +415,14 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   // record blocks, 32-line groups, residual tiles
   std::vector<int32_t> idx(6 * (n + 1));
   int cells = 0, jl = 0, kl = 0, lub = 0, grp = 0, tiles = 0, maxw = 1, maxwall = 1, maxkd = 1, moving = 0, precon = 0;
-  int maxnbc = 0;
+  int maxnbc = 0, limmask = 0;
+  int tj = 16, tk = 16;
+  rt_shape_dims(rt_shape, tj, tk);
   for (int i = 0; i < n; ++i) {
     if (sl[i].xc) moving = 1;
     if (sl[i].k_mp2 >= (R)0) precon = 1;
     maxnbc = std::max(maxnbc, (int)sl[i].nbc);
+    limmask |= sl[i].lim == 4 ? 4 : (sl[i].lim == 1 ? 2 : 1);
     idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl; idx[3 * (n + 1) + i] = lub;
     idx[4 * (n + 1) + i] = grp; idx[5 * (n + 1) + i] = tiles;
     const int jd = sl[i].jd, kd = sl[i].kd;
@@ -428,7 +431,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
     kl += jd - 2;   // j-lines solved along k
     lub += (lu_nband(kd) * lu_nstep(jd) * 32 + CELL_BS - 1) / CELL_BS;
     grp += lu_nband(kd);
-    tiles += ((jd - 2 + RT_TJ - 1) / RT_TJ) * ((kd - 2 + RT_TK - 1) / RT_TK);
+    tiles += ((jd - 2 + tj - 1) / tj) * ((kd - 2 + tk - 1) / tk);
     maxw = std::max(maxw, lu_nband(kd));
     maxwall = std::max(maxwall, jd);
     maxkd = std::max(maxkd, kd);
@@ -463,6 +466,8 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
   b.max_wall = maxwall;
   b.max_kd = maxkd;
   b.max_nbc = maxnbc;
+  b.lim_mask = limmask;
+  b.rt_shape = rt_shape;
   b.jlines = jl; b.klines = kl;
   b.lu_blocks = lub;
   b.jgroups = grp;

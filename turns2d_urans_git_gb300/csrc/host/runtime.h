@@ -83,6 +83,7 @@ struct DevBatch {
   int32_t* d_idx = nullptr;   // first / jfirst / kfirst, 3*(n+1)
   NormPart* d_part = nullptr;
   size_t cap_sl = 0, cap_part = 0;
+  int rt_shape = 0;   // residual tile shape the next build lays out (rt_shape_dims)
   int build(const std::vector<Slice<R>>& sl, cudaStream_t st);  // returns OT2D status
   void release();
 };

@@ -8,6 +8,7 @@
 // finished requests (forces in FP64, slot and memory freed).
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cmath>
 #include <cstddef>
 #include <cstring>
@@ -16,6 +17,8 @@
 #include <map>
 #include <string>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "geom.h"
 #include "io.h"
@@ -105,6 +108,10 @@ struct ot2d_solver {
   int force_every = 0;                   // iterations between force samples (0: every check)
   int force_decades = 1;                 // norm drop below the peak the force rule needs
   uint32_t poll_limit = 1u << 22;        // polls of a sweep wait (OT2D_OPT_POLL_LIMIT)
+  int lu_lag = 0, lu_group = 0;          // LU-SGS schedule (OT2D_OPT_LU_LAG, OT2D_OPT_LU_GROUP)
+  int rt_shape = 0;                      // residual tile shape (OT2D_OPT_RT_SHAPE)
+  std::vector<ot2d_tuning> tuning;       // per size class (ot2d_solver_set_tuning)
+  ot2d_tuning applied{};                 // the choice of the current batch
   int keep_q = 0;
   int since_check = 0;
   bool any_viscous = false;
@@ -115,6 +122,7 @@ struct ot2d_solver {
   DevBatch<float> f32;
   const double** d_xy = nullptr; size_t xy_cap = 0;
   int last_err = 0;
+  FILE* log = nullptr;                   // ot2d_solver_set_log: one JSON line per retired request
 };
 
 namespace {
@@ -174,9 +182,26 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   }
   s->dirty = false;
   if (sl.empty()) return OT2D_OK;
+  // launch choices: the tuning entry of the batch's largest mesh, else the options
+  ot2d_tuning ch{0, 0, s->rt_shape, s->lu_group, s->lu_lag, 0};
+  {
+    size_t best = 0;
+    int kd = 0, jd = 0;
+    for (int id : s->live) {
+      const ot2d_params& p = s->recs[id].d.P;
+      const size_t cells = (size_t)p.jd * p.kd * p.nspec;
+      if (cells > best) { best = cells; kd = p.kd; jd = p.jd; }
+    }
+    for (const ot2d_tuning& t : s->tuning)
+      if (kd <= t.kd_max && jd <= t.jd_max) { ch = t; break; }
+  }
+  s->applied = ch;
+  B.rt_shape = ch.rt_shape;
   int e = B.build(sl, s->st);
   if (e) return e;
   B.b.poll_limit = s->poll_limit;
+  B.b.lu_lag = ch.lu_lag;
+  B.b.lu_group = ch.lu_group;
   // The kernels branch on each slice's own params, so inviscid, laminar,
   // SA and SST requests can share one batch.
   Branch* br = nullptr;   // the turbulence branch's stream, created outside the capture
@@ -359,6 +384,11 @@ int admit(ot2d_solver* s, Pending& pd) {
     return OT2D_ERR_CUDA;
   }
   const int id = r.id;
+  {
+    char m[96];
+    std::snprintf(m, sizeof(m), "ot2d admit id=%d %dx%dx%d", id, (int)pd.p.jmax, (int)pd.p.kmax, (int)pd.p.nspec);
+    nvtxMarkA(m);
+  }
   s->used += r.d.bytes;
   auto prev = s->recs.find(id);
   if (prev != s->recs.end()) r.store_dir = prev->second.store_dir;   // set while it was queued
@@ -436,7 +466,31 @@ int submit(ot2d_solver* s, const ot2d_params* p, const double* xv, const double*
   return id;
 }
 
+// One JSON line per retired request (ot2d_solver_set_log).
+void log_retired(ot2d_solver* s, const Rec& r) {
+  if (!s->log) return;
+  const ot2d_params& p = r.d.P;
+  std::fprintf(s->log,
+               "{\"id\": %d, \"status\": %d, \"converged\": %d, \"iterations\": %d, \"precision\": \"%s\", "
+               "\"jmax\": %d, \"kmax\": %d, \"nspec\": %d, \"fsmach\": %.17g, \"alfa\": %.17g, \"orders\": %.17g, "
+               "\"rsum_first\": %.17g, \"rsum_last\": %.17g, \"cl\": %.17g, \"cd\": %.17g, \"cm\": %.17g, "
+               "\"t_submit\": %.6f, \"t_admit\": %.6f, \"t_done\": %.6f}\n",
+               r.id, r.res.status, r.res.converged, r.res.iterations, s->precision == OT2D_FP64 ? "fp64" : "fp32-mixed",
+               (int)p.jmax, (int)p.kmax, (int)p.nspec, p.fsmach, p.alfa, r.orders, r.res.rsum_first, r.res.rsum_last,
+               r.res.cl, r.res.cd, r.res.cm, r.res.t_submit, r.res.t_admit, r.res.t_done);
+  std::fflush(s->log);
+}
+
+int check_inner(ot2d_solver* s);
+
 int check(ot2d_solver* s) {
+  nvtxRangePushA("ot2d status check");
+  const int e = check_inner(s);
+  nvtxRangePop();
+  return e;
+}
+
+int check_inner(ot2d_solver* s) {
   s->since_check = 0;
   if (s->live.empty()) return OT2D_OK;
   cudaMemcpyAsync(s->h_red, s->d_red, sizeof(double) * RED_N * s->cap, cudaMemcpyDeviceToHost, s->st);
@@ -501,6 +555,12 @@ int check(ot2d_solver* s) {
   for (int id : done) {
     Rec& r = s->recs[id];
     r.res.t_done = t;
+    {
+      char m[80];
+      std::snprintf(m, sizeof(m), "ot2d retire id=%d status=%d converged=%d", id, r.res.status, r.res.converged);
+      nvtxMarkA(m);
+    }
+    log_retired(s, r);
     if (!r.store_dir.empty()) {
       const int se = store_rec(s, r, r.store_dir);
       if (se && !e) e = se;
@@ -556,6 +616,7 @@ void ot2d_solver_destroy(ot2d_solver* s) {
   if (s->h_ist) cudaFreeHost(s->h_ist);
   if (s->d_forces) cudaFree(s->d_forces);
   if (s->d_xy) cudaFree(s->d_xy);
+  if (s->log) std::fclose(s->log);
   cudaStreamDestroy(s->st);
   delete s;
 }
@@ -567,12 +628,39 @@ int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value) {
   if (key == OT2D_OPT_FORCE_EVERY && value >= 0) { s->force_every = value; return OT2D_OK; }
   if (key == OT2D_OPT_FORCE_DECADES && value >= 0) { s->force_decades = value; return OT2D_OK; }
   if (key == OT2D_OPT_BUDGET_MB && value >= 0) { s->budget_set = (size_t)value << 20; return OT2D_OK; }
+  if (key == OT2D_OPT_LU_LAG && value >= 0 && value <= 64) { s->lu_lag = value; s->dirty = true; return OT2D_OK; }
+  if (key == OT2D_OPT_RT_SHAPE && value >= 0 && value < RT_NSHAPE) { s->rt_shape = value; s->dirty = true; return OT2D_OK; }
+  if (key == OT2D_OPT_LU_GROUP && (value == 0 || value == 1 || value == 2 || value == 4 || value == 8)) {
+    s->lu_group = value;
+    s->dirty = true;
+    return OT2D_OK;
+  }
   if (key == OT2D_OPT_POLL_LIMIT && value >= 1) {
     s->poll_limit = (uint32_t)value;
     s->dirty = true;   // the sweeps take the limit as a launch argument
     return OT2D_OK;
   }
   return OT2D_ERR_ARG;
+}
+
+int ot2d_solver_set_log(ot2d_solver* s, const char* path) {
+  if (!s) return OT2D_ERR_ARG;
+  if (s->log) { std::fclose(s->log); s->log = nullptr; }
+  if (!path) return OT2D_OK;
+  s->log = std::fopen(path, "a");
+  return s->log ? OT2D_OK : OT2D_ERR_IO;
+}
+
+int ot2d_solver_set_tuning(ot2d_solver* s, const ot2d_tuning* t, int32_t n) {
+  if (!s || n < 0 || (n && !t)) return OT2D_ERR_ARG;
+  for (int i = 0; i < n; ++i) {
+    const ot2d_tuning& e = t[i];
+    const bool g = e.lu_group == 0 || e.lu_group == 1 || e.lu_group == 2 || e.lu_group == 4 || e.lu_group == 8;
+    if (e.rt_shape < 0 || e.rt_shape >= RT_NSHAPE || !g || e.lu_lag < 0 || e.lu_lag > 64) return OT2D_ERR_ARG;
+  }
+  s->tuning.assign(t, t + n);
+  s->dirty = true;
+  return OT2D_OK;
 }
 
 int ot2d_solver_set_force_tol(ot2d_solver* s, double dcl, double dcd) {
@@ -599,8 +687,10 @@ int ot2d_solver_iterate(ot2d_solver* s, int32_t iters) {
     long rem = chunk;
     for (int id : s->live) rem = std::min(rem, iter_cap(s->recs[id]) - s->recs[id].launched);
     chunk = (int)std::max(1L, rem);
+    nvtxRangePushA("ot2d iterations");
     for (int i = 0; i < chunk; ++i)
-      if (cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) return OT2D_ERR_CUDA;
+      if (cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) { nvtxRangePop(); return OT2D_ERR_CUDA; }
+    nvtxRangePop();
     bool capped = false;
     for (int id : s->live) {
       Rec& r = s->recs[id];

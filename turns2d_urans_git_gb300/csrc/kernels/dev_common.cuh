@@ -59,7 +59,15 @@ struct Slice {
   const double* motion;                   // per physical step: sin, cos of the pitch increment and of its negative
   int32_t nmotion;                        // physical steps in the table
   int32_t nbc;                            // &bcinp entries (params nbc)
+  int32_t lim;                            // reconstruction family: 0 central, 1 MUSCL, 4 WENO (rt_lim_class)
 };
+
+// Reconstruction family of a limiter switch, as rhsup dispatches it
+// (eulerrhs.f:85-97): ilim 4 -> weno, |ilim| 1 -> muscld_new, otherwise the
+// unlimited central slope of iflux.
+__host__ __device__ __forceinline__ int rt_lim_class(int ilim) {
+  return ilim == 4 ? 4 : ((ilim < 0 ? -ilim : ilim) == 1 ? 1 : 0);
+}
 
 // Fill the residual constants of a slice from its parameters (host side;
 // the same double expressions the kernels would evaluate).
@@ -80,6 +88,7 @@ inline void slice_consts(Slice<R>& S, const ot2d_params& p) {
   S.k_ggm1 = (R)p.ggm1;
   S.k_mp2 = p.iprecon ? (R)(p.Mp * p.Mp) : (R)-1;
   S.nbc = p.nbc;
+  S.lim = rt_lim_class(p.ilim);
   S.k_gamma = (R)p.gamma; S.k_rmue = (R)p.rmue; S.k_rey = (R)p.rey;
   S.k_eps2 = (R)(p.epse * 2.); S.k_epsv = (R)1. + S.k_eps2;
   S.k_mp = (R)p.Mp; S.k_rinf = (R)p.rinf; S.k_uinf = (R)p.uinf; S.k_vinf = (R)p.vinf;

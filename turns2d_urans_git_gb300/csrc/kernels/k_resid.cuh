@@ -1,7 +1,7 @@
 // k_resid.cuh -- the fused residual: rhsup (src/eulerrhs.f:2-280) +
 // visrhs (src/visrhs.f:2-287) + timespectralrhs (src/sources.f:2-27) + the
-// L2 / max norms of step.f:58-93, one CTA per tile of RT_TJ x RT_TK
-// interior cells.
+// L2 / max norms of step.f:58-93, one CTA per tile of TJ x TK interior
+// cells (16x16, 32x8 or 8x32: rt_shape_dims, chosen per batch).
 //
 // A tile stages its cells plus a 3-cell halo in shared memory once
 // (primitive variables, viscous cell factors, metrics), computes every
@@ -17,49 +17,58 @@
 
 namespace ot2d {
 
-constexpr int RT_H = 3;   // staged halo width (tile size RT_TJ x RT_TK: launch.h)
-constexpr int RT_RW = RT_TJ + 2 * RT_H, RT_RH = RT_TK + 2 * RT_H;   // staged region
-constexpr int RT_NR = RT_RW * RT_RH;
 constexpr int RT_BS = 256;
 // staged per-cell arrays
 enum { RS_RHO = 0, RS_U, RS_V, RS_P, RS_E, RS_VNU, RS_GKAP, RS_RJ, RS_UD, RS_VD, RS_ED, RS_XX, RS_XY, RS_YX, RS_YY, RS_N };
-// face arrays
-constexpr int RT_NF = 4 * RT_TK * (RT_TJ + 1);             // F: xi faces j0-1..j1, rows k0..k1
-constexpr int RT_NG = 4 * (RT_TK + 1) * RT_TJ;             // G: eta faces k0-1..k1, columns j0..j1
-constexpr int RT_VEH = RT_TK + 3, RT_VXW = RT_TJ + 3;
-constexpr int RT_NVE = 6 * RT_VEH * RT_TJ;                 // eta viscous, k0-2..k1+1
-constexpr int RT_NVX = 6 * RT_TK * RT_VXW;                 // xi viscous, j0-2..j1+1
+
+// Geometry of a TJ x TK tile (TJ * TK = RT_BS cells, one per thread in the
+// assembly): the staged region with its 3-cell halo and the face arrays.
+template <int TJ, int TK>
+struct RtGeo {
+  static_assert(TJ * TK == RT_BS, "one cell per thread");
+  static constexpr int H = 3;                             // staged halo width
+  static constexpr int RW = TJ + 2 * H, RH = TK + 2 * H;  // staged region
+  static constexpr int NR = RW * RH;
+  static constexpr int NF = 4 * TK * (TJ + 1);            // F: xi faces j0-1..j1, rows k0..k1
+  static constexpr int NG = 4 * (TK + 1) * TJ;            // G: eta faces k0-1..k1, columns j0..j1
+  static constexpr int VEH = TK + 3, VXW = TJ + 3;
+  static constexpr int NVE = 6 * VEH * TJ;                // eta viscous, k0-2..k1+1
+  static constexpr int NVX = 6 * TK * VXW;                // xi viscous, j0-2..j1+1
+};
 
 // |iblank| of the staged cells is kept as one byte (values above 255 are
 // clamped; the reference's blanking values are -1, 0 and 1).  The norm
 // partials of the tile reuse the staged region at the end (k_resid).
-template <class R>
+template <class R, int TJ, int TK>
 __host__ __device__ constexpr size_t rt_smem_bytes() {
-  return ((sizeof(R) * ((size_t)RS_N * RT_NR + RT_NF + RT_NG + RT_NVE + RT_NVX) + RT_NR + 15) / 16) * 16;
+  using G = RtGeo<TJ, TK>;
+  return ((sizeof(R) * ((size_t)RS_N * G::NR + G::NF + G::NG + G::NVE + G::NVX) + G::NR + 15) / 16) * 16;
 }
 
-template <class R>
+template <class R, int TJ, int TK>
 struct RtSmem {
-  R* c;          // [RS_N][RT_NR]
-  R *F, *G, *VE, *VX;
-  uint8_t* iba;  // [RT_NR]
+  using G = RtGeo<TJ, TK>;
+  static constexpr int RW = G::RW, NR = G::NR;
+  R* c;          // [RS_N][NR]
+  R *F, *G_, *VE, *VX;
+  uint8_t* iba;  // [NR]
   __device__ RtSmem(unsigned char* base) {
     c = (R*)base;
-    F = c + (size_t)RS_N * RT_NR;
-    G = F + RT_NF;
-    VE = G + RT_NG;
-    VX = VE + RT_NVE;
-    iba = (uint8_t*)(VX + RT_NVX);
+    F = c + (size_t)RS_N * G::NR;
+    G_ = F + G::NF;
+    VE = G_ + G::NG;
+    VX = VE + G::NVE;
+    iba = (uint8_t*)(VX + G::NVX);
   }
-  __device__ __forceinline__ R& at(int a, int r) const { return c[(size_t)a * RT_NR + r]; }
+  __device__ __forceinline__ R& at(int a, int r) const { return c[(size_t)a * G::NR + r]; }
 };
 
 // Stage A: cell (j,k) of the staged region -> primitive f of rhsup
 // (eulerrhs.f:55-61, :71-79), viscous cell factors of visrhs
 // (visrhs.f:48-60), the q2/q1-style divided velocities of its cross terms
 // (visrhs.f:77-89), metrics and |iblank|.
-template <class R>
-__device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_params& p, const RtSmem<R>& sm, int r,
+template <class R, class SM>
+__device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_params& p, const SM& sm, int r,
                                               int j, int k, bool visc) {
   const int64_t o = at(S.jd, j, k), qs = S.qs;
   const R q1 = S.q[o], q2 = S.q[qs + o], q3 = S.q[2 * qs + o], q4 = S.q[3 * qs + o], J = S.q[(p.nq - 1) * qs + o];
@@ -95,9 +104,9 @@ __device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_para
 // A grid line read from the staged region: line position c sits at region
 // index o0 + c*stride; positions outside [lo, hi] were not staged (and are
 // never read by the reconstruction that uses them).
-template <class R>
+template <class R, class SM>
 struct RtLine {
-  const RtSmem<R>* sm; int o0, stride, lo, hi; R gm1;
+  const SM* sm; int o0, stride, lo, hi; R gm1;
   __device__ __forceinline__ void f4(int c, R* out) const {
     if (c < lo || c > hi) { out[0] = out[1] = out[2] = out[3] = (R)0; return; }
     const int r = o0 + c * stride;
@@ -108,12 +117,12 @@ struct RtLine {
 
 // eta-direction viscous quantities at column j, index k (visrhs.f:46-131):
 // face k+1/2 (f2, f3, f4) and cell k (f2v, f3v, f4v); r = region index of
-// (j,k); the cell above is r + RT_RW, the side neighbours r -+ 1.
-template <class R>
-__device__ __forceinline__ void rt_visc_eta(const RtSmem<R>& sm, int r, R gkpr, R dre, R* out) {
+// (j,k); the cell above is r + SM::RW, the side neighbours r -+ 1.
+template <class R, class SM>
+__device__ __forceinline__ void rt_visc_eta(const SM& sm, int r, R gkpr, R dre, R* out) {
   R bv[2][4], uu[2], vv[2], ee[2];
   for (int m = 0; m < 2; ++m) {
-    const int rr = r + m * RT_RW;
+    const int rr = r + m * SM::RW;
     const R rj = sm.at(RS_RJ, rr), vnu = sm.at(RS_VNU, rr), gkap = sm.at(RS_GKAP, rr);
     uu[m] = sm.at(RS_U, rr); vv[m] = sm.at(RS_V, rr); ee[m] = sm.at(RS_E, rr);
     const R yx = sm.at(RS_YX, rr), yy = sm.at(RS_YY, rr);
@@ -170,9 +179,9 @@ __device__ __forceinline__ void rt_visc_eta(const RtSmem<R>& sm, int r, R gkpr, 
 
 // xi-direction viscous quantities at row k, index j (visrhs.f:166-251):
 // face j+1/2 and cell j; the cell to the right is r + 1, the neighbours
-// below / above r -+ RT_RW.
-template <class R>
-__device__ __forceinline__ void rt_visc_xi(const RtSmem<R>& sm, int r, R gkpr, R dre, R* out) {
+// below / above r -+ SM::RW.
+template <class R, class SM>
+__device__ __forceinline__ void rt_visc_xi(const SM& sm, int r, R gkpr, R dre, R* out) {
   R av[2][4], uu[2], vv[2], ee[2];
   for (int m = 0; m < 2; ++m) {
     const int rr = r + m;
@@ -185,7 +194,7 @@ __device__ __forceinline__ void rt_visc_xi(const RtSmem<R>& sm, int r, R gkpr, R
     av[m][3] = (xx * xy / (R)3. * rj) * vnu * dre;
     av[m][2] = a4 * gkpr * gkap * dre;
   }
-  const int rm = r - RT_RW, rp = r + RT_RW;
+  const int rm = r - SM::RW, rp = r + SM::RW;
   const R vnu = sm.at(RS_VNU, r), gkap = sm.at(RS_GKAP, r);
   const R rkm = sm.at(RS_RJ, rm), rkp = sm.at(RS_RJ, rp);
   const R xxm = sm.at(RS_XX, rm), xym = sm.at(RS_XY, rm), yxm = sm.at(RS_YX, rm), yym = sm.at(RS_YY, rm);
@@ -260,81 +269,84 @@ __device__ __forceinline__ void rhslom_cell(const Slice<R>& S, const ot2d_params
 // the thread's norm partial.  PRE: the slice runs with Turkel's low-Mach
 // preconditioning -- roetrklflx fluxes, and in the full residual (AS_NORM)
 // rhslom applied to each cell after its norm terms (step.f:121-123).
-template <class R, bool PRE>
-__device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int flags, NormPartR<R>& np) {
+template <class R, bool PRE, int LIM, int TJ, int TK>
+__device__ void resid_tile(const Slice<R>& S, const RtSmem<R, TJ, TK>& sm, int tile, int flags,
+                           NormPartR<R>& np) {
+  using G = RtGeo<TJ, TK>;
+  using SM = RtSmem<R, TJ, TK>;
   const ot2d_params& p = *S.P;
   const int jd = S.jd, kd = S.kd, t = threadIdx.x;
-  const int ntj = (p.jend - p.jbeg + RT_TJ) / RT_TJ;
-  const int j0 = p.jbeg + (tile % ntj) * RT_TJ, k0 = p.kbeg + (tile / ntj) * RT_TK;
-  const int j1 = min(j0 + RT_TJ - 1, p.jend), k1 = min(k0 + RT_TK - 1, p.kend);
-  const int jr = j0 - RT_H, kr = k0 - RT_H;
+  const int ntj = (p.jend - p.jbeg + TJ) / TJ;
+  const int j0 = p.jbeg + (tile % ntj) * TJ, k0 = p.kbeg + (tile / ntj) * TK;
+  const int j1 = min(j0 + TJ - 1, p.jend), k1 = min(k0 + TK - 1, p.kend);
+  const int jr = j0 - G::H, kr = k0 - G::H;
   const bool visc = (flags & AS_VISC) && !p.invisc;
   const bool inv = flags & AS_INV;
   const R gm1 = S.k_gm1;
   const Recon<R> rx{p.ilim, S.k_th, S.k_qt, S.k_epsl_x, S.k_mp2}, ry{p.ilim, S.k_th, S.k_qt, S.k_epsl_y, S.k_mp2};
   // A: stage the region
-  for (int r = t; r < RT_NR; r += RT_BS) {
-    const int j = jr + r % RT_RW, k = kr + r / RT_RW;
+  for (int r = t; r < G::NR; r += RT_BS) {
+    const int j = jr + r % G::RW, k = kr + r / G::RW;
     if (j >= 1 && j <= jd && k >= 1 && k <= kd) rt_stage_cell(S, p, sm, r, j, k, visc);
   }
   __syncthreads();
   // B-D: every face quantity of the tile, as one work list so that the
   // threads stay busy across the four kinds
-  const int nB = inv ? RT_TK * (RT_TJ + 1) : 0, nC = inv ? (RT_TK + 1) * RT_TJ : 0;
-  const int nD1 = visc ? RT_VEH * RT_TJ : 0, nD2 = visc ? RT_TK * RT_VXW : 0;
+  const int nB = inv ? TK * (TJ + 1) : 0, nC = inv ? (TK + 1) * TJ : 0;
+  const int nD1 = visc ? G::VEH * TJ : 0, nD2 = visc ? TK * G::VXW : 0;
   const int ntot = nB + nC + nD1 + nD2;
   const R gkpr = S.k_gkpr, dre = S.k_dre;
   for (int w = t; w < ntot; w += RT_BS) {
     if (w < nB) {
       // B: xi face j+1/2 of row k, j in j0-1..j1 (eulerrhs.f:69-167)
       const int f = w;
-      const int kk = f / (RT_TJ + 1), jf = f % (RT_TJ + 1);
+      const int kk = f / (TJ + 1), jf = f % (TJ + 1);
       const int j = j0 - 1 + jf, k = k0 + kk;
       if (j > j1 || k > k1) continue;
-      const RtLine<R> L{&sm, (k - kr) * RT_RW - jr, 1, max(1, jr), min(jd, jr + RT_RW - 1), gm1};
+      const RtLine<R, SM> L{&sm, (k - kr) * G::RW - jr, 1, max(1, jr), min(jd, jr + G::RW - 1), gm1};
       const int64_t o = at(jd, j, k);
       R fl[4];
-      face_flux_p<PRE>(L, rx, j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
+      face_flux_t<LIM, R, RtLine<R, SM>, PRE>(L, rx, j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) sm.F[v * (RT_TK * (RT_TJ + 1)) + f] = fl[v];
+      for (int v = 0; v < 4; ++v) sm.F[v * (TK * (TJ + 1)) + f] = fl[v];
     } else if (w < nB + nC) {
       // C: eta face k+1/2 of column j, k in k0-1..k1 (eulerrhs.f:170-268)
       const int f = w - nB;
-      const int kf = f / RT_TJ, jj = f % RT_TJ;
+      const int kf = f / TJ, jj = f % TJ;
       const int j = j0 + jj, k = k0 - 1 + kf;
       if (j > j1 || k > k1) continue;
-      const RtLine<R> L{&sm, (j - jr) - kr * RT_RW, RT_RW, max(1, kr), min(kd, kr + RT_RH - 1), gm1};
+      const RtLine<R, SM> L{&sm, (j - jr) - kr * G::RW, G::RW, max(1, kr), min(kd, kr + G::RH - 1), gm1};
       const int64_t o = at(jd, j, k);
       R fl[4];
-      face_flux_p<PRE>(L, ry, k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
+      face_flux_t<LIM, R, RtLine<R, SM>, PRE>(L, ry, k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) sm.G[v * ((RT_TK + 1) * RT_TJ) + f] = fl[v];
+      for (int v = 0; v < 4; ++v) sm.G_[v * ((TK + 1) * TJ) + f] = fl[v];
     } else if (w < nB + nC + nD1) {
       // D1: eta viscous terms at k0-2..k1+1 of columns j0..j1
       const int f = w - nB - nC;
-      const int kf = f / RT_TJ, jj = f % RT_TJ;
+      const int kf = f / TJ, jj = f % TJ;
       const int j = j0 + jj, k = k0 - 2 + kf;
       if (j > j1 || k < 1 || k > kd - 1 || k > k1 + 1) continue;
       R out[6];
-      rt_visc_eta(sm, (k - kr) * RT_RW + (j - jr), gkpr, dre, out);
+      rt_visc_eta(sm, (k - kr) * G::RW + (j - jr), gkpr, dre, out);
 #pragma unroll
-      for (int v = 0; v < 6; ++v) sm.VE[v * (RT_VEH * RT_TJ) + f] = out[v];
+      for (int v = 0; v < 6; ++v) sm.VE[v * (G::VEH * TJ) + f] = out[v];
     } else {
       // D2: xi viscous terms at j0-2..j1+1 of rows k0..k1
       const int f = w - nB - nC - nD1;
-      const int kk = f / RT_VXW, jf = f % RT_VXW;
+      const int kk = f / G::VXW, jf = f % G::VXW;
       const int j = j0 - 2 + jf, k = k0 + kk;
       if (k > k1 || j < 1 || j > jd - 1 || j > j1 + 1) continue;
       R out[6];
-      rt_visc_xi(sm, (k - kr) * RT_RW + (j - jr), gkpr, dre, out);
+      rt_visc_xi(sm, (k - kr) * G::RW + (j - jr), gkpr, dre, out);
 #pragma unroll
-      for (int v = 0; v < 6; ++v) sm.VX[v * (RT_TK * RT_VXW) + f] = out[v];
+      for (int v = 0; v < 6; ++v) sm.VX[v * (TK * G::VXW) + f] = out[v];
     }
   }
   __syncthreads();
   // E: per-cell assembly in the reference's order, then the time-spectral
   // term, the norm partial and the store
-  const int jj = t % RT_TJ, kk = t / RT_TJ;
+  const int jj = t % TJ, kk = t / TJ;
   const int j = j0 + jj, k = k0 + kk;
   const int nv = p.nv;
   const bool acc = flags & AS_ACC;
@@ -349,12 +361,12 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
         if (n < nv) s[n] = S.s[(int64_t)n * S.qs + o];
     }
     if (inv) {
-      const R* F = sm.F + kk * (RT_TJ + 1) + jj;
-      const R* G = sm.G + kk * RT_TJ + jj;
+      const R* F = sm.F + kk * (TJ + 1) + jj;
+      const R* G = sm.G_ + kk * TJ + jj;
 #pragma unroll
-      for (int v = 0; v < 4; ++v) s[v] = s[v] - (F[v * (RT_TK * (RT_TJ + 1)) + 1] - F[v * (RT_TK * (RT_TJ + 1))]);
+      for (int v = 0; v < 4; ++v) s[v] = s[v] - (F[v * (TK * (TJ + 1)) + 1] - F[v * (TK * (TJ + 1))]);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) s[v] = s[v] - (G[v * ((RT_TK + 1) * RT_TJ) + RT_TJ] - G[v * ((RT_TK + 1) * RT_TJ)]);
+      for (int v = 0; v < 4; ++v) s[v] = s[v] - (G[v * ((TK + 1) * TJ) + TJ] - G[v * ((TK + 1) * TJ)]);
     }
     if (S.qnewt && !p.timespectral) {
       // newton (time.f:195-206): the physical-time term, added between the
@@ -370,20 +382,20 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R>& sm, int tile, int
     }
     if (visc) {
       // VE row of cell k is kk+2; VX column of cell j is jj+2
-      const R* VE = sm.VE + (kk + 2) * RT_TJ + jj;
+      const R* VE = sm.VE + (kk + 2) * TJ + jj;
       for (int v = 0; v < 3; ++v) {
-        const R* a0 = VE + v * (RT_VEH * RT_TJ);
-        const R* b0 = VE + (v + 3) * (RT_VEH * RT_TJ);
-        const R a = a0[0] - a0[-RT_TJ];
+        const R* a0 = VE + v * (G::VEH * TJ);
+        const R* b0 = VE + (v + 3) * (G::VEH * TJ);
+        const R a = a0[0] - a0[-TJ];
         R b;
-        if (k == p.kend) b = (R)0.5 * (b0[-2 * RT_TJ] - (R)4. * b0[-RT_TJ] + (R)3 * b0[0]);
-        else b = (R)0.5 * (b0[RT_TJ] - b0[-RT_TJ]);
+        if (k == p.kend) b = (R)0.5 * (b0[-2 * TJ] - (R)4. * b0[-TJ] + (R)3 * b0[0]);
+        else b = (R)0.5 * (b0[TJ] - b0[-TJ]);
         s[v + 1] = s[v + 1] + a + b;
       }
-      const R* VX = sm.VX + kk * RT_VXW + jj + 2;
+      const R* VX = sm.VX + kk * G::VXW + jj + 2;
       for (int v = 0; v < 3; ++v) {
-        const R* a0 = VX + v * (RT_TK * RT_VXW);
-        const R* b0 = VX + (v + 3) * (RT_TK * RT_VXW);
+        const R* a0 = VX + v * (TK * G::VXW);
+        const R* b0 = VX + (v + 3) * (TK * G::VXW);
         const R a = a0[0] - a0[-1];
         R b;
         if (j == p.jend) b = (R)0.5 * (b0[-2] - (R)4. * b0[-1] + (R)3 * b0[0]);

@@ -214,21 +214,24 @@ __global__ void __launch_bounds__(CELL_BS) k_assemble(const Slice<R>* __restrict
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
-// Fused residual over tiles of RT_TJ x RT_TK interior cells: slice i owns
-// tiles [tfirst[i], tfirst[i+1]).  Dynamic shared memory: rt_smem_bytes<R>().
-// PRE selects the preconditioned slices (k_mp2 >= 0); a batch that holds
-// both kinds launches both instantiations, each returning on the other's
-// tiles (a whole block returns, so every tile is done exactly once).
-template <class R, bool PRE>
+// Fused residual over tiles of TJ x TK interior cells: slice i owns tiles
+// [tfirst[i], tfirst[i+1]) (the batch's tile table is built for the same
+// shape).  Dynamic shared memory: rt_smem_bytes<R, TJ, TK>().  PRE selects
+// the preconditioned slices (k_mp2 >= 0) and LIM the reconstruction family
+// (rt_lim_class); a batch launches one instantiation per kind it holds,
+// each returning on the other kinds' tiles (a whole block returns, so every
+// tile is done exactly once).  One family per kernel keeps the WENO windows
+// out of the MUSCL kernel's registers and code.
+template <class R, bool PRE, int LIM, int TJ, int TK>
 __global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 1) k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst,
                                                   int nslice, int flags, NormPart* __restrict__ part) {
   extern __shared__ __align__(16) unsigned char rt_raw[];
   const int si = find_slice(tfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];
-  if ((S.k_mp2 >= (R)0) != PRE) return;
-  RtSmem<R> sm(rt_raw);
+  if ((S.k_mp2 >= (R)0) != PRE || S.lim != LIM) return;
+  RtSmem<R, TJ, TK> sm(rt_raw);
   NormPartR<R> npr{0.0, 0.0, (R)0, 0x7fffffffffffffffLL};
-  resid_tile<R, PRE>(S, sm, blockIdx.x - tfirst[si], flags, npr);
+  resid_tile<R, PRE, LIM, TJ, TK>(S, sm, blockIdx.x - tfirst[si], flags, npr);
   if (!(flags & AS_NORM)) return;
   // Deterministic block reduction in a fixed order: every thread leaves its
   // cell's terms in the staged region (only the face passes read it, and
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 1) k_resid(const S
   // of each lane position in thread order and finishes with a shuffle tree.
   // One warp does the FP64 additions of the whole tile.
   static_assert(RT_BS == 256 && (size_t)RT_BS * (2 * sizeof(double) + sizeof(long long) + sizeof(R)) <=
-                                   sizeof(R) * (size_t)RS_N * RT_NR, "partials fit in the staged region");
+                                   sizeof(R) * (size_t)RS_N * RtGeo<TJ, TK>::NR, "partials fit in the staged region");
   double* prs = (double*)sm.c;
   double* prr = prs + RT_BS;
   long long* pky = (long long*)(prr + RT_BS);
@@ -378,11 +381,11 @@ __global__ void __launch_bounds__(128) k_lu_edges_ring(const Slice<R>* __restric
 }
 
 template <class R, bool FWD, int G, bool PRE>
-__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int only_lu, uint32_t poll_limit) {
+__global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int only_lu, uint32_t poll_limit, int lag) {
   extern __shared__ __align__(128) unsigned char lu_smem[];
   if (only_lu && sl[blockIdx.x].P->ilhs != 1) return;
   if ((sl[blockIdx.x].k_mp2 >= (R)0) != PRE) return;
-  lu_sweep_slice<R, FWD, G, PRE>(sl[blockIdx.x], blockDim.x >> 5, lu_smem, poll_limit);
+  lu_sweep_slice<R, FWD, G, PRE>(sl[blockIdx.x], blockDim.x >> 5, lu_smem, poll_limit, lag);
 }
 
 template <class R>

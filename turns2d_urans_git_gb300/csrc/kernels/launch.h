@@ -17,8 +17,12 @@ constexpr int CELL_BS = 256;
 constexpr int BC_BS = 512;
 // threads of a CTA of one BC entry (several CTAs per slice)
 constexpr int BCE_BS = 128;
-// residual tile: RT_TJ x RT_TK interior cells per CTA
-constexpr int RT_TJ = 16, RT_TK = 16;
+// residual tile shapes (interior cells per CTA): 0 16x16, 1 32x8, 2 8x32
+constexpr int RT_NSHAPE = 3;
+inline void rt_shape_dims(int shape, int& tj, int& tk) {
+  tj = shape == 1 ? 32 : (shape == 2 ? 8 : 16);
+  tk = shape == 1 ? 8 : (shape == 2 ? 32 : 16);
+}
 // scratch arrays per slice of the k-omega SST solve (k_sst.cuh: SSTw)
 constexpr int SST_NSCRATCH = 27;
 // scratch arrays per slice of the ADI operator (k_adi.cuh: ADIw)
@@ -62,6 +66,8 @@ struct Batch {
   int nslice = 0;          // slices in the batch
   int moving = 0;          // some slice is time accurate on a pitching grid
   int precon = 0;          // some slice runs with Turkel preconditioning (k_mp2 >= 0)
+  int lim_mask = 0;        // reconstruction families of the slices: 1 central, 2 MUSCL, 4 WENO
+  int rt_shape = 0;        // residual tile shape of the tile table (rt_shape_dims)
   int cell_blocks = 0;     // blocks of the cell-parallel kernels
   int max_lu_warps = 1;    // warps per CTA of the LU-SGS kernel
   int max_wall = 1;        // most wall cells of one slice (force kernel smem); also max jd
@@ -79,6 +85,8 @@ struct Batch {
   int tile_blocks = 0;                // residual tiles over the batch
   NormPart* d_part = nullptr;         // [max(cell_blocks, tile_blocks)] norm partials
   uint32_t poll_limit = 1u << 22;     // polls of a LU-SGS sweep wait before it gives up
+  int lu_lag = 0;                     // extra steps each LU-SGS band trails its neighbour (schedule)
+  int lu_group = 0;                   // record chunks per bulk copy of the sweeps (0: largest that fits)
 };
 
 // One full iteration of step.f for every slice of the batch:
@@ -111,6 +119,11 @@ cudaError_t launch_stqol(const double* q, double* qtn, double* qtnm1, double* qn
                          int istep, cudaStream_t st);
 template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st);
 template <class R> cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st);
+// the fused residual tiles of one tile shape (TJ x TK), every
+// (preconditioning, reconstruction family) kind the batch holds; defined in
+// k_resid_launch.cuh and instantiated in resid_*.cu
+template <class R, int TJ, int TK>
+cudaError_t launch_resid_shape(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st);
 template <class R> cudaError_t launch_rbc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 // rhslom alone (sources.f:97-148) on the interior cells of every slice
 template <class R> cudaError_t launch_rhslom(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);

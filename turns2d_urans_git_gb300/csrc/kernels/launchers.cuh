@@ -37,18 +37,13 @@ cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStr
 // preconditioned one when the batch holds a preconditioned slice
 template <class R>
 cudaError_t launch_resid_both(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st) {
-  constexpr size_t smem = rt_smem_bytes<R>();
-  static DeviceOnce once;
-  cudaError_t ae = once.run([&](int&) {
-    cudaError_t e = cudaFuncSetAttribute(k_resid<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_resid<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return e;
-  });
-  if (ae != cudaSuccess) return ae;
-  k_resid<R, false><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
-  if (b.precon) k_resid<R, true><<<b.tile_blocks, RT_BS, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
-  return cudaGetLastError();
+  // the tile shape the batch's tile table was built for (k_resid_launch.cuh,
+  // one translation unit per shape and precision)
+  switch (b.rt_shape) {
+    case 1: return launch_resid_shape<R, 32, 8>(d_sl, b, flags, st);
+    case 2: return launch_resid_shape<R, 8, 32>(d_sl, b, flags, st);
+    default: return launch_resid_shape<R, 16, 16>(d_sl, b, flags, st);
+  }
 }
 template <class R>
 cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st) {
@@ -120,7 +115,7 @@ cudaError_t launch_lusgs_sweeps_t(const Slice<R>* d_sl, const Batch& b, cudaStre
   const int nw = b.max_lu_warps;
   // chunks per bulk copy: as many as ~200 KB of shared memory allows (1..8)
   const int maxcol = b.max_wall;   // >= jd - 2 of every slice
-  int G = 8;
+  int G = (b.lu_group == 1 || b.lu_group == 2 || b.lu_group == 4 || b.lu_group == 8) ? b.lu_group : 8;
   while (G > 1 && lu_smem_bytes<R, PRE>(nw, G, maxcol) > 200 * 1024) G >>= 1;
   const size_t smem = lu_smem_bytes<R, PRE>(nw, G, maxcol);
   if (32 * nw > 1024 || smem > (size_t)SMEM_OPTIN_MAX) return cudaErrorInvalidConfiguration;
@@ -153,9 +148,9 @@ cudaError_t launch_lusgs_sweeps_t(const Slice<R>* d_sl, const Batch& b, cudaStre
   cfg.attrs = at;
   cfg.numAttrs = 1;
   auto run = [&](auto fwd, auto bwd) -> cudaError_t {
-    cudaError_t e = cudaLaunchKernelEx(&cfg, fwd, d_sl, only_lu, b.poll_limit);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, fwd, d_sl, only_lu, b.poll_limit, b.lu_lag);
     if (e != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, bwd, d_sl, only_lu, b.poll_limit);
+    return cudaLaunchKernelEx(&cfg, bwd, d_sl, only_lu, b.poll_limit, b.lu_lag);
   };
   cudaError_t e;
   switch (G) {

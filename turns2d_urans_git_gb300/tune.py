@@ -1,0 +1,167 @@
+"""Autotuner of the batched solver's launch choices.
+
+For each mesh-size class it times a batch of that class under every
+candidate choice and keeps the fastest:
+
+  rt_shape   the fused residual's tile, 16x16, 32x8 or 8x32 interior cells
+             per CTA (staged halo per cell against threads per face line)
+  lu_group   LU-SGS record chunks streamed per bulk copy (4 or 8)
+  lu_lag     LU-SGS hyperplane schedule: steps each 32-row band trails the
+             band it depends on beyond the minimum (0 or 4)
+
+Every candidate computes the same results bit for bit (the choices change
+launch geometry and schedule only), so the search is free to pick on time
+alone.  Choices are cached in a JSON file keyed by GPU name, precision and
+size class, and handed to a solver as its tuning table
+(ot2d_solver_set_tuning), which applies the entry of each batch's largest
+mesh when it builds the batch.
+"""
+import ctypes as C
+import json
+import os
+import statistics
+import time
+
+from .abi import OT2D_FP64, OT2D_FP32_MIXED, OT2D_OPT_LU_GROUP, OT2D_OPT_LU_LAG, OT2D_OPT_RT_SHAPE, Tuning
+
+# the mesh sizes of the batched configuration (vertices); a class covers
+# meshes up to its array size (jd = jmax + 1, kd = kmax + 1)
+SIZE_CLASSES = ((129, 33), (257, 65), (385, 97), (513, 129), (769, 193))
+SHAPES = {0: "16x16", 1: "32x8", 2: "8x32"}
+CANDIDATES = tuple((shape, group, lag) for shape in (0, 1, 2) for group in (4, 8) for lag in (0, 4))
+
+
+def default_cache_path():
+    root = os.environ.get("XDG_CACHE_HOME") or os.path.join(os.path.expanduser("~"), ".cache")
+    return os.path.join(root, "turns2d_gb300", "tuning.json")
+
+
+def class_key(gpu, precision, jmax, kmax):
+    return "%s|%s|%dx%d" % (gpu, "fp64" if precision == OT2D_FP64 else "fp32-mixed", jmax, kmax)
+
+
+def search(candidates, measure, repeats=3):
+    """The candidate with the smallest median of `repeats` measurements
+    (ms); returns (best, {candidate: median ms}).  Ties keep the earlier
+    candidate."""
+    times = {}
+    for c in candidates:
+        times[c] = statistics.median(measure(c) for _ in range(repeats))
+    best = min(candidates, key=lambda c: (times[c], candidates.index(c)))
+    return best, times
+
+
+def load_cache(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def save_cache(path, cache):
+    os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+    tmp = path + ".tmp%d" % os.getpid()
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def tuning_table(choices):
+    """ot2d_tuning entries from {(jmax, kmax): (shape, group, lag)}, smallest
+    class first (the solver takes the first entry that bounds a batch's
+    largest mesh)."""
+    rows = sorted(choices.items(), key=lambda kv: (kv[0][1], kv[0][0]))
+    table = (Tuning * len(rows))()
+    for t, ((jmax, kmax), (shape, group, lag)) in zip(table, rows):
+        t.kd_max, t.jd_max = kmax + 1, jmax + 1
+        t.rt_shape, t.lu_group, t.lu_lag = shape, group, lag
+    return table
+
+
+def tune(measure_for_class, classes, gpu, precision, cache_path=None, retune=False):
+    """Choices for every class: from the cache, or searched with
+    measure_for_class(jmax, kmax) -> measure(candidate) and then cached.
+    Returns ({(jmax, kmax): choice}, {class: timings or None if cached})."""
+    cache_path = cache_path or default_cache_path()
+    cache = load_cache(cache_path)
+    choices, timings = {}, {}
+    changed = False
+    for (jmax, kmax) in classes:
+        key = class_key(gpu, precision, jmax, kmax)
+        hit = cache.get(key)
+        if hit and not retune and tuple(hit["choice"]) in CANDIDATES:
+            choices[(jmax, kmax)] = tuple(hit["choice"])
+            timings[(jmax, kmax)] = None
+            continue
+        measure = measure_for_class(jmax, kmax)
+        try:
+            best, times = search(CANDIDATES, measure)
+        finally:
+            sv = getattr(measure, "solver", None)
+            if sv is not None:
+                sv.close()
+        choices[(jmax, kmax)] = best
+        timings[(jmax, kmax)] = times
+        cache[key] = {"choice": list(best), "ms": {"%d,%d,%d" % c: t for c, t in times.items()},
+                      "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
+        changed = True
+    if changed:
+        save_cache(cache_path, cache)
+    return choices, timings
+
+
+def gpu_measure_for_class(precision, batch=16, iters=10, device=0, case_for_class=None):
+    """measure_for_class on the GPU: a batch of `batch` requests of the class,
+    each candidate timed with CUDA events over `iters` iterations of the
+    captured iteration after 3 warm-up iterations."""
+    import torch
+    from . import api
+
+    def for_class(jmax, kmax):
+        if case_for_class is None:
+            # NACA 0012 RANS-SA requests of the class at moderate incidence
+            # (requests that stay finite over the timed iterations)
+            cases = [api.config_c2(jmax, kmax, fsmach=0.3, alfa=0.25 * i, rey=5e6, ds_wall=api.wall_spacing(kmax))
+                     for i in range(batch)]
+        else:
+            cases = [case_for_class(jmax, kmax, i) for i in range(batch)]
+        sv = api.Solver(precision, device=device, check_every=10 ** 8)
+        for (_, prm, xv, yv) in cases:
+            sv.add(prm, xv, yv, orders=0.0, max_iters=10 ** 8)
+
+        def measure(c):
+            shape, group, lag = c
+            sv.set_option(OT2D_OPT_RT_SHAPE, shape)
+            sv.set_option(OT2D_OPT_LU_GROUP, group)
+            sv.set_option(OT2D_OPT_LU_LAG, lag)
+            sv.iterate(3)
+            st = torch.cuda.ExternalStream(sv.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            sv.iterate(iters)
+            e1.record(st)
+            e1.synchronize()
+            return e0.elapsed_time(e1) / iters
+
+        measure.solver = sv
+        return measure
+
+    return for_class
+
+
+def apply(solver, choices):
+    """Hand the choices to a solver (api.Solver) as its tuning table."""
+    from . import api
+    table = tuning_table(choices)
+    f = api.lib().ot2d_solver_set_tuning
+    f.argtypes = [C.c_void_p, C.POINTER(Tuning), C.c_int32]
+    rc = f(solver._h, table, len(table))
+    if rc != 0:
+        raise RuntimeError("ot2d_solver_set_tuning failed (%d)" % rc)
+    return table
+
+
+def describe(choices):
+    return {"%dx%d" % k: {"rt_tile": SHAPES[v[0]], "lu_group": v[1], "lu_lag": v[2]} for k, v in sorted(choices.items())}
