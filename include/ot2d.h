@@ -276,6 +276,9 @@ typedef struct ot2d_result {
 #define OT2D_OPT_LU_GROUP      8  /* LU-SGS records streamed per bulk copy: 1, 2, 4 or 8
                                      (default 0: the largest the shared memory allows) */
 #define OT2D_OPT_RT_SHAPE      9  /* residual tile: 0 16x16 (default), 1 32x8, 2 8x32 cells */
+#define OT2D_OPT_PIPELINE     10  /* 1 (default): a batch of 16 or more time instances runs
+                                     as two halves on two streams, each half's residual
+                                     beside the other half's LU-SGS sweeps; 0: one graph */
 #define OT2D_OPT_POLL_LIMIT    5  /* polls a LU-SGS sweep wait makes before it gives up
                                      (default 4194304).  An instance whose wait gave up
                                      keeps its state and retires with OT2D_ERR_TIMEOUT;
@@ -298,7 +301,8 @@ int ot2d_solver_set_force_tol(ot2d_solver* s, double dcl, double dcd);
  * one with most cells) sets the residual tile shape, the LU-SGS copy group
  * and the LU-SGS band lag; without a matching entry the OT2D_OPT_* values
  * apply.  The choices change the launch geometry and schedule only: every
- * variant gives the same results bit for bit. */
+ * variant gives the same state bit for bit (the L2 norm is summed per
+ * residual tile, so it agrees to rounding across tile shapes). */
 typedef struct ot2d_tuning {
   int32_t kd_max, jd_max;   /* class bound: kd <= kd_max and jd <= jd_max      */
   int32_t rt_shape;         /* 0 16x16, 1 32x8, 2 8x32                          */

@@ -1,7 +1,8 @@
 """The autotuner's candidates on the GPU: every launch choice (residual tile
-shape, LU-SGS copy group, LU-SGS band lag) gives the same results bit for
-bit, in FP64 and in the FP32-mixed path, and a tuning table handed to the
-solver is applied to the batch of its size class."""
+shape, LU-SGS copy group, LU-SGS band lag) gives the same state bit for bit,
+in FP64 and in the FP32-mixed path (the L2 norm's partial sums follow the
+tile shape, so the norms agree to rounding), and a tuning table handed to
+the solver is applied to the batch of its size class."""
 import numpy as np
 import pytest
 
@@ -48,7 +49,8 @@ def test_every_tuning_candidate_is_bitwise_the_same(precision):
         out = _run(precision, cases, c)
         for (q, r), (q0, r0) in zip(out, ref):
             assert np.array_equal(q, q0), c
-            assert r.rsum_last == r0.rsum_last and r.cl == r0.cl, c
+            assert r.cl == r0.cl and r.cd == r0.cd, c
+            assert abs(r.rsum_last - r0.rsum_last) <= 1e-13 * r0.rsum_last, c
 
 
 def test_tuning_table_applies_to_its_class_only():

@@ -34,6 +34,7 @@ OT2D_OPT_BUDGET_MB = 6
 OT2D_OPT_LU_LAG = 7
 OT2D_OPT_LU_GROUP = 8
 OT2D_OPT_RT_SHAPE = 9
+OT2D_OPT_PIPELINE = 10
 
 _I = C.c_int32
 _D = C.c_double

@@ -101,6 +101,20 @@ struct ot2d_solver {
   bool dirty = true;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  // Pipelined iteration (OT2D_OPT_PIPELINE): a large batch runs as two
+  // halves, one graph each on its own stream; each half starts an iteration
+  // once the other half's residual of the same (or the previous) iteration
+  // is done, so one half's residual fills the SMs the other half's LU-SGS
+  // sweeps leave idle.
+  int pipeline = 1;
+  bool split = false;
+  DevBatch<double> h64[2];
+  DevBatch<float> h32[2];
+  cudaGraph_t hgraph[2] = {nullptr, nullptr};
+  cudaGraphExec_t hexec[2] = {nullptr, nullptr};
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_half[2] = {nullptr, nullptr};   // recorded in each half's graph after its rbc
+  cudaEvent_t ev_join = nullptr;
   int next_id = 0;
   double t0 = 0;
   int check_every = 25;
@@ -165,7 +179,40 @@ void drop_graph(ot2d_solver* s) {
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
   if (s->graph) cudaGraphDestroy(s->graph);
   s->gexec = nullptr; s->graph = nullptr;
+  for (int h = 0; h < 2; ++h) {
+    if (s->hexec[h]) cudaGraphExecDestroy(s->hexec[h]);
+    if (s->hgraph[h]) cudaGraphDestroy(s->hgraph[h]);
+    s->hexec[h] = nullptr; s->hgraph[h] = nullptr;
+  }
+  s->split = false;
 }
+
+// batches of at least this many slices run as two pipelined halves
+constexpr int PIPE_MIN_SLICES = 16;
+
+// one iteration of every live instance: the single graph, or the two halves
+// with their cross waits
+cudaError_t launch_graph_iteration(ot2d_solver* s) {
+  if (!s->split) return cudaGraphLaunch(s->gexec, s->st);
+  cudaError_t e;
+  // half 0 of iteration i after half 1's residual of iteration i-1
+  if ((e = cudaStreamWaitEvent(s->st, s->ev_half[1], 0)) != cudaSuccess) return e;
+  if ((e = cudaGraphLaunch(s->hexec[0], s->st)) != cudaSuccess) return e;
+  // half 1 of iteration i after half 0's residual of iteration i
+  if ((e = cudaStreamWaitEvent(s->st2, s->ev_half[0], 0)) != cudaSuccess) return e;
+  return cudaGraphLaunch(s->hexec[1], s->st2);
+}
+
+// make the solver stream wait for the second half's work
+cudaError_t join_halves(ot2d_solver* s) {
+  if (!s->split) return cudaSuccess;
+  cudaError_t e = cudaEventRecord(s->ev_join, s->st2);
+  return e == cudaSuccess ? cudaStreamWaitEvent(s->st, s->ev_join, 0) : e;
+}
+
+template <class R> DevBatch<R>* halves_of(ot2d_solver* s);
+template <> DevBatch<double>* halves_of<double>(ot2d_solver* s) { return s->h64; }
+template <> DevBatch<float>* halves_of<float>(ot2d_solver* s) { return s->h32; }
 
 template <class R>
 int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
@@ -206,11 +253,48 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   // SA and SST requests can share one batch.
   Branch* br = nullptr;   // the turbulence branch's stream, created outside the capture
   if (branch_of_device(br) != cudaSuccess) return OT2D_ERR_CUDA;
-  if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
-  cudaError_t le = launch_iteration<R>(B.d_sl, B.b, s->any_viscous ? 1 : 0, s->turb_bits, s->lhs_bits, s->st);
-  cudaError_t ce = cudaStreamEndCapture(s->st, &s->graph);
-  if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
-  if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
+  const int visc = s->any_viscous ? 1 : 0;
+  const bool split = s->pipeline && sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= 2;
+  if (!split) {
+    if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
+    cudaError_t le = launch_iteration<R>(B.d_sl, B.b, visc, s->turb_bits, s->lhs_bits, s->st);
+    cudaError_t ce = cudaStreamEndCapture(s->st, &s->graph);
+    if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
+    if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
+    return OT2D_OK;
+  }
+  // two halves of about equal cells (a request's time instances stay in one
+  // half: the time-spectral source couples them)
+  std::vector<int> ids = s->live;
+  auto cells_of = [&](int id) { const ot2d_params& p = s->recs[id].d.P; return (size_t)p.jd * p.kd * p.nspec; };
+  std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return cells_of(a) > cells_of(b); });
+  std::vector<Slice<R>> slh[2];
+  size_t load[2] = {0, 0};
+  for (int id : ids) {
+    const int h = load[0] <= load[1] ? 0 : 1;
+    load[h] += cells_of(id);
+    slices_of<R>(s, s->recs[id], slh[h]);
+  }
+  if (!s->st2 && cudaStreamCreateWithFlags(&s->st2, cudaStreamNonBlocking) != cudaSuccess) return OT2D_ERR_CUDA;
+  for (int h = 0; h < 2; ++h)
+    if (!s->ev_half[h] && cudaEventCreateWithFlags(&s->ev_half[h], cudaEventDisableTiming) != cudaSuccess)
+      return OT2D_ERR_CUDA;
+  if (!s->ev_join && cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) != cudaSuccess) return OT2D_ERR_CUDA;
+  DevBatch<R>* H = halves_of<R>(s);
+  for (int h = 0; h < 2; ++h) {
+    H[h].rt_shape = ch.rt_shape;
+    if ((e = H[h].build(slh[h], s->st))) return e;
+    H[h].b.poll_limit = s->poll_limit;
+    H[h].b.lu_lag = ch.lu_lag;
+    H[h].b.lu_group = ch.lu_group;
+    cudaStream_t cs = h == 0 ? s->st : s->st2;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
+    cudaError_t le = launch_iteration<R>(H[h].d_sl, H[h].b, visc, s->turb_bits, s->lhs_bits, cs, s->ev_half[h]);
+    cudaError_t ce = cudaStreamEndCapture(cs, &s->hgraph[h]);
+    if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
+    if (cudaGraphInstantiate(&s->hexec[h], s->hgraph[h], 0) != cudaSuccess) return OT2D_ERR_CUDA;
+  }
+  s->split = true;
   return OT2D_OK;
 }
 
@@ -603,8 +687,15 @@ ot2d_solver* ot2d_solver_create(int32_t device, int32_t precision) {
 void ot2d_solver_destroy(ot2d_solver* s) {
   if (!s) return;
   cudaStreamSynchronize(s->st);
+  if (s->st2) cudaStreamSynchronize(s->st2);
   if (s->st_d2h) cudaStreamSynchronize(s->st_d2h);
   drop_graph(s);
+  for (int h = 0; h < 2; ++h) {
+    s->h64[h].release(); s->h32[h].release();
+    if (s->ev_half[h]) cudaEventDestroy(s->ev_half[h]);
+  }
+  if (s->ev_join) cudaEventDestroy(s->ev_join);
+  if (s->st2) cudaStreamDestroy(s->st2);
   for (auto& kv : s->recs) solve_destroy(kv.second.d);
   for (cudaEvent_t e : s->ev_d2h) cudaEventDestroy(e);
   if (s->ev_step) cudaEventDestroy(s->ev_step);
@@ -630,6 +721,7 @@ int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value) {
   if (key == OT2D_OPT_BUDGET_MB && value >= 0) { s->budget_set = (size_t)value << 20; return OT2D_OK; }
   if (key == OT2D_OPT_LU_LAG && value >= 0 && value <= 64) { s->lu_lag = value; s->dirty = true; return OT2D_OK; }
   if (key == OT2D_OPT_RT_SHAPE && value >= 0 && value < RT_NSHAPE) { s->rt_shape = value; s->dirty = true; return OT2D_OK; }
+  if (key == OT2D_OPT_PIPELINE && (value == 0 || value == 1)) { s->pipeline = value; s->dirty = true; return OT2D_OK; }
   if (key == OT2D_OPT_LU_GROUP && (value == 0 || value == 1 || value == 2 || value == 4 || value == 8)) {
     s->lu_group = value;
     s->dirty = true;
@@ -689,8 +781,9 @@ int ot2d_solver_iterate(ot2d_solver* s, int32_t iters) {
     chunk = (int)std::max(1L, rem);
     nvtxRangePushA("ot2d iterations");
     for (int i = 0; i < chunk; ++i)
-      if (cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) { nvtxRangePop(); return OT2D_ERR_CUDA; }
+      if (launch_graph_iteration(s) != cudaSuccess) { nvtxRangePop(); return OT2D_ERR_CUDA; }
     nvtxRangePop();
+    if (join_halves(s) != cudaSuccess) return OT2D_ERR_CUDA;
     bool capped = false;
     for (int id : s->live) {
       Rec& r = s->recs[id];
@@ -785,7 +878,7 @@ int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, doub
     }
     if (!err && s->precision == OT2D_FP32_MIXED && launch_shadow<float>(s->b32.d_sl, s->b32.b, s->st) != cudaSuccess)
       err = OT2D_ERR_CUDA;
-    if (!err && cudaGraphLaunch(s->gexec, s->st) != cudaSuccess) err = OT2D_ERR_CUDA;
+    if (!err && (launch_graph_iteration(s) != cudaSuccess || join_halves(s) != cudaSuccess)) err = OT2D_ERR_CUDA;
     if (!err && (cudaEventRecord(s->ev_step, s->st) != cudaSuccess ||
                  cudaStreamWaitEvent(s->st_d2h, s->ev_step, 0) != cudaSuccess))
       err = OT2D_ERR_CUDA;

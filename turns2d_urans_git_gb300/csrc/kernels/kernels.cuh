@@ -28,6 +28,18 @@ __device__ __forceinline__ bool monitor_bad(T ggm1, const T* q) {
 
 // Cell-parallel mapping: slice i owns blocks [first[i], first[i+1]) of
 // CELL_BS threads each, covering its jd*kd cells.
+// Streaming kernels (a few loads and stores per cell) run CELL_BS / CELL_PT
+// threads per block of CELL_BS cells, each thread CELL_PT cells CELL_BS /
+// CELL_PT apart (coalesced per pass): the same prefix tables, and CELL_PT
+// times the loads in flight per block for the one slice lookup of the
+// block.
+constexpr int CELL_PT = 4;
+#define OT2D_CELL_MAP_PT()                                                    \
+  const int si = find_slice(first, nslice, blockIdx.x);                      \
+  const Slice<R>& S = sl[si];                                                \
+  const int cid0 = (blockIdx.x - first[si]) * CELL_BS + threadIdx.x;         \
+  const int ncell = S.jd * S.kd;
+
 #define OT2D_CELL_MAP()                                                      \
   const int si = find_slice(first, nslice, blockIdx.x);                      \
   const Slice<R>& S = sl[si];                                                \
@@ -36,16 +48,19 @@ __device__ __forceinline__ bool monitor_bad(T ggm1, const T* q) {
   const bool inside = cid < S.jd * S.kd;
 
 template <class R>
-__global__ void __launch_bounds__(CELL_BS) k_time_step(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
-                                                       int nslice) {
-  OT2D_CELL_MAP();
-  if (!inside) return;
+__global__ void __launch_bounds__(CELL_BS / CELL_PT) k_time_step(const Slice<R>* __restrict__ sl,
+                                                                 const int32_t* __restrict__ first, int nslice) {
+  OT2D_CELL_MAP_PT();
   const ot2d_params& p = *S.P;
   int istep = S.ist ? S.ist[1] : p.istep;   // advanced by k_iter_begin
   R oat = (R)1.0;
   if (p.ntac >= 2 && istep > 1) oat = (R)(2. / 3.);
   if (p.ntac == 3 && istep > 2) oat = (R)(6. / 11.);
-  time_step_cell(S, j, k, oat);
+#pragma unroll
+  for (int u = 0; u < CELL_PT; ++u) {
+    const int cid = cid0 + u * (CELL_BS / CELL_PT);
+    if (cid < ncell) time_step_cell(S, cid % S.jd + 1, cid / S.jd + 1, oat);
+  }
 }
 
 // Start of a solver iteration (one thread per slice): the step counters of
@@ -603,49 +618,59 @@ __global__ void __launch_bounds__(CELL_BS) k_adi_teta(const Slice<R>* __restrict
 
 // q(1:4) += s*max(iblank,0) on interior cells (step.f:203-213), FP64 state
 template <class R>
-__global__ void __launch_bounds__(CELL_BS) k_update(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
-                                                    int nslice) {
-  OT2D_CELL_MAP();
-  if (!inside) return;
+__global__ void __launch_bounds__(CELL_BS / CELL_PT) k_update(const Slice<R>* __restrict__ sl,
+                                                              const int32_t* __restrict__ first, int nslice) {
+  OT2D_CELL_MAP_PT();
   const ot2d_params& p = *S.P;
-  if (j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) return;
   // a sweep of this slice gave up (status bit 4): its correction is
   // incomplete, so the state is left as it is until the slice is retired
   if (S.ist && (__ldcg(&S.ist[2]) & 4)) return;
-  const int64_t o = at(S.jd, j, k);
-  int ibi = S.iblank[o];
-  double m = (double)(ibi > 0 ? ibi : 0);
-  // every load before the first store (the state and the residual may not
-  // alias, but the compiler cannot know): eight independent loads in flight
-  double q0[4];
-  R sv[4];
+  bool bad = false;
 #pragma unroll
-  for (int n = 0; n < 4; ++n) { q0[n] = S.q64[n * S.qs + o]; sv[n] = S.s[n * S.qs + o]; }
-  R qn[4];
+  for (int u = 0; u < CELL_PT; ++u) {
+    const int cid = cid0 + u * (CELL_BS / CELL_PT);
+    const int j = cid % S.jd + 1, k = cid / S.jd + 1;
+    if (cid >= ncell || j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) continue;
+    const int64_t o = at(S.jd, j, k);
+    int ibi = S.iblank[o];
+    double m = (double)(ibi > 0 ? ibi : 0);
+    // every load before the first store (the state and the residual may not
+    // alias, but the compiler cannot know): eight independent loads in flight
+    double q0[4];
+    R sv[4];
 #pragma unroll
-  for (int n = 0; n < 4; ++n) {
-    double v = q0[n] + (double)sv[n] * m;
-    S.q64[n * S.qs + o] = v;
-    qn[n] = (R)v;
-    if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = qn[n];
+    for (int n = 0; n < 4; ++n) { q0[n] = S.q64[n * S.qs + o]; sv[n] = S.s[n * S.qs + o]; }
+    R qn[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      double v = q0[n] + (double)sv[n] * m;
+      S.q64[n * S.qs + o] = v;
+      qn[n] = (R)v;
+      if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = qn[n];
+    }
+    // monitor of the updated cell (step.f:356-370), free of divisions:
+    // a^2 <= 0.002  <=>  ggm1*(q4*q1 - qq/2) <= 0.002*q1^2 for q1 > 0
+    bad = bad || monitor_bad<R>(S.k_ggm1, qn);
   }
-  // monitor of the updated cell (step.f:356-370), free of divisions:
-  // a^2 <= 0.002  <=>  ggm1*(q4*q1 - qq/2) <= 0.002*q1^2 for q1 > 0
-  if (S.ist && monitor_bad<R>(S.k_ggm1, qn)) atomicOr(&S.ist[2], 2);
+  if (S.ist && bad) atomicOr(&S.ist[2], 2);
 }
 
 // compute copy of the whole state from the FP64 master (after the host
 // replaced q64); a no-op on the plain FP64 path where they are one array
 template <class R>
-__global__ void __launch_bounds__(CELL_BS) k_shadow(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
-                                                    int nslice) {
+__global__ void __launch_bounds__(CELL_BS / CELL_PT) k_shadow(const Slice<R>* __restrict__ sl,
+                                                              const int32_t* __restrict__ first, int nslice) {
   if constexpr (sizeof(R) == sizeof(double)) {
     return;
   } else {
-    OT2D_CELL_MAP();
-    if (!inside) return;
-    const int64_t o = at(S.jd, j, k);
-    for (int n = 0; n < S.P->nq; ++n) S.q[n * S.qs + o] = (R)S.q64[n * S.qs + o];
+    OT2D_CELL_MAP_PT();
+    const int nq = S.P->nq;
+#pragma unroll
+    for (int u = 0; u < CELL_PT; ++u) {
+      const int cid = cid0 + u * (CELL_BS / CELL_PT);
+      if (cid >= ncell) continue;
+      for (int n = 0; n < nq; ++n) S.q[n * S.qs + cid] = (R)S.q64[n * S.qs + cid];
+    }
   }
 }
 

@@ -93,8 +93,11 @@ struct Batch {
 // time_step, bc, rhsup (+visrhs, +time-spectral), norms, rbc, ilu2d,
 // vmu_sa (turb bit 1), komegasst (turb bit 2), update, monitor.  lhs bit 1:
 // some slice uses LU-SGS (ilhs = 1), bit 2: some slice uses ADI (ilhs = 2, 3).
+// after_rbc (or null): recorded on st, as an external event of a captured
+// graph, once the residual and its boundary conditions are done.
 template <class R>
-cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st);
+cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st,
+                             cudaEvent_t after_rbc = nullptr);
 
 // The second stream of an iteration (one per device and host thread) and
 // the events of its fork and join; created on first use.  Call it once

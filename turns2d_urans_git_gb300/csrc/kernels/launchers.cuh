@@ -21,7 +21,7 @@ cudaError_t launch_pitch(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) 
 }
 template <class R>
 cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
-  k_time_step<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  k_time_step<R><<<b.cell_blocks, CELL_BS / CELL_PT, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
 }
 template <class R>
@@ -224,12 +224,12 @@ cudaError_t launch_adi(const Slice<R>* d_sl, const Batch& b, int scale, cudaStre
 }
 template <class R>
 cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
-  k_update<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  k_update<R><<<b.cell_blocks, CELL_BS / CELL_PT, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
 }
 template <class R>
 cudaError_t launch_shadow(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
-  if (sizeof(R) != sizeof(double)) k_shadow<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  if (sizeof(R) != sizeof(double)) k_shadow<R><<<b.cell_blocks, CELL_BS / CELL_PT, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
 }
 template <class R>
@@ -251,13 +251,17 @@ cudaError_t launch_forces(const Slice<R>* d_sl, const Batch& b, const double* co
   return cudaGetLastError();
 }
 template <class R>
-cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st) {
+cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st,
+                             cudaEvent_t after_rbc) {
   cudaError_t e;
   if ((e = launch_iter_begin(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_time_step(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_bc(d_sl, b, 1, st)) != cudaSuccess) return e;
   if ((e = launch_residual(d_sl, b, viscous, st)) != cudaSuccess) return e;
   if ((e = launch_rbc(d_sl, b, st)) != cudaSuccess) return e;
+  // the pipelined solver starts the other half of its batch here (an
+  // external event node of the captured graph)
+  if (after_rbc && (e = cudaEventRecordWithFlags(after_rbc, st, cudaEventRecordExternal)) != cudaSuccess) return e;
   if (lhs == 1 && turb) {
     // The turbulence solve (step.f:184-190) reads q, mu_t and tscale, which
     // the LU-SGS sweeps do not write, and writes its own variables and mu_t,
@@ -285,7 +289,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
 }
 
 #define OT2D_INSTANTIATE(R)                                                                              \
-  template cudaError_t launch_iteration<R>(const Slice<R>*, const Batch&, int, int, int, cudaStream_t); \
+  template cudaError_t launch_iteration<R>(const Slice<R>*, const Batch&, int, int, int, cudaStream_t, cudaEvent_t); \
   template cudaError_t launch_time_step<R>(const Slice<R>*, const Batch&, cudaStream_t);                \
   template cudaError_t launch_iter_begin<R>(const Slice<R>*, const Batch&, cudaStream_t);               \
   template cudaError_t launch_pitch<R>(const Slice<R>*, const Batch&, cudaStream_t);                    \

@@ -9,9 +9,10 @@ candidate choice and keeps the fastest:
   lu_lag     LU-SGS hyperplane schedule: steps each 32-row band trails the
              band it depends on beyond the minimum (0 or 4)
 
-Every candidate computes the same results bit for bit (the choices change
-launch geometry and schedule only), so the search is free to pick on time
-alone.  Choices are cached in a JSON file keyed by GPU name, precision and
+Every candidate computes the same state bit for bit (the choices change
+launch geometry and schedule only; the L2 norm's partial sums follow the
+residual tile, so the norms agree to rounding), so the search is free to
+pick on time alone.  Choices are cached in a JSON file keyed by GPU name, precision and
 size class, and handed to a solver as its tuning table
 (ot2d_solver_set_tuning), which applies the entry of each batch's largest
 mesh when it builds the batch.
