@@ -126,7 +126,7 @@ def autotune(device, classes_fp32, classes_fp64):
     t0 = time.perf_counter()
     c32, _ = tune.tune(tune.gpu_measure_for_class(OT2D_FP32_MIXED, device=device), classes_fp32, gpu,
                        OT2D_FP32_MIXED)
-    c64, _ = tune.tune(tune.gpu_measure_for_class(OT2D_FP64, batch=4, iters=3, device=device), classes_fp64, gpu,
+    c64, _ = tune.tune(tune.gpu_measure_for_class(OT2D_FP64, batch=16, iters=3, device=device), classes_fp64, gpu,
                        OT2D_FP64)
     return c32, c64, time.perf_counter() - t0
 

@@ -298,8 +298,9 @@ int ot2d_solver_set_force_tol(ot2d_solver* s, double dcl, double dcd);
 /* Launch choices for batches of one mesh-size class, as an autotuner
  * measured them (turns2d_urans_git_gb300/tune.py).  When a batch is built,
  * the first entry whose kd_max / jd_max bound the batch's largest mesh (the
- * one with most cells) sets the residual tile shape, the LU-SGS copy group
- * and the LU-SGS band lag; without a matching entry the OT2D_OPT_* values
+ * one with most cells) sets the residual tile shape, the LU-SGS copy group,
+ * the LU-SGS band lag and whether a batch of 16 or more time instances runs
+ * as two pipelined halves; without a matching entry the OT2D_OPT_* values
  * apply.  The choices change the launch geometry and schedule only: every
  * variant gives the same state bit for bit (the L2 norm is summed per
  * residual tile, so it agrees to rounding across tile shapes). */
@@ -308,7 +309,7 @@ typedef struct ot2d_tuning {
   int32_t rt_shape;         /* 0 16x16, 1 32x8, 2 8x32                          */
   int32_t lu_group;         /* 0 (largest that fits), 1, 2, 4, 8                */
   int32_t lu_lag;           /* 0..64                                            */
-  int32_t reserved;
+  int32_t pipeline;         /* 0 one graph, 1 two pipelined halves (OT2D_OPT_PIPELINE) */
 } ot2d_tuning;
 /* replace the tuning table (n entries, copied; n = 0 clears it) */
 int ot2d_solver_set_tuning(ot2d_solver* s, const ot2d_tuning* t, int32_t n);

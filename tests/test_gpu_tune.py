@@ -8,7 +8,7 @@ import pytest
 
 from turns2d_urans_git_gb300 import api, tune
 from turns2d_urans_git_gb300.abi import (OT2D_FP32_MIXED, OT2D_FP64, OT2D_OPT_LU_GROUP, OT2D_OPT_LU_LAG,
-                                         OT2D_OPT_RT_SHAPE)
+                                         OT2D_OPT_PIPELINE, OT2D_OPT_RT_SHAPE)
 
 pytestmark = pytest.mark.gpu
 
@@ -18,10 +18,11 @@ NSTEPS = 12
 def _run(precision, cases, choice=None, table=None):
     sv = api.Solver(precision, check_every=NSTEPS, keep_q=True)
     if choice is not None:
-        shape, group, lag = choice
+        shape, group, lag, pipe = choice
         sv.set_option(OT2D_OPT_RT_SHAPE, shape)
         sv.set_option(OT2D_OPT_LU_GROUP, group)
         sv.set_option(OT2D_OPT_LU_LAG, lag)
+        sv.set_option(OT2D_OPT_PIPELINE, pipe)
     if table is not None:
         tune.apply(sv, table)
     ids = [sv.add(c[1], c[2], c[3], orders=0.0, max_iters=NSTEPS) for c in cases]
@@ -44,7 +45,7 @@ def _cases():
 @pytest.mark.parametrize("precision", [OT2D_FP64, OT2D_FP32_MIXED])
 def test_every_tuning_candidate_is_bitwise_the_same(precision):
     cases = _cases()
-    ref = _run(precision, cases, (0, 0, 0))
+    ref = _run(precision, cases, (0, 0, 0, 0))
     for c in tune.CANDIDATES:
         out = _run(precision, cases, c)
         for (q, r), (q0, r0) in zip(out, ref):
@@ -57,13 +58,13 @@ def test_tuning_table_applies_to_its_class_only():
     """A table entry for this batch's class gives the same bits as the same
     choice set by options; an entry for another class leaves the default."""
     cases = _cases()
-    choice = (1, 8, 4)
+    choice = (1, 8, 4, 0)
     by_option = _run(OT2D_FP64, cases, choice)
     by_table = _run(OT2D_FP64, cases, table={(129, 69): choice})
     for (q, _), (q0, _) in zip(by_table, by_option):
         assert np.array_equal(q, q0)
-    other = _run(OT2D_FP64, cases, table={(65, 25): (2, 4, 0)})
-    default = _run(OT2D_FP64, cases, (0, 0, 0))
+    other = _run(OT2D_FP64, cases, table={(65, 25): (2, 4, 0, 0)})
+    default = _run(OT2D_FP64, cases, (0, 0, 0, 1))
     for (q, _), (q0, _) in zip(other, default):
         assert np.array_equal(q, q0)
 

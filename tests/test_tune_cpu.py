@@ -26,11 +26,12 @@ def test_tune_searches_each_class_once_then_reads_the_cache(tmp_path):
     classes = ((129, 33), (513, 129))
     # a class prefers the wide tile for wide meshes, group 8, no lag
     def costs(jmax, kmax, c):
-        shape, group, lag = c
-        return 1.0 + (0.0 if shape == (1 if jmax > 300 else 0) else 0.5) + (0.0 if group == 8 else 0.1) + 0.01 * lag
+        shape, group, lag, pipe = c
+        return (1.0 + (0.0 if shape == (1 if jmax > 300 else 0) else 0.5) + (0.0 if group == 8 else 0.1) + 0.01 * lag
+                + (0.0 if pipe == (1 if jmax > 300 else 0) else 0.05))
     calls = []
     ch, timings = tune.tune(_fake(costs, calls), classes, "GB300", OT2D_FP32_MIXED, cache_path=path)
-    assert ch == {(129, 33): (0, 8, 0), (513, 129): (1, 8, 0)}
+    assert ch == {(129, 33): (0, 8, 0, 0), (513, 129): (1, 8, 0, 1)}
     assert len(calls) == 2 * 3 * len(tune.CANDIDATES)
     assert all(v is not None for v in timings.values())
     cache = json.load(open(path))
@@ -53,18 +54,19 @@ def test_a_corrupt_or_foreign_cache_is_searched_again(tmp_path):
     path.write_text("{not json")
     calls = []
     ch, _ = tune.tune(_fake(lambda j, k, c: float(sum(c)), calls), ((129, 33),), "G", OT2D_FP64, cache_path=str(path))
-    assert ch[(129, 33)] == (0, 4, 0) and calls
+    assert ch[(129, 33)] == (0, 4, 0, 0) and calls
     # a cached choice outside the candidate set is not trusted
     cache = json.load(open(path))
-    cache["G|fp64|129x33"]["choice"] = [7, 3, 99]
+    cache["G|fp64|129x33"]["choice"] = [7, 3, 99, 0]
     path.write_text(json.dumps(cache))
     calls.clear()
     ch, _ = tune.tune(_fake(lambda j, k, c: float(sum(c)), calls), ((129, 33),), "G", OT2D_FP64, cache_path=str(path))
-    assert ch[(129, 33)] == (0, 4, 0) and calls
+    assert ch[(129, 33)] == (0, 4, 0, 0) and calls
 
 
 def test_tuning_table_is_ordered_by_class_and_bounds_array_sizes():
-    t = tune.tuning_table({(513, 129): (1, 8, 4), (129, 33): (2, 4, 0), (257, 65): (0, 8, 0)})
-    rows = [(e.kd_max, e.jd_max, e.rt_shape, e.lu_group, e.lu_lag) for e in t]
-    assert rows == [(34, 130, 2, 4, 0), (66, 258, 0, 8, 0), (130, 514, 1, 8, 4)]
-    assert tune.describe({(129, 33): (2, 4, 0)}) == {"129x33": {"rt_tile": "8x32", "lu_group": 4, "lu_lag": 0}}
+    t = tune.tuning_table({(513, 129): (1, 8, 4, 1), (129, 33): (2, 4, 0, 0), (257, 65): (0, 8, 0, 1)})
+    rows = [(e.kd_max, e.jd_max, e.rt_shape, e.lu_group, e.lu_lag, e.pipeline) for e in t]
+    assert rows == [(34, 130, 2, 4, 0, 0), (66, 258, 0, 8, 0, 1), (130, 514, 1, 8, 4, 1)]
+    assert tune.describe({(129, 33): (2, 4, 0, 1)}) == {"129x33": {"rt_tile": "8x32", "lu_group": 4, "lu_lag": 0,
+                                                                   "pipeline": 1}}

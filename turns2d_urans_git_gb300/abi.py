@@ -79,7 +79,7 @@ class Inputs(C.Structure):
 class Tuning(C.Structure):
     """ot2d_tuning: launch choices for batches of one mesh-size class."""
     _fields_ = [("kd_max", _I), ("jd_max", _I), ("rt_shape", _I), ("lu_group", _I), ("lu_lag", _I),
-                ("reserved", _I)]
+                ("pipeline", _I)]
 
 
 class Result(C.Structure):

@@ -230,7 +230,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   s->dirty = false;
   if (sl.empty()) return OT2D_OK;
   // launch choices: the tuning entry of the batch's largest mesh, else the options
-  ot2d_tuning ch{0, 0, s->rt_shape, s->lu_group, s->lu_lag, 0};
+  ot2d_tuning ch{0, 0, s->rt_shape, s->lu_group, s->lu_lag, s->pipeline};
   {
     size_t best = 0;
     int kd = 0, jd = 0;
@@ -254,7 +254,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   Branch* br = nullptr;   // the turbulence branch's stream, created outside the capture
   if (branch_of_device(br) != cudaSuccess) return OT2D_ERR_CUDA;
   const int visc = s->any_viscous ? 1 : 0;
-  const bool split = s->pipeline && sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= 2;
+  const bool split = ch.pipeline && sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= 2;
   if (!split) {
     if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
     cudaError_t le = launch_iteration<R>(B.d_sl, B.b, visc, s->turb_bits, s->lhs_bits, s->st);
@@ -748,7 +748,9 @@ int ot2d_solver_set_tuning(ot2d_solver* s, const ot2d_tuning* t, int32_t n) {
   for (int i = 0; i < n; ++i) {
     const ot2d_tuning& e = t[i];
     const bool g = e.lu_group == 0 || e.lu_group == 1 || e.lu_group == 2 || e.lu_group == 4 || e.lu_group == 8;
-    if (e.rt_shape < 0 || e.rt_shape >= RT_NSHAPE || !g || e.lu_lag < 0 || e.lu_lag > 64) return OT2D_ERR_ARG;
+    if (e.rt_shape < 0 || e.rt_shape >= RT_NSHAPE || !g || e.lu_lag < 0 || e.lu_lag > 64 ||
+        (e.pipeline != 0 && e.pipeline != 1))
+      return OT2D_ERR_ARG;
   }
   s->tuning.assign(t, t + n);
   s->dirty = true;

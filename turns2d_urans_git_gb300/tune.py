@@ -8,6 +8,9 @@ candidate choice and keeps the fastest:
   lu_group   LU-SGS record chunks streamed per bulk copy (4 or 8)
   lu_lag     LU-SGS hyperplane schedule: steps each 32-row band trails the
              band it depends on beyond the minimum (0 or 4)
+  pipeline   a batch of 16 or more time instances as one graph, or as two
+             halves on two streams with each half's residual beside the
+             other half's sweeps (0 or 1)
 
 Every candidate computes the same state bit for bit (the choices change
 launch geometry and schedule only; the L2 norm's partial sums follow the
@@ -23,13 +26,15 @@ import os
 import statistics
 import time
 
-from .abi import OT2D_FP64, OT2D_FP32_MIXED, OT2D_OPT_LU_GROUP, OT2D_OPT_LU_LAG, OT2D_OPT_RT_SHAPE, Tuning
+from .abi import (OT2D_FP64, OT2D_FP32_MIXED, OT2D_OPT_LU_GROUP, OT2D_OPT_LU_LAG, OT2D_OPT_PIPELINE,
+                  OT2D_OPT_RT_SHAPE, Tuning)
 
 # the mesh sizes of the batched configuration (vertices); a class covers
 # meshes up to its array size (jd = jmax + 1, kd = kmax + 1)
 SIZE_CLASSES = ((129, 33), (257, 65), (385, 97), (513, 129), (769, 193))
 SHAPES = {0: "16x16", 1: "32x8", 2: "8x32"}
-CANDIDATES = tuple((shape, group, lag) for shape in (0, 1, 2) for group in (4, 8) for lag in (0, 4))
+CANDIDATES = tuple((shape, group, lag, pipe) for shape in (0, 1, 2) for group in (4, 8) for lag in (0, 4)
+                   for pipe in (0, 1))
 
 
 def default_cache_path():
@@ -69,14 +74,14 @@ def save_cache(path, cache):
 
 
 def tuning_table(choices):
-    """ot2d_tuning entries from {(jmax, kmax): (shape, group, lag)}, smallest
-    class first (the solver takes the first entry that bounds a batch's
-    largest mesh)."""
+    """ot2d_tuning entries from {(jmax, kmax): (shape, group, lag, pipeline)},
+    smallest class first (the solver takes the first entry that bounds a
+    batch's largest mesh)."""
     rows = sorted(choices.items(), key=lambda kv: (kv[0][1], kv[0][0]))
     table = (Tuning * len(rows))()
-    for t, ((jmax, kmax), (shape, group, lag)) in zip(table, rows):
+    for t, ((jmax, kmax), (shape, group, lag, pipe)) in zip(table, rows):
         t.kd_max, t.jd_max = kmax + 1, jmax + 1
-        t.rt_shape, t.lu_group, t.lu_lag = shape, group, lag
+        t.rt_shape, t.lu_group, t.lu_lag, t.pipeline = shape, group, lag, pipe
     return table
 
 
@@ -104,7 +109,7 @@ def tune(measure_for_class, classes, gpu, precision, cache_path=None, retune=Fal
                 sv.close()
         choices[(jmax, kmax)] = best
         timings[(jmax, kmax)] = times
-        cache[key] = {"choice": list(best), "ms": {"%d,%d,%d" % c: t for c, t in times.items()},
+        cache[key] = {"choice": list(best), "ms": {",".join(str(x) for x in c): t for c, t in times.items()},
                       "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
         changed = True
     if changed:
@@ -132,10 +137,11 @@ def gpu_measure_for_class(precision, batch=16, iters=10, device=0, case_for_clas
             sv.add(prm, xv, yv, orders=0.0, max_iters=10 ** 8)
 
         def measure(c):
-            shape, group, lag = c
+            shape, group, lag, pipe = c
             sv.set_option(OT2D_OPT_RT_SHAPE, shape)
             sv.set_option(OT2D_OPT_LU_GROUP, group)
             sv.set_option(OT2D_OPT_LU_LAG, lag)
+            sv.set_option(OT2D_OPT_PIPELINE, pipe)
             sv.iterate(3)
             st = torch.cuda.ExternalStream(sv.stream())
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -165,4 +171,5 @@ def apply(solver, choices):
 
 
 def describe(choices):
-    return {"%dx%d" % k: {"rt_tile": SHAPES[v[0]], "lu_group": v[1], "lu_lag": v[2]} for k, v in sorted(choices.items())}
+    return {"%dx%d" % k: {"rt_tile": SHAPES[v[0]], "lu_group": v[1], "lu_lag": v[2], "pipeline": v[3]}
+            for k, v in sorted(choices.items())}
