@@ -127,8 +127,28 @@ __global__ void __launch_bounds__(BCE_BS) k_bc_entry(const Slice<R>* __restrict_
 
 // after the entries: the compute copy of the halo ring and its monitor
 template <class R>
+__device__ __forceinline__ void bc_ring_monitor(const Slice<R>& S, int advance);
+template <class R>
 __global__ void __launch_bounds__(BC_BS) k_bc(const Slice<R>* __restrict__ sl, int advance) {
+  bc_ring_monitor(sl[blockIdx.x], advance);
+}
+// All &bcinp entries of a slice in one CTA, in the reference's order with a
+// block barrier between entries (entries share corner cells), then the halo
+// ring and its monitor: one launch instead of one per entry for the mixed
+// path, whose boundary arithmetic is f32 (the FP64 path keeps several CTAs
+// per entry: its boundary arithmetic runs on the narrow FP64 pipe).
+template <class R>
+__global__ void __launch_bounds__(BC_BS) k_bc_all(const Slice<R>* __restrict__ sl, int advance) {
   const Slice<R>& S = sl[blockIdx.x];
+  const int istep0 = S.ist ? S.ist[0] : S.P->istep0;
+  for (int ib = 0; ib < S.nbc; ++ib) {
+    bc_entry(S, istep0, ib, threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
+  bc_ring_monitor(S, advance);
+}
+template <class R>
+__device__ __forceinline__ void bc_ring_monitor(const Slice<R>& S, int advance) {
   widen_ring(S, 1, 4);
   // monitor of the halo ring just set (the interior is checked by k_update)
   if (S.ist && advance) {

@@ -28,9 +28,13 @@ template <class R>
 cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st) {
   // one launch per &bcinp entry (the reference applies them in order), each
   // spread over enough CTAs per slice to cover the longest boundary
-  const int nch = (std::max(b.max_wall, b.max_kd) + BCE_BS - 1) / BCE_BS;
-  for (int ib = 0; ib < b.max_nbc; ++ib) k_bc_entry<R><<<dim3(nch, b.nslice), BCE_BS, 0, st>>>(d_sl, ib);
-  k_bc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, advance);
+  if constexpr (sizeof(R) == sizeof(float)) {
+    k_bc_all<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, advance);
+  } else {
+    const int nch = (std::max(b.max_wall, b.max_kd) + BCE_BS - 1) / BCE_BS;
+    for (int ib = 0; ib < b.max_nbc; ++ib) k_bc_entry<R><<<dim3(nch, b.nslice), BCE_BS, 0, st>>>(d_sl, ib);
+    k_bc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, advance);
+  }
   return cudaGetLastError();
 }
 // the fused residual tiles: the plain instantiation always, the
