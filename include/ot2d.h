@@ -332,6 +332,10 @@ void* ot2d_solver_stream(ot2d_solver* s);
  * norms in one tiled kernel), 3 rbc, 4 LU-SGS, 5 SA, 6 update + monitor. */
 #define OT2D_NPHASE 7
 int ot2d_solver_profile(ot2d_solver* s, int32_t iters, double* ms, int32_t nphase);
+/* Kernel launches of one batched iteration: the kernel nodes of the
+ * iteration's CUDA graph (both graphs when the batch runs as two halves),
+ * after building it for the live set; negative status on error. */
+int ot2d_solver_graph_kernels(ot2d_solver* s);
 /* Host-resident state, as a Fortran caller that owns q: every iteration
  * copies q(jd,kd,nspec,nq) of the listed live instances host->device, runs
  * one batched iteration and copies q back (the host arrays are updated). */

@@ -52,6 +52,7 @@ def lib():
         L.ot2d_instance_bytes.restype = C.c_size_t
         L.ot2d_solver_queued.argtypes = [C.c_void_p]
         L.ot2d_solver_stream.argtypes = [C.c_void_p]
+        L.ot2d_solver_graph_kernels.argtypes = [C.c_void_p]
         L.ot2d_solver_stream.restype = C.c_void_p
         _lib = L
     return _lib
@@ -320,6 +321,14 @@ class Solver:
 
     def stream(self):
         return lib().ot2d_solver_stream(self._h)
+
+    def graph_kernels(self):
+        """Kernel launches per batched iteration (kernel nodes of the
+        iteration's CUDA graph for the current live set)."""
+        n = lib().ot2d_solver_graph_kernels(self._h)
+        if n < 0:
+            raise RuntimeError("ot2d_solver_graph_kernels failed (%d)" % -n)
+        return n
 
 
 def instance_bytes(prm, precision):

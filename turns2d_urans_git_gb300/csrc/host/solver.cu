@@ -850,6 +850,30 @@ int ot2d_solver_profile(ot2d_solver* s, int32_t iters, double* ms, int32_t nphas
   return s->precision == OT2D_FP64 ? profile_t<double>(s, s->b64, iters, ms) : profile_t<float>(s, s->b32, iters, ms);
 }
 
+static int kernel_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  if (!g || cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return -OT2D_ERR_CUDA;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (n && cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return -OT2D_ERR_CUDA;
+  int k = 0;
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) != cudaSuccess) return -OT2D_ERR_CUDA;
+    if (t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
+int ot2d_solver_graph_kernels(ot2d_solver* s) {
+  if (!s) return -OT2D_ERR_ARG;
+  cudaSetDevice(s->device);
+  if (s->dirty) { int e = rebuild(s); if (e) return -e; }
+  if (s->live.empty()) return 0;
+  if (!s->split) return kernel_nodes(s->graph);
+  const int a = kernel_nodes(s->hgraph[0]), b = kernel_nodes(s->hgraph[1]);
+  return a < 0 ? a : (b < 0 ? b : a + b);
+}
+
 int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, double* const* q_host, int32_t iters) {
   if (!s || n < 0 || (n && (!ids || !q_host)) || iters < 0) return OT2D_ERR_ARG;
   cudaSetDevice(s->device);

@@ -66,12 +66,32 @@ struct RtSmem {
 // Stage A: cell (j,k) of the staged region -> primitive f of rhsup
 // (eulerrhs.f:55-61, :71-79), viscous cell factors of visrhs
 // (visrhs.f:48-60), the q2/q1-style divided velocities of its cross terms
-// (visrhs.f:77-89), metrics and |iblank|.
-template <class R, class SM>
-__device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_params& p, const SM& sm, int r,
-                                              int j, int k, bool visc) {
+// (visrhs.f:77-89), metrics and |iblank|.  Split in a load (RtRaw) and a
+// convert-and-store so that a thread issues the loads of all its staged
+// cells before it waits for the first.
+template <class R>
+struct RtRaw {
+  R q1, q2, q3, q4, J, turm, xx, xy, yx, yy;
+  int ib;
+};
+
+template <class R>
+__device__ __forceinline__ void rt_load_cell(const Slice<R>& S, const ot2d_params& p, int j, int k, bool visc,
+                                             RtRaw<R>& a) {
   const int64_t o = at(S.jd, j, k), qs = S.qs;
-  const R q1 = S.q[o], q2 = S.q[qs + o], q3 = S.q[2 * qs + o], q4 = S.q[3 * qs + o], J = S.q[(p.nq - 1) * qs + o];
+  a.q1 = S.q[o]; a.q2 = S.q[qs + o]; a.q3 = S.q[2 * qs + o]; a.q4 = S.q[3 * qs + o];
+  a.J = S.q[(p.nq - 1) * qs + o];
+  if (visc) {
+    a.turm = S.turmu[o];
+    a.xx = S.xx[o]; a.xy = S.xy[o]; a.yx = S.yx[o]; a.yy = S.yy[o];
+  }
+  a.ib = S.iblank[o];
+}
+
+template <class R, class SM>
+__device__ __forceinline__ void rt_store_cell(const Slice<R>& S, const SM& sm, int r, const RtRaw<R>& a,
+                                              bool visc) {
+  const R q1 = a.q1, q2 = a.q2, q3 = a.q3, q4 = a.q4, J = a.J;
   const R gm1 = S.k_gm1;
   const R rhoi = (R)1.0 / q1;
   sm.at(RS_RHO, r) = q1 * J;
@@ -85,7 +105,7 @@ __device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_para
     const R e = q4 * rhoi - (R).5 * (sq(u) + sq(v));
     const R tt = S.k_ggm1 * e;
     const R vmue = c2bp * tt * sqrt(tt) / (c2b + tt);
-    const R turm = S.turmu[o];
+    const R turm = a.turm;
     sm.at(RS_E, r) = e;
     sm.at(RS_VNU, r) = vmue + turm;
     sm.at(RS_GKAP, r) = vmue + prtr * turm;
@@ -94,10 +114,9 @@ __device__ __forceinline__ void rt_stage_cell(const Slice<R>& S, const ot2d_para
     sm.at(RS_UD, r) = ud;
     sm.at(RS_VD, r) = vd;
     sm.at(RS_ED, r) = q4 / q1 - (R).5 * (sq(ud) + sq(vd));
-    sm.at(RS_XX, r) = S.xx[o]; sm.at(RS_XY, r) = S.xy[o]; sm.at(RS_YX, r) = S.yx[o]; sm.at(RS_YY, r) = S.yy[o];
+    sm.at(RS_XX, r) = a.xx; sm.at(RS_XY, r) = a.xy; sm.at(RS_YX, r) = a.yx; sm.at(RS_YY, r) = a.yy;
   }
-  const int ib = S.iblank[o];
-  const int ia = ib < 0 ? -ib : ib;
+  const int ia = a.ib < 0 ? -a.ib : a.ib;
   sm.iba[r] = (uint8_t)(ia > 255 ? 255 : ia);
 }
 
@@ -284,32 +303,48 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R, TJ, TK>& sm, int t
   const bool inv = flags & AS_INV;
   const R gm1 = S.k_gm1;
   const Recon<R> rx{p.ilim, S.k_th, S.k_qt, S.k_epsl_x, S.k_mp2}, ry{p.ilim, S.k_th, S.k_qt, S.k_epsl_y, S.k_mp2};
-  // A: stage the region
-  for (int r = t; r < G::NR; r += RT_BS) {
-    const int j = jr + r % G::RW, k = kr + r / G::RW;
-    if (j >= 1 && j <= jd && k >= 1 && k <= kd) rt_stage_cell(S, p, sm, r, j, k, visc);
+  const int nB = inv ? TK * (TJ + 1) : 0, nC = inv ? (TK + 1) * TJ : 0;
+  // A: stage the region.  A thread issues the loads of all its staged cells
+  // before it converts and stores the first, so that their latencies
+  // overlap (one round trip to memory per thread instead of one per cell).
+  {
+    constexpr int NST = (G::NR + RT_BS - 1) / RT_BS;
+    RtRaw<R> raw[NST];
+#pragma unroll
+    for (int i = 0; i < NST; ++i) {
+      const int r = t + i * RT_BS;
+      const int j = jr + r % G::RW, k = kr + r / G::RW;
+      if (r < G::NR && j >= 1 && j <= jd && k >= 1 && k <= kd) rt_load_cell(S, p, j, k, visc, raw[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < NST; ++i) {
+      const int r = t + i * RT_BS;
+      const int j = jr + r % G::RW, k = kr + r / G::RW;
+      if (r < G::NR && j >= 1 && j <= jd && k >= 1 && k <= kd) rt_store_cell(S, sm, r, raw[i], visc);
+    }
   }
   __syncthreads();
   // B-D: every face quantity of the tile, as one work list so that the
   // threads stay busy across the four kinds
-  const int nB = inv ? TK * (TJ + 1) : 0, nC = inv ? (TK + 1) * TJ : 0;
   const int nD1 = visc ? G::VEH * TJ : 0, nD2 = visc ? TK * G::VXW : 0;
   const int ntot = nB + nC + nD1 + nD2;
   const R gkpr = S.k_gkpr, dre = S.k_dre;
   for (int w = t; w < ntot; w += RT_BS) {
-    if (w < nB) {
-      // B: xi face j+1/2 of row k, j in j0-1..j1 (eulerrhs.f:69-167)
-      const int f = w;
-      const int kk = f / (TJ + 1), jf = f % (TJ + 1);
-      const int j = j0 - 1 + jf, k = k0 + kk;
-      if (j > j1 || k > k1) continue;
-      const RtLine<R, SM> L{&sm, (k - kr) * G::RW - jr, 1, max(1, jr), min(jd, jr + G::RW - 1), gm1};
-      const int64_t o = at(jd, j, k);
+    if (w < nB + nC) {
       R fl[4];
-      face_flux_t<LIM, R, RtLine<R, SM>, PRE>(L, rx, j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
+      if (w < nB) {
+        // B: xi face j+1/2 of row k, j in j0-1..j1 (eulerrhs.f:69-167)
+        const int f = w;
+        const int kk = f / (TJ + 1), jf = f % (TJ + 1);
+        const int j = j0 - 1 + jf, k = k0 + kk;
+        if (j > j1 || k > k1) continue;
+        const RtLine<R, SM> L{&sm, (k - kr) * G::RW - jr, 1, max(1, jr), min(jd, jr + G::RW - 1), gm1};
+        const int64_t o = at(jd, j, k);
+        face_flux_t<LIM, R, RtLine<R, SM>, PRE>(L, rx, j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) sm.F[v * (TK * (TJ + 1)) + f] = fl[v];
-    } else if (w < nB + nC) {
+        for (int v = 0; v < 4; ++v) sm.F[v * (TK * (TJ + 1)) + f] = fl[v];
+        continue;
+      }
       // C: eta face k+1/2 of column j, k in k0-1..k1 (eulerrhs.f:170-268)
       const int f = w - nB;
       const int kf = f / TJ, jj = f % TJ;
@@ -317,7 +352,6 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R, TJ, TK>& sm, int t
       if (j > j1 || k > k1) continue;
       const RtLine<R, SM> L{&sm, (j - jr) - kr * G::RW, G::RW, max(1, kr), min(kd, kr + G::RH - 1), gm1};
       const int64_t o = at(jd, j, k);
-      R fl[4];
       face_flux_t<LIM, R, RtLine<R, SM>, PRE>(L, ry, k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sm.G_[v * ((TK + 1) * TJ) + f] = fl[v];
