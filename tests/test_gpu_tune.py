@@ -3,6 +3,8 @@ shape, LU-SGS copy group, LU-SGS band lag) gives the same state bit for bit,
 in FP64 and in the FP32-mixed path (the L2 norm's partial sums follow the
 tile shape, so the norms agree to rounding), and a tuning table handed to
 the solver is applied to the batch of its size class."""
+import json
+
 import numpy as np
 import pytest
 
@@ -77,5 +79,6 @@ def test_gpu_tune_one_class_caches_a_candidate(tmp_path):
                                  OT2D_FP32_MIXED, cache_path=path)
     assert choices[(129, 33)] in tune.CANDIDATES
     assert all(t > 0 for t in timings[(129, 33)].values())
-    again, t2 = tune.tune(None, ((129, 33),), gpu, OT2D_FP32_MIXED, cache_path=path)
+    again, t2 = tune.tune(None, ((129, 33),), gpu, OT2D_FP32_MIXED, cache_path=path, batch=4)
     assert again == choices and t2[(129, 33)] is None
+    assert set(json.load(open(path))) == {tune.class_key(gpu, OT2D_FP32_MIXED, 129, 33, 4)}

@@ -70,3 +70,20 @@ def test_tuning_table_is_ordered_by_class_and_bounds_array_sizes():
     assert rows == [(34, 130, 2, 4, 0, 0), (66, 258, 0, 8, 0, 1), (130, 514, 1, 8, 4, 1)]
     assert tune.describe({(129, 33): (2, 4, 0, 1)}) == {"129x33": {"rt_tile": "8x32", "lu_group": 4, "lu_lag": 0,
                                                                    "pipeline": 1}}
+
+
+def test_the_batch_of_a_search_is_part_of_its_key(tmp_path):
+    """Searches at two batch sizes are cached apart; the batch comes from the
+    measuring function or is given."""
+    path = str(tmp_path / "t.json")
+    calls = []
+    m = _fake(lambda j, k, c: 1.0 + c[3], calls)
+    m.batch = 16
+    ch16, _ = tune.tune(m, ((513, 129),), "G", OT2D_FP32_MIXED, cache_path=path)
+    m64 = _fake(lambda j, k, c: 2.0 - c[3], calls)
+    ch64, _ = tune.tune(m64, ((513, 129),), "G", OT2D_FP32_MIXED, cache_path=path, batch=64)
+    assert ch16[(513, 129)][3] == 0 and ch64[(513, 129)][3] == 1
+    assert set(json.load(open(path))) == {"G|fp32-mixed|513x129|b16", "G|fp32-mixed|513x129|b64"}
+    calls.clear()
+    again, t = tune.tune(None, ((513, 129),), "G", OT2D_FP32_MIXED, cache_path=path, batch=64)
+    assert again == ch64 and t[(513, 129)] is None and not calls

@@ -12,6 +12,12 @@ candidate choice and keeps the fastest:
              halves on two streams with each half's residual beside the
              other half's sweeps (0 or 1)
 
+The fastest choice depends on the batch as well as on the mesh: the
+pipelined halves pay off when the sweeps of a small batch leave most SMs
+idle, and not at 64 instances of 513x129.  A search is therefore made at a
+stated batch size (the measuring function's `batch`), and that size is part
+of the cache key; a caller tunes at the batch it serves.
+
 Every candidate computes the same state bit for bit (the choices change
 launch geometry and schedule only; the L2 norm's partial sums follow the
 residual tile, so the norms agree to rounding), so the search is free to
@@ -42,8 +48,9 @@ def default_cache_path():
     return os.path.join(root, "turns2d_gb300", "tuning.json")
 
 
-def class_key(gpu, precision, jmax, kmax):
-    return "%s|%s|%dx%d" % (gpu, "fp64" if precision == OT2D_FP64 else "fp32-mixed", jmax, kmax)
+def class_key(gpu, precision, jmax, kmax, batch=None):
+    key = "%s|%s|%dx%d" % (gpu, "fp64" if precision == OT2D_FP64 else "fp32-mixed", jmax, kmax)
+    return key + ("|b%d" % batch if batch else "")
 
 
 def search(candidates, measure, repeats=3):
@@ -85,16 +92,20 @@ def tuning_table(choices):
     return table
 
 
-def tune(measure_for_class, classes, gpu, precision, cache_path=None, retune=False):
+def tune(measure_for_class, classes, gpu, precision, cache_path=None, retune=False, batch=None):
     """Choices for every class: from the cache, or searched with
     measure_for_class(jmax, kmax) -> measure(candidate) and then cached.
+    `batch` (default: measure_for_class.batch, if it has one) is the batch
+    size the search runs at, part of the cache key.
     Returns ({(jmax, kmax): choice}, {class: timings or None if cached})."""
+    if batch is None:
+        batch = getattr(measure_for_class, "batch", None)
     cache_path = cache_path or default_cache_path()
     cache = load_cache(cache_path)
     choices, timings = {}, {}
     changed = False
     for (jmax, kmax) in classes:
-        key = class_key(gpu, precision, jmax, kmax)
+        key = class_key(gpu, precision, jmax, kmax, batch)
         hit = cache.get(key)
         if hit and not retune and tuple(hit["choice"]) in CANDIDATES:
             choices[(jmax, kmax)] = tuple(hit["choice"])
@@ -155,6 +166,7 @@ def gpu_measure_for_class(precision, batch=16, iters=10, device=0, case_for_clas
         measure.solver = sv
         return measure
 
+    for_class.batch = batch
     return for_class
 
 
