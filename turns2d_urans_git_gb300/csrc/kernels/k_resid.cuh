@@ -63,6 +63,43 @@ struct RtSmem {
   __device__ __forceinline__ R& at(int a, int r) const { return c[(size_t)a * G::NR + r]; }
 };
 
+// Phase B-D work in warp tasks of 32 items: the inviscid faces (the xi
+// faces of the tile's rows, then the eta faces of its columns: one kind,
+// since the same reconstruction and flux code serves a line of either
+// direction) and the viscous terms (eta, then xi).  Tasks are dealt to the
+// warps longest first, each to the least loaded warp, with a face task
+// counted as three viscous ones: no warp mixes face and viscous code, and
+// the slowest warp carries about the mean load.  code[w] lists warp w's
+// tasks, 7 bits each (task + 1), first task in the lowest bits.
+template <int TJ, int TK>
+struct RtTasks {
+  using G = RtGeo<TJ, TK>;
+  static constexpr int NW = RT_BS / 32;
+  static constexpr int FB = TK * (TJ + 1);                    // xi faces
+  static constexpr int NF = FB + (TK + 1) * TJ;               // + eta faces
+  static constexpr int NFT = (NF + 31) / 32;
+  static constexpr int NVT = (G::VEH * TJ + TK * G::VXW + 31) / 32;
+  uint64_t code[NW];
+  int most;                                                   // most tasks of a warp
+};
+template <int TJ, int TK>
+__host__ __device__ constexpr RtTasks<TJ, TK> rt_tasks() {
+  using T = RtTasks<TJ, TK>;
+  T s{};
+  int load[T::NW] = {}, cnt[T::NW] = {};
+  for (int task = 0; task < T::NFT + T::NVT; ++task) {
+    int w = 0;
+    for (int i = 1; i < T::NW; ++i)
+      if (load[i] < load[w]) w = i;
+    if (cnt[w] < 9) s.code[w] |= (uint64_t)(task + 1) << (7 * cnt[w]);
+    ++cnt[w];
+    load[w] += task < T::NFT ? 3 : 1;
+  }
+  for (int i = 0; i < T::NW; ++i)
+    if (cnt[i] > s.most) s.most = cnt[i];
+  return s;
+}
+
 // Stage A: cell (j,k) of the staged region -> primitive f of rhsup
 // (eulerrhs.f:55-61, :71-79), viscous cell factors of visrhs
 // (visrhs.f:48-60), the q2/q1-style divided velocities of its cross terms
@@ -303,7 +340,6 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R, TJ, TK>& sm, int t
   const bool inv = flags & AS_INV;
   const R gm1 = S.k_gm1;
   const Recon<R> rx{p.ilim, S.k_th, S.k_qt, S.k_epsl_x, S.k_mp2}, ry{p.ilim, S.k_th, S.k_qt, S.k_epsl_y, S.k_mp2};
-  const int nB = inv ? TK * (TJ + 1) : 0, nC = inv ? (TK + 1) * TJ : 0;
   // A: stage the region.  A thread issues the loads of all its staged cells
   // before it converts and stores the first, so that their latencies
   // overlap (one round trip to memory per thread instead of one per cell).
@@ -324,57 +360,67 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R, TJ, TK>& sm, int t
     }
   }
   __syncthreads();
-  // B-D: every face quantity of the tile, as one work list so that the
-  // threads stay busy across the four kinds
+  // B-D: every face quantity of the tile, in warp tasks (RtTasks)
+  using TS = RtTasks<TJ, TK>;
+  constexpr TS tasks = rt_tasks<TJ, TK>();
+  static_assert(tasks.most <= 9, "a warp's task list must fit 63 bits");
   const int nD1 = visc ? G::VEH * TJ : 0, nD2 = visc ? TK * G::VXW : 0;
-  const int ntot = nB + nC + nD1 + nD2;
   const R gkpr = S.k_gkpr, dre = S.k_dre;
-  for (int w = t; w < ntot; w += RT_BS) {
-    if (w < nB + nC) {
-      R fl[4];
-      if (w < nB) {
-        // B: xi face j+1/2 of row k, j in j0-1..j1 (eulerrhs.f:69-167)
-        const int f = w;
-        const int kk = f / (TJ + 1), jf = f % (TJ + 1);
-        const int j = j0 - 1 + jf, k = k0 + kk;
-        if (j > j1 || k > k1) continue;
-        const RtLine<R, SM> L{&sm, (k - kr) * G::RW - jr, 1, max(1, jr), min(jd, jr + G::RW - 1), gm1};
-        const int64_t o = at(jd, j, k);
-        face_flux_t<LIM, R, RtLine<R, SM>, PRE>(L, rx, j, jd, S.fxa[o], S.fya[o], S.ftj ? S.ftj[o] : (R)0.0, fl);
+  const int lane = t & 31;
+  uint64_t code = 0;
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sm.F[v * (TK * (TJ + 1)) + f] = fl[v];
-        continue;
-      }
+  for (int i = 0; i < TS::NW; ++i)
+    if (i == (t >> 5)) code = tasks.code[i];
+  for (; code; code >>= 7) {
+    const int task = (int)(code & 127) - 1;
+    if (task < TS::NFT) {
+      if (!inv) continue;
+      const int f = task * 32 + lane;
+      if (f >= TS::NF) continue;
+      // B: xi face j+1/2 of row k, j in j0-1..j1 (eulerrhs.f:69-167);
       // C: eta face k+1/2 of column j, k in k0-1..k1 (eulerrhs.f:170-268)
-      const int f = w - nB;
-      const int kf = f / TJ, jj = f % TJ;
-      const int j = j0 + jj, k = k0 - 1 + kf;
+      const bool xi = f < TS::FB;
+      const int g = xi ? f : f - TS::FB;
+      const int j = xi ? j0 - 1 + g % (TJ + 1) : j0 + g % TJ;
+      const int k = xi ? k0 + g / (TJ + 1) : k0 - 1 + g / TJ;
       if (j > j1 || k > k1) continue;
-      const RtLine<R, SM> L{&sm, (j - jr) - kr * G::RW, G::RW, max(1, kr), min(kd, kr + G::RH - 1), gm1};
+      const RtLine<R, SM> L = xi ? RtLine<R, SM>{&sm, (k - kr) * G::RW - jr, 1, max(1, jr), min(jd, jr + G::RW - 1), gm1}
+                                 : RtLine<R, SM>{&sm, (j - jr) - kr * G::RW, G::RW, max(1, kr), min(kd, kr + G::RH - 1),
+                                                 gm1};
+      const Recon<R> rc = xi ? rx : ry;
       const int64_t o = at(jd, j, k);
-      face_flux_t<LIM, R, RtLine<R, SM>, PRE>(L, ry, k, kd, S.gxa[o], S.gya[o], S.gtj ? S.gtj[o] : (R)0.0, fl);
+      const R* ma = xi ? S.fxa : S.gxa;
+      const R* mb = xi ? S.fya : S.gya;
+      const R* mc = xi ? S.ftj : S.gtj;
+      R fl[4];
+      face_flux_t<LIM, R, RtLine<R, SM>, PRE>(L, rc, xi ? j : k, xi ? jd : kd, ma[o], mb[o], mc ? mc[o] : (R)0.0, fl);
+      R* dst = xi ? sm.F + g : sm.G_ + g;
+      const int vs = xi ? TS::FB : (TK + 1) * TJ;
 #pragma unroll
-      for (int v = 0; v < 4; ++v) sm.G_[v * ((TK + 1) * TJ) + f] = fl[v];
-    } else if (w < nB + nC + nD1) {
-      // D1: eta viscous terms at k0-2..k1+1 of columns j0..j1
-      const int f = w - nB - nC;
-      const int kf = f / TJ, jj = f % TJ;
-      const int j = j0 + jj, k = k0 - 2 + kf;
-      if (j > j1 || k < 1 || k > kd - 1 || k > k1 + 1) continue;
-      R out[6];
-      rt_visc_eta(sm, (k - kr) * G::RW + (j - jr), gkpr, dre, out);
-#pragma unroll
-      for (int v = 0; v < 6; ++v) sm.VE[v * (G::VEH * TJ) + f] = out[v];
+      for (int v = 0; v < 4; ++v) dst[v * vs] = fl[v];
     } else {
-      // D2: xi viscous terms at j0-2..j1+1 of rows k0..k1
-      const int f = w - nB - nC - nD1;
-      const int kk = f / G::VXW, jf = f % G::VXW;
-      const int j = j0 - 2 + jf, k = k0 + kk;
-      if (k > k1 || j < 1 || j > jd - 1 || j > j1 + 1) continue;
-      R out[6];
-      rt_visc_xi(sm, (k - kr) * G::RW + (j - jr), gkpr, dre, out);
+      const int d = (task - TS::NFT) * 32 + lane;
+      if (d < nD1) {
+        // D1: eta viscous terms at k0-2..k1+1 of columns j0..j1
+        const int f = d;
+        const int kf = f / TJ, jj = f % TJ;
+        const int j = j0 + jj, k = k0 - 2 + kf;
+        if (j > j1 || k < 1 || k > kd - 1 || k > k1 + 1) continue;
+        R out[6];
+        rt_visc_eta(sm, (k - kr) * G::RW + (j - jr), gkpr, dre, out);
 #pragma unroll
-      for (int v = 0; v < 6; ++v) sm.VX[v * (TK * G::VXW) + f] = out[v];
+        for (int v = 0; v < 6; ++v) sm.VE[v * (G::VEH * TJ) + f] = out[v];
+      } else if (d < nD1 + nD2) {
+        // D2: xi viscous terms at j0-2..j1+1 of rows k0..k1
+        const int f = d - nD1;
+        const int kk = f / G::VXW, jf = f % G::VXW;
+        const int j = j0 - 2 + jf, k = k0 + kk;
+        if (k > k1 || j < 1 || j > jd - 1 || j > j1 + 1) continue;
+        R out[6];
+        rt_visc_xi(sm, (k - kr) * G::RW + (j - jr), gkpr, dre, out);
+#pragma unroll
+        for (int v = 0; v < 6; ++v) sm.VX[v * (TK * G::VXW) + f] = out[v];
+      }
     }
   }
   __syncthreads();
