@@ -77,3 +77,34 @@ def test_pipelined_host_buffer_path_matches():
         sv.close()
     for qa, qb in zip(qs[0], qs[1]):
         assert np.array_equal(qa, qb)
+
+
+@pytest.mark.parametrize("precision", [OT2D_FP64, OT2D_FP32_MIXED])
+@pytest.mark.parametrize("pipeline", [0, 1])
+def test_graph_iteration_is_bitwise_the_sequential_phase_order(precision, pipeline):
+    """The captured iteration runs the turbulence solve on a second stream,
+    beside the LU-SGS sweeps (and, in the mixed path, its first part beside
+    the LU-SGS records as well).  ot2d_solver_profile runs the same
+    iterations one phase after the other in step.f's order (residual, rbc,
+    ilu2d, turbulence, update) on one stream; both give the same bits, so
+    the branches share no data that one writes while the other reads."""
+    cases = _cases(18)
+    n = 12
+    sv = api.Solver(precision, check_every=10 ** 6, keep_q=True)
+    sv.set_option(OT2D_OPT_PIPELINE, pipeline)
+    ids = [sv.add(c[1], c[2], c[3], orders=0.0, max_iters=10 ** 6) for c in cases]
+    sv.iterate(n)
+    sv.sync()
+    graph = [sv.get_q(i, c[1]) for i, c in zip(ids, cases)]
+    sv.close()
+    sv = api.Solver(precision, check_every=10 ** 6, keep_q=True)
+    ids = [sv.add(c[1], c[2], c[3], orders=0.0, max_iters=10 ** 6) for c in cases]
+    L = api.lib()
+    L.ot2d_solver_profile.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int32]
+    ms = (C.c_double * 7)()
+    assert L.ot2d_solver_profile(sv._h, n, ms, 7) == 0
+    sv.sync()
+    seq = [sv.get_q(i, c[1]) for i, c in zip(ids, cases)]
+    sv.close()
+    for a, b in zip(graph, seq):
+        assert np.array_equal(a, b)
