@@ -108,3 +108,51 @@ def test_graph_iteration_is_bitwise_the_sequential_phase_order(precision, pipeli
     sv.close()
     for a, b in zip(graph, seq):
         assert np.array_equal(a, b)
+
+
+def _host_iterate(sv, ids, cases, steps):
+    qh = [np.ascontiguousarray(sv.get_q(i, cases[k][1])) for k, i in ids]
+    ptrs = (C.POINTER(C.c_double) * len(qh))(*[q.ctypes.data_as(C.POINTER(C.c_double)) for q in qh])
+    idarr = (C.c_int32 * len(ids))(*[i for _, i in ids])
+    L = api.lib()
+    L.ot2d_solver_iterate_host.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32),
+                                           C.POINTER(C.POINTER(C.c_double)), C.c_int32]
+    assert L.ot2d_solver_iterate_host(sv._h, len(ids), idarr, ptrs, steps) == 0
+    return qh
+
+
+@pytest.mark.parametrize("precision", [OT2D_FP64, OT2D_FP32_MIXED])
+@pytest.mark.parametrize("retire", [0, 3, 8])
+def test_host_buffer_path_equals_device_path(precision, retire):
+    """ot2d_solver_iterate_host on a batch of 23 time instances (20
+    requests of one, one of three) overlaps one half's copies with the
+    other half's iteration.  Listed requests end with the bits of the
+    device-resident iterations (their host buffers and the device state
+    alike).  `retire` unlisted requests stop after 3 iterations: with 3 the
+    batch keeps its halves, with 8 it falls to 15 instances, below the
+    halves' size, and the call finishes in the single graph."""
+    cases = _cases(20)          # 20 single-instance requests + one of 3 time instances
+    steps = 8
+    short = set(range(retire))  # unlisted requests capped at 3 iterations
+    out = {}
+    for path in ("device", "host"):
+        sv = api.Solver(precision, check_every=1, keep_q=True)
+        ids = [sv.add(c[1], c[2], c[3], orders=0.0, max_iters=3 if k in short else 1000)
+               for k, c in enumerate(cases)]
+        listed = [(k, i) for k, i in enumerate(ids) if k not in short]
+        if path == "device":
+            sv.iterate(steps)
+            sv.sync()
+            host = None
+        else:
+            host = _host_iterate(sv, listed, cases, steps)
+            sv.sync()
+        out[path] = ([sv.get_q(i, cases[k][1]) for k, i in listed], host)
+        for k, i in enumerate(ids):
+            r = sv.result(i)
+            assert r.status == 0 and (k not in short or r.iterations == 3)
+        sv.close()
+    dev, _ = out["device"]
+    hq, hb = out["host"]
+    for a, b, c in zip(dev, hq, hb):
+        assert np.array_equal(a, b) and np.array_equal(a, c)

@@ -44,6 +44,7 @@ struct Rec {
   long force_at = 0;       // iteration count of the last force sample
   std::string store_dir;   // ot2d_solver_store_on_retire: written when retired
   bool queued = false;     // submitted, waiting for device memory
+  int half = -1;           // its half of the batch when the batch has halves
 };
 constexpr int FORCE_WIN = 8;
 
@@ -107,7 +108,9 @@ struct ot2d_solver {
   // is done, so one half's residual fills the SMs the other half's LU-SGS
   // sweeps leave idle.
   int pipeline = 1;
-  bool split = false;
+  bool split = false;        // the device-resident iteration runs as the halves
+  bool halves = false;       // the halves' graphs exist (split, or for the host-buffer path)
+  bool want_halves = false;  // the host-buffer path asked for them
   DevBatch<double> h64[2];
   DevBatch<float> h32[2];
   cudaGraph_t hgraph[2] = {nullptr, nullptr};
@@ -115,6 +118,7 @@ struct ot2d_solver {
   cudaStream_t st2 = nullptr;
   cudaEvent_t ev_half[2] = {nullptr, nullptr};   // recorded in each half's graph after its rbc
   cudaEvent_t ev_join = nullptr;
+  cudaEvent_t ev_hdone[2] = {nullptr, nullptr};  // host-buffer path: a half's iteration done
   int next_id = 0;
   double t0 = 0;
   int check_every = 25;
@@ -185,6 +189,7 @@ void drop_graph(ot2d_solver* s) {
     s->hexec[h] = nullptr; s->hgraph[h] = nullptr;
   }
   s->split = false;
+  s->halves = false;
 }
 
 // batches of at least this many slices run as two pipelined halves
@@ -254,14 +259,18 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   Branch* br = nullptr;   // the turbulence branch's stream, created outside the capture
   if (branch_of_device(br) != cudaSuccess) return OT2D_ERR_CUDA;
   const int visc = s->any_viscous ? 1 : 0;
-  const bool split = ch.pipeline && sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= 2;
+  const bool can_split = sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= 2;
+  const bool split = ch.pipeline && can_split;
+  for (int id : s->live) s->recs[id].half = -1;
   if (!split) {
     if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
     cudaError_t le = launch_iteration<R>(B.d_sl, B.b, visc, s->turb_bits, s->lhs_bits, s->st);
     cudaError_t ce = cudaStreamEndCapture(s->st, &s->graph);
     if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
     if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
-    return OT2D_OK;
+    // the host-buffer path overlaps one half's copies with the other
+    // half's iteration, so it wants the halves' graphs as well
+    if (!(s->want_halves && can_split)) return OT2D_OK;
   }
   // two halves of about equal cells (a request's time instances stay in one
   // half: the time-spectral source couples them)
@@ -274,6 +283,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
     const int h = load[0] <= load[1] ? 0 : 1;
     load[h] += cells_of(id);
     slices_of<R>(s, s->recs[id], slh[h]);
+    s->recs[id].half = h;
   }
   if (!s->st2 && cudaStreamCreateWithFlags(&s->st2, cudaStreamNonBlocking) != cudaSuccess) return OT2D_ERR_CUDA;
   for (int h = 0; h < 2; ++h)
@@ -294,7 +304,8 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
     if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
     if (cudaGraphInstantiate(&s->hexec[h], s->hgraph[h], 0) != cudaSuccess) return OT2D_ERR_CUDA;
   }
-  s->split = true;
+  s->halves = true;
+  s->split = split;
   return OT2D_OK;
 }
 
@@ -695,6 +706,8 @@ void ot2d_solver_destroy(ot2d_solver* s) {
     if (s->ev_half[h]) cudaEventDestroy(s->ev_half[h]);
   }
   if (s->ev_join) cudaEventDestroy(s->ev_join);
+  for (int h = 0; h < 2; ++h)
+    if (s->ev_hdone[h]) cudaEventDestroy(s->ev_hdone[h]);
   if (s->st2) cudaStreamDestroy(s->st2);
   for (auto& kv : s->recs) solve_destroy(kv.second.d);
   for (cudaEvent_t e : s->ev_d2h) cudaEventDestroy(e);
@@ -874,6 +887,74 @@ int ot2d_solver_graph_kernels(ot2d_solver* s) {
   return a < 0 ? a : (b < 0 ? b : a + b);
 }
 
+// Host-buffer iterations over a batch with halves: per iteration, half h
+// uploads its listed instances on its stream (each upload after that
+// instance's previous download), makes its compute copy, runs its graph
+// (after the other half's residual, as in the device-resident pipelined
+// iteration) and downloads its instances on the download stream.  Half 1's
+// uploads thus overlap half 0's iteration, and half 0's downloads half 1's
+// iteration; every instance computes what it computes in the single graph.
+int iterate_host_halves(ot2d_solver* s, int32_t n, std::vector<Rec*>& rs, double* const* q_host, int32_t iters,
+                        int32_t& done) {
+  done = 0;
+  for (int h = 0; h < 2; ++h)
+    if (!s->ev_hdone[h] && cudaEventCreateWithFlags(&s->ev_hdone[h], cudaEventDisableTiming) != cudaSuccess)
+      return OT2D_ERR_CUDA;
+  cudaStream_t sh[2] = {s->st, s->st2};
+  int err = OT2D_OK;
+  bool halves = true;
+  for (int it = 0; it < iters && !err && halves; ++it) {
+    done = it + 1;
+    for (int h = 0; h < 2 && !err; ++h) {
+      for (int i = 0; i < n && !err; ++i) {
+        if (rs[i]->half != h) continue;
+        const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
+        if ((it > 0 && cudaStreamWaitEvent(sh[h], s->ev_d2h[i], 0) != cudaSuccess) ||
+            cudaMemcpyAsync(rs[i]->d.q64, q_host[i], bytes, cudaMemcpyHostToDevice, sh[h]) != cudaSuccess)
+          err = OT2D_ERR_CUDA;
+      }
+      if (!err && s->precision == OT2D_FP32_MIXED &&
+          launch_shadow<float>(s->h32[h].d_sl, s->h32[h].b, sh[h]) != cudaSuccess)
+        err = OT2D_ERR_CUDA;
+      if (!err && (cudaStreamWaitEvent(sh[h], s->ev_half[1 - h], 0) != cudaSuccess ||
+                   cudaGraphLaunch(s->hexec[h], sh[h]) != cudaSuccess ||
+                   cudaEventRecord(s->ev_hdone[h], sh[h]) != cudaSuccess ||
+                   cudaStreamWaitEvent(s->st_d2h, s->ev_hdone[h], 0) != cudaSuccess))
+        err = OT2D_ERR_CUDA;
+      for (int i = 0; i < n && !err; ++i) {
+        if (rs[i]->half != h) continue;
+        const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
+        if (cudaMemcpyAsync(q_host[i], rs[i]->d.q64, bytes, cudaMemcpyDeviceToHost, s->st_d2h) != cudaSuccess ||
+            cudaEventRecord(s->ev_d2h[i], s->st_d2h) != cudaSuccess)
+          err = OT2D_ERR_CUDA;
+      }
+    }
+    bool capped = false;
+    for (int id : s->live) {
+      Rec& r = s->recs[id];
+      if (++r.launched >= iter_cap(r)) capped = true;
+    }
+    if (!err && (++s->since_check >= s->check_every || capped)) {
+      // the status read sees both halves done and no upload in flight
+      if (cudaEventRecord(s->ev_join, s->st2) != cudaSuccess || cudaStreamWaitEvent(s->st, s->ev_join, 0) != cudaSuccess ||
+          cudaStreamSynchronize(s->st_d2h) != cudaSuccess)
+        err = OT2D_ERR_CUDA;
+      else
+        err = check(s);
+      if (!err && s->dirty) {
+        for (int i = 0; i < n; ++i)
+          if (!rs[i]->live) { err = OT2D_ERR_ARG; break; }
+        if (!err) err = rebuild(s);
+        halves = s->halves;   // retirements took the batch below the halves' size
+      }
+    }
+  }
+  if (cudaStreamSynchronize(s->st_d2h) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
+  if (cudaStreamSynchronize(s->st2) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
+  if (cudaStreamSynchronize(s->st) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
+  return err;
+}
+
 int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, double* const* q_host, int32_t iters) {
   if (!s || n < 0 || (n && (!ids || !q_host)) || iters < 0) return OT2D_ERR_ARG;
   cudaSetDevice(s->device);
@@ -894,8 +975,22 @@ int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, doub
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return OT2D_ERR_CUDA;
     s->ev_d2h.push_back(e);
   }
+  // A batch large enough for halves overlaps them: half 1's uploads run
+  // while half 0 iterates, half 0's downloads while half 1 iterates.
+  if (!s->halves && !s->want_halves && s->live.size() >= 2) {
+    s->want_halves = true;
+    s->dirty = true;
+    int e = rebuild(s);
+    if (e) return e;
+  }
   int err = OT2D_OK;
-  for (int it = 0; it < iters && !err; ++it) {
+  int32_t done = 0;
+  if (s->halves) {
+    // the rest (if retirements took the batch below the halves' size) in
+    // the single graph below
+    if ((err = iterate_host_halves(s, n, rs, q_host, iters, done)) != OT2D_OK || done == iters) return err;
+  }
+  for (int it = done; it < iters && !err; ++it) {
     for (int i = 0; i < n && !err; ++i) {
       const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
       if ((it > 0 && cudaStreamWaitEvent(s->st, s->ev_d2h[i], 0) != cudaSuccess) ||
