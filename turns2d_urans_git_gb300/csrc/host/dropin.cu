@@ -494,6 +494,7 @@ extern "C" {
 int ot2d_set_params(const ot2d_params* p) {
   if (!p) return fail(OT2D_ERR_ARG);
   if (p->nhalo != 1 || p->jd != p->jmax + 1 || p->kd != p->kmax + 1) return fail(OT2D_ERR_ARG);
+  if (!rt_lim_known(p->ilim)) return fail(OT2D_ERR_ARG);   // reconstructions of rhsup (eulerrhs.f:84-97)
   g_ctx.P = *p;
   g_ctx.has = true;
   return OT2D_OK;

@@ -185,6 +185,10 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
   if (!batch_fits(precision, p.iprecon != 0, p.kd, p.jd)) return OT2D_ERR_ARG;
   if (!p.lamin && p.iturb != 1 && p.iturb != 2) return OT2D_ERR_ARG;  // SA or k-omega SST
   if (p.itrans != 0) return OT2D_ERR_ARG;                            // no transition model
+  // reconstructions rhsup dispatches (eulerrhs.f:84-97): |ilim| 0 central,
+  // 1 MUSCL, 2 PPM quadratic, ilim 4 WENO5; any other value reconstructs
+  // nothing in the reference
+  if (!rt_lim_known(p.ilim)) return OT2D_ERR_ARG;
   // steady, or time accurate with the pitching grid (Turns_overset.f:372-403:
   // iunst 1, motiontype 1) at first to third order; Newton iterations only
   // in time-accurate runs; not together with the time-spectral form

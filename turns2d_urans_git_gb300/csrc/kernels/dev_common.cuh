@@ -65,6 +65,9 @@ struct Slice {
 // Reconstruction family of a limiter switch, as rhsup dispatches it
 // (eulerrhs.f:85-97): ilim 4 -> weno, |ilim| 1 -> muscld_new, otherwise the
 // unlimited central slope of iflux.
+__host__ __device__ __forceinline__ bool rt_lim_known(int ilim) {
+  return ilim == 0 || ilim == 1 || ilim == -1 || ilim == 4;
+}
 __host__ __device__ __forceinline__ int rt_lim_class(int ilim) {
   return ilim == 4 ? 4 : ((ilim < 0 ? -ilim : ilim) == 1 ? 1 : 0);
 }
