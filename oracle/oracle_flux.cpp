@@ -311,11 +311,176 @@ static void roetrklflx(const P& p, Line& L, int is, int ie) {
   }
 }
 
+/* tridag, eulerrhs.f:1562-1588: Thomas elimination of the rows ni..nl
+ * (a sub-, b main, c super-diagonal, f right-hand side) into z. */
+static void tridag(const std::vector<double>& a, const std::vector<double>& b, const std::vector<double>& c,
+                   const std::vector<double>& f, std::vector<double>& z, int ni, int nl) {
+  std::vector<double> w(nl + 2, 0.), g(nl + 2, 0.);
+  w[ni] = c[ni] / b[ni];
+  g[ni] = f[ni] / b[ni];
+  for (int j = ni + 1; j <= nl; ++j) {
+    double d = b[j] - a[j] * w[j - 1];
+    double rd = 1.0 / d;
+    w[j] = c[j] * rd;
+    g[j] = (f[j] - a[j] * g[j - 1]) * rd;
+  }
+  z[nl] = g[nl];
+  for (int j1 = 1; j1 <= nl - ni; ++j1) {
+    int j = nl - j1;
+    z[j] = g[j] - w[j] * z[j + 1];
+  }
+}
+
+/* Fortran's amedian statement function of quad (eulerrhs.f:1256-1257):
+ * b moved toward c and d by the smaller distance when both lie on one side */
+static inline double amedian(double b, double c, double d) {
+  return b + 0.5 * (fsign(1., c - b) + fsign(1., d - b)) * fmin2(std::fabs(c - b), std::fabs(d - b));
+}
+
+/* the sonic-A limited slope quad uses next to the line ends */
+static inline double quad_sonic(double at, double ati1, double sl) {
+  double t1 = ammd(at, ati1);
+  return fsign(1., t1) * fmin2(0.5 * std::fabs(at + ati1), fmax2(2. * std::fabs(sl), std::fabs(t1)));
+}
+
+/* quad, eulerrhs.f:1233-1559 (ibmin = ibmax = 1 on the path): piecewise
+ * quadratic reconstruction with compact sixth-order nodal slopes and
+ * curvatures (two tridiagonal solves per line and variable), a median
+ * correction of their signs and the monotonicity-preserving constraint
+ * ("method 2").  cm, a scalar of the reference carried from one cell to the
+ * next, starts at 0 for every line here (the reference leaves it
+ * undefined; it is only read when amedian's sum rounds to none of its
+ * arguments). */
+static void quad(Line& L, int is, int ie, double qt) {
+  if (qt == 0.0) {
+    for (int n = 1; n <= 4; ++n) for (int i = is; i <= ie; ++i) { L.ql[n][i] = L.f[n][i]; L.qr[n][i] = L.f[n][i]; }
+    return;
+  }
+  const int is1 = is + 1, is2 = is + 2, ie2 = ie - 2, ie1 = ie - 1;
+  std::vector<double> d1(ie + 2, 0.), d2(ie + 2, 0.), con1(ie + 2, 0.), con2(ie + 2, 0.), con3(ie + 2, 0.);
+  std::vector<double> s1(ie + 2, 0.), sf(ie + 2, 0.), sc(ie + 2, 0.), sb(ie + 2, 0.);
+  for (int n = 1; n <= 4; ++n) {
+    const std::vector<double>& f = L.f[n];
+    std::vector<double>& ql = L.ql[n]; std::vector<double>& qr = L.qr[n];
+    // slope: the two cells at each end (sonic-A), then the compact system
+    int i = is;
+    double f1i = f[i + 1] - f[i], f1i1 = f[i + 2] - f[i + 1], f1i2 = f[i + 3] - f[i + 2], f1i3 = f[i + 4] - f[i + 3];
+    double f2i1 = f1i1 - f1i, f2i2 = f1i2 - f1i1, f2i3 = f1i3 - f1i2;
+    double f2i = 2. * f2i1 - f2i2;
+    double f2mi = ammd(f2i, f2i1), f2mi1 = ammd(f2i1, f2i2), f2mi2 = ammd(f2i2, f2i3);
+    double at = f1i - 0.5 * f2mi;
+    d1[i] = ammd(at, 2. * f1i);
+    ql[i] = f[i] + 0.5 * d1[i];
+    qr[i] = f[i] - 0.5 * d1[i];
+    i = is1;
+    d1[i] = quad_sonic(f1i1 - 0.5 * f2mi1, f1i + 0.5 * f2mi, ammd(f1i1, f1i));
+    ql[i] = f[i] + 0.5 * d1[i];
+    qr[i] = f[i] - 0.5 * d1[i];
+    i = is2;
+    const double slopes2 = quad_sonic(f1i2 - 0.5 * f2mi2, f1i1 + 0.5 * f2mi1, ammd(f1i2, f1i1));
+    con1[i] = 0.25;
+    con2[i] = 1.;
+    con3[i] = 0.75 * (f[i + 1] - f[i - 1]);
+    con3[i] = con3[i] - con1[i] * d1[i - 1];
+    for (i = is + 3; i <= ie - 3; ++i) {
+      con1[i] = 1. / 3.;
+      con2[i] = 1.;
+      con3[i] = (f[i + 2] + 28. * f[i + 1] - 28. * f[i - 1] - f[i - 2]) / 36.;
+    }
+    i = ie;
+    f1i1 = f[i] - f[i - 1]; f1i2 = f[i - 1] - f[i - 2]; f1i3 = f[i - 2] - f[i - 3];
+    double f1i4 = f[i - 3] - f[i - 4];
+    f2i1 = f1i1 - f1i2; f2i2 = f1i2 - f1i3; f2i3 = f1i3 - f1i4;
+    f2i = 2. * f2i1 - f2i2;
+    f2mi1 = ammd(f2i1, f2i); f2mi2 = ammd(f2i2, f2i1);
+    double f2mi3 = ammd(f2i3, f2i2);
+    double at1 = f1i1 + 0.5 * f2mi1;
+    d1[i] = ammd(at1, 2. * f1i1);
+    ql[i] = f[i] + 0.5 * d1[i];
+    qr[i] = f[i] - 0.5 * d1[i];
+    i = ie1;
+    d1[i] = quad_sonic(f1i1 - 0.5 * f2mi1, f1i2 + 0.5 * f2mi2, ammd(f1i1, f1i2));
+    ql[i] = f[i] + 0.5 * d1[i];
+    qr[i] = f[i] - 0.5 * d1[i];
+    i = ie2;
+    const double slopee2 = quad_sonic(f1i2 - 0.5 * f2mi2, f1i3 + 0.5 * f2mi3, ammd(f1i2, f1i3));
+    con1[i] = 0.25;
+    con2[i] = 1.;
+    con3[i] = 0.75 * (f[i + 1] - f[i - 1]);
+    con3[i] = con3[i] - con1[i] * d1[i + 1];
+    tridag(con1, con2, con1, con3, d1, is2, ie2);
+    // curvature
+    d2[is] = 0.; d2[is1] = 0.;
+    i = is2;
+    con1[i] = 0.1;
+    con2[i] = 1.;
+    con3[i] = 1.2 * (f[i + 1] - 2. * f[i] + f[i - 1]);
+    con3[i] = con3[i] - con1[i] * d2[i - 1];
+    for (i = is + 3; i <= ie - 3; ++i) {
+      con1[i] = 2. / 11.;
+      con2[i] = 1.;
+      con3[i] = (3. * f[i + 2] + 48. * f[i + 1] - 102. * f[i] + 48. * f[i - 1] + 3. * f[i - 2]) / 44.;
+    }
+    d2[ie] = 0.; d2[ie1] = 0.;
+    i = ie2;
+    con1[i] = 0.1;
+    con2[i] = 1.;
+    con3[i] = 1.2 * (f[i + 1] - 2. * f[i] + f[i - 1]);
+    con3[i] = con3[i] - con1[i] * d2[i + 1];
+    tridag(con1, con2, con1, con3, d2, is2, ie2);
+    // signs of the slope and the curvature
+    for (i = is1; i <= ie; ++i) s1[i] = f[i] - f[i - 1];
+    for (i = is; i <= ie2; ++i) sf[i] = (-f[i + 2] + 4. * f[i + 1] - 3. * f[i]) / 2.;
+    for (i = is1; i <= ie1; ++i) sc[i] = (f[i + 1] - f[i - 1]) / 2.;
+    for (i = is2; i <= ie; ++i) sb[i] = (f[i - 2] - 4. * f[i - 1] + 3. * f[i]) / 2.;
+    double cm = 0.;
+    for (i = is2; i <= ie2; ++i) {
+      double sm = amedian(sf[i], sc[i], sb[i]);
+      if (sm == sf[i]) cm = f[i + 2] - 2. * f[i + 1] + f[i];
+      if (sm == sc[i]) cm = f[i + 1] - 2. * f[i] + f[i - 1];
+      if (sm == sb[i]) cm = f[i] - 2. * f[i - 1] + f[i - 2];
+      d1[i] = amedian(d1[i], sm, sc[i]);
+      if (d1[i] == sm) d2[i] = cm;
+      if (d1[i] == sc[i]) d2[i] = f[i + 1] - 2. * f[i] + f[i - 1];
+    }
+    // monotonicity-preserving constraint (method 2) and the quadratic
+    for (i = is2; i <= ie2; ++i) {
+      double si = d1[i], ci = d2[i], sr, cr, sl, cl;
+      const double ad = std::fabs(d1[i]);
+      if (ad > 2.0 * std::fabs(s1[i + 1]) && ad > 2.0 * std::fabs(s1[i])) {
+        if (ad <= std::fabs(d1[i + 1])) { sr = d1[i]; cr = 2. * (s1[i + 1] - d1[i]); }
+        else { sr = 2. * s1[i + 1] - d1[i + 1]; cr = 2. * (-s1[i + 1] + d1[i + 1]); }
+        if (ad <= std::fabs(d1[i - 1])) { sl = d1[i]; cl = 2. * (-s1[i] + d1[i]); }
+        else { sl = 2. * s1[i] - d1[i - 1]; cl = 2. * (s1[i] - d1[i - 1]); }
+        si = ammd(sl, sr);
+        ci = ammd(cl, cr);
+      } else {
+        if (ad > 2.0 * std::fabs(s1[i + 1])) {
+          if (ad <= std::fabs(d1[i + 1])) { sr = d1[i]; cr = 2. * (s1[i + 1] - d1[i]); }
+          else { sr = 2. * s1[i + 1] - d1[i + 1]; cr = 2. * (-s1[i + 1] + d1[i + 1]); }
+          si = ammd(d1[i], sr);
+          ci = ammd(d2[i], cr);
+        }
+        if (ad > 2.0 * std::fabs(s1[i])) {
+          if (ad <= std::fabs(d1[i - 1])) { sl = d1[i]; cl = 2. * (-s1[i] + d1[i]); }
+          else { sl = 2. * s1[i] - d1[i - 1]; cl = 2. * (s1[i] - d1[i - 1]); }
+          si = ammd(sl, d1[i]);
+          ci = ammd(cl, d2[i]);
+        }
+      }
+      ql[i] = f[i] + 0.5 * si + ci / 12.;
+      qr[i] = f[i] - 0.5 * si + ci / 12.;
+    }
+    qr[is2] = f[is2] - 0.5 * slopes2;
+    ql[ie2] = f[ie2] + 0.5 * slopee2;
+  }
+}
+
 static void reconstruct(const P& p, Line& L, int n, double th, double qt, double eps, double epsl) {
   int ilima = std::abs(p.ilim);
   if (ilima == 0) iflux(L, 1, n, qt);
   if (ilima == 1) muscld_new(L, 1, n, n - 1, th, qt, epsl);
-  if (ilima == 2) { std::fprintf(stderr, "oracle: ilim=2 (quad) not restated\n"); std::abort(); }
+  if (ilima == 2) quad(L, 1, n, qt);
   if (p.ilim == 4) weno(L, 1, n, qt);
   (void)eps;
 }
@@ -606,3 +771,14 @@ void visrhs(const P& p, A2 turmu, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy) {
 }
 
 }  // namespace oro
+
+/* Test hook: quad on one line of primitives f[0..n) (one variable; the
+ * other three lines a copy of it), ql/qr out.  No counterpart in the
+ * reference. */
+extern "C" void oro_quad_line(const double* f, int n, double qt, double* ql, double* qr) {
+  oro::Line L(n);
+  for (int v = 1; v <= 4; ++v)
+    for (int i = 1; i <= n; ++i) L.f[v][i] = f[i - 1];
+  oro::quad(L, 1, n, qt);
+  for (int i = 1; i <= n; ++i) { ql[i - 1] = L.ql[1][i]; qr[i - 1] = L.qr[1][i]; }
+}

@@ -345,3 +345,53 @@ def test_oracle_sa_source_matches_the_published_model():
     scale = np.maximum.reduce([np.abs(P / nut), np.abs(D / nut), np.abs(dP), np.abs(dD)])
     assert np.max(np.abs(bk - diag)[sel] / scale[sel]) < 1e-6
     assert not bk[~inner].any() and not sjmat[~inner].any()
+
+
+def _quad_line(f, qt=0.25):
+    L = ob.lib()
+    L.oro_quad_line.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_double, C.POINTER(C.c_double),
+                                C.POINTER(C.c_double)]
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    ql, qr = np.zeros_like(f), np.zeros_like(f)
+    L.oro_quad_line(ob.ptr(f), len(f), qt, ob.ptr(ql), ob.ptr(qr))
+    return ql, qr
+
+
+def test_oracle_quad_reconstruction_invariants():
+    """The oracle's quad (eulerrhs.f:1233-1559, ilim 2): a linear profile is
+    reconstructed exactly (every face value f(i) +- slope/2, the ends by
+    their sonic-A slopes included); qt = 0 gives first order; on a smooth
+    profile the two states of a face agree to third order or better (the
+    compact sixth-order nodal slopes and curvatures); at a step no face
+    value leaves the range of the cells beside it (the monotonicity
+    constraint)."""
+    i = np.arange(40, dtype=np.float64)
+    f = 0.3 + 0.05 * i
+    ql, qr = _quad_line(f)
+    assert np.max(np.abs(ql - (f + 0.025))) < 1e-13 and np.max(np.abs(qr - (f - 0.025))) < 1e-13
+    ql, qr = _quad_line(np.sin(i), qt=0.0)
+    assert np.array_equal(ql, np.sin(i)) and np.array_equal(qr, np.sin(i))
+    errs = []
+    for n in (48, 96, 192):
+        x = (np.arange(n) + 0.5) / n
+        ql, qr = _quad_line(np.sin(2 * np.pi * x))
+        errs.append(np.max(np.abs(ql[4:-5] - qr[5:-4])))
+    assert errs[0] / errs[1] > 7.0 and errs[1] / errs[2] > 7.0, errs
+    f = np.where(i < 20, 1.0, 0.2)
+    ql, qr = _quad_line(f)
+    for k in range(3, 37):
+        lo, hi = min(f[k - 1:k + 2]), max(f[k - 1:k + 2])
+        assert lo - 1e-14 <= ql[k] <= hi + 1e-14 and lo - 1e-14 <= qr[k] <= hi + 1e-14, k
+
+
+def test_limiter_switches_without_a_reconstruction_are_refused():
+    """rhsup reconstructs for |ilim| 0, 1, 2 and ilim 4 (eulerrhs.f:84-97);
+    the drop-in parameters refuse any other switch (OT2D_ERR_ARG) rather
+    than run a reconstruction the reference does not."""
+    L = api.lib()
+    L.ot2d_set_params.argtypes = [C.POINTER(Params)]
+    for ilim, ok in ((0, True), (1, True), (-1, True), (2, True), (-2, True), (4, True), (3, False), (-4, False),
+                     (5, False)):
+        _, prm, _, _ = api.config_c1(jmax=33, kmax=17)
+        prm.ilim = ilim
+        assert (L.ot2d_set_params(C.byref(prm)) == 0) == ok, ilim

@@ -52,7 +52,7 @@ def test_bc(visc, istep0):
     assert not np.array_equal(qo, c.q)  # the halo really changed
 
 
-@pytest.mark.parametrize("ilim,irhsy", [(0, -3), (1, -3), (1, -2), (4, -3), (1, -1)])
+@pytest.mark.parametrize("ilim,irhsy", [(0, -3), (1, -3), (1, -2), (4, -3), (1, -1), (2, -3), (-2, -2), (2, -1)])
 def test_rhsup(ilim, irhsy):
     c = Case(ilim=ilim, irhsy=irhsy, seed=3)
     so = np.random.default_rng(9).uniform(-1, 1, c.n2 * c.p.nv) * 1e-3
@@ -326,6 +326,31 @@ def test_solver_fp64_matches_oracle(kind):
     f = forces[0]
     for a, b in ((r.cl, f[0]), (r.cd, f[1]), (r.cm, f[2])):
         assert abs(a - b) <= 1e-10 * max(abs(b), 1e-3)
+
+
+@pytest.mark.parametrize("kind", ["euler", "sa"])
+def test_solver_quad_fp64_matches_oracle(kind):
+    """The piecewise quadratic reconstruction (ilim 2: quad and tridag,
+    eulerrhs.f:1233-1588) through the batched solver: k_quad's line solves
+    and the residual's faces against the oracle.  The FP32-mixed path on
+    the same request stays close to it."""
+    if kind == "euler":
+        _, prm, xv, yv = api.cmesh_case(97, 25, ds_wall=2e-3, invisc=1, lamin=1, irhsy=-3, ilim=2, ilhs=1,
+                                        iconstant_cfl=1, dt=10.0, fsmach=0.5, alfa=1.25)
+        tol = 1e-10
+    else:
+        _, prm, xv, yv = api.cmesh_case(97, 33, ds_wall=1e-4, invisc=0, lamin=0, iturb=1, irhsy=-3, ilim=2, ilhs=1,
+                                        iconstant_cfl=1, dt=20.0, fsmach=0.3, alfa=2.0, rey=2e6, vnuinf=3.0)
+        tol = 1e-9
+    r, q, hist, forces, q_o = _solver_vs_oracle(prm, xv, yv, 40, OT2D_FP64)
+    assert r.status == 0 and r.iterations == 40
+    assert abs(r.rsum_last - hist[-1, 0]) <= tol * hist[-1, 0]
+    assert relerr(q, q_o) <= tol
+    f = forces[0]
+    for a, b in ((r.cl, f[0]), (r.cd, f[1]), (r.cm, f[2])):
+        assert abs(a - b) <= tol * max(abs(b), 1e-3)
+    r32, q32, _, _, _ = _solver_vs_oracle(prm, xv, yv, 40, OT2D_FP32_MIXED)
+    assert r32.status == 0 and relerr(q32, q_o) < 1e-3
 
 
 def test_solver_fp32_mixed_close_to_fp64():

@@ -128,7 +128,8 @@ int prepare(int nslice, int& err) {
   if (!g_ctx.has) return err = OT2D_ERR_NOPARAMS;
   const size_t n2 = (size_t)g_ctx.P.jd * g_ctx.P.kd, ws = (n2 + 63) / 64 * 64;
   const size_t rec = (size_t)lu_rec_elems(g_ctx.P.jd, g_ctx.P.kd, 8);
-  const size_t need = ws * DW_SLOTS * nslice + 8 * ws + rec * nslice;
+  const size_t quad = rt_lim_class(g_ctx.P.ilim) == 2 ? (size_t)quad_elems(g_ctx.P.jd, g_ctx.P.kd) : 0;
+  const size_t need = ws * DW_SLOTS * nslice + 8 * ws + rec * nslice + quad * nslice;
   g_ctx.nslice = nslice;
   if (need > g_ctx.wcap) {
     if (g_ctx.dwork) cudaFree(g_ctx.dwork);
@@ -168,6 +169,10 @@ Slice<double> base_slice(int nsp, int nspec, int64_t qs) {
   S.lurec = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd, 8);
   S.red = g_ctx.dred + (size_t)RED_N * (nsp - 1);
   S.ist = nullptr;
+  if (rt_lim_class(p.ilim) == 2) {
+    const size_t rec = (size_t)lu_rec_elems(p.jd, p.kd, 8), qe = (size_t)quad_elems(p.jd, p.kd);
+    S.quad = g_ctx.dwork + ws * DW_SLOTS * (size_t)g_ctx.nslice + 8 * ws + rec * (size_t)g_ctx.nslice + (size_t)(nsp - 1) * qe;
+  }
   slice_consts(S, p);
   return S;
 }
@@ -495,6 +500,7 @@ int ot2d_set_params(const ot2d_params* p) {
   if (!p) return fail(OT2D_ERR_ARG);
   if (p->nhalo != 1 || p->jd != p->jmax + 1 || p->kd != p->kmax + 1) return fail(OT2D_ERR_ARG);
   if (!rt_lim_known(p->ilim)) return fail(OT2D_ERR_ARG);   // reconstructions of rhsup (eulerrhs.f:84-97)
+  if (rt_lim_class(p->ilim) == 2 && (p->jd < 7 || p->kd < 7)) return fail(OT2D_ERR_ARG);   // quad's end stencils
   g_ctx.P = *p;
   g_ctx.has = true;
   return OT2D_OK;

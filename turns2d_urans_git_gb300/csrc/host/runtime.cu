@@ -94,6 +94,7 @@ size_t plan(const ot2d_params& p, int precision, F&& assign) {
   // the freestream correction belongs to a fixed grid
   if (mixed && !mv) assign("sinf", L.take(rb * n2 * nspec * 4));
   assign("lurec", L.take(rb * (size_t)lu_rec_elems(p.jd, p.kd, (int)rb) * nspec));
+  if (rt_lim_class(p.ilim) == 2) assign("quad", L.take(rb * (size_t)quad_elems(p.jd, p.kd) * nspec));
   return L.total;
 }
 
@@ -189,6 +190,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
   // 1 MUSCL, 2 PPM quadratic, ilim 4 WENO5; any other value reconstructs
   // nothing in the reference
   if (!rt_lim_known(p.ilim)) return OT2D_ERR_ARG;
+  if (rt_lim_class(p.ilim) == 2 && (p.jd < 7 || p.kd < 7)) return OT2D_ERR_ARG;   // quad's end stencils
   // steady, or time accurate with the pitching grid (Turns_overset.f:372-403:
   // iunst 1, motiontype 1) at first to third order; Newton iterations only
   // in time-accurate runs; not together with the time-spectral form
@@ -247,6 +249,7 @@ int solve_create(DevSolve& d, const ot2d_params& p, int precision, const double*
     else if (n == "sn") d.sn = ptr;
     else if (n == "w") d.w = ptr;
     else if (n == "lurec") d.lurec = ptr;
+    else if (n == "quad") d.quad = ptr;
     else if (n == "wd2") d.wd2 = (double*)ptr;
     else if (n == "xc") d.xc = (double*)ptr;
     else if (n == "yc") d.yc = (double*)ptr;
@@ -395,6 +398,7 @@ Slice<R> make_slice(const DevSolve& d, int nsp, double* red, int32_t* ist) {
   slice_consts(S, p);
   S.wstride = (int64_t)d.wstride;
   S.lurec = (R*)d.lurec + (size_t)(nsp - 1) * (size_t)lu_rec_elems(p.jd, p.kd, (int)sizeof(R));
+  S.quad = d.quad ? (R*)d.quad + (size_t)(nsp - 1) * (size_t)quad_elems(p.jd, p.kd) : nullptr;
   S.red = red; S.ist = ist;
   S.Ds = p.timespectral ? d.Ds : nullptr;
   S.xx64 = D_(d.xx64); S.xy64 = D_(d.xy64); S.yx64 = D_(d.yx64); S.yy64 = D_(d.yy64);
@@ -426,7 +430,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
     if (sl[i].xc) moving = 1;
     if (sl[i].k_mp2 >= (R)0) precon = 1;
     maxnbc = std::max(maxnbc, (int)sl[i].nbc);
-    limmask |= sl[i].lim == 4 ? 4 : (sl[i].lim == 1 ? 2 : 1);
+    limmask |= sl[i].lim == 4 ? 4 : (sl[i].lim == 1 ? 2 : (sl[i].lim == 2 ? 8 : 1));
     idx[i] = cells; idx[(n + 1) + i] = jl; idx[2 * (n + 1) + i] = kl; idx[3 * (n + 1) + i] = lub;
     idx[4 * (n + 1) + i] = grp; idx[5 * (n + 1) + i] = tiles;
     const int jd = sl[i].jd, kd = sl[i].kd;

@@ -39,6 +39,7 @@ struct DevSolve {
   void *fxa = nullptr, *fya = nullptr, *gxa = nullptr, *gya = nullptr, *ftj = nullptr, *gtj = nullptr;
   void *ug = nullptr, *vg = nullptr, *tscale = nullptr, *bt = nullptr, *turmu = nullptr, *sn = nullptr, *w = nullptr;
   void* lurec = nullptr;
+  void* quad = nullptr;     // ilim +-2: quad's face states and line work (k_quad.cuh), per time instance
   double* wd2 = nullptr;   // SST wall term (k-omega SST instances only)
   // time-accurate moving grid (iunst = 1): centres, previous vertex levels,
   // stqol levels (itnmax > 1) and the per-step pitch table (own allocation)

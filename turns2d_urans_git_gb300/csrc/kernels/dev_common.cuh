@@ -45,6 +45,7 @@ struct Slice {
   R k_mp, k_rinf, k_uinf, k_vinf, k_einf, k_pinf;     // the q boundary conditions
   R* w;                              // scratch of this slice (phase dependent)
   R* lurec;                          // LU-SGS sweep records (skewed bands)
+  R* quad;                           // ilim +-2: face states and line work of quad (k_quad.cuh), or null
   int64_t wstride;                   // distance between scratch arrays (>= jd*kd)
   double* red;                       // per-slice reduction output
   int32_t* ist;                      // per-slice counters: istep0, istep, status bits, convergence
@@ -59,18 +60,24 @@ struct Slice {
   const double* motion;                   // per physical step: sin, cos of the pitch increment and of its negative
   int32_t nmotion;                        // physical steps in the table
   int32_t nbc;                            // &bcinp entries (params nbc)
-  int32_t lim;                            // reconstruction family: 0 central, 1 MUSCL, 4 WENO (rt_lim_class)
+  int32_t lim;                            // reconstruction family: 0 central, 1 MUSCL, 2 quad, 4 WENO (rt_lim_class)
 };
 
-// Reconstruction family of a limiter switch, as rhsup dispatches it
-// (eulerrhs.f:85-97): ilim 4 -> weno, |ilim| 1 -> muscld_new, otherwise the
-// unlimited central slope of iflux.
+// The limiter switches rhsup dispatches (eulerrhs.f:84-97): |ilim| 0
+// central, 1 MUSCL, 2 PPM quadratic, ilim 4 WENO5; any other value
+// reconstructs nothing in the reference, and is refused here.
 __host__ __device__ __forceinline__ bool rt_lim_known(int ilim) {
-  return ilim == 0 || ilim == 1 || ilim == -1 || ilim == 4;
+  return ilim == 0 || ilim == 1 || ilim == -1 || ilim == 2 || ilim == -2 || ilim == 4;
 }
+// Reconstruction family of a limiter switch: ilim 4 -> weno, |ilim| 1 ->
+// muscld_new, |ilim| 2 -> quad, otherwise the unlimited central slope of
+// iflux.
 __host__ __device__ __forceinline__ int rt_lim_class(int ilim) {
-  return ilim == 4 ? 4 : ((ilim < 0 ? -ilim : ilim) == 1 ? 1 : 0);
+  const int a = ilim < 0 ? -ilim : ilim;
+  return ilim == 4 ? 4 : (a == 1 ? 1 : (a == 2 ? 2 : 0));
 }
+// elements of R of a slice's quad block (k_quad.cuh): 40 arrays of jd*kd
+__host__ __device__ __forceinline__ int64_t quad_elems(int jd, int kd) { return (int64_t)40 * jd * kd; }
 
 // Fill the residual constants of a slice from its parameters (host side;
 // the same double expressions the kernels would evaluate).

@@ -163,6 +163,12 @@ __device__ __forceinline__ void rt_store_cell(const Slice<R>& S, const SM& sm, i
 template <class R, class SM>
 struct RtLine {
   const SM* sm; int o0, stride, lo, hi; R gm1;
+  // ilim +-2: this direction's quad face states in global memory (ql
+  // arrays, then qr; stride qn2); cell c of the line at g0 + c*gs
+  const R* qd = nullptr;
+  int64_t qn2 = 0, g0 = 0, gs = 0;
+  __device__ __forceinline__ R quad_l(int v, int c) const { return qd[v * qn2 + g0 + c * gs]; }
+  __device__ __forceinline__ R quad_r(int v, int c) const { return qd[(4 + v) * qn2 + g0 + c * gs]; }
   __device__ __forceinline__ void f4(int c, R* out) const {
     if (c < lo || c > hi) { out[0] = out[1] = out[2] = out[3] = (R)0; return; }
     const int r = o0 + c * stride;
@@ -384,9 +390,15 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R, TJ, TK>& sm, int t
       const int j = xi ? j0 - 1 + g % (TJ + 1) : j0 + g % TJ;
       const int k = xi ? k0 + g / (TJ + 1) : k0 - 1 + g / TJ;
       if (j > j1 || k > k1) continue;
-      const RtLine<R, SM> L = xi ? RtLine<R, SM>{&sm, (k - kr) * G::RW - jr, 1, max(1, jr), min(jd, jr + G::RW - 1), gm1}
-                                 : RtLine<R, SM>{&sm, (j - jr) - kr * G::RW, G::RW, max(1, kr), min(kd, kr + G::RH - 1),
-                                                 gm1};
+      RtLine<R, SM> L = xi ? RtLine<R, SM>{&sm, (k - kr) * G::RW - jr, 1, max(1, jr), min(jd, jr + G::RW - 1), gm1}
+                           : RtLine<R, SM>{&sm, (j - jr) - kr * G::RW, G::RW, max(1, kr), min(kd, kr + G::RH - 1), gm1};
+      if constexpr (LIM == 2) {
+        const int64_t n2 = (int64_t)jd * kd;
+        L.qd = S.quad + (xi ? 0 : 8) * n2;
+        L.qn2 = n2;
+        L.g0 = xi ? (int64_t)(k - 1) * jd - 1 : (int64_t)(j - 1) - jd;
+        L.gs = xi ? 1 : jd;
+      }
       const Recon<R> rc = xi ? rx : ry;
       const int64_t o = at(jd, j, k);
       const R* ma = xi ? S.fxa : S.gxa;

@@ -13,8 +13,9 @@ cudaError_t launch_resid_shape(const Slice<R>* d_sl, const Batch& b, int flags, 
   static DeviceOnce once;
   cudaError_t ae = once.run([&](int&) {
     const void* ks[] = {(const void*)k_resid<R, false, 0, TJ, TK>, (const void*)k_resid<R, false, 1, TJ, TK>,
-                        (const void*)k_resid<R, false, 4, TJ, TK>, (const void*)k_resid<R, true, 0, TJ, TK>,
-                        (const void*)k_resid<R, true, 1, TJ, TK>, (const void*)k_resid<R, true, 4, TJ, TK>};
+                        (const void*)k_resid<R, false, 2, TJ, TK>, (const void*)k_resid<R, false, 4, TJ, TK>,
+                        (const void*)k_resid<R, true, 0, TJ, TK>, (const void*)k_resid<R, true, 1, TJ, TK>,
+                        (const void*)k_resid<R, true, 2, TJ, TK>, (const void*)k_resid<R, true, 4, TJ, TK>};
     for (const void* k : ks) {
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
@@ -23,7 +24,7 @@ cudaError_t launch_resid_shape(const Slice<R>* d_sl, const Batch& b, int flags, 
   });
   if (ae != cudaSuccess) return ae;
   // one launch per (preconditioning, reconstruction family) in the batch
-  const int m = b.lim_mask ? b.lim_mask : 7;
+  const int m = b.lim_mask ? b.lim_mask : 15;
   const dim3 g(b.tile_blocks), t(RT_BS);
   for (int pre = 0; pre <= (b.precon ? 1 : 0); ++pre) {
     if (m & 1) {
@@ -37,6 +38,10 @@ cudaError_t launch_resid_shape(const Slice<R>* d_sl, const Batch& b, int flags, 
     if (m & 4) {
       if (pre) k_resid<R, true, 4, TJ, TK><<<g, t, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
       else k_resid<R, false, 4, TJ, TK><<<g, t, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
+    }
+    if (m & 8) {
+      if (pre) k_resid<R, true, 2, TJ, TK><<<g, t, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
+      else k_resid<R, false, 2, TJ, TK><<<g, t, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);
     }
   }
   return cudaGetLastError();

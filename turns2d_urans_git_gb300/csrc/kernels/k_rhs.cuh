@@ -61,7 +61,11 @@ template <class R>
 struct LineRd {
   const R* q; int64_t qs; int jd, nq, fix, dir; R gm1;
   const int32_t* ib;
+  const R* qd = nullptr;   // ilim +-2: this direction's quad face states (ql arrays, then qr), stride qn2
+  int64_t qn2 = 0;
   __device__ __forceinline__ int64_t off(int i) const { return dir == 0 ? at(jd, i, fix) : at(jd, fix, i); }
+  __device__ __forceinline__ R quad_l(int v, int i) const { return qd[v * qn2 + off(i)]; }
+  __device__ __forceinline__ R quad_r(int v, int i) const { return qd[(4 + v) * qn2 + off(i)]; }
   __device__ __forceinline__ R f(int i, int n) const {
     int64_t o = off(i);
     R q1 = q[o];
@@ -333,8 +337,9 @@ __device__ __forceinline__ void roe_turkel(R gm1, R bSq, const R* L, const R* Rr
 }
 
 // Inviscid flux through one face between cells i and i+1 of a line.  L
-// supplies f4(c, out) (the primitive f of cell c) and iba(c).  LIM is the
-// limiter family (0 central, 1 MUSCL, 4 WENO) so that the central and MUSCL
+// supplies f4(c, out) (the primitive f of cell c) and iba(c), and for quad
+// the states quad_l / quad_r k_quad left.  LIM is the limiter family (0
+// central, 1 MUSCL, 2 quad, 4 WENO) so that the central and MUSCL
 // forms index their window with constants only (the window stays in
 // registers); face_flux() dispatches on rc.ilim.  PRE: Turkel's
 // preconditioned flux (roetrklflx) in place of roeflx.
@@ -360,6 +365,13 @@ __device__ __forceinline__ void face_flux_t(const Line& L, const Recon<R>& rc, i
     for (int v = 0; v < 4; ++v) {
       ql[v] = rc.weno_l(&w8[v][0], i, n, blank_l);
       qr[v] = rc.weno_r(&w8[v][1], i + 1, n, blank_r);
+    }
+  } else if constexpr (LIM == 2) {
+    // quad: ql of cell i and qr of cell i+1, reconstructed over the whole line
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      ql[v] = L.quad_l(v, i);
+      qr[v] = L.quad_r(v, i + 1);
     }
   } else {
     // cells i-1 .. i+2 (w4[m] = f(i-1+m)); MUSCL / central read only these
@@ -403,6 +415,7 @@ __device__ __forceinline__ void face_flux_p(const Line& L, const Recon<R>& rc, i
   const int ilm = rc.ilim < 0 ? -rc.ilim : rc.ilim;
   if (rc.ilim == 4) face_flux_t<4, R, Line, PRE>(L, rc, i, n, ri1, ri2, ri3, fout);
   else if (ilm == 1) face_flux_t<1, R, Line, PRE>(L, rc, i, n, ri1, ri2, ri3, fout);
+  else if (ilm == 2) face_flux_t<2, R, Line, PRE>(L, rc, i, n, ri1, ri2, ri3, fout);
   else face_flux_t<0, R, Line, PRE>(L, rc, i, n, ri1, ri2, ri3, fout);
 }
 
@@ -433,6 +446,7 @@ template <class R>
 __device__ void xi_face(const Slice<R>& S, int j, int k, R* F) {
   const ot2d_params& p = *S.P;
   LineRd<R> L{S.q, S.qs, S.jd, p.nq, k, 0, S.k_gm1, S.iblank};
+  if (S.quad) { L.qd = S.quad; L.qn2 = (int64_t)S.jd * S.kd; }
   Recon<R> rc = make_recon<R>(p, 0);
   int64_t o = at(S.jd, j, k);
   R f[4];
@@ -446,6 +460,7 @@ template <class R>
 __device__ void eta_face(const Slice<R>& S, int j, int k, R* G) {
   const ot2d_params& p = *S.P;
   LineRd<R> L{S.q, S.qs, S.jd, p.nq, j, 1, S.k_gm1, S.iblank};
+  if (S.quad) { L.qd = S.quad + 8 * (int64_t)S.jd * S.kd; L.qn2 = (int64_t)S.jd * S.kd; }
   Recon<R> rc = make_recon<R>(p, 1);
   int64_t o = at(S.jd, j, k);
   R f[4];

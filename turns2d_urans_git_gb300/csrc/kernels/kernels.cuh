@@ -5,6 +5,7 @@
 #include "dev_common.cuh"
 #include "k_bc.cuh"
 #include "k_rhs.cuh"
+#include "k_quad.cuh"
 #include "k_lusgs.cuh"
 #include "k_sa.cuh"
 #include "k_sst.cuh"

@@ -40,7 +40,19 @@ cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStr
 // the fused residual tiles: the plain instantiation always, the
 // preconditioned one when the batch holds a preconditioned slice
 template <class R>
+cudaError_t launch_quad(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
+  // quad's face states of every line of the ilim +-2 slices, before the
+  // faces that read them
+  if (b.lim_mask & 8)
+    k_quad<R><<<dim3((4 * (b.max_kd + b.max_wall) + 127) / 128, b.nslice), 128, 0, st>>>(d_sl);
+  return cudaGetLastError();
+}
+template <class R>
 cudaError_t launch_resid_both(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st) {
+  if (flags & AS_INV) {
+    cudaError_t e = launch_quad(d_sl, b, st);
+    if (e != cudaSuccess) return e;
+  }
   // the tile shape the batch's tile table was built for (k_resid_launch.cuh,
   // one translation unit per shape and precision)
   switch (b.rt_shape) {
@@ -63,7 +75,11 @@ cudaError_t launch_resid_tiles(const Slice<R>* d_sl, const Batch& b, int flags, 
 }
 template <class R>
 cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b, int inviscid, int viscous, cudaStream_t st) {
-  if (inviscid) k_faces<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  if (inviscid) {
+    cudaError_t e = launch_quad(d_sl, b, st);
+    if (e != cudaSuccess) return e;
+    k_faces<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  }
   if (viscous) k_visc<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
 }
