@@ -384,11 +384,19 @@ __global__ void __launch_bounds__(CELL_BS) k_lu_prep(const Slice<R>* __restrict_
   __syncthreads();
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   const int c = c0 + w, band = c / nst;
-  if (band >= nb) return;
-  int4* dst = reinterpret_cast<int4*>(S.lurec + (int64_t)c * CH);   // chunk (band, t) is chunk band*nst + t
-  const int4* src = reinterpret_cast<const int4*>((R*)lp_smem + w * CHS);
-  constexpr int n16 = (int)(CH * sizeof(R) / 16);
-  for (int i = l; i < n16; i += 32) dst[i] = src[i];
+  if (band >= nb || l != 0) return;
+  // one bulk copy (TMA) per staged chunk, shared -> global: chunk (band, t)
+  // is chunk band*nst + t; both ends 16-byte aligned, 16-byte multiple size
+  static_assert((CH * sizeof(R)) % 16 == 0 && (CHS * sizeof(R)) % 16 == 0, "bulk copy alignment");
+  R* dst = S.lurec + (int64_t)c * CH;
+  const R* src = (const R*)lp_smem + w * CHS;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+               "r"((uint32_t)__cvta_generic_to_shared(src)), "r"((uint32_t)(CH * sizeof(R)))
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  // the shared source must be read before the block's shared memory goes
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
 template <class R, bool PRE>
