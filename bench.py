@@ -497,7 +497,35 @@ def e2e_rate(sv, ids, cases, steps, world, dist):
     torch.cuda.synchronize()
     secs = rank_max(time.perf_counter() - t0, dist, "cuda")
     cells = sum((prm.jmax - 1) * (prm.kmax - 1) for (_, prm, _, _) in cases)
-    return (whole_job_rate(cells * steps, world, secs) if rc == 0 else None), sum(q.nbytes for q in qh)
+    link = host_link(pinned)
+    return (whole_job_rate(cells * steps, world, secs) if rc == 0 else None), sum(q.nbytes for q in qh), link
+
+
+def host_link(pinned, reps=5):
+    """The host link's copy rates for the same pinned buffers (the bound of
+    the host-buffer path): all uploads, all downloads, and both directions at
+    once on two streams, GB/s."""
+    import torch
+    dev = [torch.empty_like(t, device="cuda") for t in pinned]
+    nbytes = sum(t.numel() * t.element_size() for t in pinned)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    out = {}
+    for kind in ("h2d", "d2h", "both"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            for d, h in zip(dev, pinned):
+                if kind in ("h2d", "both"):
+                    with torch.cuda.stream(s1):
+                        d.copy_(h, non_blocking=True)
+                if kind in ("d2h", "both"):
+                    with torch.cuda.stream(s2):
+                        h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        out[kind + "_gbs"] = (2 if kind == "both" else 1) * nbytes / dt / 1e9
+    del dev
+    return out
 
 
 def phase_roofline(sv, alg_bytes, cells, peaks, traffic=None):
@@ -580,7 +608,7 @@ def run_ours(args):
     clocks = clk.stop()
     value = whole_job_rate(B * cells * args.steps, world, ms / 1e3)
     phase_ms, roof = phase_roofline(sv, ALG_BYTES_F32, B * cells, peaks, TRAFFIC_PER_CELL)
-    e2e, qbytes = e2e_rate(sv, ids, cases, max(3, args.steps // 2), world, dist)
+    e2e, qbytes, link = e2e_rate(sv, ids, cases, max(3, args.steps // 2), world, dist)
     sv.close()
     # ---- plain FP64 on the same batch, with its own e2e and roofline
     fp64 = None
@@ -591,7 +619,7 @@ def run_ours(args):
         k64 = max(2, args.fp64_steps)
         ms64 = timed(sv64, k64)
         ph64, roof64 = phase_roofline(sv64, ALG_BYTES_F64, B * cells, peaks)
-        e64, qb64 = e2e_rate(sv64, ids64, cases, 2, world, dist)
+        e64, qb64, _ = e2e_rate(sv64, ids64, cases, 2, world, dist)
         fp64 = {"value": whole_job_rate(B * cells * k64, world, ms64 / 1e3), "unit": UNIT, "steps": k64,
                 "ms_per_step": ms64 / k64, "phase_ms": ph64, "roofline": roof64,
                 "e2e": {"value": e64, "unit": UNIT, "h2d_bytes_per_step": qb64, "d2h_bytes_per_step": qb64}}
@@ -616,7 +644,11 @@ def run_ours(args):
                 "tuning": {"fp32_mixed": tune.describe(w32), "fp64": tune.describe(c64),
                            "fp32_mixed_served_b16": tune.describe(c32), "batch": B,
                            "search_s": tune_s, "cache": tune.default_cache_path()},
-                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes},
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes,
+                        # the host link's rates for the same buffers, and the
+                        # rate the path would have if its copies alone bound it
+                        "host_link": link,
+                        "copy_bound_value": B * cells / (2 * qbytes / (link["both_gbs"] * 1e9))},
                 "fp64_plain": fp64,
                 "gpu_launches": kernels_per_step * args.steps,
                 "kernels_per_step": kernels_per_step,

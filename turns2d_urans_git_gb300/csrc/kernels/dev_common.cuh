@@ -108,6 +108,52 @@ inline void slice_consts(Slice<R>& S, const ot2d_params& p) {
 
 // Fortran SIGN(a,b): |a| with the IEEE sign of b (gfortran semantics).
 template <class R> __device__ __forceinline__ R fsign(R a, R b) { return copysign(fabs(a), b); }
+
+// f32 -> f64 from the bits (sign; exponent rebiased by 1023 - 127; mantissa
+// moved up 29 places): exact for every normal float, zero and inf, NaN
+// stays NaN, subnormal inputs become a zero of their sign as in the mixed
+// path's flush-to-zero arithmetic.  Integer operations only, so the FP64
+// state update keeps GB300's narrow FP64 pipe for its additions.
+__device__ __forceinline__ double f2d_bits_ftz(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint64_t s = (uint64_t)(u >> 31) << 63;
+  const uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  uint64_t r;
+  if (e == 0) r = s;
+  else if (e == 0xffu) r = s | (0x7ffull << 52) | ((uint64_t)m << 29);
+  else r = s | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
+  return __longlong_as_double((long long)r);
+}
+
+// f64 -> f32 from the bits, rounded to nearest, ties to even, with the
+// mixed path's flush to zero: the 29 dropped mantissa bits decide the
+// rounding (the carry of a round-up moves into the exponent, and past the
+// largest finite float into inf); a result below the smallest normal float
+// becomes a zero of its sign unless it rounds up to that float; inf stays
+// inf, NaN stays NaN.  Integer operations only (see f2d_bits_ftz).
+__device__ __forceinline__ float d2f_bits_rn_ftz(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint32_t s = (uint32_t)(b >> 63) << 31;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const uint64_t m = b & 0xfffffffffffffull;
+  uint32_t r;
+  if (e == 0x7ff) {
+    r = s | 0x7f800000u | (m ? (0x400000u | (uint32_t)(m >> 29)) : 0u);
+  } else {
+    const int E = e - 896;   // float exponent field before rounding
+    if (E >= 255) {
+      r = s | 0x7f800000u;
+    } else if (E <= 0) {
+      // [2^-127, 2^-126) rounds to 2^-126 from 2^-126 - 2^-150 up
+      r = (E == 0 && m >= 0xfffffe0000000ull) ? (s | 0x800000u) : s;
+    } else {
+      const uint32_t mant = (uint32_t)(m >> 29), rem = (uint32_t)(m & 0x1fffffffu);
+      const uint32_t up = (rem > 0x10000000u || (rem == 0x10000000u && (mant & 1u))) ? 1u : 0u;
+      r = s | (((uint32_t)E << 23) + mant + up);
+    }
+  }
+  return __uint_as_float(r);
+}
 // MAX / MIN as the oracle evaluates them (first argument on ties).
 template <class R> __device__ __forceinline__ R fmax2(R a, R b) { return (b > a) ? b : a; }
 template <class R> __device__ __forceinline__ R fmin2(R a, R b) { return (b < a) ? b : a; }

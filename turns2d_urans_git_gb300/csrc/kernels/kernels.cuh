@@ -662,7 +662,11 @@ __global__ void __launch_bounds__(CELL_BS / CELL_PT) k_update(const Slice<R>* __
     if (cid >= ncell || j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) continue;
     const int64_t o = at(S.jd, j, k);
     int ibi = S.iblank[o];
-    double m = (double)(ibi > 0 ? ibi : 0);
+    // max(iblank, 0) as a double, the common values without a conversion
+    double m;
+    if (ibi == 1) m = 1.0;
+    else if (ibi <= 0) m = 0.0;
+    else m = (double)ibi;
     // every load before the first store (the state and the residual may not
     // alias, but the compiler cannot know): eight independent loads in flight
     double q0[4];
@@ -672,9 +676,13 @@ __global__ void __launch_bounds__(CELL_BS / CELL_PT) k_update(const Slice<R>* __
     R qn[4];
 #pragma unroll
     for (int n = 0; n < 4; ++n) {
-      double v = q0[n] + (double)sv[n] * m;
+      double sd;
+      if constexpr (sizeof(R) == sizeof(float)) sd = f2d_bits_ftz(sv[n]);
+      else sd = (double)sv[n];
+      double v = q0[n] + sd * m;
       S.q64[n * S.qs + o] = v;
-      qn[n] = (R)v;
+      if constexpr (sizeof(R) == sizeof(float)) qn[n] = d2f_bits_rn_ftz(v);
+      else qn[n] = (R)v;
       if constexpr (sizeof(R) != sizeof(double)) S.q[n * S.qs + o] = qn[n];
     }
     // monitor of the updated cell (step.f:356-370), free of divisions:
