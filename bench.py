@@ -50,11 +50,11 @@ PHASES = ["time_step", "bc", "residual", "rbc", "lusgs", "sa", "update"]
 # DRAM bytes per interior cell per launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of the batch-8 capture, 0.52 M cells, summarised in
 # profiles/top_kernels_rans_sa_513x129_b8_fp32mixed.md), scaled to the batch
-TRAFFIC_PER_CELL = {"residual": (40.495616e6 + 0.305408e6) / (8 * 65536),
+TRAFFIC_PER_CELL = {"residual": (40.498176e6 + 1.443328e6) / (8 * 65536),
                     # k_lu_prep + both sweeps (k_lu_edges, ~1 % of the phase, not captured)
-                    "lusgs": (31.611136e6 + 8.900608e6 + 62.373376e6 + 2.380288e6 + 62.384384e6 + 1.123840e6)
+                    "lusgs": (31.610880e6 + 9.473536e6 + 62.373632e6 + 2.156800e6 + 62.384384e6 + 1.083648e6)
                     / (8 * 65536),
-                    "update": (27.407616e6 + 0.065024e6) / (8 * 65536)}
+                    "update": (27.421952e6 + 0.079360e6) / (8 * 65536)}
 NPH = len(PHASES)
 
 
