@@ -437,7 +437,7 @@ int DevBatch<R>::build(const std::vector<Slice<R>>& sl, cudaStream_t st) {
     cells += (jd * kd + CELL_BS - 1) / CELL_BS;
     jl += kd - 2;   // k-lines solved along j
     kl += jd - 2;   // j-lines solved along k
-    lub += (lu_nband(kd) * lu_nstep(jd) * 32 + CELL_BS - 1) / CELL_BS;
+    lub += (lu_nband(kd) * lu_nstep(jd) * 32 + LU_PREP_BS - 1) / LU_PREP_BS;
     grp += lu_nband(kd);
     tiles += ((jd - 2 + tj - 1) / tj) * ((kd - 2 + tk - 1) / tk);
     maxw = std::max(maxw, lu_nband(kd));

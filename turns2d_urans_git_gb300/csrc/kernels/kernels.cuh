@@ -350,24 +350,26 @@ __global__ void k_rbc(const Slice<R>* __restrict__ sl) {
 
 // ilu2d (lhs.f:470-814), preceded by s *= tscale on all cells when `scale`
 // (step.f:141-148).  Records of the interior cells (prefix table lfirst):
-// a block of CELL_BS threads builds LU_PREP_CH consecutive chunks of the
-// band layout.  Lane l of chunk (band, t) is cell (row 32 band + l, column
-// t - l), so the chunks' lanes walk the grid diagonally; thread i computes
-// lane i / 8 of chunk i % 8 instead, which makes eight consecutive threads
-// read eight consecutive cells of one row (the lane-per-thread order would
-// touch a different row, and cache line, per thread).  The records go to
-// the block's shared-memory copy of its chunks (chunk stride padded by 16
-// bytes so the eight chunks of one row land in different banks), then each
-// warp stores one chunk with contiguous 16-byte accesses.  PRE: the
+// a block of LU_PREP_BS threads builds LU_PREP_CH = 16 consecutive chunks of
+// the band layout.  Lane l of chunk (band, t) is cell (row 32 band + l,
+// column t - l), so the chunks' lanes walk the grid diagonally; thread i
+// computes lane i / 16 of chunk i % 16 instead, which makes sixteen
+// consecutive threads read sixteen consecutive cells (64 bytes of each
+// array) of one row (the lane-per-thread order would touch a different row,
+// and cache line, per thread).  The records go to the block's shared-memory
+// copy of its chunks (chunk stride padded by 16 bytes so the chunks of one
+// row land in different banks), then each warp stores one chunk with one
+// bulk copy.  PRE: the
 // preconditioned (preilu2d) records of the slices with k_mp2 >= 0; each
 // instantiation returns on the other kind's slices.
-constexpr int LU_PREP_CH = CELL_BS / 32;   // chunks per block
+constexpr int LU_PREP_CH = LU_PREP_BS / 32;   // chunks per block
 template <class R, bool PRE>
 __host__ __device__ constexpr int lu_prep_stride() { return LuLay<R, PRE>::CH + (int)(16 / sizeof(R)); }
 template <class R, bool PRE>
-__global__ void __launch_bounds__(CELL_BS) k_lu_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst,
+__global__ void __launch_bounds__(LU_PREP_BS) k_lu_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ lfirst,
                                                      int nslice, int scale, int only_lu) {
-  static_assert(CELL_BS == 256, "thread -> (chunk, lane) map assumes 8 chunks of 32 lanes");
+  static_assert(LU_PREP_CH * 32 == LU_PREP_BS && (LU_PREP_CH & (LU_PREP_CH - 1)) == 0,
+                "thread -> (chunk, lane) map: a power-of-two number of 32-lane chunks");
   extern __shared__ __align__(16) unsigned char lp_smem[];
   const int si = find_slice(lfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];

@@ -12,6 +12,8 @@ template <class R> struct Slice;
 struct NormPart;
 
 constexpr int CELL_BS = 256;
+// the LU-SGS record kernel: threads per block (LU_PREP_BS / 32 chunks each)
+constexpr int LU_PREP_BS = 512;
 // threads of the one-CTA-per-slice boundary kernels (their loops run along
 // the boundary rows; more threads, fewer serial passes per row)
 constexpr int BC_BS = 512;

@@ -111,7 +111,7 @@ cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale,
     return cudaFuncSetAttribute(k_lu_prep<R, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
   });
   if (ae != cudaSuccess) return ae;
-  k_lu_prep<R, PRE><<<b.lu_blocks, CELL_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
+  k_lu_prep<R, PRE><<<b.lu_blocks, LU_PREP_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
   if constexpr (sizeof(R) == sizeof(double)) {
     // every cell: the FP64 path also round-trips q (lhs.f:524-531, :805-811)
     k_lu_edges<R, PRE><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
