@@ -14,13 +14,10 @@ struct SAc {
   static constexpr double cw2 = 0.3, cw3 = 2., cv1 = 7.1, ct3 = 1.2, ct4 = 0.5;
 };
 
-// The transcendental terms of the SA source (samodel2d.f:767-778): libm in
-// the FP64 path (the reference's pow / exp); in the f32 path the hardware
-// exp2 / log2 forms (a few ulp) and r**5. as products.
-template <class R> __device__ __forceinline__ R sa_exp(R x) {
-  if constexpr (sizeof(R) == sizeof(float)) return __expf(x);
-  else return exp(x);
-}
+// The transcendental terms of the SA source (samodel2d.f:767-778): libm's
+// pow in the FP64 path, as the reference; in the f32 path the hardware
+// exp2 / log2 form (a few ulp) and r**5. as products.  (The transition
+// term's exponential multiplies fturf = 0 and is not evaluated.)
 // x**y for x > 0
 template <class R> __device__ __forceinline__ R sa_pow_pos(R x, R y) {
   if constexpr (sizeof(R) == sizeof(float)) return __powf(x, y);
@@ -148,7 +145,10 @@ __device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int 
     R fv1 = (cube(chi)) / (cube(chi) + cube(cv1));
     R fv2 = (R)1. - chi / ((R)1. + chi * fv1);
     R fv3 = (R)1.0;
-    R ft2 = fturf * ct3 * sa_exp((R)-1. * ct4 * chi * chi);
+    // ft2 = fturf * ct3 * exp(-ct4 chi^2) with fturf = 0: +0 exactly (the
+    // exponential is finite and positive), so it is not evaluated
+    R ft2 = (R)0.0;
+    (void)fturf; (void)ct3;
     R dchi = (R)1. / vnul;
     R dfv1 = ((R)3. * cube(cv1)) * (sq(chi)) * dchi * sq((R)1. / (cube(chi) + cube(cv1)));
     R dfv2 = (fv2 - (R)1.) / chi / vnul + ((R)1. - fv2) * ((R)1 - fv2) * (dfv1 + fv1 / chi / vnul);
@@ -160,12 +160,14 @@ __device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int 
     R r = q5 / (d2 * akt * akt * rey) / stilda;
     r = fmin2(r, rmax);
     R g = r + cw2 * (pow6(r) - r);
-    R fw = ((R)1. + pow6(cw3)) / (pow6(g) + pow6(cw3));
-    fw = g * (sa_pow_pos(fw, (R)(1. / 6.)));
+    // ((1 + cw3^6) / (g^6 + cw3^6))^(1/6), which fw and its derivative
+    // both take (samodel2d.f:767-778): one power for the two
+    const R fw6 = sa_pow_pos(((R)1. + pow6(cw3)) / (pow6(g) + pow6(cw3)), (R)(1. / 6.));
+    R fw = g * fw6;
     R dstild = vort * dfv3 + vnul * (dchi * fv2 + chi * dfv2) / (d2 * akt * akt * rey);
     R dr = vnul * (dchi - chi * dstild / stilda) / stilda / (d2 * akt * akt * rey);
     R dg = dr * ((R)1. + cw2 * ((R)6. * sa_pow5(r) - (R)1.));
-    R dfw = sa_pow_pos(((R)1. + pow6(cw3)) / (pow6(g) + pow6(cw3)), (R)(1. / 6.));
+    R dfw = fw6;
     dfw = dfw * dg * ((R)1. - pow6(g) / (pow6(g) + pow6(cw3)));
     R pro = cb1 * stilda * ((R)1. - ft2);
     R des = (cw1 * fw - cb1 / (akt * akt) * ft2) / d2 / rey;

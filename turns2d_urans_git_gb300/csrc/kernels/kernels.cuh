@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(CELL_BS) k_assemble(const Slice<R>* __restrict
 // tile is done exactly once).  One family per kernel keeps the WENO windows
 // out of the MUSCL kernel's registers and code.
 template <class R, bool PRE, int LIM, int TJ, int TK>
-__global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 1) k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst,
+__global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 2) k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst,
                                                   int nslice, int flags, NormPart* __restrict__ part) {
   extern __shared__ __align__(16) unsigned char rt_raw[];
   const int si = find_slice(tfirst, nslice, blockIdx.x);
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(BC_BS) k_turbc(const Slice<R>* __restrict__ sl
 }
 
 template <class R>
-__global__ void __launch_bounds__(CELL_BS, sizeof(R) == 4 ? 4 : 1) k_sa_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
+__global__ void __launch_bounds__(CELL_BS, sizeof(R) == 4 ? 4 : 2) k_sa_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
                                                     int nslice) {
   OT2D_CELL_MAP();
   if (!inside) return;
