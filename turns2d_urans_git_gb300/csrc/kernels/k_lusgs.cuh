@@ -496,7 +496,7 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
     if (__any_sync(0xffffffffu, !ok || bad)) { gfail = g; break; }
     const int gs = gsize(g);
     const R* gring = ring + (size_t)(g & 1) * G * CH;
-#pragma unroll 1
+#pragma unroll 4
     for (int u = 0; u < gs; ++u) {
       const int tl = g * G + u;
       // this lane's record: residual, (tscale/2, d, u, v), (uv2, ge, xi

@@ -51,38 +51,57 @@ struct SAnb {  // convec upwind split at one cell (samodel2d.f:477-484)
   R up, um, vp, vm;
 };
 template <class R>
-__device__ __forceinline__ SAnb<R> sa_split(const Slice<R>& S, int j, int k) {
-  const int64_t o = at(S.jd, j, k), ws = S.wstride;
-  R u = S.w[W_U * ws + o], v = S.w[W_V * ws + o];
-  R ugc = S.ug ? S.ug[o] : (R)0, vgc = S.vg ? S.vg[o] : (R)0;
-  R uu = S.xx[o] * (u - ugc) + S.xy[o] * (v - vgc);
-  R vv = S.yx[o] * (u - ugc) + S.yy[o] * (v - vgc);
+__device__ __forceinline__ SAnb<R> sa_split_of(R u, R v, R ugc, R vgc, R xx, R xy, R yx, R yy) {
+  R uu = xx * (u - ugc) + xy * (v - vgc);
+  R vv = yx * (u - ugc) + yy * (v - vgc);
   SAnb<R> r;
   r.up = (R)0.5 * (uu + fabs(uu)); r.um = (R)0.5 * (uu - fabs(uu));
   r.vp = (R)0.5 * (vv + fabs(vv)); r.vm = (R)0.5 * (vv - fabs(vv));
   return r;
 }
 
+// The values sa_rhs_cell reads at a cell and its four neighbours, staged
+// for a tile of cells in shared memory (k_sa_rhs): the velocities of
+// sa_prep, the grid speeds (zero on a fixed grid), the metrics, nu_tilde
+// and the laminar kinematic viscosity vmul/q1/J.
+enum SAst { SA_U = 0, SA_V, SA_XX, SA_XY, SA_YX, SA_YY, SA_Q5, SA_NUL, SA_UG, SA_VG, SA_NST };
+template <class R>
+struct SaTile {
+  const R* sm; int nr, rw, jr, kr; bool gs;   // region origin (jr, kr); gs: grid speeds staged
+  __device__ __forceinline__ R g(int a, int j, int k) const { return sm[a * nr + (k - kr) * rw + (j - jr)]; }
+  __device__ __forceinline__ R u(int j, int k) const { return g(SA_U, j, k); }
+  __device__ __forceinline__ R v(int j, int k) const { return g(SA_V, j, k); }
+  __device__ __forceinline__ R xx(int j, int k) const { return g(SA_XX, j, k); }
+  __device__ __forceinline__ R xy(int j, int k) const { return g(SA_XY, j, k); }
+  __device__ __forceinline__ R yx(int j, int k) const { return g(SA_YX, j, k); }
+  __device__ __forceinline__ R yy(int j, int k) const { return g(SA_YY, j, k); }
+  __device__ __forceinline__ R q5(int j, int k) const { return g(SA_Q5, j, k); }
+  __device__ __forceinline__ R nul(int j, int k) const { return g(SA_NUL, j, k); }
+  __device__ __forceinline__ SAnb<R> split(int j, int k) const {
+    return sa_split_of(u(j, k), v(j, k), gs ? g(SA_UG, j, k) : (R)0, gs ? g(SA_VG, j, k) : (R)0, xx(j, k), xy(j, k),
+                       yx(j, k), yy(j, k));
+  }
+};
+
 // RHS and bands of one interior cell: rhslhs (samodel2d.f:402-450) with
 // convec (:453-542), diffus (:545-688), source (:691-824), then the time
 // scaling of vmu_sa (:96-134).  Writes sjmat, aj, cj, ak, ck, bjmat.
-template <class R>
-__device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int k, bool bodyflag) {
+template <class R, class A>
+__device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int k, bool bodyflag,
+                            const A& a) {
   const int jd = S.jd; const int64_t qs = S.qs, ws = S.wstride;
   const int n5 = p.nmv + 1, nq = p.nq;
   const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
   auto Q = [&](int jj, int kk, int n) { return S.q[(int64_t)(n - 1) * qs + at(jd, jj, kk)]; };
-  auto W = [&](int a, int jj, int kk) { return S.w[a * ws + at(jd, jj, kk)]; };
-  auto Mx = [&](const R* a, int jj, int kk) { return a[at(jd, jj, kk)]; };
   const int64_t o = at(jd, j, k);
   const R rey = S.k_rey;
   // ---- convec
-  SAnb<R> c0 = sa_split(S, j, k), cjm = sa_split(S, j - 1, k), cjp = sa_split(S, j + 1, k);
-  SAnb<R> ckm = sa_split(S, j, k - 1), ckp = sa_split(S, j, k + 1);
-  R q5 = Q(j, k, n5);
+  SAnb<R> c0 = a.split(j, k), cjm = a.split(j - 1, k), cjp = a.split(j + 1, k);
+  SAnb<R> ckm = a.split(j, k - 1), ckp = a.split(j, k + 1);
+  R q5 = a.q5(j, k);
   R sj = S.s[(int64_t)(n5 - 1) * qs + o];
-  sj = sj - c0.up * (q5 - Q(j - 1, k, n5)) - c0.um * (Q(j + 1, k, n5) - q5);
-  sj = sj - c0.vp * (q5 - Q(j, k - 1, n5)) - c0.vm * (Q(j, k + 1, n5) - q5);
+  sj = sj - c0.up * (q5 - a.q5(j - 1, k)) - c0.um * (a.q5(j + 1, k) - q5);
+  sj = sj - c0.vp * (q5 - a.q5(j, k - 1)) - c0.vm * (a.q5(j, k + 1) - q5);
   R aj = (R)0., cj = (R)0., ak = (R)0., ck = (R)0.;
   if (j >= js + 1) aj = aj - ((c0.up > (R)1.0e-12) ? (R)1.0 : (R)0.0) * (cjm.up + cjm.um);
   if (j <= je - 1) cj = cj + ((c0.um < (R)-1.0e-12) ? (R)1.0 : (R)0.0) * (cjp.up + cjp.um);
@@ -93,17 +112,17 @@ __device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int 
   // ---- diffus
   const R chpc = (R)((1. + SAc::cb2) / SAc::sigma) / rey;
   const R c2c = (R)(SAc::cb2 / SAc::sigma) / rey;
-  auto nul = [&](int jj, int kk) { return W(W_VMUL, jj, kk) / Q(jj, kk, 1) / Q(jj, kk, nq); };
+  auto nul = [&](int jj, int kk) { return a.nul(jj, kk); };
   {
     // half points j-1/2 (index j-1) and j+1/2 (index j)
-    R dmxh_m = (R)0.5 * (Mx(S.xx, j - 1, k) + Mx(S.xx, j, k)), dmyh_m = (R)0.5 * (Mx(S.xy, j - 1, k) + Mx(S.xy, j, k));
-    R dmxh_p = (R)0.5 * (Mx(S.xx, j, k) + Mx(S.xx, j + 1, k)), dmyh_p = (R)0.5 * (Mx(S.xy, j, k) + Mx(S.xy, j + 1, k));
+    R dmxh_m = (R)0.5 * (a.xx(j - 1, k) + a.xx(j, k)), dmyh_m = (R)0.5 * (a.xy(j - 1, k) + a.xy(j, k));
+    R dmxh_p = (R)0.5 * (a.xx(j, k) + a.xx(j + 1, k)), dmyh_p = (R)0.5 * (a.xy(j, k) + a.xy(j + 1, k));
     R n0 = nul(j, k), nm = nul(j - 1, k), np = nul(j + 1, k);
-    R chp_m = chpc * ((R)0.5 * (nm + n0) + (R)0.5 * (Q(j - 1, k, n5) + q5));
-    R chp_p = chpc * ((R)0.5 * (n0 + np) + (R)0.5 * (q5 + Q(j + 1, k, n5)));
-    R dn_m = q5 - Q(j - 1, k, n5), dn_p = Q(j + 1, k, n5) - q5;
-    R dxp = dmxh_p * Mx(S.xx, j, k) + dmyh_p * Mx(S.xy, j, k);
-    R dxm = dmxh_m * Mx(S.xx, j, k) + dmyh_m * Mx(S.xy, j, k);
+    R chp_m = chpc * ((R)0.5 * (nm + n0) + (R)0.5 * (a.q5(j - 1, k) + q5));
+    R chp_p = chpc * ((R)0.5 * (n0 + np) + (R)0.5 * (q5 + a.q5(j + 1, k)));
+    R dn_m = q5 - a.q5(j - 1, k), dn_p = a.q5(j + 1, k) - q5;
+    R dxp = dmxh_p * a.xx(j, k) + dmyh_p * a.xy(j, k);
+    R dxm = dmxh_m * a.xx(j, k) + dmyh_m * a.xy(j, k);
     R c2 = c2c * (n0 + q5);
     R dcp = dxp * (chp_p - c2), dcm = dxm * (chp_m - c2);
     R ax = fmax2(dcm, (R)0.0), cx = fmax2(dcp, (R)0.0);
@@ -111,14 +130,14 @@ __device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int 
     aj = aj - ax; cj = cj - cx; bj = bj + ax + cx;
   }
   {
-    R dmxh_m = (R)0.5 * (Mx(S.yx, j, k - 1) + Mx(S.yx, j, k)), dmyh_m = (R)0.5 * (Mx(S.yy, j, k - 1) + Mx(S.yy, j, k));
-    R dmxh_p = (R)0.5 * (Mx(S.yx, j, k) + Mx(S.yx, j, k + 1)), dmyh_p = (R)0.5 * (Mx(S.yy, j, k) + Mx(S.yy, j, k + 1));
+    R dmxh_m = (R)0.5 * (a.yx(j, k - 1) + a.yx(j, k)), dmyh_m = (R)0.5 * (a.yy(j, k - 1) + a.yy(j, k));
+    R dmxh_p = (R)0.5 * (a.yx(j, k) + a.yx(j, k + 1)), dmyh_p = (R)0.5 * (a.yy(j, k) + a.yy(j, k + 1));
     R n0 = nul(j, k), nm = nul(j, k - 1), np = nul(j, k + 1);
-    R chp_m = chpc * ((R)0.5 * (nm + n0) + (R)0.5 * (Q(j, k - 1, n5) + q5));
-    R chp_p = chpc * ((R)0.5 * (n0 + np) + (R)0.5 * (q5 + Q(j, k + 1, n5)));
-    R dn_m = q5 - Q(j, k - 1, n5), dn_p = Q(j, k + 1, n5) - q5;
-    R dyp = dmxh_p * Mx(S.yx, j, k) + dmyh_p * Mx(S.yy, j, k);
-    R dym = dmxh_m * Mx(S.yx, j, k) + dmyh_m * Mx(S.yy, j, k);
+    R chp_m = chpc * ((R)0.5 * (nm + n0) + (R)0.5 * (a.q5(j, k - 1) + q5));
+    R chp_p = chpc * ((R)0.5 * (n0 + np) + (R)0.5 * (q5 + a.q5(j, k + 1)));
+    R dn_m = q5 - a.q5(j, k - 1), dn_p = a.q5(j, k + 1) - q5;
+    R dyp = dmxh_p * a.yx(j, k) + dmyh_p * a.yy(j, k);
+    R dym = dmxh_m * a.yx(j, k) + dmyh_m * a.yy(j, k);
     R c2 = c2c * (n0 + q5);
     R dcp = dyp * (chp_p - c2), dcm = dym * (chp_m - c2);
     R ay = fmax2(dcm, (R)0.0), cy = fmax2(dcp, (R)0.0);
@@ -133,13 +152,13 @@ __device__ void sa_rhs_cell(const Slice<R>& S, const ot2d_params& p, int j, int 
     R vort = (R)0.0, d = (R)1.e10;
     if (bodyflag) {
       const R dx2 = (R)0.5, dy2 = (R)0.5;
-      R ux = (W(W_U, j + 1, k) - W(W_U, j - 1, k)) * dx2, vx = (W(W_V, j + 1, k) - W(W_V, j - 1, k)) * dx2;
-      R uy = (W(W_U, j, k + 1) - W(W_U, j, k - 1)) * dy2, vy = (W(W_V, j, k + 1) - W(W_V, j, k - 1)) * dy2;
-      R tx = Mx(S.xy, j, k) * ux - Mx(S.xx, j, k) * vx + Mx(S.yy, j, k) * uy - Mx(S.yx, j, k) * vy;
+      R ux = (a.u(j + 1, k) - a.u(j - 1, k)) * dx2, vx = (a.v(j + 1, k) - a.v(j - 1, k)) * dx2;
+      R uy = (a.u(j, k + 1) - a.u(j, k - 1)) * dy2, vy = (a.v(j, k + 1) - a.v(j, k - 1)) * dy2;
+      R tx = a.xy(j, k) * ux - a.xx(j, k) * vx + a.yy(j, k) * uy - a.yx(j, k) * vy;
       vort = fabs(tx);
       d = S.sn[o];
     }
-    R vnul = W(W_VMUL, j, k) / Q(j, k, 1) / Q(j, k, nq);
+    R vnul = a.nul(j, k);
     R chi = q5 / vnul;
     chi = fmax2(chi, (R)1.e-12);
     R fv1 = (cube(chi)) / (cube(chi) + cube(cv1));

@@ -466,17 +466,64 @@ __global__ void __launch_bounds__(BC_BS) k_turbc(const Slice<R>* __restrict__ sl
   }
 }
 
-template <class R>
-__global__ void __launch_bounds__(CELL_BS, sizeof(R) == 4 ? 4 : 2) k_sa_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
-                                                    int nslice) {
-  OT2D_CELL_MAP();
-  if (!inside) return;
+// RHS and bands of the SA solve (samodel2d.f:402-450, :96-134) on tiles of
+// TJ x TK interior cells, the residual's tile table: every value read at a
+// cell and its four neighbours is staged once per tile (region with a
+// one-cell halo) in shared memory, then each thread assembles its cell.
+template <class R, int TJ, int TK>
+__global__ void __launch_bounds__(TJ * TK, sizeof(R) == 4 ? 4 : 2)
+    k_sa_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst, int nslice) {
+  static_assert(TJ * TK == 256, "one cell per thread");
+  extern __shared__ __align__(16) unsigned char sa_raw[];
+  const int si = find_slice(tfirst, nslice, blockIdx.x);
+  const Slice<R>& S = sl[si];
   const ot2d_params& p = *S.P;
-  if (p.lamin || p.iturb != 1) return;
-  if (j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) return;
+  if (p.lamin || p.iturb != 1) return;   // uniform over the block
+  const int tile = blockIdx.x - tfirst[si];
+  const int ntj = (p.jend - p.jbeg + TJ) / TJ;
+  const int j0 = p.jbeg + (tile % ntj) * TJ, k0 = p.kbeg + (tile / ntj) * TK;
+  const int j1 = min(j0 + TJ - 1, p.jend), k1 = min(k0 + TK - 1, p.kend);
+  constexpr int RW = TJ + 2, NR = RW * (TK + 2);
+  R* sm = (R*)sa_raw;
+  const int jd = S.jd, kd = S.kd, t = threadIdx.x;
+  const int64_t ws = S.wstride, n5 = p.nmv + 1, nq = p.nq;
+  const bool gs = S.ug != nullptr;
+  // every load of a thread's staged cells before the first store
+  constexpr int NSTG = (NR + TJ * TK - 1) / (TJ * TK);
+  R val[NSTG][SA_NST + 2];
+#pragma unroll
+  for (int i = 0; i < NSTG; ++i) {
+    const int r = t + i * TJ * TK;
+    const int j = j0 - 1 + r % RW, k = k0 - 1 + r / RW;
+    if (r >= NR || j < 1 || j > jd || k < 1 || k > kd) continue;
+    const int64_t o = at(jd, j, k);
+    val[i][SA_U] = S.w[W_U * ws + o]; val[i][SA_V] = S.w[W_V * ws + o];
+    val[i][SA_XX] = S.xx[o]; val[i][SA_XY] = S.xy[o]; val[i][SA_YX] = S.yx[o]; val[i][SA_YY] = S.yy[o];
+    val[i][SA_Q5] = S.q[(n5 - 1) * S.qs + o];
+    val[i][SA_NUL] = S.w[W_VMUL * ws + o];      // vmul, q1, J: nul below
+    val[i][SA_NST] = S.q[o];
+    val[i][SA_NST + 1] = S.q[(nq - 1) * S.qs + o];
+    if (gs) { val[i][SA_UG] = S.ug[o]; val[i][SA_VG] = S.vg[o]; }
+  }
+#pragma unroll
+  for (int i = 0; i < NSTG; ++i) {
+    const int r = t + i * TJ * TK;
+    const int j = j0 - 1 + r % RW, k = k0 - 1 + r / RW;
+    if (r >= NR || j < 1 || j > jd || k < 1 || k > kd) continue;
+#pragma unroll
+    for (int a = 0; a < SA_UG; ++a)
+      sm[a * NR + r] = a == SA_NUL ? val[i][SA_NUL] / val[i][SA_NST] / val[i][SA_NST + 1] : val[i][a];
+    if (gs) { sm[SA_UG * NR + r] = val[i][SA_UG]; sm[SA_VG * NR + r] = val[i][SA_VG]; }
+  }
+  __syncthreads();
   bool bodyflag = false;
   for (int ib = 0; ib < p.nbc; ++ib) if (p.ibtyp[ib] == 5) bodyflag = true;
-  sa_rhs_cell(S, p, j, k, bodyflag);
+  const int j = j0 + t % TJ, k = k0 + t / TJ;
+  if (j <= j1 && k <= k1) sa_rhs_cell(S, p, j, k, bodyflag, SaTile<R>{sm, NR, RW, j0 - 1, k0 - 1, gs});
+}
+template <class R, int TJ, int TK>
+__host__ __device__ constexpr size_t sa_rhs_smem() {
+  return sizeof(R) * (size_t)SA_NST * (TJ + 2) * (TK + 2);
 }
 
 // line solves: slice i owns lines [lfirst[i], lfirst[i+1]) (one thread each)

@@ -198,7 +198,12 @@ template <class R>
 cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_sa_prep<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 0);
-  k_sa_rhs<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
+  // on the residual's tiles (tile table of the batch's tile shape)
+  switch (b.rt_shape) {
+    case 1: k_sa_rhs<R, 32, 8><<<b.tile_blocks, 256, sa_rhs_smem<R, 32, 8>(), st>>>(d_sl, b.d_tfirst, b.nslice); break;
+    case 2: k_sa_rhs<R, 8, 32><<<b.tile_blocks, 256, sa_rhs_smem<R, 8, 32>(), st>>>(d_sl, b.d_tfirst, b.nslice); break;
+    default: k_sa_rhs<R, 16, 16><<<b.tile_blocks, 256, sa_rhs_smem<R, 16, 16>(), st>>>(d_sl, b.d_tfirst, b.nslice);
+  }
   constexpr size_t lj_smem = sizeof(R) * LJ_SMEM;
   static DeviceOnce once;
   cudaError_t ae = once.run([&](int&) {
