@@ -219,6 +219,15 @@ template <class R> DevBatch<R>* halves_of(ot2d_solver* s);
 template <> DevBatch<double>* halves_of<double>(ot2d_solver* s) { return s->h64; }
 template <> DevBatch<float>* halves_of<float>(ot2d_solver* s) { return s->h32; }
 
+// With the time step folded into the state update, the first iteration of a
+// new batch still needs it: computed now from the current state (for the
+// requests already running, the values the last update computed).
+template <class R>
+int time_step_now(ot2d_solver* s, DevBatch<R>& B) {
+  if (!B.b.ts_in_update) return OT2D_OK;
+  return launch_time_step<R>(B.d_sl, B.b, s->st) == cudaSuccess ? OT2D_OK : OT2D_ERR_CUDA;
+}
+
 template <class R>
 int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   drop_graph(s);
@@ -252,6 +261,15 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   int e = B.build(sl, s->st);
   if (e) return e;
   B.b.poll_limit = s->poll_limit;
+  // the next iteration's time step in the state update: every request
+  // steady with a first-order time step factor (nothing between the update
+  // and the next time step then changes what the time step reads)
+  bool fuse_ts = true;
+  for (int id : s->live) {
+    const ot2d_params& pp = s->recs[id].d.P;
+    if (pp.iunst != 0 || pp.ntac > 1 || pp.itnmax > 1) fuse_ts = false;
+  }
+  B.b.ts_in_update = fuse_ts ? 1 : 0;
   B.b.lu_lag = ch.lu_lag;
   B.b.lu_group = ch.lu_group;
   // The kernels branch on each slice's own params, so inviscid, laminar,
@@ -270,7 +288,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
     if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
     // the host-buffer path overlaps one half's copies with the other
     // half's iteration, so it wants the halves' graphs as well
-    if (!(s->want_halves && can_split)) return OT2D_OK;
+    if (!(s->want_halves && can_split)) return time_step_now<R>(s, B);
   }
   // two halves of about equal cells (a request's time instances stay in one
   // half: the time-spectral source couples them)
@@ -295,6 +313,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
     H[h].rt_shape = ch.rt_shape;
     if ((e = H[h].build(slh[h], s->st))) return e;
     H[h].b.poll_limit = s->poll_limit;
+    H[h].b.ts_in_update = B.b.ts_in_update;
     H[h].b.lu_lag = ch.lu_lag;
     H[h].b.lu_group = ch.lu_group;
     cudaStream_t cs = h == 0 ? s->st : s->st2;
@@ -306,7 +325,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   }
   s->halves = true;
   s->split = split;
-  return OT2D_OK;
+  return time_step_now<R>(s, B);
 }
 
 int rebuild(ot2d_solver* s) {
@@ -372,23 +391,26 @@ int profile_t(ot2d_solver* s, DevBatch<R>& B, int iters, double* ms) {
   for (auto& e : ev) cudaEventCreate(&e);
   for (int p = 0; p < OT2D_NPHASE; ++p) ms[p] = 0.0;
   const int visc = s->any_viscous ? 1 : 0, turb = s->turb_bits;
+  // each phase on its own: the time step as a kernel of its own here
+  Batch bp = B.b;
+  bp.ts_in_update = 0;
   int err = OT2D_OK;
   for (int it = 0; it < iters && !err; ++it) {
     cudaError_t e = cudaSuccess;
     auto rec = [&](int i) { cudaEventRecord(ev[i], s->st); };
     rec(0);
-    e = launch_iter_begin<R>(B.d_sl, B.b, s->st);
-    if (!e) e = launch_time_step<R>(B.d_sl, B.b, s->st); rec(1);
-    if (!e) e = launch_bc<R>(B.d_sl, B.b, 1, s->st); rec(2);
-    if (!e) e = launch_residual<R>(B.d_sl, B.b, visc, s->st); rec(3);
-    if (!e) e = launch_rbc<R>(B.d_sl, B.b, s->st); rec(4);
-    if (!e && (s->lhs_bits & 1)) e = launch_lusgs<R>(B.d_sl, B.b, 1, s->st, 1);
-    if (!e && (s->lhs_bits & 2)) e = launch_adi<R>(B.d_sl, B.b, 1, s->st, 1);
+    e = launch_iter_begin<R>(B.d_sl, bp, s->st);
+    if (!e) e = launch_time_step<R>(B.d_sl, bp, s->st); rec(1);
+    if (!e) e = launch_bc<R>(B.d_sl, bp, 1, s->st); rec(2);
+    if (!e) e = launch_residual<R>(B.d_sl, bp, visc, s->st); rec(3);
+    if (!e) e = launch_rbc<R>(B.d_sl, bp, s->st); rec(4);
+    if (!e && (s->lhs_bits & 1)) e = launch_lusgs<R>(B.d_sl, bp, 1, s->st, 1);
+    if (!e && (s->lhs_bits & 2)) e = launch_adi<R>(B.d_sl, bp, 1, s->st, 1);
     rec(5);
-    if (!e && (turb & 1)) e = launch_sa<R>(B.d_sl, B.b, s->st);
-    if (!e && (turb & 2)) e = launch_sst<R>(B.d_sl, B.b, s->st);
+    if (!e && (turb & 1)) e = launch_sa<R>(B.d_sl, bp, s->st);
+    if (!e && (turb & 2)) e = launch_sst<R>(B.d_sl, bp, s->st);
     rec(6);
-    if (!e) e = launch_update<R>(B.d_sl, B.b, s->st);
+    if (!e) e = launch_update<R>(B.d_sl, bp, s->st);
     rec(7);
     if (e != cudaSuccess || cudaEventSynchronize(ev[7]) != cudaSuccess) { err = OT2D_ERR_CUDA; break; }
     for (int p = 0; p < OT2D_NPHASE; ++p) {
@@ -887,6 +909,17 @@ int ot2d_solver_graph_kernels(ot2d_solver* s) {
   return a < 0 ? a : (b < 0 ? b : a + b);
 }
 
+// The time step of the whole batch (half < 0) or of one half, when the
+// batch folds it into the state update: after a host-buffer upload.
+cudaError_t host_time_step(ot2d_solver* s, int half, cudaStream_t st) {
+  if (s->precision == OT2D_FP32_MIXED) {
+    DevBatch<float>& B = half < 0 ? s->b32 : s->h32[half];
+    return B.b.ts_in_update ? launch_time_step<float>(B.d_sl, B.b, st) : cudaSuccess;
+  }
+  DevBatch<double>& B = half < 0 ? s->b64 : s->h64[half];
+  return B.b.ts_in_update ? launch_time_step<double>(B.d_sl, B.b, st) : cudaSuccess;
+}
+
 // Host-buffer iterations over a batch with halves: per iteration, half h
 // uploads its listed instances on its stream (each upload after that
 // instance's previous download), makes its compute copy, runs its graph
@@ -916,6 +949,8 @@ int iterate_host_halves(ot2d_solver* s, int32_t n, std::vector<Rec*>& rs, double
       if (!err && s->precision == OT2D_FP32_MIXED &&
           launch_shadow<float>(s->h32[h].d_sl, s->h32[h].b, sh[h]) != cudaSuccess)
         err = OT2D_ERR_CUDA;
+      // the uploaded state may differ from the one the last update saw
+      if (!err && host_time_step(s, h, sh[h]) != cudaSuccess) err = OT2D_ERR_CUDA;
       if (!err && (cudaStreamWaitEvent(sh[h], s->ev_half[1 - h], 0) != cudaSuccess ||
                    cudaGraphLaunch(s->hexec[h], sh[h]) != cudaSuccess ||
                    cudaEventRecord(s->ev_hdone[h], sh[h]) != cudaSuccess ||
@@ -999,6 +1034,8 @@ int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, doub
     }
     if (!err && s->precision == OT2D_FP32_MIXED && launch_shadow<float>(s->b32.d_sl, s->b32.b, s->st) != cudaSuccess)
       err = OT2D_ERR_CUDA;
+    // the uploaded state may differ from the one the last update saw
+    if (!err && host_time_step(s, -1, s->st) != cudaSuccess) err = OT2D_ERR_CUDA;
     if (!err && (launch_graph_iteration(s) != cudaSuccess || join_halves(s) != cudaSuccess)) err = OT2D_ERR_CUDA;
     if (!err && (cudaEventRecord(s->ev_step, s->st) != cudaSuccess ||
                  cudaStreamWaitEvent(s->st_d2h, s->ev_step, 0) != cudaSuccess))

@@ -9,16 +9,16 @@
 namespace ot2d {
 
 // ---------------------------------------------------------------- time step
+// The local time step of cell o (time.f:2-108) from its state: tscale and
+// bt.  J is read only in the Jacobian-scaled form (iconstant_cfl = 0),
+// q1..q4 only in the spectral-radius form.
 template <class R>
-__device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
-  const ot2d_params& p = *S.P;
-  const int jd = S.jd; const int64_t o = at(jd, j, k), qs = S.qs;
-  const R* q = S.q;
+__device__ __forceinline__ void time_step_vals(const Slice<R>& S, const ot2d_params& p, int64_t o, int ibi, R q1,
+                                               R q2, R q3, R q4, R J, R oat) {
   const R h = S.k_h, timeac = S.k_timeac;
-  int ibi = S.iblank[o]; R ib = (R)(ibi > 0 ? ibi : 0);
+  R ib = (R)(ibi > 0 ? ibi : 0);
   R jac_factor = p.invisc ? (R)0.01 : (R)0.002;
   if (p.iconstant_cfl == 0) {
-    R J = q[(p.nq - 1) * qs + o];
     if (p.idual == 0) {
       S.tscale[o] = oat * h * ib * ((R)1.0 + jac_factor * ((R)1. - timeac) * sqrt(J)) / ((R)1.0 + ((R)1. - timeac) * sqrt(J));
       S.bt[o] = (R)1.;
@@ -31,7 +31,7 @@ __device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
     }
     return;
   }
-  R q1 = q[o], u = q[qs + o] / q1, v = q[2 * qs + o] / q1, e = q[3 * qs + o] / q1;
+  R u = q2 / q1, v = q3 / q1, e = q4 / q1;
   R ugc = S.ug ? S.ug[o] : (R)0, vgc = S.vg ? S.vg[o] : (R)0;
   R xx = S.xx[o], xy = S.xy[o], yx = S.yx[o], yy = S.yy[o];
   R uu = (u - ugc) * xx + (v - vgc) * xy;
@@ -51,6 +51,16 @@ __device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
     S.tscale[o] = t;
     S.bt[o] = (R)1. / ((R)1. + t / h / oat);
   }
+}
+template <class R>
+__device__ void time_step_cell(const Slice<R>& S, int j, int k, R oat) {
+  const ot2d_params& p = *S.P;
+  const int64_t o = at(S.jd, j, k), qs = S.qs;
+  const R* q = S.q;
+  if (p.iconstant_cfl == 0)
+    time_step_vals(S, p, o, S.iblank[o], (R)0, (R)0, (R)0, (R)0, q[(p.nq - 1) * qs + o], oat);
+  else
+    time_step_vals(S, p, o, S.iblank[o], q[o], q[qs + o], q[2 * qs + o], q[3 * qs + o], (R)0, oat);
 }
 
 // ---------------------------------------------------------- reconstruction

@@ -695,7 +695,13 @@ __global__ void __launch_bounds__(CELL_BS) k_adi_teta(const Slice<R>* __restrict
 }
 
 // q(1:4) += s*max(iblank,0) on interior cells (step.f:203-213), FP64 state
-template <class R>
+// TS: also the next iteration's local time step (time.f:2-108) of every
+// cell of the slice, from the state just written (interior) or the halo the
+// boundary conditions set; the solver folds the time step in here when every
+// request of the batch is steady with a first-order time step factor, so
+// that nothing between this update and the next iteration's time step
+// changes its inputs.
+template <class R, bool TS>
 __global__ void __launch_bounds__(CELL_BS / CELL_PT) k_update(const Slice<R>* __restrict__ sl,
                                                               const int32_t* __restrict__ first, int nslice) {
   OT2D_CELL_MAP_PT();
@@ -704,11 +710,21 @@ __global__ void __launch_bounds__(CELL_BS / CELL_PT) k_update(const Slice<R>* __
   // incomplete, so the state is left as it is until the slice is retired
   if (S.ist && (__ldcg(&S.ist[2]) & 4)) return;
   bool bad = false;
+  R oat = (R)1.0;
+  if constexpr (TS) {
+    const int istep = S.ist ? S.ist[1] : p.istep;
+    if (p.ntac >= 2 && istep > 1) oat = (R)(2. / 3.);
+    if (p.ntac == 3 && istep > 2) oat = (R)(6. / 11.);
+  }
 #pragma unroll
   for (int u = 0; u < CELL_PT; ++u) {
     const int cid = cid0 + u * (CELL_BS / CELL_PT);
     const int j = cid % S.jd + 1, k = cid / S.jd + 1;
-    if (cid >= ncell || j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) continue;
+    if (cid >= ncell) continue;
+    if (j < p.jbeg || j > p.jend || k < p.kbeg || k > p.kend) {
+      if constexpr (TS) time_step_cell(S, j, k, oat);
+      continue;
+    }
     const int64_t o = at(S.jd, j, k);
     int ibi = S.iblank[o];
     // max(iblank, 0) as a double, the common values without a conversion
@@ -737,6 +753,10 @@ __global__ void __launch_bounds__(CELL_BS / CELL_PT) k_update(const Slice<R>* __
     // monitor of the updated cell (step.f:356-370), free of divisions:
     // a^2 <= 0.002  <=>  ggm1*(q4*q1 - qq/2) <= 0.002*q1^2 for q1 > 0
     bad = bad || monitor_bad<R>(S.k_ggm1, qn);
+    if constexpr (TS) {
+      const R J = p.iconstant_cfl == 0 ? S.q[(int64_t)(p.nq - 1) * S.qs + o] : (R)0;
+      time_step_vals(S, p, o, ibi, qn[0], qn[1], qn[2], qn[3], J, oat);
+    }
   }
   if (S.ist && bad) atomicOr(&S.ist[2], 2);
 }

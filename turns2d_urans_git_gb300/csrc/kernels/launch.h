@@ -68,6 +68,10 @@ struct Batch {
   int nslice = 0;          // slices in the batch
   int moving = 0;          // some slice is time accurate on a pitching grid
   int precon = 0;          // some slice runs with Turkel preconditioning (k_mp2 >= 0)
+  // the solver's batches of steady requests with a first-order time step
+  // factor: the local time step of the next iteration is computed by the
+  // state update (k_update<R, true>), not by a kernel of its own
+  int ts_in_update = 0;
   int lim_mask = 0;        // reconstruction families of the slices: 1 central, 2 MUSCL, 4 WENO, 8 quad
   int rt_shape = 0;        // residual tile shape of the tile table (rt_shape_dims)
   int cell_blocks = 0;     // blocks of the cell-parallel kernels

@@ -249,7 +249,8 @@ cudaError_t launch_adi(const Slice<R>* d_sl, const Batch& b, int scale, cudaStre
 }
 template <class R>
 cudaError_t launch_update(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
-  k_update<R><<<b.cell_blocks, CELL_BS / CELL_PT, 0, st>>>(d_sl, b.d_first, b.nslice);
+  if (b.ts_in_update) k_update<R, true><<<b.cell_blocks, CELL_BS / CELL_PT, 0, st>>>(d_sl, b.d_first, b.nslice);
+  else k_update<R, false><<<b.cell_blocks, CELL_BS / CELL_PT, 0, st>>>(d_sl, b.d_first, b.nslice);
   return cudaGetLastError();
 }
 template <class R>
@@ -280,7 +281,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
                              cudaEvent_t after_rbc) {
   cudaError_t e;
   if ((e = launch_iter_begin(d_sl, b, st)) != cudaSuccess) return e;
-  if ((e = launch_time_step(d_sl, b, st)) != cudaSuccess) return e;
+  if (!b.ts_in_update && (e = launch_time_step(d_sl, b, st)) != cudaSuccess) return e;
   if ((e = launch_bc(d_sl, b, 1, st)) != cudaSuccess) return e;
   if ((e = launch_residual(d_sl, b, viscous, st)) != cudaSuccess) return e;
   if ((e = launch_rbc(d_sl, b, st)) != cudaSuccess) return e;
