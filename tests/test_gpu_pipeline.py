@@ -125,12 +125,13 @@ def _host_iterate(sv, ids, cases, steps):
 @pytest.mark.parametrize("retire", [0, 3, 8])
 def test_host_buffer_path_equals_device_path(precision, retire):
     """ot2d_solver_iterate_host on a batch of 23 time instances (20
-    requests of one, one of three) overlaps one half's copies with the
-    other half's iteration.  Listed requests end with the bits of the
-    device-resident iterations (their host buffers and the device state
-    alike).  `retire` unlisted requests stop after 3 iterations: with 3 the
-    batch keeps its halves, with 8 it falls to 15 instances, below the
-    halves' size, and the call finishes in the single graph."""
+    requests of one, one of three) runs it in four parts, each with its own
+    graph and stream, so that some parts' copies overlap the others'
+    iterations.  Listed requests end with the bits of the device-resident
+    iterations (their host buffers and the device state alike).  `retire`
+    unlisted requests stop after 3 iterations: with 3 the batch keeps its
+    parts, with 8 it falls to 15 instances, below the parts' size, and the
+    call finishes in the single graph."""
     cases = _cases(20)          # 20 single-instance requests + one of 3 time instances
     steps = 8
     short = set(range(retire))  # unlisted requests capped at 3 iterations

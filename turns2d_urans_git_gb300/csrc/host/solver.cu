@@ -45,6 +45,7 @@ struct Rec {
   std::string store_dir;   // ot2d_solver_store_on_retire: written when retired
   bool queued = false;     // submitted, waiting for device memory
   int half = -1;           // its half of the batch when the batch has halves
+  int part = -1;           // its part of the batch in the host-buffer path
 };
 constexpr int FORCE_WIN = 8;
 
@@ -109,8 +110,7 @@ struct ot2d_solver {
   // sweeps leave idle.
   int pipeline = 1;
   bool split = false;        // the device-resident iteration runs as the halves
-  bool halves = false;       // the halves' graphs exist (split, or for the host-buffer path)
-  bool want_halves = false;  // the host-buffer path asked for them
+  bool halves = false;       // the halves' graphs exist
   DevBatch<double> h64[2];
   DevBatch<float> h32[2];
   cudaGraph_t hgraph[2] = {nullptr, nullptr};
@@ -118,7 +118,18 @@ struct ot2d_solver {
   cudaStream_t st2 = nullptr;
   cudaEvent_t ev_half[2] = {nullptr, nullptr};   // recorded in each half's graph after its rbc
   cudaEvent_t ev_join = nullptr;
-  cudaEvent_t ev_hdone[2] = {nullptr, nullptr};  // host-buffer path: a half's iteration done
+  // Host-buffer path: the batch in HP parts of about equal cells, a graph
+  // and a stream each, so that some parts' copies run while others iterate
+  // (built once that path is used)
+  static constexpr int HP = 4;
+  bool want_parts = false;
+  bool parts = false;
+  DevBatch<double> p64[HP];
+  DevBatch<float> p32[HP];
+  cudaGraph_t pgraph[HP] = {};
+  cudaGraphExec_t pexec[HP] = {};
+  cudaStream_t pst[HP] = {};
+  cudaEvent_t ev_pdone[HP] = {};
   int next_id = 0;
   double t0 = 0;
   int check_every = 25;
@@ -190,6 +201,12 @@ void drop_graph(ot2d_solver* s) {
   }
   s->split = false;
   s->halves = false;
+  for (int q = 0; q < ot2d_solver::HP; ++q) {
+    if (s->pexec[q]) cudaGraphExecDestroy(s->pexec[q]);
+    if (s->pgraph[q]) cudaGraphDestroy(s->pgraph[q]);
+    s->pexec[q] = nullptr; s->pgraph[q] = nullptr;
+  }
+  s->parts = false;
 }
 
 // batches of at least this many slices run as two pipelined halves
@@ -218,6 +235,51 @@ cudaError_t join_halves(ot2d_solver* s) {
 template <class R> DevBatch<R>* halves_of(ot2d_solver* s);
 template <> DevBatch<double>* halves_of<double>(ot2d_solver* s) { return s->h64; }
 template <> DevBatch<float>* halves_of<float>(ot2d_solver* s) { return s->h32; }
+template <class R> DevBatch<R>* parts_of(ot2d_solver* s);
+template <> DevBatch<double>* parts_of<double>(ot2d_solver* s) { return s->p64; }
+template <> DevBatch<float>* parts_of<float>(ot2d_solver* s) { return s->p32; }
+
+// The host-buffer path's parts: HP batches of about equal cells (a
+// request's time instances in one part), each captured as its own graph
+// on its own stream, with B's launch choices.
+template <class R>
+int build_parts(ot2d_solver* s, const DevBatch<R>& B, int visc) {
+  constexpr int HP = ot2d_solver::HP;
+  std::vector<int> ids = s->live;
+  auto cells_of = [&](int id) { const ot2d_params& p = s->recs[id].d.P; return (size_t)p.jd * p.kd * p.nspec; };
+  std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return cells_of(a) > cells_of(b); });
+  std::vector<Slice<R>> slp[HP];
+  size_t load[HP] = {};
+  for (int id : ids) {
+    int q = 0;
+    for (int i = 1; i < HP; ++i)
+      if (load[i] < load[q]) q = i;
+    load[q] += cells_of(id);
+    slices_of<R>(s, s->recs[id], slp[q]);
+    s->recs[id].part = q;
+  }
+  DevBatch<R>* P = parts_of<R>(s);
+  for (int q = 0; q < HP; ++q) {
+    if (!s->pst[q] && cudaStreamCreateWithFlags(&s->pst[q], cudaStreamNonBlocking) != cudaSuccess) return OT2D_ERR_CUDA;
+    if (!s->ev_pdone[q] && cudaEventCreateWithFlags(&s->ev_pdone[q], cudaEventDisableTiming) != cudaSuccess)
+      return OT2D_ERR_CUDA;
+    P[q].rt_shape = B.rt_shape;
+    int e = P[q].build(slp[q], s->st);
+    if (e) return e;
+    P[q].b.poll_limit = B.b.poll_limit;
+    P[q].b.ts_in_update = B.b.ts_in_update;
+    P[q].b.lu_lag = B.b.lu_lag;
+    P[q].b.lu_group = B.b.lu_group;
+    cudaStream_t cs = s->pst[q];
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
+    cudaError_t le = launch_iteration<R>(P[q].d_sl, P[q].b, visc, s->turb_bits, s->lhs_bits, cs);
+    cudaError_t ce = cudaStreamEndCapture(cs, &s->pgraph[q]);
+    if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
+    if (cudaGraphInstantiate(&s->pexec[q], s->pgraph[q], 0) != cudaSuccess) return OT2D_ERR_CUDA;
+  }
+  s->parts = true;
+  return OT2D_OK;
+}
 
 // With the time step folded into the state update, the first iteration of a
 // new batch still needs it: computed now from the current state (for the
@@ -279,16 +341,17 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   const int visc = s->any_viscous ? 1 : 0;
   const bool can_split = sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= 2;
   const bool split = ch.pipeline && can_split;
-  for (int id : s->live) s->recs[id].half = -1;
+  for (int id : s->live) { s->recs[id].half = -1; s->recs[id].part = -1; }
+  // the host-buffer path's parts, once that path has been used
+  const bool want_parts = s->want_parts && sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= (size_t)ot2d_solver::HP;
   if (!split) {
     if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
     cudaError_t le = launch_iteration<R>(B.d_sl, B.b, visc, s->turb_bits, s->lhs_bits, s->st);
     cudaError_t ce = cudaStreamEndCapture(s->st, &s->graph);
     if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
     if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
-    // the host-buffer path overlaps one half's copies with the other
-    // half's iteration, so it wants the halves' graphs as well
-    if (!(s->want_halves && can_split)) return time_step_now<R>(s, B);
+    if (want_parts && (e = build_parts<R>(s, B, visc))) return e;
+    return time_step_now<R>(s, B);
   }
   // two halves of about equal cells (a request's time instances stay in one
   // half: the time-spectral source couples them)
@@ -325,6 +388,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   }
   s->halves = true;
   s->split = split;
+  if (want_parts && (e = build_parts<R>(s, B, visc))) return e;
   return time_step_now<R>(s, B);
 }
 
@@ -728,8 +792,11 @@ void ot2d_solver_destroy(ot2d_solver* s) {
     if (s->ev_half[h]) cudaEventDestroy(s->ev_half[h]);
   }
   if (s->ev_join) cudaEventDestroy(s->ev_join);
-  for (int h = 0; h < 2; ++h)
-    if (s->ev_hdone[h]) cudaEventDestroy(s->ev_hdone[h]);
+  for (int q = 0; q < ot2d_solver::HP; ++q) {
+    s->p64[q].release(); s->p32[q].release();
+    if (s->ev_pdone[q]) cudaEventDestroy(s->ev_pdone[q]);
+    if (s->pst[q]) { cudaStreamSynchronize(s->pst[q]); cudaStreamDestroy(s->pst[q]); }
+  }
   if (s->st2) cudaStreamDestroy(s->st2);
   for (auto& kv : s->recs) solve_destroy(kv.second.d);
   for (cudaEvent_t e : s->ev_d2h) cudaEventDestroy(e);
@@ -909,55 +976,51 @@ int ot2d_solver_graph_kernels(ot2d_solver* s) {
   return a < 0 ? a : (b < 0 ? b : a + b);
 }
 
-// The time step of the whole batch (half < 0) or of one half, when the
-// batch folds it into the state update: after a host-buffer upload.
-cudaError_t host_time_step(ot2d_solver* s, int half, cudaStream_t st) {
+// The time step of the whole batch (part < 0) or of one host-buffer part,
+// when the batch folds it into the state update: after a host-buffer upload.
+cudaError_t host_time_step(ot2d_solver* s, int part, cudaStream_t st) {
   if (s->precision == OT2D_FP32_MIXED) {
-    DevBatch<float>& B = half < 0 ? s->b32 : s->h32[half];
+    DevBatch<float>& B = part < 0 ? s->b32 : s->p32[part];
     return B.b.ts_in_update ? launch_time_step<float>(B.d_sl, B.b, st) : cudaSuccess;
   }
-  DevBatch<double>& B = half < 0 ? s->b64 : s->h64[half];
+  DevBatch<double>& B = part < 0 ? s->b64 : s->p64[part];
   return B.b.ts_in_update ? launch_time_step<double>(B.d_sl, B.b, st) : cudaSuccess;
 }
 
-// Host-buffer iterations over a batch with halves: per iteration, half h
+// Host-buffer iterations over a batch in parts: per iteration, part q
 // uploads its listed instances on its stream (each upload after that
-// instance's previous download), makes its compute copy, runs its graph
-// (after the other half's residual, as in the device-resident pipelined
-// iteration) and downloads its instances on the download stream.  Half 1's
-// uploads thus overlap half 0's iteration, and half 0's downloads half 1's
-// iteration; every instance computes what it computes in the single graph.
-int iterate_host_halves(ot2d_solver* s, int32_t n, std::vector<Rec*>& rs, double* const* q_host, int32_t iters,
-                        int32_t& done) {
+// instance's previous download), makes its compute copy and time step, runs
+// its graph and downloads its instances on the download stream.  Some
+// parts' copies thus run while others iterate; every instance computes what
+// it computes in the single graph.
+int iterate_host_parts(ot2d_solver* s, int32_t n, std::vector<Rec*>& rs, double* const* q_host, int32_t iters,
+                       int32_t& done) {
+  constexpr int HP = ot2d_solver::HP;
   done = 0;
-  for (int h = 0; h < 2; ++h)
-    if (!s->ev_hdone[h] && cudaEventCreateWithFlags(&s->ev_hdone[h], cudaEventDisableTiming) != cudaSuccess)
-      return OT2D_ERR_CUDA;
-  cudaStream_t sh[2] = {s->st, s->st2};
   int err = OT2D_OK;
-  bool halves = true;
-  for (int it = 0; it < iters && !err && halves; ++it) {
+  bool parts = true;
+  for (int it = 0; it < iters && !err && parts; ++it) {
     done = it + 1;
-    for (int h = 0; h < 2 && !err; ++h) {
+    for (int q = 0; q < HP && !err; ++q) {
+      cudaStream_t sq = s->pst[q];
       for (int i = 0; i < n && !err; ++i) {
-        if (rs[i]->half != h) continue;
+        if (rs[i]->part != q) continue;
         const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
-        if ((it > 0 && cudaStreamWaitEvent(sh[h], s->ev_d2h[i], 0) != cudaSuccess) ||
-            cudaMemcpyAsync(rs[i]->d.q64, q_host[i], bytes, cudaMemcpyHostToDevice, sh[h]) != cudaSuccess)
+        if ((it > 0 && cudaStreamWaitEvent(sq, s->ev_d2h[i], 0) != cudaSuccess) ||
+            cudaMemcpyAsync(rs[i]->d.q64, q_host[i], bytes, cudaMemcpyHostToDevice, sq) != cudaSuccess)
           err = OT2D_ERR_CUDA;
       }
       if (!err && s->precision == OT2D_FP32_MIXED &&
-          launch_shadow<float>(s->h32[h].d_sl, s->h32[h].b, sh[h]) != cudaSuccess)
+          launch_shadow<float>(s->p32[q].d_sl, s->p32[q].b, sq) != cudaSuccess)
         err = OT2D_ERR_CUDA;
       // the uploaded state may differ from the one the last update saw
-      if (!err && host_time_step(s, h, sh[h]) != cudaSuccess) err = OT2D_ERR_CUDA;
-      if (!err && (cudaStreamWaitEvent(sh[h], s->ev_half[1 - h], 0) != cudaSuccess ||
-                   cudaGraphLaunch(s->hexec[h], sh[h]) != cudaSuccess ||
-                   cudaEventRecord(s->ev_hdone[h], sh[h]) != cudaSuccess ||
-                   cudaStreamWaitEvent(s->st_d2h, s->ev_hdone[h], 0) != cudaSuccess))
+      if (!err && host_time_step(s, q, sq) != cudaSuccess) err = OT2D_ERR_CUDA;
+      if (!err && (cudaGraphLaunch(s->pexec[q], sq) != cudaSuccess ||
+                   cudaEventRecord(s->ev_pdone[q], sq) != cudaSuccess ||
+                   cudaStreamWaitEvent(s->st_d2h, s->ev_pdone[q], 0) != cudaSuccess))
         err = OT2D_ERR_CUDA;
       for (int i = 0; i < n && !err; ++i) {
-        if (rs[i]->half != h) continue;
+        if (rs[i]->part != q) continue;
         const size_t bytes = rs[i]->d.n2 * rs[i]->d.nspec * rs[i]->d.P.nq * sizeof(double);
         if (cudaMemcpyAsync(q_host[i], rs[i]->d.q64, bytes, cudaMemcpyDeviceToHost, s->st_d2h) != cudaSuccess ||
             cudaEventRecord(s->ev_d2h[i], s->st_d2h) != cudaSuccess)
@@ -970,22 +1033,22 @@ int iterate_host_halves(ot2d_solver* s, int32_t n, std::vector<Rec*>& rs, double
       if (++r.launched >= iter_cap(r)) capped = true;
     }
     if (!err && (++s->since_check >= s->check_every || capped)) {
-      // the status read sees both halves done and no upload in flight
-      if (cudaEventRecord(s->ev_join, s->st2) != cudaSuccess || cudaStreamWaitEvent(s->st, s->ev_join, 0) != cudaSuccess ||
-          cudaStreamSynchronize(s->st_d2h) != cudaSuccess)
-        err = OT2D_ERR_CUDA;
-      else
-        err = check(s);
+      // the status read sees every part done and no upload in flight
+      for (int q = 0; q < HP && !err; ++q)
+        if (cudaStreamWaitEvent(s->st, s->ev_pdone[q], 0) != cudaSuccess) err = OT2D_ERR_CUDA;
+      if (!err && cudaStreamSynchronize(s->st_d2h) != cudaSuccess) err = OT2D_ERR_CUDA;
+      if (!err) err = check(s);
       if (!err && s->dirty) {
         for (int i = 0; i < n; ++i)
           if (!rs[i]->live) { err = OT2D_ERR_ARG; break; }
         if (!err) err = rebuild(s);
-        halves = s->halves;   // retirements took the batch below the halves' size
+        parts = s->parts;   // retirements took the batch below the parts' size
       }
     }
   }
   if (cudaStreamSynchronize(s->st_d2h) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
-  if (cudaStreamSynchronize(s->st2) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
+  for (int q = 0; q < HP; ++q)
+    if (cudaStreamSynchronize(s->pst[q]) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
   if (cudaStreamSynchronize(s->st) != cudaSuccess && !err) err = OT2D_ERR_CUDA;
   return err;
 }
@@ -1010,20 +1073,20 @@ int ot2d_solver_iterate_host(ot2d_solver* s, int32_t n, const int32_t* ids, doub
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return OT2D_ERR_CUDA;
     s->ev_d2h.push_back(e);
   }
-  // A batch large enough for halves overlaps them: half 1's uploads run
-  // while half 0 iterates, half 0's downloads while half 1 iterates.
-  if (!s->halves && !s->want_halves && s->live.size() >= 2) {
-    s->want_halves = true;
+  // A batch large enough for parts overlaps some parts' copies with the
+  // others' iterations.
+  if (!s->parts && !s->want_parts && s->live.size() >= (size_t)ot2d_solver::HP) {
+    s->want_parts = true;
     s->dirty = true;
     int e = rebuild(s);
     if (e) return e;
   }
   int err = OT2D_OK;
   int32_t done = 0;
-  if (s->halves) {
-    // the rest (if retirements took the batch below the halves' size) in
+  if (s->parts) {
+    // the rest (if retirements took the batch below the parts' size) in
     // the single graph below
-    if ((err = iterate_host_halves(s, n, rs, q_host, iters, done)) != OT2D_OK || done == iters) return err;
+    if ((err = iterate_host_parts(s, n, rs, q_host, iters, done)) != OT2D_OK || done == iters) return err;
   }
   for (int it = done; it < iters && !err; ++it) {
     for (int i = 0; i < n && !err; ++i) {
