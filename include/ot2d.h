@@ -278,7 +278,9 @@ typedef struct ot2d_result {
 #define OT2D_OPT_RT_SHAPE      9  /* residual tile: 0 16x16 (default), 1 32x8, 2 8x32 cells */
 #define OT2D_OPT_PIPELINE     10  /* 1 (default): a batch of 16 or more time instances runs
                                      as two halves on two streams, each half's residual
-                                     beside the other half's LU-SGS sweeps; 0: one graph */
+                                     beside the other half's LU-SGS sweeps; 2: as four
+                                     independent parts on four streams (and at least four
+                                     requests); 0: one graph */
 #define OT2D_OPT_POLL_LIMIT    5  /* polls a LU-SGS sweep wait makes before it gives up
                                      (default 4194304).  An instance whose wait gave up
                                      keeps its state and retires with OT2D_ERR_TIMEOUT;
@@ -309,7 +311,7 @@ typedef struct ot2d_tuning {
   int32_t rt_shape;         /* 0 16x16, 1 32x8, 2 8x32                          */
   int32_t lu_group;         /* 0 (largest that fits), 1, 2, 4, 8                */
   int32_t lu_lag;           /* 0..64                                            */
-  int32_t pipeline;         /* 0 one graph, 1 two pipelined halves (OT2D_OPT_PIPELINE) */
+  int32_t pipeline;         /* 0 one graph, 1 two pipelined halves, 2 four parts (OT2D_OPT_PIPELINE) */
 } ot2d_tuning;
 /* replace the tuning table (n entries, copied; n = 0 clears it) */
 int ot2d_solver_set_tuning(ot2d_solver* s, const ot2d_tuning* t, int32_t n);

@@ -45,11 +45,14 @@ def _run(precision, pipeline, cases, caps):
 
 
 @pytest.mark.parametrize("precision", [OT2D_FP64, OT2D_FP32_MIXED])
-def test_pipelined_iteration_is_bitwise_the_single_graph(precision):
+@pytest.mark.parametrize("pipe", [1, 2])
+def test_pipelined_iteration_is_bitwise_the_single_graph(precision, pipe):
+    """Two pipelined halves (1) or four independent parts (2) against one
+    graph (0), requests retiring at different iterations."""
     cases = _cases()
     caps = [30 + 3 * (i % 7) for i in range(len(cases))]   # requests retire at different iterations
     a = _run(precision, 0, cases, caps)
-    b = _run(precision, 1, cases, caps)
+    b = _run(precision, pipe, cases, caps)
     for (qa, ra), (qb, rb), m in zip(a, b, caps):
         assert ra.status == rb.status == 0 and ra.iterations == rb.iterations == m
         assert np.array_equal(qa, qb)
@@ -80,7 +83,7 @@ def test_pipelined_host_buffer_path_matches():
 
 
 @pytest.mark.parametrize("precision", [OT2D_FP64, OT2D_FP32_MIXED])
-@pytest.mark.parametrize("pipeline", [0, 1])
+@pytest.mark.parametrize("pipeline", [0, 1, 2])
 def test_graph_iteration_is_bitwise_the_sequential_phase_order(precision, pipeline):
     """The captured iteration runs the turbulence solve on a second stream,
     beside the LU-SGS sweeps (and, in the mixed path, its first part beside

@@ -80,7 +80,7 @@ def test_the_batch_of_a_search_is_part_of_its_key(tmp_path):
     m = _fake(lambda j, k, c: 1.0 + c[3], calls)
     m.batch = 16
     ch16, _ = tune.tune(m, ((513, 129),), "G", OT2D_FP32_MIXED, cache_path=path)
-    m64 = _fake(lambda j, k, c: 2.0 - c[3], calls)
+    m64 = _fake(lambda j, k, c: 1.0 + abs(c[3] - 1), calls)
     ch64, _ = tune.tune(m64, ((513, 129),), "G", OT2D_FP32_MIXED, cache_path=path, batch=64)
     assert ch16[(513, 129)][3] == 0 and ch64[(513, 129)][3] == 1
     assert set(json.load(open(path))) == {"G|fp32-mixed|513x129|b16", "G|fp32-mixed|513x129|b64"}

@@ -111,6 +111,7 @@ struct ot2d_solver {
   int pipeline = 1;
   bool split = false;        // the device-resident iteration runs as the halves
   bool halves = false;       // the halves' graphs exist
+  bool split4 = false;       // the device-resident iteration runs as the four parts (OT2D_OPT_PIPELINE 2)
   DevBatch<double> h64[2];
   DevBatch<float> h32[2];
   cudaGraph_t hgraph[2] = {nullptr, nullptr};
@@ -200,6 +201,7 @@ void drop_graph(ot2d_solver* s) {
     s->hexec[h] = nullptr; s->hgraph[h] = nullptr;
   }
   s->split = false;
+  s->split4 = false;
   s->halves = false;
   for (int q = 0; q < ot2d_solver::HP; ++q) {
     if (s->pexec[q]) cudaGraphExecDestroy(s->pexec[q]);
@@ -215,6 +217,16 @@ constexpr int PIPE_MIN_SLICES = 16;
 // one iteration of every live instance: the single graph, or the two halves
 // with their cross waits
 cudaError_t launch_graph_iteration(ot2d_solver* s) {
+  if (s->split4) {
+    // four independent parts, each on its own stream after what the solver
+    // stream holds (uploads, a rebuild's time step)
+    cudaError_t e = cudaEventRecord(s->ev_step, s->st);
+    for (int q = 0; q < ot2d_solver::HP && e == cudaSuccess; ++q) {
+      e = cudaStreamWaitEvent(s->pst[q], s->ev_step, 0);
+      if (e == cudaSuccess) e = cudaGraphLaunch(s->pexec[q], s->pst[q]);
+    }
+    return e;
+  }
   if (!s->split) return cudaGraphLaunch(s->gexec, s->st);
   cudaError_t e;
   // half 0 of iteration i after half 1's residual of iteration i-1
@@ -227,6 +239,14 @@ cudaError_t launch_graph_iteration(ot2d_solver* s) {
 
 // make the solver stream wait for the second half's work
 cudaError_t join_halves(ot2d_solver* s) {
+  if (s->split4) {
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < ot2d_solver::HP && e == cudaSuccess; ++q) {
+      e = cudaEventRecord(s->ev_pdone[q], s->pst[q]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s->st, s->ev_pdone[q], 0);
+    }
+    return e;
+  }
   if (!s->split) return cudaSuccess;
   cudaError_t e = cudaEventRecord(s->ev_join, s->st2);
   return e == cudaSuccess ? cudaStreamWaitEvent(s->st, s->ev_join, 0) : e;
@@ -340,10 +360,16 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
   if (branch_of_device(br) != cudaSuccess) return OT2D_ERR_CUDA;
   const int visc = s->any_viscous ? 1 : 0;
   const bool can_split = sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= 2;
-  const bool split = ch.pipeline && can_split;
+  const bool split = ch.pipeline == 1 && can_split;
+  const bool can_parts = sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= (size_t)ot2d_solver::HP;
+  const bool split4 = ch.pipeline == 2 && can_parts;
+  if (split4 && !s->ev_step && cudaEventCreateWithFlags(&s->ev_step, cudaEventDisableTiming) != cudaSuccess)
+    return OT2D_ERR_CUDA;
   for (int id : s->live) { s->recs[id].half = -1; s->recs[id].part = -1; }
-  // the host-buffer path's parts, once that path has been used
-  const bool want_parts = s->want_parts && sl.size() >= (size_t)PIPE_MIN_SLICES && s->live.size() >= (size_t)ot2d_solver::HP;
+  // the parts: for the device-resident iteration (OT2D_OPT_PIPELINE 2) or
+  // once the host-buffer path has been used
+  const bool want_parts = (s->want_parts || ch.pipeline == 2) && sl.size() >= (size_t)PIPE_MIN_SLICES &&
+                          s->live.size() >= (size_t)ot2d_solver::HP;
   if (!split) {
     if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return OT2D_ERR_CUDA;
     cudaError_t le = launch_iteration<R>(B.d_sl, B.b, visc, s->turb_bits, s->lhs_bits, s->st);
@@ -351,6 +377,7 @@ int rebuild_t(ot2d_solver* s, DevBatch<R>& B) {
     if (le != cudaSuccess || ce != cudaSuccess) return OT2D_ERR_CUDA;
     if (cudaGraphInstantiate(&s->gexec, s->graph, 0) != cudaSuccess) return OT2D_ERR_CUDA;
     if (want_parts && (e = build_parts<R>(s, B, visc))) return e;
+    s->split4 = split4;
     return time_step_now<R>(s, B);
   }
   // two halves of about equal cells (a request's time instances stay in one
@@ -823,7 +850,7 @@ int ot2d_solver_set_option(ot2d_solver* s, int32_t key, int32_t value) {
   if (key == OT2D_OPT_BUDGET_MB && value >= 0) { s->budget_set = (size_t)value << 20; return OT2D_OK; }
   if (key == OT2D_OPT_LU_LAG && value >= 0 && value <= 64) { s->lu_lag = value; s->dirty = true; return OT2D_OK; }
   if (key == OT2D_OPT_RT_SHAPE && value >= 0 && value < RT_NSHAPE) { s->rt_shape = value; s->dirty = true; return OT2D_OK; }
-  if (key == OT2D_OPT_PIPELINE && (value == 0 || value == 1)) { s->pipeline = value; s->dirty = true; return OT2D_OK; }
+  if (key == OT2D_OPT_PIPELINE && value >= 0 && value <= 2) { s->pipeline = value; s->dirty = true; return OT2D_OK; }
   if (key == OT2D_OPT_LU_GROUP && (value == 0 || value == 1 || value == 2 || value == 4 || value == 8)) {
     s->lu_group = value;
     s->dirty = true;
@@ -851,7 +878,7 @@ int ot2d_solver_set_tuning(ot2d_solver* s, const ot2d_tuning* t, int32_t n) {
     const ot2d_tuning& e = t[i];
     const bool g = e.lu_group == 0 || e.lu_group == 1 || e.lu_group == 2 || e.lu_group == 4 || e.lu_group == 8;
     if (e.rt_shape < 0 || e.rt_shape >= RT_NSHAPE || !g || e.lu_lag < 0 || e.lu_lag > 64 ||
-        (e.pipeline != 0 && e.pipeline != 1))
+        e.pipeline < 0 || e.pipeline > 2)
       return OT2D_ERR_ARG;
   }
   s->tuning.assign(t, t + n);
@@ -971,6 +998,15 @@ int ot2d_solver_graph_kernels(ot2d_solver* s) {
   cudaSetDevice(s->device);
   if (s->dirty) { int e = rebuild(s); if (e) return -e; }
   if (s->live.empty()) return 0;
+  if (s->split4) {
+    int k = 0;
+    for (int q = 0; q < ot2d_solver::HP; ++q) {
+      const int a = kernel_nodes(s->pgraph[q]);
+      if (a < 0) return a;
+      k += a;
+    }
+    return k;
+  }
   if (!s->split) return kernel_nodes(s->graph);
   const int a = kernel_nodes(s->hgraph[0]), b = kernel_nodes(s->hgraph[1]);
   return a < 0 ? a : (b < 0 ? b : a + b);

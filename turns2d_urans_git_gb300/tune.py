@@ -8,9 +8,10 @@ candidate choice and keeps the fastest:
   lu_group   LU-SGS record chunks streamed per bulk copy (4 or 8)
   lu_lag     LU-SGS hyperplane schedule: steps each 32-row band trails the
              band it depends on beyond the minimum (0 or 4)
-  pipeline   a batch of 16 or more time instances as one graph, or as two
+  pipeline   a batch of 16 or more time instances as one graph (0), as two
              halves on two streams with each half's residual beside the
-             other half's sweeps (0 or 1)
+             other half's sweeps (1), or as four independent parts on four
+             streams (2)
 
 The fastest choice depends on the batch as well as on the mesh: the
 pipelined halves pay off when the sweeps of a small batch leave most SMs
@@ -40,7 +41,7 @@ from .abi import (OT2D_FP64, OT2D_FP32_MIXED, OT2D_OPT_LU_GROUP, OT2D_OPT_LU_LAG
 SIZE_CLASSES = ((129, 33), (257, 65), (385, 97), (513, 129), (769, 193))
 SHAPES = {0: "16x16", 1: "32x8", 2: "8x32"}
 CANDIDATES = tuple((shape, group, lag, pipe) for shape in (0, 1, 2) for group in (4, 8) for lag in (0, 4)
-                   for pipe in (0, 1))
+                   for pipe in (0, 1, 2))
 
 
 def default_cache_path():
