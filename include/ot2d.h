@@ -275,7 +275,7 @@ typedef struct ot2d_result {
                                      band it depends on beyond the minimum (default 0) */
 #define OT2D_OPT_LU_GROUP      8  /* LU-SGS records streamed per bulk copy: 1, 2, 4 or 8
                                      (default 0: the largest the shared memory allows) */
-#define OT2D_OPT_RT_SHAPE      9  /* residual tile: 0 16x16 (default), 1 32x8, 2 8x32 cells */
+#define OT2D_OPT_RT_SHAPE      9  /* residual tile: 0 16x16 (default), 1 32x8, 2 8x32, 3 32x16 cells */
 #define OT2D_OPT_PIPELINE     10  /* 1 (default): a batch of 16 or more time instances runs
                                      as two halves on two streams, each half's residual
                                      beside the other half's LU-SGS sweeps; 2: as four

@@ -36,9 +36,11 @@ UNITS = [
     ("kernels/resid_f32_16x16.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("kernels/resid_f32_32x8.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("kernels/resid_f32_8x32.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
+    ("kernels/resid_f32_32x16.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]),
     ("kernels/resid_f64_16x16.cu", ["-fmad=false"]),
     ("kernels/resid_f64_32x8.cu", ["-fmad=false"]),
     ("kernels/resid_f64_8x32.cu", ["-fmad=false"]),
+    ("kernels/resid_f64_32x16.cu", ["-fmad=false"]),
     ("host/runtime.cu", ["-fmad=false"]),
     ("host/solver.cu", ["-fmad=false"]),
     ("host/dropin.cu", ["-fmad=false"]),

@@ -1,7 +1,8 @@
 // k_resid.cuh -- the fused residual: rhsup (src/eulerrhs.f:2-280) +
 // visrhs (src/visrhs.f:2-287) + timespectralrhs (src/sources.f:2-27) + the
 // L2 / max norms of step.f:58-93, one CTA per tile of TJ x TK interior
-// cells (16x16, 32x8 or 8x32: rt_shape_dims, chosen per batch).
+// cells, one thread per cell (16x16, 32x8, 8x32 or 32x16: rt_shape_dims,
+// chosen per batch).
 //
 // A tile stages its cells plus a 3-cell halo in shared memory once
 // (primitive variables, viscous cell factors, metrics), computes every
@@ -17,15 +18,16 @@
 
 namespace ot2d {
 
-constexpr int RT_BS = 256;
+constexpr int RT_BS = 256;   // threads of the 256-cell tiles
 // staged per-cell arrays
 enum { RS_RHO = 0, RS_U, RS_V, RS_P, RS_E, RS_VNU, RS_GKAP, RS_RJ, RS_UD, RS_VD, RS_ED, RS_XX, RS_XY, RS_YX, RS_YY, RS_N };
 
-// Geometry of a TJ x TK tile (TJ * TK = RT_BS cells, one per thread in the
+// Geometry of a TJ x TK tile (TJ * TK cells, one per thread in the
 // assembly): the staged region with its 3-cell halo and the face arrays.
 template <int TJ, int TK>
 struct RtGeo {
-  static_assert(TJ * TK == RT_BS, "one cell per thread");
+  static constexpr int BS = TJ * TK;                      // threads: one cell each
+  static_assert(BS % 32 == 0 && BS <= 1024, "whole warps");
   static constexpr int H = 3;                             // staged halo width
   static constexpr int RW = TJ + 2 * H, RH = TK + 2 * H;  // staged region
   static constexpr int NR = RW * RH;
@@ -74,7 +76,7 @@ struct RtSmem {
 template <int TJ, int TK>
 struct RtTasks {
   using G = RtGeo<TJ, TK>;
-  static constexpr int NW = RT_BS / 32;
+  static constexpr int NW = G::BS / 32;
   static constexpr int FB = TK * (TJ + 1);                    // xi faces
   static constexpr int NF = FB + (TK + 1) * TJ;               // + eta faces
   static constexpr int NFT = (NF + 31) / 32;
@@ -350,17 +352,17 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R, TJ, TK>& sm, int t
   // before it converts and stores the first, so that their latencies
   // overlap (one round trip to memory per thread instead of one per cell).
   {
-    constexpr int NST = (G::NR + RT_BS - 1) / RT_BS;
+    constexpr int NST = (G::NR + G::BS - 1) / G::BS;
     RtRaw<R> raw[NST];
 #pragma unroll
     for (int i = 0; i < NST; ++i) {
-      const int r = t + i * RT_BS;
+      const int r = t + i * G::BS;
       const int j = jr + r % G::RW, k = kr + r / G::RW;
       if (r < G::NR && j >= 1 && j <= jd && k >= 1 && k <= kd) rt_load_cell(S, p, j, k, visc, raw[i]);
     }
 #pragma unroll
     for (int i = 0; i < NST; ++i) {
-      const int r = t + i * RT_BS;
+      const int r = t + i * G::BS;
       const int j = jr + r % G::RW, k = kr + r / G::RW;
       if (r < G::NR && j >= 1 && j <= jd && k >= 1 && k <= kd) rt_store_cell(S, sm, r, raw[i], visc);
     }
@@ -567,7 +569,7 @@ __device__ void resid_tile(const Slice<R>& S, const RtSmem<R, TJ, TK>& sm, int t
     const int klo = (k0 == p.kbeg) ? 1 : k0, khi = (k1 == p.kend) ? kd : k1;
     const int nw = jhi - jlo + 1, nbox = nw * (khi - klo + 1);
     if (nbox > (j1 - j0 + 1) * (k1 - k0 + 1))
-      for (int i = t; i < nbox; i += RT_BS) {
+      for (int i = t; i < nbox; i += G::BS) {
         const int hj = jlo + i % nw, hk = klo + i / nw;
         if (hj >= p.jbeg && hj <= p.jend && hk >= p.kbeg && hk <= p.kend) continue;
         const int64_t o = at(jd, hj, hk);

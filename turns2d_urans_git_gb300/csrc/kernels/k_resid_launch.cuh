@@ -25,7 +25,7 @@ cudaError_t launch_resid_shape(const Slice<R>* d_sl, const Batch& b, int flags, 
   if (ae != cudaSuccess) return ae;
   // one launch per (preconditioning, reconstruction family) in the batch
   const int m = b.lim_mask ? b.lim_mask : 15;
-  const dim3 g(b.tile_blocks), t(RT_BS);
+  const dim3 g(b.tile_blocks), t(TJ * TK);
   for (int pre = 0; pre <= (b.precon ? 1 : 0); ++pre) {
     if (m & 1) {
       if (pre) k_resid<R, true, 0, TJ, TK><<<g, t, smem, st>>>(d_sl, b.d_tfirst, b.nslice, flags, b.d_part);

@@ -258,9 +258,11 @@ __global__ void __launch_bounds__(CELL_BS) k_assemble(const Slice<R>* __restrict
 // each returning on the other kinds' tiles (a whole block returns, so every
 // tile is done exactly once).  One family per kernel keeps the WENO windows
 // out of the MUSCL kernel's registers and code.
+// Occupancy: 1024 threads per SM (f32, 64 registers a thread) or 512 (f64).
 template <class R, bool PRE, int LIM, int TJ, int TK>
-__global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 2) k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst,
-                                                  int nslice, int flags, NormPart* __restrict__ part) {
+__global__ void __launch_bounds__(TJ * TK, (sizeof(R) == 4 ? 1024 : 512) / (TJ * TK))
+    k_resid(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst, int nslice, int flags,
+            NormPart* __restrict__ part) {
   extern __shared__ __align__(16) unsigned char rt_raw[];
   const int si = find_slice(tfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];
@@ -271,22 +273,23 @@ __global__ void __launch_bounds__(RT_BS, sizeof(R) == 4 ? 4 : 2) k_resid(const S
   if (!(flags & AS_NORM)) return;
   // Deterministic block reduction in a fixed order: every thread leaves its
   // cell's terms in the staged region (only the face passes read it, and
-  // they are behind the tile's last barrier), then warp 0 sums the 8 values
-  // of each lane position in thread order and finishes with a shuffle tree.
-  // One warp does the FP64 additions of the whole tile.
-  static_assert(RT_BS == 256 && (size_t)RT_BS * (2 * sizeof(double) + sizeof(long long) + sizeof(R)) <=
-                                   sizeof(R) * (size_t)RS_N * RtGeo<TJ, TK>::NR, "partials fit in the staged region");
+  // they are behind the tile's last barrier), then warp 0 sums the BS/32
+  // values of each lane position in thread order and finishes with a
+  // shuffle tree.  One warp does the FP64 additions of the whole tile.
+  constexpr int BS = TJ * TK;
+  static_assert((size_t)BS * (2 * sizeof(double) + sizeof(long long) + sizeof(R)) <=
+                    sizeof(R) * (size_t)RS_N * RtGeo<TJ, TK>::NR, "partials fit in the staged region");
   double* prs = (double*)sm.c;
-  double* prr = prs + RT_BS;
-  long long* pky = (long long*)(prr + RT_BS);
-  R* pmx = (R*)(pky + RT_BS);
+  double* prr = prs + BS;
+  long long* pky = (long long*)(prr + BS);
+  R* pmx = (R*)(pky + BS);
   const int t = threadIdx.x, lane = t & 31;
   prs[t] = npr.rsum; prr[t] = npr.resrho; pky[t] = npr.key; pmx[t] = npr.resmax;
   __syncthreads();
   if (t < 32) {
     NormPartR<R> a{prs[lane], prr[lane], pmx[lane], pky[lane]};
 #pragma unroll
-    for (int i = 1; i < RT_BS / 32; ++i) {
+    for (int i = 1; i < BS / 32; ++i) {
       const int u = lane + 32 * i;
       a.rsum = a.rsum + prs[u];
       a.resrho = a.resrho + prr[u];
@@ -471,9 +474,8 @@ __global__ void __launch_bounds__(BC_BS) k_turbc(const Slice<R>* __restrict__ sl
 // cell and its four neighbours is staged once per tile (region with a
 // one-cell halo) in shared memory, then each thread assembles its cell.
 template <class R, int TJ, int TK>
-__global__ void __launch_bounds__(TJ * TK, sizeof(R) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(TJ * TK, (sizeof(R) == 4 ? 1024 : 512) / (TJ * TK))
     k_sa_rhs(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ tfirst, int nslice) {
-  static_assert(TJ * TK == 256, "one cell per thread");
   extern __shared__ __align__(16) unsigned char sa_raw[];
   const int si = find_slice(tfirst, nslice, blockIdx.x);
   const Slice<R>& S = sl[si];

@@ -20,9 +20,9 @@ constexpr int BC_BS = 512;
 // threads of a CTA of one BC entry (several CTAs per slice)
 constexpr int BCE_BS = 128;
 // residual tile shapes (interior cells per CTA): 0 16x16, 1 32x8, 2 8x32
-constexpr int RT_NSHAPE = 3;
+constexpr int RT_NSHAPE = 4;
 inline void rt_shape_dims(int shape, int& tj, int& tk) {
-  tj = shape == 1 ? 32 : (shape == 2 ? 8 : 16);
+  tj = shape == 1 || shape == 3 ? 32 : (shape == 2 ? 8 : 16);
   tk = shape == 1 ? 8 : (shape == 2 ? 32 : 16);
 }
 // scratch arrays per slice of the k-omega SST solve (k_sst.cuh: SSTw)

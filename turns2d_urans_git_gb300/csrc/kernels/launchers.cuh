@@ -58,6 +58,7 @@ cudaError_t launch_resid_both(const Slice<R>* d_sl, const Batch& b, int flags, c
   switch (b.rt_shape) {
     case 1: return launch_resid_shape<R, 32, 8>(d_sl, b, flags, st);
     case 2: return launch_resid_shape<R, 8, 32>(d_sl, b, flags, st);
+    case 3: return launch_resid_shape<R, 32, 16>(d_sl, b, flags, st);
     default: return launch_resid_shape<R, 16, 16>(d_sl, b, flags, st);
   }
 }
@@ -202,6 +203,7 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   switch (b.rt_shape) {
     case 1: k_sa_rhs<R, 32, 8><<<b.tile_blocks, 256, sa_rhs_smem<R, 32, 8>(), st>>>(d_sl, b.d_tfirst, b.nslice); break;
     case 2: k_sa_rhs<R, 8, 32><<<b.tile_blocks, 256, sa_rhs_smem<R, 8, 32>(), st>>>(d_sl, b.d_tfirst, b.nslice); break;
+    case 3: k_sa_rhs<R, 32, 16><<<b.tile_blocks, 512, sa_rhs_smem<R, 32, 16>(), st>>>(d_sl, b.d_tfirst, b.nslice); break;
     default: k_sa_rhs<R, 16, 16><<<b.tile_blocks, 256, sa_rhs_smem<R, 16, 16>(), st>>>(d_sl, b.d_tfirst, b.nslice);
   }
   constexpr size_t lj_smem = sizeof(R) * LJ_SMEM;

@@ -3,8 +3,9 @@
 For each mesh-size class it times a batch of that class under every
 candidate choice and keeps the fastest:
 
-  rt_shape   the fused residual's tile, 16x16, 32x8 or 8x32 interior cells
-             per CTA (staged halo per cell against threads per face line)
+  rt_shape   the fused residual's tile, 16x16, 32x8, 8x32 (256 threads) or
+             32x16 (512 threads) interior cells per CTA (staged halo per
+             cell against threads per face line)
   lu_group   LU-SGS record chunks streamed per bulk copy (4 or 8)
   lu_lag     LU-SGS hyperplane schedule: steps each 32-row band trails the
              band it depends on beyond the minimum (0 or 4)
@@ -39,8 +40,8 @@ from .abi import (OT2D_FP64, OT2D_FP32_MIXED, OT2D_OPT_LU_GROUP, OT2D_OPT_LU_LAG
 # the mesh sizes of the batched configuration (vertices); a class covers
 # meshes up to its array size (jd = jmax + 1, kd = kmax + 1)
 SIZE_CLASSES = ((129, 33), (257, 65), (385, 97), (513, 129), (769, 193))
-SHAPES = {0: "16x16", 1: "32x8", 2: "8x32"}
-CANDIDATES = tuple((shape, group, lag, pipe) for shape in (0, 1, 2) for group in (4, 8) for lag in (0, 4)
+SHAPES = {0: "16x16", 1: "32x8", 2: "8x32", 3: "32x16"}
+CANDIDATES = tuple((shape, group, lag, pipe) for shape in (0, 1, 2, 3) for group in (4, 8) for lag in (0, 4)
                    for pipe in (0, 1, 2))
 
 
