@@ -50,10 +50,11 @@ PHASES = ["time_step", "bc", "residual", "rbc", "lusgs", "sa", "update"]
 # DRAM bytes per interior cell per launch measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of the batch-8 capture, 0.52 M cells, summarised in
 # profiles/top_kernels_rans_sa_513x129_b8_fp32mixed.md), scaled to the batch
-TRAFFIC_PER_CELL = {"residual": (40.498176e6 + 1.443328e6) / (8 * 65536),
+TRAFFIC_PER_CELL = {"residual": (40.496384e6 + 1.447168e6) / (8 * 65536),
                     # k_lu_prep + both sweeps (k_lu_edges, ~1 % of the phase, not captured)
-                    "lusgs": (31.610880e6 + 9.473536e6 + 62.373632e6 + 2.156800e6 + 62.384384e6 + 1.083648e6)
+                    "lusgs": (31.611136e6 + 7.541504e6 + 62.385408e6 + 2.267648e6 + 62.397696e6 + 1.084416e6)
                     / (8 * 65536),
+                    # k_update as the phase timer runs it, without the folded time step
                     "update": (27.421952e6 + 0.079360e6) / (8 * 65536)}
 NPH = len(PHASES)
 
