@@ -422,14 +422,21 @@ __device__ void rbc_slice(const Slice<R>& S) {
 }
 
 // turbc, samodel2d.f:827-1303, on variable n5 = nmv+1 of q64.  u, v are the
-// cell velocities the SA step computed at its start (samodel2d.f:74-76).
+// cell velocities the SA step computed at its start (samodel2d.f:74-76);
+// null: formed here from q as k_sa_prep forms them (q2/q1, q3/q1 in the
+// compute precision), so that turbc can run beside k_sa_prep.
 template <class R>
 __device__ void turbc_slice(const Slice<R>& S, const R* u, const R* v) {
   const ot2d_params& p = *S.P;
   const int jd = p.jd, kd = p.kd, n5 = p.nmv + 1;
   QV q{S.q64, jd, S.qs};
   const double *xx = S.xx64, *xy = S.xy64, *yx = S.yx64, *yy = S.yy64, *ug = S.ug64, *vg = S.vg64;
-  auto U = [&](const R* a, int j, int k) { return (double)a[at(jd, j, k)]; };
+  // velocity component n (1: u, 2: v) of cell (j, k)
+  auto U = [&](const R* a, int n, int j, int k) {
+    const int64_t o = at(jd, j, k);
+    if (a) return (double)a[o];
+    return (double)(S.q[n * S.qs + o] / S.q[o]);
+  };
   auto G = [&](const double* a, int j, int k) { return a ? a[at(jd, j, k)] : 0.0; };
   for (int ib = 0; ib < p.nbc; ++ib) {
     int js, je, ks, ke; bc_range(p, ib, js, je, ks, ke);
@@ -507,8 +514,8 @@ __device__ void turbc_slice(const Slice<R>& S, const R* u, const R* v) {
         for (int k = ks + threadIdx.x; k <= ke; k += blockDim.x) {
           int j = (idir == 1) ? je : js, j1 = j + iadd;
           q(j, k, n5) = p.vnuinf;
-          double uu = (U(u, j, k) - G(ug, j, k) + U(u, j1, k) - G(ug, j1, k)) * xx[at(jd, j, k)];
-          uu = uu + (U(v, j, k) - G(vg, j, k) + U(v, j1, k) - G(vg, j1, k)) * xy[at(jd, j, k)];
+          double uu = (U(u, 1, j, k) - G(ug, j, k) + U(u, 1, j1, k) - G(ug, j1, k)) * xx[at(jd, j, k)];
+          uu = uu + (U(v, 2, j, k) - G(vg, j, k) + U(v, 2, j1, k) - G(vg, j1, k)) * xy[at(jd, j, k)];
           uu = uu * iadd;
           if (uu < 0.) q(j, k, n5) = q(j1, k, n5);
           for (int jc = 1; jc <= je - js; ++jc) {
@@ -520,8 +527,8 @@ __device__ void turbc_slice(const Slice<R>& S, const R* u, const R* v) {
         for (int j = js + threadIdx.x; j <= je; j += blockDim.x) {
           int k = (idir == 2) ? ke : ks, k1 = k + iadd;
           q(j, k, n5) = p.vnuinf;
-          double uu = (U(u, j, k) - G(ug, j, k) + U(u, j, k1) - G(ug, j, k1)) * yx[at(jd, j, k)];
-          uu = uu + (U(v, j, k) - G(vg, j, k) + U(v, j, k1) - G(vg, j, k1)) * yy[at(jd, j, k)];
+          double uu = (U(u, 1, j, k) - G(ug, j, k) + U(u, 1, j, k1) - G(ug, j, k1)) * yx[at(jd, j, k)];
+          uu = uu + (U(v, 2, j, k) - G(vg, j, k) + U(v, 2, j, k1) - G(vg, j, k1)) * yy[at(jd, j, k)];
           uu = uu * iadd;
           if (uu < 0.) q(j, k, n5) = q(j, k1, n5);
           for (int kc = 1; kc <= ke - ks; ++kc) {

@@ -96,6 +96,24 @@ __device__ __forceinline__ void lu_st4(double* ch, int f, int l, double a, doubl
   *reinterpret_cast<double2*>(ch + lu_idx<double, PRE>(f + 2, l)) = make_double2(c, d);
 }
 
+// four consecutive values at a 16-byte aligned shared address (the
+// cross-band ring slots and the staged halo contributions)
+__device__ __forceinline__ Lu4<float> lu_ldv(const float* a) {
+  const float4 v = *reinterpret_cast<const float4*>(a);
+  return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Lu4<double> lu_ldv(const double* a) {
+  const double2 x = *reinterpret_cast<const double2*>(a), y = *reinterpret_cast<const double2*>(a + 2);
+  return {x.x, x.y, y.x, y.y};
+}
+__device__ __forceinline__ void lu_stv(float* a, const float* v) {
+  *reinterpret_cast<float4*>(a) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void lu_stv(double* a, const double* v) {
+  *reinterpret_cast<double2*>(a) = make_double2(v[0], v[1]);
+  *reinterpret_cast<double2*>(a + 2) = make_double2(v[2], v[3]);
+}
+
 template <class R>
 struct LuCell {
   R uu, vv, uv2, ge, ri1, ri2, rk1, rk2, qx, cx, qy, cy, vn, ugc, vgc, d;
@@ -491,84 +509,133 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
     if (l == 0 && !lu_wait_ge(&prog[wprev], min(32 + lag, nst), seen_prev, lim)) bad = true;
     seen_prev = __shfl_sync(0xffffffffu, seen_prev, 0);
   }
+  // This lane's record: residual, (tscale/2, d, u, v), (uv2, ge, xi
+  // metrics), (eta metrics, qx, qy), this sweep's (chk, spec) pairs.
+  struct Rec { Lu4<R> r0, r1, r2, r3, r4; };
+  auto ldrec = [&](const R* ch) -> Rec {
+    return {lu_ld4<PRE>(ch, LF_S, l), lu_ld4<PRE>(ch, LF_SV, l), lu_ld4<PRE>(ch, LF_UV2, l),
+            lu_ld4<PRE>(ch, LF_RK1, l), lu_ld4<PRE>(ch, FWD ? LF_FCX : LF_BCX, l)};
+  };
+  // The new correction of this lane's cell from its record and the summed
+  // neighbour contributions, its store (forward: into the record for the
+  // backward sweep; backward: into s), and its outgoing contributions:
+  // xi into aprev (the same lane's next step), eta into bout (the next lane).
+  auto cell = [&](const R* ch, const Rec& rc, int tl, int c, const R* bin) {
+    const Lu4<R>&r0 = rc.r0, &r1 = rc.r1, &r2 = rc.r2, &r3 = rc.r3, &r4 = rc.r4;
+    const R sv = r1.x, di = r1.y;
+    const R st[4] = {r0.x, r0.y, r0.z, r0.w};
+    R sn[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+      sn[n] = FWD ? (st[n] + sv * (aprev[n] + bin[n])) * di : st[n] - sv * (aprev[n] + bin[n]) * di;
+    if (FWD) {
+      lu_st4<PRE>(recw + (int64_t)tl * CH, LF_S, l, sn[0], sn[1], sn[2], sn[3]);
+    } else {
+#pragma unroll
+      for (int n = 0; n < 4; ++n) srow[n * S.qs + c] = sn[n];
+    }
+    // xi: (chk, spec) = r4.x, r4.y with ri1, ri2, qx; eta: r4.z, r4.w
+    // with rk1, rk2, qy; u, v, uv2, ge shared
+    if constexpr (PRE) {
+      // (chk*qq xi, chk*qq eta, preconditioner factor)
+      const Lu4<R> r5 = lu_ld4<PRE>(ch, FWD ? LF_PF : LF_PB, l);
+      lu_apply_pre<R, FWD>(r4.x, r5.x, r4.y, r5.z, r2.z, r2.w, r3.z, r1.z, r1.w, r2.x, r2.y, gm1, sn, aprev);
+      lu_apply_pre<R, FWD>(r4.z, r5.y, r4.w, r5.z, r3.x, r3.y, r3.w, r1.z, r1.w, r2.x, r2.y, gm1, sn, bout);
+    } else {
+      lu_apply(r4.x, r4.y, r2.z, r2.w, r3.z, r1.z, r1.w, r2.x, r2.y, gm1, sn, aprev);
+      lu_apply(r4.z, r4.w, r3.x, r3.y, r3.w, r1.z, r1.w, r2.x, r2.y, gm1, sn, bout);
+    }
+  };
+  // Steady groups: a band of 32 rows, G steps all inside columns 1..ncol-1
+  // of every lane (local steps 32 .. ncol-1), so every lane is active, no
+  // lane is on the first column, and the waits on the neighbouring bands
+  // are made once per group -- for the last step's cross-band input and the
+  // last step's ring slot -- with the progress published once at the end.
+  // The group runs without branches; the cells see the same operands as in
+  // the per-step form below.
+  const bool full = 32 * (w + 1) <= nrow;
+  const int lin = FWD ? 0 : 31;
+  const bool pout = l == lout && has_next;
   for (int g = 0; g < ngrp; ++g) {
     const bool ok = mbar_wait_bounded(&bar[g & 1], (uint32_t)((g >> 1) & 1), lim);
     if (__any_sync(0xffffffffu, !ok || bad)) { gfail = g; break; }
     const int gs = gsize(g);
     const R* gring = ring + (size_t)(g & 1) * G * CH;
-#pragma unroll 4
-    for (int u = 0; u < gs; ++u) {
-      const int tl = g * G + u;
-      // this lane's record: residual, (tscale/2, d, u, v), (uv2, ge, xi
-      // metrics), (eta metrics, qx, qy), this sweep's (chk, spec) pairs
-      // (loading the next step's record ahead of this step's arithmetic
-      // was measured slower: 0.81 against 0.71 ms at batch 64)
-      const R* ch = gring + (FWD ? u : gs - 1 - u) * CH;
-      const Lu4<R> r0 = lu_ld4<PRE>(ch, LF_S, l), r1 = lu_ld4<PRE>(ch, LF_SV, l), r2 = lu_ld4<PRE>(ch, LF_UV2, l),
-                   r3 = lu_ld4<PRE>(ch, LF_RK1, l), r4 = lu_ld4<PRE>(ch, FWD ? LF_FCX : LF_BCX, l);
-      R bin[4];
+    const int t0 = g * G;
+    if (full && gs == G && t0 >= 32 && t0 + G <= ncol) {
+      if (has_prev && l == lin && !lu_wait_ge(&prog[wprev], t0 + G - 1 + 32, seen_prev, lim)) bad = true;
+      if (pout && !lu_wait_ge(&prog[wnext], t0 + G - 1 - LU_XB + 32, seen_next, lim)) bad = true;
+      if (__any_sync(0xffffffffu, bad)) { gfail = g; break; }
 #pragma unroll
-      for (int n = 0; n < 4; ++n)
-        bin[n] = FWD ? __shfl_up_sync(0xffffffffu, bout[n], 1) : __shfl_down_sync(0xffffffffu, bout[n], 1);
-      const int c = FWD ? tl - l : ncol - 1 - (tl - (31 - l));
-      const bool act = r < nrow && c >= 0 && c < ncol;
-      if (act) {
-        if (FWD ? c == 0 : c == ncol - 1) {
-#pragma unroll
-          for (int n = 0; n < 4; ++n) aprev[n] = Ah[4 * r + n];
-        }
-        // the (j,k-1) / (j,k+1) neighbour from outside the band
-        if (FWD ? l == 0 : (l == 31 || r == nrow - 1)) {
-          if (!has_prev || (!FWD && r == nrow - 1)) {
-#pragma unroll
-            for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
-          } else if (lu_wait_ge(&prog[wprev], tl + 32, seen_prev, lim)) {
-            // produced by band wprev at its step tl + 31
-            const R* x = xin + ((tl + 31) & (LU_XB - 1)) * 4;
-#pragma unroll
-            for (int n = 0; n < 4; ++n) bin[n] = x[n];
-          } else {
-            bad = true;
-          }
-        }
-        const R sv = r1.x, di = r1.y;
-        const R st[4] = {r0.x, r0.y, r0.z, r0.w};
-        R sn[4];
+      for (int u = 0; u < G; ++u) {
+        const int tl = t0 + u;
+        const R* ch = gring + (FWD ? u : G - 1 - u) * CH;
+        const Rec rc = ldrec(ch);
+        R bin[4];
 #pragma unroll
         for (int n = 0; n < 4; ++n)
-          sn[n] = FWD ? (st[n] + sv * (aprev[n] + bin[n])) * di : st[n] - sv * (aprev[n] + bin[n]) * di;
-        if (FWD) {
-          lu_st4<PRE>(recw + (int64_t)tl * CH, LF_S, l, sn[0], sn[1], sn[2], sn[3]);
-        } else {
-#pragma unroll
-          for (int n = 0; n < 4; ++n) srow[n * S.qs + c] = sn[n];
+          bin[n] = FWD ? __shfl_up_sync(0xffffffffu, bout[n], 1) : __shfl_down_sync(0xffffffffu, bout[n], 1);
+        const int c = FWD ? tl - l : ncol - 1 - (tl - (31 - l));
+        // lane lin: from band wprev's step tl + 31, or the halo row
+        const R* xs = has_prev ? xin + ((tl + 31) & (LU_XB - 1)) * 4 : Bh + 4 * c;
+        if (l == lin) {
+          const Lu4<R> x = lu_ldv(xs);
+          bin[0] = x.x; bin[1] = x.y; bin[2] = x.z; bin[3] = x.w;
         }
-        // xi: (chk, spec) = r4.x, r4.y with ri1, ri2, qx; eta: r4.z, r4.w
-        // with rk1, rk2, qy; u, v, uv2, ge shared
-        if constexpr (PRE) {
-          // (chk*qq xi, chk*qq eta, preconditioner factor)
-          const Lu4<R> r5 = lu_ld4<PRE>(ch, FWD ? LF_PF : LF_PB, l);
-          lu_apply_pre<R, FWD>(r4.x, r5.x, r4.y, r5.z, r2.z, r2.w, r3.z, r1.z, r1.w, r2.x, r2.y, gm1, sn, aprev);
-          lu_apply_pre<R, FWD>(r4.z, r5.y, r4.w, r5.z, r3.x, r3.y, r3.w, r1.z, r1.w, r2.x, r2.y, gm1, sn, bout);
-        } else {
-          lu_apply(r4.x, r4.y, r2.z, r2.w, r3.z, r1.z, r1.w, r2.x, r2.y, gm1, sn, aprev);
-          lu_apply(r4.z, r4.w, r3.x, r3.y, r3.w, r1.z, r1.w, r2.x, r2.y, gm1, sn, bout);
-        }
+        cell(ch, rc, tl, c, bin);
+        if (pout) lu_stv(xout + (tl & (LU_XB - 1)) * 4, bout);
       }
-      // hand the boundary contribution to the next band (its slot must have
-      // been read: the consumer is at least at step tl - LU_XB + 32), then
-      // publish this band's progress
-      if (l == lout) {
-        if (act && has_next) {
-          if (lu_wait_ge(&prog[wnext], tl - LU_XB + 32, seen_next, lim)) {
-            R* x = xout + (tl & (LU_XB - 1)) * 4;
+      if (l == lout) lu_st_release(&prog[w], t0 + G);
+    } else {
+#pragma unroll 4
+      for (int u = 0; u < gs; ++u) {
+        const int tl = t0 + u;
+        // (loading the next step's record ahead of this step's arithmetic
+        // was measured slower: 0.81 against 0.71 ms at batch 64)
+        const R* ch = gring + (FWD ? u : gs - 1 - u) * CH;
+        const Rec rc = ldrec(ch);
+        R bin[4];
 #pragma unroll
-            for (int n = 0; n < 4; ++n) x[n] = bout[n];
-          } else {
-            bad = true;
+        for (int n = 0; n < 4; ++n)
+          bin[n] = FWD ? __shfl_up_sync(0xffffffffu, bout[n], 1) : __shfl_down_sync(0xffffffffu, bout[n], 1);
+        const int c = FWD ? tl - l : ncol - 1 - (tl - (31 - l));
+        const bool act = r < nrow && c >= 0 && c < ncol;
+        if (act) {
+          if (FWD ? c == 0 : c == ncol - 1) {
+#pragma unroll
+            for (int n = 0; n < 4; ++n) aprev[n] = Ah[4 * r + n];
           }
+          // the (j,k-1) / (j,k+1) neighbour from outside the band
+          if (FWD ? l == 0 : (l == 31 || r == nrow - 1)) {
+            if (!has_prev || (!FWD && r == nrow - 1)) {
+#pragma unroll
+              for (int n = 0; n < 4; ++n) bin[n] = Bh[4 * c + n];
+            } else if (lu_wait_ge(&prog[wprev], tl + 32, seen_prev, lim)) {
+              // produced by band wprev at its step tl + 31
+              const R* x = xin + ((tl + 31) & (LU_XB - 1)) * 4;
+#pragma unroll
+              for (int n = 0; n < 4; ++n) bin[n] = x[n];
+            } else {
+              bad = true;
+            }
+          }
+          cell(ch, rc, tl, c, bin);
         }
-        lu_st_release(&prog[w], tl + 1);
+        // hand the boundary contribution to the next band (its slot must have
+        // been read: the consumer is at least at step tl - LU_XB + 32), then
+        // publish this band's progress
+        if (l == lout) {
+          if (act && has_next) {
+            if (lu_wait_ge(&prog[wnext], tl - LU_XB + 32, seen_next, lim)) {
+              R* x = xout + (tl & (LU_XB - 1)) * 4;
+#pragma unroll
+              for (int n = 0; n < 4; ++n) x[n] = bout[n];
+            } else {
+              bad = true;
+            }
+          }
+          lu_st_release(&prog[w], tl + 1);
+        }
       }
     }
     // group done: refill its buffer with group g + 2

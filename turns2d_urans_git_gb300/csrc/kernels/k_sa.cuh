@@ -426,15 +426,36 @@ __device__ void sa_lsolvek_line(const Slice<R>& S, const ot2d_params& p, int j) 
     R x2 = (R)0. + x;            // s2 = s2 + sjmat, s2 = 0 on entry
     R relx = (R)1.0 * x2;        // relfac * sjmat
     s[oo] = relx;
-    double ib = (double)(ibi > 0 ? ibi : 0);
-    double v = q5o + (double)relx * ib;
-    v = (1.0e-20 > v) ? 1.0e-20 : v;
+    double v;
+    R qv;
+    if constexpr (sizeof(R) == sizeof(double)) {
+      double ib = (double)(ibi > 0 ? ibi : 0);
+      v = q5o + (double)relx * ib;
+      v = (1.0e-20 > v) ? 1.0e-20 : v;
+      qv = (R)v;
+    } else {
+      // The same values with one FP64 operation (GB300's FP64 pipe is
+      // narrow): relx * max(iblank, 0) is exact for iblank 0 (a signed zero,
+      // or NaN for a non-finite relx) and 1, so it is formed in f32 and
+      // widened on the integer pipe; the clamp compares IEEE bit patterns;
+      // the narrowing is the f32 path's round-to-nearest with flush to zero.
+      double dx;
+      if (ibi == 1) dx = f2d_bits_ftz(relx);
+      else if (ibi <= 0) dx = f2d_bits_ftz(relx * 0.0f);
+      else dx = (double)relx * (double)ibi;
+      v = q5o + dx;
+      const uint64_t vb = (uint64_t)__double_as_longlong(v), mag = vb & 0x7fffffffffffffffull;
+      // 1e-20 > v: v negative (not NaN), or positive below 1e-20
+      const bool below = (vb >> 63) ? mag <= 0x7ff0000000000000ull
+                                    : vb < (uint64_t)__double_as_longlong(1.0e-20);
+      if (below) v = 1.0e-20;
+      qv = d2f_bits_rn_ftz(v);
+    }
     q5[oo] = v;
-    if constexpr (sizeof(R) != sizeof(double)) S.q[(int64_t)(n5 - 1) * qs + oo] = (R)v;
+    if constexpr (sizeof(R) != sizeof(double)) S.q[(int64_t)(n5 - 1) * qs + oo] = qv;
     // c_turm (samodel2d.f:372-399) with q5 as just stored
     const R rhoJ = q1 * J;
     const R vnul = vm / rhoJ;
-    const R qv = (R)v;
     const R chi = qv / vnul;
     const R fv1 = cube(chi) / (cube(chi) + cube(cv1));
     S.turmu[oo] = rhoJ * qv * fv1;

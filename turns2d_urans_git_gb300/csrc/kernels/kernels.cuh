@@ -469,6 +469,31 @@ __global__ void __launch_bounds__(BC_BS) k_turbc(const Slice<R>* __restrict__ sl
   }
 }
 
+// k_sa_prep and the first turbc in one launch: blocks 0..nslice-1 apply
+// turbc to their slice, with the cell velocities formed from q as k_sa_prep
+// forms them, and the other blocks evaluate k_sa_prep's cells.  Neither part
+// reads what the other writes (k_sa_prep: laminar viscosity and velocities
+// from variables 1-4; turbc: variable n5 on the halo), so they run at once.
+template <class R>
+__global__ void __launch_bounds__(CELL_BS) k_sa_prep_bc(const Slice<R>* __restrict__ sl,
+                                                        const int32_t* __restrict__ first, int nslice) {
+  if ((int)blockIdx.x < nslice) {
+    const Slice<R>& S = sl[blockIdx.x];
+    const ot2d_params& p = *S.P;
+    if (p.lamin || p.iturb != 1) return;
+    turbc_slice<R>(S, nullptr, nullptr);
+    shadow_ring(S, p.nmv + 1, p.nmv + 1);
+    return;
+  }
+  const int bid = (int)blockIdx.x - nslice;
+  const int si = find_slice(first, nslice, bid);
+  const Slice<R>& S = sl[si];
+  const int cid = (bid - first[si]) * blockDim.x + threadIdx.x;
+  if (cid >= S.jd * S.kd) return;
+  if (S.P->lamin || S.P->iturb != 1) return;
+  sa_prep_cell(S, *S.P, cid % S.jd + 1, cid / S.jd + 1);
+}
+
 // RHS and bands of the SA solve (samodel2d.f:402-450, :96-134) on tiles of
 // TJ x TK interior cells, the residual's tile table: every value read at a
 // cell and its four neighbours is staged once per tile (region with a

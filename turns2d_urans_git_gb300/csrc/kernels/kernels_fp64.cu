@@ -34,6 +34,7 @@ cudaError_t branch_of_device(Branch*& out) {
     if ((e = cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming)) != cudaSuccess) return e;
+    if ((e = cudaEventCreateWithFlags(&b.join_end, cudaEventDisableTiming)) != cudaSuccess) return e;
   }
   out = &b;
   return cudaSuccess;

@@ -110,7 +110,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
 // before capturing an iteration into a graph.
 struct Branch {
   cudaStream_t st = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, join_end = nullptr;
 };
 cudaError_t branch_of_device(Branch*& out);
 
@@ -146,7 +146,10 @@ template <class R> cudaError_t launch_faces(const Slice<R>* d_sl, const Batch& b
 // assembly flags: see AS_* in kernels.cuh
 enum { AS_ACC = 1, AS_INV = 2, AS_VISC = 4, AS_TS = 8, AS_NORM = 16 };
 template <class R> cudaError_t launch_assemble(const Slice<R>* d_sl, const Batch& b, int flags, cudaStream_t st);
-template <class R> cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
+// vmu_sa; final_bc = 0 leaves out its closing turbc + halo c_turm, which the
+// caller then launches itself (launch_sa_final_bc)
+template <class R> cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st, int final_bc = 1);
+template <class R> cudaError_t launch_sa_final_bc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 template <class R> cudaError_t launch_sst(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 // arc2d (ilhs = 2 pentadiagonal, 3 upwind tridiagonal); scale = 1: preceded
 // by s *= tscale on all cells (step.f:141-148).  only_adi = 1: skip slices

@@ -196,9 +196,9 @@ cudaError_t launch_lusgs(const Slice<R>* d_sl, const Batch& b, int scale, cudaSt
   return launch_lusgs_sweeps(d_sl, b, st, only_lu);
 }
 template <class R>
-cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
-  k_sa_prep<R><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
-  k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 0);
+cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st, int final_bc) {
+  // k_sa_prep beside the first turbc
+  k_sa_prep_bc<R><<<b.nslice + b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice);
   // on the residual's tiles (tile table of the batch's tile shape)
   switch (b.rt_shape) {
     case 1: k_sa_rhs<R, 32, 8><<<b.tile_blocks, 256, sa_rhs_smem<R, 32, 8>(), st>>>(d_sl, b.d_tfirst, b.nslice); break;
@@ -214,6 +214,12 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   if (ae != cudaSuccess) return ae;
   k_sa_lsolvej<R><<<b.jgroups, 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sa_lsolve<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice, 1);
+  if (final_bc) k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 1);
+  return cudaGetLastError();
+}
+// the closing turbc of vmu_sa and c_turm on the halo ring
+template <class R>
+cudaError_t launch_sa_final_bc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 1);
   return cudaGetLastError();
 }
@@ -302,10 +308,21 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
     if ((e = cudaEventRecord(br->fork, st)) != cudaSuccess) return e;
     if ((e = launch_lusgs_sweeps(d_sl, b, st, 1)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(br->st, br->fork, 0)) != cudaSuccess) return e;
-    if ((turb & 1) && (e = launch_sa(d_sl, b, br->st)) != cudaSuccess) return e;
+    if ((turb & 1) && (e = launch_sa(d_sl, b, br->st, 0)) != cudaSuccess) return e;
     if ((turb & 2) && (e = launch_sst(d_sl, b, br->st)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(br->join, br->st)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(st, br->join, 0)) != cudaSuccess) return e;
+    // SA's closing turbc writes nu_tilde and mu_t on the halo ring, which
+    // the state update does not touch (it reads and writes the interior
+    // flow variables, and its time step reads the halo's flow variables):
+    // it runs beside the update and joins at the end of the iteration.
+    if (turb & 1) {
+      if ((e = launch_sa_final_bc(d_sl, b, br->st)) != cudaSuccess) return e;
+      if ((e = cudaEventRecord(br->join_end, br->st)) != cudaSuccess) return e;
+    }
+    if ((e = launch_update(d_sl, b, st)) != cudaSuccess) return e;
+    if ((turb & 1) && (e = cudaStreamWaitEvent(st, br->join_end, 0)) != cudaSuccess) return e;
+    return cudaSuccess;
   } else {
     if ((lhs & 1) && (e = launch_lusgs(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
     if ((lhs & 2) && (e = launch_adi(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
@@ -329,7 +346,8 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   template cudaError_t launch_faces<R>(const Slice<R>*, const Batch&, int, int, cudaStream_t);          \
   template cudaError_t launch_resid_tiles<R>(const Slice<R>*, const Batch&, int, cudaStream_t);         \
   template cudaError_t launch_assemble<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
-  template cudaError_t launch_sa<R>(const Slice<R>*, const Batch&, cudaStream_t);                       \
+  template cudaError_t launch_sa<R>(const Slice<R>*, const Batch&, cudaStream_t, int);                  \
+  template cudaError_t launch_sa_final_bc<R>(const Slice<R>*, const Batch&, cudaStream_t);              \
   template cudaError_t launch_sst<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
   template cudaError_t launch_adi<R>(const Slice<R>*, const Batch&, int, cudaStream_t, int);            \
   template cudaError_t launch_update<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
