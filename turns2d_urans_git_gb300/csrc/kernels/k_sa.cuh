@@ -253,15 +253,21 @@ __device__ void sa_lsolvej_line(const Slice<R>& S, const ot2d_params& p, int k) 
   }
 }
 
-// lsolvej for 32 consecutive k-lines by one warp (lane l <-> line kline0+l).
-// The lines run along j, the fast index of the arrays, so the warp stages
-// 32 x 32 tiles through shared memory (one row of a tile per load, then one
-// line per lane); the arithmetic per line is sa_lsolvej_line's, in its
-// order.  The tiles are fetched with cp.async into two buffers, the next
-// tile in flight while the current one is eliminated.
+// lsolvej for 32 consecutive k-lines by a CTA of two warps.  The lines run
+// along j, the fast index of the arrays, so 32 x 32 tiles are staged
+// through shared memory (one row of a tile per copy, then one line per
+// lane).  Warp 0 eliminates: lane l walks line kline0+l through the tile
+// with the arithmetic of sa_lsolvej_line, in its order, and reads and
+// writes only shared memory.  Warp 1 moves the data through three buffers:
+// while warp 0 works on tile t it stores the results of tile t-1 and
+// fetches tile t+2 (cp.async) into that buffer, so the recurrence neither
+// waits on global memory nor spends its issue slots on copies.  The two
+// warps meet at one named barrier per tile.
 // smem: LJ_SMEM elements of R.
 constexpr int LJ_TILE = 32 * 33;
-constexpr int LJ_SMEM = 2 * 4 * LJ_TILE;
+constexpr int LJ_NBUF = 3;
+constexpr int LJ_SMEM = LJ_NBUF * 4 * LJ_TILE;
+constexpr int LJ_THREADS = 64;
 
 template <class R>
 __device__ __forceinline__ void lj_cp_async(R* dst, const R* src) {
@@ -271,6 +277,8 @@ __device__ __forceinline__ void lj_cp_async(R* dst, const R* src) {
 __device__ __forceinline__ void lj_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void lj_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+// the two warps of the CTA meet (named barrier 1, 64 threads)
+__device__ __forceinline__ void lj_meet() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
 
 // The bands are the scratch slots sa, sb, sc, ss.  SAOUT: the result is
 // ((x + 0) - 0) * b as vmu_sa forms it (samodel2d.f:150-153); otherwise
@@ -279,6 +287,7 @@ template <class R, bool SAOUT = true>
 __device__ void sa_lsolvej_group(const Slice<R>& S, const ot2d_params& p, int kline0, R* sm, int sa = W_AJ,
                                  int sb = W_BJ, int sc = W_CJ, int ss = W_SJ) {
   const int lane = threadIdx.x & 31;
+  const bool mover = (threadIdx.x >> 5) == 1;
   const int jd = S.jd; const int64_t ws = S.wstride;
   const R* ga = S.w + sa * ws; R* gc = S.w + sc * ws; R* gs = S.w + ss * ws; const R* gb = S.w + sb * ws;
   const int js = p.jbeg, je = p.jend, ks = p.kbeg, ke = p.kend;
@@ -286,7 +295,9 @@ __device__ void sa_lsolvej_group(const Slice<R>& S, const ot2d_params& p, int kl
   const bool mine = ks + kline0 + lane <= ke;
   // buffer b of array m: sm + (b*4 + m)*LJ_TILE; element (row r, column c) at r*33 + c
   auto buf = [&](int b, int m) { return sm + (b * 4 + m) * LJ_TILE; };
-  // fetch tile t (columns j0..j0+31) of arrays m0..m0+nm-1 of {a, b, c, s}
+  // mover: issue the copies of tile t (columns j0..j0+31) of {a,} b, c, s
+  // into buffer b as one cp.async group.  Each lane copies column lane of
+  // every row, the same elements it stores below.
   auto fetch = [&](int t, int b, bool fwd) {
     const int j = js + 32 * t + lane;
     for (int r = 0; r < 32; ++r) {
@@ -301,67 +312,94 @@ __device__ void sa_lsolvej_group(const Slice<R>& S, const ot2d_params& p, int kl
     }
     lj_commit();
   };
-  R cp = (R)0, sp = (R)0;
-  // forward elimination
-  fetch(0, 0, true);
-  for (int t = 0; t < ntile; ++t) {
-    const int b = t & 1;
-    if (t + 1 < ntile) { fetch(t + 1, b ^ 1, true); lj_wait<1>(); }
-    else lj_wait<0>();
-    __syncwarp();
-    const R *A = buf(b, 0), *B = buf(b, 1);
-    R *Cm = buf(b, 2), *Sm = buf(b, 3);
-    const int j0 = js + 32 * t, j = j0 + lane;
-    if (mine) {
-      for (int jj = 0; jj < 32 && j0 + jj <= je; ++jj) {
-        const int i = lane * 33 + jj;
-        R bb;
-        if (j0 + jj == js) { bb = (R)1. / B[i]; sp = Sm[i] * bb; cp = Cm[i] * bb; }
-        else { bb = (R)1. / (B[i] - A[i] * cp); sp = (Sm[i] - A[i] * sp) * bb; cp = Cm[i] * bb; }
-        Sm[i] = sp; Cm[i] = cp;
-      }
-    }
-    __syncwarp();
+  // mover: store tile t's results from buffer b (forward: c and s; backward: s)
+  auto store = [&](int t, int b, bool fwd) {
+    const int j = js + 32 * t + lane;
+    const R *Cm = buf(b, 2), *Sm = buf(b, 3);
     for (int r = 0; r < 32; ++r) {
       const int kr = ks + kline0 + r;
       if (kr <= ke && j <= je) {
         const int64_t o = at(jd, j, kr);
-        gc[o] = Cm[r * 33 + lane]; gs[o] = Sm[r * 33 + lane];
+        if (fwd) gc[o] = Cm[r * 33 + lane];
+        gs[o] = Sm[r * 33 + lane];
       }
     }
-    __syncwarp();
-  }
-  // the stores above are read back below by the same lanes (same element
-  // -> lane mapping); order them before the asynchronous copies
-  __threadfence_block();
-  // back substitution; output x * bjmat (samodel2d.f:150-153)
-  R snext = sp;
-  fetch(ntile - 1, 0, false);
-  for (int t = ntile - 1, n = 0; t >= 0; --t, ++n) {
-    const int b = n & 1;
-    if (t > 0) { fetch(t - 1, b ^ 1, false); lj_wait<1>(); }
+  };
+  // ---- forward elimination.  Round t: warp 0 eliminates tile t (buffer
+  // t%3); warp 1 stores tile t-1 and then fetches tile t+2 into the buffer
+  // tile t-1 used (the stores read it before the copies overwrite it), and
+  // waits for tile t+1.
+  R cp = (R)0, sp = (R)0;
+  if (mover) {
+    fetch(0, 0, true);
+    if (ntile > 1) { fetch(1, 1, true); lj_wait<1>(); }
     else lj_wait<0>();
-    __syncwarp();
-    const R *B = buf(b, 1), *Cm = buf(b, 2);
-    R* Sm = buf(b, 3);
-    const int j0 = js + 32 * t, j = j0 + lane;
-    if (mine) {
-      const int jjmax = (je - j0 < 31) ? je - j0 : 31;
-      for (int jj = jjmax; jj >= 0; --jj) {
-        const int i = lane * 33 + jj;
-        R x = (j0 + jj == je) ? Sm[i] : Sm[i] - Cm[i] * snext;
-        snext = x;
-        if constexpr (SAOUT) Sm[i] = ((x + (R)0.) - (R)0.) * B[i];
-        else Sm[i] = x * B[i];
-      }
-    }
-    __syncwarp();
-    for (int r = 0; r < 32; ++r) {
-      const int kr = ks + kline0 + r;
-      if (kr <= ke && j <= je) gs[at(jd, j, kr)] = Sm[r * 33 + lane];
-    }
-    __syncwarp();
   }
+  lj_meet();
+  for (int t = 0; t < ntile; ++t) {
+    const int b = t % LJ_NBUF;
+    if (!mover) {
+      if (mine) {
+        const R *A = buf(b, 0), *B = buf(b, 1);
+        R *Cm = buf(b, 2), *Sm = buf(b, 3);
+        const int j0 = js + 32 * t;
+        for (int jj = 0; jj < 32 && j0 + jj <= je; ++jj) {
+          const int i = lane * 33 + jj;
+          R bb;
+          if (j0 + jj == js) { bb = (R)1. / B[i]; sp = Sm[i] * bb; cp = Cm[i] * bb; }
+          else { bb = (R)1. / (B[i] - A[i] * cp); sp = (Sm[i] - A[i] * sp) * bb; cp = Cm[i] * bb; }
+          Sm[i] = sp; Cm[i] = cp;
+        }
+      }
+    } else {
+      const int bf = (t + 2) % LJ_NBUF;   // = (t - 1) % 3
+      if (t >= 1) store(t - 1, bf, true);
+      __syncwarp();
+      if (t + 2 < ntile) { fetch(t + 2, bf, true); lj_wait<1>(); }
+      else lj_wait<0>();
+    }
+    lj_meet();
+  }
+  // ---- back substitution; output x * bjmat (samodel2d.f:150-153).  Round
+  // n (tile t = ntile-1-n, buffer n%3): warp 1 stores tile t+1 and fetches
+  // tile t-2.
+  if (mover) {
+    store(ntile - 1, (ntile - 1) % LJ_NBUF, true);
+    // the stores are read back below by the same lanes (same element ->
+    // lane mapping); order them before the asynchronous copies
+    __threadfence_block();
+    fetch(ntile - 1, 0, false);
+    if (ntile > 1) { fetch(ntile - 2, 1, false); lj_wait<1>(); }
+    else lj_wait<0>();
+  }
+  lj_meet();
+  R snext = sp;
+  for (int t = ntile - 1, n = 0; t >= 0; --t, ++n) {
+    const int b = n % LJ_NBUF;
+    if (!mover) {
+      if (mine) {
+        const R *B = buf(b, 1), *Cm = buf(b, 2);
+        R* Sm = buf(b, 3);
+        const int j0 = js + 32 * t;
+        const int jjmax = (je - j0 < 31) ? je - j0 : 31;
+        for (int jj = jjmax; jj >= 0; --jj) {
+          const int i = lane * 33 + jj;
+          R x = (j0 + jj == je) ? Sm[i] : Sm[i] - Cm[i] * snext;
+          snext = x;
+          if constexpr (SAOUT) Sm[i] = ((x + (R)0.) - (R)0.) * B[i];
+          else Sm[i] = x * B[i];
+        }
+      }
+    } else {
+      const int bf = (n + 2) % LJ_NBUF;   // = (n - 1) % 3
+      if (n >= 1) store(t + 1, bf, false);
+      __syncwarp();
+      if (t - 2 >= 0) { fetch(t - 2, bf, false); lj_wait<1>(); }
+      else lj_wait<0>();
+    }
+    lj_meet();
+  }
+  if (mover) store(0, (ntile - 1) % LJ_NBUF, false);
 }
 
 // lsolvek (samodel2d.f:1347-1385) on one j-line, then s2 = x and the

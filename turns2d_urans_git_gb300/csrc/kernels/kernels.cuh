@@ -568,10 +568,10 @@ __global__ void k_sa_lsolve(const Slice<R>* __restrict__ sl, const int32_t* __re
   else { int j = p.jbeg + line; if (j <= p.jend) sa_lsolvek_line(S, p, j); }
 }
 
-// lsolvej by warps of 32 k-lines (one warp per CTA); slice i owns groups
-// [gfirst[i], gfirst[i+1])
+// lsolvej by CTAs of 32 k-lines (two warps: elimination and data
+// movement); slice i owns groups [gfirst[i], gfirst[i+1])
 template <class R>
-__global__ void __launch_bounds__(32) k_sa_lsolvej(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ gfirst,
+__global__ void __launch_bounds__(LJ_THREADS) k_sa_lsolvej(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ gfirst,
                                                    int nslice) {
   extern __shared__ __align__(16) unsigned char lj_raw[];
   R* sm = (R*)lj_raw;   // LJ_SMEM elements
@@ -644,7 +644,7 @@ __global__ void __launch_bounds__(CELL_BS) k_sst_rhs(const Slice<R>* __restrict_
 
 // lsolvej2 of equation blockIdx.y by warps of 32 k-lines; output x * bjmat
 template <class R>
-__global__ void __launch_bounds__(32) k_sst_lsolvej(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ gfirst,
+__global__ void __launch_bounds__(LJ_THREADS) k_sst_lsolvej(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ gfirst,
                                                     int nslice) {
   extern __shared__ __align__(16) unsigned char lj_raw[];
   R* sm = (R*)lj_raw;   // LJ_SMEM elements

@@ -212,7 +212,7 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st, int
     return cudaFuncSetAttribute(k_sa_lsolvej<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lj_smem);
   });
   if (ae != cudaSuccess) return ae;
-  k_sa_lsolvej<R><<<b.jgroups, 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
+  k_sa_lsolvej<R><<<b.jgroups, LJ_THREADS, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sa_lsolve<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice, 1);
   if (final_bc) k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 1);
   return cudaGetLastError();
@@ -237,7 +237,7 @@ cudaError_t launch_sst(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
     return cudaFuncSetAttribute(k_sst_lsolvej<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lj_smem);
   });
   if (ae != cudaSuccess) return ae;
-  k_sst_lsolvej<R><<<dim3(b.jgroups, 2), 32, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
+  k_sst_lsolvej<R><<<dim3(b.jgroups, 2), LJ_THREADS, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sst_lsolvek<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice);
   k_sst_bc<R><<<b.nslice, 256, 0, st>>>(d_sl, 1);
   return cudaGetLastError();
