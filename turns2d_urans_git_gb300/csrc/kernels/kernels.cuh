@@ -69,10 +69,7 @@ __global__ void __launch_bounds__(CELL_BS / CELL_PT) k_time_step(const Slice<R>*
 // the first of the itnmax Newton iterations (:472-474) -- and the
 // physical-time factor 1/(oat*h) of newton (time.f:195-200) in red[8].
 template <class R>
-__global__ void k_iter_begin(const Slice<R>* __restrict__ sl, int nslice) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nslice) return;
-  const Slice<R>& S = sl[i];
+__device__ __forceinline__ void iter_begin_slice(const Slice<R>& S) {
   if (!S.ist) return;
   const ot2d_params& p = *S.P;
   int itn = 1;
@@ -84,6 +81,11 @@ __global__ void k_iter_begin(const Slice<R>* __restrict__ sl, int nslice) {
   if (p.ntac >= 2 && istep > 1) oat = 2. / 3.;
   if (p.ntac == 3 && istep > 2) oat = 6. / 11.;
   if (S.red) S.red[8] = 1. / (oat * p.h);
+}
+template <class R>
+__global__ void k_iter_begin(const Slice<R>* __restrict__ sl, int nslice) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nslice) iter_begin_slice(sl[i]);
 }
 
 // Moving slices at the start of a physical step: pitch + stqol (one thread
@@ -139,8 +141,12 @@ __global__ void __launch_bounds__(BC_BS) k_bc(const Slice<R>* __restrict__ sl, i
 // path, whose boundary arithmetic is f32 (the FP64 path keeps several CTAs
 // per entry: its boundary arithmetic runs on the narrow FP64 pipe).
 template <class R>
-__global__ void __launch_bounds__(BC_BS) k_bc_all(const Slice<R>* __restrict__ sl, int advance) {
+__global__ void __launch_bounds__(BC_BS) k_bc_all(const Slice<R>* __restrict__ sl, int advance, int begin) {
   const Slice<R>& S = sl[blockIdx.x];
+  if (begin) {
+    if (threadIdx.x == 0) iter_begin_slice(S);
+    __syncthreads();
+  }
   const int istep0 = S.ist ? S.ist[0] : S.P->istep0;
   for (int ib = 0; ib < S.nbc; ++ib) {
     bc_entry(S, istep0, ib, threadIdx.x, blockDim.x);
@@ -321,7 +327,7 @@ __global__ void k_norm_final(const Slice<R>* __restrict__ sl, const int32_t* __r
   S.red[0] = rsum; S.red[1] = resrho; S.red[2] = acc.resmax; S.red[3] = (double)acc.key;
   if (S.ist) {
     const int it = S.ist[1];
-    if (!(rsum <= 1000.0)) S.ist[2] |= 1;         // L2 norm out of bounds (step.f:105-110)
+    if (!(rsum <= 1000.0)) atomicOr(&S.ist[2], 1);   // L2 norm out of bounds (step.f:105-110)
     if (it == 1) S.red[4] = rsum;                 // first-iteration norm
     S.red[5] = rsum;
     if (rsum > S.red[6]) S.red[6] = rsum;         // running peak

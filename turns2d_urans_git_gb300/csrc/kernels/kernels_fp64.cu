@@ -35,6 +35,8 @@ cudaError_t branch_of_device(Branch*& out) {
     if ((e = cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&b.join, cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&b.join_end, cudaEventDisableTiming)) != cudaSuccess) return e;
+    for (cudaEvent_t* ev : {&b.resid, &b.rbc, &b.edges})
+      if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess) return e;
   }
   out = &b;
   return cudaSuccess;

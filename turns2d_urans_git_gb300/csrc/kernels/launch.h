@@ -111,6 +111,7 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
 struct Branch {
   cudaStream_t st = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, join_end = nullptr;
+  cudaEvent_t resid = nullptr, rbc = nullptr, edges = nullptr;   // side kernels of the mixed path
 };
 cudaError_t branch_of_device(Branch*& out);
 
@@ -126,8 +127,15 @@ template <class R> cudaError_t launch_pitch(const Slice<R>* d_sl, const Batch& b
 // current step, the stored levels and the Newton target (time.f:110-175)
 cudaError_t launch_stqol(const double* q, double* qtn, double* qtnm1, double* qnewt, int64_t qs, int nv, int ntac,
                          int istep, cudaStream_t st);
-template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st);
-template <class R> cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st);
+// begin = 1 (mixed path): each slice's boundary CTA first applies the
+// iteration's start to its slice (k_iter_begin's work), for an iteration
+// with nothing between the two
+template <class R> cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st,
+                                         int begin = 0);
+// norms = 0: without the per-slice norm reduction (launch_norm_final)
+template <class R> cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st,
+                                               int norms = 1);
+template <class R> cudaError_t launch_norm_final(const Slice<R>* d_sl, const Batch& b, cudaStream_t st);
 // the fused residual tiles of one tile shape (TJ x TK), every
 // (preconditioning, reconstruction family) kind the batch holds; defined in
 // k_resid_launch.cuh and instantiated in resid_*.cu

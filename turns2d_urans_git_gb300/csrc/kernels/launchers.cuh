@@ -25,12 +25,13 @@ cudaError_t launch_time_step(const Slice<R>* d_sl, const Batch& b, cudaStream_t 
   return cudaGetLastError();
 }
 template <class R>
-cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st) {
+cudaError_t launch_bc(const Slice<R>* d_sl, const Batch& b, int advance, cudaStream_t st, int begin) {
   // one launch per &bcinp entry (the reference applies them in order), each
   // spread over enough CTAs per slice to cover the longest boundary
   if constexpr (sizeof(R) == sizeof(float)) {
-    k_bc_all<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, advance);
+    k_bc_all<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, advance, begin);
   } else {
+    if (begin) k_iter_begin<R><<<(b.nslice + 127) / 128, 128, 0, st>>>(d_sl, b.nslice);
     const int nch = (std::max(b.max_wall, b.max_kd) + BCE_BS - 1) / BCE_BS;
     for (int ib = 0; ib < b.max_nbc; ++ib) k_bc_entry<R><<<dim3(nch, b.nslice), BCE_BS, 0, st>>>(d_sl, ib);
     k_bc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, advance);
@@ -63,10 +64,14 @@ cudaError_t launch_resid_both(const Slice<R>* d_sl, const Batch& b, int flags, c
   }
 }
 template <class R>
-cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st) {
+cudaError_t launch_residual(const Slice<R>* d_sl, const Batch& b, int viscous, cudaStream_t st, int norms) {
   const int flags = AS_INV | AS_TS | AS_NORM | (viscous ? AS_VISC : 0);
   cudaError_t e = launch_resid_both(d_sl, b, flags, st);
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess || !norms) return e;
+  return launch_norm_final(d_sl, b, st);
+}
+template <class R>
+cudaError_t launch_norm_final(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
   k_norm_final<R><<<b.nslice, 32, 0, st>>>(d_sl, b.d_tfirst, b.nslice, b.d_part);
   return cudaGetLastError();
 }
@@ -104,7 +109,8 @@ cudaError_t launch_rhslom(const Slice<R>* d_sl, const Batch& b, cudaStream_t st)
 // the FP64 path also round-trips q here).  PRE: the preilu2d records of the
 // preconditioned slices, launched only when the batch holds one.
 template <class R, bool PRE>
-cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
+cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu,
+                                int parts) {
   // one staged chunk per warp (f32 28 / 36 KB, f64 53 / 68 KB per block)
   constexpr size_t prep_smem = (size_t)LU_PREP_CH * lu_prep_stride<R, PRE>() * sizeof(R);
   static DeviceOnce once;
@@ -112,7 +118,9 @@ cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale,
     return cudaFuncSetAttribute(k_lu_prep<R, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)prep_smem);
   });
   if (ae != cudaSuccess) return ae;
-  k_lu_prep<R, PRE><<<b.lu_blocks, LU_PREP_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
+  if (parts & 1)
+    k_lu_prep<R, PRE><<<b.lu_blocks, LU_PREP_BS, prep_smem, st>>>(d_sl, b.d_lfirst, b.nslice, scale, only_lu);
+  if (!(parts & 2)) return cudaGetLastError();
   if constexpr (sizeof(R) == sizeof(double)) {
     // every cell: the FP64 path also round-trips q (lhs.f:524-531, :805-811)
     k_lu_edges<R, PRE><<<b.cell_blocks, CELL_BS, 0, st>>>(d_sl, b.d_first, b.nslice, scale, only_lu);
@@ -122,10 +130,12 @@ cudaError_t launch_lusgs_prep_t(const Slice<R>* d_sl, const Batch& b, int scale,
   }
   return cudaGetLastError();
 }
+// parts: 1 the records (k_lu_prep), 2 the halo edges (k_lu_edges*), 3 both
 template <class R>
-cudaError_t launch_lusgs_prep(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu) {
-  cudaError_t e = launch_lusgs_prep_t<R, false>(d_sl, b, scale, st, only_lu);
-  if (e == cudaSuccess && b.precon) e = launch_lusgs_prep_t<R, true>(d_sl, b, scale, st, only_lu);
+cudaError_t launch_lusgs_prep(const Slice<R>* d_sl, const Batch& b, int scale, cudaStream_t st, int only_lu,
+                              int parts = 3) {
+  cudaError_t e = launch_lusgs_prep_t<R, false>(d_sl, b, scale, st, only_lu, parts);
+  if (e == cudaSuccess && b.precon) e = launch_lusgs_prep_t<R, true>(d_sl, b, scale, st, only_lu, parts);
   return e;
 }
 // ilu2d part 2: the forward and backward sweeps, launched at the device's
@@ -288,11 +298,31 @@ template <class R>
 cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, int turb, int lhs, cudaStream_t st,
                              cudaEvent_t after_rbc) {
   cudaError_t e;
-  if ((e = launch_iter_begin(d_sl, b, st)) != cudaSuccess) return e;
+  // Mixed path, LU-SGS with a turbulence model: the side kernels (the norm
+  // reduction, read only by the host, and the LU-SGS halo edges, read only
+  // by the sweeps; the f32 edges touch the halo ring alone) run on the
+  // branch stream beside rbc and the record kernel, and the iteration's
+  // start is applied by the boundary kernel when nothing comes between.
+  const bool side = sizeof(R) == sizeof(float) && lhs == 1 && turb;
+  const bool begin_in_bc = sizeof(R) == sizeof(float) && b.ts_in_update && !b.moving;
+  Branch* br = nullptr;
+  if ((lhs == 1 && turb) && (e = branch_of_device(br)) != cudaSuccess) return e;
+  if (!begin_in_bc && (e = launch_iter_begin(d_sl, b, st)) != cudaSuccess) return e;
   if (!b.ts_in_update && (e = launch_time_step(d_sl, b, st)) != cudaSuccess) return e;
-  if ((e = launch_bc(d_sl, b, 1, st)) != cudaSuccess) return e;
-  if ((e = launch_residual(d_sl, b, viscous, st)) != cudaSuccess) return e;
+  if ((e = launch_bc(d_sl, b, 1, st, begin_in_bc ? 1 : 0)) != cudaSuccess) return e;
+  if ((e = launch_residual(d_sl, b, viscous, st, side ? 0 : 1)) != cudaSuccess) return e;
+  if (side) {
+    if ((e = cudaEventRecord(br->resid, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(br->st, br->resid, 0)) != cudaSuccess) return e;
+    if ((e = launch_norm_final(d_sl, b, br->st)) != cudaSuccess) return e;
+  }
   if ((e = launch_rbc(d_sl, b, st)) != cudaSuccess) return e;
+  if (side) {
+    if ((e = cudaEventRecord(br->rbc, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(br->st, br->rbc, 0)) != cudaSuccess) return e;
+    if ((e = launch_lusgs_prep(d_sl, b, 1, br->st, 1, 2)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(br->edges, br->st)) != cudaSuccess) return e;
+  }
   // the pipelined solver starts the other half of its batch here (an
   // external event node of the captured graph)
   if (after_rbc && (e = cudaEventRecordWithFlags(after_rbc, st, cudaEventRecordExternal)) != cudaSuccess) return e;
@@ -302,10 +332,9 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
     // which the sweeps do not read once the records are built: after the
     // record / edge kernels (mu_t read, FP64 q round trip done) it runs on
     // a second stream beside the sweeps, joined before the update.
-    Branch* br = nullptr;
-    if ((e = branch_of_device(br)) != cudaSuccess) return e;
-    if ((e = launch_lusgs_prep(d_sl, b, 1, st, 1)) != cudaSuccess) return e;
+    if ((e = launch_lusgs_prep(d_sl, b, 1, st, 1, side ? 1 : 3)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(br->fork, st)) != cudaSuccess) return e;
+    if (side && (e = cudaStreamWaitEvent(st, br->edges, 0)) != cudaSuccess) return e;
     if ((e = launch_lusgs_sweeps(d_sl, b, st, 1)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(br->st, br->fork, 0)) != cudaSuccess) return e;
     if ((turb & 1) && (e = launch_sa(d_sl, b, br->st, 0)) != cudaSuccess) return e;
@@ -338,8 +367,9 @@ cudaError_t launch_iteration(const Slice<R>* d_sl, const Batch& b, int viscous, 
   template cudaError_t launch_time_step<R>(const Slice<R>*, const Batch&, cudaStream_t);                \
   template cudaError_t launch_iter_begin<R>(const Slice<R>*, const Batch&, cudaStream_t);               \
   template cudaError_t launch_pitch<R>(const Slice<R>*, const Batch&, cudaStream_t);                    \
-  template cudaError_t launch_bc<R>(const Slice<R>*, const Batch&, int, cudaStream_t);                  \
-  template cudaError_t launch_residual<R>(const Slice<R>*, const Batch&, int, cudaStream_t);            \
+  template cudaError_t launch_bc<R>(const Slice<R>*, const Batch&, int, cudaStream_t, int);             \
+  template cudaError_t launch_residual<R>(const Slice<R>*, const Batch&, int, cudaStream_t, int);       \
+  template cudaError_t launch_norm_final<R>(const Slice<R>*, const Batch&, cudaStream_t);               \
   template cudaError_t launch_rbc<R>(const Slice<R>*, const Batch&, cudaStream_t);                      \
   template cudaError_t launch_rhslom<R>(const Slice<R>*, const Batch&, cudaStream_t);                   \
   template cudaError_t launch_lusgs<R>(const Slice<R>*, const Batch&, int, cudaStream_t, int);          \
