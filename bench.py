@@ -503,29 +503,39 @@ def e2e_rate(sv, ids, cases, steps, world, dist):
 
 
 def host_link(pinned, reps=5):
-    """The host link's copy rates for the same pinned buffers (the bound of
-    the host-buffer path): all uploads, all downloads, and both directions at
-    once on two streams, GB/s."""
+    """The host link's copy rates for the bytes the host-buffer path moves per
+    step (the bound of that path): one pinned buffer of that size copied up,
+    down, and both ways at once on two streams, timed with CUDA events (best
+    of reps, so that no host-side issue time enters), GB/s."""
     import torch
-    dev = [torch.empty_like(t, device="cuda") for t in pinned]
     nbytes = sum(t.numel() * t.element_size() for t in pinned)
+    h_up = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h_dn = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d_up = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d_dn = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
     s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
     out = {}
     for kind in ("h2d", "d2h", "both"):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        best = float("inf")
         for _ in range(reps):
-            for d, h in zip(dev, pinned):
-                if kind in ("h2d", "both"):
-                    with torch.cuda.stream(s1):
-                        d.copy_(h, non_blocking=True)
-                if kind in ("d2h", "both"):
-                    with torch.cuda.stream(s2):
-                        h.copy_(d, non_blocking=True)
-        torch.cuda.synchronize()
-        dt = (time.perf_counter() - t0) / reps
-        out[kind + "_gbs"] = (2 if kind == "both" else 1) * nbytes / dt / 1e9
-    del dev
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(torch.cuda.current_stream())
+            s1.wait_event(e0)
+            s2.wait_event(e0)
+            if kind in ("h2d", "both"):
+                with torch.cuda.stream(s1):
+                    d_up.copy_(h_up, non_blocking=True)
+            if kind in ("d2h", "both"):
+                with torch.cuda.stream(s2):
+                    h_dn.copy_(d_dn, non_blocking=True)
+            e1.record(s1)
+            e2.record(s2)
+            torch.cuda.synchronize()
+            best = min(best, max(e0.elapsed_time(e1), e0.elapsed_time(e2)) / 1e3)
+        out[kind + "_gbs"] = (2 if kind == "both" else 1) * nbytes / best / 1e9
+    del h_up, h_dn, d_up, d_dn
     return out
 
 
