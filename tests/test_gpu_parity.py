@@ -88,8 +88,14 @@ def test_rbc():
 
 
 @pytest.mark.parametrize("visc", [False, True])
-def test_ilu2d(visc):
-    c = Case(viscous=visc, seed=6)
+@pytest.mark.parametrize("size", [(65, 25), (97, 69)])
+def test_ilu2d(visc, size):
+    """ilu2d (lhs.f:470-814) drop-in against the oracle.  65x25: one band of
+    24 rows (every step in the sweep's per-step form); 97x69: two full bands
+    of 32 rows, whose steps 32..95 run as steady groups, and a band of 4
+    rows, so the cross-band hand-offs go steady -> steady -> per-step
+    (forward) and back (backward)."""
+    c = Case(jmax=size[0], kmax=size[1], viscous=visc, seed=6)
     L = ob.lib()
     L.oro_time_step(_o(c), ob.ptr(c.q), ob.ptr(c.xx), ob.ptr(c.xy), ob.ptr(c.yx), ob.ptr(c.yy), ob.ptr(c.ug),
                     ob.ptr(c.vg), ob.ptr(c.tscale), ob.ptr(c.bt), ob.ptr(c.iblank))
