@@ -772,6 +772,20 @@ void visrhs(const P& p, A2 turmu, A3 q, A3 s, A2 xx, A2 xy, A2 yx, A2 yy) {
 
 }  // namespace oro
 
+/* Test hook: roeflx on one face, left state ql and right state qr (the
+ * primitives rho, u, v, p), face vector (ri1, ri2), grid-speed term ri3;
+ * the four fluxes out in f.  No counterpart in the reference. */
+extern "C" void oro_roe_face(double gm1, const double* ql, const double* qr, double ri1, double ri2, double ri3,
+                             double* f) {
+  oro::P p{};
+  p.gm1 = gm1;
+  oro::Line L(2);
+  for (int n = 1; n <= 4; ++n) { L.ql[n][1] = ql[n - 1]; L.qr[n][2] = qr[n - 1]; }
+  L.xa[1] = ri1; L.ya[1] = ri2; L.tj[1] = ri3;
+  oro::roeflx(p, L, 1, 1);
+  for (int n = 1; n <= 4; ++n) f[n - 1] = L.f[n][1];
+}
+
 /* Test hook: quad on one line of primitives f[0..n) (one variable; the
  * other three lines a copy of it), ql/qr out.  No counterpart in the
  * reference. */

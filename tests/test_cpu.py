@@ -347,6 +347,101 @@ def test_oracle_sa_source_matches_the_published_model():
     assert not bk[~inner].any() and not sjmat[~inner].any()
 
 
+def _roe_face(ql, qr, ri, ri3=0.0, gm1=0.4):
+    L = ob.lib()
+    dp = C.POINTER(C.c_double)
+    L.oro_roe_face.argtypes = [C.c_double, dp, dp, C.c_double, C.c_double, C.c_double, dp]
+    f = np.zeros(4)
+    L.oro_roe_face(gm1, ob.ptr(np.asarray(ql, dtype=np.float64)), ob.ptr(np.asarray(qr, dtype=np.float64)),
+                   float(ri[0]), float(ri[1]), float(ri3), ob.ptr(f))
+    return f
+
+
+def _euler_normal(w, n, r3, gm1):
+    """Conservative state, moving-face normal flux (per unit face length)
+    and its Jacobian for primitives w = (rho, u, v, p) on unit normal n with
+    grid term r3: F = U qn' + p (0, nx, ny, qn) with qn' = u nx + v ny + r3,
+    qn = u nx + v ny; the Jacobian of the fixed-face flux (the textbook 2-D
+    Euler form) plus r3 I."""
+    rho, u, v, p = w
+    nx, ny = n
+    g = gm1 + 1.0
+    E = p / gm1 + 0.5 * rho * (u * u + v * v)
+    H = (E + p) / rho
+    qn = u * nx + v * ny
+    U = np.array([rho, rho * u, rho * v, E])
+    F = U * (qn + r3) + p * np.array([0.0, nx, ny, qn])
+    phi = 0.5 * gm1 * (u * u + v * v)
+    A = np.array([[0.0, nx, ny, 0.0],
+                  [phi * nx - u * qn, qn - (g - 2.0) * u * nx, u * ny - gm1 * v * nx, gm1 * nx],
+                  [phi * ny - v * qn, v * nx - gm1 * u * ny, qn - (g - 2.0) * v * ny, gm1 * ny],
+                  [qn * (phi - H), H * nx - gm1 * u * qn, H * ny - gm1 * v * qn, g * qn]])
+    return U, F, A + r3 * np.eye(4)
+
+
+@pytest.mark.parametrize("r3", [0.0, 0.23])
+def test_oracle_roe_flux_is_the_roe_scheme(r3):
+    """The oracle's roeflx (eulerrhs.f:283-446) against the published Roe
+    scheme restated independently: F = (F_L + F_R)/2 - |A(W)| (U_R - U_L)/2
+    scaled by the face length, with A(W) the Euler flux Jacobian at the
+    Roe-averaged state (sqrt(rho) weights for u, v, H) and |A| = R |Lambda|
+    R^-1 from a numerical eigen-decomposition.  States that keep every wave
+    speed outside the reference's entropy fix band |lambda| <= (4 dlambda +
+    1e-6)/2.  Also consistency F(W, W) = F(W) and, for supersonic states,
+    full upwinding F = F_L.  These pin every dissipation coefficient, which
+    the freestream and symmetry invariants cannot see."""
+    gm1 = 0.4
+    rng = np.random.default_rng(11)
+    checked = 0
+    for _ in range(40):
+        ri = rng.uniform(-2.0, 2.0, 2)
+        rr = float(np.hypot(*ri))
+        n = ri / rr
+        wl = np.array([rng.uniform(0.6, 1.4), rng.uniform(-0.4, 0.4), rng.uniform(-0.4, 0.4), rng.uniform(0.5, 0.9)])
+        wr = wl * (1.0 + rng.uniform(-0.02, 0.02, 4))
+        # consistency at W = W_L
+        _, fl, _ = _euler_normal(wl, n, r3 / rr, gm1)
+        assert np.allclose(_roe_face(wl, wl, ri, r3, gm1), rr * fl, rtol=1e-13, atol=1e-13)
+        # the Roe state and the wave speeds the reference's entropy fix sees
+        sl, sr = np.sqrt(wl[0]), np.sqrt(wr[0])
+        Ul, Fl, _ = _euler_normal(wl, n, r3 / rr, gm1)
+        Ur, Fr, _ = _euler_normal(wr, n, r3 / rr, gm1)
+        Hl, Hr = (Ul[3] + wl[3]) / wl[0], (Ur[3] + wr[3]) / wr[0]
+        u = (sl * wl[1] + sr * wr[1]) / (sl + sr)
+        v = (sl * wl[2] + sr * wr[2]) / (sl + sr)
+        H = (sl * Hl + sr * Hr) / (sl + sr)
+        c = np.sqrt(gm1 * (H - 0.5 * (u * u + v * v)))
+        rho = sl * sr
+        p = rho * (H - 0.5 * (u * u + v * v)) * gm1 / (gm1 + 1.0)
+        _, _, A = _euler_normal(np.array([rho, u, v, p]), n, r3 / rr, gm1)
+        lam, R = np.linalg.eig(A)
+        assert np.allclose(np.sort(lam.real), np.sort([u * n[0] + v * n[1] + r3 / rr + d for d in (-c, 0, 0, c)]),
+                           rtol=1e-10, atol=1e-12)
+        cl = np.sqrt((gm1 + 1.0) * wl[3] / wl[0])
+        cr = np.sqrt((gm1 + 1.0) * wr[3] / wr[0])
+        qnl = wl[1] * n[0] + wl[2] * n[1] + r3 / rr
+        qnr = wr[1] * n[0] + wr[2] * n[1] + r3 / rr
+        qn = u * n[0] + v * n[1] + r3 / rr
+        if any(abs(lav) <= 0.5 * max(4.0 * (b - a) + 1e-6, 0.0) + 1e-3
+               for lav, a, b in ((qn, qnl, qnr), (qn + c, qnl + cl, qnr + cr), (qn - c, qnl - cl, qnr - cr))):
+            continue   # a wave speed inside the entropy fix band
+        checked += 1
+        absA = (R @ np.diag(np.abs(lam)) @ np.linalg.inv(R)).real
+        want = rr * (0.5 * (Fl + Fr) - 0.5 * absA @ (Ur - Ul))
+        got = _roe_face(wl, wr, ri, r3, gm1)
+        assert np.allclose(got, want, rtol=1e-10, atol=1e-12 * rr), (got, want)
+    assert checked >= 30
+    # supersonic along the face normal: every wave runs downstream, F = F_L
+    for _ in range(10):
+        ri = rng.uniform(0.5, 2.0, 2)
+        rr = float(np.hypot(*ri))
+        n = ri / rr
+        wl = np.array([1.0, 3.0 * n[0], 3.0 * n[1], 0.7])
+        wr = wl * (1.0 + rng.uniform(-0.02, 0.02, 4))
+        _, fl, _ = _euler_normal(wl, n, 0.0, gm1)
+        assert np.allclose(_roe_face(wl, wr, ri, 0.0, gm1), rr * fl, rtol=1e-11, atol=1e-12)
+
+
 def _quad_line(f, qt=0.25):
     L = ob.lib()
     L.oro_quad_line.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_double, C.POINTER(C.c_double),
