@@ -442,6 +442,64 @@ def test_oracle_roe_flux_is_the_roe_scheme(r3):
         assert np.allclose(_roe_face(wl, wr, ri, 0.0, gm1), rr * fl, rtol=1e-11, atol=1e-12)
 
 
+@pytest.mark.parametrize("flow", ["shear", "normal"])
+def test_oracle_viscous_terms_are_the_finite_volume_stresses(flow):
+    """The oracle's visrhs (visrhs.f:2-287) against the finite-volume
+    viscous terms written from the Navier-Stokes stress tensor (Stokes'
+    hypothesis), on a Cartesian grid (spacings hx, hy) with constant density
+    and temperature (T = T_inf, so Sutherland's mu is 1) and v = 0:
+    shear: u = a y^2, tau_xy = mu du/dy; per cell of volume V the x-momentum
+    term is V mu/Re d2u/dy2 = 2 a mu V / Re, the energy term the difference
+    of u tau_xy over the two eta faces, mu/Re hx/hy (u_{k+1}^2 - 2 u_k^2 +
+    u_{k-1}^2)/2.  normal: u = a x^2, tau_xx = 4/3 mu du/dx; 4/3 2 a mu V /
+    Re and 4/3 mu/Re hy/hx (u_{j+1}^2 - 2 u_j^2 + u_{j-1}^2)/2.  Central
+    differences are exact for a parabola; the mass and y-momentum terms
+    vanish (every cross-derivative term meets a zero: a Cartesian metric,
+    v = 0 or a constant temperature).  Unlike the freestream invariants this
+    fixes the viscous coefficients and the Reynolds-number scaling."""
+    c = Case(jmax=65, kmax=25, viscous=True, perturb=0)
+    p = c.p
+    jm, km, n2, nq = p.jmax, p.kmax, c.n2, p.nq
+    hx, hy, a = 0.03, 0.02, 0.7
+    j, k = np.arange(jm), np.arange(km)
+    xv = np.ascontiguousarray((j[None, :] * hx + 0.0 * k[:, None]).ravel())
+    yv = np.ascontiguousarray((k[:, None] * hy + 0.0 * j[None, :]).ravel())
+    x, y, xx, xy, yx, yy = (np.zeros(n2) for _ in range(6))
+    q = np.zeros(n2 * nq)
+    L, pp = ob.lib(), C.byref(p)
+    L.oro_find_cellcenter(pp, ob.ptr(x), ob.ptr(y), ob.ptr(xv), ob.ptr(yv))
+    assert L.oro_metfv(pp, ob.ptr(q), ob.ptr(xv), ob.ptr(yv), ob.ptr(xx), ob.ptr(xy), ob.ptr(yx), ob.ptr(yy)) == 0
+    qq = q.reshape(nq, n2)
+    J = qq[nq - 1].copy()
+    assert np.allclose(J, 1.0 / (hx * hy), rtol=1e-12)
+    rho, pres = 1.0, 1.0 / p.gamma          # gamma p / rho = 1: T = T_inf, mu = 1
+    u = a * (y * y if flow == "shear" else x * x)
+    qq[0] = rho / J
+    qq[1] = rho * u / J
+    qq[2] = 0.0
+    qq[3] = (pres / p.gm1 + 0.5 * rho * u * u) / J
+    sres = np.zeros(n2 * p.nv)
+    L.oro_visrhs(pp, ob.ptr(np.zeros(n2)), ob.ptr(q), ob.ptr(sres), ob.ptr(xx), ob.ptr(xy), ob.ptr(yx), ob.ptr(yy))
+    sv = sres.reshape(p.nv, n2)
+    # cells whose stencils stay off the halo (the C-mesh set-up places the
+    # halo centres by its own rules, not on the Cartesian continuation)
+    jj, kk = np.meshgrid(np.arange(p.jbeg + 1, p.jend), np.arange(p.kbeg + 1, p.kend), indexing="ij")
+    o = ((kk - 1) * p.jd + (jj - 1)).ravel()
+    mu_re = 1.0 / p.rey
+    if flow == "shear":
+        f, d, ratio = 1.0, p.jd, hx / hy
+    else:
+        f, d, ratio = 4.0 / 3.0, 1, hy / hx
+    up, u0, um = u[o + d], u[o], u[o - d]
+    assert np.allclose(sv[1][o], f * 2.0 * a * mu_re * hx * hy, rtol=1e-9, atol=0)
+    # energy: the heat flux of the rounded, nearly equal internal energies
+    # (e = q4/q1 - u^2/2) leaves an absolute residue of ~1e-21
+    e4 = f * mu_re * ratio * 0.5 * (up * up - 2.0 * u0 * u0 + um * um)
+    assert np.allclose(sv[3][o], e4, rtol=1e-9, atol=1e-9 * np.abs(e4).max())
+    scale = 2.0 * a * mu_re * hx * hy
+    assert np.max(np.abs(sv[0][o])) == 0.0 and np.max(np.abs(sv[2][o])) <= 1e-12 * scale
+
+
 def _quad_line(f, qt=0.25):
     L = ob.lib()
     L.oro_quad_line.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_double, C.POINTER(C.c_double),
