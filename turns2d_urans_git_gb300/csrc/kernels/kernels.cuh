@@ -443,35 +443,26 @@ __global__ void k_lu_sweep(const Slice<R>* __restrict__ sl, int only_lu, uint32_
   lu_sweep_slice<R, FWD, G, PRE>(sl[blockIdx.x], blockDim.x >> 5, lu_smem, poll_limit, lag);
 }
 
+// vmu_sa's closing turbc (with the velocities k_sa_prep stored at the start
+// of the step) and c_turm on the halo ring (the interior was done by the
+// k-line solve right after its update; turbc leaves interior cells
+// unchanged).  The opening turbc runs inside k_sa_prep_bc.
 template <class R>
-__global__ void __launch_bounds__(CELL_BS) k_sa_prep(const Slice<R>* __restrict__ sl, const int32_t* __restrict__ first,
-                                                     int nslice) {
-  OT2D_CELL_MAP();
-  if (!inside) return;
-  if (S.P->lamin || S.P->iturb != 1) return;
-  sa_prep_cell(S, *S.P, j, k);
-}
-
-template <class R>
-__global__ void __launch_bounds__(BC_BS) k_turbc(const Slice<R>* __restrict__ sl, int final_pass) {
+__global__ void __launch_bounds__(BC_BS) k_turbc(const Slice<R>* __restrict__ sl) {
   const Slice<R>& S = sl[blockIdx.x];
   const ot2d_params& p = *S.P;
   if (p.lamin || p.iturb != 1) return;
   turbc_slice(S, S.w + W_U * S.wstride, S.w + W_V * S.wstride);
   shadow_ring(S, p.nmv + 1, p.nmv + 1);
-  if (final_pass) {
-    // c_turm on the halo ring (the interior was done by the k-line solve
-    // right after its update; turbc leaves interior cells unchanged)
-    __syncthreads();
-    const int jd = S.jd, kd = S.kd, nring = 2 * jd + 2 * (kd - 2);
-    for (int i = threadIdx.x; i < nring; i += blockDim.x) {
-      int j, k;
-      if (i < jd) { j = i + 1; k = 1; }
-      else if (i < 2 * jd) { j = i - jd + 1; k = kd; }
-      else if (i < 2 * jd + kd - 2) { j = 1; k = i - 2 * jd + 2; }
-      else { j = jd; k = i - (2 * jd + kd - 2) + 2; }
-      sa_turm_cell(S, p, j, k);
-    }
+  __syncthreads();
+  const int jd = S.jd, kd = S.kd, nring = 2 * jd + 2 * (kd - 2);
+  for (int i = threadIdx.x; i < nring; i += blockDim.x) {
+    int j, k;
+    if (i < jd) { j = i + 1; k = 1; }
+    else if (i < 2 * jd) { j = i - jd + 1; k = kd; }
+    else if (i < 2 * jd + kd - 2) { j = 1; k = i - 2 * jd + 2; }
+    else { j = jd; k = i - (2 * jd + kd - 2) + 2; }
+    sa_turm_cell(S, p, j, k);
   }
 }
 

@@ -224,13 +224,13 @@ cudaError_t launch_sa(const Slice<R>* d_sl, const Batch& b, cudaStream_t st, int
   if (ae != cudaSuccess) return ae;
   k_sa_lsolvej<R><<<b.jgroups, LJ_THREADS, lj_smem, st>>>(d_sl, b.d_gfirst, b.nslice);
   k_sa_lsolve<R><<<(b.klines + 63) / 64, 64, 0, st>>>(d_sl, b.d_kfirst, b.nslice, 1);
-  if (final_bc) k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 1);
+  if (final_bc) k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl);
   return cudaGetLastError();
 }
 // the closing turbc of vmu_sa and c_turm on the halo ring
 template <class R>
 cudaError_t launch_sa_final_bc(const Slice<R>* d_sl, const Batch& b, cudaStream_t st) {
-  k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl, 1);
+  k_turbc<R><<<b.nslice, BC_BS, 0, st>>>(d_sl);
   return cudaGetLastError();
 }
 // komegasst (komegasst.f:2-187) for the SST slices of the batch
