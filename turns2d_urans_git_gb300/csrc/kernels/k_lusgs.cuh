@@ -551,8 +551,9 @@ __device__ void lu_sweep_slice(const Slice<R>& S, int nwarp, unsigned char* smem
   // lane is on the first column, and the waits on the neighbouring bands
   // are made once per group -- for the last step's cross-band input and the
   // last step's ring slot -- with the progress published once at the end.
-  // The group runs without branches; the cells see the same operands as in
-  // the per-step form below.
+  // Its steps have no waits and no boundary cases (the boundary lane's
+  // input and output are predicated accesses); the cells see the same
+  // operands as in the per-step form below.
   const bool full = 32 * (w + 1) <= nrow;
   const int lin = FWD ? 0 : 31;
   const bool pout = l == lout && has_next;
