@@ -77,3 +77,28 @@ def test_bench_gpus2_spawns_two_replicas_gloo():
     assert line["value"] == pytest.approx(2 * line["units_per_rank"] / line["seconds"])
     a0, a1 = line["alfas"]
     assert len(a0) == len(a1) == 2 and a0[1] != a1[1]     # each rank its own seeded requests
+
+
+def test_bench_reference_arm_line():
+    """`bench.py --impl reference` (the oracle on the host cores, no GPU and
+    no product library) prints one JSON line with the contract's keys: the
+    same metric, unit and config as the GPU arm, a cpu_baseline describing
+    the run and an e2e without copies."""
+    import json
+    import subprocess
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3", "--batch", "2", "--ref-seconds", "1"],
+                       cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["unit"] == "cell-updates/s" and line["dtype"] == "f64" and line["n_gpus"] == 1
+    assert "513x129" in line["config"]["workload"] and line["config"]["batch_per_gpu"] == 2
+    cpu = line["cpu_baseline"]
+    assert cpu["kind"] in ("port", "reference") and cpu["cores"] >= 1 and cpu["sample"]
+    assert cpu["value"] == line["value"]
+    assert line["e2e"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
